@@ -1,0 +1,198 @@
+/*
+ * crt.h — C ABI of the GB300 ray-tracing core (libcrt.so).
+ *
+ * The library replaces one data-parallel path of MrBigoudi/RealTimeRaytracing:
+ * the BVH build that Scene::bindSSBO runs on the CPU
+ *     cr::BVH::BVH(nbTriangles, unsortedTriangles, meshesInTheScene)
+ *         srcCommon/scene/geometry/bvh.hpp:89-91, bvh.cpp:11-24
+ *     called at srcOpenGL/scene/scene.cpp:148, flattened at scene.cpp:189-208
+ * and the closest-hit traversal the compute shader runs per pixel
+ *     glDispatchCompute(W/16, H/16, 1)       srcOpenGL/application.cpp:245
+ *     raytracer.glsl main / getRay / getClosestHitBVH / rayTriangleIntersection
+ *         srcCommon/shaders/raytracer.glsl:92-147, 182-295, 299-331
+ * Every stage runs as hand-written CUDA kernels for sm_103a on one GPU.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Every pointer argument may point to host
+ *     or device memory; the library checks with cudaPointerGetAttributes and
+ *     copies host data in and out on the context's stream.
+ *   - Calls are ordered on the context's stream.  Functions that return data
+ *     to host memory synchronise that stream before returning.
+ *   - Errors come back as crt_status; crt_last_error_string() describes the
+ *     last failure on the calling thread.  Nothing here calls exit().
+ *   - One context per host thread.  A context owns its device buffers; a
+ *     crt_bvh owns the node array until crt_bvh_free.
+ */
+#ifndef CRT_H
+#define CRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRT_ABI_VERSION 1u
+
+typedef enum crt_status {
+    CRT_OK = 0,
+    CRT_ERR_INVALID_ARG = 1,      /* bad pointer, size or flag */
+    CRT_ERR_OOM = 2,              /* device allocation failed */
+    CRT_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    CRT_ERR_DEVICE_TIMEOUT = 4,   /* a bounded device-side wait gave up */
+    CRT_ERR_STACK_OVERFLOW = 5,   /* a ray's traversal stack overflowed */
+    CRT_ERR_UNSUPPORTED = 6,      /* no sm_103a device, or feature absent */
+    CRT_ERR_BAD_INPUT = 7         /* input data the path cannot handle (e.g. model id >= 64) */
+} crt_status;
+
+/* cr::TriangleGPU (srcCommon/scene/geometry/triangle.hpp:9-14): three vec4
+ * vertices (w = 1) and a model index, 64 bytes.  Note: the GLSL mirror of this
+ * struct names the 2nd and 3rd vec4 _P2 and _P1 (raytracer.glsl:20-25). */
+typedef struct crt_triangle {
+    float p0[4];
+    float p1[4];
+    float p2[4];
+    uint32_t model_id;
+    uint32_t pad[3];
+} crt_triangle;
+
+/* cr::MeshModelGPU (srcCommon/scene/geometry/mesh.hpp:12-15): a column-major
+ * 4x4 model matrix and a material id, 68 bytes. */
+typedef struct crt_mesh_model {
+    float m[16];
+    uint32_t material_id;
+} crt_mesh_model;
+
+/* cr::BVH_NodeGPU (srcCommon/scene/geometry/bvh.hpp:22-26, 36-42), 48 bytes:
+ * a leaf has left == right == 0 and tri = triangle index; an internal node
+ * has tri = 0.  The node array is in DFS pre-order, left subtree first, root
+ * at index 0 (srcOpenGL/scene/scene.cpp:189-208). */
+typedef struct crt_bvh_node {
+    float mn[3];
+    float pad0;
+    float mx[3];
+    float pad1;
+    uint32_t tri;
+    uint32_t left;
+    uint32_t right;
+    uint32_t pad2;
+} crt_bvh_node;
+
+/* A ray (raytracer.glsl:15-18 carries origin/direction as vec4 with w = 1/0).
+ * Hits are accepted for tmin <= t <= tmax; primary rays use [0, +inf]. */
+typedef struct crt_ray {
+    float o[3];
+    float tmin;
+    float d[3];
+    float tmax;
+} crt_ray;
+
+/* Result of a trace.  tri == CRT_MISS on a miss.  For closest-hit, t is the
+ * hit distance in units of |d|; (u, v) are the reference predicate's
+ * (_Coords.x, _Coords.y) or the watertight predicate's weights of p1 and p2.
+ * For any-hit, tri is the id of some occluder (which one is unspecified). */
+typedef struct crt_hit {
+    uint32_t tri;
+    float t;
+    float u;
+    float v;
+} crt_hit;
+#define CRT_MISS 0xFFFFFFFFu
+
+/* The part of cr::CameraGPU (srcCommon/scene/camera.hpp:21-30) that getRay
+ * reads (raytracer.glsl:92-100): column-major inverse view matrix, eye
+ * position (w = 1) and the image-plane size. */
+typedef struct crt_camera {
+    float inv_view[16];
+    float eye[4];
+    float plane_width;
+    float plane_height;
+    float plane_near;
+    float pad;
+} crt_camera;
+
+/* Trace flags. */
+#define CRT_TRACE_CLOSEST     0x0u  /* closest hit */
+#define CRT_TRACE_ANY         0x1u  /* any hit (shadow rays); stops at the first */
+#define CRT_TRI_REFERENCE     0x0u  /* raytracer.glsl:102-147 predicate, bit for bit */
+#define CRT_TRI_WATERTIGHT    0x2u  /* Woop/Benthin/Wald 2013 watertight predicate, two-sided */
+#define CRT_TRACE_USE_PREDICTOR 0x4u /* seed t_max from the learned hit predictor */
+
+typedef struct crt_config {
+    int device;                 /* CUDA device ordinal, default 0 */
+    uint32_t ploc_radius;       /* PLOC search radius, default 16 (bvh.hpp:66) */
+    uint32_t sort_digit_bits;   /* radix digit width: 4 or 8, default 8 */
+    uint32_t trace_block;       /* threads per traversal block, default 128 */
+    uint32_t stack_depth;       /* traversal stack entries per ray, default 64 */
+    uint32_t spin_limit;        /* bound on every device-side wait loop, 0 = default */
+} crt_config;
+
+typedef struct crt_ctx crt_ctx;
+typedef struct crt_bvh crt_bvh;
+
+/* Build statistics of the last crt_build on a context (device-timed). */
+typedef struct crt_build_stats {
+    uint32_t n_tris;
+    uint32_t ploc_iterations;
+    float ms_morton;     /* scene box + Morton codes */
+    float ms_sort;       /* radix sort of (code, index) */
+    float ms_ploc;       /* PLOC iterations */
+    float ms_layout;     /* DFS node layout */
+    float ms_total;
+    float scene_box[6];  /* min xyz, max xyz over the scanned buffer */
+} crt_build_stats;
+
+/* ---- context ---------------------------------------------------------- */
+uint32_t crt_abi_version(void);
+void crt_default_config(crt_config* cfg);
+crt_status crt_create(crt_ctx** ctx, const crt_config* cfg /* may be NULL */);
+crt_status crt_destroy(crt_ctx* ctx);
+crt_status crt_sync(crt_ctx* ctx);
+const char* crt_last_error_string(void);
+/* The CUDA stream (cudaStream_t) the context orders its work on. */
+void* crt_stream(crt_ctx* ctx);
+
+/* ---- build: replaces cr::BVH::BVH (bvh.cpp:11-24) + Scene::getBVH_NodesToGPUData
+ * (scene.cpp:203-208).
+ *   tris      n_buffer triangles; the reference scans all n_buffer of them for
+ *             the scene box (bvh.cpp:235-251; Scene pads to 65,536 with zero
+ *             records, scene.cpp:26-40) and builds over the first n_tris.
+ *   models    n_models <= 64 mesh models; ids >= n_models use identity, as
+ *             Scene::getMeshModelToGPUData pads (scene.cpp:17-23).
+ *   out       receives a new BVH handle (free with crt_bvh_free). */
+crt_status crt_build(crt_ctx* ctx, const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
+                     const crt_mesh_model* models, uint32_t n_models, crt_bvh** out);
+/* Rebuild into an existing handle (same or smaller capacity is reused). */
+crt_status crt_rebuild(crt_ctx* ctx, crt_bvh* bvh, const crt_triangle* tris, uint32_t n_buffer,
+                       uint32_t n_tris, const crt_mesh_model* models, uint32_t n_models);
+crt_status crt_bvh_free(crt_bvh* bvh);
+uint32_t crt_bvh_node_count(const crt_bvh* bvh);       /* 2 * n_tris - 1 */
+uint32_t crt_bvh_triangle_count(const crt_bvh* bvh);
+const crt_bvh_node* crt_bvh_nodes_device(const crt_bvh* bvh);
+/* Copy out: node array (reference layout), sorted Morton codes, permutation
+ * (sorted position -> triangle index).  dst may be host or device memory. */
+crt_status crt_bvh_copy_nodes(crt_ctx* ctx, const crt_bvh* bvh, crt_bvh_node* dst);
+crt_status crt_bvh_copy_codes(crt_ctx* ctx, const crt_bvh* bvh, uint32_t* dst);
+crt_status crt_bvh_copy_perm(crt_ctx* ctx, const crt_bvh* bvh, uint32_t* dst);
+crt_status crt_last_build_stats(crt_ctx* ctx, crt_build_stats* stats);
+
+/* ---- rays ------------------------------------------------------------- */
+/* Primary rays of getRay (raytracer.glsl:92-100) for a width x height image:
+ * ray (x, y) is stored at y * width + x and uses pos = (x / width, y / height). */
+crt_status crt_raygen_pinhole(crt_ctx* ctx, const crt_camera* cam, uint32_t width, uint32_t height,
+                              crt_ray* rays);
+/* One shadow ray per primary hit toward a point light: origin = o + t d,
+ * direction = normalize(light - origin), [tmin, tmax] = [1e-4, |light - origin|].
+ * Primary misses give an empty ray (tmin = 1, tmax = 0) that never hits. */
+crt_status crt_shadow_rays(crt_ctx* ctx, const crt_ray* primary, const crt_hit* hits, uint32_t n_rays,
+                           const float light[3], crt_ray* shadow);
+
+/* ---- trace: replaces getClosestHitBVH (raytracer.glsl:246-295) ---------- */
+crt_status crt_trace(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, uint32_t n_rays,
+                     uint32_t flags, crt_hit* hits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRT_H */

@@ -1,0 +1,83 @@
+"""Host-side mirror of the reference's BVH interface, backed by libcrt.
+
+The reference builds its BVH with
+    cr::BVH::BVH(uint32_t nbTriangles,
+                 const std::vector<TriangleGPU>& unsortedTriangles,
+                 const std::vector<MeshModelGPU>& meshesInTheScene)
+        srcCommon/scene/geometry/bvh.hpp:89-91, bvh.cpp:11-24
+and Scene::getBVH_NodesToGPUData (srcOpenGL/scene/scene.cpp:203-208)
+flattens it into the node array the shader reads; getClosestHitBVH
+(srcCommon/shaders/raytracer.glsl:246-295) traces it per pixel.  BVH and
+Raytracer below keep those names and argument meanings; all work runs in the
+CUDA library.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import crt
+
+MAX_NB_TRIANGLES = 2 << 15   # Triangle::MAX_NB_TRIANGLES (triangle.hpp:21); the GPU path has no such cap
+MAX_NB_MESHES = 2 << 5       # Mesh::MAX_NB_MESHES (mesh.hpp:26)
+
+_default_ctx = None
+
+
+def default_context() -> crt.Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = crt.Context()
+    return _default_ctx
+
+
+class BVH:
+    """cr::BVH.  `unsortedTriangles` is the (n_buffer, 16) float32 TriangleGPU
+    buffer — the reference scans every entry of it for the scene box
+    (bvh.cpp:237) and builds over the first `nbTriangles`; `meshesInTheScene`
+    is the (m <= 64, 17) MeshModelGPU buffer."""
+
+    def __init__(self, nbTriangles: int, unsortedTriangles, meshesInTheScene=None, ctx: crt.Context | None = None):
+        if nbTriangles < 1:
+            raise ValueError("nbTriangles must be >= 1")
+        self._ctx = ctx or default_context()
+        self._NbTriangles = int(nbTriangles)
+        self._bvh = self._ctx.build(unsortedTriangles, n_tris=self._NbTriangles, models=meshesInTheScene)
+        self.build_stats = self._ctx.last_build_stats()
+
+    @property
+    def _TriangleIndices(self) -> np.ndarray:
+        """Sorted position -> triangle index (BVH_Params::_TriangleIndices)."""
+        return self._bvh.perm()
+
+    @property
+    def _MortonCodes(self) -> np.ndarray:
+        """Sorted Morton codes (PlocParams::_MortonCodes after the sort)."""
+        return self._bvh.codes()
+
+    def getBVH_NodesToGPUData(self) -> np.ndarray:
+        """The (2N-1, 12) node array Scene::getBVH_NodesToGPUData returns:
+        DFS pre-order, left subtree first, BVH_NodeGPU records."""
+        return self._bvh.nodes()
+
+    @property
+    def handle(self) -> crt.Bvh:
+        return self._bvh
+
+
+class Raytracer:
+    """The compute pass of Application::drawOneFrame (application.cpp:220-262)
+    minus shading: getRay for every texel, then getClosestHitBVH."""
+
+    def __init__(self, ctx: crt.Context | None = None):
+        self._ctx = ctx or default_context()
+
+    def getRays(self, camera_gpu, width: int, height: int, out=None):
+        return self._ctx.raygen(camera_gpu, width, height, out)
+
+    def getClosestHitBVH(self, bvh: BVH, rays, watertight: bool = False, out=None):
+        flags = crt.TRACE_CLOSEST | (crt.TRI_WATERTIGHT if watertight else crt.TRI_REFERENCE)
+        return self._ctx.trace(bvh.handle, rays, flags, out)
+
+    def getAnyHitBVH(self, bvh: BVH, rays, watertight: bool = True, out=None):
+        flags = crt.TRACE_ANY | (crt.TRI_WATERTIGHT if watertight else crt.TRI_REFERENCE)
+        return self._ctx.trace(bvh.handle, rays, flags, out)

@@ -1,0 +1,246 @@
+"""ctypes binding of libcrt.so (include/crt.h).
+
+Arrays may be numpy arrays (host memory: the library copies in and out) or
+torch CUDA tensors (device memory: used in place).  Record layouts are the
+ones documented in realtimeraytracing_gb300.scenes.  Every entry point runs
+the CUDA kernels; there is no host fallback — without the built library or a
+GPU the calls raise CrtError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libcrt.so")
+
+CRT_OK = 0
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "DEVICE_TIMEOUT", 5: "STACK_OVERFLOW",
+          6: "UNSUPPORTED", 7: "BAD_INPUT"}
+
+TRACE_CLOSEST = 0x0
+TRACE_ANY = 0x1
+TRI_REFERENCE = 0x0
+TRI_WATERTIGHT = 0x2
+TRACE_USE_PREDICTOR = 0x4
+MISS = 0xFFFFFFFF
+
+# Every symbol include/crt.h declares.
+EXPORTS = [
+    "crt_abi_version", "crt_default_config", "crt_create", "crt_destroy", "crt_sync", "crt_last_error_string",
+    "crt_stream", "crt_build", "crt_rebuild", "crt_bvh_free", "crt_bvh_node_count", "crt_bvh_triangle_count",
+    "crt_bvh_nodes_device", "crt_bvh_copy_nodes", "crt_bvh_copy_codes", "crt_bvh_copy_perm", "crt_last_build_stats",
+    "crt_raygen_pinhole", "crt_shadow_rays", "crt_trace",
+]
+
+
+class CrtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("ploc_radius", C.c_uint32), ("sort_digit_bits", C.c_uint32),
+                ("trace_block", C.c_uint32), ("stack_depth", C.c_uint32), ("spin_limit", C.c_uint32)]
+
+
+class BuildStats(C.Structure):
+    _fields_ = [("n_tris", C.c_uint32), ("ploc_iterations", C.c_uint32), ("ms_morton", C.c_float),
+                ("ms_sort", C.c_float), ("ms_ploc", C.c_float), ("ms_layout", C.c_float), ("ms_total", C.c_float),
+                ("scene_box", C.c_float * 6)]
+
+    def as_dict(self):
+        return {f: (list(getattr(self, f)) if f == "scene_box" else getattr(self, f)) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Load libcrt.so (fails loudly if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with realtimeraytracing_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        sig = {
+            "crt_abi_version": ([], u32),
+            "crt_default_config": ([vp], None),
+            "crt_create": ([C.POINTER(vp), vp], i32),
+            "crt_destroy": ([vp], i32),
+            "crt_sync": ([vp], i32),
+            "crt_last_error_string": ([], C.c_char_p),
+            "crt_stream": ([vp], vp),
+            "crt_build": ([vp, vp, u32, u32, vp, u32, C.POINTER(vp)], i32),
+            "crt_rebuild": ([vp, vp, vp, u32, u32, vp, u32], i32),
+            "crt_bvh_free": ([vp], i32),
+            "crt_bvh_node_count": ([vp], u32),
+            "crt_bvh_triangle_count": ([vp], u32),
+            "crt_bvh_nodes_device": ([vp], vp),
+            "crt_bvh_copy_nodes": ([vp, vp, vp], i32),
+            "crt_bvh_copy_codes": ([vp, vp, vp], i32),
+            "crt_bvh_copy_perm": ([vp, vp, vp], i32),
+            "crt_last_build_stats": ([vp, vp], i32),
+            "crt_raygen_pinhole": ([vp, vp, u32, u32, vp], i32),
+            "crt_shadow_rays": ([vp, vp, vp, u32, vp, vp], i32),
+            "crt_trace": ([vp, vp, vp, u32, u32, vp], i32),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != CRT_OK:
+        raise CrtError(status, lib().crt_last_error_string().decode(errors="replace"))
+
+
+def _ptr(a):
+    """Address of a numpy array or torch tensor (contiguous)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return C.c_void_p(a.data_ptr())
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _rows(a):
+    return a.shape[0]
+
+
+class Bvh:
+    """A built BVH (crt_bvh): nodes in the reference's DFS layout, sorted
+    Morton codes and the sorted-position -> triangle permutation."""
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p):
+        self.ctx = ctx
+        self.handle = handle
+
+    @property
+    def n_tris(self) -> int:
+        return lib().crt_bvh_triangle_count(self.handle)
+
+    @property
+    def n_nodes(self) -> int:
+        return lib().crt_bvh_node_count(self.handle)
+
+    def nodes(self, out=None):
+        out = np.empty((self.n_nodes, 12), np.float32) if out is None else out
+        _check(lib().crt_bvh_copy_nodes(self.ctx.handle, self.handle, _ptr(out)))
+        return out
+
+    def codes(self, out=None):
+        out = np.empty(self.n_tris, np.uint32) if out is None else out
+        _check(lib().crt_bvh_copy_codes(self.ctx.handle, self.handle, _ptr(out)))
+        return out
+
+    def perm(self, out=None):
+        out = np.empty(self.n_tris, np.uint32) if out is None else out
+        _check(lib().crt_bvh_copy_perm(self.ctx.handle, self.handle, _ptr(out)))
+        return out
+
+    def rebuild(self, tris, n_tris=None, models=None, n_buffer=None):
+        models = _models(models)
+        n_buffer = _rows(tris) if n_buffer is None else n_buffer
+        n_tris = n_buffer if n_tris is None else n_tris
+        _check(lib().crt_rebuild(self.ctx.handle, self.handle, _ptr(tris), n_buffer, n_tris, _ptr(models),
+                                 0 if models is None else _rows(models)))
+        return self
+
+    def free(self):
+        if self.handle:
+            lib().crt_bvh_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _models(models):
+    if models is None:
+        return None
+    if isinstance(models, np.ndarray):
+        return np.ascontiguousarray(models, np.float32)
+    return models
+
+
+class Context:
+    """crt_ctx: one CUDA stream and the device scratch of the build."""
+
+    def __init__(self, device: int = 0, ploc_radius: int = 16, sort_digit_bits: int = 8, trace_block: int = 128,
+                 stack_depth: int = 64, spin_limit: int = 0):
+        cfg = Config()
+        lib().crt_default_config(C.byref(cfg))
+        cfg.device, cfg.ploc_radius, cfg.sort_digit_bits = device, ploc_radius, sort_digit_bits
+        cfg.trace_block, cfg.stack_depth, cfg.spin_limit = trace_block, stack_depth, spin_limit
+        h = C.c_void_p()
+        _check(lib().crt_create(C.byref(h), C.byref(cfg)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().crt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib().crt_stream(self.handle) or 0
+
+    def sync(self):
+        _check(lib().crt_sync(self.handle))
+
+    def build(self, tris, n_tris=None, models=None, n_buffer=None) -> Bvh:
+        """cr::BVH::BVH(nbTriangles, unsortedTriangles, meshesInTheScene)."""
+        models = _models(models)
+        n_buffer = _rows(tris) if n_buffer is None else n_buffer
+        n_tris = n_buffer if n_tris is None else n_tris
+        h = C.c_void_p()
+        _check(lib().crt_build(self.handle, _ptr(tris), n_buffer, n_tris, _ptr(models),
+                               0 if models is None else _rows(models), C.byref(h)))
+        return Bvh(self, h)
+
+    def last_build_stats(self) -> dict:
+        s = BuildStats()
+        _check(lib().crt_last_build_stats(self.handle, C.byref(s)))
+        return s.as_dict()
+
+    def raygen(self, cam, width: int, height: int, out=None):
+        cam = np.ascontiguousarray(cam, np.float32) if isinstance(cam, np.ndarray) else cam
+        out = np.empty((width * height, 8), np.float32) if out is None else out
+        _check(lib().crt_raygen_pinhole(self.handle, _ptr(cam), width, height, _ptr(out)))
+        return out
+
+    def shadow_rays(self, primary, hits, light, out=None):
+        n = _rows(primary)
+        out = np.empty((n, 8), np.float32) if out is None else out
+        light = np.ascontiguousarray(light, np.float32)
+        _check(lib().crt_shadow_rays(self.handle, _ptr(primary), _ptr(hits), n, _ptr(light), _ptr(out)))
+        return out
+
+    def trace(self, bvh: Bvh, rays, flags: int = 0, out=None):
+        n = _rows(rays)
+        out = np.empty((n, 4), np.float32) if out is None else out
+        _check(lib().crt_trace(self.handle, bvh.handle, _ptr(rays), n, flags, _ptr(out)))
+        return out

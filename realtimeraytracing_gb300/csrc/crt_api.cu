@@ -1,0 +1,571 @@
+// C ABI of libcrt (include/crt.h): contexts, device buffers, the build
+// pipeline (scene box -> Morton -> radix sort -> PLOC -> DFS layout) and the
+// trace entry points.  No compute happens on the host: a call that cannot
+// run its kernels returns an error instead of falling back.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cuda_runtime.h>
+#include <vector>
+
+#include "crt.h"
+#include "crt_build.cuh"
+#include "crt_common.cuh"
+
+namespace {
+
+thread_local char g_err[512] = "no error";
+
+crt_status fail(crt_status s, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return s;
+}
+
+#define CRT_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            return fail(e_ == cudaErrorMemoryAllocation ? CRT_ERR_OOM : CRT_ERR_CUDA, "%s failed: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+        }                                                                                               \
+    } while (0)
+
+#define CRT_TRY(expr)                  \
+    do {                               \
+        crt_status s_ = (expr);        \
+        if (s_ != CRT_OK) return s_;   \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    crt_status reserve(size_t bytes) {
+        if (bytes <= cap) return CRT_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = bytes + bytes / 8 + 256;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(CRT_ERR_OOM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+        }
+        cap = want;
+        return CRT_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+bool is_device_ptr(const void* ptr) {
+    if (!ptr) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+constexpr uint32_t kDefaultSpin = 1u << 22;   // ~0.3 s with back-off; far above any normal wait
+
+}  // namespace
+
+struct crt_bvh {
+    crt_ctx* ctx = nullptr;
+    uint32_t n = 0;
+    uint32_t iterations = 0;
+    float abs_eps = 0.f;
+    DevBuf nodes, xtri, codes, perm;
+};
+
+struct crt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    crt_config cfg{};
+    // build scratch
+    DevBuf tris_in, models, scene_state, err, hist, sort_lb, codes_a, codes_b, vals_a, vals_b;
+    DevBuf node_box, node_lc, pos, clus_a, clus_b, iters, ploc_lb;
+    DevBuf cam, rays_in, hits_out, rays_out;
+    // pinned host staging
+    void* pinned = nullptr;
+    size_t pinned_cap = 0;
+    cudaEvent_t ev[6] = {};
+    crt_build_stats stats{};
+    std::vector<uint2> it_host;
+
+    crt_status pinned_reserve(size_t bytes) {
+        if (bytes <= pinned_cap) return CRT_OK;
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        pinned_cap = 0;
+        CRT_CUDA(cudaMallocHost(&pinned, bytes));
+        pinned_cap = bytes;
+        return CRT_OK;
+    }
+    crt_status check_device_error() {
+        uint32_t e = 0;
+        CRT_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, stream));
+        CRT_CUDA(cudaStreamSynchronize(stream));
+        if (e & crt::kDevTimeout) return fail(CRT_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up (err=0x%x)", e);
+        if (e & crt::kDevBadModel) return fail(CRT_ERR_BAD_INPUT, "a triangle references model id >= 64");
+        if (e & crt::kDevStackOverflow) return fail(CRT_ERR_STACK_OVERFLOW, "a ray overflowed its traversal stack");
+        if (e & crt::kDevCorrupt) return fail(CRT_ERR_CUDA, "a device index check failed (err=0x%x)", e);
+        if (e) return fail(CRT_ERR_CUDA, "device error word 0x%x", e);
+        return CRT_OK;
+    }
+};
+
+extern "C" {
+
+uint32_t crt_abi_version(void) { return CRT_ABI_VERSION; }
+
+const char* crt_last_error_string(void) { return g_err; }
+
+void crt_default_config(crt_config* cfg) {
+    if (!cfg) return;
+    cfg->device = 0;
+    cfg->ploc_radius = 16;
+    cfg->sort_digit_bits = 8;
+    cfg->trace_block = 128;
+    cfg->stack_depth = 64;
+    cfg->spin_limit = 0;
+}
+
+crt_status crt_create(crt_ctx** out, const crt_config* cfg) {
+    if (!out) return fail(CRT_ERR_INVALID_ARG, "crt_create: null output pointer");
+    *out = nullptr;
+    crt_config c;
+    crt_default_config(&c);
+    if (cfg) c = *cfg;
+    if (c.ploc_radius == 0 || c.ploc_radius > static_cast<uint32_t>(crt::kPlocMaxRadius))
+        return fail(CRT_ERR_INVALID_ARG, "ploc_radius must be in [1, %d]", crt::kPlocMaxRadius);
+    if (c.sort_digit_bits != 4 && c.sort_digit_bits != 8)
+        return fail(CRT_ERR_INVALID_ARG, "sort_digit_bits must be 4 or 8");
+    if (c.trace_block != 64 && c.trace_block != 128 && c.trace_block != 256)
+        return fail(CRT_ERR_INVALID_ARG, "trace_block must be 64, 128 or 256");
+    if (c.spin_limit == 0) c.spin_limit = kDefaultSpin;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(CRT_ERR_UNSUPPORTED, "no CUDA device");
+    }
+    if (c.device < 0 || c.device >= ndev) return fail(CRT_ERR_INVALID_ARG, "device %d out of range", c.device);
+    cudaDeviceProp prop;
+    CRT_CUDA(cudaGetDeviceProperties(&prop, c.device));
+    if (prop.major * 10 + prop.minor != 103)
+        return fail(CRT_ERR_UNSUPPORTED, "libcrt is built for sm_103a; device is sm_%d%d", prop.major, prop.minor);
+    CRT_CUDA(cudaSetDevice(c.device));
+    crt_ctx* x = new crt_ctx();
+    x->device = c.device;
+    x->cfg = c;
+    crt_status s = CRT_OK;
+    if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) s = fail(CRT_ERR_CUDA, "stream");
+    for (auto& e : x->ev)
+        if (s == CRT_OK && cudaEventCreate(&e) != cudaSuccess) s = fail(CRT_ERR_CUDA, "event");
+    if (s == CRT_OK) s = x->scene_state.reserve(sizeof(crt::SceneState));
+    if (s == CRT_OK) s = x->err.reserve(16);
+    if (s == CRT_OK) s = x->models.reserve(2 * 64 * 16 * sizeof(float));
+    if (s == CRT_OK) s = x->cam.reserve(sizeof(crt_camera));
+    if (s == CRT_OK) s = x->pinned_reserve(1 << 16);
+    if (s == CRT_OK) {
+        crt::SceneState init{};
+        for (int a = 0; a < 3; ++a) { init.key_max[a] = 0ull; init.key_min[a] = ~0ull; }
+        if (cudaMemcpy(x->scene_state.p, &init, sizeof(init), cudaMemcpyHostToDevice) != cudaSuccess)
+            s = fail(CRT_ERR_CUDA, "scene state init");
+    }
+    if (s != CRT_OK) {
+        crt_destroy(x);
+        return s;
+    }
+    *out = x;
+    return CRT_OK;
+}
+
+crt_status crt_destroy(crt_ctx* x) {
+    if (!x) return CRT_OK;
+    cudaSetDevice(x->device);
+    if (x->stream) cudaStreamSynchronize(x->stream);
+    DevBuf* bufs[] = {&x->tris_in, &x->models, &x->scene_state, &x->err, &x->hist, &x->sort_lb, &x->codes_a,
+                      &x->codes_b, &x->vals_a, &x->vals_b, &x->node_box, &x->node_lc, &x->pos, &x->clus_a,
+                      &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out};
+    for (DevBuf* b : bufs) b->release();
+    for (auto& e : x->ev)
+        if (e) cudaEventDestroy(e);
+    if (x->pinned) cudaFreeHost(x->pinned);
+    if (x->stream) cudaStreamDestroy(x->stream);
+    delete x;
+    return CRT_OK;
+}
+
+crt_status crt_sync(crt_ctx* x) {
+    if (!x) return fail(CRT_ERR_INVALID_ARG, "null context");
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+void* crt_stream(crt_ctx* x) { return x ? static_cast<void*>(x->stream) : nullptr; }
+
+}  // extern "C"
+
+namespace {
+
+crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
+                      const crt_mesh_model* models, uint32_t n_models) {
+    if (!tris) return fail(CRT_ERR_INVALID_ARG, "crt_build: null triangles");
+    if (n_tris == 0) return fail(CRT_ERR_INVALID_ARG, "crt_build: n_tris must be >= 1");
+    if (n_buffer < n_tris) return fail(CRT_ERR_INVALID_ARG, "crt_build: n_buffer < n_tris");
+    if (n_tris > (1u << 30)) return fail(CRT_ERR_INVALID_ARG, "crt_build: n_tris above 2^30");
+    if (n_models > crt::kMaxModels) return fail(CRT_ERR_INVALID_ARG, "crt_build: more than 64 models");
+    if (n_models > 0 && !models) return fail(CRT_ERR_INVALID_ARG, "crt_build: null models");
+    CRT_CUDA(cudaSetDevice(x->device));
+    cudaStream_t s = x->stream;
+    const uint32_t N = n_tris;
+    const int bits = static_cast<int>(x->cfg.sort_digit_bits);
+    const int passes = (30 + bits - 1) / bits;
+    const uint32_t radix = 1u << bits;
+    const uint32_t sort_tiles = (N + crt::sort_tile_keys(bits) - 1) / crt::sort_tile_keys(bits);
+    const uint32_t ploc_tiles = (N + crt::kPlocTile - 1) / crt::kPlocTile;
+
+    // ---- buffers
+    const crt_triangle* d_tris = tris;
+    if (!is_device_ptr(tris)) {
+        CRT_TRY(x->tris_in.reserve(sizeof(crt_triangle) * static_cast<size_t>(n_buffer)));
+        CRT_CUDA(cudaMemcpyAsync(x->tris_in.p, tris, sizeof(crt_triangle) * static_cast<size_t>(n_buffer),
+                                 cudaMemcpyHostToDevice, s));
+        d_tris = x->tris_in.as<crt_triangle>();
+    }
+    const size_t hist_words = static_cast<size_t>(passes) * radix;
+    const size_t sort_lb_words = static_cast<size_t>(passes) * (sort_tiles * radix + 1);  // + ticket per pass
+    CRT_TRY(x->hist.reserve(4 * hist_words));
+    CRT_TRY(x->sort_lb.reserve(4 * sort_lb_words));
+    CRT_TRY(x->codes_a.reserve(4ull * N));
+    CRT_TRY(x->codes_b.reserve(4ull * N));
+    CRT_TRY(x->vals_a.reserve(4ull * N));
+    CRT_TRY(x->vals_b.reserve(4ull * N));
+    CRT_TRY(x->node_box.reserve(32ull * (2ull * N - 1)));
+    CRT_TRY(x->node_lc.reserve(4ull * N));
+    CRT_TRY(x->pos.reserve(4ull * N));
+    CRT_TRY(x->clus_a.reserve(32ull * N));
+    CRT_TRY(x->clus_b.reserve(32ull * N));
+    CRT_TRY(x->iters.reserve(8ull * (N + 2)));
+    CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 16));
+    CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
+    CRT_TRY(b->xtri.reserve(48ull * N));
+    CRT_TRY(b->codes.reserve(4ull * N));
+    CRT_TRY(b->perm.reserve(4ull * N));
+
+    // ---- models: 64 column-major matrices (identity past n_models) and the
+    // same matrices scaled by 1/3 for the centroid (triangle.cpp:32)
+    float* hm = static_cast<float*>(x->pinned);
+    for (uint32_t m = 0; m < 64; ++m) {
+        for (int k = 0; k < 16; ++k) hm[16 * m + k] = (k % 5 == 0) ? 1.f : 0.f;
+        if (m < n_models) {
+            crt_mesh_model mm;
+            if (is_device_ptr(models)) {
+                CRT_CUDA(cudaMemcpy(&mm, models + m, sizeof(mm), cudaMemcpyDeviceToHost));
+            } else {
+                std::memcpy(&mm, models + m, sizeof(mm));
+            }
+            std::memcpy(hm + 16 * m, mm.m, 64);
+        }
+    }
+    const volatile float third = 1.f / 3.f;
+    for (int k = 0; k < 64 * 16; ++k) hm[64 * 16 + k] = third * hm[k];
+    CRT_CUDA(cudaMemcpyAsync(x->models.p, hm, 2 * 64 * 16 * sizeof(float), cudaMemcpyHostToDevice, s));
+    const float* d_models = x->models.as<float>();
+    const float* d_models3 = d_models + 64 * 16;
+
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, s));
+    CRT_CUDA(cudaMemsetAsync(x->hist.p, 0, 4 * hist_words, s));
+    CRT_CUDA(cudaMemsetAsync(x->sort_lb.p, 0, 4 * sort_lb_words, s));
+    CRT_CUDA(cudaMemsetAsync(x->ploc_lb.p, 0, 8ull * (2ull * ploc_tiles) + 16, s));
+    uint32_t* err = x->err.as<uint32_t>();
+    auto* st = x->scene_state.as<crt::SceneState>();
+
+    CRT_CUDA(cudaEventRecord(x->ev[0], s));
+    // ---- K1: scene box + Morton codes + digit histograms
+    crt::launch_scene_box(d_tris, n_buffer, d_models, st, err, s);
+    crt::launch_morton(d_tris, N, d_models3, st, x->codes_a.as<uint32_t>(), x->hist.as<uint32_t>(), bits, s);
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaEventRecord(x->ev[1], s));
+
+    // ---- K2: LSD radix sort, one Onesweep pass per digit
+    {
+        uint32_t* kin = x->codes_a.as<uint32_t>();
+        uint32_t* vin = nullptr;
+        for (int p = 0; p < passes; ++p) {
+            const bool last = (p == passes - 1);
+            uint32_t* kout = last ? b->codes.as<uint32_t>() : ((p & 1) ? x->codes_a.as<uint32_t>() : x->codes_b.as<uint32_t>());
+            uint32_t* vout = last ? b->perm.as<uint32_t>() : ((p & 1) ? x->vals_a.as<uint32_t>() : x->vals_b.as<uint32_t>());
+            uint32_t* lb = x->sort_lb.as<uint32_t>() + static_cast<size_t>(p) * (sort_tiles * radix + 1);
+            crt::launch_onesweep(kin, vin, kout, vout, N, p * bits, bits, x->hist.as<uint32_t>() + p * radix, lb + 1, lb,
+                                 err, x->cfg.spin_limit, s);
+            kin = kout;
+            vin = vout;
+        }
+    }
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaEventRecord(x->ev[2], s));
+
+    // ---- K3: leaf clusters + PLOC iterations
+    uint2* d_it = x->iters.as<uint2>();
+    crt::launch_leaf_init(d_tris, N, d_models, b->perm.as<uint32_t>(), x->node_box.as<float4>(), x->clus_a.as<float4>(),
+                          b->xtri.as<float4>(), d_it, err, s);
+    CRT_CUDA(cudaGetLastError());
+    x->it_host.assign(1, make_uint2(N, N));
+    uint32_t iters = 0;
+    if (N > 1) {
+        uint32_t n_known = N;
+        int iter = 0;
+        double rate = 0.6;
+        float4* ca = x->clus_a.as<float4>();
+        float4* cb = x->clus_b.as<float4>();
+        unsigned long long* lb = x->ploc_lb.as<unsigned long long>();
+        uint32_t* tickets = reinterpret_cast<uint32_t*>(lb + 2ull * ploc_tiles);
+        uint2* hpin = static_cast<uint2*>(x->pinned);
+        bool done = false;
+        while (!done) {
+            // enough launches to likely finish, estimated from the observed shrink rate
+            int chunk = static_cast<int>(std::ceil(std::log(static_cast<double>(n_known)) / -std::log(rate))) + 2;
+            if (chunk < 4) chunk = 4;
+            if (chunk > 64) chunk = 64;
+            if (static_cast<uint32_t>(iter + chunk) > N) chunk = static_cast<int>(N) - iter;
+            if (chunk <= 0) return fail(CRT_ERR_CUDA, "PLOC did not converge");
+            for (int c = 0; c < chunk; ++c, ++iter) {
+                const float4* cin = (iter & 1) ? cb : ca;
+                float4* cout = (iter & 1) ? ca : cb;
+                crt::launch_ploc_iteration(cin, cout, x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), d_it, iter, N,
+                                           static_cast<int>(x->cfg.ploc_radius), n_known, lb, tickets, ploc_tiles, err,
+                                           x->cfg.spin_limit, s);
+            }
+            CRT_CUDA(cudaGetLastError());
+            const int first = iter - chunk + 1;
+            CRT_CUDA(cudaMemcpyAsync(hpin, d_it + first, sizeof(uint2) * chunk, cudaMemcpyDeviceToHost, s));
+            CRT_CUDA(cudaStreamSynchronize(s));
+            const uint32_t prev = n_known;
+            for (int c = 0; c < chunk; ++c) {
+                x->it_host.push_back(hpin[c]);
+                n_known = hpin[c].x;
+                if (n_known <= 1) {
+                    iters = static_cast<uint32_t>(first + c);
+                    done = true;
+                    break;
+                }
+                if (n_known > prev || n_known == 0) return fail(CRT_ERR_CUDA, "PLOC state corrupt (n=%u)", n_known);
+            }
+            if (!done) {
+                const double r = std::pow(static_cast<double>(n_known) / prev, 1.0 / chunk);
+                rate = std::min(0.95, std::max(0.3, r));
+                uint32_t e = 0;
+                CRT_CUDA(cudaMemcpy(&e, err, 4, cudaMemcpyDeviceToHost));
+                if (e) break;
+            }
+        }
+    }
+    CRT_CUDA(cudaEventRecord(x->ev[3], s));
+
+    // ---- K4: DFS layout, last PLOC iteration first
+    if (N == 1) {
+        crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), s);
+    } else {
+        for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
+            crt::launch_layout_level(x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), x->pos.as<uint32_t>(),
+                                     x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(), err, s);
+    }
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaEventRecord(x->ev[4], s));
+    CRT_TRY(x->check_device_error());
+
+    crt::SceneState hs;
+    CRT_CUDA(cudaMemcpy(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost));
+    float ms[4];
+    for (int k = 0; k < 4; ++k) CRT_CUDA(cudaEventElapsedTime(&ms[k], x->ev[k], x->ev[k + 1]));
+    x->stats.n_tris = N;
+    x->stats.ploc_iterations = iters;
+    x->stats.ms_morton = ms[0];
+    x->stats.ms_sort = ms[1];
+    x->stats.ms_ploc = ms[2];
+    x->stats.ms_layout = ms[3];
+    x->stats.ms_total = ms[0] + ms[1] + ms[2] + ms[3];
+    float ext = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        x->stats.scene_box[a] = hs.scene_min[a];
+        x->stats.scene_box[3 + a] = hs.scene_max[a];
+        const float e = hs.scene_max[a] - hs.scene_min[a];
+        if (std::isfinite(e) && e > ext) ext = e;
+        const float m = std::fmax(std::fabs(hs.scene_min[a]), std::fabs(hs.scene_max[a]));
+        if (std::isfinite(m) && m > ext) ext = m;
+    }
+    b->n = N;
+    b->iterations = iters;
+    b->abs_eps = std::ldexp(ext > 0.f ? ext : 1.f, -20);
+    b->ctx = x;
+    return CRT_OK;
+}
+
+crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
+    if (!dst) return fail(CRT_ERR_INVALID_ARG, "null destination");
+    CRT_CUDA(cudaMemcpyAsync(dst, src, bytes, is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+crt_status crt_build(crt_ctx* x, const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
+                     const crt_mesh_model* models, uint32_t n_models, crt_bvh** out) {
+    if (!x || !out) return fail(CRT_ERR_INVALID_ARG, "crt_build: null context or output");
+    *out = nullptr;
+    crt_bvh* b = new crt_bvh();
+    const crt_status s = build_impl(x, b, tris, n_buffer, n_tris, models, n_models);
+    if (s != CRT_OK) {
+        crt_bvh_free(b);
+        return s;
+    }
+    *out = b;
+    return CRT_OK;
+}
+
+crt_status crt_rebuild(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
+                       const crt_mesh_model* models, uint32_t n_models) {
+    if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "crt_rebuild: null context or bvh");
+    return build_impl(x, b, tris, n_buffer, n_tris, models, n_models);
+}
+
+crt_status crt_bvh_free(crt_bvh* b) {
+    if (!b) return CRT_OK;
+    b->nodes.release();
+    b->xtri.release();
+    b->codes.release();
+    b->perm.release();
+    delete b;
+    return CRT_OK;
+}
+
+uint32_t crt_bvh_node_count(const crt_bvh* b) { return (b && b->n) ? 2 * b->n - 1 : 0; }
+uint32_t crt_bvh_triangle_count(const crt_bvh* b) { return b ? b->n : 0; }
+const crt_bvh_node* crt_bvh_nodes_device(const crt_bvh* b) { return b ? b->nodes.as<crt_bvh_node>() : nullptr; }
+
+crt_status crt_bvh_copy_nodes(crt_ctx* x, const crt_bvh* b, crt_bvh_node* dst) {
+    if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "null context or bvh");
+    return copy_out(x, dst, b->nodes.p, sizeof(crt_bvh_node) * (2ull * b->n - 1));
+}
+crt_status crt_bvh_copy_codes(crt_ctx* x, const crt_bvh* b, uint32_t* dst) {
+    if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "null context or bvh");
+    return copy_out(x, dst, b->codes.p, 4ull * b->n);
+}
+crt_status crt_bvh_copy_perm(crt_ctx* x, const crt_bvh* b, uint32_t* dst) {
+    if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "null context or bvh");
+    return copy_out(x, dst, b->perm.p, 4ull * b->n);
+}
+
+crt_status crt_last_build_stats(crt_ctx* x, crt_build_stats* st) {
+    if (!x || !st) return fail(CRT_ERR_INVALID_ARG, "null context or stats");
+    *st = x->stats;
+    return CRT_OK;
+}
+
+crt_status crt_raygen_pinhole(crt_ctx* x, const crt_camera* cam, uint32_t width, uint32_t height, crt_ray* rays) {
+    if (!x || !cam || !rays) return fail(CRT_ERR_INVALID_ARG, "crt_raygen_pinhole: null argument");
+    if (width == 0 || height == 0 || height > 65535) return fail(CRT_ERR_INVALID_ARG, "bad image size");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const size_t n = static_cast<size_t>(width) * height;
+    const crt_camera* d_cam = cam;
+    if (!is_device_ptr(cam)) {
+        CRT_CUDA(cudaMemcpyAsync(x->cam.p, cam, sizeof(crt_camera), cudaMemcpyHostToDevice, x->stream));
+        d_cam = x->cam.as<crt_camera>();
+    }
+    const bool dev_out = is_device_ptr(rays);
+    crt_ray* d_rays = rays;
+    if (!dev_out) {
+        CRT_TRY(x->rays_out.reserve(sizeof(crt_ray) * n));
+        d_rays = x->rays_out.as<crt_ray>();
+    }
+    crt::launch_raygen(d_cam, width, height, d_rays, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(rays, d_rays, sizeof(crt_ray) * n, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+crt_status crt_shadow_rays(crt_ctx* x, const crt_ray* primary, const crt_hit* hits, uint32_t n, const float light[3],
+                           crt_ray* shadow) {
+    if (!x || !primary || !hits || !light || !shadow) return fail(CRT_ERR_INVALID_ARG, "crt_shadow_rays: null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n == 0) return CRT_OK;
+    const crt_ray* d_prim = primary;
+    const crt_hit* d_hits = hits;
+    if (!is_device_ptr(primary)) {
+        CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n));
+        CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, primary, sizeof(crt_ray) * n, cudaMemcpyHostToDevice, x->stream));
+        d_prim = x->rays_in.as<crt_ray>();
+    }
+    if (!is_device_ptr(hits)) {
+        CRT_TRY(x->hits_out.reserve(sizeof(crt_hit) * n));
+        CRT_CUDA(cudaMemcpyAsync(x->hits_out.p, hits, sizeof(crt_hit) * n, cudaMemcpyHostToDevice, x->stream));
+        d_hits = x->hits_out.as<crt_hit>();
+    }
+    const bool dev_out = is_device_ptr(shadow);
+    crt_ray* d_out = shadow;
+    if (!dev_out) {
+        CRT_TRY(x->rays_out.reserve(sizeof(crt_ray) * n));
+        d_out = x->rays_out.as<crt_ray>();
+    }
+    crt::launch_shadow_rays(d_prim, d_hits, n, light[0], light[1], light[2], d_out, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(shadow, d_out, sizeof(crt_ray) * n, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t n_rays, uint32_t flags, crt_hit* hits) {
+    if (!x || !b || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_trace: null argument");
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR))
+        return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
+    if (flags & CRT_TRACE_USE_PREDICTOR) return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor attached");
+    if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_trace: empty bvh");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n_rays == 0) return CRT_OK;
+    const crt_ray* d_rays = rays;
+    if (!is_device_ptr(rays)) {
+        CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
+        CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, rays, sizeof(crt_ray) * n_rays, cudaMemcpyHostToDevice, x->stream));
+        d_rays = x->rays_in.as<crt_ray>();
+    }
+    const bool dev_out = is_device_ptr(hits);
+    crt_hit* d_hits = hits;
+    if (!dev_out) {
+        CRT_TRY(x->hits_out.reserve(sizeof(crt_hit) * n_rays));
+        d_hits = x->hits_out.as<crt_hit>();
+    }
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    crt::TraceParams p{};
+    p.nodes = b->nodes.as<crt_bvh_node>();
+    p.xtri = b->xtri.as<float4>();
+    p.rays = d_rays;
+    p.hits = d_hits;
+    p.n_rays = n_rays;
+    p.n_nodes = 2 * b->n - 1;
+    p.abs_eps = b->abs_eps;
+    p.err = x->err.as<uint32_t>();
+    p.stats = nullptr;
+    const uint32_t launch_flags = (flags & 0xFFFFu) | ((b->iterations + 2 > 64) ? (1u << 16) : 0u);
+    crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(hits, d_hits, sizeof(crt_hit) * n_rays, cudaMemcpyDeviceToHost, x->stream));
+    return x->check_device_error();
+}
+
+}  // extern "C"

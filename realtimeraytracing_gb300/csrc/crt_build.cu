@@ -1,0 +1,623 @@
+// BVH build kernels of libcrt: scene box, Morton codes, Onesweep LSD radix
+// sort of (code, index), PLOC iterations and the DFS node layout.
+//
+// Reference: srcCommon/scene/geometry/bvh.cpp (CPU, OpenMP) and the DFS
+// flattening in srcOpenGL/scene/scene.cpp:189-208.  Every float result is
+// bit-identical to the reference's (this file is compiled with -fmad=false).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "crt_build.cuh"
+#include "crt_common.cuh"
+
+namespace crt {
+
+// =========================================================== K1: scene box
+// getSceneAABB (bvh.cpp:235-251) folds max(cur, max(p0, max(p1, p2))) over
+// all n_buffer records in order.  That fold ignores NaN candidates and keeps
+// the earliest of equal values, so it equals the leftmost arg-max over
+// non-NaN per-triangle values — an associative reduction.  Each candidate is
+// keyed (ordered value, index); the winner's exact value (sign of zero
+// included) is recomputed from its triangle.
+
+struct TriExtent { float hi[3], lo[3]; };
+
+__device__ __forceinline__ TriExtent tri_extent(const TriRec& t, const float* __restrict__ models) {
+    const float* M = models + 16 * (t.model & (kMaxModels - 1));
+    const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
+    TriExtent e;
+    e.hi[0] = max_std(p0.x, max_std(p1.x, p2.x));
+    e.hi[1] = max_std(p0.y, max_std(p1.y, p2.y));
+    e.hi[2] = max_std(p0.z, max_std(p1.z, p2.z));
+    e.lo[0] = min_std(p0.x, min_std(p1.x, p2.x));
+    e.lo[1] = min_std(p0.y, min_std(p1.y, p2.y));
+    e.lo[2] = min_std(p0.z, min_std(p1.z, p2.z));
+    return e;
+}
+
+__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v, int m) {
+    return __shfl_xor_sync(0xFFFFFFFFu, v, m);
+}
+
+__global__ void __launch_bounds__(256) scene_box_kernel(const crt_triangle* __restrict__ tris, uint32_t n_buffer,
+                                                        const float* __restrict__ models, SceneState* st,
+                                                        uint32_t* err) {
+    unsigned long long kmax[3] = {0ull, 0ull, 0ull};
+    unsigned long long kmin[3] = {~0ull, ~0ull, ~0ull};
+    bool bad = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_buffer; i += gridDim.x * blockDim.x) {
+        const TriRec t = load_tri(tris, i);
+        bad |= t.model >= kMaxModels;
+        const TriExtent e = tri_extent(t, models);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (e.hi[a] == e.hi[a]) {
+                const unsigned long long k = (static_cast<unsigned long long>(ordered_key(e.hi[a])) << 32) | (0xFFFFFFFFu - i);
+                kmax[a] = k > kmax[a] ? k : kmax[a];
+            }
+            if (e.lo[a] == e.lo[a]) {
+                const unsigned long long k = (static_cast<unsigned long long>(ordered_key(e.lo[a])) << 32) | i;
+                kmin[a] = k < kmin[a] ? k : kmin[a];
+            }
+        }
+    }
+    if (bad) raise_error(err, kDevBadModel);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        for (int m = 16; m > 0; m >>= 1) {
+            const unsigned long long x = shfl_xor_u64(kmax[a], m), y = shfl_xor_u64(kmin[a], m);
+            kmax[a] = x > kmax[a] ? x : kmax[a];
+            kmin[a] = y < kmin[a] ? y : kmin[a];
+        }
+    __shared__ unsigned long long s_k[6][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) { s_k[a][warp] = kmax[a]; s_k[3 + a][warp] = kmin[a]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int a = threadIdx.x;
+        const int nw = blockDim.x >> 5;
+        unsigned long long v = s_k[a][0];
+        for (int w = 1; w < nw; ++w) v = (a < 3) ? (s_k[a][w] > v ? s_k[a][w] : v) : (s_k[a][w] < v ? s_k[a][w] : v);
+        if (a < 3) atomicMax(&st->key_max[a], v); else atomicMin(&st->key_min[a - 3], v);
+    }
+    // The last block to finish turns the keys into the box and the cube.
+    __shared__ bool s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&st->blocks_done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!s_last || threadIdx.x != 0) return;
+    __threadfence();
+    const float kInf = __int_as_float(0x7F800000);
+    float smin[3], smax[3];
+    for (int a = 0; a < 3; ++a) {
+        const unsigned long long kx = atomicAdd(&st->key_max[a], 0ull);
+        const unsigned long long kn = atomicAdd(&st->key_min[a], 0ull);
+        smax[a] = -kInf;
+        smin[a] = kInf;
+        if (kx != 0ull) smax[a] = tri_extent(load_tri(tris, 0xFFFFFFFFu - static_cast<uint32_t>(kx)), models).hi[a];
+        if (kn != ~0ull) smin[a] = tri_extent(load_tri(tris, static_cast<uint32_t>(kn)), models).lo[a];
+        st->key_max[a] = 0ull;
+        st->key_min[a] = ~0ull;
+    }
+    st->blocks_done = 0u;
+    // getCircumscribedCube (bvh.cpp:253-303): X is chosen whenever distX > 0.
+    float cmn[3] = {smin[0], smin[1], smin[2]}, cmx[3] = {smax[0], smax[1], smax[2]};
+    const float dX = smax[0] - smin[0], dY = smax[1] - smin[1], dZ = smax[2] - smin[2];
+    float maxDist = 0.f;
+    int axis;
+    if (dX > maxDist) { maxDist = dX; axis = 0; }
+    else if (dY > maxDist) { maxDist = dY; axis = 1; }
+    else { maxDist = dZ; axis = 2; }
+    const float dist[3] = {dX, dY, dZ};
+    for (int a = 0; a < 3; ++a) {
+        if (a == axis) continue;
+        const float delta = (maxDist - dist[a]) / 2.f;
+        cmx[a] += delta;
+        cmn[a] -= delta;
+    }
+    for (int a = 0; a < 3; ++a) {
+        st->scene_min[a] = smin[a];
+        st->scene_max[a] = smax[a];
+        st->cube_min[a] = cmn[a];
+        st->cube_len[a] = cmx[a] - cmn[a];  // getNormalizedCentroids (bvh.cpp:319-321)
+    }
+}
+
+// ====================================================== K1: Morton codes
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v) {  // bvh.cpp:350-356
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t to_u10(float x) {  // bvh.cpp:363-367
+    x = min_std(max_std(x * 1024.0f, 0.0f), 1023.0f);
+    return __float2uint_rz(x);  // NaN -> 0, as on the reference's hosts
+}
+
+// Centroid (triangle.cpp:31-33), normalisation (bvh.cpp:314-328) and code
+// (bvh.cpp:358-372), plus the digit histograms of all radix passes.
+template <int BITS>
+__global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restrict__ tris, uint32_t n,
+                                                     const float* __restrict__ models_third,
+                                                     const SceneState* __restrict__ st,
+                                                     uint32_t* __restrict__ codes, uint32_t* __restrict__ hist) {
+    constexpr int RADIX = 1 << BITS;
+    constexpr int PASSES = (30 + BITS - 1) / BITS;
+    __shared__ uint32_t s_hist[PASSES * RADIX];
+    for (int i = threadIdx.x; i < PASSES * RADIX; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    const float cmx = st->cube_min[0], cmy = st->cube_min[1], cmz = st->cube_min[2];
+    const float lx = st->cube_len[0], ly = st->cube_len[1], lz = st->cube_len[2];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const TriRec t = load_tri(tris, i);
+        const float* M3 = models_third + 16 * (t.model & (kMaxModels - 1));
+        float4 s;
+        s.x = t.p0.x + t.p1.x + t.p2.x;
+        s.y = t.p0.y + t.p1.y + t.p2.y;
+        s.z = t.p0.z + t.p1.z + t.p2.z;
+        s.w = t.p0.w + t.p1.w + t.p2.w;
+        const float4 c = mat_vec(M3, s);
+        const float nx = (c.x - cmx) / lx, ny = (c.y - cmy) / ly, nz = (c.z - cmz) / lz;
+        const uint32_t code = (expand_bits(to_u10(nx)) << 2) | (expand_bits(to_u10(ny)) << 1) | expand_bits(to_u10(nz));
+        codes[i] = code;
+#pragma unroll
+        for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p * RADIX + ((code >> (p * BITS)) & (RADIX - 1))], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < PASSES * RADIX; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+// ============================================== K2: Onesweep digit binning
+// One stable counting pass over digit (key >> shift) & (RADIX-1) of a tile
+// of BLOCK*KPT keys: warp-level multisplit with __match_any_sync, per-warp
+// digit counters in shared memory, chained-scan decoupled look-back across
+// tiles for the global digit offsets (Adinets & Merrill, "Onesweep", 2022),
+// and a shared-memory staged scatter.  Pass 0 synthesises the values
+// (iota), which makes the result the reference's std::sort of (code, index)
+// pairs (bvh.cpp:214-232).
+constexpr uint32_t kLbAgg = 1u << 30, kLbPrefix = 2u << 30, kLbMask = (1u << 30) - 1u;
+
+template <int BITS, int BLOCK, int KPT>
+__global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restrict__ keys_in,
+                                                         const uint32_t* __restrict__ vals_in,
+                                                         uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                         uint32_t n, int shift, const uint32_t* __restrict__ pass_hist,
+                                                         uint32_t* lookback, uint32_t* ticket, uint32_t* err,
+                                                         uint32_t spin_limit) {
+    constexpr int RADIX = 1 << BITS;
+    constexpr int WARPS = BLOCK / 32;
+    constexpr int TILE = BLOCK * KPT;
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+    __shared__ uint32_t s_keys[TILE];
+    __shared__ uint32_t s_vals[TILE];
+    __shared__ uint32_t s_whist[WARPS][RADIX];
+    __shared__ uint32_t s_start[RADIX];   // block-local exclusive digit start
+    __shared__ uint32_t s_dest[RADIX];    // global destination of the digit's first key
+    __shared__ uint32_t s_scan[BLOCK / 32];
+    __shared__ uint32_t s_tile;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) (&s_whist[0][0])[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t tile_base = static_cast<uint64_t>(tile) * TILE;
+    if (tile_base >= n) return;
+    const uint64_t rem = n - tile_base;
+    const uint32_t tile_n = rem < static_cast<uint64_t>(TILE) ? static_cast<uint32_t>(rem) : static_cast<uint32_t>(TILE);
+
+    uint32_t key[KPT], val[KPT], rank[KPT];
+    const uint64_t wbase = tile_base + static_cast<uint64_t>(warp) * 32 * KPT;
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
+        const bool ok = idx < n;
+        key[j] = ok ? __ldg(keys_in + idx) : 0u;
+        val[j] = ok ? (vals_in ? __ldg(vals_in + idx) : static_cast<uint32_t>(idx)) : 0u;
+    }
+    const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
+        const uint32_t d = (idx < n) ? ((key[j] >> shift) & (RADIX - 1)) : static_cast<uint32_t>(RADIX);
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (lane == leader && d < RADIX) {
+            base = s_whist[warp][d];
+            s_whist[warp][d] = base + __popc(peers);
+        }
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        rank[j] = base + __popc(peers & lt_mask);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // Per digit: exclusive over warps, tile total, look-back, global base.
+    uint32_t total = 0, excl = 0;
+    const int d = threadIdx.x;
+    if (d < RADIX) {
+        for (int w = 0; w < WARPS; ++w) {
+            const uint32_t c = s_whist[w][d];
+            s_whist[w][d] = total;
+            total += c;
+        }
+        uint32_t* my = lookback + static_cast<size_t>(tile) * RADIX + d;
+        if (tile == 0) {
+            st_release_u32(my, kLbPrefix | total);
+        } else {
+            st_release_u32(my, kLbAgg | total);
+            int64_t k = static_cast<int64_t>(tile) - 1;
+            SpinBound spin(spin_limit);
+            while (k >= 0) {
+                const uint32_t v = ld_acquire_u32(lookback + static_cast<size_t>(k) * RADIX + d);
+                const uint32_t f = v & ~kLbMask;
+                if (f == 0u) {
+                    if (!spin.step()) { raise_error(err, kDevTimeout); break; }
+                    continue;
+                }
+                excl += v & kLbMask;
+                if (f == kLbPrefix) break;
+                --k;
+            }
+            st_release_u32(my, kLbPrefix | (excl + total));
+        }
+    }
+    // Block-wide exclusive scans over digits of (tile totals) and (global histogram).
+    uint32_t gh = (d < RADIX) ? pass_hist[d] : 0u;
+    uint32_t a = (d < RADIX) ? total : 0u;
+    // warp-level inclusive scan of a and gh packed as two 32-bit lanes of 64 bits
+    unsigned long long packed = (static_cast<unsigned long long>(gh) << 32) | a;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, packed, o);
+        if (lane >= o) packed += y;
+    }
+    __shared__ unsigned long long s_wsum[BLOCK / 32];
+    if (lane == 31) s_wsum[warp] = packed;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long run = 0;
+        for (int w = 0; w < BLOCK / 32; ++w) { const unsigned long long t = s_wsum[w]; s_wsum[w] = run; run += t; }
+    }
+    __syncthreads();
+    packed += s_wsum[warp];
+    if (d < RADIX) {
+        const uint32_t incl_a = static_cast<uint32_t>(packed & 0xFFFFFFFFull);
+        const uint32_t incl_g = static_cast<uint32_t>(packed >> 32);
+        s_start[d] = incl_a - a;
+        s_dest[d] = (incl_g - gh) + excl;
+    }
+    (void)s_scan;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
+        if (idx < n) {
+            const uint32_t dd = (key[j] >> shift) & (RADIX - 1);
+            const uint32_t p = s_start[dd] + s_whist[warp][dd] + rank[j];
+            s_keys[p] = key[j];
+            s_vals[p] = val[j];
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < tile_n; i += BLOCK) {
+        const uint32_t k = s_keys[i];
+        const uint32_t dd = (k >> shift) & (RADIX - 1);
+        const uint32_t dst = s_dest[dd] + (i - s_start[dd]);
+        keys_out[dst] = k;
+        vals_out[dst] = s_vals[i];
+    }
+}
+
+// ==================================================== leaf clusters
+// plocPreprocessing (bvh.cpp:26-46): sorted position i holds the leaf of
+// triangle perm[i] with AABB::buildFromTriangle's box (bvh.cpp:383-399).
+// Also stores the model-transformed vertices the traversal tests against.
+__global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __restrict__ tris, uint32_t n,
+                                                        const float* __restrict__ models,
+                                                        const uint32_t* __restrict__ perm,
+                                                        float4* __restrict__ node_box, float4* __restrict__ clusters,
+                                                        float4* __restrict__ xtri, uint2* it, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) it[0] = make_uint2(n, n);
+    if (i >= n) return;
+    const uint32_t ti = perm[i];
+    if (ti >= n) { raise_error(err, kDevCorrupt); return; }
+    const TriRec t = load_tri(tris, ti);
+    const float* M = models + 16 * (t.model & (kMaxModels - 1));
+    const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
+    float4 mn, mx;
+    mn.x = min_std(p0.x, min_std(p1.x, p2.x));
+    mn.y = min_std(p0.y, min_std(p1.y, p2.y));
+    mn.z = min_std(p0.z, min_std(p1.z, p2.z));
+    mx.x = max_std(p0.x, max_std(p1.x, p2.x));
+    mx.y = max_std(p0.y, max_std(p1.y, p2.y));
+    mx.z = max_std(p0.z, max_std(p1.z, p2.z));
+    mn.w = __uint_as_float(ti);
+    mx.w = 0.f;
+    node_box[2 * static_cast<size_t>(i)] = mn;
+    node_box[2 * static_cast<size_t>(i) + 1] = mx;
+    mn.w = __uint_as_float(i);
+    mx.w = __uint_as_float(1u);
+    clusters[2 * static_cast<size_t>(i)] = mn;
+    clusters[2 * static_cast<size_t>(i) + 1] = mx;
+    xtri[3 * static_cast<size_t>(ti) + 0] = make_float4(p0.x, p0.y, p0.z, 0.f);
+    xtri[3 * static_cast<size_t>(ti) + 1] = make_float4(p1.x, p1.y, p1.z, 0.f);
+    xtri[3 * static_cast<size_t>(ti) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
+}
+
+// ================================================ K3: one PLOC iteration
+// For the n live clusters (Morton order, 32-byte records: min.xyz|node id,
+// max.xyz|leaf count) this does, per tile of TILE positions:
+//   nearest neighbour in [i-R, i+R] by surface area of the merged box,
+//     first strict minimum = lowest j on ties (bvh.cpp:193-210),
+//   mutual pairs merge at the lower position (bvh.cpp:159-191),
+//   exclusive scan of survivors and compaction (bvh.cpp:125-156),
+// with the scans across tiles done by decoupled look-back, so one launch is
+// one reference iteration.  NN of positions up to R outside the tile are
+// recomputed locally (their boxes 2R outside are staged in shared memory).
+// New nodes get ids it[iter].y + (merges before them); the last tile writes
+// it[iter+1] = (live clusters, next id).
+//
+// The search compares areas computed from fminf/fmaxf boxes; those differ
+// from the std::min/max boxes only in the sign of a zero, which changes no
+// difference max - min and no comparison, so the chosen neighbour is the
+// reference's.  Stored boxes use std::min/max semantics.
+constexpr unsigned long long kPlAgg = 1ull << 62, kPlPrefix = 2ull << 62;
+constexpr unsigned long long kPlMask31 = (1ull << 31) - 1ull;
+
+__device__ __forceinline__ float sa_merged(float4 amn, float4 amx, float4 bmn, float4 bmx) {
+    const float dx = fmaxf(amx.x, bmx.x) - fminf(amn.x, bmn.x);
+    const float dy = fmaxf(amx.y, bmx.y) - fminf(amn.y, bmn.y);
+    const float dz = fmaxf(amx.z, bmx.z) - fminf(amn.z, bmn.z);
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+template <int TILE, int BLOCK, int MAXR>
+__global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __restrict__ cin, float4* __restrict__ cout,
+                                                               float4* __restrict__ node_box, uint32_t* __restrict__ node_lc,
+                                                               uint2* it, int iter, uint32_t N,
+                                                               int R, unsigned long long* lookback, uint32_t* tickets,
+                                                               uint32_t n_tiles_cap, uint32_t* err, uint32_t spin_limit) {
+    constexpr int IPT = TILE / BLOCK;
+    constexpr int SPAN = TILE + 4 * MAXR;
+    constexpr int NNSPAN = TILE + 2 * MAXR;
+    __shared__ float4 s_mn[SPAN];
+    __shared__ float4 s_mx[SPAN];
+    __shared__ uint32_t s_nn[NNSPAN];
+    __shared__ uint32_t s_wsum[BLOCK / 32];
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_prefix;
+
+    const uint2 cur = it[iter];
+    const uint32_t n = cur.x;
+    if (n <= 1u) return;
+    unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
+    unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t s = tile * TILE;
+    if (s >= n) return;
+    if (tile == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
+    if (threadIdx.x == 0) lb_next[tile] = 0ull;
+    const uint32_t e = min(n, s + TILE);
+    const int lo = max(0, static_cast<int>(s) - 2 * R);
+    const int hi = min(static_cast<int>(n), static_cast<int>(e) + 2 * R);
+    for (int p = lo + threadIdx.x; p < hi; p += BLOCK) {
+        s_mn[p - lo] = cin[2 * static_cast<size_t>(p)];
+        s_mx[p - lo] = cin[2 * static_cast<size_t>(p) + 1];
+    }
+    __syncthreads();
+    const int nlo = max(0, static_cast<int>(s) - R);
+    const int nhi = min(static_cast<int>(n), static_cast<int>(e) + R);
+    for (int p = nlo + threadIdx.x; p < nhi; p += BLOCK) {
+        const float4 amn = s_mn[p - lo], amx = s_mx[p - lo];
+        const int j0 = max(0, p - R), j1 = min(static_cast<int>(n), p + R + 1);
+        float best = __int_as_float(0x7F800000);
+        int bj = p;
+        for (int j = j0; j < j1; ++j) {
+            if (j == p) continue;
+            const float dd = sa_merged(amn, amx, s_mn[j - lo], s_mx[j - lo]);
+            if (dd < best) { best = dd; bj = j; }
+        }
+        s_nn[p - nlo] = static_cast<uint32_t>(bj);
+    }
+    __syncthreads();
+
+    // Decisions for the tile's own positions: thread t owns [s + t*IPT, +IPT).
+    uint32_t flags = 0;  // bit q: valid, bit 16+q: merge head
+    uint32_t nv = 0, nm = 0;
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+        const int p = static_cast<int>(s) + threadIdx.x * IPT + q;
+        if (p >= static_cast<int>(e)) break;
+        const int j = static_cast<int>(s_nn[p - nlo]);
+        const bool mutual = (j != p) && (static_cast<int>(s_nn[j - nlo]) == p);
+        const bool head = mutual && p < j;
+        const bool gone = mutual && p > j;
+        if (!gone) { flags |= 1u << q; ++nv; }
+        if (head) { flags |= 1u << (16 + q); ++nm; }
+    }
+    // Block exclusive scan of (nv, nm) packed as 16|16 bits.
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t packed = (nv << 16) | nm, incl = packed;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int w = 0; w < BLOCK / 32; ++w) { const uint32_t t = s_wsum[w]; s_wsum[w] = run; run += t; }
+        const unsigned long long tv = run >> 16, tm = run & 0xFFFFu;
+        // look-back over preceding tiles
+        unsigned long long ev = 0, em = 0;
+        if (tile == 0) {
+            st_release_u64(&lb_cur[0], kPlPrefix | (tv << 31) | tm);
+        } else {
+            st_release_u64(&lb_cur[tile], kPlAgg | (tv << 31) | tm);
+            int k = static_cast<int>(tile) - 1;
+            SpinBound spin(spin_limit);
+            while (k >= 0) {
+                const unsigned long long v = ld_acquire_u64(&lb_cur[k]);
+                const unsigned long long f = v & (3ull << 62);
+                if (f == 0ull) {
+                    if (!spin.step()) { raise_error(err, kDevTimeout); break; }
+                    continue;
+                }
+                ev += (v >> 31) & kPlMask31;
+                em += v & kPlMask31;
+                if (f == kPlPrefix) break;
+                --k;
+            }
+            st_release_u64(&lb_cur[tile], kPlPrefix | ((ev + tv) << 31) | (em + tm));
+        }
+        s_prefix = (ev << 32) | em;
+        if (e == n)  // last tile: size and id base of the next iteration
+            it[iter + 1] = make_uint2(static_cast<uint32_t>(ev + tv), cur.y + static_cast<uint32_t>(em + tm));
+    }
+    __syncthreads();
+    const uint32_t excl = s_wsum[warp] + (incl - packed);
+    uint32_t out_v = static_cast<uint32_t>(s_prefix >> 32) + (excl >> 16);
+    uint32_t out_m = cur.y + static_cast<uint32_t>(s_prefix & 0xFFFFFFFFull) + (excl & 0xFFFFu);
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+        if (!(flags & (1u << q))) continue;
+        const int p = static_cast<int>(s) + threadIdx.x * IPT + q;
+        float4 mn = s_mn[p - lo], mx = s_mx[p - lo];
+        if (flags & (1u << (16 + q))) {
+            const int j = static_cast<int>(s_nn[p - nlo]);
+            const float4 bmn = s_mn[j - lo], bmx = s_mx[j - lo];
+            const uint32_t id = out_m++;
+            if (id >= 2 * N - 1 || id < N) { raise_error(err, kDevCorrupt); continue; }
+            float4 m0, m1;  // AABB::merge (bvh.cpp:401-413), first argument = lower position
+            m0.x = min_std(mn.x, bmn.x); m0.y = min_std(mn.y, bmn.y); m0.z = min_std(mn.z, bmn.z);
+            m1.x = max_std(mx.x, bmx.x); m1.y = max_std(mx.y, bmx.y); m1.z = max_std(mx.z, bmx.z);
+            m0.w = mn.w;   // left child id
+            m1.w = bmn.w;  // right child id
+            node_box[2 * static_cast<size_t>(id)] = m0;
+            node_box[2 * static_cast<size_t>(id) + 1] = m1;
+            const uint32_t lc = __float_as_uint(mx.w) + __float_as_uint(bmx.w);
+            node_lc[id - N] = lc;
+            mn = make_float4(m0.x, m0.y, m0.z, __uint_as_float(id));
+            mx = make_float4(m1.x, m1.y, m1.z, __uint_as_float(lc));
+        }
+        if (out_v >= n) { raise_error(err, kDevCorrupt); continue; }
+        cout[2 * static_cast<size_t>(out_v)] = mn;
+        cout[2 * static_cast<size_t>(out_v) + 1] = mx;
+        ++out_v;
+    }
+}
+
+// ================================================== K4: DFS node layout
+// Scene::recursiveTopDownTraversalBVH (scene.cpp:189-201): pre-order, left
+// subtree first, root (the last merge, id 2N-2) at 0.  A node at position p
+// puts its left child at p+1 and its right child at p + 2*leaves(left).
+// Nodes created in PLOC iteration k only have parents from later
+// iterations, so levels are laid out from the last iteration down.
+__global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
+                                                           const uint32_t* __restrict__ node_lc,
+                                                           uint32_t* __restrict__ pos, uint32_t id_begin, uint32_t id_end,
+                                                           uint32_t N, crt_bvh_node* __restrict__ out, uint32_t* err) {
+    const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (X >= id_end) return;
+    const uint32_t p = (X == 2 * N - 2) ? 0u : pos[X - N];
+    const float4 mn = node_box[2 * static_cast<size_t>(X)], mx = node_box[2 * static_cast<size_t>(X) + 1];
+    const uint32_t a = __float_as_uint(mn.w), b = __float_as_uint(mx.w);
+    const uint32_t lca = (a < N) ? 1u : node_lc[a - N];
+    const uint32_t pl = p + 1, pr = p + 2 * lca;
+    if (pr >= 2 * N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
+        raise_error(err, kDevCorrupt);
+        return;
+    }
+    float4* o = reinterpret_cast<float4*>(out + p);
+    o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
+    o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
+    reinterpret_cast<uint4*>(o)[2] = make_uint4(0u, pl, pr, 0u);
+    const uint32_t ch[2] = {a, b}, cp[2] = {pl, pr};
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        if (ch[c] < N) {
+            const float4 lmn = node_box[2 * static_cast<size_t>(ch[c])], lmx = node_box[2 * static_cast<size_t>(ch[c]) + 1];
+            float4* lo = reinterpret_cast<float4*>(out + cp[c]);
+            lo[0] = make_float4(lmn.x, lmn.y, lmn.z, 0.f);
+            lo[1] = make_float4(lmx.x, lmx.y, lmx.z, 0.f);
+            reinterpret_cast<uint4*>(lo)[2] = make_uint4(__float_as_uint(lmn.w), 0u, 0u, 0u);
+        } else {
+            pos[ch[c] - N] = cp[c];
+        }
+    }
+}
+
+__global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out) {
+    const float4 mn = node_box[0], mx = node_box[1];
+    float4* o = reinterpret_cast<float4*>(out);
+    o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
+    o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
+    reinterpret_cast<uint4*>(o)[2] = make_uint4(__float_as_uint(mn.w), 0u, 0u, 0u);
+}
+
+// ============================================================ launchers
+void launch_scene_box(const crt_triangle* tris, uint32_t n_buffer, const float* models, SceneState* st, uint32_t* err,
+                      cudaStream_t s) {
+    const uint32_t want = (n_buffer + 255) / 256;
+    const uint32_t grid = want < static_cast<uint32_t>(kNumSms * 8) ? (want ? want : 1u) : kNumSms * 8;
+    scene_box_kernel<<<grid, 256, 0, s>>>(tris, n_buffer, models, st, err);
+}
+
+void launch_morton(const crt_triangle* tris, uint32_t n, const float* models_third, const SceneState* st,
+                   uint32_t* codes, uint32_t* hist, int bits, cudaStream_t s) {
+    const uint32_t want = (n + 255) / 256;
+    const uint32_t grid = want < static_cast<uint32_t>(kNumSms * 8) ? (want ? want : 1u) : kNumSms * 8;
+    if (bits == 4) morton_kernel<4><<<grid, 256, 0, s>>>(tris, n, models_third, st, codes, hist);
+    else morton_kernel<8><<<grid, 256, 0, s>>>(tris, n, models_third, st, codes, hist);
+}
+
+uint32_t sort_tile_keys(int bits) { return bits == 4 ? 256u * 16u : 256u * 16u; }
+
+void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, uint32_t n,
+                     int shift, int bits, const uint32_t* pass_hist, uint32_t* lookback, uint32_t* ticket, uint32_t* err,
+                     uint32_t spin_limit, cudaStream_t s) {
+    const uint32_t tiles = (n + sort_tile_keys(bits) - 1) / sort_tile_keys(bits);
+    if (bits == 4)
+        onesweep_kernel<4, 256, 16><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, pass_hist,
+                                                           lookback, ticket, err, spin_limit);
+    else
+        onesweep_kernel<8, 256, 16><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, pass_hist,
+                                                           lookback, ticket, err, spin_limit);
+}
+
+void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
+                      float4* clusters, float4* xtri, uint2* it, uint32_t* err, cudaStream_t s) {
+    leaf_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(tris, n, models, perm, node_box, clusters, xtri, it, err);
+}
+
+void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,
+                           int iter, uint32_t N, int radius, uint32_t n_upper,
+                           unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
+                           uint32_t spin_limit, cudaStream_t s) {
+    const uint32_t tiles = (n_upper + kPlocTile - 1) / kPlocTile;
+    ploc_iteration_kernel<kPlocTile, 256, kPlocMaxRadius><<<tiles ? tiles : 1u, 256, 0, s>>>(
+        cin, cout, node_box, node_lc, it, iter, N, radius, lookback, tickets, n_tiles_cap, err, spin_limit);
+}
+
+void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint32_t* pos, uint32_t id_begin,
+                         uint32_t id_end, uint32_t N, crt_bvh_node* out, uint32_t* err, cudaStream_t s) {
+    if (id_end <= id_begin || id_end > 2 * N - 1) return;
+    const uint32_t cnt = id_end - id_begin;
+    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pos, id_begin, id_end, N, out, err);
+}
+
+void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s) {
+    single_leaf_kernel<<<1, 1, 0, s>>>(node_box, out);
+}
+
+}  // namespace crt

@@ -1,0 +1,63 @@
+// Internal interface between the build kernels (crt_build.cu), the trace
+// kernels (crt_trace.cu) and the C ABI (crt_api.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "crt.h"
+
+namespace crt {
+
+constexpr uint32_t kPlocTile = 1024;      // positions per PLOC tile
+constexpr int kPlocMaxRadius = 32;        // largest supported PLOC radius
+
+// Scene box reduction state (device memory, zeroed keys at creation; the
+// finishing block resets it) and its results for the Morton pass.
+struct SceneState {
+    unsigned long long key_max[3];
+    unsigned long long key_min[3];
+    unsigned int blocks_done;
+    unsigned int pad;
+    float scene_min[3];
+    float scene_max[3];
+    float cube_min[3];
+    float cube_len[3];
+};
+
+void launch_scene_box(const crt_triangle* tris, uint32_t n_buffer, const float* models, SceneState* st, uint32_t* err,
+                      cudaStream_t s);
+void launch_morton(const crt_triangle* tris, uint32_t n, const float* models_third, const SceneState* st,
+                   uint32_t* codes, uint32_t* hist, int bits, cudaStream_t s);
+uint32_t sort_tile_keys(int bits);
+void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, uint32_t n,
+                     int shift, int bits, const uint32_t* pass_hist, uint32_t* lookback, uint32_t* ticket, uint32_t* err,
+                     uint32_t spin_limit, cudaStream_t s);
+void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
+                      float4* clusters, float4* xtri, uint2* it, uint32_t* err, cudaStream_t s);
+void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,
+                           int iter, uint32_t N, int radius, uint32_t n_upper,
+                           unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
+                           uint32_t spin_limit, cudaStream_t s);
+void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint32_t* pos, uint32_t id_begin,
+                         uint32_t id_end, uint32_t N, crt_bvh_node* out, uint32_t* err, cudaStream_t s);
+void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
+
+// Trace side (crt_trace.cu).
+struct TraceParams {
+    const crt_bvh_node* nodes;
+    const float4* xtri;      // 3 float4 per triangle: model-transformed p0, p1, p2
+    const crt_ray* rays;
+    crt_hit* hits;
+    uint32_t n_rays;
+    uint32_t n_nodes;
+    float abs_eps;           // absolute slack of pruning, from the scene extent
+    uint32_t* err;
+    unsigned long long* stats;  // optional: nodes visited, triangles tested
+};
+void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
+void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s);
+void launch_shadow_rays(const crt_ray* prim, const crt_hit* hits, uint32_t n, float lx, float ly, float lz, crt_ray* out,
+                        cudaStream_t s);
+
+}  // namespace crt

@@ -1,0 +1,329 @@
+// Ray generation and BVH2 traversal kernels of libcrt.
+//
+// Reference: srcCommon/shaders/raytracer.glsl — getRay :92-100,
+// rayTriangleIntersection :102-147, intersectBVH :182-221,
+// getClosestHitBVH :246-295.  Compiled with -fmad=false: every float
+// operation rounds once, in the shader's order, as in the CPU oracle.
+//
+// Traversal (one thread per ray, stack in local memory):
+//   * children are box-tested at their parent and visited near-first;
+//   * a subtree is skipped when its entry distance exceeds the best hit by
+//     more than a slack of |t| * 2^-14 + abs_eps (abs_eps = 2^-20 of the scene
+//     extent), so no triangle that can tie or beat the best is lost;
+//   * CRT_TRI_REFERENCE tests each leaf box with the shader's own slab test
+//     (which is monotone: a leaf box passes only if every ancestor box
+//     passes) and the triangle with the shader's predicate, so the tested set
+//     is the shader's; equal t keeps the leaf the shader visits first — the
+//     one with the higher DFS position, since the shader pops right children
+//     first;
+//   * CRT_TRI_WATERTIGHT grows every box by abs_eps and uses the watertight
+//     predicate (Woop, Benthin, Wald, JCGT 2013); equal t keeps the lower
+//     triangle index.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "crt_build.cuh"
+#include "crt_common.cuh"
+
+namespace crt {
+
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+
+struct HitRes { bool did; float t, u, v; };
+
+// raytracer.glsl:102-147; the GLSL struct order _P0,_P2,_P1 makes the
+// shader's p1 the C++ P2 and its p2 the C++ P1.
+__device__ __forceinline__ HitRes tri_reference(float3 o, float3 d, float tmin, float tmax, float3 P0, float3 P1, float3 P2) {
+    HitRes h{false, 0.f, 0.f, 0.f};
+    const float3 p0 = P0, p1 = P2, p2 = P1;
+    const float3 e0 = sub3(p1, p0);
+    const float3 e1 = sub3(p2, p0);
+    const float3 c = cross3(e1, e0);
+    const float inv = 1.0f / sqrtf(dot3(c, c));
+    const float3 nrm = make_float3(c.x * inv, c.y * inv, c.z * inv);
+    const float3 q = cross3(d, e1);
+    const float a = dot3(e0, q);
+    if (dot3(nrm, d) >= 0.f || fabsf(a) < 1e-4f) return h;
+    const float3 s = make_float3((o.x - p0.x) / a, (o.y - p0.y) / a, (o.z - p0.z) / a);
+    const float3 r = cross3(s, e0);
+    const float u = dot3(s, q);
+    const float v = dot3(r, d);
+    const float w = 1.0f - u - v;
+    if (u < 0.f || v < 0.f || w < 0.f) return h;
+    const float t = dot3(e1, r);
+    if (t < tmin || t > tmax) return h;
+    h.did = true; h.t = t; h.u = u; h.v = v;
+    return h;
+}
+
+struct WRay { int kx, ky, kz; float Sx, Sy, Sz; };
+
+__device__ __forceinline__ float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+__device__ __forceinline__ WRay wt_setup(float3 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    if (ay > ax) kz = 1;
+    if (az > (kz == 0 ? ax : ay)) kz = 2;
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    if (comp(d, kz) < 0.f) { const int t = kx; kx = ky; ky = t; }
+    WRay w;
+    w.kx = kx; w.ky = ky; w.kz = kz;
+    w.Sx = comp(d, kx) / comp(d, kz);
+    w.Sy = comp(d, ky) / comp(d, kz);
+    w.Sz = 1.0f / comp(d, kz);
+    return w;
+}
+
+__device__ __forceinline__ HitRes tri_watertight(float3 o, float tmin, float tmax, const WRay& w, float3 a3, float3 b3, float3 c3) {
+    HitRes h{false, 0.f, 0.f, 0.f};
+    const float3 A = sub3(a3, o), B = sub3(b3, o), C = sub3(c3, o);
+    const float Akz = comp(A, w.kz), Bkz = comp(B, w.kz), Ckz = comp(C, w.kz);
+    const float Ax = comp(A, w.kx) - w.Sx * Akz;
+    const float Ay = comp(A, w.ky) - w.Sy * Akz;
+    const float Bx = comp(B, w.kx) - w.Sx * Bkz;
+    const float By = comp(B, w.ky) - w.Sy * Bkz;
+    const float Cx = comp(C, w.kx) - w.Sx * Ckz;
+    const float Cy = comp(C, w.ky) - w.Sy * Ckz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = static_cast<float>(static_cast<double>(Cx) * By - static_cast<double>(Cy) * Bx);
+        V = static_cast<float>(static_cast<double>(Ax) * Cy - static_cast<double>(Ay) * Cx);
+        W = static_cast<float>(static_cast<double>(Bx) * Ay - static_cast<double>(By) * Ax);
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return h;
+    const float det = U + V + W;
+    if (det == 0.f) return h;
+    const float Az = w.Sz * Akz, Bz = w.Sz * Bkz, Cz = w.Sz * Ckz;
+    const float T = U * Az + V * Bz + W * Cz;
+    const float t = T / det;
+    if (!(t >= tmin) || !(t <= tmax)) return h;
+    h.did = true; h.t = t; h.u = V / det; h.v = W / det;
+    return h;
+}
+
+struct RayCtx {
+    float3 o, d, inv;
+    bool exact;   // some 1/d component is not finite or zero: use the shader's min/max
+};
+
+// Slab test.  exact: raytracer.glsl:182-221 with GLSL min/max and early
+// exits.  Otherwise fminf/fmaxf, which decide identically when every 1/d is
+// finite and nonzero (no NaN can arise; a zero's sign changes no comparison).
+// grow widens the box on every side (watertight mode).
+__device__ __forceinline__ bool slab(const RayCtx& r, float4 mn, float4 mx, float grow, float& t_enter) {
+    const float mnx = mn.x - grow, mny = mn.y - grow, mnz = mn.z - grow;
+    const float mxx = mx.x + grow, mxy = mx.y + grow, mxz = mx.z + grow;
+    const float tx1 = (mnx - r.o.x) * r.inv.x, tx2 = (mxx - r.o.x) * r.inv.x;
+    const float ty1 = (mny - r.o.y) * r.inv.y, ty2 = (mxy - r.o.y) * r.inv.y;
+    const float tz1 = (mnz - r.o.z) * r.inv.z, tz2 = (mxz - r.o.z) * r.inv.z;
+    if (!r.exact) {
+        const float t0 = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
+        const float t1 = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
+        t_enter = t0;
+        return t1 >= 0.f && t0 <= t1;
+    }
+    float tMin = min_std(tx1, tx2), tMax = max_std(tx1, tx2);
+    t_enter = tMin;
+    if (tMax < 0.f || tMin > tMax) return false;
+    tMin = max_std(tMin, min_std(ty1, ty2));
+    tMax = min_std(tMax, max_std(ty1, ty2));
+    t_enter = tMin;
+    if (tMax < 0.f || tMin > tMax) return false;
+    tMin = max_std(tMin, min_std(tz1, tz2));
+    tMax = min_std(tMax, max_std(tz1, tz2));
+    t_enter = tMin;
+    return tMax >= 0.f && tMin <= tMax;
+}
+
+__device__ __forceinline__ float prune_bound(float t, float abs_eps) {
+    return t + (fabsf(t) * 6.103515625e-05f + abs_eps);  // 2^-14 relative
+}
+
+template <bool ANY, bool WT, int STACK>
+__global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n_rays) return;
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
+    const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
+    RayCtx r;
+    r.o = make_float3(r0.x, r0.y, r0.z);
+    r.d = make_float3(r1.x, r1.y, r1.z);
+    const float tmin = r0.w, tmax = r1.w;
+    uint4 out = make_uint4(CRT_MISS, 0u, 0u, 0u);
+    if (!(tmin <= tmax) || p.n_nodes == 0) {
+        reinterpret_cast<uint4*>(p.hits)[i] = out;
+        return;
+    }
+    r.inv = make_float3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+    r.exact = !(isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && r.inv.x != 0.f && r.inv.y != 0.f &&
+                r.inv.z != 0.f);
+    WRay w{};
+    if (WT) w = wt_setup(r.d);
+    const float grow = WT ? p.abs_eps : 0.f;
+
+    bool have = false;
+    float bt = tmax, bu = 0.f, bv = 0.f;
+    uint32_t bkey = 0xFFFFFFFFu, btri = CRT_MISS;
+    uint64_t visited = 0, tested = 0;
+    bool overflow = false, corrupt = false;
+    const uint32_t n_tris = (p.n_nodes + 1) / 2;
+
+    uint32_t st_node[STACK];
+    float st_t[STACK];
+    int sp = 0;
+
+    const float4* nodes4 = reinterpret_cast<const float4*>(p.nodes);
+    auto test_leaf = [&](uint32_t pos, uint32_t tri) {
+        if (tri >= n_tris) { corrupt = true; return; }
+        ++tested;
+        const float4 a = __ldg(p.xtri + 3 * static_cast<size_t>(tri));
+        const float4 b = __ldg(p.xtri + 3 * static_cast<size_t>(tri) + 1);
+        const float4 c = __ldg(p.xtri + 3 * static_cast<size_t>(tri) + 2);
+        const float3 A = make_float3(a.x, a.y, a.z), B = make_float3(b.x, b.y, b.z), C = make_float3(c.x, c.y, c.z);
+        const HitRes h = WT ? tri_watertight(r.o, tmin, tmax, w, A, B, C) : tri_reference(r.o, r.d, tmin, tmax, A, B, C);
+        if (!h.did) return;
+        const uint32_t key = WT ? tri : ~pos;
+        if (!have || h.t < bt || (h.t == bt && key < bkey)) {
+            have = true; bt = h.t; bu = h.u; bv = h.v; bkey = key; btri = tri;
+        }
+    };
+
+    {  // root
+        const float4 mn = __ldg(nodes4 + 0), mx = __ldg(nodes4 + 1);
+        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(nodes4 + 2));
+        float te;
+        ++visited;
+        if (slab(r, mn, mx, grow, te) && te <= prune_bound(bt, p.abs_eps)) {
+            if (lr.y == 0u && lr.z == 0u) test_leaf(0u, lr.x);
+            else { st_node[0] = 0u; st_t[0] = te; sp = 1; }
+        }
+    }
+    while (sp > 0) {
+        if (ANY && have) break;
+        --sp;
+        const uint32_t pi = st_node[sp];
+        if (st_t[sp] > prune_bound(bt, p.abs_eps)) continue;
+        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(nodes4 + 3 * static_cast<size_t>(pi) + 2));
+        const uint32_t ch[2] = {lr.y, lr.z};
+        bool pass[2];
+        float te[2];
+        uint4 chl[2];
+        if (ch[0] >= p.n_nodes || ch[1] >= p.n_nodes) {
+            overflow = true;  // corrupt node array: reported, never dereferenced
+            corrupt = true;
+            continue;
+        }
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const float4* cn = nodes4 + 3 * static_cast<size_t>(ch[c]);
+            const float4 mn = __ldg(cn), mx = __ldg(cn + 1);
+            chl[c] = __ldg(reinterpret_cast<const uint4*>(cn + 2));
+            ++visited;
+            pass[c] = slab(r, mn, mx, grow, te[c]);
+        }
+        // near child last on the stack (visited first)
+        const int first = (te[1] < te[0]) ? 1 : 0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int c = (k == 0) ? 1 - first : first;
+            if (!pass[c] || te[c] > prune_bound(bt, p.abs_eps)) continue;
+            if (chl[c].y == 0u && chl[c].z == 0u) {
+                test_leaf(ch[c], chl[c].x);
+                if (ANY && have) break;
+            } else if (sp < STACK) {
+                st_node[sp] = ch[c];
+                st_t[sp] = te[c];
+                ++sp;
+            } else {
+                overflow = true;
+            }
+        }
+    }
+    if (have) out = make_uint4(btri, __float_as_uint(bt), __float_as_uint(bu), __float_as_uint(bv));
+    reinterpret_cast<uint4*>(p.hits)[i] = out;
+    if (corrupt) raise_error(p.err, kDevCorrupt);
+    else if (overflow) raise_error(p.err, kDevStackOverflow);
+    if (p.stats) {
+        atomicAdd(p.stats + 0, static_cast<unsigned long long>(visited));
+        atomicAdd(p.stats + 1, static_cast<unsigned long long>(tested));
+    }
+}
+
+// getRay (raytracer.glsl:92-100): pos = texel / size, direction =
+// normalize(InvView * vec4((pos - 0.5, 1) * (W, H, near), 1) - eye).
+__global__ void __launch_bounds__(256) raygen_kernel(const crt_camera* __restrict__ cam, uint32_t width, uint32_t height,
+                                                     crt_ray* __restrict__ rays) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y;
+    if (x >= width) return;
+    const float* m = cam->inv_view;
+    const float px = static_cast<float>(x) / static_cast<float>(width);
+    const float py = static_cast<float>(y) / static_cast<float>(height);
+    const float4 pv = make_float4((px - 0.5f) * cam->plane_width, (py - 0.5f) * cam->plane_height, 1.0f * cam->plane_near, 1.0f);
+    const float4 pw = mat_vec(m, pv);
+    const float dx = pw.x - cam->eye[0], dy = pw.y - cam->eye[1], dz = pw.z - cam->eye[2], dw = pw.w - cam->eye[3];
+    const float inv = 1.0f / sqrtf(((dx * dx + dy * dy) + dz * dz) + dw * dw);
+    float4* o = reinterpret_cast<float4*>(rays + static_cast<size_t>(y) * width + x);
+    o[0] = make_float4(cam->eye[0], cam->eye[1], cam->eye[2], 0.f);
+    o[1] = make_float4(dx * inv, dy * inv, dz * inv, __int_as_float(0x7F800000));
+}
+
+__global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__ prim, const crt_hit* __restrict__ hits,
+                                                     uint32_t n, float lx, float ly, float lz, crt_ray* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint4 h = __ldg(reinterpret_cast<const uint4*>(hits) + i);
+    float4* o = reinterpret_cast<float4*>(out + i);
+    if (h.x == CRT_MISS) {
+        o[0] = make_float4(0.f, 0.f, 0.f, 1.f);
+        o[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(prim + i));
+    const float4 r1 = __ldg(reinterpret_cast<const float4*>(prim + i) + 1);
+    const float t = __uint_as_float(h.y);
+    const float px = r0.x + t * r1.x, py = r0.y + t * r1.y, pz = r0.z + t * r1.z;
+    const float dx = lx - px, dy = ly - py, dz = lz - pz;
+    const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+    const float inv = 1.0f / len;
+    o[0] = make_float4(px, py, pz, 1e-4f);
+    o[1] = make_float4(dx * inv, dy * inv, dz * inv, len);
+}
+
+template <bool ANY, bool WT>
+static void launch_trace_t(const TraceParams& p, int block, bool deep, cudaStream_t s) {
+    const uint32_t grid = (p.n_rays + block - 1) / block;
+    if (grid == 0) return;
+    if (deep) trace_kernel<ANY, WT, 1024><<<grid, block, 0, s>>>(p);
+    else trace_kernel<ANY, WT, 64><<<grid, block, 0, s>>>(p);
+}
+
+void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s) {
+    const bool any = flags & CRT_TRACE_ANY, wt = flags & CRT_TRI_WATERTIGHT;
+    const bool deep = (flags >> 16) != 0;  // set by the host when the tree may be deeper than 63
+    if (any && wt) launch_trace_t<true, true>(p, block, deep, s);
+    else if (any) launch_trace_t<true, false>(p, block, deep, s);
+    else if (wt) launch_trace_t<false, true>(p, block, deep, s);
+    else launch_trace_t<false, false>(p, block, deep, s);
+}
+
+void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s) {
+    dim3 grid((width + 255) / 256, height);
+    raygen_kernel<<<grid, 256, 0, s>>>(cam_dev, width, height, rays);
+}
+
+void launch_shadow_rays(const crt_ray* prim, const crt_hit* hits, uint32_t n, float lx, float ly, float lz, crt_ray* out,
+                        cudaStream_t s) {
+    if (n == 0) return;
+    shadow_kernel<<<(n + 255) / 256, 256, 0, s>>>(prim, hits, n, lx, ly, lz, out);
+}
+
+}  // namespace crt

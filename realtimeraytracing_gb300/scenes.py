@@ -1,0 +1,239 @@
+"""Seeded synthetic scenes, cameras and record packing.
+
+The reference loads OBJ meshes (srcCommon/scene/geometry/mesh.cpp:186-263)
+and pads them into a 65,536-entry TriangleGPU buffer
+(srcOpenGL/scene/scene.cpp:26-40).  These generators make the synthetic
+scenes the benchmarks are defined on, with a counter-based SplitMix64 stream
+and only IEEE-exact float64 arithmetic (+, -, *, /, sqrt) on the paths that
+feed golden fixtures, so the same seed gives the same bytes on x86-64 and
+aarch64.
+
+Record layouts (see include/crt.h):
+  triangles  (n, 16) float32: p0.xyzw, p1.xyzw, p2.xyzw, model id (uint32 bits), pad
+  models     (m, 17) float32: column-major 4x4, material id (uint32 bits)
+  rays       (n, 8)  float32: o.xyz, tmin, d.xyz, tmax
+  hits       (n, 4)  float32: tri (uint32 bits), t, u, v
+  nodes      (2n-1, 12) float32: min.xyz, pad, max.xyz, pad, tri, left, right, pad (uint32 bits)
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, stream: int, n: int) -> np.ndarray:
+    """n values of SplitMix64 for (seed, stream), counter based."""
+    base = np.uint64((seed * 0x632BE59BD9B4E019 + stream * 0x2545F4914F6CDD1D + 1) & 0xFFFFFFFFFFFFFFFF)
+    with np.errstate(over="ignore"):
+        z = base + (np.arange(1, n + 1, dtype=np.uint64) * _GOLD)
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed: int, stream: int, n: int) -> np.ndarray:
+    """n float64 in [0, 1) with 53 random bits (exact)."""
+    return (splitmix64(seed, stream, n) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+
+
+def _unit_vectors(seed: int, stream: int, n: int) -> np.ndarray:
+    """Uniform directions on S^2 by Marsaglia's disk method (only sqrt)."""
+    out = np.empty((n, 3), np.float64)
+    todo = np.arange(n)
+    rnd = 0
+    while todo.size:
+        k = 8
+        u = uniform01(seed, stream * 64 + rnd, todo.size * 2 * k).reshape(todo.size, k, 2) * 2.0 - 1.0
+        s = u[..., 0] ** 2 + u[..., 1] ** 2
+        ok = (s < 1.0) & (s > 1e-12)
+        first = np.argmax(ok, axis=1)
+        got = ok[np.arange(todo.size), first]
+        sel = u[np.arange(todo.size), first]
+        ss = s[np.arange(todo.size), first]
+        r = np.sqrt(np.maximum(1.0 - ss, 0.0))
+        v = np.stack([2.0 * sel[:, 0] * r, 2.0 * sel[:, 1] * r, 1.0 - 2.0 * ss], axis=1)
+        out[todo[got]] = v[got]
+        todo = todo[~got]
+        rnd += 1
+    return out
+
+
+def _gaussian(seed: int, stream: int, n: int) -> np.ndarray:
+    """Standard normals (Box-Muller; uses log/cos, so not for golden fixtures)."""
+    u1 = uniform01(seed, stream, n)
+    u2 = uniform01(seed, stream + 7919, n)
+    return np.sqrt(-2.0 * np.log1p(-u1)) * np.cos(2.0 * math.pi * u2)
+
+
+def pack_triangles(v0: np.ndarray, v1: np.ndarray, v2: np.ndarray, model_id=0) -> np.ndarray:
+    n = v0.shape[0]
+    t = np.zeros((n, 16), np.float32)
+    t[:, 0:3] = v0
+    t[:, 4:7] = v1
+    t[:, 8:11] = v2
+    t[:, 3] = t[:, 7] = t[:, 11] = 1.0
+    t.view(np.uint32)[:, 12] = model_id
+    return t
+
+
+def identity_models(n: int = 1) -> np.ndarray:
+    m = np.zeros((n, 17), np.float32)
+    m[:, [0, 5, 10, 15]] = 1.0
+    return m
+
+
+def uniform_soup(n: int, seed: int = 0, edge_lo: float = 0.001, edge_hi: float = 0.02) -> np.ndarray:
+    """Random soup in the unit cube: centroid ~ U[0,1]^3, each vertex =
+    centroid + L * u with L ~ U(edge_lo, edge_hi) and u uniform on S^2."""
+    c = uniform01(seed, 1, 3 * n).reshape(n, 3)
+    verts = []
+    for k in range(3):
+        L = edge_lo + uniform01(seed, 10 + k, n) * (edge_hi - edge_lo)
+        u = _unit_vectors(seed, 20 + k, n)
+        verts.append((c + L[:, None] * u).astype(np.float32))
+    return pack_triangles(*verts)
+
+
+def clustered_soup(n: int, clusters: int, sigma: float, edge_mu: float, edge_sigma: float, seed: int = 0) -> np.ndarray:
+    """Gaussian blobs: cluster centres ~ U[0,1]^3, centroid = centre + sigma N(0,1)^3,
+    vertex offsets of length lognormal(ln edge_mu, edge_sigma) in uniform directions."""
+    centres = uniform01(seed, 101, 3 * clusters).reshape(clusters, 3)
+    which = (splitmix64(seed, 102, n) % np.uint64(clusters)).astype(np.int64)
+    g = _gaussian(seed, 103, 3 * n).reshape(n, 3)
+    c = centres[which] + sigma * g
+    verts = []
+    for k in range(3):
+        L = np.exp(math.log(edge_mu) + edge_sigma * _gaussian(seed, 110 + 2 * k, n))
+        u = _unit_vectors(seed, 120 + k, n)
+        verts.append((c + L[:, None] * u).astype(np.float32))
+    return pack_triangles(*verts)
+
+
+def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit icosphere by midpoint subdivision: (vertices float64, faces uint32)."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t],
+                  [0, -1, -t], [0, 1, -t], [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    v /= np.sqrt((v ** 2).sum(1))[:, None]
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4],
+                  [11, 10, 2], [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8],
+                  [3, 8, 9], [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], np.int64)
+    for _ in range(level):
+        a, b, c = f[:, 0], f[:, 1], f[:, 2]
+        edges = np.stack([np.stack([a, b], 1), np.stack([b, c], 1), np.stack([c, a], 1)], 1).reshape(-1, 2)
+        key = np.minimum(edges[:, 0], edges[:, 1]) * (1 << 32) + np.maximum(edges[:, 0], edges[:, 1])
+        uk, inv = np.unique(key, return_inverse=True)
+        lo, hi = uk >> 32, uk & 0xFFFFFFFF
+        mid = v[lo] + v[hi]
+        mid /= np.sqrt((mid ** 2).sum(1))[:, None]
+        base = v.shape[0]
+        v = np.concatenate([v, mid])
+        m = (inv.reshape(-1, 3) + base)
+        ab, bc, ca = m[:, 0], m[:, 1], m[:, 2]
+        f = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1),
+                            np.stack([c, ca, bc], 1), np.stack([ab, bc, ca], 1)])
+    return v, f.astype(np.uint32)
+
+
+def _value_noise(p: np.ndarray, seed: int, octave: int) -> np.ndarray:
+    """Value noise in [-1, 1]: hashed lattice values, smoothstep trilinear blend."""
+    i0 = np.floor(p)
+    fr = p - i0
+    w = fr * fr * (3.0 - 2.0 * fr)
+    ii = i0.astype(np.int64)
+    out = np.zeros(p.shape[0])
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                h = ((ii[:, 0] + dx) * 73856093) ^ ((ii[:, 1] + dy) * 19349663) ^ ((ii[:, 2] + dz) * 83492791)
+                h = (h.astype(np.uint64) + np.uint64((seed * 1000003 + octave * 7777) & 0xFFFFFFFF))
+                with np.errstate(over="ignore"):
+                    z = (h * _GOLD) ^ ((h * _GOLD) >> np.uint64(29))
+                    z = z * _M1
+                    z = z ^ (z >> np.uint64(32))
+                val = (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53) * 2.0 - 1.0
+                wx = w[:, 0] if dx else 1.0 - w[:, 0]
+                wy = w[:, 1] if dy else 1.0 - w[:, 1]
+                wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                out += wx * wy * wz * val
+    return out
+
+
+def displaced_icosphere(level: int = 8, amplitude: float = 0.05, seed: int = 0):
+    """Icosphere of radius 1 whose vertices move radially by `amplitude` times
+    a 3-octave value noise (octave frequencies 2, 4, 8; weights 1, 1/2, 1/4,
+    normalised).  Returns (vertices float32 (V,3), indices uint32 (F,3))."""
+    v, f = icosphere(level)
+    n = np.zeros(v.shape[0])
+    for o, (fq, wgt) in enumerate(((2.0, 1.0), (4.0, 0.5), (8.0, 0.25))):
+        n += wgt * _value_noise(v * fq + 17.0, seed, o)
+    n /= 1.75
+    v = v * (1.0 + amplitude * n)[:, None]
+    return v.astype(np.float32), f
+
+
+def indexed_to_triangles(verts: np.ndarray, faces: np.ndarray) -> np.ndarray:
+    return pack_triangles(verts[faces[:, 0]], verts[faces[:, 1]], verts[faces[:, 2]])
+
+
+def camera_gpu_data(eye, yaw: float = -90.0, pitch: float = 0.0, fov: float = 45.0, near: float = 0.1,
+                    aspect: float = 1.0, world_up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    """crt_camera record (24 float32) following Camera::getGpuData
+    (srcCommon/scene/camera.cpp:23-34, 44-66, 110-120): inverse of
+    lookAt(eye, eye + at, up), eye (w = 1), plane width/height/near.
+    Evaluated in float64; components below 1e-12 are snapped to 0 so the
+    default yaw of -90 looks exactly along the z axis."""
+    def snap(x):
+        x = np.asarray(x, np.float64)
+        return np.where(np.abs(x) < 1e-12, 0.0, x)
+    yr, pr = math.radians(yaw), math.radians(pitch)
+    front = snap([math.cos(yr) * math.cos(pr), math.sin(pr), math.sin(yr) * math.cos(pr)])
+    at = front / np.linalg.norm(front)
+    up_w = np.asarray(world_up, np.float64)
+    right = np.cross(at, up_w); right /= np.linalg.norm(right)
+    up = np.cross(right, at); up /= np.linalg.norm(up)
+    # lookAt: f = at, s = normalize(cross(f, up)), u = cross(s, f); view rows s, u, -f
+    f = at
+    s = np.cross(f, up); s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    e = np.asarray(eye, np.float64)
+    inv = np.zeros((4, 4))  # inverse view: columns s, u, -f, eye
+    inv[:3, 0], inv[:3, 1], inv[:3, 2], inv[:3, 3], inv[3, 3] = s, u, -f, e, 1.0
+    inv = snap(inv)
+    rec = np.zeros(24, np.float32)
+    rec[0:16] = inv.T.reshape(-1)  # column-major
+    rec[16:19] = e
+    rec[19] = 1.0
+    ph = 2.0 * near * math.tan(0.5 * math.radians(fov))
+    rec[20] = np.float32(ph * aspect)
+    rec[21] = np.float32(ph)
+    rec[22] = np.float32(near)
+    return rec
+
+
+# ---------------------------------------------------------------- workloads
+def config0_scene(seed: int = 0):
+    """65,536-triangle uniform soup, 512x512 camera at (0.5, 0.5, -1.5) toward +z."""
+    tris = uniform_soup(65536, seed)
+    cam = camera_gpu_data((0.5, 0.5, -1.5), aspect=1.0)
+    return tris, identity_models(1), cam, (512, 512)
+
+
+def config1_scene(seed: int = 0, level: int = 8):
+    """Displaced icosphere (level 8: 1,310,720 triangles), 1920x1080 camera 3
+    units out on -z looking toward +z, point light at (2, 2, -2)."""
+    v, f = displaced_icosphere(level, 0.05, seed)
+    tris = indexed_to_triangles(v, f)
+    cam = camera_gpu_data((0.0, 0.0, -3.0), aspect=1920.0 / 1080.0)
+    return tris, identity_models(1), cam, (1920, 1080), np.array([2.0, 2.0, -2.0], np.float32)
+
+
+def config3_scene(seed: int = 0, n: int = 4194304):
+    """4M-triangle clustered soup: 256 clusters, sigma 0.02, edges lognormal(ln 0.003, 0.6)."""
+    return clustered_soup(n, 256, 0.02, 0.003, 0.6, seed), identity_models(1)
