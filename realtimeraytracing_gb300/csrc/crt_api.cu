@@ -112,13 +112,16 @@ struct crt_ctx {
         return CRT_OK;
     }
     crt_status check_device_error() {
-        uint32_t e = 0;
-        CRT_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, stream));
+        uint32_t ew[4] = {0, 0, 0, 0};
+        CRT_CUDA(cudaMemcpyAsync(ew, err.p, 16, cudaMemcpyDeviceToHost, stream));
         CRT_CUDA(cudaStreamSynchronize(stream));
+        const uint32_t e = ew[0];
         if (e & crt::kDevTimeout) return fail(CRT_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up (err=0x%x)", e);
         if (e & crt::kDevBadModel) return fail(CRT_ERR_BAD_INPUT, "a triangle references model id >= 64");
         if (e & crt::kDevStackOverflow) return fail(CRT_ERR_STACK_OVERFLOW, "a ray overflowed its traversal stack");
-        if (e & crt::kDevCorrupt) return fail(CRT_ERR_CUDA, "a device index check failed (err=0x%x)", e);
+        if (e & crt::kDevCorrupt)
+            return fail(CRT_ERR_CUDA, "a device index check failed (err=0x%x site=%u iter=%u values=%u,%u)", e,
+                        ew[1] & 0xFFu, ew[1] >> 8, ew[2], ew[3]);
         if (e) return fail(CRT_ERR_CUDA, "device error word 0x%x", e);
         return CRT_OK;
     }

@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
     if (i == 0) it[0] = make_uint2(n, n);
     if (i >= n) return;
     const uint32_t ti = perm[i];
-    if (ti >= n) { raise_error(err, kDevCorrupt); return; }
+    if (ti >= n) { raise_corrupt(err, 1, i, ti); return; }
     const TriRec t = load_tri(tris, ti);
     const float* M = models + 16 * (t.model & (kMaxModels - 1));
     const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
@@ -397,7 +397,12 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 
     const uint2 cur = it[iter];
     const uint32_t n = cur.x;
-    if (n <= 1u) return;
+    if (n <= 1u) {
+        // Finished: carry the state forward so a later launch of this build
+        // never reads an entry left over from an earlier build.
+        if (blockIdx.x == 0 && threadIdx.x == 0) it[iter + 1] = cur;
+        return;
+    }
     unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
     unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
     if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
@@ -497,7 +502,7 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
             const int j = static_cast<int>(s_nn[p - nlo]);
             const float4 bmn = s_mn[j - lo], bmx = s_mx[j - lo];
             const uint32_t id = out_m++;
-            if (id >= 2 * N - 1 || id < N) { raise_error(err, kDevCorrupt); continue; }
+            if (id >= 2 * N - 1 || id < N) { raise_corrupt(err, 2 + (iter << 8), p, id); continue; }
             float4 m0, m1;  // AABB::merge (bvh.cpp:401-413), first argument = lower position
             m0.x = min_std(mn.x, bmn.x); m0.y = min_std(mn.y, bmn.y); m0.z = min_std(mn.z, bmn.z);
             m1.x = max_std(mx.x, bmx.x); m1.y = max_std(mx.y, bmx.y); m1.z = max_std(mx.z, bmx.z);
@@ -510,7 +515,7 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
             mn = make_float4(m0.x, m0.y, m0.z, __uint_as_float(id));
             mx = make_float4(m1.x, m1.y, m1.z, __uint_as_float(lc));
         }
-        if (out_v >= n) { raise_error(err, kDevCorrupt); continue; }
+        if (out_v >= n) { raise_corrupt(err, 3 + (iter << 8), p, out_v); continue; }
         cout[2 * static_cast<size_t>(out_v)] = mn;
         cout[2 * static_cast<size_t>(out_v) + 1] = mx;
         ++out_v;
@@ -535,7 +540,7 @@ __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restr
     const uint32_t lca = (a < N) ? 1u : node_lc[a - N];
     const uint32_t pl = p + 1, pr = p + 2 * lca;
     if (pr >= 2 * N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
-        raise_error(err, kDevCorrupt);
+        raise_corrupt(err, 4, X, pr);
         return;
     }
     float4* o = reinterpret_cast<float4*>(out + p);

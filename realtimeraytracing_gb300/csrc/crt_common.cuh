@@ -98,4 +98,13 @@ enum DevError : uint32_t {
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) { atomicOr(err, code); }
 
+// Records the first failed index check: err[1] = site, err[2..3] = values.
+__device__ __forceinline__ void raise_corrupt(uint32_t* err, uint32_t site, uint32_t v0, uint32_t v1) {
+    atomicOr(err, static_cast<uint32_t>(kDevCorrupt));
+    if (atomicCAS(err + 1, 0u, site) == 0u) {
+        err[2] = v0;
+        err[3] = v1;
+    }
+}
+
 }  // namespace crt

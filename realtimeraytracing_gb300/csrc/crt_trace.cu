@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
     }
     if (have) out = make_uint4(btri, __float_as_uint(bt), __float_as_uint(bu), __float_as_uint(bv));
     reinterpret_cast<uint4*>(p.hits)[i] = out;
-    if (corrupt) raise_error(p.err, kDevCorrupt);
+    if (corrupt) raise_corrupt(p.err, 5, i, 0u);
     else if (overflow) raise_error(p.err, kDevStackOverflow);
     if (p.stats) {
         atomicAdd(p.stats + 0, static_cast<unsigned long long>(visited));
