@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 ray-tracing core.
+
+Workload (one "step" = one frame of the reference's compute pass,
+Application::drawOneFrame in srcOpenGL/application.cpp:220-262, minus shading):
+  scene   1,310,720-triangle displaced icosphere (subdivision 8, radius 1,
+          3-octave value noise of amplitude 0.05), seeded synthetic data;
+          the BVH is built by the CUDA PLOC path (build time reported apart
+          as build_ms, as the reference builds once at scene load)
+  frame   1920x1080 primary rays (getRay) -> closest hit (watertight
+          predicate) -> one any-hit shadow ray per hit toward (2, 2, -2)
+  value   rays traced per second (primary + shadow rays of hits), Mrays/s,
+          inputs resident in HBM, CUDA events on the library's stream
+  e2e     the same frame through the public C ABI call crt_trace_frame with
+          the camera in from pinned host memory and both hit buffers out to
+          pinned host memory, timed on the host clock around the call
+
+--impl reference times the reference's CPU path on the host cores instead:
+its PLOC build (bvh.cpp restated for N > 65,536, the reference's own cap)
+and its shader traversal restated in C++ (right-child-first DFS without
+t pruning, the shader's triangle predicate), on a bounded sample of rays.
+
+Multi-GPU: replicas (each rank traces its own full frame); value is the
+total over ranks divided by the slowest rank's time (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s closest-hit: hit-predictor vs plain, 1 GB300, exact hits; BVH build ms"
+WORKLOAD = "displaced icosphere 1,310,720 tris; 1920x1080 primary closest-hit + shadow any-hit to (2,2,-2)"
+W, H = 1920, 1080
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_profile_traffic():
+    """Per-launch DRAM bytes of the primary trace kernel from the committed
+    ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "trace_kernel_config1.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        out_dir = os.path.join(ROOT, "gpurun_out")
+        os.makedirs(out_dir, exist_ok=True)
+        self.path = os.path.join(out_dir, f"clocks_bench_{os.getpid()}.csv")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_scene():
+    from realtimeraytracing_gb300 import scenes as S
+    tris, models, cam, (w, h), light = S.config1_scene(seed=0)
+    assert (w, h) == (W, H)
+    return tris, models, cam, light
+
+
+# --------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from realtimeraytracing_gb300 import crt
+
+    tris, models, cam, light = make_scene()
+    n_tris = tris.shape[0]
+    ctx = crt.Context(device=local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    d_tris = torch.from_numpy(tris).to(dev)
+    d_models = torch.from_numpy(models).to(dev)
+    d_cam = torch.from_numpy(cam).to(dev)
+    torch.cuda.synchronize()
+
+    # ---- BVH build (scene load), device-timed inside the library
+    bvh = ctx.build(d_tris, models=d_models)
+    build_ms = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        bvh.rebuild(d_tris, models=d_models)
+        wall = (time.perf_counter() - t0) * 1e3
+        st = ctx.last_build_stats()
+        if i >= args.warmup:
+            build_ms.append((st["ms_total"], wall, st))
+    build_dev = statistics.median(b[0] for b in build_ms)
+    build_wall = statistics.median(b[1] for b in build_ms)
+    stages = {k: round(statistics.median(b[2][k] for b in build_ms), 4)
+              for k in ("ms_morton", "ms_sort", "ms_ploc", "ms_layout")}
+    iters = build_ms[-1][2]["ploc_iterations"]
+
+    n_rays = W * H
+    hp = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+    hs = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+    flags = crt.TRI_WATERTIGHT
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def frame():
+        ctx.trace_frame(bvh, d_cam, W, H, light, flags, hits_primary=hp, hits_shadow=hs)
+
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
+    rays_per_frame = n_rays + n_hits
+
+    # ---- timed frames (device resident), L2 flushed before each frame
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            l2_flush.zero_()
+            ev[k][0].record(stream)
+            frame()
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    frame_ms = [a.elapsed_time(b) for a, b in ev]
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    t_frame = sum(frame_ms) / len(frame_ms)
+    if world > 1:
+        tt = torch.tensor([t_frame], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_frame = float(tt.item())
+    value = world * rays_per_frame / (t_frame * 1e-3) / 1e6
+
+    # ---- the dominant kernel alone: primary closest-hit trace
+    rays = torch.empty((n_rays, 8), dtype=torch.float32, device=dev)
+    ctx.raygen(d_cam, W, H, out=rays)
+    ctx.trace(bvh, rays, flags | crt.TRACE_STATS, out=hp)
+    visited, tested = ctx.last_trace_stats()
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            l2_flush.zero_()
+            kev[k][0].record(stream)
+            ctx.trace(bvh, rays, flags, out=hp)
+            kev[k][1].record(stream)
+    torch.cuda.synchronize()
+    k_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+    alg_bytes = 48.0 * visited + 48.0 * tested + (32.0 + 16.0) * n_rays
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
+    traffic = read_profile_traffic()
+
+    # ---- end to end through the public API: camera in, hits out (pinned host)
+    hp_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
+    hs_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
+    cam_h = torch.from_numpy(cam.copy()).pin_memory()
+    for _ in range(2):
+        ctx.trace_frame(bvh, cam_h, W, H, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
+    e2e_ms = []
+    for _ in range(args.steps):
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.trace_frame(bvh, cam_h, W, H, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_t = statistics.mean(e2e_ms)
+    if world > 1:
+        tt = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    e2e_value = world * rays_per_frame / (e2e_t * 1e-3) / 1e6
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(tris, models, cam)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": round(value, 2),
+            "unit": "Mrays/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(t_frame, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded displaced icosphere)",
+            "config": {"workload": WORKLOAD, "triangles": n_tris, "image": [W, H],
+                       "rays_per_step": rays_per_frame, "primary_hits": n_hits,
+                       "predicate": "watertight", "ploc_radius": 16, "sort_digit_bits": 8,
+                       "l2": "flushed (256 MB write) before every timed step",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "build_ms": round(build_dev, 4),
+            "build_ms_wall": round(build_wall, 4),
+            "build_stages_ms": stages,
+            "ploc_iterations": iters,
+            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(cam.nbytes),
+                    "d2h_bytes_per_step": int(2 * n_rays * 16), "ms_per_step": round(e2e_t, 4)},
+            "gpu_launches": 4 * args.steps,
+            "roofline": {"kernel": "trace_kernel (primary closest-hit)", "bound": "hbm",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": peak_kind, "ms_per_launch": round(k_ms, 4),
+                         "alg_bytes_per_launch": int(alg_bytes),
+                         "nodes_per_ray": round(visited / n_rays, 2), "tris_per_ray": round(tested / n_rays, 2)},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(tris, models, cam, sample_stride=8):
+    """The reference's CPU path on the host cores: the shader traversal
+    restated in C++ (oracle), every `sample_stride`-th ray of the frame."""
+    from oracle import oracle as O
+    n = tris.shape[0]
+    nb = O.build_bvh(tris, n, models, faithful=True)
+    rays = O.raygen(cam, W, H)[::sample_stride].copy()
+    O.trace(nb["nodes"], tris, models, rays[:4096], 0)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        hits, _ = O.trace(nb["nodes"], tris, models, rays, 0)
+        reps += 1
+        if time.perf_counter() - t0 > 2.0:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    cores = os.cpu_count()
+    return {"value": round(rays.shape[0] / dt / 1e6, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+            "sample": f"every {sample_stride}th primary ray of the 1920x1080 frame ({rays.shape[0]} rays), "
+                      f"shader predicate, no t pruning; shadow rays: none (the shader predicate hits nothing "
+                      f"on this mesh)",
+            "build_ms": round(float(sum(nb["ms"])), 2)}
+
+
+# --------------------------------------------------------- reference arm
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    tris, models, cam, light = make_scene()
+    n = tris.shape[0]
+    t0 = time.perf_counter()
+    nb = O.build_bvh(tris, n, models, faithful=True)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    rays_all = O.raygen(cam, W, H)
+    stride = 8
+    times, counted = [], []
+    for k in range(args.warmup + args.steps):
+        sub = rays_all[(k % stride)::stride].copy()
+        t0 = time.perf_counter()
+        hits, _ = O.trace(nb["nodes"], tris, models, sub, 0)
+        nh = int((hits[:, 0].view(np.uint32) != 0xFFFFFFFF).sum())
+        if nh:
+            sh = O.shadow_rays(sub, hits, light)
+            O.trace(nb["nodes"], tris, models, sh, 1)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            counted.append(sub.shape[0] + nh)
+    value = sum(counted) / sum(times) / 1e6
+    cores = os.cpu_count()
+    line = {
+        "metric": METRIC, "impl": "reference", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded displaced icosphere)",
+        "config": {"workload": WORKLOAD, "triangles": n, "image": [W, H], "sample": f"1/{stride} of the frame per step"},
+        "build_ms": round(build_ms, 2),
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": f"every {stride}th primary ray per step (rotating offset), shader predicate, "
+                                   f"right-child-first DFS without t pruning; shadow rays for its hits"},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

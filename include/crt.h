@@ -118,6 +118,7 @@ typedef struct crt_camera {
 #define CRT_TRI_REFERENCE     0x0u  /* raytracer.glsl:102-147 predicate, bit for bit */
 #define CRT_TRI_WATERTIGHT    0x2u  /* Woop/Benthin/Wald 2013 watertight predicate, two-sided */
 #define CRT_TRACE_USE_PREDICTOR 0x4u /* seed t_max from the learned hit predictor */
+#define CRT_TRACE_STATS       0x8u  /* count visited nodes / tested triangles (slower) */
 
 typedef struct crt_config {
     int device;                 /* CUDA device ordinal, default 0 */
@@ -191,6 +192,20 @@ crt_status crt_shadow_rays(crt_ctx* ctx, const crt_ray* primary, const crt_hit* 
 /* ---- trace: replaces getClosestHitBVH (raytracer.glsl:246-295) ---------- */
 crt_status crt_trace(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, uint32_t n_rays,
                      uint32_t flags, crt_hit* hits);
+/* Counters of the last crt_trace issued with CRT_TRACE_STATS:
+ * out[0] = node boxes tested, out[1] = triangles tested. */
+crt_status crt_last_trace_stats(crt_ctx* ctx, uint64_t out[2]);
+
+/* One frame of the reference's compute pass (Application::drawOneFrame,
+ * srcOpenGL/application.cpp:220-262, minus shading): getRay for every texel
+ * of a width x height image, closest hit with `flags`, then — when light is
+ * not NULL — one any-hit shadow ray per primary hit toward the point light.
+ * Rays live in context memory; only the camera goes in and the hits come out
+ * (hits_primary[width*height], hits_shadow[width*height] or NULL; host or
+ * device memory).  Shadow misses on primary misses are reported as CRT_MISS. */
+crt_status crt_trace_frame(crt_ctx* ctx, const crt_bvh* bvh, const crt_camera* cam, uint32_t width,
+                           uint32_t height, const float* light, uint32_t flags, crt_hit* hits_primary,
+                           crt_hit* hits_shadow);
 
 #ifdef __cplusplus
 }

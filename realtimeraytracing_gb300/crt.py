@@ -25,6 +25,7 @@ TRACE_ANY = 0x1
 TRI_REFERENCE = 0x0
 TRI_WATERTIGHT = 0x2
 TRACE_USE_PREDICTOR = 0x4
+TRACE_STATS = 0x8
 MISS = 0xFFFFFFFF
 
 # Every symbol include/crt.h declares.
@@ -32,7 +33,7 @@ EXPORTS = [
     "crt_abi_version", "crt_default_config", "crt_create", "crt_destroy", "crt_sync", "crt_last_error_string",
     "crt_stream", "crt_build", "crt_rebuild", "crt_bvh_free", "crt_bvh_node_count", "crt_bvh_triangle_count",
     "crt_bvh_nodes_device", "crt_bvh_copy_nodes", "crt_bvh_copy_codes", "crt_bvh_copy_perm", "crt_last_build_stats",
-    "crt_raygen_pinhole", "crt_shadow_rays", "crt_trace",
+    "crt_raygen_pinhole", "crt_shadow_rays", "crt_trace", "crt_last_trace_stats", "crt_trace_frame",
 ]
 
 
@@ -88,6 +89,8 @@ def lib():
             "crt_raygen_pinhole": ([vp, vp, u32, u32, vp], i32),
             "crt_shadow_rays": ([vp, vp, vp, u32, vp, vp], i32),
             "crt_trace": ([vp, vp, vp, u32, u32, vp], i32),
+            "crt_last_trace_stats": ([vp, vp], i32),
+            "crt_trace_frame": ([vp, vp, vp, u32, u32, vp, u32, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -244,3 +247,26 @@ class Context:
         out = np.empty((n, 4), np.float32) if out is None else out
         _check(lib().crt_trace(self.handle, bvh.handle, _ptr(rays), n, flags, _ptr(out)))
         return out
+
+    def last_trace_stats(self):
+        """(node boxes tested, triangles tested) of the last trace issued with TRACE_STATS."""
+        out = np.zeros(2, np.uint64)
+        _check(lib().crt_last_trace_stats(self.handle, _ptr(out)))
+        return int(out[0]), int(out[1])
+
+    def trace_frame(self, bvh: Bvh, cam, width: int, height: int, light=None, flags: int = 0,
+                    hits_primary=None, hits_shadow=None):
+        """Application::drawOneFrame's compute pass: primary closest hits and,
+        with a light, shadow any-hits.  Returns (hits_primary, hits_shadow)."""
+        n = width * height
+        cam = np.ascontiguousarray(cam, np.float32) if isinstance(cam, np.ndarray) else cam
+        hp = np.empty((n, 4), np.float32) if hits_primary is None else hits_primary
+        hs = None
+        lp = None
+        if light is not None:
+            hs = np.empty((n, 4), np.float32) if hits_shadow is None else hits_shadow
+            light = np.ascontiguousarray(light, np.float32)
+            lp = _ptr(light)
+        _check(lib().crt_trace_frame(self.handle, bvh.handle, _ptr(cam), width, height, lp, flags, _ptr(hp),
+                                     _ptr(hs)))
+        return hp, hs

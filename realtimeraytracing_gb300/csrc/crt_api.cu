@@ -94,7 +94,8 @@ struct crt_ctx {
     // build scratch
     DevBuf tris_in, models, scene_state, err, hist, sort_lb, codes_a, codes_b, vals_a, vals_b;
     DevBuf node_box, node_lc, pos, clus_a, clus_b, iters, ploc_lb;
-    DevBuf cam, rays_in, hits_out, rays_out;
+    DevBuf cam, rays_in, hits_out, rays_out, trace_stats, frame_rays, frame_hits, frame_shadow, frame_shits;
+    uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
     size_t pinned_cap = 0;
@@ -178,6 +179,7 @@ crt_status crt_create(crt_ctx** out, const crt_config* cfg) {
     if (s == CRT_OK) s = x->err.reserve(16);
     if (s == CRT_OK) s = x->models.reserve(2 * 64 * 16 * sizeof(float));
     if (s == CRT_OK) s = x->cam.reserve(sizeof(crt_camera));
+    if (s == CRT_OK) s = x->trace_stats.reserve(16);
     if (s == CRT_OK) s = x->pinned_reserve(1 << 16);
     if (s == CRT_OK) {
         crt::SceneState init{};
@@ -199,7 +201,8 @@ crt_status crt_destroy(crt_ctx* x) {
     if (x->stream) cudaStreamSynchronize(x->stream);
     DevBuf* bufs[] = {&x->tris_in, &x->models, &x->scene_state, &x->err, &x->hist, &x->sort_lb, &x->codes_a,
                       &x->codes_b, &x->vals_a, &x->vals_b, &x->node_box, &x->node_lc, &x->pos, &x->clus_a,
-                      &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out};
+                      &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
+                      &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -423,6 +426,38 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
     return CRT_OK;
 }
 
+crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS))
+        return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
+    if (flags & CRT_TRACE_USE_PREDICTOR) return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor attached");
+    if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_trace: empty bvh");
+    return CRT_OK;
+}
+
+// Enqueues one traversal launch on device-resident rays/hits (no sync).
+crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
+                        crt_hit* d_hits) {
+    if (n_rays == 0) return CRT_OK;
+    crt::TraceParams p{};
+    p.nodes = b->nodes.as<crt_bvh_node>();
+    p.xtri = b->xtri.as<float4>();
+    p.rays = d_rays;
+    p.hits = d_hits;
+    p.n_rays = n_rays;
+    p.n_nodes = 2 * b->n - 1;
+    p.abs_eps = b->abs_eps;
+    p.err = x->err.as<uint32_t>();
+    p.stats = nullptr;
+    if (flags & CRT_TRACE_STATS) {
+        CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
+        p.stats = x->trace_stats.as<unsigned long long>();
+    }
+    const uint32_t launch_flags = (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) | ((b->iterations + 2 > 64) ? (1u << 16) : 0u);
+    crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -535,10 +570,7 @@ crt_status crt_shadow_rays(crt_ctx* x, const crt_ray* primary, const crt_hit* hi
 
 crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t n_rays, uint32_t flags, crt_hit* hits) {
     if (!x || !b || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_trace: null argument");
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR))
-        return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
-    if (flags & CRT_TRACE_USE_PREDICTOR) return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor attached");
-    if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_trace: empty bvh");
+    CRT_TRY(check_trace_flags(b, flags));
     CRT_CUDA(cudaSetDevice(x->device));
     if (n_rays == 0) return CRT_OK;
     const crt_ray* d_rays = rays;
@@ -554,20 +586,60 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
         d_hits = x->hits_out.as<crt_hit>();
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
-    crt::TraceParams p{};
-    p.nodes = b->nodes.as<crt_bvh_node>();
-    p.xtri = b->xtri.as<float4>();
-    p.rays = d_rays;
-    p.hits = d_hits;
-    p.n_rays = n_rays;
-    p.n_nodes = 2 * b->n - 1;
-    p.abs_eps = b->abs_eps;
-    p.err = x->err.as<uint32_t>();
-    p.stats = nullptr;
-    const uint32_t launch_flags = (flags & 0xFFFFu) | ((b->iterations + 2 > 64) ? (1u << 16) : 0u);
-    crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
-    CRT_CUDA(cudaGetLastError());
+    CRT_TRY(trace_device(x, b, d_rays, n_rays, flags, d_hits));
     if (!dev_out) CRT_CUDA(cudaMemcpyAsync(hits, d_hits, sizeof(crt_hit) * n_rays, cudaMemcpyDeviceToHost, x->stream));
+    CRT_TRY(x->check_device_error());
+    if (flags & CRT_TRACE_STATS)
+        CRT_CUDA(cudaMemcpy(x->last_trace_stats, x->trace_stats.p, 16, cudaMemcpyDeviceToHost));
+    return CRT_OK;
+}
+
+crt_status crt_last_trace_stats(crt_ctx* x, uint64_t out[2]) {
+    if (!x || !out) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    out[0] = x->last_trace_stats[0];
+    out[1] = x->last_trace_stats[1];
+    return CRT_OK;
+}
+
+crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, uint32_t width, uint32_t height,
+                           const float* light, uint32_t flags, crt_hit* hits_primary, crt_hit* hits_shadow) {
+    if (!x || !b || !cam || !hits_primary) return fail(CRT_ERR_INVALID_ARG, "crt_trace_frame: null argument");
+    if (width == 0 || height == 0 || height > 65535) return fail(CRT_ERR_INVALID_ARG, "bad image size");
+    if (light && !hits_shadow) return fail(CRT_ERR_INVALID_ARG, "crt_trace_frame: light without shadow output");
+    CRT_TRY(check_trace_flags(b, flags));
+    if (flags & CRT_TRACE_ANY) return fail(CRT_ERR_INVALID_ARG, "crt_trace_frame: primary rays are closest-hit");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const uint32_t n = width * height;
+    CRT_TRY(x->frame_rays.reserve(sizeof(crt_ray) * static_cast<size_t>(n)));
+    const bool dev_p = is_device_ptr(hits_primary);
+    crt_hit* d_hp = hits_primary;
+    if (!dev_p) {
+        CRT_TRY(x->frame_hits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
+        d_hp = x->frame_hits.as<crt_hit>();
+    }
+    const crt_camera* d_cam = cam;
+    if (!is_device_ptr(cam)) {
+        CRT_CUDA(cudaMemcpyAsync(x->cam.p, cam, sizeof(crt_camera), cudaMemcpyHostToDevice, x->stream));
+        d_cam = x->cam.as<crt_camera>();
+    }
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    crt_ray* rays = x->frame_rays.as<crt_ray>();
+    crt::launch_raygen(d_cam, width, height, rays, x->stream);
+    CRT_TRY(trace_device(x, b, rays, n, flags, d_hp));
+    if (!dev_p) CRT_CUDA(cudaMemcpyAsync(hits_primary, d_hp, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
+    if (light) {
+        CRT_TRY(x->frame_shadow.reserve(sizeof(crt_ray) * static_cast<size_t>(n)));
+        const bool dev_s = is_device_ptr(hits_shadow);
+        crt_hit* d_hs = hits_shadow;
+        if (!dev_s) {
+            CRT_TRY(x->frame_shits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
+            d_hs = x->frame_shits.as<crt_hit>();
+        }
+        crt_ray* sh = x->frame_shadow.as<crt_ray>();
+        crt::launch_shadow_rays(rays, d_hp, n, light[0], light[1], light[2], sh, x->stream);
+        CRT_TRY(trace_device(x, b, sh, n, (flags & ~CRT_TRACE_STATS) | CRT_TRACE_ANY, d_hs));
+        if (!dev_s) CRT_CUDA(cudaMemcpyAsync(hits_shadow, d_hs, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
+    }
     return x->check_device_error();
 }
 

@@ -110,3 +110,32 @@ def test_device_resident_rays(ctx, config0):
     ctx.trace(bvh, rays, crt.TRI_REFERENCE, out=hits)
     ref, _ = O.trace(bvh.nodes(), tris, models, rays.cpu().numpy(), crt.TRI_REFERENCE)
     _cmp_hits(hits.cpu().numpy(), ref)
+
+
+def test_trace_frame_matches_separate_calls(ctx):
+    """crt_trace_frame = raygen + closest hit + shadow rays + any hit."""
+    v, f = S.displaced_icosphere(level=5, seed=8)
+    tris = S.indexed_to_triangles(v, f)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    cam = S.camera_gpu_data((0.0, 0.0, -3.0), aspect=16 / 9)
+    light = np.array([2.0, 2.0, -2.0], np.float32)
+    hp, hs = ctx.trace_frame(bvh, cam, 160, 90, light, crt.TRI_WATERTIGHT)
+    rays = O.raygen(cam, 160, 90)
+    ref_p, _ = O.trace(bvh.nodes(), tris, models, rays, crt.TRI_WATERTIGHT)
+    _cmp_hits(hp, ref_p)
+    sh = O.shadow_rays(rays, ref_p, light)
+    ref_s, _ = O.trace(bvh.nodes(), tris, models, sh, crt.TRACE_ANY | crt.TRI_WATERTIGHT)
+    _cmp_hits(hs, ref_s, any_hit=True)
+    hp2, hs2 = ctx.trace_frame(bvh, cam, 160, 90, None, crt.TRI_REFERENCE)
+    assert hs2 is None
+    _cmp_hits(hp2, O.trace(bvh.nodes(), tris, models, rays, crt.TRI_REFERENCE)[0])
+
+
+def test_trace_stats_counts(ctx, config0):
+    tris, models, cam, w, h, bvh = config0
+    rays = O.raygen(cam, 64, 64)
+    got = ctx.trace(bvh, rays, crt.TRI_REFERENCE | crt.TRACE_STATS)
+    visited, tested = ctx.last_trace_stats()
+    assert visited > rays.shape[0] and tested > 0
+    _cmp_hits(got, O.trace(bvh.nodes(), tris, models, rays, crt.TRI_REFERENCE)[0])
