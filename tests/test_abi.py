@@ -1,0 +1,100 @@
+"""The C ABI library on the CPU: it loads, exports every symbol include/crt.h
+declares, refuses to run without an sm_103a GPU (no host fallback), and the
+drop-in adapter compiles and links against the reference's own bvh.hpp."""
+import ctypes as C
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "crt.h")
+
+
+def _declared():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(crt_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from realtimeraytracing_gb300 import build, crt
+    build.build()
+    return crt.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from realtimeraytracing_gb300 import crt
+    decl = _declared()
+    assert len(decl) >= 20
+    for name in decl:
+        assert hasattr(lib, name), name
+    assert sorted(crt.EXPORTS) == decl
+
+
+def test_abi_version(lib):
+    assert lib.crt_abi_version() == 1
+
+
+def test_no_gpu_means_an_error_not_a_fallback(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from realtimeraytracing_gb300 import crt
+    with pytest.raises(crt.CrtError) as e:
+        crt.Context()
+    assert e.value.status == 6  # CRT_ERR_UNSUPPORTED
+
+
+def test_invalid_config_rejected(lib):
+    from realtimeraytracing_gb300 import crt
+    with pytest.raises(crt.CrtError) as e:
+        crt.Context(ploc_radius=0)
+    assert e.value.status == 1
+    with pytest.raises(crt.CrtError):
+        crt.Context(sort_digit_bits=5)
+
+
+def test_struct_sizes_match_reference_records():
+    code = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "crt.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(crt_triangle), sizeof(crt_mesh_model),
+         sizeof(crt_bvh_node), sizeof(crt_ray), sizeof(crt_hit), offsetof(crt_bvh_node, mx),
+         offsetof(crt_bvh_node, tri), offsetof(crt_bvh_node, right), offsetof(crt_triangle, model_id));
+  return 0;
+}'''
+    tmp = os.path.join(ROOT, "_work", "abi_sizes")
+    os.makedirs(tmp, exist_ok=True)
+    src = os.path.join(tmp, "sizes.c")
+    with open(src, "w") as f:
+        f.write(code)
+    exe = os.path.join(tmp, "sizes")
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    # TriangleGPU 64, MeshModelGPU 68, BVH_NodeGPU 48 (max @16, tri @32, right @40)
+    assert [int(x) for x in out] == [64, 68, 48, 32, 16, 16, 32, 40, 48]
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/srcCommon"), reason="reference checkout not present")
+def test_adapter_compiles_and_links_against_reference_header(lib):
+    gxx = shutil.which("g++")
+    tmp = os.path.join(ROOT, "_work", "adapter_build")
+    os.makedirs(tmp, exist_ok=True)
+    inc = ["-I", os.path.join(ROOT, "oracle", "glm_shim"), "-I", "/root/reference/srcCommon/scene/geometry",
+           "-I", os.path.join(ROOT, "include")]
+    obj = os.path.join(tmp, "bvh_cuda.o")
+    subprocess.run([gxx, "-std=gnu++20", "-O2", "-c", os.path.join(ROOT, "adapter", "bvh_cuda.cpp"), *inc, "-o", obj],
+                   check=True)
+    main = os.path.join(tmp, "main.cpp")
+    with open(main, "w") as f:
+        f.write('#include "bvh.hpp"\nint main(){ std::vector<cr::TriangleGPU> t(4); '
+                'std::vector<cr::MeshModelGPU> m(cr::Mesh::MAX_NB_MESHES); cr::BVH b(4, t, m); return 0; }\n')
+    libdir = os.path.join(ROOT, "realtimeraytracing_gb300")
+    subprocess.run([gxx, "-std=gnu++20", main, obj, *inc, "-L", libdir, "-lcrt", f"-Wl,-rpath,{libdir}",
+                    "-o", os.path.join(tmp, "main")], check=True)
