@@ -207,6 +207,30 @@ crt_status crt_trace_frame(crt_ctx* ctx, const crt_bvh* bvh, const crt_camera* c
                            uint32_t height, const float* light, uint32_t flags, crt_hit* hits_primary,
                            crt_hit* hits_shadow);
 
+/* ---- allocation-free Morton + sort ------------------------------------
+ * No counterpart in the reference (its build allocates std::vectors freely).
+ * For callers that must not have this library allocate device memory — e.g.
+ * an engine that gives all device memory to its own pool and forbids the
+ * libraries it embeds from calling cudaMalloc, whose allocations would escape
+ * its budget and can stall the device mid-frame.  Computes what crt_build
+ * computes first: Morton codes of the first n_tris of n_buffer triangles,
+ * sorted with their indices; codes_out / perm_out match crt_bvh_copy_codes /
+ * crt_bvh_copy_perm of crt_build on the same input.
+ *   tris, codes_out, perm_out  device memory; models: host memory (or NULL
+ *   when n_models == 0); stream: a cudaStream_t, NULL for the default stream.
+ * It calls no cudaMalloc/cudaFree: its scratch is one fixed array of about
+ * 4.5 MB compiled into the library and kept on every GPU that loads it until
+ * the process exits, which caps n_tris at CRT_NOALLOC_MAX_TRIANGLES (larger
+ * inputs return CRT_ERR_INVALID_ARG).  All calls share that array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks up the array's device address and must come
+ * before any stream capture on that device.  Returns after the stream
+ * synchronises. */
+#define CRT_NOALLOC_MAX_TRIANGLES 262144u
+crt_status crt_morton_sort_noalloc(const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
+                                   const crt_mesh_model* models, uint32_t n_models, uint32_t* codes_out,
+                                   uint32_t* perm_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,7 @@ EXPORTS = [
     "crt_stream", "crt_build", "crt_rebuild", "crt_bvh_free", "crt_bvh_node_count", "crt_bvh_triangle_count",
     "crt_bvh_nodes_device", "crt_bvh_copy_nodes", "crt_bvh_copy_codes", "crt_bvh_copy_perm", "crt_last_build_stats",
     "crt_raygen_pinhole", "crt_shadow_rays", "crt_trace", "crt_last_trace_stats", "crt_trace_frame",
+    "crt_morton_sort_noalloc",
 ]
 
 
@@ -91,6 +92,7 @@ def lib():
             "crt_trace": ([vp, vp, vp, u32, u32, vp], i32),
             "crt_last_trace_stats": ([vp, vp], i32),
             "crt_trace_frame": ([vp, vp, vp, u32, u32, vp, u32, vp, vp], i32),
+            "crt_morton_sort_noalloc": ([vp, u32, u32, vp, u32, vp, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -79,6 +79,10 @@ constexpr uint32_t kDefaultSpin = 1u << 22;   // ~0.3 s with back-off; far above
 
 }  // namespace
 
+namespace crt {
+void set_last_error(const char* msg) { std::snprintf(g_err, sizeof(g_err), "%s", msg); }
+}  // namespace crt
+
 struct crt_bvh {
     crt_ctx* ctx = nullptr;
     uint32_t n = 0;

@@ -56,6 +56,9 @@ struct TraceParams {
     unsigned long long* stats;  // optional: nodes visited, triangles tested
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
+// Sets the message crt_last_error_string() returns on the calling thread.
+void set_last_error(const char* msg);
+
 void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s);
 void launch_shadow_rays(const crt_ray* prim, const crt_hit* hits, uint32_t n, float lx, float ly, float lz, crt_ray* out,
                         cudaStream_t s);
