@@ -225,7 +225,7 @@ def run_ours(args):
             kev[k][1].record(stream)
     torch.cuda.synchronize()
     k_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
-    alg_bytes = 48.0 * visited + 48.0 * tested + (32.0 + 16.0) * n_rays
+    alg_bytes = 64.0 * visited + 48.0 * tested + (32.0 + 16.0) * n_rays
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     traffic = read_profile_traffic()
@@ -285,7 +285,7 @@ def run_ours(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": peak_kind, "ms_per_launch": round(k_ms, 4),
                          "alg_bytes_per_launch": int(alg_bytes),
-                         "nodes_per_ray": round(visited / n_rays, 2), "tris_per_ray": round(tested / n_rays, 2)},
+                         "node_fetches_per_ray": round(visited / n_rays, 2), "tris_per_ray": round(tested / n_rays, 2)},
             "cpu_baseline": cpu,
             "clocks": clk,
         }

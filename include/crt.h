@@ -193,7 +193,7 @@ crt_status crt_shadow_rays(crt_ctx* ctx, const crt_ray* primary, const crt_hit* 
 crt_status crt_trace(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, uint32_t n_rays,
                      uint32_t flags, crt_hit* hits);
 /* Counters of the last crt_trace issued with CRT_TRACE_STATS:
- * out[0] = node boxes tested, out[1] = triangles tested. */
+ * out[0] = 64-byte traversal nodes fetched, out[1] = triangles tested. */
 crt_status crt_last_trace_stats(crt_ctx* ctx, uint64_t out[2]);
 
 /* One frame of the reference's compute pass (Application::drawOneFrame,

@@ -88,7 +88,7 @@ struct crt_bvh {
     uint32_t n = 0;
     uint32_t iterations = 0;
     float abs_eps = 0.f;
-    DevBuf nodes, xtri, codes, perm;
+    DevBuf nodes, wide, xtri, codes, perm;
 };
 
 struct crt_ctx {
@@ -263,13 +263,14 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(x->vals_b.reserve(4ull * N));
     CRT_TRY(x->node_box.reserve(32ull * (2ull * N - 1)));
     CRT_TRY(x->node_lc.reserve(4ull * N));
-    CRT_TRY(x->pos.reserve(4ull * N));
+    CRT_TRY(x->pos.reserve(8ull * N));
     CRT_TRY(x->clus_a.reserve(32ull * N));
     CRT_TRY(x->clus_b.reserve(32ull * N));
     CRT_TRY(x->iters.reserve(8ull * (N + 2)));
     CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 16));
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
+    CRT_TRY(b->wide.reserve(64ull * N));
     CRT_TRY(b->codes.reserve(4ull * N));
     CRT_TRY(b->perm.reserve(4ull * N));
 
@@ -388,8 +389,9 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), s);
     } else {
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
-            crt::launch_layout_level(x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), x->pos.as<uint32_t>(),
-                                     x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(), err, s);
+            crt::launch_layout_level(x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), x->pos.as<uint2>(),
+                                     x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(),
+                                     b->wide.as<float4>(), err, s);
     }
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->ev[4], s));
@@ -445,6 +447,7 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
     p.xtri = b->xtri.as<float4>();
+    p.wide = b->wide.as<float4>();
     p.rays = d_rays;
     p.hits = d_hits;
     p.n_rays = n_rays;
@@ -490,6 +493,7 @@ crt_status crt_bvh_free(crt_bvh* b) {
     if (!b) return CRT_OK;
     b->nodes.release();
     b->xtri.release();
+    b->wide.release();
     b->codes.release();
     b->perm.release();
     delete b;

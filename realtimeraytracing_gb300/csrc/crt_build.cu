@@ -347,9 +347,10 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
     mx.w = __uint_as_float(1u);
     clusters[2 * static_cast<size_t>(i)] = mn;
     clusters[2 * static_cast<size_t>(i) + 1] = mx;
-    xtri[3 * static_cast<size_t>(ti) + 0] = make_float4(p0.x, p0.y, p0.z, 0.f);
-    xtri[3 * static_cast<size_t>(ti) + 1] = make_float4(p1.x, p1.y, p1.z, 0.f);
-    xtri[3 * static_cast<size_t>(ti) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
+    // leaf order (= left-to-right order of the final tree), triangle id in .w
+    xtri[3 * static_cast<size_t>(i) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(ti));
+    xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, 0.f);
+    xtri[3 * static_cast<size_t>(i) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
 }
 
 // ================================================ K3: one PLOC iteration
@@ -528,18 +529,29 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 // puts its left child at p+1 and its right child at p + 2*leaves(left).
 // Nodes created in PLOC iteration k only have parents from later
 // iterations, so levels are laid out from the last iteration down.
+//
+// The same pass writes the traversal's own node format: one 64-byte record
+// per internal node holding both children's boxes and references, indexed by
+// the node's rank among internal nodes in DFS order (position minus the
+// leaves before it, i.e. minus its first leaf).  Leaves are referenced by
+// their sorted position, which is also their left-to-right order in the tree
+// (PLOC merges keep Morton order), so the traversal's triangles are stored
+// in that order.
 __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
                                                            const uint32_t* __restrict__ node_lc,
-                                                           uint32_t* __restrict__ pos, uint32_t id_begin, uint32_t id_end,
-                                                           uint32_t N, crt_bvh_node* __restrict__ out, uint32_t* err) {
+                                                           uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
+                                                           uint32_t N, crt_bvh_node* __restrict__ out,
+                                                           float4* __restrict__ wide, uint32_t* err) {
     const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (X >= id_end) return;
-    const uint32_t p = (X == 2 * N - 2) ? 0u : pos[X - N];
+    // (DFS position, first leaf below) of X; the root sits at (0, 0)
+    const uint2 me = (X == 2 * N - 2) ? make_uint2(0u, 0u) : pf[X - N];
+    const uint32_t p = me.x, f = me.y;
     const float4 mn = node_box[2 * static_cast<size_t>(X)], mx = node_box[2 * static_cast<size_t>(X) + 1];
     const uint32_t a = __float_as_uint(mn.w), b = __float_as_uint(mx.w);
     const uint32_t lca = (a < N) ? 1u : node_lc[a - N];
     const uint32_t pl = p + 1, pr = p + 2 * lca;
-    if (pr >= 2 * N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
+    if (pr >= 2 * N - 1 || p < f || p - f >= N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
         raise_corrupt(err, 4, X, pr);
         return;
     }
@@ -547,19 +559,30 @@ __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restr
     o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
     o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
     reinterpret_cast<uint4*>(o)[2] = make_uint4(0u, pl, pr, 0u);
-    const uint32_t ch[2] = {a, b}, cp[2] = {pl, pr};
+    const uint32_t ch[2] = {a, b}, cp[2] = {pl, pr}, cf[2] = {f, f + lca};
+    float4 cmn[2], cmx[2];
+    uint32_t cref[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
+        cmn[c] = node_box[2 * static_cast<size_t>(ch[c])];
+        cmx[c] = node_box[2 * static_cast<size_t>(ch[c]) + 1];
         if (ch[c] < N) {
-            const float4 lmn = node_box[2 * static_cast<size_t>(ch[c])], lmx = node_box[2 * static_cast<size_t>(ch[c]) + 1];
             float4* lo = reinterpret_cast<float4*>(out + cp[c]);
-            lo[0] = make_float4(lmn.x, lmn.y, lmn.z, 0.f);
-            lo[1] = make_float4(lmx.x, lmx.y, lmx.z, 0.f);
-            reinterpret_cast<uint4*>(lo)[2] = make_uint4(__float_as_uint(lmn.w), 0u, 0u, 0u);
+            lo[0] = make_float4(cmn[c].x, cmn[c].y, cmn[c].z, 0.f);
+            lo[1] = make_float4(cmx[c].x, cmx[c].y, cmx[c].z, 0.f);
+            reinterpret_cast<uint4*>(lo)[2] = make_uint4(__float_as_uint(cmn[c].w), 0u, 0u, 0u);
+            cref[c] = kLeafRef | ch[c];          // leaf: its sorted position
         } else {
-            pos[ch[c] - N] = cp[c];
+            pf[ch[c] - N] = make_uint2(cp[c], cf[c]);
+            cref[c] = cp[c] - cf[c];             // internal: its rank among internal nodes in DFS order
         }
     }
+    // traversal node: both child boxes and references in 64 bytes
+    float4* w = wide + 4 * static_cast<size_t>(p - f);
+    w[0] = make_float4(cmn[0].x, cmn[0].y, cmn[0].z, __uint_as_float(cref[0]));
+    w[1] = make_float4(cmx[0].x, cmx[0].y, cmx[0].z, __uint_as_float(cref[1]));
+    w[2] = make_float4(cmn[1].x, cmn[1].y, cmn[1].z, 0.f);
+    w[3] = make_float4(cmx[1].x, cmx[1].y, cmx[1].z, 0.f);
 }
 
 __global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out) {
@@ -614,11 +637,11 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
         cin, cout, node_box, node_lc, it, iter, N, radius, lookback, tickets, n_tiles_cap, err, spin_limit);
 }
 
-void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint32_t* pos, uint32_t id_begin,
-                         uint32_t id_end, uint32_t N, crt_bvh_node* out, uint32_t* err, cudaStream_t s) {
+void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
+                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint32_t* err, cudaStream_t s) {
     if (id_end <= id_begin || id_end > 2 * N - 1) return;
     const uint32_t cnt = id_end - id_begin;
-    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pos, id_begin, id_end, N, out, err);
+    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pf, id_begin, id_end, N, out, wide, err);
 }
 
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s) {

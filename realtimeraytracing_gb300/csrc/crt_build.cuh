@@ -11,6 +11,7 @@ namespace crt {
 
 constexpr uint32_t kPlocTile = 1024;      // positions per PLOC tile
 constexpr int kPlocMaxRadius = 32;        // largest supported PLOC radius
+constexpr uint32_t kLeafRef = 0x80000000u;  // traversal child reference: leaf flag | sorted position
 
 // Scene box reduction state (device memory, zeroed keys at creation; the
 // finishing block resets it) and its results for the Morton pass.
@@ -39,14 +40,15 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
                            int iter, uint32_t N, int radius, uint32_t n_upper,
                            unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
                            uint32_t spin_limit, cudaStream_t s);
-void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint32_t* pos, uint32_t id_begin,
-                         uint32_t id_end, uint32_t N, crt_bvh_node* out, uint32_t* err, cudaStream_t s);
+void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
+                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint32_t* err, cudaStream_t s);
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
 
 // Trace side (crt_trace.cu).
 struct TraceParams {
-    const crt_bvh_node* nodes;
-    const float4* xtri;      // 3 float4 per triangle: model-transformed p0, p1, p2
+    const crt_bvh_node* nodes;  // reference layout (root box read from nodes[0])
+    const float4* wide;      // 64-B traversal nodes: child boxes + child references
+    const float4* xtri;      // 3 float4 per leaf (sorted order): transformed p0 | tri id, p1, p2
     const crt_ray* rays;
     crt_hit* hits;
     uint32_t n_rays;

@@ -5,8 +5,10 @@
 // getClosestHitBVH :246-295.  Compiled with -fmad=false: every float
 // operation rounds once, in the shader's order, as in the CPU oracle.
 //
-// Traversal (one thread per ray, stack in local memory):
-//   * children are box-tested at their parent and visited near-first;
+// Traversal (one thread per ray, stack in local memory) over the 64-byte
+// traversal nodes the layout pass writes (both child boxes + references):
+//   * children are box-tested at their parent, leaves tested at once, the
+//     nearer internal child entered without a stack round trip;
 //   * a subtree is skipped when its entry distance exceeds the best hit by
 //     more than a slack of |t| * 2^-14 + abs_eps (abs_eps = 2^-20 of the scene
 //     extent), so no triangle that can tie or beat the best is lost;
@@ -168,83 +170,85 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
     WRay w{};
     if (WT) w = wt_setup(r.d);
     const float grow = WT ? p.abs_eps : 0.f;
+    const uint32_t n_leaves = (p.n_nodes + 1) / 2;
 
     bool have = false;
     float bt = tmax, bu = 0.f, bv = 0.f;
     uint32_t bkey = 0xFFFFFFFFu, btri = CRT_MISS;
-    uint64_t visited = 0, tested = 0;
+    uint32_t fetched = 0, tested = 0;
     bool overflow = false, corrupt = false;
-    const uint32_t n_tris = (p.n_nodes + 1) / 2;
 
-    uint32_t st_node[STACK];
-    float st_t[STACK];
-    int sp = 0;
-
-    const float4* nodes4 = reinterpret_cast<const float4*>(p.nodes);
-    auto test_leaf = [&](uint32_t pos, uint32_t tri) {
-        if (tri >= n_tris) { corrupt = true; return; }
+    // Leaf L (sorted position = left-to-right order): equal t keeps the leaf
+    // the shader visits first, the rightmost, so its key is ~L; watertight
+    // ties keep the lower triangle id.
+    auto test_leaf = [&](uint32_t L) {
+        if (L >= n_leaves) { corrupt = true; return; }
         ++tested;
-        const float4 a = __ldg(p.xtri + 3 * static_cast<size_t>(tri));
-        const float4 b = __ldg(p.xtri + 3 * static_cast<size_t>(tri) + 1);
-        const float4 c = __ldg(p.xtri + 3 * static_cast<size_t>(tri) + 2);
+        const float4* t = p.xtri + 3 * static_cast<size_t>(L);
+        const float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
         const float3 A = make_float3(a.x, a.y, a.z), B = make_float3(b.x, b.y, b.z), C = make_float3(c.x, c.y, c.z);
         const HitRes h = WT ? tri_watertight(r.o, tmin, tmax, w, A, B, C) : tri_reference(r.o, r.d, tmin, tmax, A, B, C);
         if (!h.did) return;
-        const uint32_t key = WT ? tri : ~pos;
+        const uint32_t tri = __float_as_uint(a.w);
+        const uint32_t key = WT ? tri : ~L;
         if (!have || h.t < bt || (h.t == bt && key < bkey)) {
             have = true; bt = h.t; bu = h.u; bv = h.v; bkey = key; btri = tri;
         }
     };
 
-    {  // root
-        const float4 mn = __ldg(nodes4 + 0), mx = __ldg(nodes4 + 1);
-        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(nodes4 + 2));
+    uint32_t st_node[STACK];
+    float st_t[STACK];
+    int sp = 0;
+    uint32_t cur = 0xFFFFFFFFu;
+    {  // root box (reference record 0)
+        const float4* n4 = reinterpret_cast<const float4*>(p.nodes);
+        const float4 mn = __ldg(n4), mx = __ldg(n4 + 1);
+        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(n4 + 2));
         float te;
-        ++visited;
         if (slab(r, mn, mx, grow, te) && te <= prune_bound(bt, p.abs_eps)) {
-            if (lr.y == 0u && lr.z == 0u) test_leaf(0u, lr.x);
-            else { st_node[0] = 0u; st_t[0] = te; sp = 1; }
+            if (lr.y == 0u && lr.z == 0u) test_leaf(0u);
+            else cur = 0u;
         }
     }
-    while (sp > 0) {
+    while (cur != 0xFFFFFFFFu) {
+        if (cur >= n_leaves - 1) { corrupt = true; break; }
+        ++fetched;
+        const float4* nd = p.wide + 4 * static_cast<size_t>(cur);
+        const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
+        const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
+        float t0, t1;
+        bool h0 = slab(r, w0, w1, grow, t0);
+        bool h1 = slab(r, w2, w3, grow, t1);
+        const float bnd = prune_bound(bt, p.abs_eps);
+        h0 = h0 && t0 <= bnd;
+        h1 = h1 && t1 <= bnd;
+        if (h0 && (ref0 & kLeafRef)) { test_leaf(ref0 & ~kLeafRef); h0 = false; }
+        if (h1 && (ref1 & kLeafRef)) { test_leaf(ref1 & ~kLeafRef); h1 = false; }
         if (ANY && have) break;
-        --sp;
-        const uint32_t pi = st_node[sp];
-        if (st_t[sp] > prune_bound(bt, p.abs_eps)) continue;
-        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(nodes4 + 3 * static_cast<size_t>(pi) + 2));
-        const uint32_t ch[2] = {lr.y, lr.z};
-        bool pass[2];
-        float te[2];
-        uint4 chl[2];
-        if (ch[0] >= p.n_nodes || ch[1] >= p.n_nodes) {
-            overflow = true;  // corrupt node array: reported, never dereferenced
-            corrupt = true;
-            continue;
+        if (h0 || h1) {
+            const float bnd2 = prune_bound(bt, p.abs_eps);
+            h0 = h0 && t0 <= bnd2;
+            h1 = h1 && t1 <= bnd2;
         }
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const float4* cn = nodes4 + 3 * static_cast<size_t>(ch[c]);
-            const float4 mn = __ldg(cn), mx = __ldg(cn + 1);
-            chl[c] = __ldg(reinterpret_cast<const uint4*>(cn + 2));
-            ++visited;
-            pass[c] = slab(r, mn, mx, grow, te[c]);
-        }
-        // near child last on the stack (visited first)
-        const int first = (te[1] < te[0]) ? 1 : 0;
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const int c = (k == 0) ? 1 - first : first;
-            if (!pass[c] || te[c] > prune_bound(bt, p.abs_eps)) continue;
-            if (chl[c].y == 0u && chl[c].z == 0u) {
-                test_leaf(ch[c], chl[c].x);
-                if (ANY && have) break;
-            } else if (sp < STACK) {
-                st_node[sp] = ch[c];
-                st_t[sp] = te[c];
+        if (h0 && h1) {
+            const bool near1 = t1 < t0;
+            if (sp < STACK) {
+                st_node[sp] = near1 ? ref0 : ref1;
+                st_t[sp] = near1 ? t0 : t1;
                 ++sp;
             } else {
                 overflow = true;
             }
+            cur = near1 ? ref1 : ref0;
+            continue;
+        }
+        if (h0) { cur = ref0; continue; }
+        if (h1) { cur = ref1; continue; }
+        cur = 0xFFFFFFFFu;
+        const float bnd3 = prune_bound(bt, p.abs_eps);
+        while (sp > 0) {
+            --sp;
+            if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
         }
     }
     if (have) out = make_uint4(btri, __float_as_uint(bt), __float_as_uint(bu), __float_as_uint(bv));
@@ -252,7 +256,7 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
     if (corrupt) raise_corrupt(p.err, 5, i, 0u);
     else if (overflow) raise_error(p.err, kDevStackOverflow);
     if (p.stats) {
-        atomicAdd(p.stats + 0, static_cast<unsigned long long>(visited));
+        atomicAdd(p.stats + 0, static_cast<unsigned long long>(fetched));
         atomicAdd(p.stats + 1, static_cast<unsigned long long>(tested));
     }
 }
