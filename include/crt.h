@@ -207,6 +207,62 @@ crt_status crt_trace_frame(crt_ctx* ctx, const crt_bvh* bvh, const crt_camera* c
                            uint32_t height, const float* light, uint32_t flags, crt_hit* hits_primary,
                            crt_hit* hits_shadow);
 
+/* ---- learned hit predictor (no counterpart in the reference) --------------
+ * An FP16 MLP on tcgen05 tensor cores maps a ray (origin cell on a 64^3 grid,
+ * direction in 32x32 octahedral bins, each through a learned 16-wide
+ * embedding) through 32 -> 64 -> 64 -> 128 to a treelet of the BVH (the BVH
+ * cut into <= 127 subtrees, class 127 = miss).  crt_trace with
+ * CRT_TRACE_USE_PREDICTOR first searches the predicted treelet exactly and
+ * seeds t_max with that hit, then runs the full traversal: results are
+ * identical to the plain traversal; only the work changes.  Training is
+ * online on the tracer's own exact hits (softmax cross-entropy, Adam with
+ * FP32 master weights).  A predictor is bound to one BVH; call
+ * crt_predictor_retarget after rebuilding that BVH. */
+typedef struct crt_predictor crt_predictor;
+typedef struct crt_predictor_config {
+    uint32_t seed;          /* weight initialisation seed */
+    float lr;               /* Adam learning rate, default 1e-3 */
+    uint32_t train_stride;  /* train on every train_stride-th ray (20 = 5%) */
+    uint32_t batch;         /* samples per Adam step, default 16384 */
+    float miss_threshold;   /* seed the likeliest treelet unless P(miss) >= this, default 0.9 */
+} crt_predictor_config;
+#define CRT_PREDICTOR_CLASSES 128u
+#define CRT_PREDICTOR_PARAMS 4225280u   /* floats in the flat parameter / gradient vector */
+
+void crt_predictor_default_config(crt_predictor_config* cfg);
+crt_status crt_predictor_create(crt_ctx* ctx, crt_bvh* bvh, const crt_predictor_config* cfg, crt_predictor** out);
+crt_status crt_predictor_destroy(crt_predictor* pred);
+/* Recompute the treelet cut and classes after the bound BVH was rebuilt. */
+crt_status crt_predictor_retarget(crt_ctx* ctx, crt_predictor* pred);
+/* Train on rays offset, offset + stride, ... of (rays, hits) — hits from the
+ * exact tracer — in Adam steps of `batch` samples; mean loss to *loss. */
+crt_status crt_predictor_train(crt_ctx* ctx, crt_predictor* pred, const crt_ray* rays, const crt_hit* hits,
+                               uint32_t n_rays, uint32_t offset, float* loss);
+/* crt_trace seeded from caller-given classes instead of the network's (for
+ * measuring a given prediction quality, e.g. the true classes). */
+crt_status crt_trace_seeded(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, uint32_t n_rays, uint32_t flags,
+                            const uint16_t* classes, crt_hit* hits);
+/* Predicted class per ray: the likeliest treelet, or 127 when the network
+ * gives a miss at least miss_threshold probability. */
+crt_status crt_predictor_infer(crt_ctx* ctx, crt_predictor* pred, const crt_ray* rays, uint32_t n, uint16_t* classes);
+/* The class an exact hit belongs to (treelet of its triangle, or 127). */
+crt_status crt_predictor_classes_of_hits(crt_ctx* ctx, crt_predictor* pred, const crt_hit* hits, uint32_t n,
+                                         uint16_t* classes);
+/* Forward + backward only, on explicit target classes: gradient sums (not
+ * averaged) over the n rays into grad[CRT_PREDICTOR_PARAMS], summed loss. */
+crt_status crt_predictor_gradients(crt_ctx* ctx, crt_predictor* pred, const crt_ray* rays, const uint16_t* targets,
+                                   uint32_t n, float* grad, float* loss);
+/* Copy the FP32 master parameters out (set = 0) or in (set = 1). */
+crt_status crt_predictor_params(crt_ctx* ctx, crt_predictor* pred, float* params, int set);
+/* info[0] = parameters, [1] = classes, [2] = treelets, [3] = Adam steps taken. */
+crt_status crt_predictor_info(const crt_predictor* pred, uint32_t info[4]);
+
+/* Cosine-weighted diffuse bounce rays about the geometric normal of primary
+ * hits: ray j starts at the first hit at or after a scrambled primary index
+ * (incoherent order); [tmin, tmax] = [1e-4, +inf]. */
+crt_status crt_bounce_rays(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* primary, const crt_hit* hits,
+                           uint32_t n_primary, uint32_t n_out, uint32_t seed, crt_ray* out);
+
 /* ---- allocation-free Morton + sort ------------------------------------
  * No counterpart in the reference (its build allocates std::vectors freely).
  * For callers that must not have this library allocate device memory — e.g.

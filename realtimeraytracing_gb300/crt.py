@@ -26,6 +26,7 @@ TRI_REFERENCE = 0x0
 TRI_WATERTIGHT = 0x2
 TRACE_USE_PREDICTOR = 0x4
 TRACE_STATS = 0x8
+USE_PREDICTOR = TRACE_USE_PREDICTOR
 MISS = 0xFFFFFFFF
 
 # Every symbol include/crt.h declares.
@@ -34,8 +35,13 @@ EXPORTS = [
     "crt_stream", "crt_build", "crt_rebuild", "crt_bvh_free", "crt_bvh_node_count", "crt_bvh_triangle_count",
     "crt_bvh_nodes_device", "crt_bvh_copy_nodes", "crt_bvh_copy_codes", "crt_bvh_copy_perm", "crt_last_build_stats",
     "crt_raygen_pinhole", "crt_shadow_rays", "crt_trace", "crt_last_trace_stats", "crt_trace_frame",
-    "crt_morton_sort_noalloc",
+    "crt_morton_sort_noalloc", "crt_predictor_default_config", "crt_predictor_create", "crt_predictor_destroy",
+    "crt_predictor_retarget", "crt_predictor_train", "crt_predictor_infer", "crt_predictor_classes_of_hits",
+    "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
 ]
+
+PREDICTOR_CLASSES = 128
+PREDICTOR_PARAMS = 4225280
 
 
 class CrtError(RuntimeError):
@@ -93,6 +99,18 @@ def lib():
             "crt_last_trace_stats": ([vp, vp], i32),
             "crt_trace_frame": ([vp, vp, vp, u32, u32, vp, u32, vp, vp], i32),
             "crt_morton_sort_noalloc": ([vp, u32, u32, vp, u32, vp, vp, vp], i32),
+            "crt_predictor_default_config": ([vp], None),
+            "crt_predictor_create": ([vp, vp, vp, C.POINTER(vp)], i32),
+            "crt_predictor_destroy": ([vp], i32),
+            "crt_predictor_retarget": ([vp, vp], i32),
+            "crt_predictor_train": ([vp, vp, vp, vp, u32, u32, vp], i32),
+            "crt_predictor_infer": ([vp, vp, vp, u32, vp], i32),
+            "crt_predictor_classes_of_hits": ([vp, vp, vp, u32, vp], i32),
+            "crt_predictor_gradients": ([vp, vp, vp, vp, u32, vp, vp], i32),
+            "crt_predictor_params": ([vp, vp, vp, i32], i32),
+            "crt_predictor_info": ([vp, vp], i32),
+            "crt_bounce_rays": ([vp, vp, vp, vp, u32, u32, u32, vp], i32),
+            "crt_trace_seeded": ([vp, vp, vp, u32, u32, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -124,6 +142,78 @@ def _ptr(a):
 
 def _rows(a):
     return a.shape[0]
+
+
+class PredictorConfig(C.Structure):
+    _fields_ = [("seed", C.c_uint32), ("lr", C.c_float), ("train_stride", C.c_uint32), ("batch", C.c_uint32),
+                ("miss_threshold", C.c_float)]
+
+
+class Predictor:
+    """The learned hit predictor bound to one BVH (crt_predictor)."""
+
+    def __init__(self, ctx: "Context", bvh: "Bvh", seed: int = 1, lr: float = 1e-3, train_stride: int = 20,
+                 batch: int = 16384, miss_threshold: float = 0.9):
+        cfg = PredictorConfig()
+        lib().crt_predictor_default_config(C.byref(cfg))
+        cfg.seed, cfg.lr, cfg.train_stride, cfg.batch = seed, lr, train_stride, batch
+        cfg.miss_threshold = miss_threshold
+        h = C.c_void_p()
+        _check(lib().crt_predictor_create(ctx.handle, bvh.handle, C.byref(cfg), C.byref(h)))
+        self.ctx, self.bvh, self.handle = ctx, bvh, h
+
+    def info(self) -> dict:
+        out = np.zeros(4, np.uint32)
+        _check(lib().crt_predictor_info(self.handle, _ptr(out)))
+        return {"params": int(out[0]), "classes": int(out[1]), "treelets": int(out[2]), "steps": int(out[3])}
+
+    def retarget(self):
+        _check(lib().crt_predictor_retarget(self.ctx.handle, self.handle))
+
+    def train(self, rays, hits, offset: int = 0) -> float:
+        loss = C.c_float()
+        _check(lib().crt_predictor_train(self.ctx.handle, self.handle, _ptr(rays), _ptr(hits), _rows(rays), offset,
+                                         C.byref(loss)))
+        return loss.value
+
+    def infer(self, rays, out=None):
+        out = np.empty(_rows(rays), np.uint16) if out is None else out
+        _check(lib().crt_predictor_infer(self.ctx.handle, self.handle, _ptr(rays), _rows(rays), _ptr(out)))
+        return out
+
+    def classes_of_hits(self, hits, out=None):
+        out = np.empty(_rows(hits), np.uint16) if out is None else out
+        _check(lib().crt_predictor_classes_of_hits(self.ctx.handle, self.handle, _ptr(hits), _rows(hits), _ptr(out)))
+        return out
+
+    def gradients(self, rays, targets):
+        grad = np.empty(PREDICTOR_PARAMS, np.float32)
+        loss = C.c_float()
+        targets = np.ascontiguousarray(targets, np.uint16)
+        _check(lib().crt_predictor_gradients(self.ctx.handle, self.handle, _ptr(rays), _ptr(targets), _rows(rays),
+                                             _ptr(grad), C.byref(loss)))
+        return grad, loss.value
+
+    def params(self):
+        out = np.empty(PREDICTOR_PARAMS, np.float32)
+        _check(lib().crt_predictor_params(self.ctx.handle, self.handle, _ptr(out), 0))
+        return out
+
+    def set_params(self, params):
+        params = np.ascontiguousarray(params, np.float32)
+        assert params.shape == (PREDICTOR_PARAMS,)
+        _check(lib().crt_predictor_params(self.ctx.handle, self.handle, _ptr(params), 1))
+
+    def free(self):
+        if self.handle:
+            lib().crt_predictor_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class Bvh:
@@ -248,6 +338,18 @@ class Context:
         n = _rows(rays)
         out = np.empty((n, 4), np.float32) if out is None else out
         _check(lib().crt_trace(self.handle, bvh.handle, _ptr(rays), n, flags, _ptr(out)))
+        return out
+
+    def bounce_rays(self, bvh: "Bvh", primary, hits, n_out: int, seed: int = 7, out=None):
+        out = np.empty((n_out, 8), np.float32) if out is None else out
+        _check(lib().crt_bounce_rays(self.handle, bvh.handle, _ptr(primary), _ptr(hits), _rows(primary), n_out, seed,
+                                     _ptr(out)))
+        return out
+
+    def trace_seeded(self, bvh: "Bvh", rays, classes, flags: int = 0, out=None):
+        """Trace with the treelet of classes[i] searched first (device arrays)."""
+        _check(lib().crt_trace_seeded(self.handle, bvh.handle, _ptr(rays), _rows(rays), flags, _ptr(classes),
+                                      _ptr(out)))
         return out
 
     def last_trace_stats(self):

@@ -2,6 +2,7 @@
 // pipeline (scene box -> Morton -> radix sort -> PLOC -> DFS layout) and the
 // trace entry points.  No compute happens on the host: a call that cannot
 // run its kernels returns an error instead of falling back.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -88,7 +89,34 @@ struct crt_bvh {
     uint32_t n = 0;
     uint32_t iterations = 0;
     float abs_eps = 0.f;
-    DevBuf nodes, wide, xtri, codes, perm;
+    DevBuf nodes, wide, xtri, codes, perm, inv_perm;
+    crt_predictor* predictor = nullptr;
+};
+
+struct crt_predictor {
+    crt_bvh* bvh = nullptr;
+    crt_predictor_config cfg{};
+    DevBuf params;      // master | m | v | grad, CRT_PREDICTOR_PARAMS floats each
+    DevBuf w16;         // fp16 copies
+    DevBuf tri_class;   // triangle -> class
+    DevBuf treelets;    // Treelet[127] + count
+    DevBuf classes;     // per-ray predicted classes (trace scratch)
+    DevBuf scratch;     // loss accumulator
+    DevBuf rays_in, hits_in, targets_in;
+    uint32_t step = 0;
+    uint32_t n_treelets = 0;
+    crt::PredictorDev dev() const {
+        crt::PredictorDev d;
+        float* base = params.as<float>();
+        d.master = base;
+        d.m = base + crt::pred::kParams;
+        d.v = base + 2 * crt::pred::kParams;
+        d.grad = base + 3 * crt::pred::kParams;
+        d.w16 = w16.as<__half>();
+        d.tri_class = tri_class.as<uint8_t>();
+        d.n_tris = bvh ? bvh->n : 0;
+        return d;
+    }
 };
 
 struct crt_ctx {
@@ -271,6 +299,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
     CRT_TRY(b->wide.reserve(64ull * N));
+    CRT_TRY(b->inv_perm.reserve(4ull * N));
     CRT_TRY(b->codes.reserve(4ull * N));
     CRT_TRY(b->perm.reserve(4ull * N));
 
@@ -330,7 +359,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     // ---- K3: leaf clusters + PLOC iterations
     uint2* d_it = x->iters.as<uint2>();
     crt::launch_leaf_init(d_tris, N, d_models, b->perm.as<uint32_t>(), x->node_box.as<float4>(), x->clus_a.as<float4>(),
-                          b->xtri.as<float4>(), d_it, err, s);
+                          b->xtri.as<float4>(), b->inv_perm.as<uint32_t>(), d_it, err, s);
     CRT_CUDA(cudaGetLastError());
     x->it_host.assign(1, make_uint2(N, N));
     uint32_t iters = 0;
@@ -435,14 +464,15 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
 crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
     if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
-    if (flags & CRT_TRACE_USE_PREDICTOR) return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor attached");
+    if ((flags & CRT_TRACE_USE_PREDICTOR) && !b->predictor)
+        return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor bound to this bvh (crt_predictor_create)");
     if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_trace: empty bvh");
     return CRT_OK;
 }
 
 // Enqueues one traversal launch on device-resident rays/hits (no sync).
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
-                        crt_hit* d_hits) {
+                        crt_hit* d_hits, const uint16_t* seed_classes = nullptr) {
     if (n_rays == 0) return CRT_OK;
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
@@ -458,6 +488,19 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     if (flags & CRT_TRACE_STATS) {
         CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
         p.stats = x->trace_stats.as<unsigned long long>();
+    }
+    if (seed_classes) {
+        p.pred_class = seed_classes;
+        p.treelets = b->predictor->treelets.as<crt::Treelet>();
+        p.n_treelets = reinterpret_cast<const uint32_t*>(b->predictor->treelets.as<crt::Treelet>() + 128);
+    } else if (flags & CRT_TRACE_USE_PREDICTOR) {
+        crt_predictor* pr = b->predictor;
+        CRT_TRY(pr->classes.reserve(2ull * n_rays));
+        CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, n_rays, pr->classes.as<uint16_t>(),
+                                 pr->cfg.miss_threshold, x->err.as<uint32_t>(), x->stream));
+        p.pred_class = pr->classes.as<uint16_t>();
+        p.treelets = pr->treelets.as<crt::Treelet>();
+        p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
     }
     const uint32_t launch_flags = (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) | ((b->iterations + 2 > 64) ? (1u << 16) : 0u);
     crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
@@ -494,6 +537,8 @@ crt_status crt_bvh_free(crt_bvh* b) {
     b->nodes.release();
     b->xtri.release();
     b->wide.release();
+    b->inv_perm.release();
+    if (b->predictor) b->predictor->bvh = nullptr;
     b->codes.release();
     b->perm.release();
     delete b;
@@ -602,6 +647,23 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
     return CRT_OK;
 }
 
+crt_status crt_trace_seeded(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t n_rays, uint32_t flags,
+                            const uint16_t* classes, crt_hit* hits) {
+    if (!x || !b || !rays || !hits || !classes) return fail(CRT_ERR_INVALID_ARG, "crt_trace_seeded: null argument");
+    if (!b->predictor) return fail(CRT_ERR_UNSUPPORTED, "crt_trace_seeded: the bvh has no treelet cut (crt_predictor_create)");
+    CRT_TRY(check_trace_flags(b, flags & ~CRT_TRACE_USE_PREDICTOR));
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n_rays == 0) return CRT_OK;
+    if (!is_device_ptr(rays) || !is_device_ptr(hits) || !is_device_ptr(classes))
+        return fail(CRT_ERR_INVALID_ARG, "crt_trace_seeded: rays, classes and hits must be device memory");
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    CRT_TRY(trace_device(x, b, rays, n_rays, flags & ~CRT_TRACE_USE_PREDICTOR, hits, classes));
+    CRT_TRY(x->check_device_error());
+    if (flags & CRT_TRACE_STATS)
+        CRT_CUDA(cudaMemcpy(x->last_trace_stats, x->trace_stats.p, 16, cudaMemcpyDeviceToHost));
+    return CRT_OK;
+}
+
 crt_status crt_last_trace_stats(crt_ctx* x, uint64_t out[2]) {
     if (!x || !out) return fail(CRT_ERR_INVALID_ARG, "null argument");
     out[0] = x->last_trace_stats[0];
@@ -649,6 +711,242 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
         if (!dev_s) CRT_CUDA(cudaMemcpyAsync(hits_shadow, d_hs, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
     }
     return x->check_device_error();
+}
+
+}  // extern "C"
+
+// ===================================================================== predictor
+namespace {
+
+crt_status stage_in(crt_ctx* x, DevBuf& buf, const void* src, size_t bytes, const void** dev) {
+    if (is_device_ptr(src)) { *dev = src; return CRT_OK; }
+    CRT_TRY(buf.reserve(bytes));
+    CRT_CUDA(cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, x->stream));
+    *dev = buf.p;
+    return CRT_OK;
+}
+
+crt_status predictor_targets(crt_ctx* x, crt_predictor* pr) {
+    crt_bvh* b = pr->bvh;
+    CRT_TRY(pr->tri_class.reserve(b->n));
+    CRT_TRY(pr->treelets.reserve(sizeof(crt::Treelet) * 128 + 16));
+    CRT_CUDA(cudaMemsetAsync(pr->tri_class.p, crt::pred::kMissClass, b->n, x->stream));
+    uint32_t* n_tl = reinterpret_cast<uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
+    crt::pred_treelets(b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->perm.as<uint32_t>(), b->n,
+                       pr->treelets.as<crt::Treelet>(), n_tl, pr->tri_class.as<uint8_t>(), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaMemcpyAsync(&pr->n_treelets, n_tl, 4, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+__global__ void classes_of_hits_kernel(const crt_hit* hits, uint32_t n, const uint8_t* tri_class, uint32_t n_tris,
+                                       uint16_t* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t t = hits[i].tri;
+    out[i] = (t == CRT_MISS || t >= n_tris) ? static_cast<uint16_t>(crt::pred::kMissClass) : tri_class[t];
+}
+
+}  // namespace
+
+extern "C" {
+
+void crt_predictor_default_config(crt_predictor_config* cfg) {
+    if (!cfg) return;
+    cfg->seed = 1;
+    cfg->lr = 1e-3f;
+    cfg->train_stride = 20;
+    cfg->batch = 16384;
+    cfg->miss_threshold = 0.9f;
+}
+
+crt_status crt_predictor_create(crt_ctx* x, crt_bvh* b, const crt_predictor_config* cfg, crt_predictor** out) {
+    if (!x || !b || !out) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_create: null argument");
+    if (b->n < 2) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_create: the bvh needs at least 2 triangles");
+    if (b->predictor) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_create: the bvh already has a predictor");
+    static_assert(crt::pred::kParams == CRT_PREDICTOR_PARAMS, "parameter count");
+    CRT_CUDA(cudaSetDevice(x->device));
+    crt_predictor* pr = new crt_predictor();
+    crt_predictor_default_config(&pr->cfg);
+    if (cfg) pr->cfg = *cfg;
+    if (pr->cfg.train_stride == 0) pr->cfg.train_stride = 1;
+    if (pr->cfg.batch == 0) pr->cfg.batch = 16384;
+    pr->bvh = b;
+    crt_status s = pr->params.reserve(4 * sizeof(float) * crt::pred::kParams);
+    if (s == CRT_OK) s = pr->w16.reserve(sizeof(__half) * crt::pred::kHalfs);
+    if (s == CRT_OK) s = pr->scratch.reserve(16);
+    if (s == CRT_OK) {
+        crt::pred_init(pr->dev(), pr->cfg.seed, x->stream);
+        s = predictor_targets(x, pr);
+    }
+    if (s != CRT_OK) {
+        crt_predictor_destroy(pr);
+        return s;
+    }
+    b->predictor = pr;
+    *out = pr;
+    return CRT_OK;
+}
+
+crt_status crt_predictor_destroy(crt_predictor* pr) {
+    if (!pr) return CRT_OK;
+    if (pr->bvh) pr->bvh->predictor = nullptr;
+    DevBuf* bufs[] = {&pr->params, &pr->w16, &pr->tri_class, &pr->treelets, &pr->classes, &pr->scratch,
+                      &pr->rays_in, &pr->hits_in, &pr->targets_in};
+    for (DevBuf* d : bufs) d->release();
+    delete pr;
+    return CRT_OK;
+}
+
+crt_status crt_predictor_retarget(crt_ctx* x, crt_predictor* pr) {
+    if (!x || !pr || !pr->bvh) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_retarget: null or unbound predictor");
+    CRT_CUDA(cudaSetDevice(x->device));
+    return predictor_targets(x, pr);
+}
+
+crt_status crt_predictor_train(crt_ctx* x, crt_predictor* pr, const crt_ray* rays, const crt_hit* hits,
+                               uint32_t n_rays, uint32_t offset, float* loss) {
+    if (!x || !pr || !pr->bvh || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_train: null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const void* d_rays;
+    const void* d_hits;
+    CRT_TRY(stage_in(x, pr->rays_in, rays, sizeof(crt_ray) * static_cast<size_t>(n_rays), &d_rays));
+    CRT_TRY(stage_in(x, pr->hits_in, hits, sizeof(crt_hit) * static_cast<size_t>(n_rays), &d_hits));
+    const uint32_t stride = pr->cfg.train_stride;
+    const uint32_t total = offset < n_rays ? (n_rays - offset + stride - 1) / stride : 0;
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    CRT_CUDA(cudaMemsetAsync(pr->scratch.p, 0, 16, x->stream));
+    for (uint32_t done = 0; done < total; done += pr->cfg.batch) {
+        const uint32_t nb = std::min(pr->cfg.batch, total - done);
+        CRT_CUDA(crt::pred_train_step(pr->dev(), pr->bvh->nodes.as<crt_bvh_node>(),
+                                      static_cast<const crt_ray*>(d_rays), n_rays, static_cast<const crt_hit*>(d_hits),
+                                      nullptr, nb, stride, offset + done * stride, pr->scratch.as<float>(),
+                                      x->err.as<uint32_t>(), x->stream));
+        ++pr->step;
+        crt::pred_adam(pr->dev(), 1.f / static_cast<float>(nb), pr->cfg.lr, pr->step, x->stream);
+        CRT_CUDA(cudaGetLastError());
+    }
+    float ls = 0.f;
+    CRT_CUDA(cudaMemcpyAsync(&ls, pr->scratch.p, 4, cudaMemcpyDeviceToHost, x->stream));
+    CRT_TRY(x->check_device_error());
+    if (loss) *loss = total ? ls / static_cast<float>(total) : 0.f;
+    return CRT_OK;
+}
+
+crt_status crt_predictor_infer(crt_ctx* x, crt_predictor* pr, const crt_ray* rays, uint32_t n, uint16_t* classes) {
+    if (!x || !pr || !pr->bvh || !rays || !classes) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_infer: null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n == 0) return CRT_OK;
+    const void* d_rays;
+    CRT_TRY(stage_in(x, pr->rays_in, rays, sizeof(crt_ray) * static_cast<size_t>(n), &d_rays));
+    const bool dev_out = is_device_ptr(classes);
+    uint16_t* d_out = classes;
+    if (!dev_out) {
+        CRT_TRY(pr->classes.reserve(2ull * n));
+        d_out = pr->classes.as<uint16_t>();
+    }
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    CRT_CUDA(crt::pred_infer(pr->dev(), pr->bvh->nodes.as<crt_bvh_node>(), static_cast<const crt_ray*>(d_rays), n,
+                             d_out, pr->cfg.miss_threshold, x->err.as<uint32_t>(), x->stream));
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(classes, d_out, 2ull * n, cudaMemcpyDeviceToHost, x->stream));
+    return x->check_device_error();
+}
+
+crt_status crt_predictor_classes_of_hits(crt_ctx* x, crt_predictor* pr, const crt_hit* hits, uint32_t n,
+                                         uint16_t* classes) {
+    if (!x || !pr || !pr->bvh || !hits || !classes) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n == 0) return CRT_OK;
+    const void* d_hits;
+    CRT_TRY(stage_in(x, pr->hits_in, hits, sizeof(crt_hit) * static_cast<size_t>(n), &d_hits));
+    const bool dev_out = is_device_ptr(classes);
+    uint16_t* d_out = classes;
+    if (!dev_out) {
+        CRT_TRY(pr->targets_in.reserve(2ull * n));
+        d_out = pr->targets_in.as<uint16_t>();
+    }
+    classes_of_hits_kernel<<<(n + 255) / 256, 256, 0, x->stream>>>(static_cast<const crt_hit*>(d_hits), n,
+                                                                    pr->tri_class.as<uint8_t>(), pr->bvh->n, d_out);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(classes, d_out, 2ull * n, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+crt_status crt_predictor_gradients(crt_ctx* x, crt_predictor* pr, const crt_ray* rays, const uint16_t* targets,
+                                   uint32_t n, float* grad, float* loss) {
+    if (!x || !pr || !pr->bvh || !rays || !targets || !grad) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const void* d_rays;
+    const void* d_t;
+    CRT_TRY(stage_in(x, pr->rays_in, rays, sizeof(crt_ray) * static_cast<size_t>(n), &d_rays));
+    CRT_TRY(stage_in(x, pr->targets_in, targets, 2ull * n, &d_t));
+    const crt::PredictorDev d = pr->dev();
+    CRT_CUDA(cudaMemsetAsync(d.grad, 0, sizeof(float) * crt::pred::kParams, x->stream));
+    CRT_CUDA(cudaMemsetAsync(pr->scratch.p, 0, 16, x->stream));
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    CRT_CUDA(crt::pred_train_step(d, pr->bvh->nodes.as<crt_bvh_node>(), static_cast<const crt_ray*>(d_rays), n, nullptr,
+                                  static_cast<const uint16_t*>(d_t), n, 1, 0, pr->scratch.as<float>(),
+                                  x->err.as<uint32_t>(), x->stream));
+    CRT_CUDA(cudaMemcpyAsync(grad, d.grad, sizeof(float) * crt::pred::kParams,
+                             is_device_ptr(grad) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, x->stream));
+    float ls = 0.f;
+    CRT_CUDA(cudaMemcpyAsync(&ls, pr->scratch.p, 4, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaMemsetAsync(d.grad, 0, sizeof(float) * crt::pred::kParams, x->stream));
+    CRT_TRY(x->check_device_error());
+    if (loss) *loss = ls;
+    return CRT_OK;
+}
+
+crt_status crt_predictor_params(crt_ctx* x, crt_predictor* pr, float* params, int set) {
+    if (!x || !pr || !params) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const size_t bytes = sizeof(float) * crt::pred::kParams;
+    const bool dev = is_device_ptr(params);
+    if (set) {
+        CRT_CUDA(cudaMemcpyAsync(pr->params.p, params, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 x->stream));
+        crt::pred_refresh_fp16(pr->dev(), x->stream);
+        CRT_CUDA(cudaGetLastError());
+    } else {
+        CRT_CUDA(cudaMemcpyAsync(params, pr->params.p, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                 x->stream));
+    }
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+crt_status crt_predictor_info(const crt_predictor* pr, uint32_t info[4]) {
+    if (!pr || !info) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    info[0] = static_cast<uint32_t>(crt::pred::kParams);
+    info[1] = crt::pred::kClasses;
+    info[2] = pr->n_treelets;
+    info[3] = pr->step;
+    return CRT_OK;
+}
+
+crt_status crt_bounce_rays(crt_ctx* x, const crt_bvh* b, const crt_ray* primary, const crt_hit* hits,
+                           uint32_t n_primary, uint32_t n_out, uint32_t seed, crt_ray* out) {
+    if (!x || !b || !primary || !hits || !out) return fail(CRT_ERR_INVALID_ARG, "crt_bounce_rays: null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n_out == 0) return CRT_OK;
+    const void* d_prim;
+    const void* d_hits;
+    CRT_TRY(stage_in(x, x->rays_in, primary, sizeof(crt_ray) * static_cast<size_t>(n_primary), &d_prim));
+    CRT_TRY(stage_in(x, x->hits_out, hits, sizeof(crt_hit) * static_cast<size_t>(n_primary), &d_hits));
+    const bool dev_out = is_device_ptr(out);
+    crt_ray* d_out = out;
+    if (!dev_out) {
+        CRT_TRY(x->rays_out.reserve(sizeof(crt_ray) * static_cast<size_t>(n_out)));
+        d_out = x->rays_out.as<crt_ray>();
+    }
+    crt::launch_bounce(static_cast<const crt_ray*>(d_prim), static_cast<const crt_hit*>(d_hits), n_primary,
+                       b->xtri.as<float4>(), b->inv_perm.as<uint32_t>(), b->n, n_out, seed, d_out, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(out, d_out, sizeof(crt_ray) * static_cast<size_t>(n_out), cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
 }
 
 }  // extern "C"

@@ -323,12 +323,14 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
                                                         const float* __restrict__ models,
                                                         const uint32_t* __restrict__ perm,
                                                         float4* __restrict__ node_box, float4* __restrict__ clusters,
-                                                        float4* __restrict__ xtri, uint2* it, uint32_t* err) {
+                                                        float4* __restrict__ xtri, uint32_t* __restrict__ inv_perm,
+                                                        uint2* it, uint32_t* err) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) it[0] = make_uint2(n, n);
     if (i >= n) return;
     const uint32_t ti = perm[i];
     if (ti >= n) { raise_corrupt(err, 1, i, ti); return; }
+    inv_perm[ti] = i;
     const TriRec t = load_tri(tris, ti);
     const float* M = models + 16 * (t.model & (kMaxModels - 1));
     const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
@@ -581,8 +583,9 @@ __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restr
     float4* w = wide + 4 * static_cast<size_t>(p - f);
     w[0] = make_float4(cmn[0].x, cmn[0].y, cmn[0].z, __uint_as_float(cref[0]));
     w[1] = make_float4(cmx[0].x, cmx[0].y, cmx[0].z, __uint_as_float(cref[1]));
-    w[2] = make_float4(cmn[1].x, cmn[1].y, cmn[1].z, 0.f);
-    w[3] = make_float4(cmx[1].x, cmx[1].y, cmx[1].z, 0.f);
+    const uint32_t lcb = (b < N) ? 1u : node_lc[b - N];
+    w[2] = make_float4(cmn[1].x, cmn[1].y, cmn[1].z, __uint_as_float(lca));  // leaf counts of the children
+    w[3] = make_float4(cmx[1].x, cmx[1].y, cmx[1].z, __uint_as_float(lcb));
 }
 
 __global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out) {
@@ -624,8 +627,9 @@ void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t*
 }
 
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
-                      float4* clusters, float4* xtri, uint2* it, uint32_t* err, cudaStream_t s) {
-    leaf_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(tris, n, models, perm, node_box, clusters, xtri, it, err);
+                      float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, uint32_t* err, cudaStream_t s) {
+    leaf_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(tris, n, models, perm, node_box, clusters, xtri, inv_perm, it,
+                                                     err);
 }
 
 void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "crt.h"
+#include "crt_predictor.cuh"
 
 namespace crt {
 
@@ -35,7 +36,7 @@ void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t*
                      int shift, int bits, const uint32_t* pass_hist, uint32_t* lookback, uint32_t* ticket, uint32_t* err,
                      uint32_t spin_limit, cudaStream_t s);
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
-                      float4* clusters, float4* xtri, uint2* it, uint32_t* err, cudaStream_t s);
+                      float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, uint32_t* err, cudaStream_t s);
 void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,
                            int iter, uint32_t N, int radius, uint32_t n_upper,
                            unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
@@ -56,6 +57,10 @@ struct TraceParams {
     float abs_eps;           // absolute slack of pruning, from the scene extent
     uint32_t* err;
     unsigned long long* stats;  // optional: nodes visited, triangles tested
+    // learned seeding (CRT_TRACE_USE_PREDICTOR): per-ray predicted treelet
+    const uint16_t* pred_class = nullptr;
+    const Treelet* treelets = nullptr;
+    const uint32_t* n_treelets = nullptr;
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
 // Sets the message crt_last_error_string() returns on the calling thread.

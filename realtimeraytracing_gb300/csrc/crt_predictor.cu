@@ -1,0 +1,728 @@
+// Learned hit predictor: an FP16 MLP on tcgen05 tensor cores that guesses,
+// per ray, which treelet (subtree of a fixed BVH cut) holds its closest hit.
+// The traversal tests that treelet exactly first and uses the hit to seed
+// t_max (crt_trace.cu), so a wrong guess costs time, never correctness.
+//
+// Network (per ray):
+//   features  origin cell on a 64^3 grid over the scene box -> 16 learned fp16
+//             values; direction in 32x32 octahedral bins -> 16 learned values
+//   MLP       32 -> 64 (ReLU) -> 64 (ReLU) -> 128 logits (127 treelets + miss)
+// Every layer is one CTA-wide tcgen05.mma chain over a 128-ray tile: fp16
+// operands in shared memory (K-major, no swizzle), FP32 accumulators in TMEM,
+// read back with tcgen05.ld for the bias/ReLU/softmax epilogues.  Training
+// runs the forward pass, the softmax cross-entropy gradient and the backward
+// GEMMs (weight and input gradients) on the tensor cores as well, sums the
+// gradients into FP32 buffers, and an Adam kernel updates FP32 master
+// weights and refreshes the fp16 copies (and the transposed copies the
+// backward GEMMs read).
+#include <cmath>
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "crt_build.cuh"
+#include "crt_common.cuh"
+#include "crt_predictor.cuh"
+#include "crt_tc.cuh"
+
+namespace crt {
+namespace pred {
+
+using tc::kmajor_offset;
+
+// ------------------------------------------------------------ features
+struct SceneFrame {
+    float mnx, mny, mnz, sx, sy, sz;  // cell = (o - mn) * s
+};
+
+__device__ __forceinline__ SceneFrame scene_frame(const crt_bvh_node* nodes) {
+    const float4 mn = __ldg(reinterpret_cast<const float4*>(nodes));
+    const float4 mx = __ldg(reinterpret_cast<const float4*>(nodes) + 1);
+    SceneFrame f;
+    f.mnx = mn.x; f.mny = mn.y; f.mnz = mn.z;
+    const float ex = fmaxf(mx.x - mn.x, 1e-20f), ey = fmaxf(mx.y - mn.y, 1e-20f), ez = fmaxf(mx.z - mn.z, 1e-20f);
+    f.sx = kGrid / ex; f.sy = kGrid / ey; f.sz = kGrid / ez;
+    return f;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ void ray_keys(const float4 r0, const float4 r1, const SceneFrame& f, uint32_t& cell,
+                                         uint32_t& bin) {
+    const int cx = clampi(static_cast<int>(floorf((r0.x - f.mnx) * f.sx)), 0, kGrid - 1);
+    const int cy = clampi(static_cast<int>(floorf((r0.y - f.mny) * f.sy)), 0, kGrid - 1);
+    const int cz = clampi(static_cast<int>(floorf((r0.z - f.mnz) * f.sz)), 0, kGrid - 1);
+    cell = (static_cast<uint32_t>(cx) * kGrid + cy) * kGrid + cz;
+    // octahedral map of the direction to [-1, 1]^2
+    const float s = fabsf(r1.x) + fabsf(r1.y) + fabsf(r1.z);
+    float px = s > 0.f ? r1.x / s : 0.f, py = s > 0.f ? r1.y / s : 0.f;
+    if (r1.z < 0.f) {
+        const float qx = (1.f - fabsf(py)) * (px >= 0.f ? 1.f : -1.f);
+        const float qy = (1.f - fabsf(px)) * (py >= 0.f ? 1.f : -1.f);
+        px = qx; py = qy;
+    }
+    const int bu = clampi(static_cast<int>((px + 1.f) * (0.5f * kDirBins)), 0, kDirBins - 1);
+    const int bv = clampi(static_cast<int>((py + 1.f) * (0.5f * kDirBins)), 0, kDirBins - 1);
+    bin = static_cast<uint32_t>(bu) * kDirBins + bv;
+}
+
+// ---------------------------------------------------- smem tile helpers
+// Copy a row-major fp16 matrix (rows x cols) into the K-major core layout.
+__device__ __forceinline__ void load_kmajor(unsigned char* dst, const __half* src, int rows, int cols) {
+    for (int i = threadIdx.x; i < rows * cols / 8; i += blockDim.x) {
+        const int r = (i * 8) / cols, k = (i * 8) % cols;
+        *reinterpret_cast<uint4*>(dst + kmajor_offset(r, k, cols)) = __ldg(reinterpret_cast<const uint4*>(src) + i);
+    }
+}
+
+__device__ __forceinline__ void zero_bytes(unsigned char* dst, int bytes) {
+    for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) reinterpret_cast<uint4*>(dst)[i] = make_uint4(0, 0, 0, 0);
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Row `row` of a K-major tile with Kd columns, 8 values starting at column k (k % 8 == 0).
+__device__ __forceinline__ void store_row8(unsigned char* tile, int Kd, int row, int k, const float* v) {
+    uint4 q;
+    q.x = pack2(v[0], v[1]); q.y = pack2(v[2], v[3]); q.z = pack2(v[4], v[5]); q.w = pack2(v[6], v[7]);
+    *reinterpret_cast<uint4*>(tile + kmajor_offset(row, k, Kd)) = q;
+}
+
+__device__ __forceinline__ void store_h(unsigned char* tile, int Kd, int row, int k, float v) {
+    *reinterpret_cast<__half*>(tile + kmajor_offset(row, k, Kd)) = __float2half_rn(v);
+}
+
+__device__ __forceinline__ float load_h(const unsigned char* tile, int Kd, int row, int k) {
+    return __half2float(*reinterpret_cast<const __half*>(tile + kmajor_offset(row, k, Kd)));
+}
+
+// Issue D = A * B^T over Kd columns (Kd / 16 MMAs) from one thread.
+__device__ __forceinline__ void gemm(uint32_t d_tmem, const unsigned char* A, const unsigned char* B, int Kd, int M,
+                                     int N) {
+    const uint32_t sbo = static_cast<uint32_t>(Kd / 8) * 128u;
+    const uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(B);
+    const uint32_t id = tc::idesc_f16_f32(M, N);
+    for (int kk = 0; kk < Kd / 16; ++kk)
+        tc::mma_f16(d_tmem, tc::smem_desc(a0 + kk * 256, tc::kLbo, sbo), tc::smem_desc(b0 + kk * 256, tc::kLbo, sbo),
+                    id, kk > 0);
+}
+
+struct Sync {
+    uint64_t* mbar;
+    uint32_t phase = 0;
+    uint32_t* err;
+    // Publish generic smem writes to the tensor core and order tcgen05 work.
+    __device__ __forceinline__ void before_mma() {
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    }
+    __device__ __forceinline__ void commit_and_wait() {
+        if (threadIdx.x == 0) tc::mma_commit(mbar);
+        if (!tc::mbar_wait(mbar, phase, 1u << 26)) raise_error(err, kDevTimeout);
+        phase ^= 1u;
+        tc::fence_after_sync();
+    }
+};
+
+__device__ __forceinline__ uint32_t lane_addr(uint32_t tbase, uint32_t col) {
+    const uint32_t warp = threadIdx.x >> 5;
+    return tbase + ((32u * warp) << 16) + col;
+}
+
+// ---------------------------------------------------------- inference
+// Persistent: each CTA (128 threads, one ray per thread) loads the weights
+// once and walks 128-ray tiles.  TMEM: D1 cols 0-63, D2 64-127, logits 128-255.
+constexpr int kInferSmemUsed = 64 * 32 * 2 + 64 * 64 * 2 + 128 * 64 * 2 + 128 * 32 * 2 + 2 * 128 * 64 * 2 +
+                               (64 + 64 + 128) * 4 + 64;
+// Requested size caps residency at two CTAs per SM, the number whose
+// 256-column TMEM allocations fit the SM's 512 columns together.
+constexpr int kInferSmem = 100 * 1024;
+static_assert(kInferSmemUsed <= kInferSmem, "inference tile layout");
+
+__global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bvh_node* nodes, const crt_ray* rays,
+                                                    uint32_t n, uint16_t* classes, float miss_threshold, uint32_t* err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sW1 = smem;
+    unsigned char* sW2 = sW1 + 64 * 32 * 2;
+    unsigned char* sW3 = sW2 + 64 * 64 * 2;
+    unsigned char* sX = sW3 + 128 * 64 * 2;
+    unsigned char* sH1 = sX + 128 * 32 * 2;
+    unsigned char* sH2 = sH1 + 128 * 64 * 2;
+    float* sB = reinterpret_cast<float*>(sH2 + 128 * 64 * 2);
+    uint32_t* sT = reinterpret_cast<uint32_t*>(sB + 256);
+    uint64_t* sM = reinterpret_cast<uint64_t*>(sT + 2);
+
+    load_kmajor(sW1, P.w16 + hW1, 64, 32);
+    load_kmajor(sW2, P.w16 + hW2, 64, 64);
+    load_kmajor(sW3, P.w16 + hW3, 128, 64);
+    for (int i = threadIdx.x; i < 256; i += 128) {
+        const float b = i < 64 ? P.master[oB1 + i] : (i < 128 ? P.master[oB2 + i - 64] : P.master[oB3 + i - 128]);
+        sB[i] = b;
+    }
+    if (threadIdx.x < 32) { tc::tmem_alloc(sT, 256); tc::tmem_relinquish(); }
+    if (threadIdx.x == 0) tc::mbar_init(sM, 1);
+    Sync sy{sM, 0, err};
+    sy.before_mma();
+    const uint32_t tb = *sT;
+    const SceneFrame fr = scene_frame(nodes);
+    const int tid = threadIdx.x;
+
+    for (uint32_t tile = blockIdx.x; static_cast<uint64_t>(tile) * 128 < n; tile += gridDim.x) {
+        const uint32_t i = tile * 128 + tid;
+        const bool valid = i < n;
+        uint4 e[4] = {};
+        if (valid) {
+            const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
+            const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+            uint32_t cell, bin;
+            ray_keys(r0, r1, fr, cell, bin);
+            const uint4* eo = reinterpret_cast<const uint4*>(P.w16 + hEo + static_cast<size_t>(cell) * kEmb);
+            const uint4* ed = reinterpret_cast<const uint4*>(P.w16 + hEd + static_cast<size_t>(bin) * kEmb);
+            e[0] = __ldg(eo); e[1] = __ldg(eo + 1); e[2] = __ldg(ed); e[3] = __ldg(ed + 1);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4*>(sX + kmajor_offset(tid, 8 * c, 32)) = e[c];
+        sy.before_mma();
+        if (tid == 0) gemm(tb + 0, sX, sW1, 32, 128, 64);
+        sy.commit_and_wait();
+        for (int c = 0; c < 64; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + sB[c + j], 0.f);
+            store_row8(sH1, 64, tid, c, v);
+            store_row8(sH1, 64, tid, c + 8, v + 8);
+        }
+        sy.before_mma();
+        if (tid == 0) gemm(tb + 64, sH1, sW2, 64, 128, 64);
+        sy.commit_and_wait();
+        for (int c = 0; c < 64; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 64 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + sB[64 + c + j], 0.f);
+            store_row8(sH2, 64, tid, c, v);
+            store_row8(sH2, 64, tid, c + 8, v + 8);
+        }
+        sy.before_mma();
+        if (tid == 0) gemm(tb + 128, sH2, sW3, 64, 128, 128);
+        sy.commit_and_wait();
+        // Seed the most likely treelet unless the miss class holds at least
+        // `miss_threshold` of the probability mass.
+        float best = -INFINITY, lmax = -INFINITY, lmiss = 0.f;
+        int bc = 0;
+        for (int c = 0; c < 128; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float l = v[j] + sB[128 + c + j];
+                lmax = fmaxf(lmax, l);
+                if (c + j == kMissClass) lmiss = l;
+                else if (l > best) { best = l; bc = c + j; }
+            }
+        }
+        float sum = 0.f;
+        for (int c = 0; c < 128; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - lmax);
+        }
+        const float p_miss = __expf(lmiss - lmax) / sum;
+        if (valid) classes[i] = static_cast<uint16_t>(p_miss >= miss_threshold ? kMissClass : bc);
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_dealloc(tb, 256);
+}
+
+// ------------------------------------------------------------ training
+// One 128-sample tile per CTA: forward, softmax cross-entropy gradient
+// (p - onehot, unscaled; the optimiser divides by the sample count), backward
+// GEMMs, FP32 atomics into the gradient buffers.  Shared memory:
+//   weights  W1 W1T W2 W2T W3 W3T                       56 KB
+//   acts     X XT H1 H1T H2 H2T                         80 KB
+//   grads    G3 G3T, then G2 G2T(padded to 128 rows),
+//            then G1 G1T(padded)                       64 KB
+// TMEM (256 cols): D1 0-63, D2 64-127, logits 128-255; then dW3 0-63,
+// dH2 64-127; dW2 128-191, dH1 192-255; dW1 0-31, dX 32-63.
+constexpr int kTrainSmem = 56 * 1024 + 80 * 1024 + 64 * 1024 + 256 * 4 + 64;
+
+__global__ void __launch_bounds__(128) train_kernel(PredictorDev P, const crt_bvh_node* nodes, const crt_ray* rays,
+                                                    uint32_t n_rays, const crt_hit* hits, const uint16_t* targets,
+                                                    uint32_t n_samples, uint32_t stride, uint32_t offset,
+                                                    float* grad, float* loss_sum, uint32_t* err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sW1 = smem;
+    unsigned char* sW1T = sW1 + 4096;
+    unsigned char* sW2 = sW1T + 4096;
+    unsigned char* sW2T = sW2 + 8192;
+    unsigned char* sW3 = sW2T + 8192;
+    unsigned char* sW3T = sW3 + 16384;
+    unsigned char* sX = sW3T + 16384;
+    unsigned char* sXT = sX + 8192;
+    unsigned char* sH1 = sXT + 8192;
+    unsigned char* sH1T = sH1 + 16384;
+    unsigned char* sH2 = sH1T + 16384;
+    unsigned char* sH2T = sH2 + 16384;
+    unsigned char* sGA = sH2T + 16384;
+    float* sB = reinterpret_cast<float*>(sGA + 65536);
+    uint32_t* sT = reinterpret_cast<uint32_t*>(sB + 256);
+    uint64_t* sM = reinterpret_cast<uint64_t*>(sT + 2);
+    unsigned char* sG3 = sGA;
+    unsigned char* sG3T = sGA + 32768;
+    unsigned char* sG = sGA;            // G2 / G1: 128 x 64
+    unsigned char* sGT = sGA + 16384;   // G2T / G1T padded: 128 x 128
+
+    load_kmajor(sW1, P.w16 + hW1, 64, 32);
+    load_kmajor(sW1T, P.w16 + hW1T, 32, 64);
+    load_kmajor(sW2, P.w16 + hW2, 64, 64);
+    load_kmajor(sW2T, P.w16 + hW2T, 64, 64);
+    load_kmajor(sW3, P.w16 + hW3, 128, 64);
+    load_kmajor(sW3T, P.w16 + hW3T, 64, 128);
+    for (int i = threadIdx.x; i < 256; i += 128)
+        sB[i] = i < 64 ? P.master[oB1 + i] : (i < 128 ? P.master[oB2 + i - 64] : P.master[oB3 + i - 128]);
+    if (threadIdx.x < 32) { tc::tmem_alloc(sT, 256); tc::tmem_relinquish(); }
+    if (threadIdx.x == 0) tc::mbar_init(sM, 1);
+    const int tid = threadIdx.x;
+    const uint32_t s = blockIdx.x * 128 + tid;
+    const uint64_t ri = static_cast<uint64_t>(s) * stride + offset;
+    const bool valid = s < n_samples && ri < n_rays;
+    uint32_t cell = 0, bin = 0;
+    int target = -1;
+    uint4 e[4] = {};
+    if (valid) {
+        const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + ri));
+        const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + ri) + 1);
+        ray_keys(r0, r1, scene_frame(nodes), cell, bin);
+        const uint4* eo = reinterpret_cast<const uint4*>(P.w16 + hEo + static_cast<size_t>(cell) * kEmb);
+        const uint4* ed = reinterpret_cast<const uint4*>(P.w16 + hEd + static_cast<size_t>(bin) * kEmb);
+        e[0] = __ldg(eo); e[1] = __ldg(eo + 1); e[2] = __ldg(ed); e[3] = __ldg(ed + 1);
+        if (targets) {
+            target = targets[ri];
+        } else {
+            const uint32_t tri = __ldg(reinterpret_cast<const uint32_t*>(hits + ri));
+            target = (tri == CRT_MISS || tri >= P.n_tris) ? kMissClass : P.tri_class[tri];
+        }
+        if (target < 0 || target >= kClasses) target = kMissClass;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        *reinterpret_cast<uint4*>(sX + kmajor_offset(tid, 8 * c, 32)) = e[c];
+        const __half* hv = reinterpret_cast<const __half*>(&e[c]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            *reinterpret_cast<__half*>(sXT + kmajor_offset(8 * c + j, tid, 128)) = hv[j];
+    }
+    Sync sy{sM, 0, err};
+    sy.before_mma();
+    const uint32_t tb = *sT;
+
+    // ---- forward
+    if (tid == 0) gemm(tb + 0, sX, sW1, 32, 128, 64);
+    sy.commit_and_wait();
+    for (int c = 0; c < 64; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, c), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            v[j] = __half2float(__float2half_rn(fmaxf(v[j] + sB[c + j], 0.f)));
+            store_h(sH1T, 128, c + j, tid, v[j]);
+        }
+        store_row8(sH1, 64, tid, c, v);
+        store_row8(sH1, 64, tid, c + 8, v + 8);
+    }
+    sy.before_mma();
+    if (tid == 0) gemm(tb + 64, sH1, sW2, 64, 128, 64);
+    sy.commit_and_wait();
+    for (int c = 0; c < 64; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 64 + c), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            v[j] = __half2float(__float2half_rn(fmaxf(v[j] + sB[64 + c + j], 0.f)));
+            store_h(sH2T, 128, c + j, tid, v[j]);
+        }
+        store_row8(sH2, 64, tid, c, v);
+        store_row8(sH2, 64, tid, c + 8, v + 8);
+    }
+    sy.before_mma();
+    if (tid == 0) gemm(tb + 128, sH2, sW3, 64, 128, 128);
+    sy.commit_and_wait();
+
+    // ---- softmax cross-entropy: G3 = p - onehot(target)
+    float mx = -INFINITY;
+    for (int c = 0; c < 128; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) mx = fmaxf(mx, v[j] + sB[128 + c + j]);
+    }
+    float sum = 0.f;
+    for (int c = 0; c < 128; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - mx);
+    }
+    const float inv = 1.f / sum;
+    for (int c = 0; c < 128; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float l = v[j] + sB[128 + c + j];
+            const float p = __expf(l - mx) * inv;
+            float g = p - ((c + j) == target ? 1.f : 0.f);
+            if (!valid) g = 0.f;
+            if (valid && (c + j) == target) atomicAdd(loss_sum, -(l - mx - __logf(sum)));
+            v[j] = __half2float(__float2half_rn(g));
+            store_h(sG3T, 128, c + j, tid, v[j]);
+        }
+        store_row8(sG3, 128, tid, c, v);
+        store_row8(sG3, 128, tid, c + 8, v + 8);
+    }
+    // ---- dW3 = G3^T H2 and dH2 = G3 W3
+    sy.before_mma();
+    if (tid == 0) {
+        gemm(tb + 0, sG3T, sH2T, 128, 128, 64);
+        gemm(tb + 64, sG3, sW3T, 128, 128, 64);
+    }
+    sy.commit_and_wait();
+    {
+        float acc = 0.f;  // db3[tid] = sum over samples of G3[:, tid]
+        for (int b = 0; b < 128; ++b) acc += load_h(sG3T, 128, tid, b);
+        atomicAdd(grad + oB3 + tid, acc);
+    }
+    for (int c = 0; c < 64; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, c), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) atomicAdd(grad + oW3 + tid * 64 + c + j, v[j]);
+    }
+    float dh[64];
+    for (int c = 0; c < 64; c += 16) tc::tmem_ld16(lane_addr(tb, 64 + c), dh + c);
+    tc::fence_before_sync();
+    __syncthreads();  // G3 / G3T fully consumed
+    zero_bytes(sGT + 64 * 128 * 2, 64 * 128 * 2);  // padding rows 64..127 of G2T
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+        dh[j] = (load_h(sH2, 64, tid, j) > 0.f) ? __half2float(__float2half_rn(dh[j])) : 0.f;
+        store_h(sGT, 128, j, tid, dh[j]);
+    }
+    for (int c = 0; c < 64; c += 8) store_row8(sG, 64, tid, c, dh + c);
+    // ---- dW2 = G2^T H1 and dH1 = G2 W2
+    sy.before_mma();
+    if (tid == 0) {
+        gemm(tb + 128, sGT, sH1T, 128, 128, 64);
+        gemm(tb + 192, sG, sW2T, 64, 128, 64);
+    }
+    sy.commit_and_wait();
+    if (tid < 64) {
+        float acc = 0.f;
+        for (int b = 0; b < 128; ++b) acc += load_h(sGT, 128, tid, b);
+        atomicAdd(grad + oB2 + tid, acc);
+    }
+    for (int c = 0; c < 64; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+        if (tid < 64) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) atomicAdd(grad + oW2 + tid * 64 + c + j, v[j]);
+        }
+    }
+    for (int c = 0; c < 64; c += 16) tc::tmem_ld16(lane_addr(tb, 192 + c), dh + c);
+    tc::fence_before_sync();
+    __syncthreads();
+    zero_bytes(sGT + 64 * 128 * 2, 64 * 128 * 2);
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+        dh[j] = (load_h(sH1, 64, tid, j) > 0.f) ? __half2float(__float2half_rn(dh[j])) : 0.f;
+        store_h(sGT, 128, j, tid, dh[j]);
+    }
+    for (int c = 0; c < 64; c += 8) store_row8(sG, 64, tid, c, dh + c);
+    // ---- dW1 = G1^T X and dX = G1 W1
+    sy.before_mma();
+    if (tid == 0) {
+        gemm(tb + 0, sGT, sXT, 128, 128, 32);
+        gemm(tb + 32, sG, sW1T, 64, 128, 32);
+    }
+    sy.commit_and_wait();
+    if (tid < 64) {
+        float acc = 0.f;
+        for (int b = 0; b < 128; ++b) acc += load_h(sGT, 128, tid, b);
+        atomicAdd(grad + oB1 + tid, acc);
+    }
+    for (int c = 0; c < 32; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, c), v);
+        if (tid < 64) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) atomicAdd(grad + oW1 + tid * 32 + c + j, v[j]);
+        }
+    }
+    for (int c = 0; c < 32; c += 16) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 32 + c), v);
+        if (valid) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int ee = c + j;
+                float* dst = ee < kEmb ? grad + oEo + static_cast<size_t>(cell) * kEmb + ee
+                                       : grad + oEd + static_cast<size_t>(bin) * kEmb + (ee - kEmb);
+                atomicAdd(dst, v[j]);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_dealloc(tb, 256);
+}
+
+// ------------------------------------------------------------ optimiser
+__global__ void adam_kernel(PredictorDev P, float* grad, float scale, float lr, float b1t, float b2t) {
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < kParams;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const float g = grad[i] * scale;
+        grad[i] = 0.f;
+        const float m = b1 * P.m[i] + (1.f - b1) * g;
+        const float v = b2 * P.v[i] + (1.f - b2) * g * g;
+        P.m[i] = m;
+        P.v[i] = v;
+        const float w = P.master[i] - lr * (m / b1t) / (sqrtf(v / b2t) + eps);
+        P.master[i] = w;
+    }
+}
+
+// fp16 copies of the master weights, plus the transposed copies.
+__global__ void convert_kernel(PredictorDev P) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < kParams;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const __half h = __float2half_rn(P.master[i]);
+        if (i < oB1) {                       // W1 [64][32]
+            P.w16[hW1 + i] = h;
+            const size_t r = i / 32, c = i % 32;
+            P.w16[hW1T + c * 64 + r] = h;
+        } else if (i >= oW2 && i < oB2) {    // W2 [64][64]
+            const size_t k = i - oW2, r = k / 64, c = k % 64;
+            P.w16[hW2 + k] = h;
+            P.w16[hW2T + c * 64 + r] = h;
+        } else if (i >= oW3 && i < oB3) {    // W3 [128][64]
+            const size_t k = i - oW3, r = k / 64, c = k % 64;
+            P.w16[hW3 + k] = h;
+            P.w16[hW3T + c * 128 + r] = h;
+        } else if (i >= oEo && i < oEd) {
+            P.w16[hEo + (i - oEo)] = h;
+        } else if (i >= oEd) {
+            P.w16[hEd + (i - oEd)] = h;
+        }
+    }
+}
+
+__device__ __forceinline__ float hash_uniform(uint64_t x) {  // SplitMix64 -> [0, 1)
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return static_cast<float>(x >> 40) * (1.0f / 16777216.0f);
+}
+
+// Kaiming-uniform weights, zero biases, embeddings U(-0.1, 0.1); zero moments.
+__global__ void init_kernel(PredictorDev P, uint32_t seed) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < kParams;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const float u = hash_uniform((static_cast<uint64_t>(seed) << 32) ^ i) * 2.f - 1.f;
+        float w = 0.f;
+        if (i < oB1) w = u * sqrtf(6.f / kIn);
+        else if (i >= oW2 && i < oB2) w = u * sqrtf(6.f / kHid);
+        else if (i >= oW3 && i < oB3) w = u * sqrtf(6.f / kHid);
+        else if (i >= oEo) w = 0.1f * u;
+        P.master[i] = w;
+        P.m[i] = 0.f;
+        P.v[i] = 0.f;
+        P.grad[i] = 0.f;
+    }
+}
+
+// ------------------------------------------------------------- treelets
+// Cut the BVH into at most kClasses-1 subtrees: starting from the root,
+// repeatedly split the frontier subtree with the most leaves (its children
+// come from the 64-byte traversal node).  Single thread; <= 127 splits.
+__global__ void treelet_cut_kernel(const crt_bvh_node* nodes, const float4* wide, uint32_t n_leaves, Treelet* out,
+                                   uint32_t* n_out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const float4 rmn = reinterpret_cast<const float4*>(nodes)[0];
+    const float4 rmx = reinterpret_cast<const float4*>(nodes)[1];
+    const uint4 lr = reinterpret_cast<const uint4*>(nodes)[2];
+    uint32_t cnt = 1;
+    out[0].mn[0] = rmn.x; out[0].mn[1] = rmn.y; out[0].mn[2] = rmn.z;
+    out[0].mx[0] = rmx.x; out[0].mx[1] = rmx.y; out[0].mx[2] = rmx.z;
+    out[0].ref = (lr.y == 0u && lr.z == 0u) ? kLeafRef : 0u;
+    out[0].first = 0;
+    out[0].count = n_leaves;
+    while (cnt < static_cast<uint32_t>(kMissClass)) {
+        int best = -1;
+        uint32_t bc = 1;
+        for (uint32_t k = 0; k < cnt; ++k)
+            if (!(out[k].ref & kLeafRef) && out[k].count > bc) { bc = out[k].count; best = static_cast<int>(k); }
+        if (best < 0) break;
+        const Treelet t = out[best];
+        const float4* w = wide + 4 * static_cast<size_t>(t.ref);
+        const float4 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
+        Treelet a, b;
+        a.mn[0] = w0.x; a.mn[1] = w0.y; a.mn[2] = w0.z; a.mx[0] = w1.x; a.mx[1] = w1.y; a.mx[2] = w1.z;
+        a.ref = __float_as_uint(w0.w); a.first = t.first; a.count = __float_as_uint(w2.w);
+        b.mn[0] = w2.x; b.mn[1] = w2.y; b.mn[2] = w2.z; b.mx[0] = w3.x; b.mx[1] = w3.y; b.mx[2] = w3.z;
+        b.ref = __float_as_uint(w1.w); b.first = t.first + a.count; b.count = __float_as_uint(w3.w);
+        out[best] = a;
+        out[cnt++] = b;
+    }
+    // sort by first leaf (insertion sort, <= 127 entries)
+    for (uint32_t k = 1; k < cnt; ++k) {
+        const Treelet t = out[k];
+        int j = static_cast<int>(k) - 1;
+        while (j >= 0 && out[j].first > t.first) { out[j + 1] = out[j]; --j; }
+        out[j + 1] = t;
+    }
+    *n_out = cnt;
+}
+
+// Class of every triangle: the treelet whose leaf range holds its leaf.
+__global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, const uint32_t* perm, uint32_t n_leaves,
+                                     uint8_t* tri_class) {
+    const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= n_leaves) return;
+    const uint32_t n = *n_tl;
+    int lo = 0, hi = static_cast<int>(n) - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (tl[mid].first <= L) lo = mid; else hi = mid - 1;
+    }
+    const uint32_t tri = perm[L];
+    if (tri < n_leaves) tri_class[tri] = static_cast<uint8_t>(lo);
+}
+
+// ------------------------------------------------------------ bounce rays
+// Cosine-weighted diffuse bounce rays from primary hits (incoherent: ray j
+// starts from the first hit at or after a scrambled primary index).
+__global__ void bounce_kernel(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
+                              const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_out) return;
+    float4* o = reinterpret_cast<float4*>(out + j);
+    uint32_t s = static_cast<uint32_t>((static_cast<uint64_t>(j) * 2654435761ull + seed) % n_prim);
+    uint32_t tri = CRT_MISS;
+    for (uint32_t probe = 0; probe < 4096; ++probe) {
+        tri = hits[s].tri;
+        if (tri != CRT_MISS && tri < n_tris) break;
+        tri = CRT_MISS;
+        s = (s + 1 == n_prim) ? 0u : s + 1;
+    }
+    if (tri == CRT_MISS) {
+        o[0] = make_float4(0.f, 0.f, 0.f, 1.f);
+        o[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float t = hits[s].t;
+    const float4 r0 = reinterpret_cast<const float4*>(prim + s)[0], r1 = reinterpret_cast<const float4*>(prim + s)[1];
+    const float px = r0.x + t * r1.x, py = r0.y + t * r1.y, pz = r0.z + t * r1.z;
+    const uint32_t L = inv_perm[tri];
+    const float4 a = xtri[3 * static_cast<size_t>(L)], b = xtri[3 * static_cast<size_t>(L) + 1],
+                 c = xtri[3 * static_cast<size_t>(L) + 2];
+    float nx = (b.y - a.y) * (c.z - a.z) - (b.z - a.z) * (c.y - a.y);
+    float ny = (b.z - a.z) * (c.x - a.x) - (b.x - a.x) * (c.z - a.z);
+    float nz = (b.x - a.x) * (c.y - a.y) - (b.y - a.y) * (c.x - a.x);
+    const float nl = rsqrtf(fmaxf(nx * nx + ny * ny + nz * nz, 1e-30f));
+    nx *= nl; ny *= nl; nz *= nl;
+    if (nx * r1.x + ny * r1.y + nz * r1.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
+    // orthonormal basis (Duff et al. 2017)
+    const float sg = nz >= 0.f ? 1.f : -1.f;
+    const float aa = -1.f / (sg + nz), bb = nx * ny * aa;
+    const float tx = 1.f + sg * nx * nx * aa, ty = sg * bb, tz = -sg * nx;
+    const float bx = bb, by = sg + ny * ny * aa, bz = -ny;
+    const float u1 = hash_uniform((static_cast<uint64_t>(seed) << 33) ^ (2ull * j));
+    const float u2 = hash_uniform((static_cast<uint64_t>(seed) << 33) ^ (2ull * j + 1));
+    const float r = sqrtf(u1), phi = 6.28318530718f * u2;
+    const float lx = r * __cosf(phi), ly = r * __sinf(phi), lz = sqrtf(fmaxf(1.f - u1, 0.f));
+    float dx = lx * tx + ly * bx + lz * nx, dy = lx * ty + ly * by + lz * ny, dz = lx * tz + ly * bz + lz * nz;
+    const float dl = rsqrtf(dx * dx + dy * dy + dz * dz);
+    o[0] = make_float4(px, py, pz, 1e-4f);
+    o[1] = make_float4(dx * dl, dy * dl, dz * dl, __int_as_float(0x7F800000));
+}
+
+}  // namespace pred
+
+// ------------------------------------------------------------ launchers
+void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s) {
+    pred::init_kernel<<<kNumSms * 8, 256, 0, s>>>(P, seed);
+    pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
+}
+
+cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
+                       uint16_t* classes, float miss_threshold, uint32_t* err, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(pred::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             pred::kInferSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint32_t tiles = (n + 127) / 128;
+    const uint32_t grid = tiles < 2u * kNumSms ? tiles : 2u * kNumSms;
+    if (grid == 0) return cudaSuccess;
+    pred::infer_kernel<<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold, err);
+    return cudaGetLastError();
+}
+
+cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n_rays,
+                            const crt_hit* hits, const uint16_t* targets, uint32_t n_samples, uint32_t stride,
+                            uint32_t offset, float* loss_sum, uint32_t* err, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(pred::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             pred::kTrainSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint32_t grid = (n_samples + 127) / 128;
+    if (grid == 0) return cudaSuccess;
+    pred::train_kernel<<<grid, 128, pred::kTrainSmem, s>>>(P, nodes, rays, n_rays, hits, targets, n_samples, stride,
+                                                          offset, P.grad, loss_sum, err);
+    return cudaGetLastError();
+}
+
+void pred_adam(const PredictorDev& P, float scale, float lr, uint32_t step, cudaStream_t s) {
+    const float b1t = 1.f - std::pow(0.9f, static_cast<float>(step));
+    const float b2t = 1.f - std::pow(0.999f, static_cast<float>(step));
+    pred::adam_kernel<<<kNumSms * 8, 256, 0, s>>>(P, P.grad, scale, lr, b1t, b2t);
+    pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
+}
+
+void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s) {
+    pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
+}
+
+void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t* perm, uint32_t n_leaves,
+                   Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s) {
+    pred::treelet_cut_kernel<<<1, 1, 0, s>>>(nodes, wide, n_leaves, tl, n_tl);
+    pred::treelet_label_kernel<<<(n_leaves + 255) / 256, 256, 0, s>>>(tl, n_tl, perm, n_leaves, tri_class);
+}
+
+void launch_bounce(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
+                   const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out,
+                   cudaStream_t s) {
+    if (n_out == 0 || n_prim == 0) return;
+    pred::bounce_kernel<<<(n_out + 255) / 256, 256, 0, s>>>(prim, hits, n_prim, xtri, inv_perm, n_tris, n_out, seed,
+                                                           out);
+}
+
+}  // namespace crt

@@ -1,0 +1,85 @@
+// Learned hit predictor: parameter layout and the device view shared by the
+// predictor kernels (crt_predictor.cu), the seeded traversal (crt_trace.cu)
+// and the C ABI (crt_api.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "crt.h"
+
+namespace crt {
+namespace pred {
+
+constexpr int kIn = 32;            // input features: 16 origin-cell + 16 direction-bin embedding values
+constexpr int kHid = 64;           // hidden width
+constexpr int kClasses = 128;      // 127 treelets + "miss"
+constexpr int kMissClass = kClasses - 1;
+constexpr int kGrid = 64;          // origin cells per axis
+constexpr int kDirBins = 32;       // octahedral direction bins per axis
+constexpr int kEmb = 16;           // embedding width per table
+constexpr size_t kEo = static_cast<size_t>(kGrid) * kGrid * kGrid;
+constexpr size_t kEd = static_cast<size_t>(kDirBins) * kDirBins;
+
+// FP32 master parameters (and Adam moments, gradients) in one flat array.
+constexpr size_t oW1 = 0;                        // [64][32]  (out, in)
+constexpr size_t oB1 = oW1 + kHid * kIn;         // [64]
+constexpr size_t oW2 = oB1 + kHid;               // [64][64]
+constexpr size_t oB2 = oW2 + kHid * kHid;        // [64]
+constexpr size_t oW3 = oB2 + kHid;               // [128][64]
+constexpr size_t oB3 = oW3 + kClasses * kHid;    // [128]
+constexpr size_t oEo = oB3 + kClasses;           // [64^3][16]
+constexpr size_t oEd = oEo + kEo * kEmb;         // [32*32][16]
+constexpr size_t kParams = oEd + kEd * kEmb;
+
+// fp16 copies read by the kernels (row-major), incl. transposes for backward.
+constexpr size_t hW1 = 0;                        // [64][32]
+constexpr size_t hW2 = hW1 + kHid * kIn;         // [64][64]
+constexpr size_t hW3 = hW2 + kHid * kHid;        // [128][64]
+constexpr size_t hW1T = hW3 + kClasses * kHid;   // [32][64]
+constexpr size_t hW2T = hW1T + kIn * kHid;       // [64][64]
+constexpr size_t hW3T = hW2T + kHid * kHid;      // [64][128]
+constexpr size_t hEo = hW3T + kHid * kClasses;   // [64^3][16]
+constexpr size_t hEd = hEo + kEo * kEmb;         // [1024][16]
+constexpr size_t kHalfs = hEd + kEd * kEmb;
+
+}  // namespace pred
+
+struct PredictorDev {
+    float* master = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;
+    __half* w16 = nullptr;
+    const uint8_t* tri_class = nullptr;   // triangle id -> treelet class
+    uint32_t n_tris = 0;
+};
+
+// A subtree of the BVH cut: its box, traversal reference and leaf range.
+struct Treelet {
+    float mn[3];
+    uint32_t ref;
+    float mx[3];
+    uint32_t first;
+    uint32_t count;
+    uint32_t pad[3];
+};
+static_assert(sizeof(Treelet) == 48, "treelet record");
+
+void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s);
+cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
+                       uint16_t* classes, float miss_threshold, uint32_t* err, cudaStream_t s);
+cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n_rays,
+                            const crt_hit* hits, const uint16_t* targets, uint32_t n_samples, uint32_t stride,
+                            uint32_t offset, float* loss_sum, uint32_t* err, cudaStream_t s);
+void pred_adam(const PredictorDev& P, float scale, float lr, uint32_t step, cudaStream_t s);
+void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s);
+void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t* perm, uint32_t n_leaves,
+                   Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
+void launch_bounce(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
+                   const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out,
+                   cudaStream_t s);
+
+}  // namespace crt

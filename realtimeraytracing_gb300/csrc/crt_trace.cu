@@ -149,7 +149,7 @@ __device__ __forceinline__ float prune_bound(float t, float abs_eps) {
     return t + (fabsf(t) * 6.103515625e-05f + abs_eps);  // 2^-14 relative
 }
 
-template <bool ANY, bool WT, int STACK>
+template <bool ANY, bool WT, int STACK, bool SEED>
 __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n_rays) return;
@@ -198,58 +198,81 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
 
     uint32_t st_node[STACK];
     float st_t[STACK];
-    int sp = 0;
-    uint32_t cur = 0xFFFFFFFFu;
-    {  // root box (reference record 0)
-        const float4* n4 = reinterpret_cast<const float4*>(p.nodes);
-        const float4 mn = __ldg(n4), mx = __ldg(n4 + 1);
-        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(n4 + 2));
+    // Depth-first walk below internal node `cur` (children box-tested at
+    // their parent, leaves tested at once, nearer child entered directly).
+    // `skip` names a subtree already searched exactly (the seeded treelet).
+    auto walk = [&](uint32_t cur, uint32_t skip) {
+        int sp = 0;
+        while (cur != 0xFFFFFFFFu) {
+            if (cur >= n_leaves - 1) { corrupt = true; break; }
+            ++fetched;
+            const float4* nd = p.wide + 4 * static_cast<size_t>(cur);
+            const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
+            const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
+            float t0, t1;
+            bool h0 = ref0 != skip && slab(r, w0, w1, grow, t0);
+            bool h1 = ref1 != skip && slab(r, w2, w3, grow, t1);
+            const float bnd = prune_bound(bt, p.abs_eps);
+            h0 = h0 && t0 <= bnd;
+            h1 = h1 && t1 <= bnd;
+            if (h0 && (ref0 & kLeafRef)) { test_leaf(ref0 & ~kLeafRef); h0 = false; }
+            if (h1 && (ref1 & kLeafRef)) { test_leaf(ref1 & ~kLeafRef); h1 = false; }
+            if (ANY && have) break;
+            if (h0 || h1) {
+                const float bnd2 = prune_bound(bt, p.abs_eps);
+                h0 = h0 && t0 <= bnd2;
+                h1 = h1 && t1 <= bnd2;
+            }
+            if (h0 && h1) {
+                const bool near1 = t1 < t0;
+                if (sp < STACK) {
+                    st_node[sp] = near1 ? ref0 : ref1;
+                    st_t[sp] = near1 ? t0 : t1;
+                    ++sp;
+                } else {
+                    overflow = true;
+                }
+                cur = near1 ? ref1 : ref0;
+                continue;
+            }
+            if (h0) { cur = ref0; continue; }
+            if (h1) { cur = ref1; continue; }
+            cur = 0xFFFFFFFFu;
+            const float bnd3 = prune_bound(bt, p.abs_eps);
+            while (sp > 0) {
+                --sp;
+                if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
+            }
+        }
+    };
+    // Enter a subtree whose box (mn, mx) and reference are known.
+    auto enter = [&](float4 mn, float4 mx, uint32_t ref, uint32_t skip) {
         float te;
-        if (slab(r, mn, mx, grow, te) && te <= prune_bound(bt, p.abs_eps)) {
-            if (lr.y == 0u && lr.z == 0u) test_leaf(0u);
-            else cur = 0u;
+        if (ref == skip || !slab(r, mn, mx, grow, te) || te > prune_bound(bt, p.abs_eps)) return;
+        if (ref & kLeafRef) test_leaf(ref & ~kLeafRef);
+        else walk(ref, skip);
+    };
+    constexpr uint32_t kNoSkip = 0xFFFFFFFFu;  // never a reference: leaf indices stay below 2^30
+    uint32_t skip = kNoSkip;
+
+    if (SEED) {
+        // Learned seeding: the predicted treelet first (an exact search of
+        // that subtree), so t_max starts at a real hit distance; the full
+        // walk below then finds the same closest hit with less work.
+        const uint32_t k = p.pred_class[i];
+        // The full walk then leaves that treelet out: its closest hit is
+        // already known exactly.
+        if (k < __ldg(p.n_treelets)) {
+            const Treelet* T = p.treelets + k;
+            const float4 a = __ldg(reinterpret_cast<const float4*>(T)), b = __ldg(reinterpret_cast<const float4*>(T) + 1);
+            enter(a, b, __float_as_uint(a.w), kNoSkip);
+            skip = __float_as_uint(a.w);
         }
     }
-    while (cur != 0xFFFFFFFFu) {
-        if (cur >= n_leaves - 1) { corrupt = true; break; }
-        ++fetched;
-        const float4* nd = p.wide + 4 * static_cast<size_t>(cur);
-        const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
-        const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
-        float t0, t1;
-        bool h0 = slab(r, w0, w1, grow, t0);
-        bool h1 = slab(r, w2, w3, grow, t1);
-        const float bnd = prune_bound(bt, p.abs_eps);
-        h0 = h0 && t0 <= bnd;
-        h1 = h1 && t1 <= bnd;
-        if (h0 && (ref0 & kLeafRef)) { test_leaf(ref0 & ~kLeafRef); h0 = false; }
-        if (h1 && (ref1 & kLeafRef)) { test_leaf(ref1 & ~kLeafRef); h1 = false; }
-        if (ANY && have) break;
-        if (h0 || h1) {
-            const float bnd2 = prune_bound(bt, p.abs_eps);
-            h0 = h0 && t0 <= bnd2;
-            h1 = h1 && t1 <= bnd2;
-        }
-        if (h0 && h1) {
-            const bool near1 = t1 < t0;
-            if (sp < STACK) {
-                st_node[sp] = near1 ? ref0 : ref1;
-                st_t[sp] = near1 ? t0 : t1;
-                ++sp;
-            } else {
-                overflow = true;
-            }
-            cur = near1 ? ref1 : ref0;
-            continue;
-        }
-        if (h0) { cur = ref0; continue; }
-        if (h1) { cur = ref1; continue; }
-        cur = 0xFFFFFFFFu;
-        const float bnd3 = prune_bound(bt, p.abs_eps);
-        while (sp > 0) {
-            --sp;
-            if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
-        }
+    if (!(ANY && have)) {
+        const float4* n4 = reinterpret_cast<const float4*>(p.nodes);
+        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(n4 + 2));
+        enter(__ldg(n4), __ldg(n4 + 1), (lr.y == 0u && lr.z == 0u) ? kLeafRef : 0u, skip);
     }
     if (have) out = make_uint4(btri, __float_as_uint(bt), __float_as_uint(bu), __float_as_uint(bv));
     reinterpret_cast<uint4*>(p.hits)[i] = out;
@@ -303,20 +326,26 @@ __global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__
 }
 
 template <bool ANY, bool WT>
-static void launch_trace_t(const TraceParams& p, int block, bool deep, cudaStream_t s) {
+static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, cudaStream_t s) {
     const uint32_t grid = (p.n_rays + block - 1) / block;
     if (grid == 0) return;
-    if (deep) trace_kernel<ANY, WT, 1024><<<grid, block, 0, s>>>(p);
-    else trace_kernel<ANY, WT, 64><<<grid, block, 0, s>>>(p);
+    if (seed) {
+        if (deep) trace_kernel<ANY, WT, 1024, true><<<grid, block, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, true><<<grid, block, 0, s>>>(p);
+    } else {
+        if (deep) trace_kernel<ANY, WT, 1024, false><<<grid, block, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, false><<<grid, block, 0, s>>>(p);
+    }
 }
 
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s) {
     const bool any = flags & CRT_TRACE_ANY, wt = flags & CRT_TRI_WATERTIGHT;
     const bool deep = (flags >> 16) != 0;  // set by the host when the tree may be deeper than 63
-    if (any && wt) launch_trace_t<true, true>(p, block, deep, s);
-    else if (any) launch_trace_t<true, false>(p, block, deep, s);
-    else if (wt) launch_trace_t<false, true>(p, block, deep, s);
-    else launch_trace_t<false, false>(p, block, deep, s);
+    const bool seed = p.pred_class != nullptr;
+    if (any && wt) launch_trace_t<true, true>(p, block, deep, seed, s);
+    else if (any) launch_trace_t<true, false>(p, block, deep, seed, s);
+    else if (wt) launch_trace_t<false, true>(p, block, deep, seed, s);
+    else launch_trace_t<false, false>(p, block, deep, seed, s);
 }
 
 void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s) {
