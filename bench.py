@@ -253,6 +253,11 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(tris, models, cam)
+    predictor = None
+    if rank == 0 and not args.no_predictor:
+        del d_tris, bvh
+        torch.cuda.empty_cache()
+        predictor = run_predictor_experiment(ctx, torch, crt, dev, stream, args)
 
     if rank == 0:
         line = {
@@ -288,10 +293,99 @@ def run_ours(args):
                          "node_fetches_per_ray": round(visited / n_rays, 2), "tris_per_ray": round(tested / n_rays, 2)},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "predictor": predictor,
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
+    """Learned hit predictor vs plain traversal on the incoherent-bounce
+    workload: 4,194,304-triangle clustered soup (256 Gaussian clusters,
+    sigma 0.02, edges lognormal(ln 0.003, 0.6)), 2048x2048 primary rays from
+    (0.5, 0.5, -1.5) toward +z, 8,388,608 cosine-weighted bounce rays from
+    their first hits.  The network trains online on every 20th traced ray
+    (5%) for `passes` passes, then plain and seeded traversal are timed on
+    the same rays; the hits must be identical."""
+    from realtimeraytracing_gb300 import scenes as S
+    tris, models = S.config3_scene(seed=0)
+    d_tris = torch.from_numpy(tris).to(dev)
+    bvh = ctx.build(d_tris, models=torch.from_numpy(models).to(dev))
+    build_ms = ctx.last_build_stats()["ms_total"]
+    del d_tris
+    cam = torch.from_numpy(S.camera_gpu_data((0.5, 0.5, -1.5))).to(dev)
+    w = 2048
+    prim = torch.empty((w * w, 8), dtype=torch.float32, device=dev)
+    ctx.raygen(cam, w, w, out=prim)
+    ph = torch.empty((w * w, 4), dtype=torch.float32, device=dev)
+    ctx.trace(bvh, prim, crt.TRI_WATERTIGHT, out=ph)
+    n = 8 * 1024 * 1024
+    rays = torch.empty((n, 8), dtype=torch.float32, device=dev)
+    ctx.bounce_rays(bvh, prim, ph, n, seed=11, out=rays)
+    del prim, ph
+    plain = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    seeded = torch.empty_like(plain)
+    cls = torch.empty((n,), dtype=torch.int16, device=dev)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        with torch.cuda.stream(stream):
+            for a, b in evs:
+                a.record(stream)
+                fn()
+                b.record(stream)
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+    reps = max(3, min(args.steps, 10))
+    t_plain = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=plain), reps)
+    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=plain)
+    f_plain, _ = ctx.last_trace_stats()
+    pred = crt.Predictor(ctx, bvh, seed=1, miss_threshold=0.9)
+    truth = pred.classes_of_hits(plain)
+    hit = truth != 127
+    passes = 20
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = [pred.train(rays, plain, offset=k % 20) for k in range(passes)]
+    train_ms = (time.perf_counter() - t0) * 1e3 / passes
+    t_infer = timed(lambda: pred.infer(rays, out=cls), reps)
+    t_seeded = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR, out=seeded), reps)
+    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR | crt.TRACE_STATS, out=seeded)
+    f_seeded, _ = ctx.last_trace_stats()
+    identical = bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
+    pc = cls.cpu().numpy().view(np.uint16)
+    hit_rate = float((pc[hit] == truth[hit]).mean()) if hit.any() else 0.0
+    tcls = torch.from_numpy(truth.astype(np.int16)).to(dev)
+    t_perfect = timed(lambda: ctx.trace_seeded(bvh, rays, tcls, crt.TRI_WATERTIGHT, out=seeded), reps)
+    ctx.trace_seeded(bvh, rays, tcls, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=seeded)
+    f_perfect, _ = ctx.last_trace_stats()
+    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
+    info = pred.info()
+    pred.free()
+    bvh.free()
+    return {
+        "workload": "clustered soup 4,194,304 tris (256 clusters); 8,388,608 cosine bounce rays from 2048x2048 primary hits",
+        "build_ms": round(build_ms, 3),
+        "plain_mrays_s": round(n / t_plain / 1e3, 1),
+        "seeded_mrays_s": round(n / t_seeded / 1e3, 1),
+        "speedup": round(t_plain / t_seeded, 3),
+        "infer_ms": round(t_infer, 3),
+        "overhead_frac": round(t_infer / t_seeded, 3),
+        "identical_hits": identical,
+        "treelet_hit_rate": round(hit_rate, 4),
+        "rays_hitting": round(float(hit.mean()), 4),
+        "treelets": info["treelets"],
+        "node_fetches_per_ray": {"plain": round(f_plain / n, 2), "seeded": round(f_seeded / n, 2),
+                                 "perfect_prediction": round(f_perfect / n, 2)},
+        "perfect_prediction_speedup": round(t_plain / t_perfect, 3),
+        "training": {"passes": passes, "adam_steps": info["steps"], "loss_first": round(losses[0], 4),
+                     "loss_last": round(losses[-1], 4), "ms_per_pass": round(train_ms, 2),
+                     "samples_per_pass": n // 20},
+    }
 
 
 def cpu_baseline(tris, models, cam, sample_stride=8):
@@ -369,6 +463,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-predictor", action="store_true", help="skip the learned-predictor (4M-triangle) experiment")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

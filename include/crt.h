@@ -258,8 +258,9 @@ crt_status crt_predictor_params(crt_ctx* ctx, crt_predictor* pred, float* params
 crt_status crt_predictor_info(const crt_predictor* pred, uint32_t info[4]);
 
 /* Cosine-weighted diffuse bounce rays about the geometric normal of primary
- * hits: ray j starts at the first hit at or after a scrambled primary index
- * (incoherent order); [tmin, tmax] = [1e-4, +inf]. */
+ * hits: ray j starts at entry (j * 2654435761 + seed) mod n_hits of the
+ * ordered list of primary hits (incoherent order); [tmin, tmax] =
+ * [1e-4, +inf].  With no primary hit every output ray is empty. */
 crt_status crt_bounce_rays(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* primary, const crt_hit* hits,
                            uint32_t n_primary, uint32_t n_out, uint32_t seed, crt_ray* out);
 

@@ -941,8 +941,10 @@ crt_status crt_bounce_rays(crt_ctx* x, const crt_bvh* b, const crt_ray* primary,
         CRT_TRY(x->rays_out.reserve(sizeof(crt_ray) * static_cast<size_t>(n_out)));
         d_out = x->rays_out.as<crt_ray>();
     }
+    CRT_TRY(x->pos.reserve(crt::bounce_scratch_bytes(n_primary)));  // build scratch, idle between builds
     crt::launch_bounce(static_cast<const crt_ray*>(d_prim), static_cast<const crt_hit*>(d_hits), n_primary,
-                       b->xtri.as<float4>(), b->inv_perm.as<uint32_t>(), b->n, n_out, seed, d_out, x->stream);
+                       b->xtri.as<float4>(), b->inv_perm.as<uint32_t>(), b->n, n_out, seed, d_out,
+                       x->pos.as<uint32_t>(), x->stream);
     CRT_CUDA(cudaGetLastError());
     if (!dev_out) CRT_CUDA(cudaMemcpyAsync(out, d_out, sizeof(crt_ray) * static_cast<size_t>(n_out), cudaMemcpyDeviceToHost, x->stream));
     CRT_CUDA(cudaStreamSynchronize(x->stream));

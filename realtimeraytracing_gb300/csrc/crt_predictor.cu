@@ -612,26 +612,68 @@ __global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, co
 }
 
 // ------------------------------------------------------------ bounce rays
-// Cosine-weighted diffuse bounce rays from primary hits (incoherent: ray j
-// starts from the first hit at or after a scrambled primary index).
-__global__ void bounce_kernel(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
-                              const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out) {
+// Stable compaction of the primary hits (block counts, one-block scan,
+// ordered writes), then cosine-weighted diffuse bounce rays: ray j starts at
+// hit list entry (j * 2654435761 + seed) mod n_hits, so consecutive rays come
+// from unrelated pixels (incoherent).
+constexpr int kCompactBlock = 1024;
+
+__global__ void __launch_bounds__(kCompactBlock) hit_count_kernel(const crt_hit* hits, uint32_t n, uint32_t n_tris,
+                                                                 uint32_t* counts) {
+    const uint32_t i = blockIdx.x * kCompactBlock + threadIdx.x;
+    const bool h = i < n && hits[i].tri != CRT_MISS && hits[i].tri < n_tris;
+    const int c = __syncthreads_count(h);
+    if (threadIdx.x == 0) counts[blockIdx.x] = static_cast<uint32_t>(c);
+}
+
+__global__ void __launch_bounds__(1024) hit_scan_kernel(uint32_t* counts, uint32_t nb, uint32_t* total) {
+    __shared__ uint32_t s_part[1024];
+    const uint32_t per = (nb + 1023) / 1024, lo = threadIdx.x * per, hi = min(nb, lo + per);
+    uint32_t acc = 0;
+    for (uint32_t b = lo; b < hi; ++b) acc += counts[b];
+    s_part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < 1024; ++k) { const uint32_t t = s_part[k]; s_part[k] = run; run += t; }
+        *total = run;
+    }
+    __syncthreads();
+    uint32_t run = s_part[threadIdx.x];
+    for (uint32_t b = lo; b < hi; ++b) { const uint32_t t = counts[b]; counts[b] = run; run += t; }
+}
+
+__global__ void __launch_bounds__(kCompactBlock) hit_write_kernel(const crt_hit* hits, uint32_t n, uint32_t n_tris,
+                                                                 const uint32_t* offsets, uint32_t* list) {
+    __shared__ uint32_t s_warp[kCompactBlock / 32];
+    const uint32_t i = blockIdx.x * kCompactBlock + threadIdx.x;
+    const bool h = i < n && hits[i].tri != CRT_MISS && hits[i].tri < n_tris;
+    const uint32_t ball = __ballot_sync(0xFFFFFFFFu, h);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) s_warp[warp] = __popc(ball);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int w = 0; w < kCompactBlock / 32; ++w) { const uint32_t t = s_warp[w]; s_warp[w] = run; run += t; }
+    }
+    __syncthreads();
+    if (h) list[offsets[blockIdx.x] + s_warp[warp] + __popc(ball & ((1u << lane) - 1u))] = i;
+}
+
+__global__ void bounce_kernel(const crt_ray* prim, const crt_hit* hits, const uint32_t* list, const uint32_t* n_list,
+                              const float4* xtri, const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out,
+                              uint32_t seed, crt_ray* out) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n_out) return;
     float4* o = reinterpret_cast<float4*>(out + j);
-    uint32_t s = static_cast<uint32_t>((static_cast<uint64_t>(j) * 2654435761ull + seed) % n_prim);
-    uint32_t tri = CRT_MISS;
-    for (uint32_t probe = 0; probe < 4096; ++probe) {
-        tri = hits[s].tri;
-        if (tri != CRT_MISS && tri < n_tris) break;
-        tri = CRT_MISS;
-        s = (s + 1 == n_prim) ? 0u : s + 1;
-    }
-    if (tri == CRT_MISS) {
+    const uint32_t nh = *n_list;
+    if (nh == 0) {
         o[0] = make_float4(0.f, 0.f, 0.f, 1.f);
         o[1] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
+    const uint32_t s = list[static_cast<uint32_t>((static_cast<uint64_t>(j) * 2654435761ull + seed) % nh)];
+    const uint32_t tri = hits[s].tri;
     const float t = hits[s].t;
     const float4 r0 = reinterpret_cast<const float4*>(prim + s)[0], r1 = reinterpret_cast<const float4*>(prim + s)[1];
     const float px = r0.x + t * r1.x, py = r0.y + t * r1.y, pz = r0.z + t * r1.z;
@@ -653,7 +695,7 @@ __global__ void bounce_kernel(const crt_ray* prim, const crt_hit* hits, uint32_t
     const float u2 = hash_uniform((static_cast<uint64_t>(seed) << 33) ^ (2ull * j + 1));
     const float r = sqrtf(u1), phi = 6.28318530718f * u2;
     const float lx = r * __cosf(phi), ly = r * __sinf(phi), lz = sqrtf(fmaxf(1.f - u1, 0.f));
-    float dx = lx * tx + ly * bx + lz * nx, dy = lx * ty + ly * by + lz * ny, dz = lx * tz + ly * bz + lz * nz;
+    const float dx = lx * tx + ly * bx + lz * nx, dy = lx * ty + ly * by + lz * ny, dz = lx * tz + ly * bz + lz * nz;
     const float dl = rsqrtf(dx * dx + dy * dy + dz * dz);
     o[0] = make_float4(px, py, pz, 1e-4f);
     o[1] = make_float4(dx * dl, dy * dl, dz * dl, __int_as_float(0x7F800000));
@@ -717,12 +759,24 @@ void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t
     pred::treelet_label_kernel<<<(n_leaves + 255) / 256, 256, 0, s>>>(tl, n_tl, perm, n_leaves, tri_class);
 }
 
+size_t bounce_scratch_bytes(uint32_t n_prim) {
+    const size_t nb = (n_prim + pred::kCompactBlock - 1) / pred::kCompactBlock;
+    return 4 * (nb + 4 + static_cast<size_t>(n_prim));
+}
+
 void launch_bounce(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
                    const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out,
-                   cudaStream_t s) {
+                   uint32_t* scratch, cudaStream_t s) {
     if (n_out == 0 || n_prim == 0) return;
-    pred::bounce_kernel<<<(n_out + 255) / 256, 256, 0, s>>>(prim, hits, n_prim, xtri, inv_perm, n_tris, n_out, seed,
-                                                           out);
+    const uint32_t nb = (n_prim + pred::kCompactBlock - 1) / pred::kCompactBlock;
+    uint32_t* counts = scratch;
+    uint32_t* total = scratch + nb;
+    uint32_t* list = scratch + nb + 4;
+    pred::hit_count_kernel<<<nb, pred::kCompactBlock, 0, s>>>(hits, n_prim, n_tris, counts);
+    pred::hit_scan_kernel<<<1, 1024, 0, s>>>(counts, nb, total);
+    pred::hit_write_kernel<<<nb, pred::kCompactBlock, 0, s>>>(hits, n_prim, n_tris, counts, list);
+    pred::bounce_kernel<<<(n_out + 255) / 256, 256, 0, s>>>(prim, hits, list, total, xtri, inv_perm, n_tris, n_out,
+                                                           seed, out);
 }
 
 }  // namespace crt

@@ -78,8 +78,9 @@ void pred_adam(const PredictorDev& P, float scale, float lr, uint32_t step, cuda
 void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s);
 void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t* perm, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
+size_t bounce_scratch_bytes(uint32_t n_prim);
 void launch_bounce(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
                    const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out,
-                   cudaStream_t s);
+                   uint32_t* scratch, cudaStream_t s);
 
 }  // namespace crt
