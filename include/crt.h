@@ -127,7 +127,9 @@ typedef struct crt_config {
     uint32_t trace_block;       /* threads per traversal block, default 128 */
     uint32_t stack_depth;       /* traversal stack entries per ray, default 64 */
     uint32_t spin_limit;        /* bound on every device-side wait loop, 0 = default */
+    uint32_t build_flags;       /* CRT_BUILD_MULTI_LAUNCH: one launch per PLOC iteration and layout level */
 } crt_config;
+#define CRT_BUILD_MULTI_LAUNCH 0x1u
 
 typedef struct crt_ctx crt_ctx;
 typedef struct crt_bvh crt_bvh;
@@ -138,8 +140,8 @@ typedef struct crt_build_stats {
     uint32_t ploc_iterations;
     float ms_morton;     /* scene box + Morton codes */
     float ms_sort;       /* radix sort of (code, index) */
-    float ms_ploc;       /* PLOC iterations */
-    float ms_layout;     /* DFS node layout */
+    float ms_ploc;       /* PLOC iterations (+ the DFS layout on the one-launch path) */
+    float ms_layout;     /* DFS node layout when it runs as separate launches */
     float ms_total;
     float scene_box[6];  /* min xyz, max xyz over the scanned buffer */
 } crt_build_stats;

@@ -52,7 +52,8 @@ class CrtError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("ploc_radius", C.c_uint32), ("sort_digit_bits", C.c_uint32),
-                ("trace_block", C.c_uint32), ("stack_depth", C.c_uint32), ("spin_limit", C.c_uint32)]
+                ("trace_block", C.c_uint32), ("stack_depth", C.c_uint32), ("spin_limit", C.c_uint32),
+                ("build_flags", C.c_uint32)]
 
 
 class BuildStats(C.Structure):
@@ -279,11 +280,12 @@ class Context:
     """crt_ctx: one CUDA stream and the device scratch of the build."""
 
     def __init__(self, device: int = 0, ploc_radius: int = 16, sort_digit_bits: int = 8, trace_block: int = 128,
-                 stack_depth: int = 64, spin_limit: int = 0):
+                 stack_depth: int = 64, spin_limit: int = 0, multi_launch_build: bool = False):
         cfg = Config()
         lib().crt_default_config(C.byref(cfg))
         cfg.device, cfg.ploc_radius, cfg.sort_digit_bits = device, ploc_radius, sort_digit_bits
         cfg.trace_block, cfg.stack_depth, cfg.spin_limit = trace_block, stack_depth, spin_limit
+        cfg.build_flags = 1 if multi_launch_build else 0
         h = C.c_void_p()
         _check(lib().crt_create(C.byref(h), C.byref(cfg)))
         self.handle = h

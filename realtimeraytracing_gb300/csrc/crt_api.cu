@@ -134,6 +134,7 @@ struct crt_ctx {
     cudaEvent_t ev[6] = {};
     crt_build_stats stats{};
     std::vector<uint2> it_host;
+    bool force_multi_launch = false;  // testing: run PLOC/layout as one launch per iteration
 
     crt_status pinned_reserve(size_t bytes) {
         if (bytes <= pinned_cap) return CRT_OK;
@@ -174,6 +175,7 @@ void crt_default_config(crt_config* cfg) {
     cfg->trace_block = 128;
     cfg->stack_depth = 64;
     cfg->spin_limit = 0;
+    cfg->build_flags = 0;
 }
 
 crt_status crt_create(crt_ctx** out, const crt_config* cfg) {
@@ -203,6 +205,7 @@ crt_status crt_create(crt_ctx** out, const crt_config* cfg) {
     crt_ctx* x = new crt_ctx();
     x->device = c.device;
     x->cfg = c;
+    x->force_multi_launch = (c.build_flags & CRT_BUILD_MULTI_LAUNCH) != 0;
     crt_status s = CRT_OK;
     if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) s = fail(CRT_ERR_CUDA, "stream");
     for (auto& e : x->ev)
@@ -295,7 +298,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(x->clus_a.reserve(32ull * N));
     CRT_TRY(x->clus_b.reserve(32ull * N));
     CRT_TRY(x->iters.reserve(8ull * (N + 2)));
-    CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 16));
+    CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 32));  // + tickets[2], barrier[2], iteration count
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
     CRT_TRY(b->wide.reserve(64ull * N));
@@ -327,7 +330,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, s));
     CRT_CUDA(cudaMemsetAsync(x->hist.p, 0, 4 * hist_words, s));
     CRT_CUDA(cudaMemsetAsync(x->sort_lb.p, 0, 4 * sort_lb_words, s));
-    CRT_CUDA(cudaMemsetAsync(x->ploc_lb.p, 0, 8ull * (2ull * ploc_tiles) + 16, s));
+    CRT_CUDA(cudaMemsetAsync(x->ploc_lb.p, 0, 8ull * (2ull * ploc_tiles) + 32, s));
     uint32_t* err = x->err.as<uint32_t>();
     auto* st = x->scene_state.as<crt::SceneState>();
 
@@ -363,7 +366,27 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_CUDA(cudaGetLastError());
     x->it_host.assign(1, make_uint2(N, N));
     uint32_t iters = 0;
-    if (N > 1) {
+    bool laid_out = false;
+    if (N > 1 && !x->force_multi_launch) {
+        // one cooperative launch: every PLOC iteration, then the DFS layout
+        unsigned long long* lb = x->ploc_lb.as<unsigned long long>();
+        uint32_t* tail = reinterpret_cast<uint32_t*>(lb + 2ull * ploc_tiles);
+        const cudaError_t e = crt::launch_ploc_persistent(
+            x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), d_it, N,
+            static_cast<int>(x->cfg.ploc_radius), lb, tail, ploc_tiles, x->pos.as<uint2>(), b->nodes.as<crt_bvh_node>(),
+            b->wide.as<float4>(), tail + 2, tail + 4, err, x->cfg.spin_limit, s);
+        if (e == cudaSuccess) {
+            CRT_CUDA(cudaEventRecord(x->ev[3], s));
+            CRT_CUDA(cudaMemcpyAsync(&iters, tail + 4, 4, cudaMemcpyDeviceToHost, s));
+            CRT_CUDA(cudaStreamSynchronize(s));
+            laid_out = true;
+        } else if (e != cudaErrorNotSupported && e != cudaErrorCooperativeLaunchTooLarge) {
+            return fail(CRT_ERR_CUDA, "PLOC launch failed: %s", cudaGetErrorString(e));
+        } else {
+            cudaGetLastError();
+        }
+    }
+    if (N > 1 && !laid_out) {
         uint32_t n_known = N;
         int iter = 0;
         double rate = 0.6;
@@ -411,12 +434,12 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
             }
         }
     }
-    CRT_CUDA(cudaEventRecord(x->ev[3], s));
+    if (!laid_out) CRT_CUDA(cudaEventRecord(x->ev[3], s));
 
-    // ---- K4: DFS layout, last PLOC iteration first
+    // ---- K4: DFS layout, last PLOC iteration first (done above on the persistent path)
     if (N == 1) {
         crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), s);
-    } else {
+    } else if (!laid_out) {
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
             crt::launch_layout_level(x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), x->pos.as<uint2>(),
                                      x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(),

@@ -383,59 +383,49 @@ __device__ __forceinline__ float sa_merged(float4 amn, float4 amx, float4 bmn, f
 }
 
 template <int TILE, int BLOCK, int MAXR>
-__global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __restrict__ cin, float4* __restrict__ cout,
-                                                               float4* __restrict__ node_box, uint32_t* __restrict__ node_lc,
-                                                               uint2* it, int iter, uint32_t N,
-                                                               int R, unsigned long long* lookback, uint32_t* tickets,
-                                                               uint32_t n_tiles_cap, uint32_t* err, uint32_t spin_limit) {
-    constexpr int IPT = TILE / BLOCK;
-    constexpr int SPAN = TILE + 4 * MAXR;
-    constexpr int NNSPAN = TILE + 2 * MAXR;
-    __shared__ float4 s_mn[SPAN];
-    __shared__ float4 s_mx[SPAN];
-    __shared__ uint32_t s_nn[NNSPAN];
-    __shared__ uint32_t s_wsum[BLOCK / 32];
-    __shared__ uint32_t s_tile;
-    __shared__ unsigned long long s_prefix;
+struct PlocSmem {
+    float4 mn[TILE + 4 * MAXR];
+    float4 mx[TILE + 4 * MAXR];
+    uint32_t nn[TILE + 2 * MAXR];
+    uint32_t wsum[BLOCK / 32];
+    unsigned long long prefix;
+};
 
-    const uint2 cur = it[iter];
+// One tile of one PLOC iteration (see above).  Reads of data other blocks
+// wrote (the cluster array) bypass L1 (__ldcg), so the same code is correct
+// inside the persistent kernel, where no launch boundary separates iterations.
+template <int TILE, int BLOCK, int MAXR>
+__device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32_t tile, const uint2 cur, int iter,
+                                          const float4* __restrict__ cin, float4* __restrict__ cout,
+                                          float4* __restrict__ node_box, uint32_t* __restrict__ node_lc, uint2* it,
+                                          uint32_t N, int R, unsigned long long* lb_cur, unsigned long long* lb_next,
+                                          uint32_t* err, uint32_t spin_limit) {
+    constexpr int IPT = TILE / BLOCK;
     const uint32_t n = cur.x;
-    if (n <= 1u) {
-        // Finished: carry the state forward so a later launch of this build
-        // never reads an entry left over from an earlier build.
-        if (blockIdx.x == 0 && threadIdx.x == 0) it[iter + 1] = cur;
-        return;
-    }
-    unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
-    unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
-    if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
     const uint32_t s = tile * TILE;
-    if (s >= n) return;
-    if (tile == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
+    __syncthreads();  // the previous tile of this block is done with S
     if (threadIdx.x == 0) lb_next[tile] = 0ull;
     const uint32_t e = min(n, s + TILE);
     const int lo = max(0, static_cast<int>(s) - 2 * R);
     const int hi = min(static_cast<int>(n), static_cast<int>(e) + 2 * R);
     for (int p = lo + threadIdx.x; p < hi; p += BLOCK) {
-        s_mn[p - lo] = cin[2 * static_cast<size_t>(p)];
-        s_mx[p - lo] = cin[2 * static_cast<size_t>(p) + 1];
+        S.mn[p - lo] = __ldcg(cin + 2 * static_cast<size_t>(p));
+        S.mx[p - lo] = __ldcg(cin + 2 * static_cast<size_t>(p) + 1);
     }
     __syncthreads();
     const int nlo = max(0, static_cast<int>(s) - R);
     const int nhi = min(static_cast<int>(n), static_cast<int>(e) + R);
     for (int p = nlo + threadIdx.x; p < nhi; p += BLOCK) {
-        const float4 amn = s_mn[p - lo], amx = s_mx[p - lo];
+        const float4 amn = S.mn[p - lo], amx = S.mx[p - lo];
         const int j0 = max(0, p - R), j1 = min(static_cast<int>(n), p + R + 1);
         float best = __int_as_float(0x7F800000);
         int bj = p;
         for (int j = j0; j < j1; ++j) {
             if (j == p) continue;
-            const float dd = sa_merged(amn, amx, s_mn[j - lo], s_mx[j - lo]);
+            const float dd = sa_merged(amn, amx, S.mn[j - lo], S.mx[j - lo]);
             if (dd < best) { best = dd; bj = j; }
         }
-        s_nn[p - nlo] = static_cast<uint32_t>(bj);
+        S.nn[p - nlo] = static_cast<uint32_t>(bj);
     }
     __syncthreads();
 
@@ -446,8 +436,8 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
     for (int q = 0; q < IPT; ++q) {
         const int p = static_cast<int>(s) + threadIdx.x * IPT + q;
         if (p >= static_cast<int>(e)) break;
-        const int j = static_cast<int>(s_nn[p - nlo]);
-        const bool mutual = (j != p) && (static_cast<int>(s_nn[j - nlo]) == p);
+        const int j = static_cast<int>(S.nn[p - nlo]);
+        const bool mutual = (j != p) && (static_cast<int>(S.nn[j - nlo]) == p);
         const bool head = mutual && p < j;
         const bool gone = mutual && p > j;
         if (!gone) { flags |= 1u << q; ++nv; }
@@ -460,11 +450,11 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
         if (lane >= o) incl += y;
     }
-    if (lane == 31) s_wsum[warp] = incl;
+    if (lane == 31) S.wsum[warp] = incl;
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t run = 0;
-        for (int w = 0; w < BLOCK / 32; ++w) { const uint32_t t = s_wsum[w]; s_wsum[w] = run; run += t; }
+        for (int w = 0; w < BLOCK / 32; ++w) { const uint32_t t = S.wsum[w]; S.wsum[w] = run; run += t; }
         const unsigned long long tv = run >> 16, tm = run & 0xFFFFu;
         // look-back over preceding tiles
         unsigned long long ev = 0, em = 0;
@@ -488,22 +478,22 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
             }
             st_release_u64(&lb_cur[tile], kPlPrefix | ((ev + tv) << 31) | (em + tm));
         }
-        s_prefix = (ev << 32) | em;
+        S.prefix = (ev << 32) | em;
         if (e == n)  // last tile: size and id base of the next iteration
             it[iter + 1] = make_uint2(static_cast<uint32_t>(ev + tv), cur.y + static_cast<uint32_t>(em + tm));
     }
     __syncthreads();
-    const uint32_t excl = s_wsum[warp] + (incl - packed);
-    uint32_t out_v = static_cast<uint32_t>(s_prefix >> 32) + (excl >> 16);
-    uint32_t out_m = cur.y + static_cast<uint32_t>(s_prefix & 0xFFFFFFFFull) + (excl & 0xFFFFu);
+    const uint32_t excl = S.wsum[warp] + (incl - packed);
+    uint32_t out_v = static_cast<uint32_t>(S.prefix >> 32) + (excl >> 16);
+    uint32_t out_m = cur.y + static_cast<uint32_t>(S.prefix & 0xFFFFFFFFull) + (excl & 0xFFFFu);
 #pragma unroll
     for (int q = 0; q < IPT; ++q) {
         if (!(flags & (1u << q))) continue;
         const int p = static_cast<int>(s) + threadIdx.x * IPT + q;
-        float4 mn = s_mn[p - lo], mx = s_mx[p - lo];
+        float4 mn = S.mn[p - lo], mx = S.mx[p - lo];
         if (flags & (1u << (16 + q))) {
-            const int j = static_cast<int>(s_nn[p - nlo]);
-            const float4 bmn = s_mn[j - lo], bmx = s_mx[j - lo];
+            const int j = static_cast<int>(S.nn[p - nlo]);
+            const float4 bmn = S.mn[j - lo], bmx = S.mx[j - lo];
             const uint32_t id = out_m++;
             if (id >= 2 * N - 1 || id < N) { raise_corrupt(err, 2 + (iter << 8), p, id); continue; }
             float4 m0, m1;  // AABB::merge (bvh.cpp:401-413), first argument = lower position
@@ -525,6 +515,33 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
     }
 }
 
+template <int TILE, int BLOCK, int MAXR>
+__global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __restrict__ cin, float4* __restrict__ cout,
+                                                               float4* __restrict__ node_box, uint32_t* __restrict__ node_lc,
+                                                               uint2* it, int iter, uint32_t N,
+                                                               int R, unsigned long long* lookback, uint32_t* tickets,
+                                                               uint32_t n_tiles_cap, uint32_t* err, uint32_t spin_limit) {
+    __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
+    __shared__ uint32_t s_tile;
+    const uint2 cur = it[iter];
+    const uint32_t n = cur.x;
+    if (n <= 1u) {
+        // Finished: carry the state forward so a later launch of this build
+        // never reads an entry left over from an earlier build.
+        if (blockIdx.x == 0 && threadIdx.x == 0) it[iter + 1] = cur;
+        return;
+    }
+    unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
+    unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
+    if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile * TILE >= n) return;
+    if (tile == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
+    ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_lc, it, N, R, lb_cur, lb_next, err,
+                                 spin_limit);
+}
+
 // ================================================== K4: DFS node layout
 // Scene::recursiveTopDownTraversalBVH (scene.cpp:189-201): pre-order, left
 // subtree first, root (the last merge, id 2N-2) at 0.  A node at position p
@@ -539,19 +556,15 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 // their sorted position, which is also their left-to-right order in the tree
 // (PLOC merges keep Morton order), so the traversal's triangles are stored
 // in that order.
-__global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
-                                                           const uint32_t* __restrict__ node_lc,
-                                                           uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
-                                                           uint32_t N, crt_bvh_node* __restrict__ out,
-                                                           float4* __restrict__ wide, uint32_t* err) {
-    const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (X >= id_end) return;
+__device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict__ node_box,
+                                            const uint32_t* __restrict__ node_lc, uint2* __restrict__ pf, uint32_t N,
+                                            crt_bvh_node* __restrict__ out, float4* __restrict__ wide, uint32_t* err) {
     // (DFS position, first leaf below) of X; the root sits at (0, 0)
-    const uint2 me = (X == 2 * N - 2) ? make_uint2(0u, 0u) : pf[X - N];
+    const uint2 me = (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
     const uint32_t p = me.x, f = me.y;
-    const float4 mn = node_box[2 * static_cast<size_t>(X)], mx = node_box[2 * static_cast<size_t>(X) + 1];
+    const float4 mn = __ldcg(node_box + 2 * static_cast<size_t>(X)), mx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
     const uint32_t a = __float_as_uint(mn.w), b = __float_as_uint(mx.w);
-    const uint32_t lca = (a < N) ? 1u : node_lc[a - N];
+    const uint32_t lca = (a < N) ? 1u : __ldcg(node_lc + (a - N));
     const uint32_t pl = p + 1, pr = p + 2 * lca;
     if (pr >= 2 * N - 1 || p < f || p - f >= N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
         raise_corrupt(err, 4, X, pr);
@@ -566,8 +579,8 @@ __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restr
     uint32_t cref[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-        cmn[c] = node_box[2 * static_cast<size_t>(ch[c])];
-        cmx[c] = node_box[2 * static_cast<size_t>(ch[c]) + 1];
+        cmn[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]));
+        cmx[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]) + 1);
         if (ch[c] < N) {
             float4* lo = reinterpret_cast<float4*>(out + cp[c]);
             lo[0] = make_float4(cmn[c].x, cmn[c].y, cmn[c].z, 0.f);
@@ -580,12 +593,87 @@ __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restr
         }
     }
     // traversal node: both child boxes and references in 64 bytes
+    const uint32_t lcb = (b < N) ? 1u : __ldcg(node_lc + (b - N));
     float4* w = wide + 4 * static_cast<size_t>(p - f);
     w[0] = make_float4(cmn[0].x, cmn[0].y, cmn[0].z, __uint_as_float(cref[0]));
     w[1] = make_float4(cmx[0].x, cmx[0].y, cmx[0].z, __uint_as_float(cref[1]));
-    const uint32_t lcb = (b < N) ? 1u : node_lc[b - N];
     w[2] = make_float4(cmn[1].x, cmn[1].y, cmn[1].z, __uint_as_float(lca));  // leaf counts of the children
     w[3] = make_float4(cmx[1].x, cmx[1].y, cmx[1].z, __uint_as_float(lcb));
+}
+
+__global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
+                                                           const uint32_t* __restrict__ node_lc,
+                                                           uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
+                                                           uint32_t N, crt_bvh_node* __restrict__ out,
+                                                           float4* __restrict__ wide, uint32_t* err) {
+    const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (X >= id_end) return;
+    layout_node(X, node_box, node_lc, pf, N, out, wide, err);
+}
+
+// ================================== K3+K4 fused: one persistent launch
+// All PLOC iterations, then all layout levels, separated by a grid-wide
+// barrier (co-residency guaranteed by a cooperative launch; every wait is
+// bounded and a timeout ends every block).  Saves the per-iteration launch
+// and the host round trips the multi-launch path needs.
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, uint32_t* err, uint32_t spin_limit) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int gen = ld_acquire_u32(bar + 1);
+        __threadfence();
+        const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            st_release_u32(bar + 1, gen + 1u);
+        } else {
+            SpinBound spin(spin_limit);
+            while (ld_acquire_u32(bar + 1) == gen)
+                if (!spin.step()) { raise_error(err, kDevTimeout); break; }
+        }
+    }
+    __syncthreads();
+    return (ld_acquire_u32(err) & kDevTimeout) == 0u;
+}
+
+template <int TILE, int BLOCK, int MAXR>
+__global__ void __launch_bounds__(BLOCK) ploc_persistent_kernel(float4* ca, float4* cb, float4* __restrict__ node_box,
+                                                                uint32_t* __restrict__ node_lc, uint2* it, uint32_t N,
+                                                                int R, unsigned long long* lookback, uint32_t* tickets,
+                                                                uint32_t n_tiles_cap, uint2* pf, crt_bvh_node* out,
+                                                                float4* wide, unsigned int* bar, uint32_t* iters_out,
+                                                                uint32_t* err, uint32_t spin_limit) {
+    __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
+    __shared__ uint32_t s_tile;
+    int iter = 0;
+    for (;; ++iter) {
+        const uint2 cur = __ldcg(it + iter);
+        if (cur.x <= 1u) break;
+        const float4* cin = (iter & 1) ? cb : ca;
+        float4* cout = (iter & 1) ? ca : cb;
+        unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
+        unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
+        for (;;) {
+            __syncthreads();
+            if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
+            __syncthreads();
+            const uint32_t tile = s_tile;
+            if (tile * TILE >= cur.x) break;
+            if (tile == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
+            ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_lc, it, N, R, lb_cur, lb_next,
+                                         err, spin_limit);
+        }
+        if (!grid_barrier(bar, err, spin_limit)) return;
+        if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *iters_out = static_cast<uint32_t>(iter);
+    // DFS layout, last iteration's nodes first
+    for (int k = iter - 1; k >= 0; --k) {
+        const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
+        for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
+            layout_node(X, node_box, node_lc, pf, N, out, wide, err);
+        if (k > 0 && !grid_barrier(bar, err, spin_limit)) return;
+    }
 }
 
 __global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out) {
@@ -646,6 +734,36 @@ void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2*
     if (id_end <= id_begin || id_end > 2 * N - 1) return;
     const uint32_t cnt = id_end - id_begin;
     layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pf, id_begin, id_end, N, out, wide, err);
+}
+
+int ploc_persistent_grid() {
+    static int grid = -1;
+    if (grid < 0) {
+        int per_sm = 0, dev = 0, sms = kNumSms, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                        &per_sm, ploc_persistent_kernel<kPlocTile, 256, kPlocMaxRadius>, 256, 0) == cudaSuccess &&
+            per_sm > 0)
+            grid = (per_sm < 2 ? per_sm : 2) * sms;
+        else
+            grid = 0;
+        cudaGetLastError();
+    }
+    return grid;
+}
+
+cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint32_t* node_lc, uint2* it, uint32_t N,
+                                   int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
+                                   uint2* pf, crt_bvh_node* out, float4* wide, unsigned int* bar, uint32_t* iters_out,
+                                   uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+    const int grid = ploc_persistent_grid();
+    if (grid <= 0) return cudaErrorNotSupported;
+    void* args[] = {&ca, &cb, &node_box, &node_lc, &it, &N, &radius, &lookback, &tickets, &n_tiles_cap, &pf, &out,
+                    &wide, &bar, &iters_out, &err, &spin_limit};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ploc_persistent_kernel<kPlocTile, 256, kPlocMaxRadius>),
+                                       dim3(grid), dim3(256), args, 0, s);
 }
 
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s) {

@@ -44,6 +44,12 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
 void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
                          uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint32_t* err, cudaStream_t s);
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
+// All PLOC iterations and the DFS layout in one cooperative launch; returns
+// cudaErrorNotSupported when a cooperative launch is unavailable.
+cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint32_t* node_lc, uint2* it, uint32_t N,
+                                   int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
+                                   uint2* pf, crt_bvh_node* out, float4* wide, unsigned int* bar, uint32_t* iters_out,
+                                   uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 
 // Trace side (crt_trace.cu).
 struct TraceParams {

@@ -125,3 +125,14 @@ def test_bad_model_id_is_an_error(ctx):
     with pytest.raises(crt.CrtError) as e:
         ctx.build(tris, models=S.identity_models(1))
     assert e.value.status == 7
+
+
+@pytest.mark.parametrize("n", [2, 1000, 70000])
+def test_multi_launch_build_matches(ctx, n):
+    """The one-launch persistent PLOC+layout and the per-iteration launches
+    produce the same node array."""
+    from realtimeraytracing_gb300 import crt
+    c = crt.Context(multi_launch_build=True)
+    tris = S.uniform_soup(n, seed=60 + n)
+    _check_build(c, tris, n, S.identity_models(1))
+    c.close()
