@@ -119,6 +119,7 @@ typedef struct crt_camera {
 #define CRT_TRI_WATERTIGHT    0x2u  /* Woop/Benthin/Wald 2013 watertight predicate, two-sided */
 #define CRT_TRACE_USE_PREDICTOR 0x4u /* seed t_max from the learned hit predictor */
 #define CRT_TRACE_STATS       0x8u  /* count visited nodes / tested triangles (slower) */
+#define CRT_TRACE_WIDE        0x10u /* walk the 4-wide nodes instead of the binary ones (same hits) */
 
 typedef struct crt_config {
     int device;                 /* CUDA device ordinal, default 0 */
@@ -195,7 +196,8 @@ crt_status crt_shadow_rays(crt_ctx* ctx, const crt_ray* primary, const crt_hit* 
 crt_status crt_trace(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, uint32_t n_rays,
                      uint32_t flags, crt_hit* hits);
 /* Counters of the last crt_trace issued with CRT_TRACE_STATS:
- * out[0] = 64-byte traversal nodes fetched, out[1] = triangles tested. */
+ * out[0] = traversal nodes fetched (64-byte binary, or 128-byte 4-wide with
+ * CRT_TRACE_WIDE), out[1] = triangles tested. */
 crt_status crt_last_trace_stats(crt_ctx* ctx, uint64_t out[2]);
 
 /* One frame of the reference's compute pass (Application::drawOneFrame,

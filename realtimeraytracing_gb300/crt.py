@@ -26,6 +26,7 @@ TRI_REFERENCE = 0x0
 TRI_WATERTIGHT = 0x2
 TRACE_USE_PREDICTOR = 0x4
 TRACE_STATS = 0x8
+TRACE_WIDE = 0x10
 USE_PREDICTOR = TRACE_USE_PREDICTOR
 MISS = 0xFFFFFFFF
 

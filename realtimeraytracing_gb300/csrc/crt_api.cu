@@ -89,7 +89,7 @@ struct crt_bvh {
     uint32_t n = 0;
     uint32_t iterations = 0;
     float abs_eps = 0.f;
-    DevBuf nodes, wide, xtri, codes, perm, inv_perm;
+    DevBuf nodes, wide, wide4, depth_odd, xtri, codes, perm, inv_perm;
     crt_predictor* predictor = nullptr;
 };
 
@@ -302,6 +302,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
     CRT_TRY(b->wide.reserve(64ull * N));
+    CRT_TRY(b->wide4.reserve(128ull * N));
+    CRT_TRY(b->depth_odd.reserve(N));
     CRT_TRY(b->inv_perm.reserve(4ull * N));
     CRT_TRY(b->codes.reserve(4ull * N));
     CRT_TRY(b->perm.reserve(4ull * N));
@@ -374,7 +376,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         const cudaError_t e = crt::launch_ploc_persistent(
             x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), d_it, N,
             static_cast<int>(x->cfg.ploc_radius), lb, tail, ploc_tiles, x->pos.as<uint2>(), b->nodes.as<crt_bvh_node>(),
-            b->wide.as<float4>(), tail + 2, tail + 4, err, x->cfg.spin_limit, s);
+            b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), tail + 2, tail + 4, err, x->cfg.spin_limit, s);
         if (e == cudaSuccess) {
             CRT_CUDA(cudaEventRecord(x->ev[3], s));
             CRT_CUDA(cudaMemcpyAsync(&iters, tail + 4, 4, cudaMemcpyDeviceToHost, s));
@@ -443,8 +445,9 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
             crt::launch_layout_level(x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), x->pos.as<uint2>(),
                                      x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(),
-                                     b->wide.as<float4>(), err, s);
+                                     b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), err, s);
     }
+    if (N > 1) crt::launch_wide4(b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), N - 1, b->wide4.as<float4>(), s);
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->ev[4], s));
     CRT_TRY(x->check_device_error());
@@ -485,7 +488,7 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
 }
 
 crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS))
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS | CRT_TRACE_WIDE))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
     if ((flags & CRT_TRACE_USE_PREDICTOR) && !b->predictor)
         return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor bound to this bvh (crt_predictor_create)");
@@ -495,12 +498,13 @@ crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
 
 // Enqueues one traversal launch on device-resident rays/hits (no sync).
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
-                        crt_hit* d_hits, const uint16_t* seed_classes = nullptr) {
+                        crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0) {
     if (n_rays == 0) return CRT_OK;
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
     p.xtri = b->xtri.as<float4>();
     p.wide = b->wide.as<float4>();
+    p.wide4 = (b->n > 1) ? b->wide4.as<float4>() : nullptr;
     p.rays = d_rays;
     p.hits = d_hits;
     p.n_rays = n_rays;
@@ -508,6 +512,7 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     p.abs_eps = b->abs_eps;
     p.err = x->err.as<uint32_t>();
     p.stats = nullptr;
+    p.tile_width = tile_width;
     if (flags & CRT_TRACE_STATS) {
         CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
         p.stats = x->trace_stats.as<unsigned long long>();
@@ -525,7 +530,9 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
         p.treelets = pr->treelets.as<crt::Treelet>();
         p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
     }
-    const uint32_t launch_flags = (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) | ((b->iterations + 2 > 64) ? (1u << 16) : 0u);
+    // binary walk: stack <= tree height <= PLOC iterations + 1; 4-wide walk: <= 3 per two levels
+    const bool deep = (b->iterations + 2 > 64) || (3 * ((b->iterations + 2) / 2) + 3 > 96);
+    const uint32_t launch_flags = (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_WIDE)) | (deep ? (1u << 16) : 0u);
     crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
@@ -560,6 +567,8 @@ crt_status crt_bvh_free(crt_bvh* b) {
     b->nodes.release();
     b->xtri.release();
     b->wide.release();
+    b->wide4.release();
+    b->depth_odd.release();
     b->inv_perm.release();
     if (b->predictor) b->predictor->bvh = nullptr;
     b->codes.release();
@@ -718,7 +727,8 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     crt_ray* rays = x->frame_rays.as<crt_ray>();
     crt::launch_raygen(d_cam, width, height, rays, x->stream);
-    CRT_TRY(trace_device(x, b, rays, n, flags, d_hp));
+    const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
+    CRT_TRY(trace_device(x, b, rays, n, flags, d_hp, nullptr, tw));
     if (!dev_p) CRT_CUDA(cudaMemcpyAsync(hits_primary, d_hp, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
     if (light) {
         CRT_TRY(x->frame_shadow.reserve(sizeof(crt_ray) * static_cast<size_t>(n)));
@@ -730,7 +740,7 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
         }
         crt_ray* sh = x->frame_shadow.as<crt_ray>();
         crt::launch_shadow_rays(rays, d_hp, n, light[0], light[1], light[2], sh, x->stream);
-        CRT_TRY(trace_device(x, b, sh, n, (flags & ~CRT_TRACE_STATS) | CRT_TRACE_ANY, d_hs));
+        CRT_TRY(trace_device(x, b, sh, n, (flags & ~CRT_TRACE_STATS) | CRT_TRACE_ANY, d_hs, nullptr, tw));
         if (!dev_s) CRT_CUDA(cudaMemcpyAsync(hits_shadow, d_hs, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
     }
     return x->check_device_error();

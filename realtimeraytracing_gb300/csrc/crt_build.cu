@@ -558,10 +558,11 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 // in that order.
 __device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict__ node_box,
                                             const uint32_t* __restrict__ node_lc, uint2* __restrict__ pf, uint32_t N,
-                                            crt_bvh_node* __restrict__ out, float4* __restrict__ wide, uint32_t* err) {
+                                            crt_bvh_node* __restrict__ out, float4* __restrict__ wide,
+                                            uint8_t* __restrict__ depth_odd, uint32_t* err) {
     // (DFS position, first leaf below) of X; the root sits at (0, 0)
     const uint2 me = (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
-    const uint32_t p = me.x, f = me.y;
+    const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;  // bit 31: depth parity
     const float4 mn = __ldcg(node_box + 2 * static_cast<size_t>(X)), mx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
     const uint32_t a = __float_as_uint(mn.w), b = __float_as_uint(mx.w);
     const uint32_t lca = (a < N) ? 1u : __ldcg(node_lc + (a - N));
@@ -588,12 +589,13 @@ __device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict
             reinterpret_cast<uint4*>(lo)[2] = make_uint4(__float_as_uint(cmn[c].w), 0u, 0u, 0u);
             cref[c] = kLeafRef | ch[c];          // leaf: its sorted position
         } else {
-            pf[ch[c] - N] = make_uint2(cp[c], cf[c]);
+            pf[ch[c] - N] = make_uint2(cp[c], cf[c] | ((odd ^ 1u) << 31));
             cref[c] = cp[c] - cf[c];             // internal: its rank among internal nodes in DFS order
         }
     }
     // traversal node: both child boxes and references in 64 bytes
     const uint32_t lcb = (b < N) ? 1u : __ldcg(node_lc + (b - N));
+    if (depth_odd) depth_odd[p - f] = static_cast<uint8_t>(odd);
     float4* w = wide + 4 * static_cast<size_t>(p - f);
     w[0] = make_float4(cmn[0].x, cmn[0].y, cmn[0].z, __uint_as_float(cref[0]));
     w[1] = make_float4(cmx[0].x, cmx[0].y, cmx[0].z, __uint_as_float(cref[1]));
@@ -605,10 +607,11 @@ __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restr
                                                            const uint32_t* __restrict__ node_lc,
                                                            uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
                                                            uint32_t N, crt_bvh_node* __restrict__ out,
-                                                           float4* __restrict__ wide, uint32_t* err) {
+                                                           float4* __restrict__ wide, uint8_t* __restrict__ depth_odd,
+                                                           uint32_t* err) {
     const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (X >= id_end) return;
-    layout_node(X, node_box, node_lc, pf, N, out, wide, err);
+    layout_node(X, node_box, node_lc, pf, N, out, wide, depth_odd, err);
 }
 
 // ================================== K3+K4 fused: one persistent launch
@@ -641,8 +644,8 @@ __global__ void __launch_bounds__(BLOCK) ploc_persistent_kernel(float4* ca, floa
                                                                 uint32_t* __restrict__ node_lc, uint2* it, uint32_t N,
                                                                 int R, unsigned long long* lookback, uint32_t* tickets,
                                                                 uint32_t n_tiles_cap, uint2* pf, crt_bvh_node* out,
-                                                                float4* wide, unsigned int* bar, uint32_t* iters_out,
-                                                                uint32_t* err, uint32_t spin_limit) {
+                                                                float4* wide, uint8_t* depth_odd, unsigned int* bar,
+                                                                uint32_t* iters_out, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile;
     int iter = 0;
@@ -671,7 +674,7 @@ __global__ void __launch_bounds__(BLOCK) ploc_persistent_kernel(float4* ca, floa
     for (int k = iter - 1; k >= 0; --k) {
         const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
         for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
-            layout_node(X, node_box, node_lc, pf, N, out, wide, err);
+            layout_node(X, node_box, node_lc, pf, N, out, wide, depth_odd, err);
         if (k > 0 && !grid_barrier(bar, err, spin_limit)) return;
     }
 }
@@ -682,6 +685,60 @@ __global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_
     o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
     o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
     reinterpret_cast<uint4*>(o)[2] = make_uint4(__float_as_uint(mn.w), 0u, 0u, 0u);
+}
+
+// ========================================== K4b: 4-wide traversal nodes
+// Every internal node at even depth becomes a 128-byte 4-wide node holding
+// its children's children (a leaf child stays itself): SoA boxes (min x of
+// the four, min y, ..., max z) and the four references; empty slots carry
+// kNoChild and an empty box.  Nodes keep the binary node's index (odd-depth
+// slots stay unused), so references are unchanged and exact boxes stay exact.
+__global__ void __launch_bounds__(256) wide4_kernel(const float4* __restrict__ wide, const uint8_t* __restrict__ depth_odd,
+                                                    uint32_t n_internal, float4* __restrict__ wide4) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal || depth_odd[i]) return;
+    float mnx[4], mny[4], mnz[4], mxx[4], mxy[4], mxz[4];
+    uint32_t ref[4];
+    int k = 0;
+    const float4* w = wide + 4 * static_cast<size_t>(i);
+    const float4 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
+    const float4 cmn[2] = {w0, w2}, cmx[2] = {w1, w3};
+    const uint32_t cref[2] = {__float_as_uint(w0.w), __float_as_uint(w1.w)};
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        if (cref[c] & kLeafRef) {
+            mnx[k] = cmn[c].x; mny[k] = cmn[c].y; mnz[k] = cmn[c].z;
+            mxx[k] = cmx[c].x; mxy[k] = cmx[c].y; mxz[k] = cmx[c].z;
+            ref[k++] = cref[c];
+        } else {
+            const float4* g = wide + 4 * static_cast<size_t>(cref[c]);
+            const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
+            mnx[k] = g0.x; mny[k] = g0.y; mnz[k] = g0.z; mxx[k] = g1.x; mxy[k] = g1.y; mxz[k] = g1.z;
+            ref[k++] = __float_as_uint(g0.w);
+            mnx[k] = g2.x; mny[k] = g2.y; mnz[k] = g2.z; mxx[k] = g3.x; mxy[k] = g3.y; mxz[k] = g3.z;
+            ref[k++] = __float_as_uint(g1.w);
+        }
+    }
+    const float inf = __int_as_float(0x7F800000);
+    for (; k < 4; ++k) {
+        mnx[k] = mny[k] = mnz[k] = inf;
+        mxx[k] = mxy[k] = mxz[k] = -inf;
+        ref[k] = kNoChild;
+    }
+    float4* o = wide4 + 8 * static_cast<size_t>(i);
+    o[0] = make_float4(mnx[0], mnx[1], mnx[2], mnx[3]);
+    o[1] = make_float4(mny[0], mny[1], mny[2], mny[3]);
+    o[2] = make_float4(mnz[0], mnz[1], mnz[2], mnz[3]);
+    o[3] = make_float4(mxx[0], mxx[1], mxx[2], mxx[3]);
+    o[4] = make_float4(mxy[0], mxy[1], mxy[2], mxy[3]);
+    o[5] = make_float4(mxz[0], mxz[1], mxz[2], mxz[3]);
+    reinterpret_cast<uint4*>(o)[6] = make_uint4(ref[0], ref[1], ref[2], ref[3]);
+    o[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s) {
+    if (n_internal == 0) return;
+    wide4_kernel<<<(n_internal + 255) / 256, 256, 0, s>>>(wide, depth_odd, n_internal, wide4);
 }
 
 // ============================================================ launchers
@@ -730,10 +787,12 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
 }
 
 void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
-                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint32_t* err, cudaStream_t s) {
+                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint8_t* depth_odd,
+                         uint32_t* err, cudaStream_t s) {
     if (id_end <= id_begin || id_end > 2 * N - 1) return;
     const uint32_t cnt = id_end - id_begin;
-    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pf, id_begin, id_end, N, out, wide, err);
+    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pf, id_begin, id_end, N, out, wide,
+                                                          depth_odd, err);
 }
 
 int ploc_persistent_grid() {
@@ -756,12 +815,12 @@ int ploc_persistent_grid() {
 
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint32_t* node_lc, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
-                                   uint2* pf, crt_bvh_node* out, float4* wide, unsigned int* bar, uint32_t* iters_out,
-                                   uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+                                   uint2* pf, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, unsigned int* bar,
+                                   uint32_t* iters_out, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
     const int grid = ploc_persistent_grid();
     if (grid <= 0) return cudaErrorNotSupported;
     void* args[] = {&ca, &cb, &node_box, &node_lc, &it, &N, &radius, &lookback, &tickets, &n_tiles_cap, &pf, &out,
-                    &wide, &bar, &iters_out, &err, &spin_limit};
+                    &wide, &depth_odd, &bar, &iters_out, &err, &spin_limit};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ploc_persistent_kernel<kPlocTile, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }

@@ -13,6 +13,7 @@ namespace crt {
 constexpr uint32_t kPlocTile = 1024;      // positions per PLOC tile
 constexpr int kPlocMaxRadius = 32;        // largest supported PLOC radius
 constexpr uint32_t kLeafRef = 0x80000000u;  // traversal child reference: leaf flag | sorted position
+constexpr uint32_t kNoChild = 0xFFFFFFFFu;  // empty slot of a 4-wide node
 
 // Scene box reduction state (device memory, zeroed keys at creation; the
 // finishing block resets it) and its results for the Morton pass.
@@ -42,19 +43,22 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
                            unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
                            uint32_t spin_limit, cudaStream_t s);
 void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
-                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint32_t* err, cudaStream_t s);
+                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint8_t* depth_odd,
+                         uint32_t* err, cudaStream_t s);
+void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s);
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
 // All PLOC iterations and the DFS layout in one cooperative launch; returns
 // cudaErrorNotSupported when a cooperative launch is unavailable.
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint32_t* node_lc, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
-                                   uint2* pf, crt_bvh_node* out, float4* wide, unsigned int* bar, uint32_t* iters_out,
-                                   uint32_t* err, uint32_t spin_limit, cudaStream_t s);
+                                   uint2* pf, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, unsigned int* bar,
+                                   uint32_t* iters_out, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 
 // Trace side (crt_trace.cu).
 struct TraceParams {
     const crt_bvh_node* nodes;  // reference layout (root box read from nodes[0])
     const float4* wide;      // 64-B traversal nodes: child boxes + child references
+    const float4* wide4;     // 128-B 4-wide traversal nodes (even-depth internal nodes)
     const float4* xtri;      // 3 float4 per leaf (sorted order): transformed p0 | tri id, p1, p2
     const crt_ray* rays;
     crt_hit* hits;
@@ -62,6 +66,7 @@ struct TraceParams {
     uint32_t n_nodes;
     float abs_eps;           // absolute slack of pruning, from the scene extent
     uint32_t* err;
+    uint32_t tile_width = 0;    // image width when rays are pixels (multiple of 8, height multiple of 4)
     unsigned long long* stats;  // optional: nodes visited, triangles tested
     // learned seeding (CRT_TRACE_USE_PREDICTOR): per-ray predicted treelet
     const uint16_t* pred_class = nullptr;

@@ -6,7 +6,9 @@
 // operation rounds once, in the shader's order, as in the CPU oracle.
 //
 // Traversal (one thread per ray, stack in local memory) over the 64-byte
-// traversal nodes the layout pass writes (both child boxes + references):
+// binary nodes the layout pass writes (both child boxes + references), or
+// with CRT_TRACE_WIDE over 128-byte 4-wide nodes (half the fetches, more
+// work per fetch — slower on GB300 today, kept for comparison):
 //   * children are box-tested at their parent, leaves tested at once, the
 //     nearer internal child entered without a stack round trip;
 //   * a subtree is skipped when its entry distance exceeds the best hit by
@@ -149,10 +151,20 @@ __device__ __forceinline__ float prune_bound(float t, float abs_eps) {
     return t + (fabsf(t) * 6.103515625e-05f + abs_eps);  // 2^-14 relative
 }
 
-template <bool ANY, bool WT, int STACK, bool SEED>
+// Rays of an image (p.tile_width != 0): each warp takes an 8x4 pixel tile
+// instead of a 32-pixel row strip, so its rays stay closer together.
+__device__ __forceinline__ uint32_t ray_of_thread(uint32_t t, uint32_t width) {
+    if (width == 0) return t;
+    const uint32_t tile = t >> 5, lane = t & 31u, tiles_x = width >> 3;
+    const uint32_t ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    return ((ty << 2) + (lane >> 3)) * width + (tx << 3) + (lane & 7u);
+}
+
+template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE>
 __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n_rays) return;
+    const uint32_t t_id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t_id >= p.n_rays) return;
+    const uint32_t i = ray_of_thread(t_id, p.tile_width);
     const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
     const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
     RayCtx r;
@@ -245,11 +257,80 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
             }
         }
     };
+    // Same walk over the 4-wide nodes: up to four children tested per fetch,
+    // leaves tested at once, internal hits ordered by entry distance with a
+    // 4-input sorting network; the nearest is entered, the rest pushed.
+    auto walk4 = [&](uint32_t cur) {
+        int sp = 0;
+        while (cur != 0xFFFFFFFFu) {
+            if (cur >= n_leaves - 1) { corrupt = true; break; }
+            ++fetched;
+            const float4* nd = p.wide4 + 8 * static_cast<size_t>(cur);
+            const float4 qnx = __ldg(nd), qny = __ldg(nd + 1), qnz = __ldg(nd + 2);
+            const float4 qxx = __ldg(nd + 3), qxy = __ldg(nd + 4), qxz = __ldg(nd + 5);
+            const uint4 qr = __ldg(reinterpret_cast<const uint4*>(nd + 6));
+            const float nx[4] = {qnx.x, qnx.y, qnx.z, qnx.w}, ny[4] = {qny.x, qny.y, qny.z, qny.w};
+            const float nz[4] = {qnz.x, qnz.y, qnz.z, qnz.w}, xx[4] = {qxx.x, qxx.y, qxx.z, qxx.w};
+            const float xy[4] = {qxy.x, qxy.y, qxy.z, qxy.w}, xz[4] = {qxz.x, qxz.y, qxz.z, qxz.w};
+            const uint32_t rf[4] = {qr.x, qr.y, qr.z, qr.w};
+            const float kInf = __int_as_float(0x7F800000);
+            float ht[4];
+            uint32_t hr[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                ht[c] = kInf;
+                hr[c] = 0xFFFFFFFFu;
+                if (rf[c] == kNoChild) continue;
+                float te;
+                if (!slab(r, make_float4(nx[c], ny[c], nz[c], 0.f), make_float4(xx[c], xy[c], xz[c], 0.f), grow, te))
+                    continue;
+                if (te > prune_bound(bt, p.abs_eps)) continue;
+                if (rf[c] & kLeafRef) {
+                    test_leaf(rf[c] & ~kLeafRef);
+                } else {
+                    ht[c] = te;
+                    hr[c] = rf[c];
+                }
+            }
+            if (ANY && have) break;
+            const float bnd = prune_bound(bt, p.abs_eps);
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (ht[c] > bnd) { ht[c] = kInf; hr[c] = 0xFFFFFFFFu; }
+            // sorting network, ascending entry distance (misses sort last)
+#define CRT_CSWAP(a, b)                                                           \
+    if (ht[b] < ht[a]) {                                                          \
+        const float tt = ht[a]; ht[a] = ht[b]; ht[b] = tt;                        \
+        const uint32_t rr = hr[a]; hr[a] = hr[b]; hr[b] = rr;                     \
+    }
+            CRT_CSWAP(0, 1) CRT_CSWAP(2, 3) CRT_CSWAP(0, 2) CRT_CSWAP(1, 3) CRT_CSWAP(1, 2)
+#undef CRT_CSWAP
+#pragma unroll
+            for (int c = 3; c >= 1; --c) {
+                if (hr[c] == 0xFFFFFFFFu) continue;
+                if (sp < STACK) {
+                    st_node[sp] = hr[c];
+                    st_t[sp] = ht[c];
+                    ++sp;
+                } else {
+                    overflow = true;
+                }
+            }
+            cur = hr[0];
+            if (cur != 0xFFFFFFFFu) continue;
+            const float bnd3 = prune_bound(bt, p.abs_eps);
+            while (sp > 0) {
+                --sp;
+                if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
+            }
+        }
+    };
     // Enter a subtree whose box (mn, mx) and reference are known.
     auto enter = [&](float4 mn, float4 mx, uint32_t ref, uint32_t skip) {
         float te;
         if (ref == skip || !slab(r, mn, mx, grow, te) || te > prune_bound(bt, p.abs_eps)) return;
         if (ref & kLeafRef) test_leaf(ref & ~kLeafRef);
+        else if (WIDE) walk4(ref);   // the root has depth 0, so it is a 4-wide node
         else walk(ref, skip);
     };
     constexpr uint32_t kNoSkip = 0xFFFFFFFFu;  // never a reference: leaf indices stay below 2^30
@@ -326,26 +407,30 @@ __global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__
 }
 
 template <bool ANY, bool WT>
-static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, cudaStream_t s) {
+static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, bool wide, cudaStream_t s) {
     const uint32_t grid = (p.n_rays + block - 1) / block;
     if (grid == 0) return;
     if (seed) {
-        if (deep) trace_kernel<ANY, WT, 1024, true><<<grid, block, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 64, true><<<grid, block, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, true, false><<<grid, block, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, true, false><<<grid, block, 0, s>>>(p);
+    } else if (wide) {
+        if (deep) trace_kernel<ANY, WT, 1024, false, true><<<grid, block, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 96, false, true><<<grid, block, 0, s>>>(p);
     } else {
-        if (deep) trace_kernel<ANY, WT, 1024, false><<<grid, block, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 64, false><<<grid, block, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, false, false><<<grid, block, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, false, false><<<grid, block, 0, s>>>(p);
     }
 }
 
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s) {
     const bool any = flags & CRT_TRACE_ANY, wt = flags & CRT_TRI_WATERTIGHT;
-    const bool deep = (flags >> 16) != 0;  // set by the host when the tree may be deeper than 63
+    const bool deep = (flags >> 16) != 0;  // set by the host when the tree may be deeper than the stacks allow
     const bool seed = p.pred_class != nullptr;
-    if (any && wt) launch_trace_t<true, true>(p, block, deep, seed, s);
-    else if (any) launch_trace_t<true, false>(p, block, deep, seed, s);
-    else if (wt) launch_trace_t<false, true>(p, block, deep, seed, s);
-    else launch_trace_t<false, false>(p, block, deep, seed, s);
+    const bool wide = (flags & CRT_TRACE_WIDE) && p.wide4 != nullptr;
+    if (any && wt) launch_trace_t<true, true>(p, block, deep, seed, wide, s);
+    else if (any) launch_trace_t<true, false>(p, block, deep, seed, wide, s);
+    else if (wt) launch_trace_t<false, true>(p, block, deep, seed, wide, s);
+    else launch_trace_t<false, false>(p, block, deep, seed, wide, s);
 }
 
 void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s) {

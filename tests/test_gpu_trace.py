@@ -139,3 +139,15 @@ def test_trace_stats_counts(ctx, config0):
     visited, tested = ctx.last_trace_stats()
     assert visited > rays.shape[0] and tested > 0
     _cmp_hits(got, O.trace(bvh.nodes(), tris, models, rays, crt.TRI_REFERENCE)[0])
+
+
+@pytest.mark.parametrize("flags", [crt.TRI_REFERENCE, crt.TRI_WATERTIGHT, crt.TRI_WATERTIGHT | crt.TRACE_ANY])
+def test_binary_and_wide_walks_agree(ctx, config0, flags):
+    """The binary walk (default) and the 4-wide walk (CRT_TRACE_WIDE) return
+    the oracle's hits."""
+    tris, models, cam, w, h, bvh = config0
+    rays = O.raygen(cam, w, h)
+    ref, _ = O.trace(bvh.nodes(), tris, models, rays, flags)
+    any_hit = bool(flags & crt.TRACE_ANY)
+    _cmp_hits(ctx.trace(bvh, rays, flags), ref, any_hit)
+    _cmp_hits(ctx.trace(bvh, rays, flags | crt.TRACE_WIDE), ref, any_hit)
