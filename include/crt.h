@@ -268,6 +268,43 @@ crt_status crt_predictor_info(const crt_predictor* pred, uint32_t info[4]);
 crt_status crt_bounce_rays(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* primary, const crt_hit* hits,
                            uint32_t n_primary, uint32_t n_out, uint32_t seed, crt_ray* out);
 
+/* ---- batched scenes (many scenes, one launch per stage) -----------------
+ * n_scenes <= 256 scenes whose triangles and rays are concatenated in scene
+ * order (scene s owns tri_counts[s] triangles and ray_counts[s] rays).  Every
+ * stage runs as one launch over all scenes (per-scene scene boxes and Morton
+ * codes, one radix sort with a final pass that regroups the scenes, all
+ * scenes' PLOC iterations in one persistent launch, one trace launch), and
+ * crt_batch_run can capture build + trace into a CUDA graph and replay it.
+ * Each scene's node array equals crt_build on that scene alone.  Hits carry
+ * scene-local triangle indices. */
+typedef struct crt_batch crt_batch;
+crt_status crt_batch_create(crt_ctx* ctx, const uint32_t* tri_counts, const uint32_t* ray_counts, uint32_t n_scenes,
+                            crt_batch** out);
+crt_status crt_batch_free(crt_batch* batch);
+/* Model matrices shared by all scenes (host memory, <= 64). */
+crt_status crt_batch_set_models(crt_ctx* ctx, crt_batch* batch, const crt_mesh_model* models, uint32_t n_models);
+/* Build parameters (ploc_radius, sort_digit_bits) and trace parameters
+ * (trace_block 128/256/512, stack_depth 64 or 1024) of this batch. */
+crt_status crt_batch_set_config(crt_batch* batch, const crt_config* cfg);
+crt_status crt_batch_get_config(const crt_batch* batch, crt_config* cfg);
+/* tris, rays, hits: device memory. */
+crt_status crt_batch_build(crt_ctx* ctx, crt_batch* batch, const crt_triangle* tris);
+crt_status crt_batch_trace(crt_ctx* ctx, crt_batch* batch, const crt_ray* rays, uint32_t flags, crt_hit* hits);
+/* Build + trace; use_graph != 0 captures the sequence into a CUDA graph on
+ * first use (per argument set) and replays it.  *graph_used (optional)
+ * reports whether the graph path ran. */
+crt_status crt_batch_run(crt_ctx* ctx, crt_batch* batch, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
+                         crt_hit* hits, int use_graph, int* graph_used);
+crt_status crt_batch_copy_nodes(crt_ctx* ctx, const crt_batch* batch, uint32_t scene, crt_bvh_node* dst);
+/* info[0] = triangles, [1] = rays, [2] = PLOC iterations, [3] = first triangle (concatenated index). */
+crt_status crt_batch_scene_info(const crt_batch* batch, uint32_t scene, uint32_t info[4]);
+/* Project-written autotuner: times build + trace for PLOC radius {8, 16, 32}
+ * x digit width {4, 8}, then the trace for block {128, 256, 512} x stack
+ * {64 when the trees allow, 1024}; keeps the fastest in the batch and
+ * returns it (and its build + trace ms). */
+crt_status crt_batch_autotune(crt_ctx* ctx, crt_batch* batch, const crt_triangle* tris, const crt_ray* rays,
+                              uint32_t flags, crt_hit* hits, crt_config* best, float* best_ms);
+
 /* ---- allocation-free Morton + sort ------------------------------------
  * No counterpart in the reference (its build allocates std::vectors freely).
  * For callers that must not have this library allocate device memory — e.g.

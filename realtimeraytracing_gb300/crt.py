@@ -39,6 +39,9 @@ EXPORTS = [
     "crt_morton_sort_noalloc", "crt_predictor_default_config", "crt_predictor_create", "crt_predictor_destroy",
     "crt_predictor_retarget", "crt_predictor_train", "crt_predictor_infer", "crt_predictor_classes_of_hits",
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
+    "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
+    "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
+    "crt_batch_autotune",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -113,6 +116,17 @@ def lib():
             "crt_predictor_info": ([vp, vp], i32),
             "crt_bounce_rays": ([vp, vp, vp, vp, u32, u32, u32, vp], i32),
             "crt_trace_seeded": ([vp, vp, vp, u32, u32, vp, vp], i32),
+            "crt_batch_create": ([vp, vp, vp, u32, C.POINTER(vp)], i32),
+            "crt_batch_free": ([vp], i32),
+            "crt_batch_set_models": ([vp, vp, vp, u32], i32),
+            "crt_batch_set_config": ([vp, vp], i32),
+            "crt_batch_get_config": ([vp, vp], i32),
+            "crt_batch_build": ([vp, vp, vp], i32),
+            "crt_batch_trace": ([vp, vp, vp, u32, vp], i32),
+            "crt_batch_run": ([vp, vp, vp, vp, u32, vp, i32, vp], i32),
+            "crt_batch_copy_nodes": ([vp, vp, u32, vp], i32),
+            "crt_batch_scene_info": ([vp, u32, vp], i32),
+            "crt_batch_autotune": ([vp, vp, vp, vp, u32, vp, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -209,6 +223,79 @@ class Predictor:
     def free(self):
         if self.handle:
             lib().crt_predictor_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many scenes built and traced with one launch per stage (crt_batch).
+    Triangles, rays and hits are concatenated in scene order on the device."""
+
+    def __init__(self, ctx: "Context", tri_counts, ray_counts, models=None):
+        tc = np.ascontiguousarray(tri_counts, np.uint32)
+        rc = np.ascontiguousarray(ray_counts, np.uint32)
+        assert tc.shape == rc.shape
+        h = C.c_void_p()
+        _check(lib().crt_batch_create(ctx.handle, _ptr(tc), _ptr(rc), tc.shape[0], C.byref(h)))
+        self.ctx, self.handle, self.n_scenes = ctx, h, int(tc.shape[0])
+        self.tri_counts, self.ray_counts = tc, rc
+        if models is not None:
+            self.set_models(models)
+
+    def set_models(self, models):
+        m = np.ascontiguousarray(models, np.float32)
+        _check(lib().crt_batch_set_models(self.ctx.handle, self.handle, _ptr(m), m.shape[0]))
+
+    def config(self) -> dict:
+        c = Config()
+        _check(lib().crt_batch_get_config(self.handle, C.byref(c)))
+        return {f: getattr(c, f) for f, _ in Config._fields_}
+
+    def set_config(self, ploc_radius=16, sort_digit_bits=8, trace_block=128, stack_depth=64):
+        c = Config()
+        lib().crt_default_config(C.byref(c))
+        c.ploc_radius, c.sort_digit_bits, c.trace_block, c.stack_depth = ploc_radius, sort_digit_bits, trace_block, stack_depth
+        _check(lib().crt_batch_set_config(self.handle, C.byref(c)))
+
+    def build(self, tris):
+        _check(lib().crt_batch_build(self.ctx.handle, self.handle, _ptr(tris)))
+
+    def trace(self, rays, hits, flags: int = 0):
+        _check(lib().crt_batch_trace(self.ctx.handle, self.handle, _ptr(rays), flags, _ptr(hits)))
+        return hits
+
+    def run(self, tris, rays, hits, flags: int = 0, graph: bool = True) -> bool:
+        used = C.c_int()
+        _check(lib().crt_batch_run(self.ctx.handle, self.handle, _ptr(tris), _ptr(rays), flags, _ptr(hits),
+                                   1 if graph else 0, C.byref(used)))
+        return bool(used.value)
+
+    def nodes(self, scene: int):
+        n = int(self.tri_counts[scene])
+        out = np.empty((2 * n - 1, 12), np.float32)
+        _check(lib().crt_batch_copy_nodes(self.ctx.handle, self.handle, scene, _ptr(out)))
+        return out
+
+    def scene_info(self, scene: int) -> dict:
+        out = np.zeros(4, np.uint32)
+        _check(lib().crt_batch_scene_info(self.handle, scene, _ptr(out)))
+        return {"tris": int(out[0]), "rays": int(out[1]), "iterations": int(out[2]), "tri_off": int(out[3])}
+
+    def autotune(self, tris, rays, hits, flags: int = 0):
+        c = Config()
+        ms = C.c_float()
+        _check(lib().crt_batch_autotune(self.ctx.handle, self.handle, _ptr(tris), _ptr(rays), flags, _ptr(hits),
+                                        C.byref(c), C.byref(ms)))
+        return {f: getattr(c, f) for f, _ in Config._fields_}, ms.value
+
+    def free(self):
+        if self.handle:
+            lib().crt_batch_free(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -985,3 +985,406 @@ crt_status crt_bounce_rays(crt_ctx* x, const crt_bvh* b, const crt_ray* primary,
 }
 
 }  // extern "C"
+
+// ===================================================================== batches
+struct crt_batch {
+    crt_ctx* ctx = nullptr;
+    uint32_t n_scenes = 0;
+    uint32_t n_tris = 0, n_rays = 0;
+    std::vector<crt::BatchScene> hs;
+    std::vector<uint32_t> tri_off, ray_off;
+    uint32_t n_chunks = 0, lb_cap = 0, max_n = 0, max_iters = 0;
+    crt_config cfg{};
+    DevBuf scenes, seg_off, seg_hist, chunks, states, models, err;
+    DevBuf codes_a, codes_b, vals_a, vals_b, codes, perm_global, perm_local;
+    DevBuf node_box, node_lc, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
+    DevBuf nodes, wide, depth_odd, xtri, inv_perm;
+    bool models_set = false;
+    cudaGraphExec_t graph = nullptr;
+    const void* g_tris = nullptr;
+    const void* g_rays = nullptr;
+    const void* g_hits = nullptr;
+    uint32_t g_flags = 0;
+    crt_config g_cfg{};
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+};
+
+namespace {
+
+crt_status batch_upload_models(crt_ctx* x, crt_batch* bt, const crt_mesh_model* models, uint32_t n_models) {
+    std::vector<float> hm(2 * 64 * 16);
+    for (uint32_t m = 0; m < 64; ++m) {
+        for (int k = 0; k < 16; ++k) hm[16 * m + k] = (k % 5 == 0) ? 1.f : 0.f;
+        if (models && m < n_models) std::memcpy(&hm[16 * m], models[m].m, 64);
+    }
+    const volatile float third = 1.f / 3.f;
+    for (int k = 0; k < 64 * 16; ++k) hm[64 * 16 + k] = third * hm[k];
+    CRT_CUDA(cudaMemcpy(bt->models.p, hm.data(), hm.size() * 4, cudaMemcpyHostToDevice));
+    bt->models_set = true;
+    (void)x;
+    return CRT_OK;
+}
+
+// Enqueue build (and trace when rays != null) without synchronising.
+crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
+                         crt_hit* hits, cudaEvent_t ev_built) {
+    cudaStream_t s = x->stream;
+    const int bits = static_cast<int>(bt->cfg.sort_digit_bits);
+    const int passes = (30 + bits - 1) / bits;
+    const uint32_t radix = 1u << bits;
+    const uint32_t tiles = (bt->n_tris + crt::sort_tile_keys(bits) - 1) / crt::sort_tile_keys(bits);
+    const size_t lb_words = static_cast<size_t>(tiles) * 256 + 1;  // per pass (room for 256-digit scene pass)
+    uint32_t* err = bt->err.as<uint32_t>();
+    CRT_CUDA(cudaMemsetAsync(bt->err.p, 0, 16, s));
+    CRT_CUDA(cudaMemsetAsync(bt->states.p, 0, crt::batch_box_state_bytes() * bt->n_scenes, s));
+    CRT_CUDA(cudaMemsetAsync(bt->hist.p, 0, 4ull * passes * radix, s));
+    CRT_CUDA(cudaMemsetAsync(bt->sort_lb.p, 0, 4ull * (passes + 1) * lb_words, s));
+    CRT_CUDA(cudaMemsetAsync(bt->ploc_lb.p, 0, 8ull * 2 * bt->lb_cap + 32, s));
+    crt::launch_batch_box(tris, bt->chunks.p, bt->n_chunks, bt->models.as<float>(), bt->states.p,
+                          bt->scenes.as<crt::BatchScene>(), err, s);
+    crt::launch_batch_morton(tris, bt->chunks.p, bt->n_chunks, bt->models.as<float>() + 64 * 16, bt->states.p,
+                             bt->codes_a.as<uint32_t>(), bt->hist.as<uint32_t>(), bits, s);
+    uint32_t* kin = bt->codes_a.as<uint32_t>();
+    uint32_t* vin = nullptr;
+    for (int p = 0; p < passes; ++p) {
+        uint32_t* kout = (p & 1) ? bt->codes_a.as<uint32_t>() : bt->codes_b.as<uint32_t>();
+        uint32_t* vout = (p & 1) ? bt->vals_a.as<uint32_t>() : bt->vals_b.as<uint32_t>();
+        uint32_t* lb = bt->sort_lb.as<uint32_t>() + static_cast<size_t>(p) * lb_words;
+        crt::launch_onesweep(kin, vin, kout, vout, bt->n_tris, p * bits, bits, bt->hist.as<uint32_t>() + p * radix, lb + 1,
+                             lb, err, x->cfg.spin_limit, s);
+        kin = kout;
+        vin = vout;
+    }
+    {
+        uint32_t* lb = bt->sort_lb.as<uint32_t>() + static_cast<size_t>(passes) * lb_words;
+        crt::launch_onesweep_segments(kin, vin, bt->codes.as<uint32_t>(), bt->perm_global.as<uint32_t>(), bt->n_tris,
+                                      bt->seg_off.as<uint32_t>(), bt->n_scenes, bt->seg_hist.as<uint32_t>(), lb + 1, lb,
+                                      err, x->cfg.spin_limit, s);
+    }
+    crt::launch_batch_leaf_init(tris, bt->n_tris, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->models.as<float>(),
+                                bt->perm_global.as<uint32_t>(), bt->perm_local.as<uint32_t>(), bt->node_box.as<float4>(),
+                                bt->clus_a.as<float4>(), bt->xtri.as<float4>(), bt->inv_perm.as<uint32_t>(),
+                                bt->it.as<uint2>(), bt->nodes.as<crt_bvh_node>(), err, s);
+    {
+        unsigned long long* lb = bt->ploc_lb.as<unsigned long long>();
+        uint32_t* tail = reinterpret_cast<uint32_t*>(lb + 2ull * bt->lb_cap);
+        const cudaError_t e = crt::launch_batch_ploc(
+            bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->clus_a.as<float4>(), bt->clus_b.as<float4>(),
+            bt->node_box.as<float4>(), bt->node_lc.as<uint32_t>(), bt->it.as<uint2>(), static_cast<int>(bt->cfg.ploc_radius),
+            lb, bt->lb_cap, tail, bt->pf.as<uint2>(), bt->nodes.as<crt_bvh_node>(), bt->wide.as<float4>(),
+            bt->depth_odd.as<uint8_t>(), tail + 2, bt->max_n + 1, err, x->cfg.spin_limit, s);
+        if (e != cudaSuccess) return fail(CRT_ERR_UNSUPPORTED, "batched PLOC launch failed: %s", cudaGetErrorString(e));
+    }
+    CRT_CUDA(cudaGetLastError());
+    if (ev_built) CRT_CUDA(cudaEventRecord(ev_built, s));
+    if (rays) {
+        crt::TraceParams p{};
+        p.nodes = bt->nodes.as<crt_bvh_node>();
+        p.wide = bt->wide.as<float4>();
+        p.xtri = bt->xtri.as<float4>();
+        p.rays = rays;
+        p.hits = hits;
+        p.n_rays = bt->n_rays;
+        p.err = err;
+        crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
+                                flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block),
+                                bt->cfg.stack_depth > 64, s);
+        CRT_CUDA(cudaGetLastError());
+    }
+    return CRT_OK;
+}
+
+crt_status batch_check(crt_ctx* x, crt_batch* bt) {
+    uint32_t ew[4] = {0, 0, 0, 0};
+    CRT_CUDA(cudaMemcpyAsync(ew, bt->err.p, 16, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaMemcpyAsync(bt->hs.data(), bt->scenes.p, sizeof(crt::BatchScene) * bt->n_scenes, cudaMemcpyDeviceToHost,
+                             x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    bt->max_iters = 0;
+    for (const auto& sc : bt->hs) bt->max_iters = std::max(bt->max_iters, sc.iters);
+    if (ew[0] & crt::kDevTimeout) return fail(CRT_ERR_DEVICE_TIMEOUT, "batch: a bounded device wait gave up");
+    if (ew[0] & crt::kDevBadModel) return fail(CRT_ERR_BAD_INPUT, "batch: a triangle references model id >= 64");
+    if (ew[0] & crt::kDevStackOverflow)
+        return fail(CRT_ERR_STACK_OVERFLOW, "batch: a ray overflowed its traversal stack (use stack_depth 1024)");
+    if (ew[0]) return fail(CRT_ERR_CUDA, "batch: device error word 0x%x (site %u, %u, %u)", ew[0], ew[1], ew[2], ew[3]);
+    return CRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32_t* ray_counts, uint32_t n_scenes,
+                            crt_batch** out) {
+    if (!x || !tri_counts || !ray_counts || !out) return fail(CRT_ERR_INVALID_ARG, "crt_batch_create: null argument");
+    if (n_scenes == 0 || n_scenes > crt::kMaxBatchScenes)
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_create: 1 to %u scenes", crt::kMaxBatchScenes);
+    CRT_CUDA(cudaSetDevice(x->device));
+    crt_batch* bt = new crt_batch();
+    bt->ctx = x;
+    bt->n_scenes = n_scenes;
+    bt->cfg = x->cfg;
+    bt->cfg.stack_depth = 64;
+    uint64_t nt = 0, nr = 0, lb = 0;
+    std::vector<crt::BatchScene> hs(n_scenes);
+    std::vector<uint32_t> chunks;
+    for (uint32_t k = 0; k < n_scenes; ++k) {
+        if (tri_counts[k] == 0) { delete bt; return fail(CRT_ERR_INVALID_ARG, "crt_batch_create: empty scene %u", k); }
+        hs[k] = crt::BatchScene{};
+        hs[k].tri_off = static_cast<uint32_t>(nt);
+        hs[k].n_tris = tri_counts[k];
+        hs[k].node_off = static_cast<uint32_t>(2 * nt - k);
+        hs[k].wide_off = static_cast<uint32_t>(nt - k);
+        hs[k].ray_off = static_cast<uint32_t>(nr);
+        hs[k].n_rays = ray_counts[k];
+        hs[k].it_off = static_cast<uint32_t>(nt + 2ull * k);
+        hs[k].lb_off = static_cast<uint32_t>(lb);
+        lb += (tri_counts[k] + crt::kPlocTile - 1) / crt::kPlocTile;
+        const uint32_t ck = crt::batch_box_chunk();
+        hs[k].n_chunks = static_cast<uint32_t>((tri_counts[k] + ck - 1) / ck);
+        for (uint64_t b = 0; b < tri_counts[k]; b += ck) {
+            chunks.push_back(k);
+            chunks.push_back(static_cast<uint32_t>(nt + b));
+            chunks.push_back(static_cast<uint32_t>(nt + std::min<uint64_t>(tri_counts[k], b + ck)));
+            chunks.push_back(0);
+        }
+        bt->max_n = std::max(bt->max_n, tri_counts[k]);
+        nt += tri_counts[k];
+        nr += ray_counts[k];
+    }
+    if (nt >= (1ull << 30) || nr >= (1ull << 31)) { delete bt; return fail(CRT_ERR_INVALID_ARG, "crt_batch_create: too large"); }
+    bt->n_tris = static_cast<uint32_t>(nt);
+    bt->n_rays = static_cast<uint32_t>(nr);
+    bt->hs = hs;
+    bt->n_chunks = static_cast<uint32_t>(chunks.size() / 4);
+    bt->lb_cap = static_cast<uint32_t>(lb);
+    const uint32_t N = bt->n_tris;
+    const uint32_t max_tiles = (N + crt::sort_tile_keys(4) - 1) / crt::sort_tile_keys(4);
+    crt_status st = CRT_OK;
+    auto R = [&](DevBuf& b, size_t bytes) { if (st == CRT_OK) st = b.reserve(bytes); };
+    R(bt->scenes, sizeof(crt::BatchScene) * n_scenes);
+    R(bt->seg_off, 4ull * (n_scenes + 1));
+    R(bt->seg_hist, 4ull * 256);
+    R(bt->chunks, crt::batch_chunk_bytes() * bt->n_chunks);
+    R(bt->states, crt::batch_box_state_bytes() * n_scenes);
+    R(bt->models, 2 * 64 * 16 * 4);
+    R(bt->err, 16);
+    for (DevBuf* b : {&bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global, &bt->perm_local,
+                      &bt->node_lc, &bt->inv_perm})
+        R(*b, 4ull * N);
+    R(bt->node_box, 32ull * (2ull * N));
+    R(bt->pf, 8ull * N);
+    R(bt->clus_a, 32ull * N);
+    R(bt->clus_b, 32ull * N);
+    R(bt->it, 8ull * (N + 2ull * n_scenes + 2));
+    R(bt->ploc_lb, 8ull * 2 * bt->lb_cap + 32);
+    R(bt->hist, 4ull * 8 * 256);
+    R(bt->sort_lb, 4ull * 9 * (static_cast<size_t>(max_tiles) * 256 + 1));
+    R(bt->nodes, sizeof(crt_bvh_node) * 2ull * N);
+    R(bt->wide, 64ull * N);
+    R(bt->depth_odd, N);
+    R(bt->xtri, 48ull * N);
+    if (st != CRT_OK) { crt_batch_free(bt); return st; }
+    std::vector<uint32_t> seg(n_scenes + 1), segh(256, 0);
+    for (uint32_t k = 0; k < n_scenes; ++k) { seg[k] = hs[k].tri_off; segh[k] = hs[k].n_tris; }
+    seg[n_scenes] = N;
+    bt->tri_off = seg;
+    st = CRT_OK;
+    if (cudaMemcpy(bt->scenes.p, hs.data(), sizeof(crt::BatchScene) * n_scenes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(bt->seg_off.p, seg.data(), 4ull * seg.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(bt->seg_hist.p, segh.data(), 4ull * 256, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(bt->chunks.p, chunks.data(), 4ull * chunks.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        crt_batch_free(bt);
+        return fail(CRT_ERR_CUDA, "crt_batch_create: upload failed");
+    }
+    CRT_TRY(batch_upload_models(x, bt, nullptr, 0));
+    bt->models_set = false;
+    *out = bt;
+    return CRT_OK;
+}
+
+crt_status crt_batch_free(crt_batch* bt) {
+    if (!bt) return CRT_OK;
+    bt->drop_graph();
+    DevBuf* bufs[] = {&bt->scenes, &bt->seg_off, &bt->seg_hist, &bt->chunks, &bt->states, &bt->models, &bt->err,
+                      &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
+                      &bt->perm_local, &bt->node_box, &bt->node_lc, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
+                      &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->depth_odd, &bt->xtri,
+                      &bt->inv_perm};
+    for (DevBuf* b : bufs) b->release();
+    delete bt;
+    return CRT_OK;
+}
+
+crt_status crt_batch_set_models(crt_ctx* x, crt_batch* bt, const crt_mesh_model* models, uint32_t n_models) {
+    if (!x || !bt) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    if (n_models > 64 || (n_models && !models)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_set_models: bad models");
+    bt->drop_graph();
+    return batch_upload_models(x, bt, models, n_models);
+}
+
+crt_status crt_batch_set_config(crt_batch* bt, const crt_config* cfg) {
+    if (!bt || !cfg) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    if (cfg->ploc_radius == 0 || cfg->ploc_radius > static_cast<uint32_t>(crt::kPlocMaxRadius) ||
+        (cfg->sort_digit_bits != 4 && cfg->sort_digit_bits != 8) ||
+        (cfg->trace_block != 128 && cfg->trace_block != 256 && cfg->trace_block != 512))
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_set_config: unsupported parameters");
+    bt->cfg.ploc_radius = cfg->ploc_radius;
+    bt->cfg.sort_digit_bits = cfg->sort_digit_bits;
+    bt->cfg.trace_block = cfg->trace_block;
+    bt->cfg.stack_depth = cfg->stack_depth > 64 ? 1024 : 64;
+    bt->drop_graph();
+    return CRT_OK;
+}
+
+crt_status crt_batch_get_config(const crt_batch* bt, crt_config* cfg) {
+    if (!bt || !cfg) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    *cfg = bt->cfg;
+    return CRT_OK;
+}
+
+crt_status crt_batch_build(crt_ctx* x, crt_batch* bt, const crt_triangle* tris) {
+    if (!x || !bt || !tris) return fail(CRT_ERR_INVALID_ARG, "crt_batch_build: null argument");
+    if (!is_device_ptr(tris)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_build: triangles must be device memory");
+    CRT_CUDA(cudaSetDevice(x->device));
+    CRT_TRY(batch_enqueue(x, bt, tris, nullptr, 0, nullptr, nullptr));
+    return batch_check(x, bt);
+}
+
+crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint32_t flags, crt_hit* hits) {
+    if (!x || !bt || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: null argument");
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: unsupported flags");
+    if (!is_device_ptr(rays) || !is_device_ptr(hits)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: device memory only");
+    CRT_CUDA(cudaSetDevice(x->device));
+    CRT_CUDA(cudaMemsetAsync(bt->err.p, 0, 16, x->stream));
+    crt::TraceParams p{};
+    p.nodes = bt->nodes.as<crt_bvh_node>();
+    p.wide = bt->wide.as<float4>();
+    p.xtri = bt->xtri.as<float4>();
+    p.rays = rays;
+    p.hits = hits;
+    p.n_rays = bt->n_rays;
+    p.err = bt->err.as<uint32_t>();
+    const bool deep = bt->cfg.stack_depth > 64 || bt->max_iters + 2 > 64;
+    crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays, flags,
+                            static_cast<int>(bt->cfg.trace_block), deep, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    return batch_check(x, bt);
+}
+
+crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
+                         crt_hit* hits, int use_graph, int* graph_used) {
+    if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: null argument");
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: unsupported flags");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (graph_used) *graph_used = 0;
+    if (bt->max_iters + 2 > 64) bt->cfg.stack_depth = 1024;
+    if (use_graph) {
+        const bool same = bt->graph && bt->g_tris == tris && bt->g_rays == rays && bt->g_hits == hits &&
+                          bt->g_flags == flags && std::memcmp(&bt->g_cfg, &bt->cfg, sizeof(crt_config)) == 0;
+        if (!same) {
+            bt->drop_graph();
+            cudaGraph_t g = nullptr;
+            bool ok = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            crt_status es = CRT_OK;
+            if (ok) es = batch_enqueue(x, bt, tris, rays, flags, hits, nullptr);
+            cudaError_t ce = cudaStreamEndCapture(x->stream, &g);
+            ok = ok && es == CRT_OK && ce == cudaSuccess && g != nullptr;
+            if (ok) ok = cudaGraphInstantiate(&bt->graph, g, 0) == cudaSuccess;
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (!ok) {
+                bt->graph = nullptr;
+            } else {
+                bt->g_tris = tris; bt->g_rays = rays; bt->g_hits = hits; bt->g_flags = flags; bt->g_cfg = bt->cfg;
+            }
+        }
+        if (bt->graph) {
+            CRT_CUDA(cudaGraphLaunch(bt->graph, x->stream));
+            if (graph_used) *graph_used = 1;
+            return batch_check(x, bt);
+        }
+    }
+    CRT_TRY(batch_enqueue(x, bt, tris, rays, flags, hits, nullptr));
+    return batch_check(x, bt);
+}
+
+crt_status crt_batch_copy_nodes(crt_ctx* x, const crt_batch* bt, uint32_t scene, crt_bvh_node* dst) {
+    if (!x || !bt || !dst || scene >= bt->n_scenes) return fail(CRT_ERR_INVALID_ARG, "crt_batch_copy_nodes: bad argument");
+    const crt::BatchScene& sc = bt->hs[scene];
+    return copy_out(x, dst, bt->nodes.as<crt_bvh_node>() + sc.node_off, sizeof(crt_bvh_node) * (2ull * sc.n_tris - 1));
+}
+
+crt_status crt_batch_scene_info(const crt_batch* bt, uint32_t scene, uint32_t info[4]) {
+    if (!bt || !info || scene >= bt->n_scenes) return fail(CRT_ERR_INVALID_ARG, "crt_batch_scene_info: bad argument");
+    const crt::BatchScene& sc = bt->hs[scene];
+    info[0] = sc.n_tris;
+    info[1] = sc.n_rays;
+    info[2] = sc.n_tris > 1 ? sc.iters : 0;
+    info[3] = sc.tri_off;
+    return CRT_OK;
+}
+
+crt_status crt_batch_autotune(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
+                              crt_hit* hits, crt_config* best, float* best_ms) {
+    if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_autotune: null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    cudaEvent_t e0, e1, e2;
+    CRT_CUDA(cudaEventCreate(&e0));
+    CRT_CUDA(cudaEventCreate(&e1));
+    CRT_CUDA(cudaEventCreate(&e2));
+    const crt_config start = bt->cfg;
+    crt_config bestc = start;
+    float best_total = 1e30f, best_build = 0.f;
+    auto run = [&](float* ms_build, float* ms_total) -> crt_status {
+        CRT_CUDA(cudaEventRecord(e0, x->stream));
+        CRT_TRY(batch_enqueue(x, bt, tris, rays, flags, hits, e1));
+        CRT_CUDA(cudaEventRecord(e2, x->stream));
+        CRT_TRY(batch_check(x, bt));
+        CRT_CUDA(cudaEventElapsedTime(ms_build, e0, e1));
+        CRT_CUDA(cudaEventElapsedTime(ms_total, e0, e2));
+        return CRT_OK;
+    };
+    // build parameters (with the default trace shape)
+    for (uint32_t radius : {8u, 16u, 32u})
+        for (uint32_t bits : {4u, 8u}) {
+            bt->cfg = start;
+            bt->cfg.ploc_radius = radius;
+            bt->cfg.sort_digit_bits = bits;
+            bt->cfg.trace_block = 128;
+            bt->cfg.stack_depth = 1024;
+            float b = 0.f, t = 0.f;
+            CRT_TRY(run(&b, &t));  // warm-up (also sizes the trees)
+            CRT_TRY(run(&b, &t));
+            if (t < best_total) { best_total = t; best_build = b; bestc = bt->cfg; }
+        }
+    // trace parameters on the chosen build
+    bt->cfg = bestc;
+    float b = 0.f, t = 0.f;
+    CRT_TRY(run(&b, &t));
+    const bool shallow = bt->max_iters + 2 <= 64;
+    float best_trace = 1e30f;
+    crt_config bt_cfg = bestc;
+    for (uint32_t block : {128u, 256u, 512u})
+        for (uint32_t stack : {64u, 1024u}) {
+            if (stack == 64 && !shallow) continue;
+            bt->cfg.trace_block = block;
+            bt->cfg.stack_depth = stack;
+            CRT_TRY(run(&b, &t));
+            CRT_TRY(run(&b, &t));
+            if (t - b < best_trace) { best_trace = t - b; bt_cfg = bt->cfg; }
+        }
+    bt->cfg = bt_cfg;
+    bt->drop_graph();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (best) *best = bt->cfg;
+    if (best_ms) *best_ms = best_build + best_trace;
+    return CRT_OK;
+}
+
+}  // extern "C"

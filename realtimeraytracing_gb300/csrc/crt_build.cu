@@ -183,13 +183,17 @@ __global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restr
 // pairs (bvh.cpp:214-232).
 constexpr uint32_t kLbAgg = 1u << 30, kLbPrefix = 2u << 30, kLbMask = (1u << 30) - 1u;
 
-template <int BITS, int BLOCK, int KPT>
+// SEG: the digit is not taken from the key but is the segment (scene) whose
+// range [seg_off[d], seg_off[d+1]) holds the value — one extra stable pass
+// that groups concatenated scenes back together after the code passes.
+template <int BITS, int BLOCK, int KPT, bool SEG>
 __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restrict__ keys_in,
                                                          const uint32_t* __restrict__ vals_in,
                                                          uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                          uint32_t n, int shift, const uint32_t* __restrict__ pass_hist,
                                                          uint32_t* lookback, uint32_t* ticket, uint32_t* err,
-                                                         uint32_t spin_limit) {
+                                                         uint32_t spin_limit, const uint32_t* __restrict__ seg_off,
+                                                         uint32_t n_seg) {
     constexpr int RADIX = 1 << BITS;
     constexpr int WARPS = BLOCK / 32;
     constexpr int TILE = BLOCK * KPT;
@@ -202,10 +206,22 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restr
     __shared__ uint32_t s_scan[BLOCK / 32];
     __shared__ uint32_t s_tile;
 
+    __shared__ uint32_t s_seg[SEG ? RADIX + 1 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
     for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) (&s_whist[0][0])[i] = 0u;
+    if (SEG)
+        for (int i = threadIdx.x; i <= RADIX; i += BLOCK) s_seg[i] = (static_cast<uint32_t>(i) <= n_seg) ? seg_off[i] : 0xFFFFFFFFu;
     __syncthreads();
+    auto digit_of = [&](uint32_t key, uint32_t val) -> uint32_t {
+        if (!SEG) return (key >> shift) & (RADIX - 1);
+        uint32_t lo = 0, hi = n_seg - 1;  // last segment start <= val
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (s_seg[mid] <= val) lo = mid; else hi = mid - 1;
+        }
+        return lo;
+    };
     const uint32_t tile = s_tile;
     const uint64_t tile_base = static_cast<uint64_t>(tile) * TILE;
     if (tile_base >= n) return;
@@ -225,7 +241,7 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restr
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
         const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
-        const uint32_t d = (idx < n) ? ((key[j] >> shift) & (RADIX - 1)) : static_cast<uint32_t>(RADIX);
+        const uint32_t d = (idx < n) ? digit_of(key[j], val[j]) : static_cast<uint32_t>(RADIX);
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
@@ -299,7 +315,7 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restr
     for (int j = 0; j < KPT; ++j) {
         const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
         if (idx < n) {
-            const uint32_t dd = (key[j] >> shift) & (RADIX - 1);
+            const uint32_t dd = digit_of(key[j], val[j]);
             const uint32_t p = s_start[dd] + s_whist[warp][dd] + rank[j];
             s_keys[p] = key[j];
             s_vals[p] = val[j];
@@ -308,7 +324,7 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restr
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < tile_n; i += BLOCK) {
         const uint32_t k = s_keys[i];
-        const uint32_t dd = (k >> shift) & (RADIX - 1);
+        const uint32_t dd = digit_of(k, s_vals[i]);
         const uint32_t dst = s_dest[dd] + (i - s_start[dd]);
         keys_out[dst] = k;
         vals_out[dst] = s_vals[i];
@@ -764,11 +780,19 @@ void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t*
                      uint32_t spin_limit, cudaStream_t s) {
     const uint32_t tiles = (n + sort_tile_keys(bits) - 1) / sort_tile_keys(bits);
     if (bits == 4)
-        onesweep_kernel<4, 256, 16><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, pass_hist,
-                                                           lookback, ticket, err, spin_limit);
+        onesweep_kernel<4, 256, 16, false><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
+                                                                  pass_hist, lookback, ticket, err, spin_limit, nullptr, 0);
     else
-        onesweep_kernel<8, 256, 16><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, pass_hist,
-                                                           lookback, ticket, err, spin_limit);
+        onesweep_kernel<8, 256, 16, false><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
+                                                                  pass_hist, lookback, ticket, err, spin_limit, nullptr, 0);
+}
+
+void launch_onesweep_segments(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                              uint32_t n, const uint32_t* seg_off, uint32_t n_seg, const uint32_t* seg_hist,
+                              uint32_t* lookback, uint32_t* ticket, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+    const uint32_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
+    onesweep_kernel<8, 256, 16, true><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, 0, seg_hist,
+                                                             lookback, ticket, err, spin_limit, seg_off, n_seg);
 }
 
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
@@ -830,3 +854,5 @@ void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t 
 }
 
 }  // namespace crt
+
+#include "crt_batch_kernels.cuh"

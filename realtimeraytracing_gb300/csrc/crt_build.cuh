@@ -36,6 +36,10 @@ uint32_t sort_tile_keys(int bits);
 void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, uint32_t n,
                      int shift, int bits, const uint32_t* pass_hist, uint32_t* lookback, uint32_t* ticket, uint32_t* err,
                      uint32_t spin_limit, cudaStream_t s);
+// One stable pass whose digit is the segment holding each value (n_seg <= 256).
+void launch_onesweep_segments(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                              uint32_t n, const uint32_t* seg_off, uint32_t n_seg, const uint32_t* seg_hist,
+                              uint32_t* lookback, uint32_t* ticket, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
                       float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, uint32_t* err, cudaStream_t s);
 void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,
@@ -74,6 +78,42 @@ struct TraceParams {
     const uint32_t* n_treelets = nullptr;
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
+
+// Batched scenes: per-scene offsets into the concatenated arrays.
+constexpr uint32_t kMaxBatchScenes = 256;
+struct BatchScene {
+    uint32_t tri_off;     // first triangle / leaf / cluster of the scene
+    uint32_t n_tris;
+    uint32_t node_off;    // 2 * tri_off - scene index: first reference-layout node
+    uint32_t wide_off;    // tri_off - scene index: first binary traversal node
+    uint32_t ray_off;
+    uint32_t n_rays;
+    uint32_t it_off;      // tri_off + 2 * scene index: first PLOC iteration record
+    uint32_t lb_off;      // first PLOC look-back word (per parity)
+    float abs_eps;
+    uint32_t iters;       // PLOC iterations (0 while running)
+    uint32_t n_chunks;    // scene-box chunks of the scene
+    uint32_t pad;
+};
+static_assert(sizeof(BatchScene) == 48, "batch scene record");
+void launch_trace_batch(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t n_rays,
+                        uint32_t flags, int block, bool deep, cudaStream_t s);
+// Batched build stages (crt_batch_kernels.cuh).
+size_t batch_box_state_bytes();
+size_t batch_chunk_bytes();
+uint32_t batch_box_chunk();
+void launch_batch_box(const crt_triangle* tris, const void* chunks, uint32_t n_chunks, const float* models, void* states,
+                      BatchScene* scenes, uint32_t* err, cudaStream_t s);
+void launch_batch_morton(const crt_triangle* tris, const void* chunks, uint32_t n_chunks, const float* models_third,
+                         const void* states, uint32_t* codes, uint32_t* hist, int bits, cudaStream_t s);
+void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchScene* scenes, uint32_t n_scenes,
+                            const float* models, const uint32_t* perm_global, uint32_t* perm_local, float4* node_box,
+                            float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, crt_bvh_node* nodes,
+                            uint32_t* err, cudaStream_t s);
+cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
+                              uint32_t* node_lc, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
+                              uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
+                              unsigned int* bar, uint32_t max_iters, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 // Sets the message crt_last_error_string() returns on the calling thread.
 void set_last_error(const char* msg);
 

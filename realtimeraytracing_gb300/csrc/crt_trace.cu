@@ -160,11 +160,9 @@ __device__ __forceinline__ uint32_t ray_of_thread(uint32_t t, uint32_t width) {
     return ((ty << 2) + (lane >> 3)) * width + (tx << 3) + (lane & 7u);
 }
 
+// Closest hit (or any hit) of ray i of p.rays into p.hits[i].
 template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE>
-__global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
-    const uint32_t t_id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t_id >= p.n_rays) return;
-    const uint32_t i = ray_of_thread(t_id, p.tile_width);
+__device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i) {
     const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
     const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
     RayCtx r;
@@ -365,6 +363,39 @@ __global__ void __launch_bounds__(128) trace_kernel(TraceParams p) {
     }
 }
 
+template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) trace_kernel(TraceParams p) {
+    const uint32_t t_id = blockIdx.x * BLOCK + threadIdx.x;
+    if (t_id >= p.n_rays) return;
+    trace_ray<ANY, WT, STACK, SEED, WIDE>(p, ray_of_thread(t_id, p.tile_width));
+}
+
+// Many scenes in one launch: ray i belongs to the scene whose ray range holds
+// it and is traced against that scene's BVH (same walk as above).
+template <bool ANY, bool WT, int STACK, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, const BatchScene* __restrict__ scenes,
+                                                            uint32_t n_scenes, uint32_t n_rays_total) {
+    __shared__ uint32_t s_ray_off[kMaxBatchScenes + 1];
+    for (uint32_t k = threadIdx.x; k <= n_scenes; k += BLOCK) s_ray_off[k] = scenes[k < n_scenes ? k : n_scenes - 1].ray_off +
+                                                                            (k < n_scenes ? 0u : scenes[n_scenes - 1].n_rays);
+    __syncthreads();
+    const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= n_rays_total) return;
+    uint32_t lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (s_ray_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const BatchScene sc = scenes[lo];
+    TraceParams p = base;
+    p.nodes = base.nodes + sc.node_off;
+    p.wide = base.wide + 4 * static_cast<size_t>(sc.wide_off);
+    p.xtri = base.xtri + 3 * static_cast<size_t>(sc.tri_off);
+    p.n_nodes = 2 * sc.n_tris - 1;
+    p.abs_eps = sc.abs_eps;
+    trace_ray<ANY, WT, STACK, false, false>(p, i);
+}
+
 // getRay (raytracer.glsl:92-100): pos = texel / size, direction =
 // normalize(InvView * vec4((pos - 0.5, 1) * (W, H, near), 1) - eye).
 __global__ void __launch_bounds__(256) raygen_kernel(const crt_camera* __restrict__ cam, uint32_t width, uint32_t height,
@@ -406,20 +437,27 @@ __global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__
     o[1] = make_float4(dx * inv, dy * inv, dz * inv, len);
 }
 
-template <bool ANY, bool WT>
-static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, bool wide, cudaStream_t s) {
-    const uint32_t grid = (p.n_rays + block - 1) / block;
+template <bool ANY, bool WT, int BLOCK>
+static void launch_trace_b(const TraceParams& p, bool deep, bool seed, bool wide, cudaStream_t s) {
+    const uint32_t grid = (p.n_rays + BLOCK - 1) / BLOCK;
     if (grid == 0) return;
     if (seed) {
-        if (deep) trace_kernel<ANY, WT, 1024, true, false><<<grid, block, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 64, true, false><<<grid, block, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, true, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, true, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
     } else if (wide) {
-        if (deep) trace_kernel<ANY, WT, 1024, false, true><<<grid, block, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 96, false, true><<<grid, block, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, false, true, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 96, false, true, BLOCK><<<grid, BLOCK, 0, s>>>(p);
     } else {
-        if (deep) trace_kernel<ANY, WT, 1024, false, false><<<grid, block, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 64, false, false><<<grid, block, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, false, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, false, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
     }
+}
+
+template <bool ANY, bool WT>
+static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, bool wide, cudaStream_t s) {
+    if (block == 256) launch_trace_b<ANY, WT, 256>(p, deep, seed, wide, s);
+    else if (block == 64) launch_trace_b<ANY, WT, 64>(p, deep, seed, wide, s);
+    else launch_trace_b<ANY, WT, 128>(p, deep, seed, wide, s);
 }
 
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s) {
@@ -431,6 +469,32 @@ void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t 
     else if (any) launch_trace_t<true, false>(p, block, deep, seed, wide, s);
     else if (wt) launch_trace_t<false, true>(p, block, deep, seed, wide, s);
     else launch_trace_t<false, false>(p, block, deep, seed, wide, s);
+}
+
+template <bool ANY, bool WT, int BLOCK>
+static void launch_batch_b(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t n_rays,
+                           bool deep, cudaStream_t s) {
+    const uint32_t grid = (n_rays + BLOCK - 1) / BLOCK;
+    if (grid == 0) return;
+    if (deep) trace_batch_kernel<ANY, WT, 1024, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+    else trace_batch_kernel<ANY, WT, 64, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+}
+
+template <bool ANY, bool WT>
+static void launch_batch_t(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t n_rays,
+                           int block, bool deep, cudaStream_t s) {
+    if (block == 512) launch_batch_b<ANY, WT, 512>(p, scenes, n_scenes, n_rays, deep, s);
+    else if (block == 256) launch_batch_b<ANY, WT, 256>(p, scenes, n_scenes, n_rays, deep, s);
+    else launch_batch_b<ANY, WT, 128>(p, scenes, n_scenes, n_rays, deep, s);
+}
+
+void launch_trace_batch(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t n_rays,
+                        uint32_t flags, int block, bool deep, cudaStream_t s) {
+    const bool any = flags & CRT_TRACE_ANY, wt = flags & CRT_TRI_WATERTIGHT;
+    if (any && wt) launch_batch_t<true, true>(p, scenes, n_scenes, n_rays, block, deep, s);
+    else if (any) launch_batch_t<true, false>(p, scenes, n_scenes, n_rays, block, deep, s);
+    else if (wt) launch_batch_t<false, true>(p, scenes, n_scenes, n_rays, block, deep, s);
+    else launch_batch_t<false, false>(p, scenes, n_scenes, n_rays, block, deep, s);
 }
 
 void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s) {

@@ -237,3 +237,35 @@ def config1_scene(seed: int = 0, level: int = 8):
 def config3_scene(seed: int = 0, n: int = 4194304):
     """4M-triangle clustered soup: 256 clusters, sigma 0.02, edges lognormal(ln 0.003, 0.6)."""
     return clustered_soup(n, 256, 0.02, 0.003, 0.6, seed), identity_models(1)
+
+
+def sphere_rays(n: int, seed: int = 0, radius: float = 2.0, center=(0.5, 0.5, 0.5)) -> np.ndarray:
+    """Rays from points uniform on a sphere toward points uniform in the unit cube."""
+    o = np.asarray(center, np.float64) + radius * _unit_vectors(seed, 301, n)
+    target = uniform01(seed, 302, 3 * n).reshape(n, 3)
+    d = target - o
+    d /= np.sqrt((d ** 2).sum(1))[:, None]
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3] = o
+    r[:, 4:7] = d
+    r[:, 7] = np.inf
+    return r
+
+
+def config2_sizes(n_scenes: int = 64, seed: int = 0, tri_range=(1000, 2_000_000), ray_range=(65536, 4_194_304)):
+    """Log-uniform triangle and ray counts of the batched workload."""
+    u = uniform01(seed, 401, n_scenes)
+    v = uniform01(seed, 402, n_scenes)
+    lt, ht = np.log(tri_range[0]), np.log(tri_range[1])
+    lr, hr = np.log(ray_range[0]), np.log(ray_range[1])
+    tris = np.floor(np.exp(lt + u * (ht - lt))).astype(np.int64)
+    rays = np.floor(np.exp(lr + v * (hr - lr))).astype(np.int64)
+    return tris, rays
+
+
+def config2_scene(k: int, n_tris: int, seed: int = 0) -> np.ndarray:
+    """Scene k of the batched workload: even k uniform soups (as config 0),
+    odd k clustered soups (32 blobs, sigma 0.03, edges lognormal(ln 0.005, 0.5))."""
+    if k % 2 == 0:
+        return uniform_soup(int(n_tris), seed=seed * 1000 + k)
+    return clustered_soup(int(n_tris), 32, 0.03, 0.005, 0.5, seed=seed * 1000 + k)
