@@ -253,6 +253,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(tris, models, cam)
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = run_batch_experiment(ctx, torch, crt, dev, args)
     predictor = None
     if rank == 0 and not args.no_predictor:
         del d_tris, bvh
@@ -293,11 +296,86 @@ def run_ours(args):
                          "node_fetches_per_ray": round(visited / n_rays, 2), "tris_per_ray": round(tested / n_rays, 2)},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "batch": batch,
             "predictor": predictor,
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batch_experiment(ctx, torch, crt, dev, args):
+    """Config 2: 64 scenes, triangle counts log-uniform over 1k-2M (even scenes
+    uniform soups, odd scenes 32-blob clustered soups), each with its own
+    log-uniform 64k-4M rays from a radius-2 sphere toward the unit cube.  The
+    whole build + trace runs as one launch per stage, autotuned, replayed
+    from a CUDA graph; the same work as 64 separate crt_build + crt_trace
+    calls is timed beside it."""
+    from realtimeraytracing_gb300 import scenes as S
+    tri_n, ray_n = S.config2_sizes(64, seed=0)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(2)
+    tris = torch.cat([S.device_soup(int(n), gen, clustered=(k % 2 == 1)) for k, n in enumerate(tri_n)])
+    rays = torch.cat([S.device_sphere_rays(int(m), gen) for m in ray_n])
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+    models = S.identity_models(1)
+    b = crt.Batch(ctx, tri_n, ray_n, models=models)
+    flags = crt.TRI_WATERTIGHT
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / reps
+
+    reps = max(3, min(args.steps, 5))
+    b.run(tris, rays, hits, flags, graph=False)
+    t_default = timed(lambda: b.run(tris, rays, hits, flags, graph=True), reps)
+    default_cfg = b.config()
+    cfg, tuned_ms = b.autotune(tris, rays, hits, flags)
+    used = b.run(tris, rays, hits, flags, graph=True)
+    t_graph = timed(lambda: b.run(tris, rays, hits, flags, graph=True), reps)
+    t_nograph = timed(lambda: b.run(tris, rays, hits, flags, graph=False), reps)
+    t_build = timed(lambda: b.build(tris), reps)
+    ref_hits = hits.clone()
+    # the same work scene by scene through the single-scene API
+    c1 = crt.Context(device=dev.index or 0)
+    tri_off = np.concatenate([[0], np.cumsum(tri_n)])
+    ray_off = np.concatenate([[0], np.cumsum(ray_n)])
+    seq_hits = torch.empty_like(hits)
+    bvhs = [None] * 64
+
+    def sequential():
+        for k in range(64):
+            tk = tris[int(tri_off[k]):int(tri_off[k + 1])]
+            if bvhs[k] is None:
+                bvhs[k] = c1.build(tk, models=models)
+            else:
+                bvhs[k].rebuild(tk, models=models)
+            c1.trace(bvhs[k], rays[int(ray_off[k]):int(ray_off[k + 1])], flags,
+                     out=seq_hits[int(ray_off[k]):int(ray_off[k + 1])])
+
+    t_seq = timed(sequential, max(2, reps // 2))
+    identical = bool(torch.equal(seq_hits.view(torch.int32), ref_hits.view(torch.int32)))
+    for bv in bvhs:
+        bv.free()
+    c1.close()
+    b.free()
+    n_rays = int(ray_n.sum())
+    return {
+        "workload": "64 scenes, tris log-uniform 1k-2M (half uniform, half 32-blob clustered), rays log-uniform 64k-4M",
+        "triangles": int(tri_n.sum()), "rays": n_rays,
+        "pipeline_ms": round(t_graph, 3), "mrays_s": round(n_rays / t_graph / 1e3, 1),
+        "pipeline_ms_no_graph": round(t_nograph, 3), "build_ms": round(t_build, 3),
+        "graph_used": used, "default_config_ms": round(t_default, 3),
+        "autotuned": {k: cfg[k] for k in ("ploc_radius", "sort_digit_bits", "trace_block", "stack_depth")},
+        "default_config": {k: default_cfg[k] for k in ("ploc_radius", "sort_digit_bits", "trace_block", "stack_depth")},
+        "sequential_single_scene_ms": round(t_seq, 3), "speedup_vs_sequential": round(t_seq / t_graph, 3),
+        "hits_identical_to_sequential": identical,
+    }
 
 
 def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
@@ -464,6 +542,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-predictor", action="store_true", help="skip the learned-predictor (4M-triangle) experiment")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched experiment")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -269,3 +269,50 @@ def config2_scene(k: int, n_tris: int, seed: int = 0) -> np.ndarray:
     if k % 2 == 0:
         return uniform_soup(int(n_tris), seed=seed * 1000 + k)
     return clustered_soup(int(n_tris), 32, 0.03, 0.005, 0.5, seed=seed * 1000 + k)
+
+
+# ------------------------------------------------- on-device generators (torch)
+# Same distributions as the numpy generators above, drawn on the GPU with a
+# seeded torch generator (reproducible on the same device type); used where
+# host generation of tens of millions of records would dominate a benchmark.
+def _torch():
+    import torch
+    return torch
+
+
+def device_soup(n: int, gen, clustered: bool = False, clusters: int = 32, sigma: float = 0.03,
+                edge_mu: float = 0.005, edge_sigma: float = 0.5):
+    torch = _torch()
+    dev = gen.device
+    if clustered:
+        centres = torch.rand((clusters, 3), generator=gen, device=dev, dtype=torch.float64)
+        which = torch.randint(0, clusters, (n,), generator=gen, device=dev)
+        c = centres[which] + sigma * torch.randn((n, 3), generator=gen, device=dev, dtype=torch.float64)
+    else:
+        c = torch.rand((n, 3), generator=gen, device=dev, dtype=torch.float64)
+    out = torch.zeros((n, 16), dtype=torch.float32, device=dev)
+    for k in range(3):
+        if clustered:
+            L = torch.exp(np.log(edge_mu) + edge_sigma * torch.randn(n, generator=gen, device=dev, dtype=torch.float64))
+        else:
+            L = 0.001 + 0.019 * torch.rand(n, generator=gen, device=dev, dtype=torch.float64)
+        u = torch.randn((n, 3), generator=gen, device=dev, dtype=torch.float64)
+        u /= u.norm(dim=1, keepdim=True).clamp_min(1e-12)
+        out[:, 4 * k:4 * k + 3] = (c + L[:, None] * u).float()
+        out[:, 4 * k + 3] = 1.0
+    return out
+
+
+def device_sphere_rays(n: int, gen, radius: float = 2.0, center=(0.5, 0.5, 0.5)):
+    torch = _torch()
+    dev = gen.device
+    u = torch.randn((n, 3), generator=gen, device=dev, dtype=torch.float64)
+    u /= u.norm(dim=1, keepdim=True).clamp_min(1e-12)
+    o = torch.tensor(center, dtype=torch.float64, device=dev) + radius * u
+    d = torch.rand((n, 3), generator=gen, device=dev, dtype=torch.float64) - o
+    d /= d.norm(dim=1, keepdim=True)
+    r = torch.zeros((n, 8), dtype=torch.float32, device=dev)
+    r[:, 0:3] = o.float()
+    r[:, 4:7] = d.float()
+    r[:, 7] = float("inf")
+    return r
