@@ -256,6 +256,9 @@ def run_ours(args):
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch_experiment(ctx, torch, crt, dev, args)
+    dynamic = None
+    if rank == 0 and not args.no_dynamic:
+        dynamic = run_dynamic_experiment(ctx, torch, crt, dev, args)
     predictor = None
     if rank == 0 and not args.no_predictor:
         del d_tris, bvh
@@ -297,6 +300,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
             "batch": batch,
+            "dynamic": dynamic,
             "predictor": predictor,
         }
         print(json.dumps(line))
@@ -375,6 +379,84 @@ def run_batch_experiment(ctx, torch, crt, dev, args):
         "default_config": {k: default_cfg[k] for k in ("ploc_radius", "sort_digit_bits", "trace_block", "stack_depth")},
         "sequential_single_scene_ms": round(t_seq, 3), "speedup_vs_sequential": round(t_seq / t_graph, 3),
         "hits_identical_to_sequential": identical,
+    }
+
+
+def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
+    """Config 4: a 16,777,216-triangle clustered soup (1024 clusters, sigma
+    0.02, edges lognormal(ln 0.003, 0.6)) animated over 60 frames: every
+    vertex moves by 0.01 sin(2 pi f / 60 + 7 x) along y and the whole PLOC BVH
+    is rebuilt each frame; per frame 1920x1080 primary rays and 2 cosine
+    bounce rays per hit are traced, and the hit predictor is retrained on the
+    frame's exact hits (5%) and used for the bounce rays.  Frame = rebuild +
+    primary + bounce generation + training + seeded bounce trace."""
+    from realtimeraytracing_gb300 import scenes as S
+    n = 16 * 1024 * 1024
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4)
+    base = S.device_soup(n, gen, clustered=True, clusters=1024, sigma=0.02, edge_mu=0.003, edge_sigma=0.6)
+    x0 = base[:, [0, 4, 8]].clone()
+    y0 = base[:, [1, 5, 9]].clone()
+    tris = base.clone()
+    models = torch.from_numpy(S.identity_models(1)).to(dev)
+    cam = torch.from_numpy(S.camera_gpu_data((0.5, 0.5, -1.5), aspect=1920 / 1080)).to(dev)
+    W, H = 1920, 1080
+    hp = torch.empty((W * H, 4), dtype=torch.float32, device=dev)
+    prim = torch.empty((W * H, 8), dtype=torch.float32, device=dev)
+    bvh = ctx.build(tris, models=models)
+    pred = crt.Predictor(ctx, bvh, seed=3)
+    frame_ms, build_ms, sort_ms, plain_ms, seeded_ms, rays_traced = [], [], [], [], [], []
+    identical = True
+    bounce = hb_plain = hb_seed = None
+    for f in range(frames):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tris[:, [1, 5, 9]] = y0 + 0.01 * torch.sin(2 * np.pi * f / 60 + 7 * x0)
+        bvh.rebuild(tris, models=models)
+        st = ctx.last_build_stats()
+        pred.retarget()
+        ctx.raygen(cam, W, H, out=prim)
+        ctx.trace(bvh, prim, crt.TRI_WATERTIGHT, out=hp)
+        n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
+        nb = max(2 * n_hits, 1)
+        if bounce is None or bounce.shape[0] < nb:
+            bounce = torch.empty((nb, 8), dtype=torch.float32, device=dev)
+            hb_plain = torch.empty((nb, 4), dtype=torch.float32, device=dev)
+            hb_seed = torch.empty((nb, 4), dtype=torch.float32, device=dev)
+        br, hs = bounce[:nb], hb_seed[:nb]
+        ctx.bounce_rays(bvh, prim, hp, nb, seed=100 + f, out=br)
+        ts = time.perf_counter()
+        ctx.trace(bvh, br, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR, out=hs)
+        torch.cuda.synchronize()
+        seeded_ms.append((time.perf_counter() - ts) * 1e3)
+        pred.train(br, hs, offset=f % 20)   # retrain on this frame's exact hits
+        torch.cuda.synchronize()
+        frame_ms.append((time.perf_counter() - t0) * 1e3)
+        build_ms.append(st["ms_total"])
+        sort_ms.append(st["ms_sort"])
+        rays_traced.append(W * H + nb)
+        if f % 15 == 0 or f == frames - 1:
+            # plain traversal of the same bounce rays, off the frame clock, for the comparison
+            tp = time.perf_counter()
+            ctx.trace(bvh, br, crt.TRI_WATERTIGHT, out=hb_plain[:nb])
+            torch.cuda.synchronize()
+            plain_ms.append(((time.perf_counter() - tp) * 1e3, seeded_ms[-1], nb))
+            identical = identical and bool(torch.equal(hb_plain[:nb].view(torch.int32), hs.view(torch.int32)))
+    pred.free()
+    bvh.free()
+    fm = np.array(frame_ms[1:])
+    sort_bytes = 16.0 * n * 4 - 4.0 * n  # 4 passes x (8 B in + 8 B out); pass 0 synthesises values
+    return {
+        "workload": "16,777,216-tri clustered soup (1024 clusters), 60 animated frames, full rebuild per frame, "
+                    "1920x1080 primary + 2 bounce rays per hit, predictor retrained per frame",
+        "frames": frames,
+        "frame_ms_p50": round(float(np.percentile(fm, 50)), 3), "frame_ms_p99": round(float(np.percentile(fm, 99)), 3),
+        "build_ms_p50": round(float(np.median(build_ms[1:])), 3),
+        "mrays_s": round(float(sum(rays_traced[1:]) / fm.sum() / 1e3), 1),
+        "sort_ms_p50": round(float(np.median(sort_ms[1:])), 4),
+        "sort_gbs": round(sort_bytes / (float(np.median(sort_ms[1:])) * 1e-3) / 1e9, 1),
+        "bounce_seeded_vs_plain": [{"plain_ms": round(a, 3), "seeded_ms": round(b, 3), "rays": int(c)} for a, b, c in plain_ms],
+        "identical_hits": identical,
     }
 
 
@@ -543,6 +625,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-predictor", action="store_true", help="skip the learned-predictor (4M-triangle) experiment")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched experiment")
+    ap.add_argument("--no-dynamic", action="store_true", help="skip the 16M-triangle 60-frame dynamic experiment")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
