@@ -175,38 +175,58 @@ __global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restr
 
 // ============================================== K2: Onesweep digit binning
 // One stable counting pass over digit (key >> shift) & (RADIX-1) of a tile
-// of BLOCK*KPT keys: warp-level multisplit with __match_any_sync, per-warp
-// digit counters in shared memory, chained-scan decoupled look-back across
-// tiles for the global digit offsets (Adinets & Merrill, "Onesweep", 2022),
-// and a shared-memory staged scatter.  Pass 0 synthesises the values
-// (iota), which makes the result the reference's std::sort of (code, index)
-// pairs (bvh.cpp:214-232).
+// of BLOCK*KPT keys (Adinets & Merrill, "Onesweep", 2022):
+//  * warp multisplit: the lanes holding the same digit are found with BITS
+//    ballots (cheaper than match.any on this part), the highest of them adds
+//    the group's size to the warp's shared-memory digit counter and
+//    broadcasts the old count;
+//  * chained-scan decoupled look-back across tiles for the global digit
+//    offsets; each digit's thread reads a window of LB_WIN predecessor tiles
+//    per round trip with relaxed loads (flag and count share one word);
+//  * a shared-memory staged scatter, first of the digit-carrying array
+//    (keys, or values for SEG) then of the other, so that every warp's
+//    global stores fall in a few contiguous runs.
+// Pass 0 synthesises the values (iota), which makes the result the
+// reference's std::sort of (code, index) pairs (bvh.cpp:214-232).
 constexpr uint32_t kLbAgg = 1u << 30, kLbPrefix = 2u << 30, kLbMask = (1u << 30) - 1u;
+constexpr int kLbWindow = 4;
+
+template <int BITS>
+__device__ __forceinline__ uint32_t ballot_peers(uint32_t d, bool ok) {
+    uint32_t peers = __ballot_sync(0xFFFFFFFFu, ok);
+    if (!ok) peers = ~peers;
+#pragma unroll
+    for (int b = 0; b < BITS; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, bit);
+        peers &= bit ? bal : ~bal;
+    }
+    return peers;
+}
 
 // SEG: the digit is not taken from the key but is the segment (scene) whose
 // range [seg_off[d], seg_off[d+1]) holds the value — one extra stable pass
 // that groups concatenated scenes back together after the code passes.
 template <int BITS, int BLOCK, int KPT, bool SEG>
-__global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restrict__ keys_in,
-                                                         const uint32_t* __restrict__ vals_in,
-                                                         uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-                                                         uint32_t n, int shift, const uint32_t* __restrict__ pass_hist,
-                                                         uint32_t* lookback, uint32_t* ticket, uint32_t* err,
-                                                         uint32_t spin_limit, const uint32_t* __restrict__ seg_off,
-                                                         uint32_t n_seg) {
+__global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __restrict__ keys_in,
+                                                            const uint32_t* __restrict__ vals_in,
+                                                            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                            uint32_t n, int shift, const uint32_t* __restrict__ pass_hist,
+                                                            uint32_t* lookback, uint32_t* ticket, uint32_t* err,
+                                                            uint32_t spin_limit, const uint32_t* __restrict__ seg_off,
+                                                            uint32_t n_seg) {
     constexpr int RADIX = 1 << BITS;
     constexpr int WARPS = BLOCK / 32;
     constexpr int TILE = BLOCK * KPT;
     static_assert(BLOCK >= RADIX, "one thread per digit");
-    __shared__ uint32_t s_keys[TILE];
-    __shared__ uint32_t s_vals[TILE];
-    __shared__ uint32_t s_whist[WARPS][RADIX];
-    __shared__ uint32_t s_start[RADIX];   // block-local exclusive digit start
-    __shared__ uint32_t s_dest[RADIX];    // global destination of the digit's first key
-    __shared__ uint32_t s_scan[BLOCK / 32];
+    __shared__ uint32_t s_buf[TILE];            // staging for the scatter
+    __shared__ uint32_t s_whist[WARPS][RADIX];  // per-warp digit counters, then per-warp offsets
+    __shared__ uint32_t s_start[RADIX];         // block-local exclusive digit start
+    __shared__ uint32_t s_adj[RADIX];           // global destination of sorted slot i is s_adj[d] + i
+    __shared__ unsigned long long s_wsum[WARPS];
     __shared__ uint32_t s_tile;
-
     __shared__ uint32_t s_seg[SEG ? RADIX + 1 : 1];
+
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
     for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) (&s_whist[0][0])[i] = 0u;
@@ -227,107 +247,127 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(const uint32_t* __restr
     if (tile_base >= n) return;
     const uint64_t rem = n - tile_base;
     const uint32_t tile_n = rem < static_cast<uint64_t>(TILE) ? static_cast<uint32_t>(rem) : static_cast<uint32_t>(TILE);
+    // Warp w ranks the contiguous keys [w*32*KPT, (w+1)*32*KPT) of the tile, j-major.
+    const uint32_t wofs = static_cast<uint32_t>(warp) * 32u * KPT + lane;
+    const uint32_t* kin = keys_in + tile_base;
+    const uint32_t* vin = vals_in ? vals_in + tile_base : nullptr;
+    const uint32_t ibase = static_cast<uint32_t>(tile_base);
 
-    uint32_t key[KPT], val[KPT], rank[KPT];
-    const uint64_t wbase = tile_base + static_cast<uint64_t>(warp) * 32 * KPT;
+    uint32_t key[KPT], val[KPT], pos[KPT];
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
-        const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
-        const bool ok = idx < n;
-        key[j] = ok ? __ldg(keys_in + idx) : 0u;
-        val[j] = ok ? (vals_in ? __ldg(vals_in + idx) : static_cast<uint32_t>(idx)) : 0u;
+        const uint32_t lo = wofs + j * 32u;
+        key[j] = lo < tile_n ? __ldg(kin + lo) : 0u;
+        val[j] = lo < tile_n ? (vin ? __ldg(vin + lo) : ibase + lo) : 0u;
     }
     const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t* my_hist = &s_whist[warp][0];
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
-        const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
-        const uint32_t d = (idx < n) ? digit_of(key[j], val[j]) : static_cast<uint32_t>(RADIX);
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-        const int leader = __ffs(peers) - 1;
+        const bool ok = wofs + j * 32u < tile_n;
+        const uint32_t d = ok ? digit_of(key[j], val[j]) : 0u;
+        const uint32_t peers = ballot_peers<BITS>(d, ok);
+        const int leader = 31 - __clz(peers);
         uint32_t base = 0;
-        if (lane == leader && d < RADIX) {
-            base = s_whist[warp][d];
-            s_whist[warp][d] = base + __popc(peers);
-        }
-        base = __shfl_sync(0xFFFFFFFFu, base, leader);
-        rank[j] = base + __popc(peers & lt_mask);
+        if (lane == leader && ok) base = atomicAdd(my_hist + d, static_cast<uint32_t>(__popc(peers)));
+        pos[j] = __shfl_sync(0xFFFFFFFFu, base, leader) + __popc(peers & lt_mask);
         __syncwarp();
     }
     __syncthreads();
 
-    // Per digit: exclusive over warps, tile total, look-back, global base.
-    uint32_t total = 0, excl = 0;
+    // Per digit: exclusive over warps, tile total, publication.
     const int d = threadIdx.x;
+    uint32_t total = 0, excl = 0;
     if (d < RADIX) {
         for (int w = 0; w < WARPS; ++w) {
             const uint32_t c = s_whist[w][d];
             s_whist[w][d] = total;
             total += c;
         }
-        uint32_t* my = lookback + static_cast<size_t>(tile) * RADIX + d;
-        if (tile == 0) {
-            st_release_u32(my, kLbPrefix | total);
-        } else {
-            st_release_u32(my, kLbAgg | total);
-            int64_t k = static_cast<int64_t>(tile) - 1;
-            SpinBound spin(spin_limit);
-            while (k >= 0) {
-                const uint32_t v = ld_acquire_u32(lookback + static_cast<size_t>(k) * RADIX + d);
-                const uint32_t f = v & ~kLbMask;
-                if (f == 0u) {
-                    if (!spin.step()) { raise_error(err, kDevTimeout); break; }
-                    continue;
-                }
-                excl += v & kLbMask;
-                if (f == kLbPrefix) break;
-                --k;
-            }
-            st_release_u32(my, kLbPrefix | (excl + total));
-        }
+        st_relaxed_u32(lookback + static_cast<size_t>(tile) * RADIX + d, (tile == 0 ? kLbPrefix : kLbAgg) | total);
     }
-    // Block-wide exclusive scans over digits of (tile totals) and (global histogram).
-    uint32_t gh = (d < RADIX) ? pass_hist[d] : 0u;
-    uint32_t a = (d < RADIX) ? total : 0u;
-    // warp-level inclusive scan of a and gh packed as two 32-bit lanes of 64 bits
+    // Block-wide exclusive scans over digits of (tile totals) and (global
+    // histogram), packed as two 32-bit halves of one 64-bit scan.
+    const uint32_t gh = (d < RADIX) ? pass_hist[d] : 0u;
+    const uint32_t a = (d < RADIX) ? total : 0u;
     unsigned long long packed = (static_cast<unsigned long long>(gh) << 32) | a;
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, packed, o);
         if (lane >= o) packed += y;
     }
-    __shared__ unsigned long long s_wsum[BLOCK / 32];
     if (lane == 31) s_wsum[warp] = packed;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long run = 0;
-        for (int w = 0; w < BLOCK / 32; ++w) { const unsigned long long t = s_wsum[w]; s_wsum[w] = run; run += t; }
+        for (int w = 0; w < WARPS; ++w) { const unsigned long long t = s_wsum[w]; s_wsum[w] = run; run += t; }
     }
     __syncthreads();
     packed += s_wsum[warp];
     if (d < RADIX) {
+        if (tile > 0) {
+            // Look-back: sum the predecessors' counts of digit d down to the
+            // nearest inclusive prefix; tile 0 always publishes one.
+            int64_t k = static_cast<int64_t>(tile) - 1;
+            SpinBound spin(spin_limit);
+            while (true) {
+                uint32_t v[kLbWindow];
+#pragma unroll
+                for (int q = 0; q < kLbWindow; ++q)
+                    v[q] = (k - q >= 0) ? ld_relaxed_u32(lookback + static_cast<size_t>(k - q) * RADIX + d) : kLbPrefix;
+                int q = 0;
+                bool done = false;
+#pragma unroll
+                for (; q < kLbWindow; ++q) {
+                    const uint32_t f = v[q] & ~kLbMask;
+                    if (f == 0u) break;
+                    excl += v[q] & kLbMask;
+                    if (f == kLbPrefix) { done = true; break; }
+                }
+                if (done) break;
+                k -= q;
+                if (q < kLbWindow && !spin.step()) { raise_error(err, kDevTimeout); break; }
+            }
+            st_relaxed_u32(lookback + static_cast<size_t>(tile) * RADIX + d, kLbPrefix | (excl + total));
+        }
         const uint32_t incl_a = static_cast<uint32_t>(packed & 0xFFFFFFFFull);
         const uint32_t incl_g = static_cast<uint32_t>(packed >> 32);
         s_start[d] = incl_a - a;
-        s_dest[d] = (incl_g - gh) + excl;
+        s_adj[d] = (incl_g - gh) + excl - (incl_a - a);
     }
-    (void)s_scan;
     __syncthreads();
+    // Tile-local sorted slot of each element.
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
-        const uint64_t idx = wbase + static_cast<uint64_t>(j) * 32 + lane;
-        if (idx < n) {
-            const uint32_t dd = digit_of(key[j], val[j]);
-            const uint32_t p = s_start[dd] + s_whist[warp][dd] + rank[j];
-            s_keys[p] = key[j];
-            s_vals[p] = val[j];
+        const bool ok = wofs + j * 32u < tile_n;
+        const uint32_t dd = ok ? digit_of(key[j], val[j]) : 0u;
+        pos[j] += s_start[dd] + my_hist[dd];
+        if (ok) s_buf[pos[j]] = SEG ? val[j] : key[j];
+    }
+    __syncthreads();
+    uint32_t dst[KPT];
+#pragma unroll
+    for (int k = 0; k < KPT; ++k) {
+        const uint32_t i = k * BLOCK + threadIdx.x;
+        if (i < tile_n) {
+            const uint32_t x = s_buf[i];
+            dst[k] = s_adj[SEG ? digit_of(0u, x) : digit_of(x, 0u)] + i;
+            if (SEG) vals_out[dst[k]] = x;
+            else keys_out[dst[k]] = x;
         }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < tile_n; i += BLOCK) {
-        const uint32_t k = s_keys[i];
-        const uint32_t dd = digit_of(k, s_vals[i]);
-        const uint32_t dst = s_dest[dd] + (i - s_start[dd]);
-        keys_out[dst] = k;
-        vals_out[dst] = s_vals[i];
+#pragma unroll
+    for (int j = 0; j < KPT; ++j)
+        if (wofs + j * 32u < tile_n) s_buf[pos[j]] = SEG ? key[j] : val[j];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < KPT; ++k) {
+        const uint32_t i = k * BLOCK + threadIdx.x;
+        if (i < tile_n) {
+            if (SEG) keys_out[dst[k]] = s_buf[i];
+            else vals_out[dst[k]] = s_buf[i];
+        }
     }
 }
 

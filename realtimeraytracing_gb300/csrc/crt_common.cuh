@@ -84,6 +84,17 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const unsigned int* p) {
 __device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Relaxed (not ordering) gpu-scope accesses: for a status word whose flag and
+// payload share one 32-bit word, so no other data has to be made visible.
+// Unlike acquire loads, several of these can be in flight at once.
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(unsigned int* p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 // Device-side error word, set by any kernel whose bounded wait ran out or
 // whose input is unusable; read by the host after each stage.
