@@ -89,8 +89,13 @@ struct crt_bvh {
     uint32_t n = 0;
     uint32_t iterations = 0;
     float abs_eps = 0.f;
-    DevBuf nodes, wide, wide4, depth_odd, xtri, codes, perm, inv_perm;
+    DevBuf nodes, wide, depth_odd, xtri, codes, perm, inv_perm;
+    mutable DevBuf wide4;
     crt_predictor* predictor = nullptr;
+    // The 4-wide traversal nodes are derived on the first CRT_TRACE_WIDE
+    // trace after a build, so builds whose trees are never walked 4-wide
+    // neither compute nor store them.
+    mutable bool wide4_ready = false;
 };
 
 struct crt_predictor {
@@ -125,7 +130,7 @@ struct crt_ctx {
     crt_config cfg{};
     // build scratch
     DevBuf tris_in, models, scene_state, err, hist, sort_lb, codes_a, codes_b, vals_a, vals_b;
-    DevBuf node_box, node_lc, pos, clus_a, clus_b, iters, ploc_lb;
+    DevBuf node_box, node_kids, pos, clus_a, clus_b, iters, ploc_lb;
     DevBuf cam, rays_in, hits_out, rays_out, trace_stats, frame_rays, frame_hits, frame_shadow, frame_shits;
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
@@ -235,7 +240,7 @@ crt_status crt_destroy(crt_ctx* x) {
     cudaSetDevice(x->device);
     if (x->stream) cudaStreamSynchronize(x->stream);
     DevBuf* bufs[] = {&x->tris_in, &x->models, &x->scene_state, &x->err, &x->hist, &x->sort_lb, &x->codes_a,
-                      &x->codes_b, &x->vals_a, &x->vals_b, &x->node_box, &x->node_lc, &x->pos, &x->clus_a,
+                      &x->codes_b, &x->vals_a, &x->vals_b, &x->node_box, &x->node_kids, &x->pos, &x->clus_a,
                       &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits};
     for (DevBuf* b : bufs) b->release();
@@ -274,7 +279,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     const int passes = (30 + bits - 1) / bits;
     const uint32_t radix = 1u << bits;
     const uint32_t sort_tiles = (N + crt::sort_tile_keys(bits) - 1) / crt::sort_tile_keys(bits);
-    const uint32_t ploc_tiles = (N + crt::kPlocTile - 1) / crt::kPlocTile;
+    const uint32_t ploc_tiles = (N + crt::kPlocMinOwn - 1) / crt::kPlocMinOwn;
 
     // ---- buffers
     const crt_triangle* d_tris = tris;
@@ -293,16 +298,17 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(x->vals_a.reserve(4ull * N));
     CRT_TRY(x->vals_b.reserve(4ull * N));
     CRT_TRY(x->node_box.reserve(32ull * (2ull * N - 1)));
-    CRT_TRY(x->node_lc.reserve(4ull * N));
+    CRT_TRY(x->node_kids.reserve(16ull * N));
     CRT_TRY(x->pos.reserve(8ull * N));
     CRT_TRY(x->clus_a.reserve(32ull * N));
     CRT_TRY(x->clus_b.reserve(32ull * N));
     CRT_TRY(x->iters.reserve(8ull * (N + 2)));
-    CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 32));  // + tickets[2], barrier[2], iteration count
+    // + tail: tickets[2], barrier[2], iteration count, finished blocks, 3 timer stamps
+    CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 64));
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
     CRT_TRY(b->wide.reserve(64ull * N));
-    CRT_TRY(b->wide4.reserve(128ull * N));
+    b->wide4_ready = false;
     CRT_TRY(b->depth_odd.reserve(N));
     CRT_TRY(b->inv_perm.reserve(4ull * N));
     CRT_TRY(b->codes.reserve(4ull * N));
@@ -332,7 +338,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, s));
     CRT_CUDA(cudaMemsetAsync(x->hist.p, 0, 4 * hist_words, s));
     CRT_CUDA(cudaMemsetAsync(x->sort_lb.p, 0, 4 * sort_lb_words, s));
-    CRT_CUDA(cudaMemsetAsync(x->ploc_lb.p, 0, 8ull * (2ull * ploc_tiles) + 32, s));
+    CRT_CUDA(cudaMemsetAsync(x->ploc_lb.p, 0, 8ull * (2ull * ploc_tiles) + 64, s));
     uint32_t* err = x->err.as<uint32_t>();
     auto* st = x->scene_state.as<crt::SceneState>();
 
@@ -369,18 +375,24 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     x->it_host.assign(1, make_uint2(N, N));
     uint32_t iters = 0;
     bool laid_out = false;
+    float layout_in_kernel_ms = 0.f;  // the persistent launch's layout phase, from its timer stamps
     if (N > 1 && !x->force_multi_launch) {
         // one cooperative launch: every PLOC iteration, then the DFS layout
         unsigned long long* lb = x->ploc_lb.as<unsigned long long>();
         uint32_t* tail = reinterpret_cast<uint32_t*>(lb + 2ull * ploc_tiles);
         const cudaError_t e = crt::launch_ploc_persistent(
-            x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), d_it, N,
+            x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_kids.as<uint4>(), d_it, N,
             static_cast<int>(x->cfg.ploc_radius), lb, tail, ploc_tiles, x->pos.as<uint2>(), b->nodes.as<crt_bvh_node>(),
             b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), tail + 2, tail + 4, err, x->cfg.spin_limit, s);
         if (e == cudaSuccess) {
             CRT_CUDA(cudaEventRecord(x->ev[3], s));
-            CRT_CUDA(cudaMemcpyAsync(&iters, tail + 4, 4, cudaMemcpyDeviceToHost, s));
+            uint32_t* hp = static_cast<uint32_t*>(x->pinned);
+            CRT_CUDA(cudaMemcpyAsync(hp, tail + 4, 32, cudaMemcpyDeviceToHost, s));
             CRT_CUDA(cudaStreamSynchronize(s));
+            iters = hp[0];
+            unsigned long long stamp[3];
+            std::memcpy(stamp, hp + 2, sizeof(stamp));
+            if (stamp[2] > stamp[1]) layout_in_kernel_ms = static_cast<float>(static_cast<double>(stamp[2] - stamp[1]) * 1e-6);
             laid_out = true;
         } else if (e != cudaErrorNotSupported && e != cudaErrorCooperativeLaunchTooLarge) {
             return fail(CRT_ERR_CUDA, "PLOC launch failed: %s", cudaGetErrorString(e));
@@ -408,7 +420,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
             for (int c = 0; c < chunk; ++c, ++iter) {
                 const float4* cin = (iter & 1) ? cb : ca;
                 float4* cout = (iter & 1) ? ca : cb;
-                crt::launch_ploc_iteration(cin, cout, x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), d_it, iter, N,
+                crt::launch_ploc_iteration(cin, cout, x->node_box.as<float4>(), x->node_kids.as<uint4>(), d_it, iter, N,
                                            static_cast<int>(x->cfg.ploc_radius), n_known, lb, tickets, ploc_tiles, err,
                                            x->cfg.spin_limit, s);
             }
@@ -442,12 +454,13 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     if (N == 1) {
         crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), s);
     } else if (!laid_out) {
+        uint32_t* dfs = x->clus_a.as<uint32_t>();  // the cluster buffers are free after PLOC
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
-            crt::launch_layout_level(x->node_box.as<float4>(), x->node_lc.as<uint32_t>(), x->pos.as<uint2>(),
-                                     x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(),
-                                     b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), err, s);
+            crt::launch_layout_level(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(),
+                                     x->it_host[k].y, x->it_host[k + 1].y, N, dfs, err, s);
+        crt::launch_layout_emit(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(), N, dfs,
+                                b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), err, s);
     }
-    if (N > 1) crt::launch_wide4(b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), N - 1, b->wide4.as<float4>(), s);
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->ev[4], s));
     CRT_TRY(x->check_device_error());
@@ -460,8 +473,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     x->stats.ploc_iterations = iters;
     x->stats.ms_morton = ms[0];
     x->stats.ms_sort = ms[1];
-    x->stats.ms_ploc = ms[2];
-    x->stats.ms_layout = ms[3];
+    x->stats.ms_ploc = ms[2] - layout_in_kernel_ms;
+    x->stats.ms_layout = ms[3] + layout_in_kernel_ms;
     x->stats.ms_total = ms[0] + ms[1] + ms[2] + ms[3];
     float ext = 0.f;
     for (int a = 0; a < 3; ++a) {
@@ -496,10 +509,22 @@ crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
     return CRT_OK;
 }
 
+// Derives the 4-wide traversal nodes of b on x's stream if the last build
+// has not yet done so.
+crt_status ensure_wide4(crt_ctx* x, const crt_bvh* b) {
+    if (b->wide4_ready || b->n <= 1) return CRT_OK;
+    CRT_TRY(b->wide4.reserve(128ull * b->n));
+    crt::launch_wide4(b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), b->n - 1, b->wide4.as<float4>(), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    b->wide4_ready = true;
+    return CRT_OK;
+}
+
 // Enqueues one traversal launch on device-resident rays/hits (no sync).
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
                         crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0) {
     if (n_rays == 0) return CRT_OK;
+    if (flags & CRT_TRACE_WIDE) CRT_TRY(ensure_wide4(x, b));
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
     p.xtri = b->xtri.as<float4>();
@@ -997,7 +1022,7 @@ struct crt_batch {
     crt_config cfg{};
     DevBuf scenes, seg_off, seg_hist, chunks, states, models, err;
     DevBuf codes_a, codes_b, vals_a, vals_b, codes, perm_global, perm_local;
-    DevBuf node_box, node_lc, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
+    DevBuf node_box, node_kids, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
     DevBuf nodes, wide, depth_odd, xtri, inv_perm;
     bool models_set = false;
     cudaGraphExec_t graph = nullptr;
@@ -1073,7 +1098,7 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
         uint32_t* tail = reinterpret_cast<uint32_t*>(lb + 2ull * bt->lb_cap);
         const cudaError_t e = crt::launch_batch_ploc(
             bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->clus_a.as<float4>(), bt->clus_b.as<float4>(),
-            bt->node_box.as<float4>(), bt->node_lc.as<uint32_t>(), bt->it.as<uint2>(), static_cast<int>(bt->cfg.ploc_radius),
+            bt->node_box.as<float4>(), bt->node_kids.as<uint4>(), bt->it.as<uint2>(), static_cast<int>(bt->cfg.ploc_radius),
             lb, bt->lb_cap, tail, bt->pf.as<uint2>(), bt->nodes.as<crt_bvh_node>(), bt->wide.as<float4>(),
             bt->depth_odd.as<uint8_t>(), tail + 2, bt->max_n + 1, err, x->cfg.spin_limit, s);
         if (e != cudaSuccess) return fail(CRT_ERR_UNSUPPORTED, "batched PLOC launch failed: %s", cudaGetErrorString(e));
@@ -1142,7 +1167,7 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
         hs[k].n_rays = ray_counts[k];
         hs[k].it_off = static_cast<uint32_t>(nt + 2ull * k);
         hs[k].lb_off = static_cast<uint32_t>(lb);
-        lb += (tri_counts[k] + crt::kPlocTile - 1) / crt::kPlocTile;
+        lb += (tri_counts[k] + crt::kPlocMinOwn - 1) / crt::kPlocMinOwn;
         const uint32_t ck = crt::batch_box_chunk();
         hs[k].n_chunks = static_cast<uint32_t>((tri_counts[k] + ck - 1) / ck);
         for (uint64_t b = 0; b < tri_counts[k]; b += ck) {
@@ -1173,8 +1198,9 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
     R(bt->models, 2 * 64 * 16 * 4);
     R(bt->err, 16);
     for (DevBuf* b : {&bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global, &bt->perm_local,
-                      &bt->node_lc, &bt->inv_perm})
+                      &bt->inv_perm})
         R(*b, 4ull * N);
+    R(bt->node_kids, 16ull * N);
     R(bt->node_box, 32ull * (2ull * N));
     R(bt->pf, 8ull * N);
     R(bt->clus_a, 32ull * N);
@@ -1211,7 +1237,7 @@ crt_status crt_batch_free(crt_batch* bt) {
     bt->drop_graph();
     DevBuf* bufs[] = {&bt->scenes, &bt->seg_off, &bt->seg_hist, &bt->chunks, &bt->states, &bt->models, &bt->err,
                       &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
-                      &bt->perm_local, &bt->node_box, &bt->node_lc, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
+                      &bt->perm_local, &bt->node_box, &bt->node_kids, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
                       &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->depth_odd, &bt->xtri,
                       &bt->inv_perm};
     for (DevBuf* b : bufs) b->release();

@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(256) batch_leaf_init_kernel(const crt_triangle
 // counter, maps a ticket to (scene, tile) and runs the single-scene tile
 // code on that scene's slices.  A grid barrier separates iterations.
 template <int TILE, int BLOCK, int MAXR>
-__global__ void __launch_bounds__(BLOCK) batch_ploc_kernel(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb,
-                                                           float4* node_box, uint32_t* node_lc, uint2* it, int R,
+__global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb,
+                                                           float4* node_box, uint4* node_kids, uint2* it, int R,
                                                            unsigned long long* lookback, uint32_t lb_cap, uint32_t* tickets,
                                                            uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
                                                            unsigned int* bar, uint32_t max_iters, uint32_t* err,
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(BLOCK) batch_ploc_kernel(BatchScene* scenes, u
             uint32_t run = 0;
             for (uint32_t k = 0; k < n_scenes; ++k) {
                 s_tile_pre[k] = run;
-                run += s_n[k] > 1 ? (s_n[k] + TILE - 1) / TILE : 0u;
+                run += s_n[k] > 1 ? (s_n[k] + ploc_own(R) - 1) / ploc_own(R) : 0u;
             }
             s_tile_pre[n_scenes] = run;
         }
@@ -311,14 +311,17 @@ __global__ void __launch_bounds__(BLOCK) batch_ploc_kernel(BatchScene* scenes, u
             unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * lb_cap + B.lb_off;
             unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * lb_cap + B.lb_off;
             ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box + 2 * static_cast<size_t>(B.node_off),
-                                         node_lc + B.tri_off, it + B.it_off, B.n_tris, R, lb_cur, lb_next, err, spin_limit);
-            if ((tile + 1) * TILE >= cur.x && threadIdx.x == 0) {  // the scene's last tile wrote its next record
+                                         node_kids + B.tri_off, it + B.it_off, B.n_tris, R, lb_cur, lb_next, err, spin_limit);
+            if ((tile + 1) * ploc_own(R) >= cur.x && threadIdx.x == 0) {  // the scene's last tile wrote its next record
                 if (it[B.it_off + iter + 1].x <= 1u) scenes[sc].iters = static_cast<uint32_t>(iter + 1);
             }
         }
         if (!grid_barrier(bar, err, spin_limit)) return;
     }
-    // DFS layout: step r handles level (iters - 1 - r) of every scene that has it
+    // DFS layout: step r handles level (iters - 1 - r) of every scene that has
+    // it, recording node ids by DFS position in dfs (the first cluster buffer,
+    // free now); then every position is emitted in order.
+    uint32_t* dfs = reinterpret_cast<uint32_t*>(ca);
     uint32_t max_it = 0;
     for (uint32_t k = 0; k < n_scenes; ++k) max_it = max(max_it, __ldcg(&scenes[k].iters));
     for (uint32_t r = 0; r < max_it; ++r) {
@@ -347,10 +350,33 @@ __global__ void __launch_bounds__(BLOCK) batch_ploc_kernel(BatchScene* scenes, u
             const BatchScene B = scenes[lo];
             const uint32_t lv = B.iters - 1 - r;
             const uint32_t X = __ldcg(it + B.it_off + lv).y + (q - s_tile_pre[lo]);
-            layout_node(X, node_box + 2 * static_cast<size_t>(B.node_off), node_lc + B.tri_off, pf + B.tri_off, B.n_tris,
-                        nodes + B.node_off, wide + 4 * static_cast<size_t>(B.wide_off), depth_odd + B.wide_off, err);
+            layout_down(X, node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off, pf + B.tri_off, B.n_tris,
+                        dfs + B.node_off, err);
         }
-        if (r + 1 < max_it && !grid_barrier(bar, err, spin_limit)) return;
+        if (!grid_barrier(bar, err, spin_limit)) return;
+    }
+    // every DFS position of every scene with more than one triangle, in order
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t k = 0; k < n_scenes; ++k) {
+            s_tile_pre[k] = run;
+            if (scenes[k].n_tris > 1) run += 2 * scenes[k].n_tris - 1;
+        }
+        s_tile_pre[n_scenes] = run;
+    }
+    __syncthreads();
+    const uint32_t total_slots = s_tile_pre[n_scenes];
+    for (uint32_t q = blockIdx.x * BLOCK + threadIdx.x; q < total_slots; q += gridDim.x * BLOCK) {
+        uint32_t lo = 0, hi = n_scenes - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (s_tile_pre[mid] <= q) lo = mid; else hi = mid - 1;
+        }
+        const BatchScene B = scenes[lo];
+        layout_emit(q - s_tile_pre[lo], node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off,
+                    pf + B.tri_off, B.n_tris, dfs + B.node_off, nodes + B.node_off,
+                    wide + 4 * static_cast<size_t>(B.wide_off), depth_odd + B.wide_off, err);
     }
 }
 
@@ -363,8 +389,8 @@ int batch_ploc_grid() {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                        &per_sm, batch_ploc_kernel<kPlocTile, 256, kPlocMaxRadius>, 256, 0) == cudaSuccess && per_sm > 0)
-            grid = (per_sm < 2 ? per_sm : 2) * sms;
+                        &per_sm, batch_ploc_kernel<kPlocSpan, 256, kPlocMaxRadius>, 256, 0) == cudaSuccess && per_sm > 0)
+            grid = (per_sm < kPlocBlocksPerSm ? per_sm : kPlocBlocksPerSm) * sms;
         else
             grid = 0;
         cudaGetLastError();
@@ -398,14 +424,14 @@ void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchSce
 }
 
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
-                              uint32_t* node_lc, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
+                              uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
                               unsigned int* bar, uint32_t max_iters, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
     const int grid = batch_ploc_grid();
     if (grid <= 0) return cudaErrorNotSupported;
-    void* args[] = {&scenes, &n_scenes, &ca, &cb, &node_box, &node_lc, &it, &radius, &lookback, &lb_cap, &tickets,
+    void* args[] = {&scenes, &n_scenes, &ca, &cb, &node_box, &node_kids, &it, &radius, &lookback, &lb_cap, &tickets,
                     &pf, &nodes, &wide, &depth_odd, &bar, &max_iters, &err, &spin_limit};
-    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(batch_ploc_kernel<kPlocTile, 256, kPlocMaxRadius>),
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(batch_ploc_kernel<kPlocSpan, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }
 

@@ -413,16 +413,24 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
 
 // ================================================ K3: one PLOC iteration
 // For the n live clusters (Morton order, 32-byte records: min.xyz|node id,
-// max.xyz|leaf count) this does, per tile of TILE positions:
-//   nearest neighbour in [i-R, i+R] by surface area of the merged box,
-//     first strict minimum = lowest j on ties (bvh.cpp:193-210),
-//   mutual pairs merge at the lower position (bvh.cpp:159-191),
-//   exclusive scan of survivors and compaction (bvh.cpp:125-156),
-// with the scans across tiles done by decoupled look-back, so one launch is
-// one reference iteration.  NN of positions up to R outside the tile are
-// recomputed locally (their boxes 2R outside are staged in shared memory).
-// New nodes get ids it[iter].y + (merges before them); the last tile writes
-// it[iter+1] = (live clusters, next id).
+// max.xyz|leaf count) a tile starting at position s with R = radius does:
+//   nearest neighbour of the TILE positions [s-R, s-R+TILE) in [i-R, i+R]
+//     by surface area of the merged box, first strict minimum = lowest j on
+//     ties (bvh.cpp:193-210);
+//   merge decisions for its own ploc_own(R) = TILE-2R positions [s, e):
+//     mutual pairs merge at the lower position (bvh.cpp:159-191);
+//   exclusive scan of survivors and compaction (bvh.cpp:125-156), with the
+//     scan across tiles done by decoupled look-back,
+// so one launch is one reference iteration.  New nodes get ids it[iter].y +
+// (merges before them); the last tile writes it[iter+1] = (live clusters,
+// next id).
+//
+// Boxes of positions [s-2R, e+2R) are staged in shared memory as separate
+// min/max coordinate arrays.  Each thread keeps the boxes of its 4
+// consecutive positions in registers and walks the 2R+4 boxes around them
+// once, so a box read serves up to 4 area evaluations.  The threads of a warp
+// read at a stride of 4 positions; the index swizzle ploc_swz makes those
+// reads free of bank conflicts.
 //
 // The search compares areas computed from fminf/fmaxf boxes; those differ
 // from the std::min/max boxes only in the sign of a zero, which changes no
@@ -440,12 +448,67 @@ __device__ __forceinline__ float sa_merged(float4 amn, float4 amx, float4 bmn, f
 
 template <int TILE, int BLOCK, int MAXR>
 struct PlocSmem {
-    float4 mn[TILE + 4 * MAXR];
-    float4 mx[TILE + 4 * MAXR];
-    uint32_t nn[TILE + 2 * MAXR];
-    uint32_t wsum[BLOCK / 32];
+    static_assert(TILE == 4 * BLOCK, "four nearest-neighbour positions per thread");
+    static constexpr int kWin = TILE + 2 * MAXR;  // positions [s-2R, e+2R), e - s <= TILE - 2R
+    static_assert(kWin % 32 == 0, "the swizzle stays inside 32-entry rows");
+    float mnx[kWin], mny[kWin], mnz[kWin], mxx[kWin], mxy[kWin], mxz[kWin];
+    uint32_t id[kWin], lc[kWin];
+    uint32_t nn[TILE];  // nearest neighbour of position s - R + i
+    unsigned long long wsum[BLOCK / 32];
     unsigned long long prefix;
 };
+
+// Bank-conflict-free index of window entry w for reads at a stride of 4.
+__device__ __forceinline__ int ploc_swz(int w) { return w ^ ((w >> 5) & 3); }
+
+// Nearest neighbours of this thread's positions q0..q0+3, q0 = s - R + 4t.
+// RC > 0: the radius is the compile-time RC; RC == 0: runtime radius R.
+template <int RC, int TILE, int BLOCK, int MAXR>
+__device__ __forceinline__ void ploc_nearest(PlocSmem<TILE, BLOCK, MAXR>& S, int s, int e, int n, int R_rt) {
+    const int R = RC > 0 ? RC : R_rt;
+    const int q0 = s - R + 4 * static_cast<int>(threadIdx.x);
+    const int wq = 4 * static_cast<int>(threadIdx.x) + R;  // window index of q0
+    float amnx[4], amny[4], amnz[4], amxx[4], amxy[4], amxz[4], best[4];
+    int bj[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int w = ploc_swz(wq + i);
+        amnx[i] = S.mnx[w]; amny[i] = S.mny[w]; amnz[i] = S.mnz[w];
+        amxx[i] = S.mxx[w]; amxy[i] = S.mxy[w]; amxz[i] = S.mxz[w];
+        best[i] = __int_as_float(0x7F800000);
+        bj[i] = q0 + i;
+    }
+    auto visit = [&](int d, int i) {
+        const int j = q0 + d;
+        const int w = ploc_swz(wq + d);
+        const float dx = fmaxf(amxx[i], S.mxx[w]) - fminf(amnx[i], S.mnx[w]);
+        const float dy = fmaxf(amxy[i], S.mxy[w]) - fminf(amny[i], S.mny[w]);
+        const float dz = fmaxf(amxz[i], S.mxz[w]) - fminf(amnz[i], S.mnz[w]);
+        const float v = 2.0f * (dx * dy + dy * dz + dz * dx);
+        if (static_cast<unsigned>(j) < static_cast<unsigned>(n) && v < best[i]) { best[i] = v; bj[i] = j; }
+    };
+    if (RC > 0) {
+#pragma unroll
+        for (int d = -RC; d <= RC + 3; ++d)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int k = d - i;
+                if (k != 0 && k >= -RC && k <= RC) visit(d, i);
+            }
+    } else {
+        for (int d = -R; d <= R + 3; ++d)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int k = d - i;
+                if (k != 0 && k >= -R && k <= R) visit(d, i);
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int p = q0 + i;
+        if (p >= 0 && p < n && p < e + R) S.nn[4 * threadIdx.x + i] = static_cast<uint32_t>(bj[i]);
+    }
+}
 
 // One tile of one PLOC iteration (see above).  Reads of data other blocks
 // wrote (the cluster array) bypass L1 (__ldcg), so the same code is correct
@@ -453,47 +516,44 @@ struct PlocSmem {
 template <int TILE, int BLOCK, int MAXR>
 __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32_t tile, const uint2 cur, int iter,
                                           const float4* __restrict__ cin, float4* __restrict__ cout,
-                                          float4* __restrict__ node_box, uint32_t* __restrict__ node_lc, uint2* it,
+                                          float4* __restrict__ node_box, uint4* __restrict__ node_kids, uint2* it,
                                           uint32_t N, int R, unsigned long long* lb_cur, unsigned long long* lb_next,
                                           uint32_t* err, uint32_t spin_limit) {
-    constexpr int IPT = TILE / BLOCK;
-    const uint32_t n = cur.x;
-    const uint32_t s = tile * TILE;
+    constexpr int IPT = 4;
+    const int n = static_cast<int>(cur.x);
+    const int s = static_cast<int>(tile * ploc_own(R));
     __syncthreads();  // the previous tile of this block is done with S
-    if (threadIdx.x == 0) lb_next[tile] = 0ull;
-    const uint32_t e = min(n, s + TILE);
-    const int lo = max(0, static_cast<int>(s) - 2 * R);
-    const int hi = min(static_cast<int>(n), static_cast<int>(e) + 2 * R);
+    if (threadIdx.x == 0) st_relaxed_u64(&lb_next[tile], 0ull);
+    const int e = min(n, s + static_cast<int>(ploc_own(R)));
+    const int wbase = s - 2 * R;  // window index 0
+    const int lo = max(0, wbase);
+    const int hi = min(n, e + 2 * R);
     for (int p = lo + threadIdx.x; p < hi; p += BLOCK) {
-        S.mn[p - lo] = __ldcg(cin + 2 * static_cast<size_t>(p));
-        S.mx[p - lo] = __ldcg(cin + 2 * static_cast<size_t>(p) + 1);
+        const float4 a = __ldcg(cin + 2 * static_cast<size_t>(p));
+        const float4 b = __ldcg(cin + 2 * static_cast<size_t>(p) + 1);
+        const int w = ploc_swz(p - wbase);
+        S.mnx[w] = a.x; S.mny[w] = a.y; S.mnz[w] = a.z; S.id[w] = __float_as_uint(a.w);
+        S.mxx[w] = b.x; S.mxy[w] = b.y; S.mxz[w] = b.z; S.lc[w] = __float_as_uint(b.w);
     }
     __syncthreads();
-    const int nlo = max(0, static_cast<int>(s) - R);
-    const int nhi = min(static_cast<int>(n), static_cast<int>(e) + R);
-    for (int p = nlo + threadIdx.x; p < nhi; p += BLOCK) {
-        const float4 amn = S.mn[p - lo], amx = S.mx[p - lo];
-        const int j0 = max(0, p - R), j1 = min(static_cast<int>(n), p + R + 1);
-        float best = __int_as_float(0x7F800000);
-        int bj = p;
-        for (int j = j0; j < j1; ++j) {
-            if (j == p) continue;
-            const float dd = sa_merged(amn, amx, S.mn[j - lo], S.mx[j - lo]);
-            if (dd < best) { best = dd; bj = j; }
-        }
-        S.nn[p - nlo] = static_cast<uint32_t>(bj);
+    switch (R) {
+        case 8: ploc_nearest<8>(S, s, e, n, R); break;
+        case 16: ploc_nearest<16>(S, s, e, n, R); break;
+        case 32: ploc_nearest<32>(S, s, e, n, R); break;
+        default: ploc_nearest<0>(S, s, e, n, R); break;
     }
     __syncthreads();
 
     // Decisions for the tile's own positions: thread t owns [s + t*IPT, +IPT).
-    uint32_t flags = 0;  // bit q: valid, bit 16+q: merge head
+    const int nbase = s - R;  // S.nn index 0
+    uint32_t flags = 0;       // bit q: valid, bit 16+q: merge head
     uint32_t nv = 0, nm = 0;
 #pragma unroll
     for (int q = 0; q < IPT; ++q) {
-        const int p = static_cast<int>(s) + threadIdx.x * IPT + q;
-        if (p >= static_cast<int>(e)) break;
-        const int j = static_cast<int>(S.nn[p - nlo]);
-        const bool mutual = (j != p) && (static_cast<int>(S.nn[j - nlo]) == p);
+        const int p = s + static_cast<int>(threadIdx.x) * IPT + q;
+        if (p >= e) break;
+        const int j = static_cast<int>(S.nn[p - nbase]);
+        const bool mutual = (j != p) && (static_cast<int>(S.nn[j - nbase]) == p);
         const bool head = mutual && p < j;
         const bool gone = mutual && p > j;
         if (!gone) { flags |= 1u << q; ++nv; }
@@ -501,70 +561,96 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
     }
     // Block exclusive scan of (nv, nm) packed as 16|16 bits.
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t packed = (nv << 16) | nm, incl = packed;
+    const uint32_t packed = (nv << 16) | nm;
+    uint32_t incl = packed;
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
         if (lane >= o) incl += y;
     }
     if (lane == 31) S.wsum[warp] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int w = 0; w < BLOCK / 32; ++w) { const uint32_t t = S.wsum[w]; S.wsum[w] = run; run += t; }
+    if (warp == 0) {
+        // Warp 0: exclusive scan of the warp sums, then the look-back over
+        // the preceding tiles, 32 status words per round trip.
+        uint32_t ws = lane < BLOCK / 32 ? static_cast<uint32_t>(S.wsum[lane]) : 0u, wi = ws;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        if (lane < BLOCK / 32) S.wsum[lane] = wi - ws;
+        const uint32_t run = __shfl_sync(0xFFFFFFFFu, wi, 31);
         const unsigned long long tv = run >> 16, tm = run & 0xFFFFu;
-        // look-back over preceding tiles
         unsigned long long ev = 0, em = 0;
         if (tile == 0) {
-            st_release_u64(&lb_cur[0], kPlPrefix | (tv << 31) | tm);
+            if (lane == 0) st_relaxed_u64(&lb_cur[0], kPlPrefix | (tv << 31) | tm);
         } else {
-            st_release_u64(&lb_cur[tile], kPlAgg | (tv << 31) | tm);
-            int k = static_cast<int>(tile) - 1;
+            if (lane == 0) st_relaxed_u64(&lb_cur[tile], kPlAgg | (tv << 31) | tm);
+            long long k0 = static_cast<long long>(tile) - 1;
             SpinBound spin(spin_limit);
-            while (k >= 0) {
-                const unsigned long long v = ld_acquire_u64(&lb_cur[k]);
+            while (true) {
+                const long long k = k0 - lane;
+                const unsigned long long v = k >= 0 ? ld_relaxed_u64(&lb_cur[k]) : kPlPrefix;
                 const unsigned long long f = v & (3ull << 62);
-                if (f == 0ull) {
+                const uint32_t pm = __ballot_sync(0xFFFFFFFFu, f == kPlPrefix);
+                const uint32_t zm = __ballot_sync(0xFFFFFFFFu, f == 0ull);
+                const int stop = pm ? __ffs(pm) - 1 : 31;  // lanes 0..stop are summed
+                const uint32_t upto = stop == 31 ? 0xFFFFFFFFu : ((2u << stop) - 1u);
+                if (zm & upto) {  // a tile before the nearest prefix has not published yet
                     if (!spin.step()) { raise_error(err, kDevTimeout); break; }
                     continue;
                 }
-                ev += (v >> 31) & kPlMask31;
-                em += v & kPlMask31;
-                if (f == kPlPrefix) break;
-                --k;
+                unsigned long long cv = lane <= stop ? ((v >> 31) & kPlMask31) : 0ull;
+                unsigned long long cm = lane <= stop ? (v & kPlMask31) : 0ull;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    cv += __shfl_xor_sync(0xFFFFFFFFu, cv, o);
+                    cm += __shfl_xor_sync(0xFFFFFFFFu, cm, o);
+                }
+                ev += cv;
+                em += cm;
+                if (pm) break;
+                k0 -= 32;
             }
-            st_release_u64(&lb_cur[tile], kPlPrefix | ((ev + tv) << 31) | (em + tm));
+            if (lane == 0) st_relaxed_u64(&lb_cur[tile], kPlPrefix | ((ev + tv) << 31) | (em + tm));
         }
-        S.prefix = (ev << 32) | em;
-        if (e == n)  // last tile: size and id base of the next iteration
-            it[iter + 1] = make_uint2(static_cast<uint32_t>(ev + tv), cur.y + static_cast<uint32_t>(em + tm));
+        if (lane == 0) {
+            S.prefix = (ev << 32) | em;
+            if (e == n)  // last tile: size and id base of the next iteration
+                it[iter + 1] = make_uint2(static_cast<uint32_t>(ev + tv), cur.y + static_cast<uint32_t>(em + tm));
+        }
     }
     __syncthreads();
-    const uint32_t excl = S.wsum[warp] + (incl - packed);
+    const uint32_t excl = static_cast<uint32_t>(S.wsum[warp]) + (incl - packed);
     uint32_t out_v = static_cast<uint32_t>(S.prefix >> 32) + (excl >> 16);
     uint32_t out_m = cur.y + static_cast<uint32_t>(S.prefix & 0xFFFFFFFFull) + (excl & 0xFFFFu);
 #pragma unroll
     for (int q = 0; q < IPT; ++q) {
         if (!(flags & (1u << q))) continue;
-        const int p = static_cast<int>(s) + threadIdx.x * IPT + q;
-        float4 mn = S.mn[p - lo], mx = S.mx[p - lo];
+        const int p = s + static_cast<int>(threadIdx.x) * IPT + q;
+        const int wp = ploc_swz(p - wbase);
+        float4 mn = make_float4(S.mnx[wp], S.mny[wp], S.mnz[wp], __uint_as_float(S.id[wp]));
+        float4 mx = make_float4(S.mxx[wp], S.mxy[wp], S.mxz[wp], __uint_as_float(S.lc[wp]));
         if (flags & (1u << (16 + q))) {
-            const int j = static_cast<int>(S.nn[p - nlo]);
-            const float4 bmn = S.mn[j - lo], bmx = S.mx[j - lo];
+            const int j = static_cast<int>(S.nn[p - nbase]);
+            const int wj = ploc_swz(j - wbase);
             const uint32_t id = out_m++;
             if (id >= 2 * N - 1 || id < N) { raise_corrupt(err, 2 + (iter << 8), p, id); continue; }
             float4 m0, m1;  // AABB::merge (bvh.cpp:401-413), first argument = lower position
-            m0.x = min_std(mn.x, bmn.x); m0.y = min_std(mn.y, bmn.y); m0.z = min_std(mn.z, bmn.z);
-            m1.x = max_std(mx.x, bmx.x); m1.y = max_std(mx.y, bmx.y); m1.z = max_std(mx.z, bmx.z);
-            m0.w = mn.w;   // left child id
-            m1.w = bmn.w;  // right child id
+            m0.x = min_std(mn.x, S.mnx[wj]); m0.y = min_std(mn.y, S.mny[wj]); m0.z = min_std(mn.z, S.mnz[wj]);
+            m1.x = max_std(mx.x, S.mxx[wj]); m1.y = max_std(mx.y, S.mxy[wj]); m1.z = max_std(mx.z, S.mxz[wj]);
+            m0.w = mn.w;                      // left child id
+            m1.w = __uint_as_float(S.id[wj]); // right child id
             node_box[2 * static_cast<size_t>(id)] = m0;
             node_box[2 * static_cast<size_t>(id) + 1] = m1;
-            const uint32_t lc = __float_as_uint(mx.w) + __float_as_uint(bmx.w);
-            node_lc[id - N] = lc;
+            const uint32_t lc = S.lc[wp] + S.lc[wj];
+            // children and their leaf counts, read by the DFS layout
+            node_kids[id - N] = make_uint4(S.id[wp], S.id[wj], S.lc[wp], S.lc[wj]);
             mn = make_float4(m0.x, m0.y, m0.z, __uint_as_float(id));
             mx = make_float4(m1.x, m1.y, m1.z, __uint_as_float(lc));
         }
-        if (out_v >= n) { raise_corrupt(err, 3 + (iter << 8), p, out_v); continue; }
+        if (out_v >= static_cast<uint32_t>(n)) { raise_corrupt(err, 3 + (iter << 8), p, out_v); continue; }
         cout[2 * static_cast<size_t>(out_v)] = mn;
         cout[2 * static_cast<size_t>(out_v) + 1] = mx;
         ++out_v;
@@ -573,7 +659,7 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
 
 template <int TILE, int BLOCK, int MAXR>
 __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __restrict__ cin, float4* __restrict__ cout,
-                                                               float4* __restrict__ node_box, uint32_t* __restrict__ node_lc,
+                                                               float4* __restrict__ node_box, uint4* __restrict__ node_kids,
                                                                uint2* it, int iter, uint32_t N,
                                                                int R, unsigned long long* lookback, uint32_t* tickets,
                                                                uint32_t n_tiles_cap, uint32_t* err, uint32_t spin_limit) {
@@ -592,9 +678,9 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
     if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
-    if (tile * TILE >= n) return;
+    if (tile * ploc_own(R) >= n) return;
     if (tile == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
-    ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_lc, it, N, R, lb_cur, lb_next, err,
+    ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur, lb_next, err,
                                  spin_limit);
 }
 
@@ -602,34 +688,65 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 // Scene::recursiveTopDownTraversalBVH (scene.cpp:189-201): pre-order, left
 // subtree first, root (the last merge, id 2N-2) at 0.  A node at position p
 // puts its left child at p+1 and its right child at p + 2*leaves(left).
-// Nodes created in PLOC iteration k only have parents from later
-// iterations, so levels are laid out from the last iteration down.
 //
-// The same pass writes the traversal's own node format: one 64-byte record
+// Two passes.  (a) Top-down: nodes created in PLOC iteration k only have
+// parents from later iterations, so levels run from the last iteration
+// down; a node reads its (DFS position, first leaf below, depth parity),
+// passes them to its children and records dfs[p] = node id for itself and
+// for its leaf children.  Only these few words move per node.  (b) One
+// parallel pass over the DFS positions in order writes every output record
+// once, so the node array and the traversal nodes are written coalesced.
+//
+// Output (b) also writes the traversal's own node format: one 64-byte record
 // per internal node holding both children's boxes and references, indexed by
 // the node's rank among internal nodes in DFS order (position minus the
 // leaves before it, i.e. minus its first leaf).  Leaves are referenced by
 // their sorted position, which is also their left-to-right order in the tree
 // (PLOC merges keep Morton order), so the traversal's triangles are stored
 // in that order.
-__device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict__ node_box,
-                                            const uint32_t* __restrict__ node_lc, uint2* __restrict__ pf, uint32_t N,
-                                            crt_bvh_node* __restrict__ out, float4* __restrict__ wide,
-                                            uint8_t* __restrict__ depth_odd, uint32_t* err) {
-    // (DFS position, first leaf below) of X; the root sits at (0, 0)
-    const uint2 me = (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
-    const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;  // bit 31: depth parity
-    const float4 mn = __ldcg(node_box + 2 * static_cast<size_t>(X)), mx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
-    const uint32_t a = __float_as_uint(mn.w), b = __float_as_uint(mx.w);
-    const uint32_t lca = (a < N) ? 1u : __ldcg(node_lc + (a - N));
+__device__ __forceinline__ uint2 layout_place(uint32_t X, const uint2* __restrict__ pf, uint32_t N) {
+    // (DFS position, first leaf below | depth parity << 31) of X; the root sits at (0, 0)
+    return (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
+}
+
+__device__ __forceinline__ void layout_down(uint32_t X, const float4* __restrict__ node_box,
+                                            const uint4* __restrict__ node_kids, uint2* __restrict__ pf, uint32_t N,
+                                            uint32_t* __restrict__ dfs, uint32_t* err) {
+    const uint2 me = layout_place(X, pf, N);
+    const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
+    const uint4 kids = __ldcg(node_kids + (X - N));  // left id, right id, their leaf counts
+    const uint32_t a = kids.x, b = kids.y, lca = kids.z;
     const uint32_t pl = p + 1, pr = p + 2 * lca;
     if (pr >= 2 * N - 1 || p < f || p - f >= N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
         raise_corrupt(err, 4, X, pr);
         return;
     }
+    dfs[p] = X;
+    const uint32_t nodd = (odd ^ 1u) << 31;
+    if (a < N) dfs[pl] = a; else pf[a - N] = make_uint2(pl, f | nodd);
+    if (b < N) dfs[pr] = b; else pf[b - N] = make_uint2(pr, (f + lca) | nodd);
+}
+
+__device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict__ node_box,
+                                            const uint4* __restrict__ node_kids, const uint2* __restrict__ pf,
+                                            uint32_t N, const uint32_t* __restrict__ dfs, crt_bvh_node* __restrict__ out,
+                                            float4* __restrict__ wide, uint8_t* __restrict__ depth_odd, uint32_t* err) {
+    const uint32_t X = __ldcg(dfs + p);
+    if (X >= 2 * N - 1) { raise_corrupt(err, 5, p, X); return; }
+    const float4 mn = __ldcg(node_box + 2 * static_cast<size_t>(X)), mx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
     float4* o = reinterpret_cast<float4*>(out + p);
     o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
     o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
+    if (X < N) {  // leaf: its triangle
+        reinterpret_cast<uint4*>(o)[2] = make_uint4(__float_as_uint(mn.w), 0u, 0u, 0u);
+        return;
+    }
+    const uint2 me = layout_place(X, pf, N);
+    const uint32_t f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
+    const uint4 kids = __ldcg(node_kids + (X - N));
+    const uint32_t a = kids.x, b = kids.y, lca = kids.z, lcb = kids.w;
+    const uint32_t pl = p + 1, pr = p + 2 * lca;
+    if (p < f || p - f >= N - 1) { raise_corrupt(err, 6, p, f); return; }
     reinterpret_cast<uint4*>(o)[2] = make_uint4(0u, pl, pr, 0u);
     const uint32_t ch[2] = {a, b}, cp[2] = {pl, pr}, cf[2] = {f, f + lca};
     float4 cmn[2], cmx[2];
@@ -638,19 +755,9 @@ __device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict
     for (int c = 0; c < 2; ++c) {
         cmn[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]));
         cmx[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]) + 1);
-        if (ch[c] < N) {
-            float4* lo = reinterpret_cast<float4*>(out + cp[c]);
-            lo[0] = make_float4(cmn[c].x, cmn[c].y, cmn[c].z, 0.f);
-            lo[1] = make_float4(cmx[c].x, cmx[c].y, cmx[c].z, 0.f);
-            reinterpret_cast<uint4*>(lo)[2] = make_uint4(__float_as_uint(cmn[c].w), 0u, 0u, 0u);
-            cref[c] = kLeafRef | ch[c];          // leaf: its sorted position
-        } else {
-            pf[ch[c] - N] = make_uint2(cp[c], cf[c] | ((odd ^ 1u) << 31));
-            cref[c] = cp[c] - cf[c];             // internal: its rank among internal nodes in DFS order
-        }
+        cref[c] = (ch[c] < N) ? (kLeafRef | ch[c])  // leaf: its sorted position
+                              : (cp[c] - cf[c]);    // internal: its rank among internal nodes in DFS order
     }
-    // traversal node: both child boxes and references in 64 bytes
-    const uint32_t lcb = (b < N) ? 1u : __ldcg(node_lc + (b - N));
     if (depth_odd) depth_odd[p - f] = static_cast<uint8_t>(odd);
     float4* w = wide + 4 * static_cast<size_t>(p - f);
     w[0] = make_float4(cmn[0].x, cmn[0].y, cmn[0].z, __uint_as_float(cref[0]));
@@ -660,14 +767,23 @@ __device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict
 }
 
 __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
-                                                           const uint32_t* __restrict__ node_lc,
+                                                           const uint4* __restrict__ node_kids,
                                                            uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
-                                                           uint32_t N, crt_bvh_node* __restrict__ out,
-                                                           float4* __restrict__ wide, uint8_t* __restrict__ depth_odd,
-                                                           uint32_t* err) {
+                                                           uint32_t N, uint32_t* __restrict__ dfs, uint32_t* err) {
     const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (X >= id_end) return;
-    layout_node(X, node_box, node_lc, pf, N, out, wide, depth_odd, err);
+    layout_down(X, node_box, node_kids, pf, N, dfs, err);
+}
+
+__global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restrict__ node_box,
+                                                          const uint4* __restrict__ node_kids,
+                                                          const uint2* __restrict__ pf, uint32_t N,
+                                                          const uint32_t* __restrict__ dfs, crt_bvh_node* __restrict__ out,
+                                                          float4* __restrict__ wide, uint8_t* __restrict__ depth_odd,
+                                                          uint32_t* err) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= 2 * N - 1) return;
+    layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, depth_odd, err);
 }
 
 // ================================== K3+K4 fused: one persistent launch
@@ -696,14 +812,18 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, uint32_t* err, u
 }
 
 template <int TILE, int BLOCK, int MAXR>
-__global__ void __launch_bounds__(BLOCK) ploc_persistent_kernel(float4* ca, float4* cb, float4* __restrict__ node_box,
-                                                                uint32_t* __restrict__ node_lc, uint2* it, uint32_t N,
+__global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kernel(float4* ca, float4* cb, float4* __restrict__ node_box,
+                                                                uint4* __restrict__ node_kids, uint2* it, uint32_t N,
                                                                 int R, unsigned long long* lookback, uint32_t* tickets,
                                                                 uint32_t n_tiles_cap, uint2* pf, crt_bvh_node* out,
                                                                 float4* wide, uint8_t* depth_odd, unsigned int* bar,
                                                                 uint32_t* iters_out, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile;
+    // iters_out[0]: iterations; [1]: blocks finished; then 64-bit globaltimer
+    // stamps: start, end of the PLOC loop, end of the layout.
+    unsigned long long* stamp = reinterpret_cast<unsigned long long*>(iters_out + 2);
+    if (blockIdx.x == 0 && threadIdx.x == 0) stamp[0] = global_ns();
     int iter = 0;
     for (;; ++iter) {
         const uint2 cur = __ldcg(it + iter);
@@ -717,22 +837,31 @@ __global__ void __launch_bounds__(BLOCK) ploc_persistent_kernel(float4* ca, floa
             if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
             __syncthreads();
             const uint32_t tile = s_tile;
-            if (tile * TILE >= cur.x) break;
+            if (tile * ploc_own(R) >= cur.x) break;
             if (tile == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
-            ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_lc, it, N, R, lb_cur, lb_next,
+            ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur, lb_next,
                                          err, spin_limit);
         }
         if (!grid_barrier(bar, err, spin_limit)) return;
         if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *iters_out = static_cast<uint32_t>(iter);
-    // DFS layout, last iteration's nodes first
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        iters_out[0] = static_cast<uint32_t>(iter);
+        stamp[1] = global_ns();
+    }
+    // DFS layout: top-down levels, last iteration's nodes first, into dfs
+    // (the first cluster buffer, free now), then every position in order.
+    uint32_t* dfs = reinterpret_cast<uint32_t*>(ca);
     for (int k = iter - 1; k >= 0; --k) {
         const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
         for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
-            layout_node(X, node_box, node_lc, pf, N, out, wide, depth_odd, err);
-        if (k > 0 && !grid_barrier(bar, err, spin_limit)) return;
+            layout_down(X, node_box, node_kids, pf, N, dfs, err);
+        if (!grid_barrier(bar, err, spin_limit)) return;
     }
+    for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
+        layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, depth_odd, err);
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(iters_out + 1, 1u) + 1u == gridDim.x) stamp[2] = global_ns();
 }
 
 __global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out) {
@@ -841,22 +970,27 @@ void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models,
                                                      err);
 }
 
-void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,
+void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint4* node_kids, uint2* it,
                            int iter, uint32_t N, int radius, uint32_t n_upper,
                            unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
                            uint32_t spin_limit, cudaStream_t s) {
-    const uint32_t tiles = (n_upper + kPlocTile - 1) / kPlocTile;
-    ploc_iteration_kernel<kPlocTile, 256, kPlocMaxRadius><<<tiles ? tiles : 1u, 256, 0, s>>>(
-        cin, cout, node_box, node_lc, it, iter, N, radius, lookback, tickets, n_tiles_cap, err, spin_limit);
+    const uint32_t tiles = (n_upper + ploc_own(radius) - 1) / ploc_own(radius);
+    ploc_iteration_kernel<kPlocSpan, 256, kPlocMaxRadius><<<tiles ? tiles : 1u, 256, 0, s>>>(
+        cin, cout, node_box, node_kids, it, iter, N, radius, lookback, tickets, n_tiles_cap, err, spin_limit);
 }
 
-void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
-                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint8_t* depth_odd,
-                         uint32_t* err, cudaStream_t s) {
+void launch_layout_level(const float4* node_box, const uint4* node_kids, uint2* pf, uint32_t id_begin,
+                         uint32_t id_end, uint32_t N, uint32_t* dfs, uint32_t* err, cudaStream_t s) {
     if (id_end <= id_begin || id_end > 2 * N - 1) return;
     const uint32_t cnt = id_end - id_begin;
-    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_lc, pf, id_begin, id_end, N, out, wide,
-                                                          depth_odd, err);
+    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, id_begin, id_end, N, dfs, err);
+}
+
+void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
+                        const uint32_t* dfs, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, uint32_t* err,
+                        cudaStream_t s) {
+    const uint32_t cnt = 2 * N - 1;
+    layout_emit_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, N, dfs, out, wide, depth_odd, err);
 }
 
 int ploc_persistent_grid() {
@@ -867,9 +1001,9 @@ int ploc_persistent_grid() {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
         if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                        &per_sm, ploc_persistent_kernel<kPlocTile, 256, kPlocMaxRadius>, 256, 0) == cudaSuccess &&
+                        &per_sm, ploc_persistent_kernel<kPlocSpan, 256, kPlocMaxRadius>, 256, 0) == cudaSuccess &&
             per_sm > 0)
-            grid = (per_sm < 2 ? per_sm : 2) * sms;
+            grid = (per_sm < kPlocBlocksPerSm ? per_sm : kPlocBlocksPerSm) * sms;
         else
             grid = 0;
         cudaGetLastError();
@@ -877,15 +1011,15 @@ int ploc_persistent_grid() {
     return grid;
 }
 
-cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint32_t* node_lc, uint2* it, uint32_t N,
+cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
                                    uint2* pf, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, unsigned int* bar,
                                    uint32_t* iters_out, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
     const int grid = ploc_persistent_grid();
     if (grid <= 0) return cudaErrorNotSupported;
-    void* args[] = {&ca, &cb, &node_box, &node_lc, &it, &N, &radius, &lookback, &tickets, &n_tiles_cap, &pf, &out,
+    void* args[] = {&ca, &cb, &node_box, &node_kids, &it, &N, &radius, &lookback, &tickets, &n_tiles_cap, &pf, &out,
                     &wide, &depth_odd, &bar, &iters_out, &err, &spin_limit};
-    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ploc_persistent_kernel<kPlocTile, 256, kPlocMaxRadius>),
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ploc_persistent_kernel<kPlocSpan, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }
 

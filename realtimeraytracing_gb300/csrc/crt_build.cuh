@@ -10,8 +10,15 @@
 
 namespace crt {
 
-constexpr uint32_t kPlocTile = 1024;      // positions per PLOC tile
+// A PLOC tile: one 256-thread block finds the nearest neighbours of
+// kPlocSpan consecutive positions (4 per thread) and decides the merges of
+// the ploc_own(R) = kPlocSpan - 2R positions in their middle.
+constexpr uint32_t kPlocSpan = 1024;
 constexpr int kPlocMaxRadius = 32;        // largest supported PLOC radius
+// Co-resident blocks per SM of the persistent (cooperative) PLOC launches.
+constexpr int kPlocBlocksPerSm = 3;
+constexpr uint32_t kPlocMinOwn = kPlocSpan - 2u * kPlocMaxRadius;  // sizes look-back arrays for any radius
+__host__ __device__ constexpr uint32_t ploc_own(int radius) { return kPlocSpan - 2u * static_cast<uint32_t>(radius); }
 constexpr uint32_t kLeafRef = 0x80000000u;  // traversal child reference: leaf flag | sorted position
 constexpr uint32_t kNoChild = 0xFFFFFFFFu;  // empty slot of a 4-wide node
 
@@ -42,18 +49,23 @@ void launch_onesweep_segments(const uint32_t* keys_in, const uint32_t* vals_in, 
                               uint32_t* lookback, uint32_t* ticket, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
                       float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, uint32_t* err, cudaStream_t s);
-void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint32_t* node_lc, uint2* it,
+void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint4* node_kids, uint2* it,
                            int iter, uint32_t N, int radius, uint32_t n_upper,
                            unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
                            uint32_t spin_limit, cudaStream_t s);
-void launch_layout_level(const float4* node_box, const uint32_t* node_lc, uint2* pf, uint32_t id_begin,
-                         uint32_t id_end, uint32_t N, crt_bvh_node* out, float4* wide, uint8_t* depth_odd,
-                         uint32_t* err, cudaStream_t s);
+// DFS layout as separate launches: one top-down level (nodes [id_begin,
+// id_end)) recording dfs[position] = node, then the emit pass over all
+// positions.
+void launch_layout_level(const float4* node_box, const uint4* node_kids, uint2* pf, uint32_t id_begin,
+                         uint32_t id_end, uint32_t N, uint32_t* dfs, uint32_t* err, cudaStream_t s);
+void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
+                        const uint32_t* dfs, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, uint32_t* err,
+                        cudaStream_t s);
 void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s);
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
 // All PLOC iterations and the DFS layout in one cooperative launch; returns
 // cudaErrorNotSupported when a cooperative launch is unavailable.
-cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint32_t* node_lc, uint2* it, uint32_t N,
+cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
                                    uint2* pf, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, unsigned int* bar,
                                    uint32_t* iters_out, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
@@ -111,7 +123,7 @@ void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchSce
                             float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, crt_bvh_node* nodes,
                             uint32_t* err, cudaStream_t s);
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
-                              uint32_t* node_lc, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
+                              uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
                               unsigned int* bar, uint32_t max_iters, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 // Sets the message crt_last_error_string() returns on the calling thread.
