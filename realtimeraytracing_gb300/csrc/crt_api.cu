@@ -89,7 +89,7 @@ struct crt_bvh {
     uint32_t n = 0;
     uint32_t iterations = 0;
     float abs_eps = 0.f;
-    DevBuf nodes, wide, depth_odd, xtri, codes, perm, inv_perm;
+    DevBuf nodes, wide, wide_wt, depth_odd, xtri, codes, perm, inv_perm;  // wide_wt: boxes grown by abs_eps
     mutable DevBuf wide4;
     crt_predictor* predictor = nullptr;
     // The 4-wide traversal nodes are derived on the first CRT_TRACE_WIDE
@@ -308,6 +308,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
     CRT_TRY(b->wide.reserve(64ull * N));
+    CRT_TRY(b->wide_wt.reserve(64ull * N));
     b->wide4_ready = false;
     CRT_TRY(b->depth_odd.reserve(N));
     CRT_TRY(b->inv_perm.reserve(4ull * N));
@@ -383,7 +384,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         const cudaError_t e = crt::launch_ploc_persistent(
             x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_kids.as<uint4>(), d_it, N,
             static_cast<int>(x->cfg.ploc_radius), lb, tail, ploc_tiles, x->pos.as<uint2>(), b->nodes.as<crt_bvh_node>(),
-            b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), tail + 2, tail + 4, err, x->cfg.spin_limit, s);
+            b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), st, tail + 2, tail + 4, err,
+            x->cfg.spin_limit, s);
         if (e == cudaSuccess) {
             CRT_CUDA(cudaEventRecord(x->ev[3], s));
             uint32_t* hp = static_cast<uint32_t*>(x->pinned);
@@ -459,7 +461,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
             crt::launch_layout_level(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(),
                                      x->it_host[k].y, x->it_host[k + 1].y, N, dfs, err, s);
         crt::launch_layout_emit(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(), N, dfs,
-                                b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), err, s);
+                                b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->wide_wt.as<float4>(),
+                                b->depth_odd.as<uint8_t>(), st, err, s);
     }
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->ev[4], s));
@@ -476,18 +479,13 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     x->stats.ms_ploc = ms[2] - layout_in_kernel_ms;
     x->stats.ms_layout = ms[3] + layout_in_kernel_ms;
     x->stats.ms_total = ms[0] + ms[1] + ms[2] + ms[3];
-    float ext = 0.f;
     for (int a = 0; a < 3; ++a) {
         x->stats.scene_box[a] = hs.scene_min[a];
         x->stats.scene_box[3 + a] = hs.scene_max[a];
-        const float e = hs.scene_max[a] - hs.scene_min[a];
-        if (std::isfinite(e) && e > ext) ext = e;
-        const float m = std::fmax(std::fabs(hs.scene_min[a]), std::fabs(hs.scene_max[a]));
-        if (std::isfinite(m) && m > ext) ext = m;
     }
     b->n = N;
     b->iterations = iters;
-    b->abs_eps = std::ldexp(ext > 0.f ? ext : 1.f, -20);
+    b->abs_eps = hs.abs_eps;  // the value the layout grew the watertight nodes by
     b->ctx = x;
     return CRT_OK;
 }
@@ -528,7 +526,7 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
     p.xtri = b->xtri.as<float4>();
-    p.wide = b->wide.as<float4>();
+    p.wide = (flags & CRT_TRI_WATERTIGHT) ? b->wide_wt.as<float4>() : b->wide.as<float4>();
     p.wide4 = (b->n > 1) ? b->wide4.as<float4>() : nullptr;
     p.rays = d_rays;
     p.hits = d_hits;
@@ -592,6 +590,7 @@ crt_status crt_bvh_free(crt_bvh* b) {
     b->nodes.release();
     b->xtri.release();
     b->wide.release();
+    b->wide_wt.release();
     b->wide4.release();
     b->depth_odd.release();
     b->inv_perm.release();
@@ -1023,7 +1022,7 @@ struct crt_batch {
     DevBuf scenes, seg_off, seg_hist, chunks, states, models, err;
     DevBuf codes_a, codes_b, vals_a, vals_b, codes, perm_global, perm_local;
     DevBuf node_box, node_kids, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
-    DevBuf nodes, wide, depth_odd, xtri, inv_perm;
+    DevBuf nodes, wide, wide_wt, depth_odd, xtri, inv_perm;
     bool models_set = false;
     cudaGraphExec_t graph = nullptr;
     const void* g_tris = nullptr;
@@ -1100,7 +1099,7 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
             bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->clus_a.as<float4>(), bt->clus_b.as<float4>(),
             bt->node_box.as<float4>(), bt->node_kids.as<uint4>(), bt->it.as<uint2>(), static_cast<int>(bt->cfg.ploc_radius),
             lb, bt->lb_cap, tail, bt->pf.as<uint2>(), bt->nodes.as<crt_bvh_node>(), bt->wide.as<float4>(),
-            bt->depth_odd.as<uint8_t>(), tail + 2, bt->max_n + 1, err, x->cfg.spin_limit, s);
+            bt->wide_wt.as<float4>(), bt->depth_odd.as<uint8_t>(), tail + 2, bt->max_n + 1, err, x->cfg.spin_limit, s);
         if (e != cudaSuccess) return fail(CRT_ERR_UNSUPPORTED, "batched PLOC launch failed: %s", cudaGetErrorString(e));
     }
     CRT_CUDA(cudaGetLastError());
@@ -1108,7 +1107,7 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
     if (rays) {
         crt::TraceParams p{};
         p.nodes = bt->nodes.as<crt_bvh_node>();
-        p.wide = bt->wide.as<float4>();
+        p.wide = (flags & CRT_TRI_WATERTIGHT) ? bt->wide_wt.as<float4>() : bt->wide.as<float4>();
         p.xtri = bt->xtri.as<float4>();
         p.rays = rays;
         p.hits = hits;
@@ -1211,6 +1210,7 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
     R(bt->sort_lb, 4ull * 9 * (static_cast<size_t>(max_tiles) * 256 + 1));
     R(bt->nodes, sizeof(crt_bvh_node) * 2ull * N);
     R(bt->wide, 64ull * N);
+    R(bt->wide_wt, 64ull * N);
     R(bt->depth_odd, N);
     R(bt->xtri, 48ull * N);
     if (st != CRT_OK) { crt_batch_free(bt); return st; }
@@ -1238,7 +1238,7 @@ crt_status crt_batch_free(crt_batch* bt) {
     DevBuf* bufs[] = {&bt->scenes, &bt->seg_off, &bt->seg_hist, &bt->chunks, &bt->states, &bt->models, &bt->err,
                       &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
                       &bt->perm_local, &bt->node_box, &bt->node_kids, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
-                      &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->depth_odd, &bt->xtri,
+                      &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->wide_wt, &bt->depth_odd, &bt->xtri,
                       &bt->inv_perm};
     for (DevBuf* b : bufs) b->release();
     delete bt;
@@ -1288,7 +1288,7 @@ crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint3
     CRT_CUDA(cudaMemsetAsync(bt->err.p, 0, 16, x->stream));
     crt::TraceParams p{};
     p.nodes = bt->nodes.as<crt_bvh_node>();
-    p.wide = bt->wide.as<float4>();
+    p.wide = (flags & CRT_TRI_WATERTIGHT) ? bt->wide_wt.as<float4>() : bt->wide.as<float4>();
     p.xtri = bt->xtri.as<float4>();
     p.rays = rays;
     p.hits = hits;

@@ -135,16 +135,11 @@ __global__ void __launch_bounds__(256) batch_box_kernel(const crt_triangle* __re
         cmx[a] += delta;
         cmn[a] -= delta;
     }
-    float ext = 0.f;
     for (int a = 0; a < 3; ++a) {
         st->cube_min[a] = cmn[a];
         st->cube_len[a] = cmx[a] - cmn[a];
-        const float e = smax[a] - smin[a];
-        if (isfinite(e) && e > ext) ext = e;
-        const float m = fmaxf(fabsf(smin[a]), fabsf(smax[a]));
-        if (isfinite(m) && m > ext) ext = m;
     }
-    scenes[ch.scene].abs_eps = ldexpf(ext > 0.f ? ext : 1.f, -20);
+    scenes[ch.scene].abs_eps = scene_abs_eps(smin, smax);
 }
 
 __device__ __forceinline__ uint32_t expand_bits_b(uint32_t v) {
@@ -256,9 +251,9 @@ template <int TILE, int BLOCK, int MAXR>
 __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb,
                                                            float4* node_box, uint4* node_kids, uint2* it, int R,
                                                            unsigned long long* lookback, uint32_t lb_cap, uint32_t* tickets,
-                                                           uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
-                                                           unsigned int* bar, uint32_t max_iters, uint32_t* err,
-                                                           uint32_t spin_limit) {
+                                                           uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
+                                                           uint8_t* depth_odd, unsigned int* bar, uint32_t max_iters,
+                                                           uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile_pre[kMaxBatchScenes + 1];
     __shared__ uint32_t s_n[kMaxBatchScenes];
@@ -376,7 +371,8 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
         const BatchScene B = scenes[lo];
         layout_emit(q - s_tile_pre[lo], node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off,
                     pf + B.tri_off, B.n_tris, dfs + B.node_off, nodes + B.node_off,
-                    wide + 4 * static_cast<size_t>(B.wide_off), depth_odd + B.wide_off, err);
+                    wide + 4 * static_cast<size_t>(B.wide_off), wide_wt + 4 * static_cast<size_t>(B.wide_off),
+                    depth_odd + B.wide_off, B.abs_eps, err);
     }
 }
 
@@ -425,12 +421,13 @@ void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchSce
 
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
                               uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
-                              uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
-                              unsigned int* bar, uint32_t max_iters, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+                              uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
+                              uint8_t* depth_odd, unsigned int* bar, uint32_t max_iters, uint32_t* err,
+                              uint32_t spin_limit, cudaStream_t s) {
     const int grid = batch_ploc_grid();
     if (grid <= 0) return cudaErrorNotSupported;
     void* args[] = {&scenes, &n_scenes, &ca, &cb, &node_box, &node_kids, &it, &radius, &lookback, &lb_cap, &tickets,
-                    &pf, &nodes, &wide, &depth_odd, &bar, &max_iters, &err, &spin_limit};
+                    &pf, &nodes, &wide, &wide_wt, &depth_odd, &bar, &max_iters, &err, &spin_limit};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(batch_ploc_kernel<kPlocSpan, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }

@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(256) scene_box_kernel(const crt_triangle* __re
         st->cube_min[a] = cmn[a];
         st->cube_len[a] = cmx[a] - cmn[a];  // getNormalizedCentroids (bvh.cpp:319-321)
     }
+    st->abs_eps = scene_abs_eps(smin, smax);
 }
 
 // ====================================================== K1: Morton codes
@@ -727,10 +728,14 @@ __device__ __forceinline__ void layout_down(uint32_t X, const float4* __restrict
     if (b < N) dfs[pr] = b; else pf[b - N] = make_uint2(pr, (f + lca) | nodd);
 }
 
+// grow: the scene's abs_eps; wide_wt receives the traversal nodes with every
+// child box grown by it (min - grow, max + grow, rounded as the traversal's
+// own box growth would round them), for watertight traces.
 __device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict__ node_box,
                                             const uint4* __restrict__ node_kids, const uint2* __restrict__ pf,
                                             uint32_t N, const uint32_t* __restrict__ dfs, crt_bvh_node* __restrict__ out,
-                                            float4* __restrict__ wide, uint8_t* __restrict__ depth_odd, uint32_t* err) {
+                                            float4* __restrict__ wide, float4* __restrict__ wide_wt,
+                                            uint8_t* __restrict__ depth_odd, float grow, uint32_t* err) {
     const uint32_t X = __ldcg(dfs + p);
     if (X >= 2 * N - 1) { raise_corrupt(err, 5, p, X); return; }
     const float4 mn = __ldcg(node_box + 2 * static_cast<size_t>(X)), mx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
@@ -764,6 +769,11 @@ __device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict
     w[1] = make_float4(cmx[0].x, cmx[0].y, cmx[0].z, __uint_as_float(cref[1]));
     w[2] = make_float4(cmn[1].x, cmn[1].y, cmn[1].z, __uint_as_float(lca));  // leaf counts of the children
     w[3] = make_float4(cmx[1].x, cmx[1].y, cmx[1].z, __uint_as_float(lcb));
+    float4* g = wide_wt + 4 * static_cast<size_t>(p - f);
+    g[0] = make_float4(cmn[0].x - grow, cmn[0].y - grow, cmn[0].z - grow, __uint_as_float(cref[0]));
+    g[1] = make_float4(cmx[0].x + grow, cmx[0].y + grow, cmx[0].z + grow, __uint_as_float(cref[1]));
+    g[2] = make_float4(cmn[1].x - grow, cmn[1].y - grow, cmn[1].z - grow, __uint_as_float(lca));
+    g[3] = make_float4(cmx[1].x + grow, cmx[1].y + grow, cmx[1].z + grow, __uint_as_float(lcb));
 }
 
 __global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
@@ -779,11 +789,12 @@ __global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restri
                                                           const uint4* __restrict__ node_kids,
                                                           const uint2* __restrict__ pf, uint32_t N,
                                                           const uint32_t* __restrict__ dfs, crt_bvh_node* __restrict__ out,
-                                                          float4* __restrict__ wide, uint8_t* __restrict__ depth_odd,
-                                                          uint32_t* err) {
+                                                          float4* __restrict__ wide, float4* __restrict__ wide_wt,
+                                                          uint8_t* __restrict__ depth_odd,
+                                                          const SceneState* __restrict__ st, uint32_t* err) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= 2 * N - 1) return;
-    layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, depth_odd, err);
+    layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, st->abs_eps, err);
 }
 
 // ================================== K3+K4 fused: one persistent launch
@@ -816,7 +827,8 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
                                                                 uint4* __restrict__ node_kids, uint2* it, uint32_t N,
                                                                 int R, unsigned long long* lookback, uint32_t* tickets,
                                                                 uint32_t n_tiles_cap, uint2* pf, crt_bvh_node* out,
-                                                                float4* wide, uint8_t* depth_odd, unsigned int* bar,
+                                                                float4* wide, float4* wide_wt, uint8_t* depth_odd,
+                                                                const SceneState* st, unsigned int* bar,
                                                                 uint32_t* iters_out, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile;
@@ -858,8 +870,9 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
             layout_down(X, node_box, node_kids, pf, N, dfs, err);
         if (!grid_barrier(bar, err, spin_limit)) return;
     }
+    const float grow = st->abs_eps;
     for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
-        layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, depth_odd, err);
+        layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, grow, err);
     __syncthreads();
     if (threadIdx.x == 0 && atomicAdd(iters_out + 1, 1u) + 1u == gridDim.x) stamp[2] = global_ns();
 }
@@ -987,10 +1000,11 @@ void launch_layout_level(const float4* node_box, const uint4* node_kids, uint2* 
 }
 
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
-                        const uint32_t* dfs, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, uint32_t* err,
-                        cudaStream_t s) {
+                        const uint32_t* dfs, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
+                        const SceneState* st, uint32_t* err, cudaStream_t s) {
     const uint32_t cnt = 2 * N - 1;
-    layout_emit_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, N, dfs, out, wide, depth_odd, err);
+    layout_emit_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd,
+                                                         st, err);
 }
 
 int ploc_persistent_grid() {
@@ -1013,12 +1027,13 @@ int ploc_persistent_grid() {
 
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
-                                   uint2* pf, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, unsigned int* bar,
-                                   uint32_t* iters_out, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+                                   uint2* pf, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
+                                   const SceneState* st, unsigned int* bar, uint32_t* iters_out, uint32_t* err,
+                                   uint32_t spin_limit, cudaStream_t s) {
     const int grid = ploc_persistent_grid();
     if (grid <= 0) return cudaErrorNotSupported;
     void* args[] = {&ca, &cb, &node_box, &node_kids, &it, &N, &radius, &lookback, &tickets, &n_tiles_cap, &pf, &out,
-                    &wide, &depth_odd, &bar, &iters_out, &err, &spin_limit};
+                    &wide, &wide_wt, &depth_odd, &st, &bar, &iters_out, &err, &spin_limit};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ploc_persistent_kernel<kPlocSpan, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }

@@ -33,7 +33,21 @@ struct SceneState {
     float scene_max[3];
     float cube_min[3];
     float cube_len[3];
+    float abs_eps;  // traversal slack of the scene, scene_abs_eps(scene_min, scene_max)
 };
+
+// Absolute slack of traversal pruning and of the watertight box growth:
+// 2^-20 of the largest finite extent or coordinate magnitude of the scene box.
+__host__ __device__ inline float scene_abs_eps(const float* smin, const float* smax) {
+    float ext = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        const float e = smax[a] - smin[a];
+        if (isfinite(e) && e > ext) ext = e;
+        const float m = fmaxf(fabsf(smin[a]), fabsf(smax[a]));
+        if (isfinite(m) && m > ext) ext = m;
+    }
+    return ldexpf(ext > 0.f ? ext : 1.f, -20);
+}
 
 void launch_scene_box(const crt_triangle* tris, uint32_t n_buffer, const float* models, SceneState* st, uint32_t* err,
                       cudaStream_t s);
@@ -59,21 +73,23 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
 void launch_layout_level(const float4* node_box, const uint4* node_kids, uint2* pf, uint32_t id_begin,
                          uint32_t id_end, uint32_t N, uint32_t* dfs, uint32_t* err, cudaStream_t s);
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
-                        const uint32_t* dfs, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, uint32_t* err,
-                        cudaStream_t s);
+                        const uint32_t* dfs, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
+                        const SceneState* st, uint32_t* err, cudaStream_t s);
 void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s);
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
 // All PLOC iterations and the DFS layout in one cooperative launch; returns
 // cudaErrorNotSupported when a cooperative launch is unavailable.
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
-                                   uint2* pf, crt_bvh_node* out, float4* wide, uint8_t* depth_odd, unsigned int* bar,
-                                   uint32_t* iters_out, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
+                                   uint2* pf, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
+                                   const SceneState* st, unsigned int* bar, uint32_t* iters_out, uint32_t* err,
+                                   uint32_t spin_limit, cudaStream_t s);
 
 // Trace side (crt_trace.cu).
 struct TraceParams {
     const crt_bvh_node* nodes;  // reference layout (root box read from nodes[0])
-    const float4* wide;      // 64-B traversal nodes: child boxes + child references
+    const float4* wide;      // 64-B traversal nodes: child boxes + child references (watertight
+                             // traces: boxes already grown by abs_eps)
     const float4* wide4;     // 128-B 4-wide traversal nodes (even-depth internal nodes)
     const float4* xtri;      // 3 float4 per leaf (sorted order): transformed p0 | tri id, p1, p2
     const crt_ray* rays;
@@ -124,8 +140,9 @@ void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchSce
                             uint32_t* err, cudaStream_t s);
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
                               uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
-                              uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, uint8_t* depth_odd,
-                              unsigned int* bar, uint32_t max_iters, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
+                              uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
+                              uint8_t* depth_odd, unsigned int* bar, uint32_t max_iters, uint32_t* err,
+                              uint32_t spin_limit, cudaStream_t s);
 // Sets the message crt_last_error_string() returns on the calling thread.
 void set_last_error(const char* msg);
 

@@ -121,10 +121,12 @@ struct RayCtx {
 // Slab test.  exact: raytracer.glsl:182-221 with GLSL min/max and early
 // exits.  Otherwise fminf/fmaxf, which decide identically when every 1/d is
 // finite and nonzero (no NaN can arise; a zero's sign changes no comparison).
-// grow widens the box on every side (watertight mode).
+// GROW widens the box by grow on every side (watertight mode); the binary
+// traversal nodes of watertight traces already hold grown boxes.
+template <bool GROW>
 __device__ __forceinline__ bool slab(const RayCtx& r, float4 mn, float4 mx, float grow, float& t_enter) {
-    const float mnx = mn.x - grow, mny = mn.y - grow, mnz = mn.z - grow;
-    const float mxx = mx.x + grow, mxy = mx.y + grow, mxz = mx.z + grow;
+    const float mnx = GROW ? mn.x - grow : mn.x, mny = GROW ? mn.y - grow : mn.y, mnz = GROW ? mn.z - grow : mn.z;
+    const float mxx = GROW ? mx.x + grow : mx.x, mxy = GROW ? mx.y + grow : mx.y, mxz = GROW ? mx.z + grow : mx.z;
     const float tx1 = (mnx - r.o.x) * r.inv.x, tx2 = (mxx - r.o.x) * r.inv.x;
     const float ty1 = (mny - r.o.y) * r.inv.y, ty2 = (mxy - r.o.y) * r.inv.y;
     const float tz1 = (mnz - r.o.z) * r.inv.z, tz2 = (mxz - r.o.z) * r.inv.z;
@@ -184,6 +186,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
 
     bool have = false;
     float bt = tmax, bu = 0.f, bv = 0.f;
+    float bound = prune_bound(bt, p.abs_eps);  // subtrees entered beyond this cannot hold the closest hit
     uint32_t bkey = 0xFFFFFFFFu, btri = CRT_MISS;
     uint32_t fetched = 0, tested = 0;
     bool overflow = false, corrupt = false;
@@ -203,6 +206,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
         const uint32_t key = WT ? tri : ~L;
         if (!have || h.t < bt || (h.t == bt && key < bkey)) {
             have = true; bt = h.t; bu = h.u; bv = h.v; bkey = key; btri = tri;
+            bound = prune_bound(bt, p.abs_eps);
         }
     };
 
@@ -220,16 +224,16 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
             const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
             const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
             float t0, t1;
-            bool h0 = ref0 != skip && slab(r, w0, w1, grow, t0);
-            bool h1 = ref1 != skip && slab(r, w2, w3, grow, t1);
-            const float bnd = prune_bound(bt, p.abs_eps);
+            bool h0 = ref0 != skip && slab<false>(r, w0, w1, 0.f, t0);
+            bool h1 = ref1 != skip && slab<false>(r, w2, w3, 0.f, t1);
+            const float bnd = bound;
             h0 = h0 && t0 <= bnd;
             h1 = h1 && t1 <= bnd;
             if (h0 && (ref0 & kLeafRef)) { test_leaf(ref0 & ~kLeafRef); h0 = false; }
             if (h1 && (ref1 & kLeafRef)) { test_leaf(ref1 & ~kLeafRef); h1 = false; }
             if (ANY && have) break;
             if (h0 || h1) {
-                const float bnd2 = prune_bound(bt, p.abs_eps);
+                const float bnd2 = bound;
                 h0 = h0 && t0 <= bnd2;
                 h1 = h1 && t1 <= bnd2;
             }
@@ -248,7 +252,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
             if (h0) { cur = ref0; continue; }
             if (h1) { cur = ref1; continue; }
             cur = 0xFFFFFFFFu;
-            const float bnd3 = prune_bound(bt, p.abs_eps);
+            const float bnd3 = bound;
             while (sp > 0) {
                 --sp;
                 if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
@@ -280,9 +284,9 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
                 hr[c] = 0xFFFFFFFFu;
                 if (rf[c] == kNoChild) continue;
                 float te;
-                if (!slab(r, make_float4(nx[c], ny[c], nz[c], 0.f), make_float4(xx[c], xy[c], xz[c], 0.f), grow, te))
+                if (!slab<WT>(r, make_float4(nx[c], ny[c], nz[c], 0.f), make_float4(xx[c], xy[c], xz[c], 0.f), grow, te))
                     continue;
-                if (te > prune_bound(bt, p.abs_eps)) continue;
+                if (te > bound) continue;
                 if (rf[c] & kLeafRef) {
                     test_leaf(rf[c] & ~kLeafRef);
                 } else {
@@ -291,7 +295,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
                 }
             }
             if (ANY && have) break;
-            const float bnd = prune_bound(bt, p.abs_eps);
+            const float bnd = bound;
 #pragma unroll
             for (int c = 0; c < 4; ++c)
                 if (ht[c] > bnd) { ht[c] = kInf; hr[c] = 0xFFFFFFFFu; }
@@ -316,7 +320,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
             }
             cur = hr[0];
             if (cur != 0xFFFFFFFFu) continue;
-            const float bnd3 = prune_bound(bt, p.abs_eps);
+            const float bnd3 = bound;
             while (sp > 0) {
                 --sp;
                 if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
@@ -326,7 +330,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
     // Enter a subtree whose box (mn, mx) and reference are known.
     auto enter = [&](float4 mn, float4 mx, uint32_t ref, uint32_t skip) {
         float te;
-        if (ref == skip || !slab(r, mn, mx, grow, te) || te > prune_bound(bt, p.abs_eps)) return;
+        if (ref == skip || !slab<WT>(r, mn, mx, grow, te) || te > bound) return;
         if (ref & kLeafRef) test_leaf(ref & ~kLeafRef);
         else if (WIDE) walk4(ref);   // the root has depth 0, so it is a 4-wide node
         else walk(ref, skip);
