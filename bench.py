@@ -128,6 +128,23 @@ def dist_setup():
     return world, rank, local
 
 
+def slowest_ms(t_ms: float, world: int, dev=None) -> float:
+    """Max of a per-rank time over all ranks (every rank gets it): replicas
+    finish together only when the slowest one does."""
+    if world <= 1:
+        return t_ms
+    import torch
+    tt = torch.tensor([t_ms], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_mrays(world: int, rays_per_replica: int, t_ms: float) -> float:
+    """Weak scaling: every replica traces its own frame of rays_per_replica
+    rays; the job's throughput is all of them over the slowest time."""
+    return world * rays_per_replica / (t_ms * 1e-3) / 1e6
+
+
 def make_scene():
     from realtimeraytracing_gb300 import scenes as S
     tris, models, cam, (w, h), light = S.config1_scene(seed=0)
@@ -204,12 +221,8 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    t_frame = sum(frame_ms) / len(frame_ms)
-    if world > 1:
-        tt = torch.tensor([t_frame], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_frame = float(tt.item())
-    value = world * rays_per_frame / (t_frame * 1e-3) / 1e6
+    t_frame = slowest_ms(sum(frame_ms) / len(frame_ms), world, dev)
+    value = whole_job_mrays(world, rays_per_frame, t_frame)
 
     # ---- the dominant kernel alone: primary closest-hit trace
     rays = torch.empty((n_rays, 8), dtype=torch.float32, device=dev)
@@ -243,12 +256,8 @@ def run_ours(args):
         t0 = time.perf_counter()
         ctx.trace_frame(bvh, cam_h, W, H, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_t = statistics.mean(e2e_ms)
-    if world > 1:
-        tt = torch.tensor([e2e_t], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(tt.item())
-    e2e_value = world * rays_per_frame / (e2e_t * 1e-3) / 1e6
+    e2e_t = slowest_ms(statistics.mean(e2e_ms), world, dev)
+    e2e_value = whole_job_mrays(world, rays_per_frame, e2e_t)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
