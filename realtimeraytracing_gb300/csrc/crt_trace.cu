@@ -115,6 +115,7 @@ __device__ __forceinline__ HitRes tri_watertight(float3 o, float tmin, float tma
 
 struct RayCtx {
     float3 o, d, inv;
+    float3 oi;    // o * inv, rounded: slab distances as one fma per plane (watertight walks)
     bool exact;   // some 1/d component is not finite or zero: use the shader's min/max
 };
 
@@ -149,6 +150,23 @@ __device__ __forceinline__ bool slab(const RayCtx& r, float4 mn, float4 mx, floa
     return tMax >= 0.f && tMin <= tMax;
 }
 
+// Watertight walks over the pre-grown traversal boxes: t = plane * (1/d) - o * (1/d) as one
+// fused multiply-add per plane.  Its error, like the shader form's, is a few ulps of the
+// plane's distance from the origin, which stays below the abs_eps the boxes are grown by
+// (2^-20 of the scene's largest coordinate or extent) for origins within 8 times that range,
+// so no box that the ray crosses is missed.  Rays with an infinite or zero 1/d take the
+// shader's form.
+__device__ __forceinline__ bool slab_wt(const RayCtx& r, float4 mn, float4 mx, float& t_enter) {
+    if (r.exact) return slab<false>(r, mn, mx, 0.f, t_enter);
+    const float tx1 = __fmaf_rn(mn.x, r.inv.x, -r.oi.x), tx2 = __fmaf_rn(mx.x, r.inv.x, -r.oi.x);
+    const float ty1 = __fmaf_rn(mn.y, r.inv.y, -r.oi.y), ty2 = __fmaf_rn(mx.y, r.inv.y, -r.oi.y);
+    const float tz1 = __fmaf_rn(mn.z, r.inv.z, -r.oi.z), tz2 = __fmaf_rn(mx.z, r.inv.z, -r.oi.z);
+    const float t0 = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
+    const float t1 = fminf(fminf(fmaxf(tx1, tx2), fmaxf(ty1, ty2)), fmaxf(tz1, tz2));
+    t_enter = t0;
+    return t1 >= 0.f && t0 <= t1;
+}
+
 __device__ __forceinline__ float prune_bound(float t, float abs_eps) {
     return t + (fabsf(t) * 6.103515625e-05f + abs_eps);  // 2^-14 relative
 }
@@ -177,6 +195,7 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
         return;
     }
     r.inv = make_float3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+    r.oi = make_float3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
     r.exact = !(isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && r.inv.x != 0.f && r.inv.y != 0.f &&
                 r.inv.z != 0.f);
     WRay w{};
@@ -224,8 +243,14 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
             const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
             const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
             float t0, t1;
-            bool h0 = ref0 != skip && slab<false>(r, w0, w1, 0.f, t0);
-            bool h1 = ref1 != skip && slab<false>(r, w2, w3, 0.f, t1);
+            bool h0, h1;
+            if (WT) {
+                h0 = ref0 != skip && slab_wt(r, w0, w1, t0);
+                h1 = ref1 != skip && slab_wt(r, w2, w3, t1);
+            } else {
+                h0 = ref0 != skip && slab<false>(r, w0, w1, 0.f, t0);
+                h1 = ref1 != skip && slab<false>(r, w2, w3, 0.f, t1);
+            }
             const float bnd = bound;
             h0 = h0 && t0 <= bnd;
             h1 = h1 && t1 <= bnd;
@@ -238,7 +263,9 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
                 h1 = h1 && t1 <= bnd2;
             }
             if (h0 && h1) {
-                const bool near1 = t1 < t0;
+                // closest hit: nearer child first; any hit: farther child first (an
+                // occluder of a ray leaving a surface is rarely next to its origin)
+                const bool near1 = ANY ? !(t1 < t0) : (t1 < t0);
                 if (sp < STACK) {
                     st_node[sp] = near1 ? ref0 : ref1;
                     st_t[sp] = near1 ? t0 : t1;
