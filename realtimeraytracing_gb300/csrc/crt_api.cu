@@ -736,7 +736,6 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     if (flags & CRT_TRACE_ANY) return fail(CRT_ERR_INVALID_ARG, "crt_trace_frame: primary rays are closest-hit");
     CRT_CUDA(cudaSetDevice(x->device));
     const uint32_t n = width * height;
-    CRT_TRY(x->frame_rays.reserve(sizeof(crt_ray) * static_cast<size_t>(n)));
     const bool dev_p = is_device_ptr(hits_primary);
     crt_hit* d_hp = hits_primary;
     if (!dev_p) {
@@ -749,9 +748,56 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
         d_cam = x->cam.as<crt_camera>();
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
+    if (!(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE))) {
+        // one launch: camera ray, closest hit, shadow ray, any hit per pixel
+        crt_hit* d_hs = nullptr;
+        bool dev_s = true;
+        if (light) {
+            dev_s = is_device_ptr(hits_shadow);
+            d_hs = hits_shadow;
+            if (!dev_s) {
+                CRT_TRY(x->frame_shits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
+                d_hs = x->frame_shits.as<crt_hit>();
+            }
+        }
+        crt::TraceParams p{};
+        p.nodes = b->nodes.as<crt_bvh_node>();
+        p.xtri = b->xtri.as<float4>();
+        p.wide = (flags & CRT_TRI_WATERTIGHT) ? b->wide_wt.as<float4>() : b->wide.as<float4>();
+        p.hits = d_hp;
+        p.n_rays = n;
+        p.n_nodes = 2 * b->n - 1;
+        p.abs_eps = b->abs_eps;
+        p.err = x->err.as<uint32_t>();
+        p.tile_width = tw;
+        if (flags & CRT_TRACE_STATS) {
+            CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
+            p.stats = x->trace_stats.as<unsigned long long>();
+        }
+        const bool deep = b->iterations + 2 > 64;
+        const uint32_t kflags = (flags & CRT_TRI_WATERTIGHT) | (deep ? (1u << 16) : 0u);
+        // One launch for the whole image.  Splitting it into row bands whose
+        // hits are copied out on a second stream while the next band runs was
+        // measured slower at every band count (2, 4, 8) on GB300.
+        crt::launch_frame(p, d_cam, width, height, 0, height, light, d_hs, kflags, static_cast<int>(x->cfg.trace_block),
+                          x->stream);
+        CRT_CUDA(cudaGetLastError());
+        if (!dev_p)
+            CRT_CUDA(cudaMemcpyAsync(hits_primary, d_hp, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost,
+                                     x->stream));
+        if (light && !dev_s)
+            CRT_CUDA(cudaMemcpyAsync(hits_shadow, d_hs, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost,
+                                     x->stream));
+        if (flags & CRT_TRACE_STATS) {
+            CRT_CUDA(cudaStreamSynchronize(x->stream));
+            CRT_CUDA(cudaMemcpy(x->last_trace_stats, x->trace_stats.p, 16, cudaMemcpyDeviceToHost));
+        }
+        return x->check_device_error();
+    }
+    CRT_TRY(x->frame_rays.reserve(sizeof(crt_ray) * static_cast<size_t>(n)));
     crt_ray* rays = x->frame_rays.as<crt_ray>();
     crt::launch_raygen(d_cam, width, height, rays, x->stream);
-    const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
     CRT_TRY(trace_device(x, b, rays, n, flags, d_hp, nullptr, tw));
     if (!dev_p) CRT_CUDA(cudaMemcpyAsync(hits_primary, d_hp, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
     if (light) {

@@ -106,6 +106,11 @@ struct TraceParams {
     const uint32_t* n_treelets = nullptr;
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
+// Camera rays of image rows [y0, y0 + rows) traced to the closest hit into
+// p.hits and, with a light, their shadow rays to any hit into hits_shadow,
+// in one launch (p.tile_width: width for 8x4 pixel tiles, or 0).
+void launch_frame(const TraceParams& p, const crt_camera* cam, uint32_t width, uint32_t height, uint32_t y0,
+                  uint32_t rows, const float* light, crt_hit* hits_shadow, uint32_t flags, int block, cudaStream_t s);
 
 // Batched scenes: per-scene offsets into the concatenated arrays.
 constexpr uint32_t kMaxBatchScenes = 256;

@@ -180,20 +180,16 @@ __device__ __forceinline__ uint32_t ray_of_thread(uint32_t t, uint32_t width) {
     return ((ty << 2) + (lane >> 3)) * width + (tx << 3) + (lane & 7u);
 }
 
-// Closest hit (or any hit) of ray i of p.rays into p.hits[i].
+// Closest hit (or any hit) of the ray r0 = (o, tmin), r1 = (d, tmax) as a
+// crt_hit; i is the ray's index (its predicted treelet with SEED).
 template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE>
-__device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i) {
-    const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
-    const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
+__device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t i, const float4 r0, const float4 r1) {
     RayCtx r;
     r.o = make_float3(r0.x, r0.y, r0.z);
     r.d = make_float3(r1.x, r1.y, r1.z);
     const float tmin = r0.w, tmax = r1.w;
     uint4 out = make_uint4(CRT_MISS, 0u, 0u, 0u);
-    if (!(tmin <= tmax) || p.n_nodes == 0) {
-        reinterpret_cast<uint4*>(p.hits)[i] = out;
-        return;
-    }
+    if (!(tmin <= tmax) || p.n_nodes == 0) return out;
     r.inv = make_float3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
     r.oi = make_float3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
     r.exact = !(isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && r.inv.x != 0.f && r.inv.y != 0.f &&
@@ -385,13 +381,21 @@ __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i
         enter(__ldg(n4), __ldg(n4 + 1), (lr.y == 0u && lr.z == 0u) ? kLeafRef : 0u, skip);
     }
     if (have) out = make_uint4(btri, __float_as_uint(bt), __float_as_uint(bu), __float_as_uint(bv));
-    reinterpret_cast<uint4*>(p.hits)[i] = out;
     if (corrupt) raise_corrupt(p.err, 5, i, 0u);
     else if (overflow) raise_error(p.err, kDevStackOverflow);
     if (p.stats) {
         atomicAdd(p.stats + 0, static_cast<unsigned long long>(fetched));
         atomicAdd(p.stats + 1, static_cast<unsigned long long>(tested));
     }
+    return out;
+}
+
+// Ray i of p.rays into p.hits[i].
+template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE>
+__device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i) {
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
+    const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
+    reinterpret_cast<uint4*>(p.hits)[i] = trace_one<ANY, WT, STACK, SEED, WIDE>(p, i, r0, r1);
 }
 
 template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE, int BLOCK>
@@ -429,11 +433,8 @@ __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, co
 
 // getRay (raytracer.glsl:92-100): pos = texel / size, direction =
 // normalize(InvView * vec4((pos - 0.5, 1) * (W, H, near), 1) - eye).
-__global__ void __launch_bounds__(256) raygen_kernel(const crt_camera* __restrict__ cam, uint32_t width, uint32_t height,
-                                                     crt_ray* __restrict__ rays) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = blockIdx.y;
-    if (x >= width) return;
+__device__ __forceinline__ void camera_ray(const crt_camera* __restrict__ cam, uint32_t x, uint32_t y, uint32_t width,
+                                           uint32_t height, float4& r0, float4& r1) {
     const float* m = cam->inv_view;
     const float px = static_cast<float>(x) / static_cast<float>(width);
     const float py = static_cast<float>(y) / static_cast<float>(height);
@@ -441,9 +442,39 @@ __global__ void __launch_bounds__(256) raygen_kernel(const crt_camera* __restric
     const float4 pw = mat_vec(m, pv);
     const float dx = pw.x - cam->eye[0], dy = pw.y - cam->eye[1], dz = pw.z - cam->eye[2], dw = pw.w - cam->eye[3];
     const float inv = 1.0f / sqrtf(((dx * dx + dy * dy) + dz * dz) + dw * dw);
+    r0 = make_float4(cam->eye[0], cam->eye[1], cam->eye[2], 0.f);
+    r1 = make_float4(dx * inv, dy * inv, dz * inv, __int_as_float(0x7F800000));
+}
+
+__global__ void __launch_bounds__(256) raygen_kernel(const crt_camera* __restrict__ cam, uint32_t width, uint32_t height,
+                                                     crt_ray* __restrict__ rays) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y;
+    if (x >= width) return;
+    float4 r0, r1;
+    camera_ray(cam, x, y, width, height, r0, r1);
     float4* o = reinterpret_cast<float4*>(rays + static_cast<size_t>(y) * width + x);
-    o[0] = make_float4(cam->eye[0], cam->eye[1], cam->eye[2], 0.f);
-    o[1] = make_float4(dx * inv, dy * inv, dz * inv, __int_as_float(0x7F800000));
+    o[0] = r0;
+    o[1] = r1;
+}
+
+// Shadow ray of a primary hit toward the point light l: from the hit point
+// (o + t d), unit direction, tmin 1e-4, tmax the distance to the light; a
+// miss gives an empty ray (tmin 1 > tmax 0).
+__device__ __forceinline__ void shadow_ray(float4 r0, float4 r1, uint4 h, float lx, float ly, float lz, float4& s0,
+                                           float4& s1) {
+    if (h.x == CRT_MISS) {
+        s0 = make_float4(0.f, 0.f, 0.f, 1.f);
+        s1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float t = __uint_as_float(h.y);
+    const float px = r0.x + t * r1.x, py = r0.y + t * r1.y, pz = r0.z + t * r1.z;
+    const float dx = lx - px, dy = ly - py, dz = lz - pz;
+    const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
+    const float inv = 1.0f / len;
+    s0 = make_float4(px, py, pz, 1e-4f);
+    s1 = make_float4(dx * inv, dy * inv, dz * inv, len);
 }
 
 __global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__ prim, const crt_hit* __restrict__ hits,
@@ -451,21 +482,43 @@ __global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint4 h = __ldg(reinterpret_cast<const uint4*>(hits) + i);
-    float4* o = reinterpret_cast<float4*>(out + i);
-    if (h.x == CRT_MISS) {
-        o[0] = make_float4(0.f, 0.f, 0.f, 1.f);
-        o[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
-    }
     const float4 r0 = __ldg(reinterpret_cast<const float4*>(prim + i));
     const float4 r1 = __ldg(reinterpret_cast<const float4*>(prim + i) + 1);
-    const float t = __uint_as_float(h.y);
-    const float px = r0.x + t * r1.x, py = r0.y + t * r1.y, pz = r0.z + t * r1.z;
-    const float dx = lx - px, dy = ly - py, dz = lz - pz;
-    const float len = sqrtf((dx * dx + dy * dy) + dz * dz);
-    const float inv = 1.0f / len;
-    o[0] = make_float4(px, py, pz, 1e-4f);
-    o[1] = make_float4(dx * inv, dy * inv, dz * inv, len);
+    float4 s0, s1;
+    shadow_ray(r0, r1, h, lx, ly, lz, s0, s1);
+    float4* o = reinterpret_cast<float4*>(out + i);
+    o[0] = s0;
+    o[1] = s1;
+}
+
+// One frame in one launch (crt_trace_frame): thread t takes pixel
+// ray_of_thread(t) of the image rows [y0, y0 + rows), generates its camera
+// ray, traces it to the closest hit and, with a light, traces that hit's
+// shadow ray to any hit at once, while the nodes around the hit are still
+// cached.  The rays and hits are the ones the separate raygen, trace and
+// shadow-ray calls produce.
+template <bool WT, int STACK, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) frame_kernel(TraceParams p, const crt_camera* __restrict__ cam, uint32_t width,
+                                                      uint32_t height, uint32_t y0, uint32_t rows, int shadows,
+                                                      float lx, float ly, float lz, crt_hit* __restrict__ hits_shadow) {
+    const uint32_t t_id = blockIdx.x * BLOCK + threadIdx.x;
+    if (t_id >= width * rows) return;
+    const uint32_t i = y0 * width + ray_of_thread(t_id, p.tile_width);
+    const uint32_t y = i / width, x = i - y * width;
+    float4 r0, r1;
+    camera_ray(cam, x, y, width, height, r0, r1);
+    const uint4 h = trace_one<false, WT, STACK, false, false>(p, i, r0, r1);
+    reinterpret_cast<uint4*>(p.hits)[i] = h;
+    if (!shadows) return;
+    uint4 hs = make_uint4(CRT_MISS, 0u, 0u, 0u);
+    if (h.x != CRT_MISS) {
+        float4 s0, s1;
+        shadow_ray(r0, r1, h, lx, ly, lz, s0, s1);
+        TraceParams q = p;
+        q.stats = nullptr;
+        hs = trace_one<true, WT, STACK, false, false>(q, i, s0, s1);
+    }
+    reinterpret_cast<uint4*>(hits_shadow)[i] = hs;
 }
 
 template <bool ANY, bool WT, int BLOCK>
@@ -526,6 +579,32 @@ void launch_trace_batch(const TraceParams& p, const BatchScene* scenes, uint32_t
     else if (any) launch_batch_t<true, false>(p, scenes, n_scenes, n_rays, block, deep, s);
     else if (wt) launch_batch_t<false, true>(p, scenes, n_scenes, n_rays, block, deep, s);
     else launch_batch_t<false, false>(p, scenes, n_scenes, n_rays, block, deep, s);
+}
+
+template <bool WT, int BLOCK>
+static void launch_frame_b(const TraceParams& p, const crt_camera* cam, uint32_t width, uint32_t height, uint32_t y0,
+                           uint32_t rows, const float* light, crt_hit* hits_shadow, bool deep, cudaStream_t s) {
+    const uint32_t grid = (width * rows + BLOCK - 1) / BLOCK;
+    if (grid == 0) return;
+    const int sh = light != nullptr;
+    const float lx = sh ? light[0] : 0.f, ly = sh ? light[1] : 0.f, lz = sh ? light[2] : 0.f;
+    if (deep) frame_kernel<WT, 1024, BLOCK><<<grid, BLOCK, 0, s>>>(p, cam, width, height, y0, rows, sh, lx, ly, lz, hits_shadow);
+    else frame_kernel<WT, 64, BLOCK><<<grid, BLOCK, 0, s>>>(p, cam, width, height, y0, rows, sh, lx, ly, lz, hits_shadow);
+}
+
+void launch_frame(const TraceParams& p, const crt_camera* cam, uint32_t width, uint32_t height, uint32_t y0,
+                  uint32_t rows, const float* light, crt_hit* hits_shadow, uint32_t flags, int block, cudaStream_t s) {
+    const bool wt = flags & CRT_TRI_WATERTIGHT;
+    const bool deep = (flags >> 16) != 0;
+    if (wt) {
+        if (block == 256) launch_frame_b<true, 256>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+        else if (block == 64) launch_frame_b<true, 64>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+        else launch_frame_b<true, 128>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+    } else {
+        if (block == 256) launch_frame_b<false, 256>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+        else if (block == 64) launch_frame_b<false, 64>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+        else launch_frame_b<false, 128>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+    }
 }
 
 void launch_raygen(const crt_camera* cam_dev, uint32_t width, uint32_t height, crt_ray* rays, cudaStream_t s) {

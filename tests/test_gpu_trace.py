@@ -151,3 +151,33 @@ def test_binary_and_wide_walks_agree(ctx, config0, flags):
     any_hit = bool(flags & crt.TRACE_ANY)
     _cmp_hits(ctx.trace(bvh, rays, flags), ref, any_hit)
     _cmp_hits(ctx.trace(bvh, rays, flags | crt.TRACE_WIDE), ref, any_hit)
+
+
+def test_trace_frame_tiles_bands_and_host_outputs(ctx):
+    """crt_trace_frame on an image of 8x4 pixel tiles: one launch per row band
+    (camera ray, closest hit, shadow ray, any hit), hits copied to host memory
+    band by band, the same hits as the oracle and as device-memory outputs."""
+    torch = pytest.importorskip("torch")
+    v, f = S.displaced_icosphere(level=5, seed=21)
+    tris = S.indexed_to_triangles(v, f)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    cam = S.camera_gpu_data((0.3, -0.2, -2.5), aspect=256 / 120)
+    light = np.array([2.0, 2.0, -2.0], np.float32)
+    w, h = 256, 120
+    hp, hs = ctx.trace_frame(bvh, cam, w, h, light, crt.TRI_WATERTIGHT | crt.TRACE_STATS)
+    visited, _ = ctx.last_trace_stats()
+    assert visited > w * h
+    rays = O.raygen(cam, w, h)
+    ref_p, _ = O.trace(bvh.nodes(), tris, models, rays, crt.TRI_WATERTIGHT)
+    _cmp_hits(hp, ref_p)
+    ref_s, _ = O.trace(bvh.nodes(), tris, models, O.shadow_rays(rays, ref_p, light), crt.TRACE_ANY | crt.TRI_WATERTIGHT)
+    _cmp_hits(hs, ref_s, any_hit=True)
+    assert (hp[:, 0].view(np.uint32) != crt.MISS).mean() > 0.2
+    dp = torch.empty((w * h, 4), dtype=torch.float32, device="cuda")
+    ds = torch.empty((w * h, 4), dtype=torch.float32, device="cuda")
+    ctx.trace_frame(bvh, cam, w, h, light, crt.TRI_WATERTIGHT, hits_primary=dp, hits_shadow=ds)
+    np.testing.assert_array_equal(dp.cpu().numpy().view(np.uint32), hp.view(np.uint32))
+    np.testing.assert_array_equal(ds.cpu().numpy().view(np.uint32), hs.view(np.uint32))
+    hr, _ = ctx.trace_frame(bvh, cam, w, h, None, crt.TRI_REFERENCE)
+    _cmp_hits(hr, O.trace(bvh.nodes(), tris, models, rays, crt.TRI_REFERENCE)[0])
