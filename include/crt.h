@@ -206,7 +206,10 @@ crt_status crt_last_trace_stats(crt_ctx* ctx, uint64_t out[2]);
  * not NULL — one any-hit shadow ray per primary hit toward the point light.
  * Rays live in context memory; only the camera goes in and the hits come out
  * (hits_primary[width*height], hits_shadow[width*height] or NULL; host or
- * device memory).  Shadow misses on primary misses are reported as CRT_MISS. */
+ * device memory).  Shadow misses on primary misses are reported as CRT_MISS.
+ * Plain frames (no CRT_TRACE_USE_PREDICTOR / CRT_TRACE_WIDE) run in one
+ * launch: each pixel's camera ray, closest hit, shadow ray and any hit; with
+ * CRT_TRACE_STATS the counts cover the primary and the shadow traversals. */
 crt_status crt_trace_frame(crt_ctx* ctx, const crt_bvh* bvh, const crt_camera* cam, uint32_t width,
                            uint32_t height, const float* light, uint32_t flags, crt_hit* hits_primary,
                            crt_hit* hits_shadow);

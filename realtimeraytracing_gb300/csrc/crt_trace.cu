@@ -514,9 +514,7 @@ __global__ void __launch_bounds__(BLOCK) frame_kernel(TraceParams p, const crt_c
     if (h.x != CRT_MISS) {
         float4 s0, s1;
         shadow_ray(r0, r1, h, lx, ly, lz, s0, s1);
-        TraceParams q = p;
-        q.stats = nullptr;
-        hs = trace_one<true, WT, STACK, false, false>(q, i, s0, s1);
+        hs = trace_one<true, WT, STACK, false, false>(p, i, s0, s1);
     }
     reinterpret_cast<uint4*>(hits_shadow)[i] = hs;
 }
