@@ -491,7 +491,8 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
     tris, models = S.config3_scene(seed=0)
     d_tris = torch.from_numpy(tris).to(dev)
     bvh = ctx.build(d_tris, models=torch.from_numpy(models).to(dev))
-    build_ms = ctx.last_build_stats()["ms_total"]
+    bst = ctx.last_build_stats()
+    build_ms, scene_box = bst["ms_total"], bst["scene_box"]  # scene box = root box (no padding)
     del d_tris
     cam = torch.from_numpy(S.camera_gpu_data((0.5, 0.5, -1.5))).to(dev)
     w = 2048
@@ -508,10 +509,12 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
     cls = torch.empty((n,), dtype=torch.int16, device=dev)
 
     def timed(fn, reps):
-        fn()
-        torch.cuda.synchronize()
+        # every call, the warm-up included, on the library's stream: torch work
+        # inside fn is then ordered with the library's kernels
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
         with torch.cuda.stream(stream):
+            fn()
+            torch.cuda.synchronize()
             for a, b in evs:
                 a.record(stream)
                 fn()
@@ -543,6 +546,27 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
     ctx.trace_seeded(bvh, rays, tcls, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=seeded)
     f_perfect, _ = ctx.last_trace_stats()
     identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
+    # rays grouped by predicted treelet (inference + one radix pass + trace), alone and with seeding
+    t_ordered = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER, out=seeded), reps)
+    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
+    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER | crt.TRACE_STATS, out=seeded)
+    f_ordered, _ = ctx.last_trace_stats()
+    t_ord_seed = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER | crt.USE_PREDICTOR,
+                                         out=seeded), reps)
+    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
+    # no network: rays sorted by the network's own input key (origin cell on the 64^3 grid of the scene
+    # box, octahedral direction bin 32x32), gathered, traced; the sort + gather is timed apart
+    key = ray_input_keys(torch, rays, scene_box)
+    def key_sort():
+        order = torch.argsort(key)
+        return rays.index_select(0, order), order
+    t_keysort = timed(key_sort, reps)
+    with torch.cuda.stream(stream):
+        srays, sorder = key_sort()
+        sh = torch.empty_like(plain)
+    torch.cuda.synchronize()
+    t_keytrace = timed(lambda: ctx.trace(bvh, srays, crt.TRI_WATERTIGHT, out=sh), reps)
+    keysort_identical = bool(torch.equal(sh.view(torch.int32), plain.index_select(0, sorder).view(torch.int32)))
     info = pred.info()
     pred.free()
     bvh.free()
@@ -561,10 +585,41 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
         "node_fetches_per_ray": {"plain": round(f_plain / n, 2), "seeded": round(f_seeded / n, 2),
                                  "perfect_prediction": round(f_perfect / n, 2)},
         "perfect_prediction_speedup": round(t_plain / t_perfect, 3),
+        "predictor_ordered": {"mrays_s": round(n / t_ordered / 1e3, 1), "speedup": round(t_plain / t_ordered, 3),
+                              "node_fetches_per_ray": round(f_ordered / n, 2),
+                              "note": "CRT_TRACE_PREDICTOR_ORDER: inference + order by (predicted treelet, origin-cell Morton code, direction bin) + trace"},
+        "predictor_ordered_seeded": {"mrays_s": round(n / t_ord_seed / 1e3, 1),
+                                     "speedup": round(t_plain / t_ord_seed, 3)},
+        "key_sorted_no_network": {"sort_gather_ms": round(t_keysort, 3), "trace_ms": round(t_keytrace, 3),
+                                  "speedup_trace_only": round(t_plain / t_keytrace, 3),
+                                  "speedup_with_sort": round(t_plain / (t_keysort + t_keytrace), 3),
+                                  "identical_hits": keysort_identical},
         "training": {"passes": passes, "adam_steps": info["steps"], "loss_first": round(losses[0], 4),
                      "loss_last": round(losses[-1], 4), "ms_per_pass": round(train_ms, 2),
                      "samples_per_pass": n // 20},
     }
+
+
+def ray_input_keys(torch, rays, box):
+    """The predictor's input key of each ray without the network: origin cell
+    on the 64^3 grid of the scene box (min xyz, max xyz; x-major) * 1024 +
+    octahedral direction bin on 32x32, as int64 (the quantisation the
+    network's embeddings use)."""
+    mn = torch.tensor(list(box[0:3]), dtype=torch.float32, device=rays.device)
+    mx = torch.tensor(list(box[3:6]), dtype=torch.float32, device=rays.device)
+    ext = torch.clamp(mx - mn, min=1e-20)
+    c = torch.clamp(((rays[:, 0:3] - mn) * (64.0 / ext)).floor().long(), 0, 63)
+    cell = (c[:, 0] * 64 + c[:, 1]) * 64 + c[:, 2]
+    d = rays[:, 4:7]
+    a = d.abs().sum(dim=1).clamp(min=1e-30)
+    px, py = d[:, 0] / a, d[:, 1] / a
+    neg = d[:, 2] < 0
+    qx = (1 - py.abs()) * torch.where(px >= 0, 1.0, -1.0)
+    qy = (1 - px.abs()) * torch.where(py >= 0, 1.0, -1.0)
+    px, py = torch.where(neg, qx, px), torch.where(neg, qy, py)
+    bu = torch.clamp(((px + 1) * 16).long(), 0, 31)
+    bv = torch.clamp(((py + 1) * 16).long(), 0, 31)
+    return cell * 1024 + bu * 32 + bv
 
 
 def cpu_baseline(tris, models, cam, sample_stride=8):

@@ -120,6 +120,7 @@ typedef struct crt_camera {
 #define CRT_TRACE_USE_PREDICTOR 0x4u /* seed t_max from the learned hit predictor */
 #define CRT_TRACE_STATS       0x8u  /* count visited nodes / tested triangles (slower) */
 #define CRT_TRACE_WIDE        0x10u /* walk the 4-wide nodes instead of the binary ones (same hits) */
+#define CRT_TRACE_PREDICTOR_ORDER 0x20u /* trace the rays grouped by their predicted treelet (same hits) */
 
 typedef struct crt_config {
     int device;                 /* CUDA device ordinal, default 0 */

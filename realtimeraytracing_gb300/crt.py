@@ -9,6 +9,7 @@ GPU the calls raise CrtError.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 import os
 
 import numpy as np
@@ -27,6 +28,7 @@ TRI_WATERTIGHT = 0x2
 TRACE_USE_PREDICTOR = 0x4
 TRACE_STATS = 0x8
 TRACE_WIDE = 0x10
+PREDICTOR_ORDER = 0x20  # CRT_TRACE_PREDICTOR_ORDER: trace rays grouped by predicted treelet
 USE_PREDICTOR = TRACE_USE_PREDICTOR
 MISS = 0xFFFFFFFF
 
@@ -187,22 +189,26 @@ class Predictor:
         _check(lib().crt_predictor_retarget(self.ctx.handle, self.handle))
 
     def train(self, rays, hits, offset: int = 0) -> float:
+        self.ctx._after_torch()
         loss = C.c_float()
         _check(lib().crt_predictor_train(self.ctx.handle, self.handle, _ptr(rays), _ptr(hits), _rows(rays), offset,
                                          C.byref(loss)))
         return loss.value
 
     def infer(self, rays, out=None):
+        self.ctx._after_torch()
         out = np.empty(_rows(rays), np.uint16) if out is None else out
         _check(lib().crt_predictor_infer(self.ctx.handle, self.handle, _ptr(rays), _rows(rays), _ptr(out)))
         return out
 
     def classes_of_hits(self, hits, out=None):
+        self.ctx._after_torch()
         out = np.empty(_rows(hits), np.uint16) if out is None else out
         _check(lib().crt_predictor_classes_of_hits(self.ctx.handle, self.handle, _ptr(hits), _rows(hits), _ptr(out)))
         return out
 
     def gradients(self, rays, targets):
+        self.ctx._after_torch()
         grad = np.empty(PREDICTOR_PARAMS, np.float32)
         loss = C.c_float()
         targets = np.ascontiguousarray(targets, np.uint16)
@@ -248,6 +254,7 @@ class Batch:
             self.set_models(models)
 
     def set_models(self, models):
+        self.ctx._after_torch()
         m = np.ascontiguousarray(models, np.float32)
         _check(lib().crt_batch_set_models(self.ctx.handle, self.handle, _ptr(m), m.shape[0]))
 
@@ -263,13 +270,16 @@ class Batch:
         _check(lib().crt_batch_set_config(self.handle, C.byref(c)))
 
     def build(self, tris):
+        self.ctx._after_torch()
         _check(lib().crt_batch_build(self.ctx.handle, self.handle, _ptr(tris)))
 
     def trace(self, rays, hits, flags: int = 0):
+        self.ctx._after_torch()
         _check(lib().crt_batch_trace(self.ctx.handle, self.handle, _ptr(rays), flags, _ptr(hits)))
         return hits
 
     def run(self, tris, rays, hits, flags: int = 0, graph: bool = True) -> bool:
+        self.ctx._after_torch()
         used = C.c_int()
         _check(lib().crt_batch_run(self.ctx.handle, self.handle, _ptr(tris), _ptr(rays), flags, _ptr(hits),
                                    1 if graph else 0, C.byref(used)))
@@ -287,6 +297,7 @@ class Batch:
         return {"tris": int(out[0]), "rays": int(out[1]), "iterations": int(out[2]), "tri_off": int(out[3])}
 
     def autotune(self, tris, rays, hits, flags: int = 0):
+        self.ctx._after_torch()
         c = Config()
         ms = C.c_float()
         _check(lib().crt_batch_autotune(self.ctx.handle, self.handle, _ptr(tris), _ptr(rays), flags, _ptr(hits),
@@ -337,6 +348,7 @@ class Bvh:
         return out
 
     def rebuild(self, tris, n_tris=None, models=None, n_buffer=None):
+        self.ctx._after_torch()
         models = _models(models)
         n_buffer = _rows(tris) if n_buffer is None else n_buffer
         n_tris = n_buffer if n_tris is None else n_tris
@@ -377,6 +389,24 @@ class Context:
         h = C.c_void_p()
         _check(lib().crt_create(C.byref(h), C.byref(cfg)))
         self.handle = h
+        self.device = device
+        self._ext = None
+
+    def _after_torch(self):
+        """Orders the library's stream after the work torch has queued on its
+        current stream, so device inputs torch produced are complete before
+        the library reads them (an event wait on the GPU, no host sync).  The
+        library's calls return with their outputs complete."""
+        t = sys.modules.get("torch")
+        if t is None or not t.cuda.is_available() or not t.cuda.is_initialized():
+            return
+        dev = t.device("cuda", self.device)
+        cur = t.cuda.current_stream(dev)
+        if cur.cuda_stream == self.stream:
+            return
+        if self._ext is None:
+            self._ext = t.cuda.ExternalStream(self.stream, device=dev)
+        self._ext.wait_stream(cur)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -398,6 +428,7 @@ class Context:
 
     def build(self, tris, n_tris=None, models=None, n_buffer=None) -> Bvh:
         """cr::BVH::BVH(nbTriangles, unsortedTriangles, meshesInTheScene)."""
+        self._after_torch()
         models = _models(models)
         n_buffer = _rows(tris) if n_buffer is None else n_buffer
         n_tris = n_buffer if n_tris is None else n_tris
@@ -412,12 +443,14 @@ class Context:
         return s.as_dict()
 
     def raygen(self, cam, width: int, height: int, out=None):
+        self._after_torch()
         cam = np.ascontiguousarray(cam, np.float32) if isinstance(cam, np.ndarray) else cam
         out = np.empty((width * height, 8), np.float32) if out is None else out
         _check(lib().crt_raygen_pinhole(self.handle, _ptr(cam), width, height, _ptr(out)))
         return out
 
     def shadow_rays(self, primary, hits, light, out=None):
+        self._after_torch()
         n = _rows(primary)
         out = np.empty((n, 8), np.float32) if out is None else out
         light = np.ascontiguousarray(light, np.float32)
@@ -425,12 +458,14 @@ class Context:
         return out
 
     def trace(self, bvh: Bvh, rays, flags: int = 0, out=None):
+        self._after_torch()
         n = _rows(rays)
         out = np.empty((n, 4), np.float32) if out is None else out
         _check(lib().crt_trace(self.handle, bvh.handle, _ptr(rays), n, flags, _ptr(out)))
         return out
 
     def bounce_rays(self, bvh: "Bvh", primary, hits, n_out: int, seed: int = 7, out=None):
+        self._after_torch()
         out = np.empty((n_out, 8), np.float32) if out is None else out
         _check(lib().crt_bounce_rays(self.handle, bvh.handle, _ptr(primary), _ptr(hits), _rows(primary), n_out, seed,
                                      _ptr(out)))
@@ -438,6 +473,7 @@ class Context:
 
     def trace_seeded(self, bvh: "Bvh", rays, classes, flags: int = 0, out=None):
         """Trace with the treelet of classes[i] searched first (device arrays)."""
+        self._after_torch()
         _check(lib().crt_trace_seeded(self.handle, bvh.handle, _ptr(rays), _rows(rays), flags, _ptr(classes),
                                       _ptr(out)))
         return out
@@ -452,6 +488,7 @@ class Context:
                     hits_primary=None, hits_shadow=None):
         """Application::drawOneFrame's compute pass: primary closest hits and,
         with a light, shadow any-hits.  Returns (hits_primary, hits_shadow)."""
+        self._after_torch()
         n = width * height
         cam = np.ascontiguousarray(cam, np.float32) if isinstance(cam, np.ndarray) else cam
         hp = np.empty((n, 4), np.float32) if hits_primary is None else hits_primary

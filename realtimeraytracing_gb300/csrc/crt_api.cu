@@ -106,6 +106,7 @@ struct crt_predictor {
     DevBuf tri_class;   // triangle -> class
     DevBuf treelets;    // Treelet[127] + count
     DevBuf classes;     // per-ray predicted classes (trace scratch)
+    DevBuf order, order_scratch;  // rays grouped by predicted class (CRT_TRACE_PREDICTOR_ORDER)
     DevBuf scratch;     // loss accumulator
     DevBuf rays_in, hits_in, targets_in;
     uint32_t step = 0;
@@ -499,9 +500,10 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
 }
 
 crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS | CRT_TRACE_WIDE))
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS | CRT_TRACE_WIDE |
+                  CRT_TRACE_PREDICTOR_ORDER))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
-    if ((flags & CRT_TRACE_USE_PREDICTOR) && !b->predictor)
+    if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && !b->predictor)
         return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor bound to this bvh (crt_predictor_create)");
     if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_trace: empty bvh");
     return CRT_OK;
@@ -544,14 +546,25 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
         p.pred_class = seed_classes;
         p.treelets = b->predictor->treelets.as<crt::Treelet>();
         p.n_treelets = reinterpret_cast<const uint32_t*>(b->predictor->treelets.as<crt::Treelet>() + 128);
-    } else if (flags & CRT_TRACE_USE_PREDICTOR) {
+    } else if (flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) {
         crt_predictor* pr = b->predictor;
         CRT_TRY(pr->classes.reserve(2ull * n_rays));
         CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, n_rays, pr->classes.as<uint16_t>(),
                                  pr->cfg.miss_threshold, x->err.as<uint32_t>(), x->stream));
-        p.pred_class = pr->classes.as<uint16_t>();
-        p.treelets = pr->treelets.as<crt::Treelet>();
-        p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
+        if (flags & CRT_TRACE_USE_PREDICTOR) {
+            p.pred_class = pr->classes.as<uint16_t>();
+            p.treelets = pr->treelets.as<crt::Treelet>();
+            p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
+        }
+        if (flags & CRT_TRACE_PREDICTOR_ORDER) {
+            CRT_TRY(pr->order.reserve(4ull * n_rays));
+            CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
+            crt::pred_order(b->nodes.as<crt_bvh_node>(), d_rays, pr->classes.as<uint16_t>(), n_rays,
+                            pr->order.as<uint32_t>(), pr->order_scratch.p, x->err.as<uint32_t>(), x->cfg.spin_limit,
+                            x->stream);
+            CRT_CUDA(cudaGetLastError());
+            p.order = pr->order.as<uint32_t>();
+        }
     }
     // binary walk: stack <= tree height <= PLOC iterations + 1; 4-wide walk: <= 3 per two levels
     const bool deep = (b->iterations + 2 > 64) || (3 * ((b->iterations + 2) / 2) + 3 > 96);
@@ -896,7 +909,7 @@ crt_status crt_predictor_destroy(crt_predictor* pr) {
     if (!pr) return CRT_OK;
     if (pr->bvh) pr->bvh->predictor = nullptr;
     DevBuf* bufs[] = {&pr->params, &pr->w16, &pr->tri_class, &pr->treelets, &pr->classes, &pr->scratch,
-                      &pr->rays_in, &pr->hits_in, &pr->targets_in};
+                      &pr->rays_in, &pr->hits_in, &pr->targets_in, &pr->order, &pr->order_scratch};
     for (DevBuf* d : bufs) d->release();
     delete pr;
     return CRT_OK;

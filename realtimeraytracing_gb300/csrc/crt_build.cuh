@@ -104,6 +104,9 @@ struct TraceParams {
     const uint16_t* pred_class = nullptr;
     const Treelet* treelets = nullptr;
     const uint32_t* n_treelets = nullptr;
+    // optional order of the rays (thread t traces ray order[t]), e.g. grouped
+    // by predicted treelet (CRT_TRACE_PREDICTOR_ORDER)
+    const uint32_t* order = nullptr;
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
 // Camera rays of image rows [y0, y0 + rows) traced to the closest hit into

@@ -16,6 +16,7 @@
 // weights and refreshes the fp16 copies (and the transposed copies the
 // backward GEMMs read).
 #include <cmath>
+#include <algorithm>
 #include <cstdint>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -701,9 +702,70 @@ __global__ void bounce_kernel(const crt_ray* prim, const crt_hit* hits, const ui
     o[1] = make_float4(dx * dl, dy * dl, dz * dl, __int_as_float(0x7F800000));
 }
 
+// Trace order of a ray: predicted class (7 bits) | Morton code of its origin
+// cell on a 32^3 grid of the scene box (15 bits) | direction bin (10 bits),
+// with the histograms of the four 8-bit digits.  Rays of one class go
+// together, and within a class nearby origins and similar directions.
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {
+    v &= 31u;
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6) | ((v & 16u) << 8);
+}
+
+__global__ void __launch_bounds__(256) order_keys_kernel(const crt_bvh_node* nodes, const crt_ray* __restrict__ rays,
+                                                         const uint16_t* __restrict__ classes, uint32_t n,
+                                                         uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[4 * 256];
+    for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x) h[k] = 0u;
+    __syncthreads();
+    const SceneFrame fr = scene_frame(nodes);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
+        const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+        uint32_t cell, bin;
+        ray_keys(r0, r1, fr, cell, bin);
+        const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
+        const uint32_t m = (spread5(cx >> 1) << 2) | (spread5(cy >> 1) << 1) | spread5(cz >> 1);
+        const uint32_t key = ((static_cast<uint32_t>(classes[i]) & 0x7Fu) << 25) | (m << 10) | (bin & 1023u);
+        keys[i] = key;
+#pragma unroll
+        for (int p = 0; p < 4; ++p) atomicAdd(&h[p * 256 + ((key >> (8 * p)) & 255u)], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 4 * 256; k += blockDim.x)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
 }  // namespace pred
 
 // ------------------------------------------------------------ launchers
+size_t pred_order_scratch_bytes(uint32_t n) {
+    const size_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
+    return 4 * (3 * static_cast<size_t>(n) + 4 * 256 + 4 * (tiles * 256 + 1) + 64);
+}
+
+void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes, uint32_t n, uint32_t* order,
+                void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+    if (n == 0) return;
+    uint32_t* ka = static_cast<uint32_t*>(scratch);
+    uint32_t* kb = ka + n;
+    uint32_t* vt = kb + n;
+    uint32_t* hist = vt + n;
+    uint32_t* lb = hist + 4 * 256;  // per pass: ticket, then the look-back words
+    const size_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
+    const size_t lb_words = tiles * 256 + 1;
+    cudaMemsetAsync(hist, 0, 4 * (4 * 256 + 4 * lb_words), s);
+    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, kNumSms * 8);
+    pred::order_keys_kernel<<<grid, 256, 0, s>>>(nodes, rays, classes, n, ka, hist);
+    // four stable 8-bit passes; pass 0 synthesises the ray indices
+    const uint32_t* kin[4] = {ka, kb, ka, kb};
+    uint32_t* kout[4] = {kb, ka, kb, ka};
+    const uint32_t* vin[4] = {nullptr, vt, order, vt};
+    uint32_t* vout[4] = {vt, order, vt, order};
+    for (int p = 0; p < 4; ++p) {
+        uint32_t* l = lb + p * lb_words;
+        launch_onesweep(kin[p], vin[p], kout[p], vout[p], n, 8 * p, 8, hist + 256 * p, l + 1, l, err, spin_limit, s);
+    }
+}
 void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s) {
     pred::init_kernel<<<kNumSms * 8, 256, 0, s>>>(P, seed);
     pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);

@@ -76,6 +76,13 @@ cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, co
                             uint32_t offset, float* loss_sum, uint32_t* err, cudaStream_t s);
 void pred_adam(const PredictorDev& P, float scale, float lr, uint32_t step, cudaStream_t s);
 void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s);
+// Trace order of rays: by predicted class, then the Morton code of the origin
+// cell (32^3 grid of the root box), then the direction bin (a stable radix
+// sort of 32-bit keys); order[k] = index of the k-th ray.  scratch holds
+// pred_order_scratch_bytes(n).
+size_t pred_order_scratch_bytes(uint32_t n);
+void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes, uint32_t n, uint32_t* order,
+                void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t* perm, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
 size_t bounce_scratch_bytes(uint32_t n_prim);

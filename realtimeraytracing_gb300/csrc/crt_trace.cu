@@ -402,7 +402,9 @@ template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) trace_kernel(TraceParams p) {
     const uint32_t t_id = blockIdx.x * BLOCK + threadIdx.x;
     if (t_id >= p.n_rays) return;
-    trace_ray<ANY, WT, STACK, SEED, WIDE>(p, ray_of_thread(t_id, p.tile_width));
+    const uint32_t i = p.order ? __ldg(p.order + t_id) : ray_of_thread(t_id, p.tile_width);
+    if (i >= p.n_rays) { raise_corrupt(p.err, 7, t_id, i); return; }
+    trace_ray<ANY, WT, STACK, SEED, WIDE>(p, i);
 }
 
 // Many scenes in one launch: ray i belongs to the scene whose ray range holds

@@ -140,3 +140,25 @@ def test_bounce_rays_deterministic_and_traced_like_the_oracle(ctx, scene):
     got = ctx.trace(bvh, sub, crt.TRI_WATERTIGHT)
     ref, _ = O.trace(bvh.nodes(), tris, S.identity_models(1), sub, crt.TRI_WATERTIGHT)
     np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("flags", [crt.TRI_WATERTIGHT, crt.TRI_REFERENCE, crt.TRI_WATERTIGHT | crt.TRACE_ANY])
+def test_predictor_ordered_traversal_is_exact(ctx, scene, flags):
+    """CRT_TRACE_PREDICTOR_ORDER traces the rays grouped by predicted treelet
+    (alone and with seeding): every ray gets the plain traversal's hit."""
+    bvh, bounce = scene
+    pred = crt.Predictor(ctx, bvh, seed=8)
+    n = bounce.shape[0]
+    plain = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    ctx.trace(bvh, bounce, flags, out=plain)
+    pred.train(bounce, plain)
+    got = torch.empty_like(plain)
+    ctx.trace(bvh, bounce, flags | crt.PREDICTOR_ORDER, out=got)
+    ok = torch.equal(_i32(got), _i32(plain)) if not flags & crt.TRACE_ANY else \
+        torch.equal(_i32(got)[:, 0] == -1, _i32(plain)[:, 0] == -1)
+    assert ok
+    ctx.trace(bvh, bounce, flags | crt.PREDICTOR_ORDER | crt.USE_PREDICTOR, out=got)
+    ok = torch.equal(_i32(got), _i32(plain)) if not flags & crt.TRACE_ANY else \
+        torch.equal(_i32(got)[:, 0] == -1, _i32(plain)[:, 0] == -1)
+    assert ok
+    pred.free()
