@@ -364,6 +364,11 @@ def run_batch_experiment(ctx, torch, crt, dev, args):
     t_nograph = timed(lambda: b.run(tris, rays, hits, flags, graph=False), reps)
     t_build = timed(lambda: b.build(tris), reps)
     ref_hits = hits.clone()
+    # the same pipeline with every scene's rays traced in coherence order
+    sorted_hits = torch.empty_like(hits)
+    b.run(tris, rays, sorted_hits, flags | crt.SORT_RAYS, graph=True)
+    t_sorted = timed(lambda: b.run(tris, rays, sorted_hits, flags | crt.SORT_RAYS, graph=True), reps)
+    sorted_identical = bool(torch.equal(sorted_hits.view(torch.int32), ref_hits.view(torch.int32)))
     # the same work scene by scene through the single-scene API
     c1 = crt.Context(device=dev.index or 0)
     tri_off = np.concatenate([[0], np.cumsum(tri_n)])
@@ -398,6 +403,9 @@ def run_batch_experiment(ctx, torch, crt, dev, args):
         "default_config": {k: default_cfg[k] for k in ("ploc_radius", "sort_digit_bits", "trace_block", "stack_depth")},
         "sequential_single_scene_ms": round(t_seq, 3), "speedup_vs_sequential": round(t_seq / t_graph, 3),
         "hits_identical_to_sequential": identical,
+        "sorted_rays": {"pipeline_ms": round(t_sorted, 3), "mrays_s": round(n_rays / t_sorted / 1e3, 1),
+                        "speedup": round(t_graph / t_sorted, 3), "hits_identical": sorted_identical,
+                        "note": "CRT_TRACE_SORT_RAYS: rays traced by (scene, origin-cell Morton code, direction bin)"},
     }
 
 
@@ -566,6 +574,8 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
         sh = torch.empty_like(plain)
     torch.cuda.synchronize()
     t_keytrace = timed(lambda: ctx.trace(bvh, srays, crt.TRI_WATERTIGHT, out=sh), reps)
+    t_native_sort = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.SORT_RAYS, out=seeded), reps)
+    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
     keysort_identical = bool(torch.equal(sh.view(torch.int32), plain.index_select(0, sorder).view(torch.int32)))
     info = pred.info()
     pred.free()
@@ -590,6 +600,9 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
                               "note": "CRT_TRACE_PREDICTOR_ORDER: inference + order by (predicted treelet, origin-cell Morton code, direction bin) + trace"},
         "predictor_ordered_seeded": {"mrays_s": round(n / t_ord_seed / 1e3, 1),
                                      "speedup": round(t_plain / t_ord_seed, 3)},
+        "sorted_rays_no_network": {"mrays_s": round(n / t_native_sort / 1e3, 1),
+                                   "speedup": round(t_plain / t_native_sort, 3),
+                                   "note": "CRT_TRACE_SORT_RAYS: order by (origin-cell Morton code, direction bin) + trace"},
         "key_sorted_no_network": {"sort_gather_ms": round(t_keysort, 3), "trace_ms": round(t_keytrace, 3),
                                   "speedup_trace_only": round(t_plain / t_keytrace, 3),
                                   "speedup_with_sort": round(t_plain / (t_keysort + t_keytrace), 3),

@@ -29,6 +29,7 @@ TRACE_USE_PREDICTOR = 0x4
 TRACE_STATS = 0x8
 TRACE_WIDE = 0x10
 PREDICTOR_ORDER = 0x20  # CRT_TRACE_PREDICTOR_ORDER: trace rays grouped by predicted treelet
+SORT_RAYS = 0x40  # CRT_TRACE_SORT_RAYS: trace rays ordered by origin cell and direction
 USE_PREDICTOR = TRACE_USE_PREDICTOR
 MISS = 0xFFFFFFFF
 

@@ -133,6 +133,7 @@ struct crt_ctx {
     DevBuf tris_in, models, scene_state, err, hist, sort_lb, codes_a, codes_b, vals_a, vals_b;
     DevBuf node_box, node_kids, pos, clus_a, clus_b, iters, ploc_lb;
     DevBuf cam, rays_in, hits_out, rays_out, trace_stats, frame_rays, frame_hits, frame_shadow, frame_shits;
+    DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -243,7 +244,8 @@ crt_status crt_destroy(crt_ctx* x) {
     DevBuf* bufs[] = {&x->tris_in, &x->models, &x->scene_state, &x->err, &x->hist, &x->sort_lb, &x->codes_a,
                       &x->codes_b, &x->vals_a, &x->vals_b, &x->node_box, &x->node_kids, &x->pos, &x->clus_a,
                       &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
-                      &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits};
+                      &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
+                      &x->ray_order, &x->ray_order_scratch};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -501,7 +503,7 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
 
 crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
     if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS | CRT_TRACE_WIDE |
-                  CRT_TRACE_PREDICTOR_ORDER))
+                  CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_SORT_RAYS))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
     if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && !b->predictor)
         return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor bound to this bvh (crt_predictor_create)");
@@ -556,7 +558,7 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
             p.treelets = pr->treelets.as<crt::Treelet>();
             p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
         }
-        if (flags & CRT_TRACE_PREDICTOR_ORDER) {
+        if (flags & CRT_TRACE_PREDICTOR_ORDER) {  // includes the coherence order of CRT_TRACE_SORT_RAYS
             CRT_TRY(pr->order.reserve(4ull * n_rays));
             CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
             crt::pred_order(b->nodes.as<crt_bvh_node>(), d_rays, pr->classes.as<uint16_t>(), n_rays,
@@ -565,6 +567,14 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
             CRT_CUDA(cudaGetLastError());
             p.order = pr->order.as<uint32_t>();
         }
+    }
+    if ((flags & CRT_TRACE_SORT_RAYS) && !p.order && n_rays > 1) {
+        CRT_TRY(x->ray_order.reserve(4ull * n_rays));
+        CRT_TRY(x->ray_order_scratch.reserve(crt::ray_order_scratch_bytes(n_rays)));
+        crt::launch_ray_order(d_rays, n_rays, b->nodes.as<crt_bvh_node>(), nullptr, 0, x->ray_order.as<uint32_t>(),
+                              x->ray_order_scratch.p, x->err.as<uint32_t>(), x->cfg.spin_limit, x->stream);
+        CRT_CUDA(cudaGetLastError());
+        p.order = x->ray_order.as<uint32_t>();
     }
     // binary walk: stack <= tree height <= PLOC iterations + 1; 4-wide walk: <= 3 per two levels
     const bool deep = (b->iterations + 2 > 64) || (3 * ((b->iterations + 2) / 2) + 3 > 96);
@@ -1082,6 +1092,7 @@ struct crt_batch {
     DevBuf codes_a, codes_b, vals_a, vals_b, codes, perm_global, perm_local;
     DevBuf node_box, node_kids, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
     DevBuf nodes, wide, wide_wt, depth_odd, xtri, inv_perm;
+    DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
     bool models_set = false;
     cudaGraphExec_t graph = nullptr;
     const void* g_tris = nullptr;
@@ -1172,11 +1183,25 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
         p.hits = hits;
         p.n_rays = bt->n_rays;
         p.err = err;
+        if ((flags & CRT_TRACE_SORT_RAYS) && bt->n_rays > 1) {
+            crt::launch_ray_order(rays, bt->n_rays, bt->nodes.as<crt_bvh_node>(), bt->scenes.as<crt::BatchScene>(),
+                                  bt->n_scenes, bt->ray_order.as<uint32_t>(), bt->ray_order_scratch.p, err,
+                                  x->cfg.spin_limit, s);
+            p.order = bt->ray_order.as<uint32_t>();
+        }
         crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
                                 flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block),
                                 bt->cfg.stack_depth > 64, s);
         CRT_CUDA(cudaGetLastError());
     }
+    return CRT_OK;
+}
+
+// Scratch of CRT_TRACE_SORT_RAYS for a batch, reserved outside graph capture.
+crt_status batch_order_buffers(crt_batch* bt, uint32_t flags) {
+    if (!(flags & CRT_TRACE_SORT_RAYS) || bt->n_rays <= 1) return CRT_OK;
+    CRT_TRY(bt->ray_order.reserve(4ull * bt->n_rays));
+    CRT_TRY(bt->ray_order_scratch.reserve(crt::ray_order_scratch_bytes(bt->n_rays)));
     return CRT_OK;
 }
 
@@ -1297,7 +1322,7 @@ crt_status crt_batch_free(crt_batch* bt) {
     DevBuf* bufs[] = {&bt->scenes, &bt->seg_off, &bt->seg_hist, &bt->chunks, &bt->states, &bt->models, &bt->err,
                       &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
                       &bt->perm_local, &bt->node_box, &bt->node_kids, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
-                      &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->wide_wt, &bt->depth_odd, &bt->xtri,
+                      &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->wide_wt, &bt->depth_odd, &bt->xtri, &bt->ray_order, &bt->ray_order_scratch,
                       &bt->inv_perm};
     for (DevBuf* b : bufs) b->release();
     delete bt;
@@ -1341,9 +1366,11 @@ crt_status crt_batch_build(crt_ctx* x, crt_batch* bt, const crt_triangle* tris) 
 
 crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint32_t flags, crt_hit* hits) {
     if (!x || !bt || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: null argument");
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: unsupported flags");
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS))
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: unsupported flags");
     if (!is_device_ptr(rays) || !is_device_ptr(hits)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: device memory only");
     CRT_CUDA(cudaSetDevice(x->device));
+    CRT_TRY(batch_order_buffers(bt, flags));
     CRT_CUDA(cudaMemsetAsync(bt->err.p, 0, 16, x->stream));
     crt::TraceParams p{};
     p.nodes = bt->nodes.as<crt_bvh_node>();
@@ -1354,8 +1381,15 @@ crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint3
     p.n_rays = bt->n_rays;
     p.err = bt->err.as<uint32_t>();
     const bool deep = bt->cfg.stack_depth > 64 || bt->max_iters + 2 > 64;
-    crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays, flags,
-                            static_cast<int>(bt->cfg.trace_block), deep, x->stream);
+    if ((flags & CRT_TRACE_SORT_RAYS) && bt->n_rays > 1) {
+        crt::launch_ray_order(rays, bt->n_rays, bt->nodes.as<crt_bvh_node>(), bt->scenes.as<crt::BatchScene>(),
+                              bt->n_scenes, bt->ray_order.as<uint32_t>(), bt->ray_order_scratch.p, p.err,
+                              x->cfg.spin_limit, x->stream);
+        p.order = bt->ray_order.as<uint32_t>();
+    }
+    crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
+                            flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block), deep,
+                            x->stream);
     CRT_CUDA(cudaGetLastError());
     return batch_check(x, bt);
 }
@@ -1363,8 +1397,10 @@ crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint3
 crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
                          crt_hit* hits, int use_graph, int* graph_used) {
     if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: null argument");
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: unsupported flags");
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS))
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: unsupported flags");
     CRT_CUDA(cudaSetDevice(x->device));
+    CRT_TRY(batch_order_buffers(bt, flags));  // before any graph capture: no allocation inside it
     if (graph_used) *graph_used = 0;
     if (bt->max_iters + 2 > 64) bt->cfg.stack_depth = 1024;
     if (use_graph) {
@@ -1417,6 +1453,7 @@ crt_status crt_batch_autotune(crt_ctx* x, crt_batch* bt, const crt_triangle* tri
                               crt_hit* hits, crt_config* best, float* best_ms) {
     if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_autotune: null argument");
     CRT_CUDA(cudaSetDevice(x->device));
+    CRT_TRY(batch_order_buffers(bt, flags));
     cudaEvent_t e0, e1, e2;
     CRT_CUDA(cudaEventCreate(&e0));
     CRT_CUDA(cudaEventCreate(&e1));

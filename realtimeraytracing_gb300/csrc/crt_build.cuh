@@ -134,6 +134,12 @@ struct BatchScene {
 static_assert(sizeof(BatchScene) == 48, "batch scene record");
 void launch_trace_batch(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t n_rays,
                         uint32_t flags, int block, bool deep, cudaStream_t s);
+// CRT_TRACE_SORT_RAYS: order[k] = k-th ray by coherence key (origin cell,
+// direction; with scenes, scene first).  scratch: ray_order_scratch_bytes(n).
+size_t ray_order_scratch_bytes(uint32_t n);
+void launch_ray_order(const crt_ray* rays, uint32_t n, const crt_bvh_node* nodes, const BatchScene* scenes,
+                      uint32_t n_scenes, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit,
+                      cudaStream_t s);
 // Batched build stages (crt_batch_kernels.cuh).
 size_t batch_box_state_bytes();
 size_t batch_chunk_bytes();

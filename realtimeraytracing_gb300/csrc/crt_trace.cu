@@ -416,8 +416,10 @@ __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, co
     for (uint32_t k = threadIdx.x; k <= n_scenes; k += BLOCK) s_ray_off[k] = scenes[k < n_scenes ? k : n_scenes - 1].ray_off +
                                                                             (k < n_scenes ? 0u : scenes[n_scenes - 1].n_rays);
     __syncthreads();
-    const uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
-    if (i >= n_rays_total) return;
+    const uint32_t t = blockIdx.x * BLOCK + threadIdx.x;
+    if (t >= n_rays_total) return;
+    const uint32_t i = base.order ? __ldg(base.order + t) : t;
+    if (i >= n_rays_total) { raise_corrupt(base.err, 7, t, i); return; }
     uint32_t lo = 0, hi = n_scenes - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
@@ -431,6 +433,80 @@ __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, co
     p.n_nodes = 2 * sc.n_tris - 1;
     p.abs_eps = sc.abs_eps;
     trace_ray<ANY, WT, STACK, false, false>(p, i);
+}
+
+// ------------------------------------------------------ ray ordering
+// CRT_TRACE_SORT_RAYS: rays are traced in the order of a 24-bit coherence
+// key — Morton code of the origin's cell on a 32^3 grid of the scene box
+// (15 bits), then an octahedral direction bin (32 x 16, 9 bits) — so warps
+// hold rays that start close together and point the same way.  In a batch
+// the scene index (8 bits) goes on top, which keeps every ray inside its
+// scene's range.  A stable LSD radix sort (the build's digit pass) makes the
+// order; every ray still gets its own hit.
+__device__ __forceinline__ uint32_t spread5_bits(uint32_t v) {
+    v &= 31u;
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6) | ((v & 16u) << 8);
+}
+
+__device__ __forceinline__ uint32_t coherence_key(float4 r0, float4 r1, float4 mn, float4 mx) {
+    const float sx = 32.f / fmaxf(mx.x - mn.x, 1e-20f), sy = 32.f / fmaxf(mx.y - mn.y, 1e-20f);
+    const float sz = 32.f / fmaxf(mx.z - mn.z, 1e-20f);
+    const int cx = min(max(static_cast<int>(floorf((r0.x - mn.x) * sx)), 0), 31);
+    const int cy = min(max(static_cast<int>(floorf((r0.y - mn.y) * sy)), 0), 31);
+    const int cz = min(max(static_cast<int>(floorf((r0.z - mn.z) * sz)), 0), 31);
+    const uint32_t m = (spread5_bits(cx) << 2) | (spread5_bits(cy) << 1) | spread5_bits(cz);
+    const float a = fabsf(r1.x) + fabsf(r1.y) + fabsf(r1.z);
+    float px = a > 0.f ? r1.x / a : 0.f, py = a > 0.f ? r1.y / a : 0.f;
+    if (r1.z < 0.f) {
+        const float qx = (1.f - fabsf(py)) * (px >= 0.f ? 1.f : -1.f);
+        const float qy = (1.f - fabsf(px)) * (py >= 0.f ? 1.f : -1.f);
+        px = qx;
+        py = qy;
+    }
+    const int bu = min(max(static_cast<int>((px + 1.f) * 16.f), 0), 31);
+    const int bv = min(max(static_cast<int>((py + 1.f) * 8.f), 0), 15);
+    return (m << 9) | (static_cast<uint32_t>(bu) << 4) | static_cast<uint32_t>(bv);
+}
+
+// Keys of all rays and the histograms of their PASSES 8-bit digits; with
+// scenes, ray i belongs to the scene whose ray range holds it and is keyed
+// on that scene's root box.
+template <int PASSES>
+__global__ void __launch_bounds__(256) ray_key_kernel(const crt_ray* __restrict__ rays, uint32_t n,
+                                                      const crt_bvh_node* __restrict__ nodes,
+                                                      const BatchScene* __restrict__ scenes, uint32_t n_scenes,
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[PASSES * 256];
+    __shared__ uint32_t s_ray_off[kMaxBatchScenes + 1];
+    for (int k = threadIdx.x; k < PASSES * 256; k += blockDim.x) h[k] = 0u;
+    if (scenes)
+        for (uint32_t k = threadIdx.x; k <= n_scenes; k += blockDim.x)
+            s_ray_off[k] = k < n_scenes ? scenes[k].ray_off : scenes[n_scenes - 1].ray_off + scenes[n_scenes - 1].n_rays;
+    __syncthreads();
+    float4 mn = __ldg(reinterpret_cast<const float4*>(nodes)), mx = __ldg(reinterpret_cast<const float4*>(nodes) + 1);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t top = 0;
+        if (scenes) {
+            uint32_t lo = 0, hi = n_scenes - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (s_ray_off[mid] <= i) lo = mid; else hi = mid - 1;
+            }
+            const float4* root = reinterpret_cast<const float4*>(nodes + scenes[lo].node_off);
+            mn = __ldg(root);
+            mx = __ldg(root + 1);
+            top = lo << 24;
+        }
+        const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
+        const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+        const uint32_t key = top | coherence_key(r0, r1, mn, mx);
+        keys[i] = key;
+#pragma unroll
+        for (int p = 0; p < PASSES; ++p) atomicAdd(&h[p * 256 + ((key >> (8 * p)) & 255u)], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < PASSES * 256; k += blockDim.x)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
 }
 
 // getRay (raytracer.glsl:92-100): pos = texel / size, direction =
@@ -604,6 +680,41 @@ void launch_frame(const TraceParams& p, const crt_camera* cam, uint32_t width, u
         if (block == 256) launch_frame_b<false, 256>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
         else if (block == 64) launch_frame_b<false, 64>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
         else launch_frame_b<false, 128>(p, cam, width, height, y0, rows, light, hits_shadow, deep, s);
+    }
+}
+
+size_t ray_order_scratch_bytes(uint32_t n) {
+    const size_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
+    return 4 * (3 * static_cast<size_t>(n) + 4 * 256 + 4 * (tiles * 256 + 1) + 64);
+}
+
+void launch_ray_order(const crt_ray* rays, uint32_t n, const crt_bvh_node* nodes, const BatchScene* scenes,
+                      uint32_t n_scenes, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit,
+                      cudaStream_t s) {
+    if (n == 0) return;
+    const int passes = scenes ? 4 : 3;
+    uint32_t* ka = static_cast<uint32_t*>(scratch);
+    uint32_t* kb = ka + n;
+    uint32_t* vt = kb + n;
+    uint32_t* hist = vt + n;
+    uint32_t* lb = hist + 4 * 256;  // per pass: ticket, then the look-back words
+    const size_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
+    const size_t lb_words = tiles * 256 + 1;
+    cudaMemsetAsync(hist, 0, 4 * (4 * 256 + 4 * lb_words), s);
+    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, kNumSms * 8);
+    if (scenes) ray_key_kernel<4><<<grid, 256, 0, s>>>(rays, n, nodes, scenes, n_scenes, ka, hist);
+    else ray_key_kernel<3><<<grid, 256, 0, s>>>(rays, n, nodes, nullptr, 0, ka, hist);
+    // stable 8-bit passes; the values alternate between order and vt so
+    // that the last pass writes order
+    const uint32_t* kin = ka;
+    const uint32_t* vin = nullptr;
+    for (int p = 0; p < passes; ++p) {
+        uint32_t* kout = (p & 1) ? ka : kb;
+        uint32_t* vout = ((passes - 1 - p) & 1) ? vt : order;
+        uint32_t* l = lb + p * lb_words;
+        launch_onesweep(kin, vin, kout, vout, n, 8 * p, 8, hist + 256 * p, l + 1, l, err, spin_limit, s);
+        kin = kout;
+        vin = vout;
     }
 }
 

@@ -79,3 +79,27 @@ def test_graph_replay_and_autotune(ctx, batch_data):
     b.run(tris, r, h2, crt.TRI_WATERTIGHT, graph=True)
     # watertight closest hits do not depend on the BVH (ties keep the lower triangle id)
     assert torch.equal(_i32(h0), _i32(h2))
+
+
+@pytest.mark.parametrize("flags", [crt.TRI_WATERTIGHT, crt.TRI_REFERENCE, crt.TRI_WATERTIGHT | crt.TRACE_ANY])
+def test_batch_sorted_rays_same_hits(ctx, batch_data, flags):
+    """CRT_TRACE_SORT_RAYS traces every scene's rays in coherence order
+    (scene, origin cell, direction); each ray keeps its own hit, through
+    crt_batch_trace and through the graph-replayed crt_batch_run."""
+    scenes, rays, tris, r, b = batch_data
+    b.build(tris)
+    h0 = torch.empty((r.shape[0], 4), dtype=torch.float32, device="cuda")
+    h1 = torch.empty_like(h0)
+    b.trace(r, h0, flags)
+    b.trace(r, h1, flags | crt.SORT_RAYS)
+    if flags & crt.TRACE_ANY:
+        assert torch.equal(_i32(h0)[:, 0] == -1, _i32(h1)[:, 0] == -1)
+    else:
+        assert torch.equal(_i32(h0), _i32(h1))
+    h2 = torch.empty_like(h0)
+    b.run(tris, r, h2, flags | crt.SORT_RAYS, graph=True)
+    b.run(tris, r, h2, flags | crt.SORT_RAYS, graph=True)
+    if flags & crt.TRACE_ANY:
+        assert torch.equal(_i32(h0)[:, 0] == -1, _i32(h2)[:, 0] == -1)
+    else:
+        assert torch.equal(_i32(h0), _i32(h2))

@@ -181,3 +181,18 @@ def test_trace_frame_tiles_bands_and_host_outputs(ctx):
     np.testing.assert_array_equal(ds.cpu().numpy().view(np.uint32), hs.view(np.uint32))
     hr, _ = ctx.trace_frame(bvh, cam, w, h, None, crt.TRI_REFERENCE)
     _cmp_hits(hr, O.trace(bvh.nodes(), tris, models, rays, crt.TRI_REFERENCE)[0])
+
+
+@pytest.mark.parametrize("flags", [crt.TRI_REFERENCE, crt.TRI_WATERTIGHT, crt.TRI_WATERTIGHT | crt.TRACE_ANY])
+def test_sorted_rays_same_hits(ctx, flags):
+    """CRT_TRACE_SORT_RAYS: incoherent rays traced in coherence order (origin
+    cell, direction bin) get the oracle's hits, for any ray count."""
+    v, f = S.displaced_icosphere(level=5, seed=31)
+    tris = S.indexed_to_triangles(v, f)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    rays = S.sphere_rays(12345, seed=3, radius=1.5, center=(0.0, 0.0, 0.0))
+    ref, _ = O.trace(bvh.nodes(), tris, models, rays, flags)
+    any_hit = bool(flags & crt.TRACE_ANY)
+    _cmp_hits(ctx.trace(bvh, rays, flags | crt.SORT_RAYS), ref, any_hit)
+    _cmp_hits(ctx.trace(bvh, rays[:1], flags | crt.SORT_RAYS), ref[:1], any_hit)
