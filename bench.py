@@ -415,8 +415,11 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
     vertex moves by 0.01 sin(2 pi f / 60 + 7 x) along y and the whole PLOC BVH
     is rebuilt each frame; per frame 1920x1080 primary rays and 2 cosine
     bounce rays per hit are traced, and the hit predictor is retrained on the
-    frame's exact hits (5%) and used for the bounce rays.  Frame = rebuild +
-    primary + bounce generation + training + seeded bounce trace."""
+    frame's exact hits (5%) and used for the bounce rays, which are traced in
+    the order of their predicted treelets (CRT_TRACE_PREDICTOR_ORDER).  Frame =
+    rebuild + primary + bounce generation + ordered bounce trace + training.
+    Every 15 frames the same bounce rays are also traced plain, seeded and
+    sorted without the network, off the frame clock."""
     from realtimeraytracing_gb300 import scenes as S
     n = 16 * 1024 * 1024
     gen = torch.Generator(device=dev)
@@ -432,7 +435,7 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
     prim = torch.empty((W * H, 8), dtype=torch.float32, device=dev)
     bvh = ctx.build(tris, models=models)
     pred = crt.Predictor(ctx, bvh, seed=3)
-    frame_ms, build_ms, sort_ms, plain_ms, seeded_ms, rays_traced = [], [], [], [], [], []
+    frame_ms, build_ms, sort_ms, compare, ordered_ms, rays_traced = [], [], [], [], [], []
     identical = True
     bounce = hb_plain = hb_seed = None
     for f in range(frames):
@@ -453,9 +456,9 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
         br, hs = bounce[:nb], hb_seed[:nb]
         ctx.bounce_rays(bvh, prim, hp, nb, seed=100 + f, out=br)
         ts = time.perf_counter()
-        ctx.trace(bvh, br, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR, out=hs)
+        ctx.trace(bvh, br, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER, out=hs)
         torch.cuda.synchronize()
-        seeded_ms.append((time.perf_counter() - ts) * 1e3)
+        ordered_ms.append((time.perf_counter() - ts) * 1e3)
         pred.train(br, hs, offset=f % 20)   # retrain on this frame's exact hits
         torch.cuda.synchronize()
         frame_ms.append((time.perf_counter() - t0) * 1e3)
@@ -463,26 +466,30 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
         sort_ms.append(st["ms_sort"])
         rays_traced.append(W * H + nb)
         if f % 15 == 0 or f == frames - 1:
-            # plain traversal of the same bounce rays, off the frame clock, for the comparison
-            tp = time.perf_counter()
-            ctx.trace(bvh, br, crt.TRI_WATERTIGHT, out=hb_plain[:nb])
-            torch.cuda.synchronize()
-            plain_ms.append(((time.perf_counter() - tp) * 1e3, seeded_ms[-1], nb))
-            identical = identical and bool(torch.equal(hb_plain[:nb].view(torch.int32), hs.view(torch.int32)))
+            # the same bounce rays plain, seeded and sorted without the network, off the frame clock
+            row = {"rays": int(nb), "predictor_ordered_ms": round(ordered_ms[-1], 3)}
+            for name, fl in (("plain_ms", 0), ("seeded_ms", crt.USE_PREDICTOR), ("sorted_no_network_ms", crt.SORT_RAYS)):
+                tp = time.perf_counter()
+                ctx.trace(bvh, br, crt.TRI_WATERTIGHT | fl, out=hb_plain[:nb])
+                torch.cuda.synchronize()
+                row[name] = round((time.perf_counter() - tp) * 1e3, 3)
+                identical = identical and bool(torch.equal(hb_plain[:nb].view(torch.int32), hs.view(torch.int32)))
+            compare.append(row)
     pred.free()
     bvh.free()
     fm = np.array(frame_ms[1:])
     sort_bytes = 16.0 * n * 4 - 4.0 * n  # 4 passes x (8 B in + 8 B out); pass 0 synthesises values
     return {
         "workload": "16,777,216-tri clustered soup (1024 clusters), 60 animated frames, full rebuild per frame, "
-                    "1920x1080 primary + 2 bounce rays per hit, predictor retrained per frame",
+                    "1920x1080 primary + 2 bounce rays per hit traced in predicted-treelet order, predictor retrained "
+                    "per frame",
         "frames": frames,
         "frame_ms_p50": round(float(np.percentile(fm, 50)), 3), "frame_ms_p99": round(float(np.percentile(fm, 99)), 3),
         "build_ms_p50": round(float(np.median(build_ms[1:])), 3),
         "mrays_s": round(float(sum(rays_traced[1:]) / fm.sum() / 1e3), 1),
         "sort_ms_p50": round(float(np.median(sort_ms[1:])), 4),
         "sort_gbs": round(sort_bytes / (float(np.median(sort_ms[1:])) * 1e-3) / 1e9, 1),
-        "bounce_seeded_vs_plain": [{"plain_ms": round(a, 3), "seeded_ms": round(b, 3), "rays": int(c)} for a, b, c in plain_ms],
+        "bounce_trace_ms": compare,
         "identical_hits": identical,
     }
 
