@@ -405,7 +405,7 @@ def run_batch_experiment(ctx, torch, crt, dev, args):
         "hits_identical_to_sequential": identical,
         "sorted_rays": {"pipeline_ms": round(t_sorted, 3), "mrays_s": round(n_rays / t_sorted / 1e3, 1),
                         "speedup": round(t_graph / t_sorted, 3), "hits_identical": sorted_identical,
-                        "note": "CRT_TRACE_SORT_RAYS: rays traced by (scene, origin-cell Morton code, direction bin)"},
+                        "note": "CRT_TRACE_SORT_RAYS: rays traced by (scene, Morton code of the cell where the ray enters the scene box, direction bin)"},
     }
 
 

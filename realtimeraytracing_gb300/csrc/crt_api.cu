@@ -461,7 +461,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     } else if (!laid_out) {
         uint32_t* dfs = x->clus_a.as<uint32_t>();  // the cluster buffers are free after PLOC
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
-            crt::launch_layout_level(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(),
+            crt::launch_layout_level(x->node_kids.as<uint4>(), x->pos.as<uint2>(),
                                      x->it_host[k].y, x->it_host[k + 1].y, N, dfs, err, s);
         crt::launch_layout_emit(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(), N, dfs,
                                 b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->wide_wt.as<float4>(),

@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
             const BatchScene B = scenes[lo];
             const uint32_t lv = B.iters - 1 - r;
             const uint32_t X = __ldcg(it + B.it_off + lv).y + (q - s_tile_pre[lo]);
-            layout_down(X, node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off, pf + B.tri_off, B.n_tris,
+            layout_down(X, node_kids + B.tri_off, pf + B.tri_off, B.n_tris,
                         dfs + B.node_off, err);
         }
         if (!grid_barrier(bar, err, spin_limit)) return;

@@ -710,8 +710,7 @@ __device__ __forceinline__ uint2 layout_place(uint32_t X, const uint2* __restric
     return (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
 }
 
-__device__ __forceinline__ void layout_down(uint32_t X, const float4* __restrict__ node_box,
-                                            const uint4* __restrict__ node_kids, uint2* __restrict__ pf, uint32_t N,
+__device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict__ node_kids, uint2* __restrict__ pf, uint32_t N,
                                             uint32_t* __restrict__ dfs, uint32_t* err) {
     const uint2 me = layout_place(X, pf, N);
     const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
@@ -776,13 +775,12 @@ __device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict
     g[3] = make_float4(cmx[1].x + grow, cmx[1].y + grow, cmx[1].z + grow, __uint_as_float(lcb));
 }
 
-__global__ void __launch_bounds__(256) layout_level_kernel(const float4* __restrict__ node_box,
-                                                           const uint4* __restrict__ node_kids,
+__global__ void __launch_bounds__(256) layout_level_kernel(const uint4* __restrict__ node_kids,
                                                            uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
                                                            uint32_t N, uint32_t* __restrict__ dfs, uint32_t* err) {
     const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (X >= id_end) return;
-    layout_down(X, node_box, node_kids, pf, N, dfs, err);
+    layout_down(X, node_kids, pf, N, dfs, err);
 }
 
 __global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restrict__ node_box,
@@ -867,7 +865,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     for (int k = iter - 1; k >= 0; --k) {
         const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
         for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
-            layout_down(X, node_box, node_kids, pf, N, dfs, err);
+            layout_down(X, node_kids, pf, N, dfs, err);
         if (!grid_barrier(bar, err, spin_limit)) return;
     }
     const float grow = st->abs_eps;
@@ -992,11 +990,11 @@ void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, ui
         cin, cout, node_box, node_kids, it, iter, N, radius, lookback, tickets, n_tiles_cap, err, spin_limit);
 }
 
-void launch_layout_level(const float4* node_box, const uint4* node_kids, uint2* pf, uint32_t id_begin,
+void launch_layout_level(const uint4* node_kids, uint2* pf, uint32_t id_begin,
                          uint32_t id_end, uint32_t N, uint32_t* dfs, uint32_t* err, cudaStream_t s) {
     if (id_end <= id_begin || id_end > 2 * N - 1) return;
     const uint32_t cnt = id_end - id_begin;
-    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, id_begin, id_end, N, dfs, err);
+    layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_kids, pf, id_begin, id_end, N, dfs, err);
 }
 
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,

@@ -437,9 +437,10 @@ __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, co
 
 // ------------------------------------------------------ ray ordering
 // CRT_TRACE_SORT_RAYS: rays are traced in the order of a 24-bit coherence
-// key — Morton code of the origin's cell on a 32^3 grid of the scene box
-// (15 bits), then an octahedral direction bin (32 x 16, 9 bits) — so warps
-// hold rays that start close together and point the same way.  In a batch
+// key — Morton code of the cell, on a 32^3 grid of the scene box, where the
+// ray enters the box (its origin if it starts inside; 15 bits), then an
+// octahedral direction bin (32 x 16, 9 bits) — so warps hold rays that
+// reach the scene close together and point the same way.  In a batch
 // the scene index (8 bits) goes on top, which keeps every ray inside its
 // scene's range.  A stable LSD radix sort (the build's digit pass) makes the
 // order; every ray still gets its own hit.
@@ -449,11 +450,19 @@ __device__ __forceinline__ uint32_t spread5_bits(uint32_t v) {
 }
 
 __device__ __forceinline__ uint32_t coherence_key(float4 r0, float4 r1, float4 mn, float4 mx) {
+    // entry distance into the box (a key only: any rounding is harmless)
+    const float ix = 1.f / r1.x, iy = 1.f / r1.y, iz = 1.f / r1.z;
+    const float tx1 = (mn.x - r0.x) * ix, tx2 = (mx.x - r0.x) * ix;
+    const float ty1 = (mn.y - r0.y) * iy, ty2 = (mx.y - r0.y) * iy;
+    const float tz1 = (mn.z - r0.z) * iz, tz2 = (mx.z - r0.z) * iz;
+    float te = fmaxf(fmaxf(fminf(tx1, tx2), fminf(ty1, ty2)), fminf(tz1, tz2));
+    if (!(te > 0.f) || !isfinite(te)) te = 0.f;
+    const float ex = r0.x + te * r1.x, ey = r0.y + te * r1.y, ez = r0.z + te * r1.z;
     const float sx = 32.f / fmaxf(mx.x - mn.x, 1e-20f), sy = 32.f / fmaxf(mx.y - mn.y, 1e-20f);
     const float sz = 32.f / fmaxf(mx.z - mn.z, 1e-20f);
-    const int cx = min(max(static_cast<int>(floorf((r0.x - mn.x) * sx)), 0), 31);
-    const int cy = min(max(static_cast<int>(floorf((r0.y - mn.y) * sy)), 0), 31);
-    const int cz = min(max(static_cast<int>(floorf((r0.z - mn.z) * sz)), 0), 31);
+    const int cx = min(max(static_cast<int>(floorf((ex - mn.x) * sx)), 0), 31);
+    const int cy = min(max(static_cast<int>(floorf((ey - mn.y) * sy)), 0), 31);
+    const int cz = min(max(static_cast<int>(floorf((ez - mn.z) * sz)), 0), 31);
     const uint32_t m = (spread5_bits(cx) << 2) | (spread5_bits(cy) << 1) | spread5_bits(cz);
     const float a = fabsf(r1.x) + fabsf(r1.y) + fabsf(r1.z);
     float px = a > 0.f ? r1.x / a : 0.f, py = a > 0.f ? r1.y / a : 0.f;
