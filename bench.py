@@ -14,7 +14,8 @@ Application::drawOneFrame in srcOpenGL/application.cpp:220-262, minus shading):
           inputs resident in HBM, CUDA events on the library's stream
   e2e     the same frame through the public C ABI call crt_trace_frame with
           the camera in from pinned host memory and both hit buffers out to
-          pinned host memory, timed on the host clock around the call
+          pinned host memory (the frame kernel writes them there directly),
+          timed on the host clock around the call
 
 --impl reference times the reference's CPU path on the host cores instead:
 its PLOC build (bvh.cpp restated for N > 65,536, the reference's own cap)
@@ -304,7 +305,9 @@ def run_ours(args):
             "build_stages_ms": stages,
             "ploc_iterations": iters,
             "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(cam.nbytes),
-                    "d2h_bytes_per_step": int(2 * n_rays * 16), "ms_per_step": round(e2e_t, 4)},
+                    "d2h_bytes_per_step": int(2 * n_rays * 16), "ms_per_step": round(e2e_t, 4),
+                    "transfer": "camera in by cudaMemcpyAsync; both hit buffers (page-locked host memory) written by "
+                                "the frame kernel over the CPU-GPU link, host-timed around crt_trace_frame"},
             "gpu_launches": args.steps,
             "roofline": {"kernel": "frame_kernel (camera ray, closest hit, shadow ray, any hit)", "bound": "hbm",
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

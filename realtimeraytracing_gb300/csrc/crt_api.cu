@@ -76,6 +76,19 @@ bool is_device_ptr(const void* ptr) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The device address of page-locked host memory the GPU can write directly
+// (cudaMallocHost / cudaHostRegister, mapped under unified addressing), or
+// null for device, pageable or unknown memory.
+void* mapped_host_ptr(void* ptr) {
+    if (!ptr) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 constexpr uint32_t kDefaultSpin = 1u << 22;   // ~0.3 s with back-off; far above any normal wait
 
 }  // namespace
@@ -759,8 +772,15 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     if (flags & CRT_TRACE_ANY) return fail(CRT_ERR_INVALID_ARG, "crt_trace_frame: primary rays are closest-hit");
     CRT_CUDA(cudaSetDevice(x->device));
     const uint32_t n = width * height;
-    const bool dev_p = is_device_ptr(hits_primary);
+    const bool fused = !(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE));
+    bool dev_p = is_device_ptr(hits_primary);
     crt_hit* d_hp = hits_primary;
+    if (!dev_p && fused) {  // page-locked host output: the frame kernel writes it over the CPU-GPU link
+        if (void* m = mapped_host_ptr(hits_primary)) {
+            d_hp = static_cast<crt_hit*>(m);
+            dev_p = true;
+        }
+    }
     if (!dev_p) {
         CRT_TRY(x->frame_hits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
         d_hp = x->frame_hits.as<crt_hit>();
@@ -772,16 +792,23 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
-    if (!(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE))) {
-        // one launch: camera ray, closest hit, shadow ray, any hit per pixel
+    if (fused) {
+        // one launch: camera ray, closest hit, shadow ray, any hit per pixel.
+        // Page-locked host outputs are written by the kernel itself over the
+        // CPU-GPU link while it runs; only pageable ones go through a copy.
         crt_hit* d_hs = nullptr;
         bool dev_s = true;
         if (light) {
             dev_s = is_device_ptr(hits_shadow);
             d_hs = hits_shadow;
             if (!dev_s) {
-                CRT_TRY(x->frame_shits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
-                d_hs = x->frame_shits.as<crt_hit>();
+                if (void* m = mapped_host_ptr(hits_shadow)) {
+                    d_hs = static_cast<crt_hit*>(m);
+                    dev_s = true;
+                } else {
+                    CRT_TRY(x->frame_shits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
+                    d_hs = x->frame_shits.as<crt_hit>();
+                }
             }
         }
         crt::TraceParams p{};

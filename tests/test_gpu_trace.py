@@ -179,6 +179,12 @@ def test_trace_frame_tiles_bands_and_host_outputs(ctx):
     ctx.trace_frame(bvh, cam, w, h, light, crt.TRI_WATERTIGHT, hits_primary=dp, hits_shadow=ds)
     np.testing.assert_array_equal(dp.cpu().numpy().view(np.uint32), hp.view(np.uint32))
     np.testing.assert_array_equal(ds.cpu().numpy().view(np.uint32), hs.view(np.uint32))
+    # page-locked host outputs: written by the frame kernel itself
+    pp = torch.empty((w * h, 4), dtype=torch.float32, pin_memory=True)
+    ps = torch.empty((w * h, 4), dtype=torch.float32, pin_memory=True)
+    ctx.trace_frame(bvh, cam, w, h, light, crt.TRI_WATERTIGHT, hits_primary=pp, hits_shadow=ps)
+    np.testing.assert_array_equal(pp.numpy().view(np.uint32), hp.view(np.uint32))
+    np.testing.assert_array_equal(ps.numpy().view(np.uint32), hs.view(np.uint32))
     hr, _ = ctx.trace_frame(bvh, cam, w, h, None, crt.TRI_REFERENCE)
     _cmp_hits(hr, O.trace(bvh.nodes(), tris, models, rays, crt.TRI_REFERENCE)[0])
 
