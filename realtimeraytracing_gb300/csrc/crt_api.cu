@@ -724,8 +724,14 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
         CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, rays, sizeof(crt_ray) * n_rays, cudaMemcpyHostToDevice, x->stream));
         d_rays = x->rays_in.as<crt_ray>();
     }
-    const bool dev_out = is_device_ptr(hits);
+    bool dev_out = is_device_ptr(hits);
     crt_hit* d_hits = hits;
+    if (!dev_out) {  // page-locked host hits: written by the trace kernel itself
+        if (void* m = mapped_host_ptr(hits)) {
+            d_hits = static_cast<crt_hit*>(m);
+            dev_out = true;
+        }
+    }
     if (!dev_out) {
         CRT_TRY(x->hits_out.reserve(sizeof(crt_hit) * n_rays));
         d_hits = x->hits_out.as<crt_hit>();

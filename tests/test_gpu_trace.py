@@ -202,3 +202,16 @@ def test_sorted_rays_same_hits(ctx, flags):
     any_hit = bool(flags & crt.TRACE_ANY)
     _cmp_hits(ctx.trace(bvh, rays, flags | crt.SORT_RAYS), ref, any_hit)
     _cmp_hits(ctx.trace(bvh, rays[:1], flags | crt.SORT_RAYS), ref[:1], any_hit)
+
+
+def test_trace_into_page_locked_host_memory(ctx, config0):
+    """crt_trace with page-locked host hits (written by the kernel directly)
+    and pageable host hits give the oracle's hits."""
+    torch = pytest.importorskip("torch")
+    tris, models, cam, w, h, bvh = config0
+    rays = O.raygen(cam, w, h)
+    ref, _ = O.trace(bvh.nodes(), tris, models, rays, crt.TRI_WATERTIGHT)
+    pinned = torch.empty((rays.shape[0], 4), dtype=torch.float32, pin_memory=True)
+    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=pinned)
+    _cmp_hits(pinned.numpy(), ref)
+    _cmp_hits(ctx.trace(bvh, rays, crt.TRI_WATERTIGHT), ref)
