@@ -250,6 +250,28 @@ def run_ours(args):
     torch.cuda.synchronize()
     p_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
 
+    # ---- the reference's whole compute pass (getRay, closest hit, getColor,
+    # imageStore) into a device RGBA32F image: crt_render_frame, one launch
+    img = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+    d_mats = torch.tensor([[0.8, 0.7, 0.6, 1.0]], dtype=torch.float32, device=dev)
+    shaded = {}
+    for name, sflags, depth in (("plain", 0, 0), ("wireframe_bvh_depth3", crt.SHADE_WIREFRAME | crt.SHADE_BVH, 3)):
+        def render():
+            ctx.render_frame(bvh, d_cam, W, H, models=d_models, materials=d_mats, shade_flags=sflags,
+                             bvh_depth=depth, flags=flags, out=img)
+        for _ in range(2):
+            render()
+        sev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                l2_flush.zero_()
+                sev[k][0].record(stream)
+                render()
+                sev[k][1].record(stream)
+        torch.cuda.synchronize()
+        s_ms = statistics.mean(a.elapsed_time(b) for a, b in sev)
+        shaded[name] = {"ms": round(s_ms, 4), "mrays_s": round(n_rays / (s_ms * 1e-3) / 1e6, 1)}
+
     # ---- end to end through the public API: camera in, hits out (pinned host)
     hp_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
     hs_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
@@ -319,6 +341,8 @@ def run_ours(args):
             "primary_trace_kernel": {"ms": round(p_ms, 4), "mrays_s": round(n_rays / (p_ms * 1e-3) / 1e6, 1),
                                      "node_fetches_per_ray": round(p_visited / n_rays, 2),
                                      "tris_per_ray": round(p_tested / n_rays, 2)},
+            "shaded_frame": dict(shaded, note="crt_render_frame: camera ray, closest hit, getColor and "
+                                              "imageStore per texel into a device RGBA32F image, no shadow rays"),
             "cpu_baseline": cpu,
             "clocks": clk,
             "batch": batch,

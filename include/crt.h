@@ -216,6 +216,57 @@ crt_status crt_trace_frame(crt_ctx* ctx, const crt_bvh* bvh, const crt_camera* c
                            uint32_t height, const float* light, uint32_t flags, crt_hit* hits_primary,
                            crt_hit* hits_shadow);
 
+/* ---- shading: replaces getColor + imageStore (raytracer.glsl:159-179, 319-330) ----
+ * cr::MaterialGPU (srcCommon/scene/pbr/material.hpp:9-11): an RGBA colour, 16 bytes. */
+typedef struct crt_material {
+    float color[4];
+} crt_material;
+
+#define CRT_SHADE_WIREFRAME 0x1u  /* uIsWireframeModeOn: hits with a barycentric coordinate < 0.02 are black */
+#define CRT_SHADE_BVH       0x2u  /* uIsBVHDisplayed: texels start from the colour of the BVH boxes at bvh_depth */
+#define CRT_SHADE_MAX_BVH_DEPTH 63u
+
+/* What getColor reads besides the hit: the shader's uniforms
+ * (srcOpenGL/application.cpp:229-232) and its model and material buffers
+ * (srcOpenGL/scene/scene.cpp:17-23, 42-48, 110-121).  Only material_id of a
+ * model is read; model ids >= n_models use material 0 (the default records of
+ * the shader's 64-entry model buffer), and material ids >= n_materials read
+ * (0, 0, 0, 0) (the never-uploaded part of its material buffer). */
+typedef struct crt_shading {
+    const crt_mesh_model* models;    /* uModels; may be NULL when n_models == 0 */
+    uint32_t n_models;               /* <= 64 */
+    const crt_material* materials;   /* uMaterials; may be NULL when n_materials == 0 */
+    uint32_t n_materials;
+    uint32_t flags;                  /* CRT_SHADE_* */
+    uint32_t bvh_depth;              /* uDepthDisplayBVH, <= CRT_SHADE_MAX_BVH_DEPTH */
+} crt_shading;
+
+/* Texel i of n (rgba[4i .. 4i+3], RGBA32F) for hit i of ray i, as main and
+ * getColor compute it:
+ *   value = (0, 0, 0, 1);
+ *   with CRT_SHADE_BVH, value = bvhColor: (0.5, 0, 0.5, 0.1) for the box at
+ *     depth bvh_depth that the shader's walk (getClosestHitBVH, right child
+ *     popped first, every intersected box entered) meets last, (0.7, 0, 0.7,
+ *     0.1) if the ray enters that box within 0.05 / (bvh_depth + 1) of its
+ *     faces on two axes (intersectBVH returns 2), (0, 0, 0, 0) if no box at
+ *     that depth is met;
+ *   on a hit, value += the colour of the hit triangle's model's material, then
+ *     with CRT_SHADE_WIREFRAME value = (0, 0, 0, 1) where u, v or 1 - u - v
+ *     is below 0.02.
+ * rays are read only with CRT_SHADE_BVH (else they may be NULL); hits come
+ * from a trace of those rays on bvh.  Every pointer may be host or device
+ * memory; device rgba must be 16-byte aligned. */
+crt_status crt_shade(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, const crt_hit* hits, uint32_t n,
+                     const crt_shading* shading, float* rgba);
+/* The reference's whole compute pass for one frame (raytracer.glsl main,
+ * dispatched at srcOpenGL/application.cpp:245): getRay for every texel,
+ * closest hit with `flags` (as crt_trace_frame), getColor and imageStore into
+ * rgba[4 * (y * width + x)] (row y = 0 is the texture's first row, the bottom
+ * of the displayed image).  Plain frames (no CRT_TRACE_USE_PREDICTOR /
+ * CRT_TRACE_WIDE) run in one launch. */
+crt_status crt_render_frame(crt_ctx* ctx, const crt_bvh* bvh, const crt_camera* cam, uint32_t width, uint32_t height,
+                            uint32_t flags, const crt_shading* shading, float* rgba);
+
 /* ---- learned hit predictor (no counterpart in the reference) --------------
  * An FP16 MLP on tcgen05 tensor cores maps a ray (origin cell on a 64^3 grid,
  * direction in 32x32 octahedral bins, each through a learned 16-wide

@@ -629,3 +629,93 @@ void oracle_trace_brute(const crt_triangle* tris, uint32_t n_tris, const crt_mes
 }
 
 }  // extern "C"
+
+// ===================================================================== shade
+namespace {
+
+// intersectBVH (raytracer.glsl:182-236) with its border test: 0 = miss,
+// 1 = hit, 2 = hit whose entry point o + d * tMin lies within `line` of a
+// face of the box on at least two axes.
+inline int slab_display(const crt_ray& r, const crt_bvh_node& n, float line) {
+    const float ix = 1.0f / r.d[0];
+    const float tx1 = (n.mn[0] - r.o[0]) * ix, tx2 = (n.mx[0] - r.o[0]) * ix;
+    float tMin = fmin_std(tx1, tx2), tMax = fmax_std(tx1, tx2);
+    if (tMax < 0.f || tMin > tMax) return 0;
+    const float iy = 1.0f / r.d[1];
+    const float ty1 = (n.mn[1] - r.o[1]) * iy, ty2 = (n.mx[1] - r.o[1]) * iy;
+    tMin = fmax_std(tMin, fmin_std(ty1, ty2));
+    tMax = fmin_std(tMax, fmax_std(ty1, ty2));
+    if (tMax < 0.f || tMin > tMax) return 0;
+    const float iz = 1.0f / r.d[2];
+    const float tz1 = (n.mn[2] - r.o[2]) * iz, tz2 = (n.mx[2] - r.o[2]) * iz;
+    tMin = fmax_std(tMin, fmin_std(tz1, tz2));
+    tMax = fmin_std(tMax, fmax_std(tz1, tz2));
+    if (!(tMax >= 0.f && tMin <= tMax)) return 0;
+    bool close[3];
+    for (int k = 0; k < 3; ++k) {
+        const float e = r.o[k] + r.d[k] * tMin;
+        close[k] = std::fabs(e - n.mn[k]) < line || std::fabs(e - n.mx[k]) < line;
+    }
+    return ((close[0] && close[1]) || (close[0] && close[2]) || (close[1] && close[2])) ? 2 : 1;
+}
+
+// bvhColor as getClosestHitBVH leaves it (raytracer.glsl:246-277): the
+// shader's own walk — pop a node, test its box, on a hit assign bvhColor if
+// its depth is D, then push left and right (right popped first) — where the
+// last assignment stands.  Nodes below depth D cannot assign, so the walk
+// does not push past depth D.
+inline V4 bvh_color(const crt_bvh_node* nodes, uint32_t n_nodes, const crt_ray& r, uint32_t D) {
+    const float line = 0.05f / (static_cast<float>(D) + 1.f);
+    V4 color{0.f, 0.f, 0.f, 0.f};
+    if (n_nodes == 0) return color;
+    std::vector<std::pair<uint32_t, uint32_t>> stack{{0u, 0u}};
+    while (!stack.empty()) {
+        const auto [ni, depth] = stack.back();
+        stack.pop_back();
+        const crt_bvh_node& nd = nodes[ni];
+        const int hit = slab_display(r, nd, line);
+        if (hit == 0) continue;
+        if (depth == D) color = hit == 2 ? V4{0.7f, 0.f, 0.7f, 0.1f} : V4{0.5f, 0.f, 0.5f, 0.1f};
+        const bool leaf = nd.left == 0 && nd.right == 0;
+        if (!leaf && depth < D) {
+            stack.push_back({nd.left, depth + 1});
+            stack.push_back({nd.right, depth + 1});
+        }
+    }
+    return color;
+}
+
+}  // namespace
+
+extern "C" {
+
+// getColor + imageStore (raytracer.glsl:159-179, 319-330) for hit i of ray i
+// into rgba[4i .. 4i+3].  Material of a hit: the triangle's model's
+// material_id (model ids >= n_models: 0), colour (0,0,0,0) for material ids
+// >= n_materials.  flags: CRT_SHADE_WIREFRAME | CRT_SHADE_BVH; depth =
+// uDepthDisplayBVH.
+void oracle_shade(const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris, uint32_t n_tris,
+                  const crt_mesh_model* models, uint32_t n_models, const float* materials, uint32_t n_materials,
+                  const crt_ray* rays, const crt_hit* hits, uint32_t n, uint32_t flags, uint32_t depth, float* rgba) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) {
+        V4 value{0.f, 0.f, 0.f, 1.f};
+        if (flags & CRT_SHADE_BVH) value = bvh_color(nodes, n_nodes, rays[i], depth);
+        const crt_hit& h = hits[i];
+        if (h.tri != CRT_MISS && h.tri < n_tris) {
+            const uint32_t model = tris[h.tri].model_id;
+            const uint32_t mat = (models && model < n_models) ? models[model].material_id : 0u;
+            V4 c{0.f, 0.f, 0.f, 0.f};
+            if (mat < n_materials) c = load4(materials + 4 * static_cast<size_t>(mat));
+            value = V4{value.x + c.x, value.y + c.y, value.z + c.z, value.w + c.w};
+            if (flags & CRT_SHADE_WIREFRAME) {
+                const float w = 1.0f - h.u - h.v;
+                if (h.u < 0.02f || h.v < 0.02f || w < 0.02f) value = V4{0.f, 0.f, 0.f, 1.f};
+            }
+        }
+        float* o = rgba + 4 * static_cast<size_t>(i);
+        o[0] = value.x; o[1] = value.y; o[2] = value.z; o[3] = value.w;
+    }
+}
+
+}  // extern "C"

@@ -57,6 +57,7 @@ def lib():
         L.oracle_shadow_rays.argtypes = [vp, vp, u32, vp, vp]
         L.oracle_trace.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, u32, vp, vp]
         L.oracle_trace_brute.argtypes = [vp, u32, vp, u32, vp, u32, u32, vp]
+        L.oracle_shade.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, vp, vp, u32, u32, u32, vp]
         _lib = L
     return _lib
 
@@ -153,3 +154,15 @@ def trace_brute(tris, models, rays, flags=0):
     hits = np.zeros((rays.shape[0], 4), np.float32)
     lib().oracle_trace_brute(_p(tris), tris.shape[0], _p(models), models.shape[0], _p(rays), rays.shape[0], flags, _p(hits))
     return hits
+
+
+def shade(nodes, tris, models, materials, rays, hits, flags=0, depth=0):
+    """getColor + imageStore per hit: (n, 4) float32 RGBA (rays read with the BVH flag)."""
+    nodes = _f32(nodes, 12)
+    tris, models, rays = _f32(tris, 16), _f32(models, 17), _f32(rays, 8)
+    materials = _f32(materials, 4)
+    hits = np.ascontiguousarray(hits, np.float32)
+    out = np.zeros((hits.shape[0], 4), np.float32)
+    lib().oracle_shade(_p(nodes), nodes.shape[0], _p(tris), tris.shape[0], _p(models), models.shape[0],
+                       _p(materials), materials.shape[0], _p(rays), _p(hits), hits.shape[0], flags, depth, _p(out))
+    return out

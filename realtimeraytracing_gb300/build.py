@@ -26,6 +26,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE
 UNITS = [
     ("crt_build.cu", ["-fmad=false"]),
     ("crt_trace.cu", ["-fmad=false"]),
+    ("crt_frame.cu", ["-fmad=false"]),
     ("crt_api.cu", ["-fmad=false"]),
     ("crt_noalloc.cu", ["-fmad=false"]),
     ("crt_predictor.cu", []),

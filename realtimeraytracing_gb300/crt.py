@@ -33,6 +33,10 @@ SORT_RAYS = 0x40  # CRT_TRACE_SORT_RAYS: trace rays ordered by origin cell and d
 USE_PREDICTOR = TRACE_USE_PREDICTOR
 MISS = 0xFFFFFFFF
 
+SHADE_WIREFRAME = 0x1  # CRT_SHADE_WIREFRAME: uIsWireframeModeOn
+SHADE_BVH = 0x2  # CRT_SHADE_BVH: uIsBVHDisplayed
+SHADE_MAX_BVH_DEPTH = 63
+
 # Every symbol include/crt.h declares.
 EXPORTS = [
     "crt_abi_version", "crt_default_config", "crt_create", "crt_destroy", "crt_sync", "crt_last_error_string",
@@ -44,7 +48,7 @@ EXPORTS = [
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
-    "crt_batch_autotune",
+    "crt_batch_autotune", "crt_shade", "crt_render_frame",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -130,6 +134,8 @@ def lib():
             "crt_batch_copy_nodes": ([vp, vp, u32, vp], i32),
             "crt_batch_scene_info": ([vp, u32, vp], i32),
             "crt_batch_autotune": ([vp, vp, vp, vp, u32, vp, vp, vp], i32),
+            "crt_shade": ([vp, vp, vp, vp, u32, vp, vp], i32),
+            "crt_render_frame": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -161,6 +167,26 @@ def _ptr(a):
 
 def _rows(a):
     return a.shape[0]
+
+
+class Shading(C.Structure):
+    """crt_shading: getColor's uniforms and its model / material buffers."""
+    _fields_ = [("models", C.c_void_p), ("n_models", C.c_uint32), ("materials", C.c_void_p),
+                ("n_materials", C.c_uint32), ("flags", C.c_uint32), ("bvh_depth", C.c_uint32)]
+
+
+def _shading(models, materials, flags, bvh_depth):
+    """(crt_shading, arrays it points to — keep them alive for the call)."""
+    models = _models(models)
+    if materials is not None and isinstance(materials, np.ndarray):
+        materials = np.ascontiguousarray(materials, np.float32)
+    sh = Shading()
+    sh.models = _ptr(models) if models is not None else None
+    sh.n_models = 0 if models is None else _rows(models)
+    sh.materials = _ptr(materials) if materials is not None else None
+    sh.n_materials = 0 if materials is None else _rows(materials)
+    sh.flags, sh.bvh_depth = flags, bvh_depth
+    return sh, (models, materials)
 
 
 class PredictorConfig(C.Structure):
@@ -502,3 +528,29 @@ class Context:
         _check(lib().crt_trace_frame(self.handle, bvh.handle, _ptr(cam), width, height, lp, flags, _ptr(hp),
                                      _ptr(hs)))
         return hp, hs
+
+    def shade(self, bvh: Bvh, rays, hits, models=None, materials=None, shade_flags: int = 0, bvh_depth: int = 0,
+              out=None):
+        """getColor + imageStore for each hit: (n, 4) RGBA32F texels.  rays are
+        read only with SHADE_BVH (else they may be None)."""
+        self._after_torch()
+        n = _rows(hits)
+        out = np.empty((n, 4), np.float32) if out is None else out
+        sh, keep = _shading(models, materials, shade_flags, bvh_depth)
+        _check(lib().crt_shade(self.handle, bvh.handle, _ptr(rays), _ptr(hits), n, C.byref(sh), _ptr(out)))
+        del keep
+        return out
+
+    def render_frame(self, bvh: Bvh, cam, width: int, height: int, models=None, materials=None,
+                     shade_flags: int = 0, bvh_depth: int = 0, flags: int = 0, out=None):
+        """The reference's compute pass (raytracer.glsl main): camera ray,
+        closest hit, getColor and imageStore per texel, (width*height, 4)
+        RGBA32F with texel (x, y) at row y * width + x."""
+        self._after_torch()
+        cam = np.ascontiguousarray(cam, np.float32) if isinstance(cam, np.ndarray) else cam
+        out = np.empty((width * height, 4), np.float32) if out is None else out
+        sh, keep = _shading(models, materials, shade_flags, bvh_depth)
+        _check(lib().crt_render_frame(self.handle, bvh.handle, _ptr(cam), width, height, flags, C.byref(sh),
+                                      _ptr(out)))
+        del keep
+        return out

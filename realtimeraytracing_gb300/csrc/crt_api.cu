@@ -147,6 +147,7 @@ struct crt_ctx {
     DevBuf node_box, node_kids, pos, clus_a, clus_b, iters, ploc_lb;
     DevBuf cam, rays_in, hits_out, rays_out, trace_stats, frame_rays, frame_hits, frame_shadow, frame_shits;
     DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
+    DevBuf shade_models, shade_materials, shade_rays, shade_hits, image;  // crt_shade / crt_render_frame
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -258,7 +259,8 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->codes_b, &x->vals_a, &x->vals_b, &x->node_box, &x->node_kids, &x->pos, &x->clus_a,
                       &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
-                      &x->ray_order, &x->ray_order_scratch};
+                      &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
+                      &x->shade_rays, &x->shade_hits, &x->image};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -837,7 +839,7 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
         // hits are copied out on a second stream while the next band runs was
         // measured slower at every band count (2, 4, 8) on GB300.
         crt::launch_frame(p, d_cam, width, height, 0, height, light, d_hs, kflags, static_cast<int>(x->cfg.trace_block),
-                          x->stream);
+                          nullptr, x->stream);
         CRT_CUDA(cudaGetLastError());
         if (!dev_p)
             CRT_CUDA(cudaMemcpyAsync(hits_primary, d_hp, sizeof(crt_hit) * static_cast<size_t>(n), cudaMemcpyDeviceToHost,
@@ -1539,6 +1541,164 @@ crt_status crt_batch_autotune(crt_ctx* x, crt_batch* bt, const crt_triangle* tri
     cudaEventDestroy(e2);
     if (best) *best = bt->cfg;
     if (best_ms) *best_ms = best_build + best_trace;
+    return CRT_OK;
+}
+
+}  // extern "C"
+
+// ===================================================================== shading
+namespace {
+
+static_assert(sizeof(crt_mesh_model) == 17 * 4, "crt_mesh_model: 16 floats + material id");
+static_assert(sizeof(crt_material) == 16, "crt_material: one RGBA colour");
+
+bool aligned(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+// Checks a crt_shading and stages what getColor reads (model material ids,
+// material colours) in device memory.
+crt_status shade_setup(crt_ctx* x, const crt_bvh* b, const crt_shading* sh, crt::ShadeParams* sp) {
+    if (!sh) return fail(CRT_ERR_INVALID_ARG, "shading: null crt_shading");
+    if (sh->flags & ~(CRT_SHADE_WIREFRAME | CRT_SHADE_BVH))
+        return fail(CRT_ERR_INVALID_ARG, "shading: unknown flags 0x%x", sh->flags);
+    if (sh->bvh_depth > CRT_SHADE_MAX_BVH_DEPTH)
+        return fail(CRT_ERR_INVALID_ARG, "shading: bvh_depth %u > %u", sh->bvh_depth, CRT_SHADE_MAX_BVH_DEPTH);
+    if (sh->n_models > crt::kMaxModels) return fail(CRT_ERR_INVALID_ARG, "shading: n_models %u > 64", sh->n_models);
+    if ((sh->n_models && !sh->models) || (sh->n_materials && !sh->materials))
+        return fail(CRT_ERR_INVALID_ARG, "shading: null models or materials");
+    *sp = crt::ShadeParams{};
+    sp->flags = sh->flags;
+    sp->bvh_depth = sh->bvh_depth;
+    sp->inv_perm = b->inv_perm.as<uint32_t>();
+    sp->n_tris = b->n;
+    if (sh->n_models) {
+        const void* d = nullptr;
+        CRT_TRY(stage_in(x, x->shade_models, sh->models, sizeof(crt_mesh_model) * sh->n_models, &d));
+        if (!aligned(d, 4)) return fail(CRT_ERR_INVALID_ARG, "shading: models must be 4-byte aligned");
+        sp->models = static_cast<const uint32_t*>(d);
+        sp->n_models = sh->n_models;
+    }
+    if (sh->n_materials) {
+        const void* d = nullptr;
+        CRT_TRY(stage_in(x, x->shade_materials, sh->materials, sizeof(crt_material) * sh->n_materials, &d));
+        if (!aligned(d, 16)) return fail(CRT_ERR_INVALID_ARG, "shading: materials must be 16-byte aligned");
+        sp->materials = static_cast<const float4*>(d);
+        sp->n_materials = sh->n_materials;
+    }
+    return CRT_OK;
+}
+
+// Where the kernel writes n texels for the caller's rgba: device memory,
+// page-locked host memory (written by the kernel over the CPU-GPU link), or
+// a context buffer that is copied out afterwards (*copy_out).
+crt_status image_target(crt_ctx* x, float* rgba, size_t n, float4** dev, bool* copy_out) {
+    *copy_out = false;
+    void* d = is_device_ptr(rgba) ? static_cast<void*>(rgba) : mapped_host_ptr(rgba);
+    if (d) {
+        if (!aligned(d, 16)) return fail(CRT_ERR_INVALID_ARG, "rgba must be 16-byte aligned");
+        *dev = static_cast<float4*>(d);
+        return CRT_OK;
+    }
+    CRT_TRY(x->image.reserve(16 * n));
+    *dev = x->image.as<float4>();
+    *copy_out = true;
+    return CRT_OK;
+}
+
+crt::TraceParams bvh_params(crt_ctx* x, const crt_bvh* b, uint32_t flags) {
+    crt::TraceParams p{};
+    p.nodes = b->nodes.as<crt_bvh_node>();
+    p.xtri = b->xtri.as<float4>();
+    p.wide = (flags & CRT_TRI_WATERTIGHT) ? b->wide_wt.as<float4>() : b->wide.as<float4>();
+    p.n_nodes = 2 * b->n - 1;
+    p.abs_eps = b->abs_eps;
+    p.err = x->err.as<uint32_t>();
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+crt_status crt_shade(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, const crt_hit* hits, uint32_t n,
+                     const crt_shading* sh, float* rgba) {
+    if (!x || !b || !hits || !rgba) return fail(CRT_ERR_INVALID_ARG, "crt_shade: null argument");
+    if (sh && (sh->flags & CRT_SHADE_BVH) && !rays)
+        return fail(CRT_ERR_INVALID_ARG, "crt_shade: CRT_SHADE_BVH reads the rays");
+    if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_shade: empty bvh");
+    CRT_CUDA(cudaSetDevice(x->device));
+    crt::ShadeParams sp;
+    CRT_TRY(shade_setup(x, b, sh, &sp));
+    if (n == 0) return CRT_OK;
+    const void* d_hits = nullptr;
+    CRT_TRY(stage_in(x, x->shade_hits, hits, sizeof(crt_hit) * n, &d_hits));
+    const void* d_rays = nullptr;
+    if (sp.flags & CRT_SHADE_BVH) CRT_TRY(stage_in(x, x->shade_rays, rays, sizeof(crt_ray) * n, &d_rays));
+    if (!aligned(d_hits, 16) || !aligned(d_rays, 16))
+        return fail(CRT_ERR_INVALID_ARG, "crt_shade: rays and hits must be 16-byte aligned");
+    bool copy_out = false;
+    CRT_TRY(image_target(x, rgba, n, &sp.image, &copy_out));
+    crt::TraceParams p = bvh_params(x, b, 0);
+    p.rays = static_cast<const crt_ray*>(d_rays);
+    p.hits = static_cast<crt_hit*>(const_cast<void*>(d_hits));
+    p.n_rays = n;
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    crt::launch_shade(p, sp, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (copy_out) CRT_CUDA(cudaMemcpyAsync(rgba, sp.image, 16 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
+    return x->check_device_error();
+}
+
+crt_status crt_render_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, uint32_t width, uint32_t height,
+                            uint32_t flags, const crt_shading* sh, float* rgba) {
+    if (!x || !b || !cam || !rgba) return fail(CRT_ERR_INVALID_ARG, "crt_render_frame: null argument");
+    if (width == 0 || height == 0 || height > 65535 || static_cast<uint64_t>(width) * height > (1ull << 31))
+        return fail(CRT_ERR_INVALID_ARG, "bad image size");
+    CRT_TRY(check_trace_flags(b, flags));
+    if (flags & CRT_TRACE_ANY) return fail(CRT_ERR_INVALID_ARG, "crt_render_frame: primary rays are closest-hit");
+    CRT_CUDA(cudaSetDevice(x->device));
+    crt::ShadeParams sp;
+    CRT_TRY(shade_setup(x, b, sh, &sp));
+    const uint32_t n = width * height;
+    bool copy_out = false;
+    CRT_TRY(image_target(x, rgba, n, &sp.image, &copy_out));
+    const crt_camera* d_cam = cam;
+    if (!is_device_ptr(cam)) {
+        CRT_CUDA(cudaMemcpyAsync(x->cam.p, cam, sizeof(crt_camera), cudaMemcpyHostToDevice, x->stream));
+        d_cam = x->cam.as<crt_camera>();
+    }
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
+    if (!(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE))) {
+        // one launch: camera ray, closest hit and texel per pixel
+        crt::TraceParams p = bvh_params(x, b, flags);
+        p.n_rays = n;
+        p.tile_width = tw;
+        if (flags & CRT_TRACE_STATS) {
+            CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
+            p.stats = x->trace_stats.as<unsigned long long>();
+        }
+        const bool deep = b->iterations + 2 > 64;
+        const uint32_t kflags = (flags & CRT_TRI_WATERTIGHT) | (deep ? (1u << 16) : 0u);
+        crt::launch_frame(p, d_cam, width, height, 0, height, nullptr, nullptr, kflags,
+                          static_cast<int>(x->cfg.trace_block), &sp, x->stream);
+        CRT_CUDA(cudaGetLastError());
+    } else {
+        CRT_TRY(x->frame_rays.reserve(sizeof(crt_ray) * static_cast<size_t>(n)));
+        CRT_TRY(x->frame_hits.reserve(sizeof(crt_hit) * static_cast<size_t>(n)));
+        crt_ray* rays = x->frame_rays.as<crt_ray>();
+        crt_hit* hits = x->frame_hits.as<crt_hit>();
+        crt::launch_raygen(d_cam, width, height, rays, x->stream);
+        CRT_TRY(trace_device(x, b, rays, n, flags, hits, nullptr, tw));
+        crt::TraceParams p = bvh_params(x, b, flags);
+        p.rays = rays;
+        p.hits = hits;
+        p.n_rays = n;
+        crt::launch_shade(p, sp, x->stream);
+        CRT_CUDA(cudaGetLastError());
+    }
+    if (copy_out) CRT_CUDA(cudaMemcpyAsync(rgba, sp.image, 16 * static_cast<size_t>(n), cudaMemcpyDeviceToHost, x->stream));
+    CRT_TRY(x->check_device_error());
+    if (flags & CRT_TRACE_STATS) CRT_CUDA(cudaMemcpy(x->last_trace_stats, x->trace_stats.p, 16, cudaMemcpyDeviceToHost));
     return CRT_OK;
 }
 

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(256) batch_leaf_init_kernel(const crt_triangle
     clusters[2 * static_cast<size_t>(i)] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(li));
     clusters[2 * static_cast<size_t>(i) + 1] = make_float4(mx.x, mx.y, mx.z, __uint_as_float(1u));
     xtri[3 * static_cast<size_t>(i) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(tl));
-    xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, 0.f);
+    xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
     xtri[3 * static_cast<size_t>(i) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
     if (sc.n_tris == 1) {
         float4* o = reinterpret_cast<float4*>(nodes + sc.node_off);

@@ -406,9 +406,10 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
     mx.w = __uint_as_float(1u);
     clusters[2 * static_cast<size_t>(i)] = mn;
     clusters[2 * static_cast<size_t>(i) + 1] = mx;
-    // leaf order (= left-to-right order of the final tree), triangle id in .w
+    // leaf order (= left-to-right order of the final tree): triangle id in
+    // the first .w, model id in the second (read by the shading pass)
     xtri[3 * static_cast<size_t>(i) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(ti));
-    xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, 0.f);
+    xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
     xtri[3 * static_cast<size_t>(i) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
 }
 

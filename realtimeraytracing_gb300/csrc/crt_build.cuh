@@ -109,11 +109,31 @@ struct TraceParams {
     const uint32_t* order = nullptr;
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
+
+// Shading (getColor + imageStore) inputs; the BVH, leaf records and error
+// word come from the TraceParams it runs with.
+constexpr uint32_t kShadeMaxDepth = 64;   // display-walk stack: CRT_SHADE_MAX_BVH_DEPTH + 1
+struct ShadeParams {
+    const uint32_t* models = nullptr;     // crt_mesh_model records as 32-bit words, 17 per model (word 16: material id)
+    uint32_t n_models = 0;
+    const float4* materials = nullptr;    // crt_material colours
+    uint32_t n_materials = 0;
+    uint32_t flags = 0;                   // CRT_SHADE_*
+    uint32_t bvh_depth = 0;
+    const uint32_t* inv_perm = nullptr;   // triangle -> leaf position (its xtri record holds the model id)
+    uint32_t n_tris = 0;
+    float4* image = nullptr;              // RGBA32F texels
+};
+// Texels of p.n_rays hits p.hits of rays p.rays (rays read with CRT_SHADE_BVH only).
+void launch_shade(const TraceParams& p, const ShadeParams& sp, cudaStream_t s);
+
 // Camera rays of image rows [y0, y0 + rows) traced to the closest hit into
-// p.hits and, with a light, their shadow rays to any hit into hits_shadow,
+// p.hits (may be null with shading) and, with a light, their shadow rays to
+// any hit into hits_shadow, and with shade, their texels into shade->image,
 // in one launch (p.tile_width: width for 8x4 pixel tiles, or 0).
 void launch_frame(const TraceParams& p, const crt_camera* cam, uint32_t width, uint32_t height, uint32_t y0,
-                  uint32_t rows, const float* light, crt_hit* hits_shadow, uint32_t flags, int block, cudaStream_t s);
+                  uint32_t rows, const float* light, crt_hit* hits_shadow, uint32_t flags, int block,
+                  const ShadeParams* shade, cudaStream_t s);
 
 // Batched scenes: per-scene offsets into the concatenated arrays.
 constexpr uint32_t kMaxBatchScenes = 256;

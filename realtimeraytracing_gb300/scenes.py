@@ -13,6 +13,8 @@ Record layouts (see include/crt.h):
   models     (m, 17) float32: column-major 4x4, material id (uint32 bits)
   rays       (n, 8)  float32: o.xyz, tmin, d.xyz, tmax
   hits       (n, 4)  float32: tri (uint32 bits), t, u, v
+  materials  (m, 4)  float32: RGBA colour
+  texels     (n, 4)  float32: RGBA, texel (x, y) at row y * width + x
   nodes      (2n-1, 12) float32: min.xyz, pad, max.xyz, pad, tri, left, right, pad (uint32 bits)
 """
 from __future__ import annotations
@@ -86,6 +88,19 @@ def identity_models(n: int = 1) -> np.ndarray:
     m = np.zeros((n, 17), np.float32)
     m[:, [0, 5, 10, 15]] = 1.0
     return m
+
+
+def models_with_materials(material_ids) -> np.ndarray:
+    """Identity model records whose material ids are material_ids."""
+    ids = np.asarray(material_ids, np.uint32).reshape(-1)
+    m = identity_models(ids.shape[0])
+    m.view(np.uint32)[:, 16] = ids
+    return m
+
+
+def materials(colors) -> np.ndarray:
+    """crt_material records (m, 4) float32: RGBA colours (Material::_Color)."""
+    return np.ascontiguousarray(np.asarray(colors, np.float32).reshape(-1, 4))
 
 
 def uniform_soup(n: int, seed: int = 0, edge_lo: float = 0.001, edge_hi: float = 0.02) -> np.ndarray:

@@ -58,34 +58,33 @@ def test_invalid_config_rejected(lib):
         crt.Context(sort_digit_bits=5)
 
 
-def test_struct_sizes_match_reference_records():
+def test_struct_sizes_match_reference_records(tmp_path):
     code = r'''
 #include <stdio.h>
 #include <stddef.h>
 #include "crt.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(crt_triangle), sizeof(crt_mesh_model),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(crt_triangle), sizeof(crt_mesh_model),
          sizeof(crt_bvh_node), sizeof(crt_ray), sizeof(crt_hit), offsetof(crt_bvh_node, mx),
-         offsetof(crt_bvh_node, tri), offsetof(crt_bvh_node, right), offsetof(crt_triangle, model_id));
+         offsetof(crt_bvh_node, tri), offsetof(crt_bvh_node, right), offsetof(crt_triangle, model_id),
+         sizeof(crt_material), sizeof(crt_shading), offsetof(crt_shading, bvh_depth));
   return 0;
 }'''
-    tmp = os.path.join(ROOT, "_work", "abi_sizes")
-    os.makedirs(tmp, exist_ok=True)
-    src = os.path.join(tmp, "sizes.c")
-    with open(src, "w") as f:
-        f.write(code)
-    exe = os.path.join(tmp, "sizes")
-    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+    src = tmp_path / "sizes.c"
+    src.write_text(code)
+    exe = str(tmp_path / "sizes")
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
     out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
-    # TriangleGPU 64, MeshModelGPU 68, BVH_NodeGPU 48 (max @16, tri @32, right @40)
-    assert [int(x) for x in out] == [64, 68, 48, 32, 16, 16, 32, 40, 48]
+    # TriangleGPU 64, MeshModelGPU 68, BVH_NodeGPU 48 (max @16, tri @32, right @40), MaterialGPU 16
+    assert [int(x) for x in out] == [64, 68, 48, 32, 16, 16, 32, 40, 48, 16, 40, 32]
+    from realtimeraytracing_gb300 import crt
+    assert C.sizeof(crt.Shading) == 40 and crt.Shading.bvh_depth.offset == 32
 
 
 @pytest.mark.skipif(not os.path.isdir("/root/reference/srcCommon"), reason="reference checkout not present")
-def test_adapter_compiles_and_links_against_reference_header(lib):
+def test_adapter_compiles_and_links_against_reference_header(lib, tmp_path):
     gxx = shutil.which("g++")
-    tmp = os.path.join(ROOT, "_work", "adapter_build")
-    os.makedirs(tmp, exist_ok=True)
+    tmp = str(tmp_path)
     inc = ["-I", os.path.join(ROOT, "oracle", "glm_shim"), "-I", "/root/reference/srcCommon/scene/geometry",
            "-I", os.path.join(ROOT, "include")]
     obj = os.path.join(tmp, "bvh_cuda.o")
