@@ -7,9 +7,9 @@ The reference builds its BVH with
         srcCommon/scene/geometry/bvh.hpp:89-91, bvh.cpp:11-24
 and Scene::getBVH_NodesToGPUData (srcOpenGL/scene/scene.cpp:203-208)
 flattens it into the node array the shader reads; getClosestHitBVH
-(srcCommon/shaders/raytracer.glsl:246-295) traces it per pixel.  BVH and
-Raytracer below keep those names and argument meanings; all work runs in the
-CUDA library.
+(srcCommon/shaders/raytracer.glsl:246-295) traces it per pixel and getColor
+(:159-179) shades it.  BVH and Raytracer below keep those names and argument
+meanings; all work runs in the CUDA library.
 """
 from __future__ import annotations
 
@@ -65,11 +65,31 @@ class BVH:
 
 
 class Raytracer:
-    """The compute pass of Application::drawOneFrame (application.cpp:220-262)
-    minus shading: getRay for every texel, then getClosestHitBVH."""
+    """The compute pass of Application::drawOneFrame (application.cpp:220-262):
+    getRay for every texel, getClosestHitBVH, getColor and imageStore.  The
+    shader's uniforms (application.cpp:229-232) are the attributes below."""
 
     def __init__(self, ctx: crt.Context | None = None):
         self._ctx = ctx or default_context()
+        self.uIsWireframeModeOn = False
+        self.uIsBVHDisplayed = False
+        self.uDepthDisplayBVH = 0
+
+    def _shade_flags(self) -> int:
+        return (crt.SHADE_WIREFRAME if self.uIsWireframeModeOn else 0) | (crt.SHADE_BVH if self.uIsBVHDisplayed else 0)
+
+    def getColor(self, bvh: BVH, rays, hits, models=None, materials=None, out=None):
+        """getColor (raytracer.glsl:159-179) for each hit: (n, 4) RGBA32F texels."""
+        return self._ctx.shade(bvh.handle, rays, hits, models, materials, self._shade_flags(),
+                               self.uDepthDisplayBVH, out)
+
+    def drawOneFrame(self, bvh: BVH, camera_gpu, width: int, height: int, models=None, materials=None,
+                     watertight: bool = False, out=None):
+        """One dispatch of raytracer.glsl main: the (width*height, 4) RGBA32F
+        oImage texels, texel (x, y) at row y * width + x."""
+        flags = crt.TRI_WATERTIGHT if watertight else crt.TRI_REFERENCE
+        return self._ctx.render_frame(bvh.handle, camera_gpu, width, height, models, materials,
+                                      self._shade_flags(), self.uDepthDisplayBVH, flags, out)
 
     def getRays(self, camera_gpu, width: int, height: int, out=None):
         return self._ctx.raygen(camera_gpu, width, height, out)
