@@ -446,7 +446,10 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
     the order of their predicted treelets (CRT_TRACE_PREDICTOR_ORDER).  Frame =
     rebuild + primary + bounce generation + ordered bounce trace + training.
     Every 15 frames the same bounce rays are also traced plain, seeded and
-    sorted without the network, off the frame clock."""
+    sorted without the network, off the frame clock.  The same 60 frames then
+    run again with crt_refit of the frame-0 tree in place of the rebuild; the
+    primary hits of every frame must equal the rebuild run's (watertight hits
+    do not depend on the tree)."""
     from realtimeraytracing_gb300 import scenes as S
     n = 16 * 1024 * 1024
     gen = torch.Generator(device=dev)
@@ -460,65 +463,99 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
     W, H = 1920, 1080
     hp = torch.empty((W * H, 4), dtype=torch.float32, device=dev)
     prim = torch.empty((W * H, 8), dtype=torch.float32, device=dev)
-    bvh = ctx.build(tris, models=models)
-    pred = crt.Predictor(ctx, bvh, seed=3)
-    frame_ms, build_ms, sort_ms, compare, ordered_ms, rays_traced = [], [], [], [], [], []
-    identical = True
-    bounce = hb_plain = hb_seed = None
-    for f in range(frames):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        tris[:, [1, 5, 9]] = y0 + 0.01 * torch.sin(2 * np.pi * f / 60 + 7 * x0)
-        bvh.rebuild(tris, models=models)
-        st = ctx.last_build_stats()
-        pred.retarget()
-        ctx.raygen(cam, W, H, out=prim)
-        ctx.trace(bvh, prim, crt.TRI_WATERTIGHT, out=hp)
-        n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
-        nb = max(2 * n_hits, 1)
-        if bounce is None or bounce.shape[0] < nb:
-            bounce = torch.empty((nb, 8), dtype=torch.float32, device=dev)
-            hb_plain = torch.empty((nb, 4), dtype=torch.float32, device=dev)
-            hb_seed = torch.empty((nb, 4), dtype=torch.float32, device=dev)
-        br, hs = bounce[:nb], hb_seed[:nb]
-        ctx.bounce_rays(bvh, prim, hp, nb, seed=100 + f, out=br)
-        ts = time.perf_counter()
-        ctx.trace(bvh, br, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER, out=hs)
-        torch.cuda.synchronize()
-        ordered_ms.append((time.perf_counter() - ts) * 1e3)
-        pred.train(br, hs, offset=f % 20)   # retrain on this frame's exact hits
-        torch.cuda.synchronize()
-        frame_ms.append((time.perf_counter() - t0) * 1e3)
-        build_ms.append(st["ms_total"])
-        sort_ms.append(st["ms_sort"])
-        rays_traced.append(W * H + nb)
-        if f % 15 == 0 or f == frames - 1:
-            # the same bounce rays plain, seeded and sorted without the network, off the frame clock
-            row = {"rays": int(nb), "predictor_ordered_ms": round(ordered_ms[-1], 3)}
-            for name, fl in (("plain_ms", 0), ("seeded_ms", crt.USE_PREDICTOR), ("sorted_no_network_ms", crt.SORT_RAYS)):
-                tp = time.perf_counter()
-                ctx.trace(bvh, br, crt.TRI_WATERTIGHT | fl, out=hb_plain[:nb])
-                torch.cuda.synchronize()
-                row[name] = round((time.perf_counter() - tp) * 1e3, 3)
-                identical = identical and bool(torch.equal(hb_plain[:nb].view(torch.int32), hs.view(torch.int32)))
-            compare.append(row)
-    pred.free()
-    bvh.free()
-    fm = np.array(frame_ms[1:])
-    sort_bytes = 16.0 * n * 4 - 4.0 * n  # 4 passes x (8 B in + 8 B out); pass 0 synthesises values
-    return {
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    primary_sums = {}
+
+    def animate(refit):
+        bvh = ctx.build(base, models=models)
+        pred = crt.Predictor(ctx, bvh, seed=3)
+        frame_ms, update_ms, sort_ms, prim_ms, compare, ordered_ms, rays_traced = [], [], [], [], [], [], []
+        identical = True
+        bounce = hb_plain = hb_seed = None
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        for f in range(frames):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tris[:, [1, 5, 9]] = y0 + 0.01 * torch.sin(2 * np.pi * f / 60 + 7 * x0)
+            if refit:
+                stream.wait_stream(torch.cuda.current_stream(dev))  # the clock starts after the vertex update
+                e[0].record(stream)
+                bvh.refit(tris, models=models)
+                e[1].record(stream)
+            else:
+                bvh.rebuild(tris, models=models)
+                st = ctx.last_build_stats()
+                sort_ms.append(st["ms_sort"])
+                update_ms.append(st["ms_total"])
+            pred.retarget()
+            ctx.raygen(cam, W, H, out=prim)
+            ts = time.perf_counter()
+            ctx.trace(bvh, prim, crt.TRI_WATERTIGHT, out=hp)
+            prim_ms.append((time.perf_counter() - ts) * 1e3)
+            # order-independent digest of the frame's primary hits (ids and t bits)
+            hv = hp.view(torch.int32).to(torch.int64)
+            digest = int(((hv[:, 0] * 1000003 + hv[:, 1]) * (torch.arange(W * H, device=dev) + 1)).sum().item())
+            if refit:
+                identical = identical and primary_sums.get(f) == digest
+            else:
+                primary_sums[f] = digest
+            n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
+            nb = max(2 * n_hits, 1)
+            if bounce is None or bounce.shape[0] < nb:
+                bounce = torch.empty((nb, 8), dtype=torch.float32, device=dev)
+                hb_plain = torch.empty((nb, 4), dtype=torch.float32, device=dev)
+                hb_seed = torch.empty((nb, 4), dtype=torch.float32, device=dev)
+            br, hs = bounce[:nb], hb_seed[:nb]
+            ctx.bounce_rays(bvh, prim, hp, nb, seed=100 + f, out=br)
+            ts = time.perf_counter()
+            ctx.trace(bvh, br, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER, out=hs)
+            torch.cuda.synchronize()
+            ordered_ms.append((time.perf_counter() - ts) * 1e3)
+            pred.train(br, hs, offset=f % 20)   # retrain on this frame's exact hits
+            torch.cuda.synchronize()
+            frame_ms.append((time.perf_counter() - t0) * 1e3)
+            if refit:
+                update_ms.append(e[0].elapsed_time(e[1]))
+            rays_traced.append(W * H + nb)
+            if not refit and (f % 15 == 0 or f == frames - 1):
+                # the same bounce rays plain, seeded and sorted without the network, off the frame clock
+                row = {"rays": int(nb), "predictor_ordered_ms": round(ordered_ms[-1], 3)}
+                for name, fl in (("plain_ms", 0), ("seeded_ms", crt.USE_PREDICTOR),
+                                 ("sorted_no_network_ms", crt.SORT_RAYS)):
+                    tp = time.perf_counter()
+                    ctx.trace(bvh, br, crt.TRI_WATERTIGHT | fl, out=hb_plain[:nb])
+                    torch.cuda.synchronize()
+                    row[name] = round((time.perf_counter() - tp) * 1e3, 3)
+                    identical = identical and bool(torch.equal(hb_plain[:nb].view(torch.int32), hs.view(torch.int32)))
+                compare.append(row)
+        pred.free()
+        bvh.free()
+        fm = np.array(frame_ms[1:])
+        out = {
+            "frame_ms_p50": round(float(np.percentile(fm, 50)), 3), "frame_ms_p99": round(float(np.percentile(fm, 99)), 3),
+            ("refit_ms_p50" if refit else "build_ms_p50"): round(float(np.median(update_ms[1:])), 3),
+            "primary_trace_ms_p50": round(float(np.median(prim_ms[1:])), 3),
+            "primary_trace_ms_last": round(prim_ms[-1], 3),
+            "mrays_s": round(float(sum(rays_traced[1:]) / fm.sum() / 1e3), 1),
+            "identical_hits": identical,
+        }
+        if not refit:
+            sort_bytes = 16.0 * n * 4 - 4.0 * n  # 4 passes x (8 B in + 8 B out); pass 0 synthesises values
+            out["sort_ms_p50"] = round(float(np.median(sort_ms[1:])), 4)
+            out["sort_gbs"] = round(sort_bytes / (float(np.median(sort_ms[1:])) * 1e-3) / 1e9, 1)
+            out["bounce_trace_ms"] = compare
+        return out
+
+    rebuild = animate(refit=False)
+    refit = animate(refit=True)
+    return dict(rebuild, **{
         "workload": "16,777,216-tri clustered soup (1024 clusters), 60 animated frames, full rebuild per frame, "
                     "1920x1080 primary + 2 bounce rays per hit traced in predicted-treelet order, predictor retrained "
                     "per frame",
         "frames": frames,
-        "frame_ms_p50": round(float(np.percentile(fm, 50)), 3), "frame_ms_p99": round(float(np.percentile(fm, 99)), 3),
-        "build_ms_p50": round(float(np.median(build_ms[1:])), 3),
-        "mrays_s": round(float(sum(rays_traced[1:]) / fm.sum() / 1e3), 1),
-        "sort_ms_p50": round(float(np.median(sort_ms[1:])), 4),
-        "sort_gbs": round(sort_bytes / (float(np.median(sort_ms[1:])) * 1e-3) / 1e9, 1),
-        "bounce_trace_ms": compare,
-        "identical_hits": identical,
-    }
+        "refit": dict(refit, note="the same 60 frames with crt_refit of the frame-0 tree instead of a rebuild; "
+                                  "identical_hits compares every frame's primary hits with the rebuild run's"),
+    })
 
 
 def run_predictor_experiment(ctx, torch, crt, dev, stream, args):

@@ -172,6 +172,19 @@ crt_status crt_build(crt_ctx* ctx, const crt_triangle* tris, uint32_t n_buffer, 
 /* Rebuild into an existing handle (same or smaller capacity is reused). */
 crt_status crt_rebuild(crt_ctx* ctx, crt_bvh* bvh, const crt_triangle* tris, uint32_t n_buffer,
                        uint32_t n_tris, const crt_mesh_model* models, uint32_t n_models);
+/* Refit instead of rebuild, for moving geometry (no counterpart in the
+ * reference, which rebuilds).  The n_tris triangles (the count of the last
+ * build, same order and tree positions) carry new vertices and/or models; the
+ * tree keeps the last build's topology and every box is recomputed bottom-up
+ * with the build's rules — AABB::buildFromTriangle for leaves, AABB::merge(left,
+ * right) for internal nodes (bvh.cpp:383-413) — so unmoved triangles give the
+ * built node array bit for bit.  Traces afterwards are exact for the moved
+ * geometry (with CRT_TRI_REFERENCE, equal-t ties follow this tree's DFS
+ * order; watertight hits equal those of a rebuild).  The tree gets slower to
+ * trace as the motion grows: rebuild when it does.  A bound predictor needs
+ * crt_predictor_retarget afterwards, as after a rebuild. */
+crt_status crt_refit(crt_ctx* ctx, crt_bvh* bvh, const crt_triangle* tris, uint32_t n_tris,
+                     const crt_mesh_model* models, uint32_t n_models);
 crt_status crt_bvh_free(crt_bvh* bvh);
 uint32_t crt_bvh_node_count(const crt_bvh* bvh);       /* 2 * n_tris - 1 */
 uint32_t crt_bvh_triangle_count(const crt_bvh* bvh);

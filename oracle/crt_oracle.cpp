@@ -719,3 +719,33 @@ void oracle_shade(const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangl
 }
 
 }  // extern "C"
+
+// ===================================================================== refit
+extern "C" {
+
+// Refit of a DFS node array (the product's crt_refit): topology kept, boxes
+// recomputed from the moved triangles — leaves as AABB::buildFromTriangle
+// (bvh.cpp:383-399), internal nodes as AABB::merge(left, right)
+// (bvh.cpp:401-413), children before parents (in pre-order every child
+// follows its parent, so a reverse sweep suffices).  nodes is updated in place.
+void oracle_refit(crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris, uint32_t n_tris,
+                  const crt_mesh_model* models, uint32_t n_models) {
+    const Models M(models, n_models);
+    for (int64_t d = static_cast<int64_t>(n_nodes) - 1; d >= 0; --d) {
+        crt_bvh_node& nd = nodes[d];
+        Box b;
+        if (nd.left == 0 && nd.right == 0) {
+            if (nd.tri >= n_tris) continue;
+            b = leaf_box(tris[nd.tri], M.of(tris[nd.tri]));
+        } else {
+            const crt_bvh_node& l = nodes[nd.left];
+            const crt_bvh_node& r = nodes[nd.right];
+            b = merge(Box{{l.mn[0], l.mn[1], l.mn[2]}, {l.mx[0], l.mx[1], l.mx[2]}},
+                      Box{{r.mn[0], r.mn[1], r.mn[2]}, {r.mx[0], r.mx[1], r.mx[2]}});
+        }
+        nd.mn[0] = b.mn.x; nd.mn[1] = b.mn.y; nd.mn[2] = b.mn.z;
+        nd.mx[0] = b.mx.x; nd.mx[1] = b.mx.y; nd.mx[2] = b.mx.z;
+    }
+}
+
+}  // extern "C"

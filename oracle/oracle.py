@@ -58,6 +58,7 @@ def lib():
         L.oracle_trace.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, u32, vp, vp]
         L.oracle_trace_brute.argtypes = [vp, u32, vp, u32, vp, u32, u32, vp]
         L.oracle_shade.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, vp, vp, u32, u32, u32, vp]
+        L.oracle_refit.argtypes = [vp, u32, vp, u32, vp, u32]
         _lib = L
     return _lib
 
@@ -165,4 +166,12 @@ def shade(nodes, tris, models, materials, rays, hits, flags=0, depth=0):
     out = np.zeros((hits.shape[0], 4), np.float32)
     lib().oracle_shade(_p(nodes), nodes.shape[0], _p(tris), tris.shape[0], _p(models), models.shape[0],
                        _p(materials), materials.shape[0], _p(rays), _p(hits), hits.shape[0], flags, depth, _p(out))
+    return out
+
+
+def refit(nodes, tris, models):
+    """The node array with every box recomputed from the moved triangles (same topology)."""
+    out = np.array(_f32(nodes, 12), copy=True)
+    tris, models = _f32(tris, 16), _f32(models, 17)
+    lib().oracle_refit(_p(out), out.shape[0], _p(tris), tris.shape[0], _p(models), models.shape[0])
     return out

@@ -27,6 +27,7 @@ UNITS = [
     ("crt_build.cu", ["-fmad=false"]),
     ("crt_trace.cu", ["-fmad=false"]),
     ("crt_frame.cu", ["-fmad=false"]),
+    ("crt_refit.cu", ["-fmad=false"]),
     ("crt_api.cu", ["-fmad=false"]),
     ("crt_noalloc.cu", ["-fmad=false"]),
     ("crt_predictor.cu", []),

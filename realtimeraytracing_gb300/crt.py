@@ -48,7 +48,7 @@ EXPORTS = [
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
-    "crt_batch_autotune", "crt_shade", "crt_render_frame",
+    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -136,6 +136,7 @@ def lib():
             "crt_batch_autotune": ([vp, vp, vp, vp, u32, vp, vp, vp], i32),
             "crt_shade": ([vp, vp, vp, vp, u32, vp, vp], i32),
             "crt_render_frame": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
+            "crt_refit": ([vp, vp, vp, u32, vp, u32], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -381,6 +382,15 @@ class Bvh:
         n_tris = n_buffer if n_tris is None else n_tris
         _check(lib().crt_rebuild(self.ctx.handle, self.handle, _ptr(tris), n_buffer, n_tris, _ptr(models),
                                  0 if models is None else _rows(models)))
+        return self
+
+    def refit(self, tris, models=None):
+        """crt_refit: the first n_tris triangles moved (same order), same tree
+        topology, every box recomputed bottom-up."""
+        self.ctx._after_torch()
+        models = _models(models)
+        _check(lib().crt_refit(self.ctx.handle, self.handle, _ptr(tris), self.n_tris, _ptr(models),
+                               0 if models is None else _rows(models)))
         return self
 
     def free(self):

@@ -109,6 +109,9 @@ struct crt_bvh {
     // trace after a build, so builds whose trees are never walked 4-wide
     // neither compute nor store them.
     mutable bool wide4_ready = false;
+    // Refit topology of the last build (crt_refit, derived on its first call).
+    DevBuf refit_parent, refit_rank, refit_leaf, refit_cnt;
+    bool refit_ready = false;
 };
 
 struct crt_predictor {
@@ -148,6 +151,7 @@ struct crt_ctx {
     DevBuf cam, rays_in, hits_out, rays_out, trace_stats, frame_rays, frame_hits, frame_shadow, frame_shits;
     DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
     DevBuf shade_models, shade_materials, shade_rays, shade_hits, image;  // crt_shade / crt_render_frame
+    DevBuf refit_state;  // crt::RefitState
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -260,7 +264,7 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
                       &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
-                      &x->shade_rays, &x->shade_hits, &x->image};
+                      &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -281,6 +285,30 @@ void* crt_stream(crt_ctx* x) { return x ? static_cast<void*>(x->stream) : nullpt
 }  // extern "C"
 
 namespace {
+
+// Models: 64 column-major matrices (identity past n_models) and the same
+// matrices scaled by 1/3 for the centroid (triangle.cpp:32), into x->models.
+crt_status stage_model_matrices(crt_ctx* x, const crt_mesh_model* models, uint32_t n_models) {
+    float* hm = static_cast<float*>(x->pinned);
+    CRT_CUDA(cudaStreamSynchronize(x->stream));  // the pinned staging area may still feed an earlier copy
+    const bool dev = n_models > 0 && is_device_ptr(models);
+    for (uint32_t m = 0; m < 64; ++m) {
+        for (int k = 0; k < 16; ++k) hm[16 * m + k] = (k % 5 == 0) ? 1.f : 0.f;
+        if (m < n_models) {
+            crt_mesh_model mm;
+            if (dev) {
+                CRT_CUDA(cudaMemcpy(&mm, models + m, sizeof(mm), cudaMemcpyDeviceToHost));
+            } else {
+                std::memcpy(&mm, models + m, sizeof(mm));
+            }
+            std::memcpy(hm + 16 * m, mm.m, 64);
+        }
+    }
+    const volatile float third = 1.f / 3.f;
+    for (int k = 0; k < 64 * 16; ++k) hm[64 * 16 + k] = third * hm[k];
+    CRT_CUDA(cudaMemcpyAsync(x->models.p, hm, 2 * 64 * 16 * sizeof(float), cudaMemcpyHostToDevice, x->stream));
+    return CRT_OK;
+}
 
 crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
                       const crt_mesh_model* models, uint32_t n_models) {
@@ -328,29 +356,13 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(b->wide.reserve(64ull * N));
     CRT_TRY(b->wide_wt.reserve(64ull * N));
     b->wide4_ready = false;
+    b->refit_ready = false;
     CRT_TRY(b->depth_odd.reserve(N));
     CRT_TRY(b->inv_perm.reserve(4ull * N));
     CRT_TRY(b->codes.reserve(4ull * N));
     CRT_TRY(b->perm.reserve(4ull * N));
 
-    // ---- models: 64 column-major matrices (identity past n_models) and the
-    // same matrices scaled by 1/3 for the centroid (triangle.cpp:32)
-    float* hm = static_cast<float*>(x->pinned);
-    for (uint32_t m = 0; m < 64; ++m) {
-        for (int k = 0; k < 16; ++k) hm[16 * m + k] = (k % 5 == 0) ? 1.f : 0.f;
-        if (m < n_models) {
-            crt_mesh_model mm;
-            if (is_device_ptr(models)) {
-                CRT_CUDA(cudaMemcpy(&mm, models + m, sizeof(mm), cudaMemcpyDeviceToHost));
-            } else {
-                std::memcpy(&mm, models + m, sizeof(mm));
-            }
-            std::memcpy(hm + 16 * m, mm.m, 64);
-        }
-    }
-    const volatile float third = 1.f / 3.f;
-    for (int k = 0; k < 64 * 16; ++k) hm[64 * 16 + k] = third * hm[k];
-    CRT_CUDA(cudaMemcpyAsync(x->models.p, hm, 2 * 64 * 16 * sizeof(float), cudaMemcpyHostToDevice, s));
+    CRT_TRY(stage_model_matrices(x, models, n_models));
     const float* d_models = x->models.as<float>();
     const float* d_models3 = d_models + 64 * 16;
 
@@ -623,6 +635,57 @@ crt_status crt_rebuild(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_
     return build_impl(x, b, tris, n_buffer, n_tris, models, n_models);
 }
 
+crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t n_tris, const crt_mesh_model* models,
+                     uint32_t n_models) {
+    if (!x || !b || !tris) return fail(CRT_ERR_INVALID_ARG, "crt_refit: null argument");
+    if (b->n == 0 || n_tris != b->n)
+        return fail(CRT_ERR_INVALID_ARG, "crt_refit: %u triangles for a bvh built over %u", n_tris, b->n);
+    if (n_models > crt::kMaxModels) return fail(CRT_ERR_INVALID_ARG, "crt_refit: more than 64 models");
+    if (n_models > 0 && !models) return fail(CRT_ERR_INVALID_ARG, "crt_refit: null models");
+    CRT_CUDA(cudaSetDevice(x->device));
+    cudaStream_t s = x->stream;
+    const uint32_t N = b->n;
+    const crt_triangle* d_tris = tris;
+    if (!is_device_ptr(tris)) {
+        CRT_TRY(x->tris_in.reserve(sizeof(crt_triangle) * static_cast<size_t>(N)));
+        CRT_CUDA(cudaMemcpyAsync(x->tris_in.p, tris, sizeof(crt_triangle) * static_cast<size_t>(N), cudaMemcpyHostToDevice, s));
+        d_tris = x->tris_in.as<crt_triangle>();
+    }
+    CRT_TRY(stage_model_matrices(x, models, n_models));
+    CRT_TRY(x->refit_state.reserve(sizeof(crt::RefitState)));
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, s));
+    if (!b->refit_ready) {
+        CRT_TRY(b->refit_parent.reserve(4ull * (2ull * N - 1)));
+        CRT_TRY(b->refit_rank.reserve(4ull * (2ull * N - 1)));
+        CRT_TRY(b->refit_leaf.reserve(4ull * N));
+        CRT_TRY(b->refit_cnt.reserve(4ull * std::max<size_t>(N - 1, crt::refit_topo_blocks(N))));
+        // the counters' buffer holds the per-block counts of the topology pass first
+        crt::launch_refit_topology(b->nodes.as<crt_bvh_node>(), b->inv_perm.as<uint32_t>(), N,
+                                   b->refit_parent.as<uint32_t>(), b->refit_leaf.as<uint32_t>(),
+                                   b->refit_rank.as<uint32_t>(), b->refit_cnt.as<uint32_t>(), x->err.as<uint32_t>(), s);
+        CRT_CUDA(cudaGetLastError());
+        b->refit_ready = true;
+    }
+    if (N > 1) CRT_CUDA(cudaMemsetAsync(b->refit_cnt.p, 0, 4ull * (N - 1), s));
+    CRT_CUDA(cudaMemsetAsync(x->refit_state.p, 0, sizeof(crt::RefitState), s));
+    crt::launch_refit(d_tris, N, x->models.as<float>(), b->perm.as<uint32_t>(), b->refit_leaf.as<uint32_t>(),
+                      b->refit_parent.as<uint32_t>(), b->refit_rank.as<uint32_t>(), b->refit_cnt.as<uint32_t>(),
+                      b->nodes.as<crt_bvh_node>(), b->xtri.as<float4>(), b->wide.as<float4>(), b->wide_wt.as<float4>(),
+                      x->refit_state.as<crt::RefitState>(), x->err.as<uint32_t>(), s);
+    CRT_CUDA(cudaGetLastError());
+    float* h_eps = static_cast<float*>(x->pinned);
+    CRT_CUDA(cudaMemcpyAsync(h_eps, &x->refit_state.as<crt::RefitState>()->abs_eps, sizeof(float),
+                             cudaMemcpyDeviceToHost, s));
+    b->wide4_ready = false;
+    const crt_status st = x->check_device_error();
+    if (st != CRT_OK) {
+        b->refit_ready = false;  // derive the topology again next time
+        return st;
+    }
+    b->abs_eps = *h_eps;
+    return CRT_OK;
+}
+
 crt_status crt_bvh_free(crt_bvh* b) {
     if (!b) return CRT_OK;
     b->nodes.release();
@@ -635,6 +698,10 @@ crt_status crt_bvh_free(crt_bvh* b) {
     if (b->predictor) b->predictor->bvh = nullptr;
     b->codes.release();
     b->perm.release();
+    b->refit_parent.release();
+    b->refit_rank.release();
+    b->refit_leaf.release();
+    b->refit_cnt.release();
     delete b;
     return CRT_OK;
 }

@@ -85,6 +85,26 @@ cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uin
                                    const SceneState* st, unsigned int* bar, uint32_t* iters_out, uint32_t* err,
                                    uint32_t spin_limit, cudaStream_t s);
 
+// Refit (crt_refit.cu).  State zeroed before each refit: the scene box of
+// the moved triangles as order-preserving keys, and the resulting slack.
+struct RefitState {
+    unsigned int key_max[3];
+    unsigned int key_min_inv[3];  // complemented keys, so that atomicMax finds the minimum
+    float abs_eps;
+    unsigned int pad;
+};
+uint32_t refit_topo_blocks(uint32_t N);
+// Once per build: parent of every node (DFS index), DFS index of every leaf,
+// traversal-node rank of every internal node.  block_count: refit_topo_blocks(N) words.
+void launch_refit_topology(const crt_bvh_node* nodes, const uint32_t* inv_perm, uint32_t N, uint32_t* parent,
+                           uint32_t* leaf_dfs, uint32_t* rank, uint32_t* block_count, uint32_t* err, cudaStream_t s);
+// New leaf records and every box of the node array and both traversal node
+// arrays; cnt (N - 1 words) and st zeroed before.
+void launch_refit(const crt_triangle* tris, uint32_t N, const float* models, const uint32_t* perm,
+                  const uint32_t* leaf_dfs, const uint32_t* parent, const uint32_t* rank, uint32_t* cnt,
+                  crt_bvh_node* nodes, float4* xtri, float4* wide, float4* wide_wt, RefitState* st, uint32_t* err,
+                  cudaStream_t s);
+
 // Trace side (crt_trace.cu).
 struct TraceParams {
     const crt_bvh_node* nodes;  // reference layout (root box read from nodes[0])
