@@ -102,7 +102,9 @@ struct crt_bvh {
     uint32_t n = 0;
     uint32_t iterations = 0;
     float abs_eps = 0.f;
-    DevBuf nodes, wide, wide_wt, depth_odd, xtri, codes, perm, inv_perm;  // wide_wt: boxes grown by abs_eps
+    // wide_wt: boxes grown by abs_eps; xtri: transformed triangles in the tree's
+    // left-to-right leaf order; inv_perm: triangle -> its position in that order
+    DevBuf nodes, wide, wide_wt, depth_odd, xtri, codes, perm, inv_perm;
     mutable DevBuf wide4;
     crt_predictor* predictor = nullptr;
     // The 4-wide traversal nodes are derived on the first CRT_TRACE_WIDE
@@ -110,8 +112,11 @@ struct crt_bvh {
     // neither compute nor store them.
     mutable bool wide4_ready = false;
     // Refit topology of the last build (crt_refit, derived on its first call).
-    DevBuf refit_parent, refit_rank, refit_leaf, refit_cnt;
+    DevBuf refit_link, refit_leaf, refit_dfs, refit_cnt;
     bool refit_ready = false;
+    // After a refit only the root box of the node array is current; the
+    // others are derived from the traversal nodes when the array is read.
+    mutable bool node_boxes_stale = false;
 };
 
 struct crt_predictor {
@@ -152,6 +157,7 @@ struct crt_ctx {
     DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
     DevBuf shade_models, shade_materials, shade_rays, shade_hits, image;  // crt_shade / crt_render_frame
     DevBuf refit_state;  // crt::RefitState
+    DevBuf xtri_sorted;  // leaf records in sorted order until the layout moves them
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -264,7 +270,7 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
                       &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
-                      &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state};
+                      &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state, &x->xtri_sorted};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -353,10 +359,12 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(x->ploc_lb.reserve(8ull * (2ull * ploc_tiles) + 64));
     CRT_TRY(b->nodes.reserve(sizeof(crt_bvh_node) * (2ull * N - 1)));
     CRT_TRY(b->xtri.reserve(48ull * N));
+    CRT_TRY(x->xtri_sorted.reserve(48ull * N));
     CRT_TRY(b->wide.reserve(64ull * N));
     CRT_TRY(b->wide_wt.reserve(64ull * N));
     b->wide4_ready = false;
     b->refit_ready = false;
+    b->node_boxes_stale = false;
     CRT_TRY(b->depth_odd.reserve(N));
     CRT_TRY(b->inv_perm.reserve(4ull * N));
     CRT_TRY(b->codes.reserve(4ull * N));
@@ -401,7 +409,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     // ---- K3: leaf clusters + PLOC iterations
     uint2* d_it = x->iters.as<uint2>();
     crt::launch_leaf_init(d_tris, N, d_models, b->perm.as<uint32_t>(), x->node_box.as<float4>(), x->clus_a.as<float4>(),
-                          b->xtri.as<float4>(), b->inv_perm.as<uint32_t>(), d_it, err, s);
+                          x->xtri_sorted.as<float4>(), d_it, err, s);
+    const crt::LeafOut leaves{x->xtri_sorted.as<float4>(), b->xtri.as<float4>(), b->inv_perm.as<uint32_t>()};
     CRT_CUDA(cudaGetLastError());
     x->it_host.assign(1, make_uint2(N, N));
     uint32_t iters = 0;
@@ -414,8 +423,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         const cudaError_t e = crt::launch_ploc_persistent(
             x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_kids.as<uint4>(), d_it, N,
             static_cast<int>(x->cfg.ploc_radius), lb, tail, ploc_tiles, x->pos.as<uint2>(), b->nodes.as<crt_bvh_node>(),
-            b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), st, tail + 2, tail + 4, err,
-            x->cfg.spin_limit, s);
+            b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves, st, tail + 2, tail + 4,
+            err, x->cfg.spin_limit, s);
         if (e == cudaSuccess) {
             CRT_CUDA(cudaEventRecord(x->ev[3], s));
             uint32_t* hp = static_cast<uint32_t*>(x->pinned);
@@ -484,7 +493,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
 
     // ---- K4: DFS layout, last PLOC iteration first (done above on the persistent path)
     if (N == 1) {
-        crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), s);
+        crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), leaves, s);
     } else if (!laid_out) {
         uint32_t* dfs = x->clus_a.as<uint32_t>();  // the cluster buffers are free after PLOC
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
@@ -492,7 +501,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
                                      x->it_host[k].y, x->it_host[k + 1].y, N, dfs, err, s);
         crt::launch_layout_emit(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(), N, dfs,
                                 b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->wide_wt.as<float4>(),
-                                b->depth_odd.as<uint8_t>(), st, err, s);
+                                b->depth_odd.as<uint8_t>(), leaves, st, err, s);
     }
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->ev[4], s));
@@ -635,6 +644,16 @@ crt_status crt_rebuild(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_
     return build_impl(x, b, tris, n_buffer, n_tris, models, n_models);
 }
 
+// Brings the node array's boxes up to date after a refit (on x's stream).
+static crt_status ensure_node_boxes(crt_ctx* x, const crt_bvh* b) {
+    if (!b->node_boxes_stale) return CRT_OK;
+    crt::launch_refit_nodes(b->wide.as<float4>(), b->refit_dfs.as<uint32_t>(), b->n,
+                            const_cast<crt_bvh_node*>(b->nodes.as<crt_bvh_node>()), x->err.as<uint32_t>(), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    b->node_boxes_stale = false;
+    return CRT_OK;
+}
+
 crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t n_tris, const crt_mesh_model* models,
                      uint32_t n_models) {
     if (!x || !b || !tris) return fail(CRT_ERR_INVALID_ARG, "crt_refit: null argument");
@@ -655,28 +674,29 @@ crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t 
     CRT_TRY(x->refit_state.reserve(sizeof(crt::RefitState)));
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, s));
     if (!b->refit_ready) {
-        CRT_TRY(b->refit_parent.reserve(4ull * (2ull * N - 1)));
-        CRT_TRY(b->refit_rank.reserve(4ull * (2ull * N - 1)));
-        CRT_TRY(b->refit_leaf.reserve(4ull * N));
-        CRT_TRY(b->refit_cnt.reserve(4ull * std::max<size_t>(N - 1, crt::refit_topo_blocks(N))));
+        const size_t n_int = std::max<size_t>(N - 1, 1);
+        CRT_TRY(b->refit_leaf.reserve(16ull * N));
+        CRT_TRY(b->refit_link.reserve(16ull * n_int));
+        CRT_TRY(b->refit_dfs.reserve(4ull * n_int));
+        CRT_TRY(b->refit_cnt.reserve(4ull * std::max<size_t>(n_int, crt::refit_topo_blocks(N))));
         // the counters' buffer holds the per-block counts of the topology pass first
-        crt::launch_refit_topology(b->nodes.as<crt_bvh_node>(), b->inv_perm.as<uint32_t>(), N,
-                                   b->refit_parent.as<uint32_t>(), b->refit_leaf.as<uint32_t>(),
-                                   b->refit_rank.as<uint32_t>(), b->refit_cnt.as<uint32_t>(), x->err.as<uint32_t>(), s);
+        crt::launch_refit_topology(b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), N, b->refit_leaf.as<uint4>(),
+                                   b->refit_link.as<uint4>(), b->refit_dfs.as<uint32_t>(), b->refit_cnt.as<uint32_t>(),
+                                   x->err.as<uint32_t>(), s);
         CRT_CUDA(cudaGetLastError());
         b->refit_ready = true;
     }
     if (N > 1) CRT_CUDA(cudaMemsetAsync(b->refit_cnt.p, 0, 4ull * (N - 1), s));
-    CRT_CUDA(cudaMemsetAsync(x->refit_state.p, 0, sizeof(crt::RefitState), s));
-    crt::launch_refit(d_tris, N, x->models.as<float>(), b->perm.as<uint32_t>(), b->refit_leaf.as<uint32_t>(),
-                      b->refit_parent.as<uint32_t>(), b->refit_rank.as<uint32_t>(), b->refit_cnt.as<uint32_t>(),
-                      b->nodes.as<crt_bvh_node>(), b->xtri.as<float4>(), b->wide.as<float4>(), b->wide_wt.as<float4>(),
-                      x->refit_state.as<crt::RefitState>(), x->err.as<uint32_t>(), s);
+    crt::launch_refit(d_tris, N, x->models.as<float>(), b->refit_leaf.as<uint4>(), b->refit_link.as<uint4>(),
+                      b->refit_cnt.as<uint32_t>(), b->nodes.as<crt_bvh_node>(), b->xtri.as<float4>(),
+                      b->wide.as<float4>(), b->wide_wt.as<float4>(), x->refit_state.as<crt::RefitState>(),
+                      x->err.as<uint32_t>(), s);
     CRT_CUDA(cudaGetLastError());
     float* h_eps = static_cast<float*>(x->pinned);
     CRT_CUDA(cudaMemcpyAsync(h_eps, &x->refit_state.as<crt::RefitState>()->abs_eps, sizeof(float),
                              cudaMemcpyDeviceToHost, s));
     b->wide4_ready = false;
+    b->node_boxes_stale = N > 1;
     const crt_status st = x->check_device_error();
     if (st != CRT_OK) {
         b->refit_ready = false;  // derive the topology again next time
@@ -698,9 +718,9 @@ crt_status crt_bvh_free(crt_bvh* b) {
     if (b->predictor) b->predictor->bvh = nullptr;
     b->codes.release();
     b->perm.release();
-    b->refit_parent.release();
-    b->refit_rank.release();
+    b->refit_link.release();
     b->refit_leaf.release();
+    b->refit_dfs.release();
     b->refit_cnt.release();
     delete b;
     return CRT_OK;
@@ -708,10 +728,16 @@ crt_status crt_bvh_free(crt_bvh* b) {
 
 uint32_t crt_bvh_node_count(const crt_bvh* b) { return (b && b->n) ? 2 * b->n - 1 : 0; }
 uint32_t crt_bvh_triangle_count(const crt_bvh* b) { return b ? b->n : 0; }
-const crt_bvh_node* crt_bvh_nodes_device(const crt_bvh* b) { return b ? b->nodes.as<crt_bvh_node>() : nullptr; }
+const crt_bvh_node* crt_bvh_nodes_device(const crt_bvh* b) {
+    if (!b) return nullptr;
+    if (b->ctx && ensure_node_boxes(b->ctx, b) != CRT_OK) return nullptr;
+    if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+    return b->nodes.as<crt_bvh_node>();
+}
 
 crt_status crt_bvh_copy_nodes(crt_ctx* x, const crt_bvh* b, crt_bvh_node* dst) {
     if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "null context or bvh");
+    CRT_TRY(ensure_node_boxes(x, b));
     return copy_out(x, dst, b->nodes.p, sizeof(crt_bvh_node) * (2ull * b->n - 1));
 }
 crt_status crt_bvh_copy_codes(crt_ctx* x, const crt_bvh* b, uint32_t* dst) {
@@ -960,7 +986,7 @@ crt_status predictor_targets(crt_ctx* x, crt_predictor* pr) {
     CRT_TRY(pr->treelets.reserve(sizeof(crt::Treelet) * 128 + 16));
     CRT_CUDA(cudaMemsetAsync(pr->tri_class.p, crt::pred::kMissClass, b->n, x->stream));
     uint32_t* n_tl = reinterpret_cast<uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
-    crt::pred_treelets(b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->perm.as<uint32_t>(), b->n,
+    crt::pred_treelets(b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->xtri.as<float4>(), b->n,
                        pr->treelets.as<crt::Treelet>(), n_tl, pr->tri_class.as<uint8_t>(), x->stream);
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaMemcpyAsync(&pr->n_treelets, n_tl, 4, cudaMemcpyDeviceToHost, x->stream));
@@ -1193,7 +1219,7 @@ struct crt_batch {
     DevBuf scenes, seg_off, seg_hist, chunks, states, models, err;
     DevBuf codes_a, codes_b, vals_a, vals_b, codes, perm_global, perm_local;
     DevBuf node_box, node_kids, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
-    DevBuf nodes, wide, wide_wt, depth_odd, xtri, inv_perm;
+    DevBuf nodes, wide, wide_wt, depth_odd, xtri, xtri_sorted, inv_perm;
     DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
     bool models_set = false;
     cudaGraphExec_t graph = nullptr;
@@ -1262,8 +1288,8 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
     }
     crt::launch_batch_leaf_init(tris, bt->n_tris, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->models.as<float>(),
                                 bt->perm_global.as<uint32_t>(), bt->perm_local.as<uint32_t>(), bt->node_box.as<float4>(),
-                                bt->clus_a.as<float4>(), bt->xtri.as<float4>(), bt->inv_perm.as<uint32_t>(),
-                                bt->it.as<uint2>(), bt->nodes.as<crt_bvh_node>(), err, s);
+                                bt->clus_a.as<float4>(), bt->xtri_sorted.as<float4>(), bt->xtri.as<float4>(),
+                                bt->inv_perm.as<uint32_t>(), bt->it.as<uint2>(), bt->nodes.as<crt_bvh_node>(), err, s);
     {
         unsigned long long* lb = bt->ploc_lb.as<unsigned long long>();
         uint32_t* tail = reinterpret_cast<uint32_t*>(lb + 2ull * bt->lb_cap);
@@ -1271,7 +1297,9 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
             bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->clus_a.as<float4>(), bt->clus_b.as<float4>(),
             bt->node_box.as<float4>(), bt->node_kids.as<uint4>(), bt->it.as<uint2>(), static_cast<int>(bt->cfg.ploc_radius),
             lb, bt->lb_cap, tail, bt->pf.as<uint2>(), bt->nodes.as<crt_bvh_node>(), bt->wide.as<float4>(),
-            bt->wide_wt.as<float4>(), bt->depth_odd.as<uint8_t>(), tail + 2, bt->max_n + 1, err, x->cfg.spin_limit, s);
+            bt->wide_wt.as<float4>(), bt->depth_odd.as<uint8_t>(),
+            crt::LeafOut{bt->xtri_sorted.as<float4>(), bt->xtri.as<float4>(), bt->inv_perm.as<uint32_t>()}, tail + 2,
+            bt->max_n + 1, err, x->cfg.spin_limit, s);
         if (e != cudaSuccess) return fail(CRT_ERR_UNSUPPORTED, "batched PLOC launch failed: %s", cudaGetErrorString(e));
     }
     CRT_CUDA(cudaGetLastError());
@@ -1399,6 +1427,7 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
     R(bt->wide_wt, 64ull * N);
     R(bt->depth_odd, N);
     R(bt->xtri, 48ull * N);
+    R(bt->xtri_sorted, 48ull * N);
     if (st != CRT_OK) { crt_batch_free(bt); return st; }
     std::vector<uint32_t> seg(n_scenes + 1), segh(256, 0);
     for (uint32_t k = 0; k < n_scenes; ++k) { seg[k] = hs[k].tri_off; segh[k] = hs[k].n_tris; }
@@ -1425,7 +1454,7 @@ crt_status crt_batch_free(crt_batch* bt) {
                       &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
                       &bt->perm_local, &bt->node_box, &bt->node_kids, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
                       &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->wide_wt, &bt->depth_odd, &bt->xtri, &bt->ray_order, &bt->ray_order_scratch,
-                      &bt->inv_perm};
+                      &bt->inv_perm, &bt->xtri_sorted};
     for (DevBuf* b : bufs) b->release();
     delete bt;
     return CRT_OK;
@@ -1637,6 +1666,7 @@ crt_status shade_setup(crt_ctx* x, const crt_bvh* b, const crt_shading* sh, crt:
     sp->bvh_depth = sh->bvh_depth;
     sp->inv_perm = b->inv_perm.as<uint32_t>();
     sp->n_tris = b->n;
+    if (sh->flags & CRT_SHADE_BVH) CRT_TRY(ensure_node_boxes(x, b));  // the box display walks the node array
     if (sh->n_models) {
         const void* d = nullptr;
         CRT_TRY(stage_in(x, x->shade_models, sh->models, sizeof(crt_mesh_model) * sh->n_models, &d));

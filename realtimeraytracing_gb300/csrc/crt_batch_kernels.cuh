@@ -196,8 +196,9 @@ __global__ void __launch_bounds__(256) batch_leaf_init_kernel(const crt_triangle
                                                               const float* __restrict__ models,
                                                               const uint32_t* __restrict__ perm_global,
                                                               uint32_t* __restrict__ perm_local, float4* __restrict__ node_box,
-                                                              float4* __restrict__ clusters, float4* __restrict__ xtri,
-                                                              uint32_t* __restrict__ inv_perm, uint2* __restrict__ it,
+                                                              float4* __restrict__ clusters,
+                                                              float4* __restrict__ xtri_sorted, float4* __restrict__ xtri,
+                                                              uint32_t* __restrict__ leaf_of_tri, uint2* __restrict__ it,
                                                               crt_bvh_node* __restrict__ nodes, uint32_t* err) {
     __shared__ uint32_t s_off[kMaxBatchScenes];
     for (uint32_t k = threadIdx.x; k < n_scenes; k += 256) s_off[k] = scenes[k].tri_off;
@@ -215,7 +216,6 @@ __global__ void __launch_bounds__(256) batch_leaf_init_kernel(const crt_triangle
         scenes[s].iters = sc.n_tris > 1 ? 0u : 1u;   // one-triangle scenes need no iteration
     }
     perm_local[i] = tl;
-    inv_perm[sc.tri_off + tl] = li;
     const TriRec t = load_tri(tris, tg);
     const float* M = models + 16 * (t.model & (kMaxModels - 1));
     const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
@@ -231,10 +231,14 @@ __global__ void __launch_bounds__(256) batch_leaf_init_kernel(const crt_triangle
     node_box[nb + 1] = make_float4(mx.x, mx.y, mx.z, 0.f);
     clusters[2 * static_cast<size_t>(i)] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(li));
     clusters[2 * static_cast<size_t>(i) + 1] = make_float4(mx.x, mx.y, mx.z, __uint_as_float(1u));
-    xtri[3 * static_cast<size_t>(i) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(tl));
-    xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
-    xtri[3 * static_cast<size_t>(i) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
+    // sorted order; the layout moves them into tree order (a one-triangle
+    // scene's single leaf is in both orders at once)
+    float4* xo = (sc.n_tris == 1 ? xtri : xtri_sorted) + 3 * static_cast<size_t>(i);
+    xo[0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(tl));
+    xo[1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
+    xo[2] = make_float4(p2.x, p2.y, p2.z, 0.f);
     if (sc.n_tris == 1) {
+        leaf_of_tri[sc.tri_off] = 0u;
         float4* o = reinterpret_cast<float4*>(nodes + sc.node_off);
         o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
         o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
@@ -252,8 +256,8 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
                                                            float4* node_box, uint4* node_kids, uint2* it, int R,
                                                            unsigned long long* lookback, uint32_t lb_cap, uint32_t* tickets,
                                                            uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
-                                                           uint8_t* depth_odd, unsigned int* bar, uint32_t max_iters,
-                                                           uint32_t* err, uint32_t spin_limit) {
+                                                           uint8_t* depth_odd, LeafOut lv, unsigned int* bar,
+                                                           uint32_t max_iters, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile_pre[kMaxBatchScenes + 1];
     __shared__ uint32_t s_n[kMaxBatchScenes];
@@ -369,10 +373,12 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
             if (s_tile_pre[mid] <= q) lo = mid; else hi = mid - 1;
         }
         const BatchScene B = scenes[lo];
+        const LeafOut slv{lv.xtri_sorted + 3 * static_cast<size_t>(B.tri_off), lv.xtri + 3 * static_cast<size_t>(B.tri_off),
+                          lv.leaf_of_tri + B.tri_off};
         layout_emit(q - s_tile_pre[lo], node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off,
                     pf + B.tri_off, B.n_tris, dfs + B.node_off, nodes + B.node_off,
                     wide + 4 * static_cast<size_t>(B.wide_off), wide_wt + 4 * static_cast<size_t>(B.wide_off),
-                    depth_odd + B.wide_off, B.abs_eps, err);
+                    depth_odd + B.wide_off, slv, B.abs_eps, err);
     }
 }
 
@@ -412,22 +418,24 @@ void launch_batch_morton(const crt_triangle* tris, const void* chunks, uint32_t 
 
 void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchScene* scenes, uint32_t n_scenes,
                             const float* models, const uint32_t* perm_global, uint32_t* perm_local, float4* node_box,
-                            float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, crt_bvh_node* nodes,
+                            float4* clusters, float4* xtri_sorted, float4* xtri, uint32_t* leaf_of_tri, uint2* it,
+                            crt_bvh_node* nodes,
                             uint32_t* err, cudaStream_t s) {
     batch_leaf_init_kernel<<<(n_total + 255) / 256, 256, 0, s>>>(tris, n_total, scenes, n_scenes, models, perm_global,
-                                                                 perm_local, node_box, clusters, xtri, inv_perm, it, nodes,
+                                                                 perm_local, node_box, clusters, xtri_sorted, xtri,
+                                                                 leaf_of_tri, it, nodes,
                                                                  err);
 }
 
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
                               uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
-                              uint8_t* depth_odd, unsigned int* bar, uint32_t max_iters, uint32_t* err,
+                              uint8_t* depth_odd, LeafOut lv, unsigned int* bar, uint32_t max_iters, uint32_t* err,
                               uint32_t spin_limit, cudaStream_t s) {
     const int grid = batch_ploc_grid();
     if (grid <= 0) return cudaErrorNotSupported;
     void* args[] = {&scenes, &n_scenes, &ca, &cb, &node_box, &node_kids, &it, &radius, &lookback, &lb_cap, &tickets,
-                    &pf, &nodes, &wide, &wide_wt, &depth_odd, &bar, &max_iters, &err, &spin_limit};
+                    &pf, &nodes, &wide, &wide_wt, &depth_odd, &lv, &bar, &max_iters, &err, &spin_limit};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(batch_ploc_kernel<kPlocSpan, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }

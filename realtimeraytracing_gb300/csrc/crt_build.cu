@@ -375,19 +375,18 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
 // ==================================================== leaf clusters
 // plocPreprocessing (bvh.cpp:26-46): sorted position i holds the leaf of
 // triangle perm[i] with AABB::buildFromTriangle's box (bvh.cpp:383-399).
-// Also stores the model-transformed vertices the traversal tests against.
+// Also stores the model-transformed vertices the traversal tests against,
+// in sorted order (the layout moves them into tree order).
 __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __restrict__ tris, uint32_t n,
                                                         const float* __restrict__ models,
                                                         const uint32_t* __restrict__ perm,
                                                         float4* __restrict__ node_box, float4* __restrict__ clusters,
-                                                        float4* __restrict__ xtri, uint32_t* __restrict__ inv_perm,
-                                                        uint2* it, uint32_t* err) {
+                                                        float4* __restrict__ xtri, uint2* it, uint32_t* err) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) it[0] = make_uint2(n, n);
     if (i >= n) return;
     const uint32_t ti = perm[i];
     if (ti >= n) { raise_corrupt(err, 1, i, ti); return; }
-    inv_perm[ti] = i;
     const TriRec t = load_tri(tris, ti);
     const float* M = models + 16 * (t.model & (kMaxModels - 1));
     const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
@@ -406,8 +405,8 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
     mx.w = __uint_as_float(1u);
     clusters[2 * static_cast<size_t>(i)] = mn;
     clusters[2 * static_cast<size_t>(i) + 1] = mx;
-    // leaf order (= left-to-right order of the final tree): triangle id in
-    // the first .w, model id in the second (read by the shading pass)
+    // sorted order: triangle id in the first .w, model id in the second
+    // (read by the shading pass)
     xtri[3 * static_cast<size_t>(i) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(ti));
     xtri[3 * static_cast<size_t>(i) + 1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
     xtri[3 * static_cast<size_t>(i) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
@@ -703,9 +702,13 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 // per internal node holding both children's boxes and references, indexed by
 // the node's rank among internal nodes in DFS order (position minus the
 // leaves before it, i.e. minus its first leaf).  Leaves are referenced by
-// their sorted position, which is also their left-to-right order in the tree
-// (PLOC merges keep Morton order), so the traversal's triangles are stored
-// in that order.
+// their position in the tree's left-to-right leaf order (the number of
+// leaves before them in DFS order) — which is not their sorted position:
+// PLOC merges clusters that are not adjacent in Morton order, so subtrees
+// interleave there — and the parent of each leaf moves that leaf's
+// transformed triangle into that order.  The traversal's tie rule (equal t:
+// the leaf later in DFS order, which the shader visits first) and every
+// subtree's leaves forming one contiguous range rest on this order.
 __device__ __forceinline__ uint2 layout_place(uint32_t X, const uint2* __restrict__ pf, uint32_t N) {
     // (DFS position, first leaf below | depth parity << 31) of X; the root sits at (0, 0)
     return (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
@@ -735,7 +738,8 @@ __device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict
                                             const uint4* __restrict__ node_kids, const uint2* __restrict__ pf,
                                             uint32_t N, const uint32_t* __restrict__ dfs, crt_bvh_node* __restrict__ out,
                                             float4* __restrict__ wide, float4* __restrict__ wide_wt,
-                                            uint8_t* __restrict__ depth_odd, float grow, uint32_t* err) {
+                                            uint8_t* __restrict__ depth_odd, const LeafOut& lv, float grow,
+                                            uint32_t* err) {
     const uint32_t X = __ldcg(dfs + p);
     if (X >= 2 * N - 1) { raise_corrupt(err, 5, p, X); return; }
     const float4 mn = __ldcg(node_box + 2 * static_cast<size_t>(X)), mx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
@@ -760,8 +764,20 @@ __device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict
     for (int c = 0; c < 2; ++c) {
         cmn[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]));
         cmx[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]) + 1);
-        cref[c] = (ch[c] < N) ? (kLeafRef | ch[c])  // leaf: its sorted position
+        cref[c] = (ch[c] < N) ? (kLeafRef | cf[c])  // leaf: its position in tree order
                               : (cp[c] - cf[c]);    // internal: its rank among internal nodes in DFS order
+        if (ch[c] < N) {  // move the leaf's triangle from sorted to tree order
+            if (cf[c] >= N) { raise_corrupt(err, 6, p, cf[c]); continue; }
+            const float4* src = lv.xtri_sorted + 3 * static_cast<size_t>(ch[c]);
+            float4* dst = lv.xtri + 3 * static_cast<size_t>(cf[c]);
+            const float4 t0 = __ldcg(src), t1 = __ldcg(src + 1), t2 = __ldcg(src + 2);
+            dst[0] = t0;
+            dst[1] = t1;
+            dst[2] = t2;
+            const uint32_t ti = __float_as_uint(t0.w);
+            if (ti < N) lv.leaf_of_tri[ti] = cf[c];
+            else raise_corrupt(err, 6, p, ti);
+        }
     }
     if (depth_odd) depth_odd[p - f] = static_cast<uint8_t>(odd);
     float4* w = wide + 4 * static_cast<size_t>(p - f);
@@ -789,11 +805,11 @@ __global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restri
                                                           const uint2* __restrict__ pf, uint32_t N,
                                                           const uint32_t* __restrict__ dfs, crt_bvh_node* __restrict__ out,
                                                           float4* __restrict__ wide, float4* __restrict__ wide_wt,
-                                                          uint8_t* __restrict__ depth_odd,
+                                                          uint8_t* __restrict__ depth_odd, LeafOut lv,
                                                           const SceneState* __restrict__ st, uint32_t* err) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= 2 * N - 1) return;
-    layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, st->abs_eps, err);
+    layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, st->abs_eps, err);
 }
 
 // ================================== K3+K4 fused: one persistent launch
@@ -827,7 +843,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
                                                                 int R, unsigned long long* lookback, uint32_t* tickets,
                                                                 uint32_t n_tiles_cap, uint2* pf, crt_bvh_node* out,
                                                                 float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                                                                const SceneState* st, unsigned int* bar,
+                                                                LeafOut lv, const SceneState* st, unsigned int* bar,
                                                                 uint32_t* iters_out, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile;
@@ -871,17 +887,19 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     }
     const float grow = st->abs_eps;
     for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
-        layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, grow, err);
+        layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, grow, err);
     __syncthreads();
     if (threadIdx.x == 0 && atomicAdd(iters_out + 1, 1u) + 1u == gridDim.x) stamp[2] = global_ns();
 }
 
-__global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out) {
+__global__ void single_leaf_kernel(const float4* __restrict__ node_box, crt_bvh_node* __restrict__ out, LeafOut lv) {
     const float4 mn = node_box[0], mx = node_box[1];
     float4* o = reinterpret_cast<float4*>(out);
     o[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
     o[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
     reinterpret_cast<uint4*>(o)[2] = make_uint4(__float_as_uint(mn.w), 0u, 0u, 0u);
+    for (int k = 0; k < 3; ++k) lv.xtri[k] = lv.xtri_sorted[k];
+    lv.leaf_of_tri[0] = 0u;
 }
 
 // ========================================== K4b: 4-wide traversal nodes
@@ -977,9 +995,8 @@ void launch_onesweep_segments(const uint32_t* keys_in, const uint32_t* vals_in, 
 }
 
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
-                      float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, uint32_t* err, cudaStream_t s) {
-    leaf_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(tris, n, models, perm, node_box, clusters, xtri, inv_perm, it,
-                                                     err);
+                      float4* clusters, float4* xtri_sorted, uint2* it, uint32_t* err, cudaStream_t s) {
+    leaf_init_kernel<<<(n + 255) / 256, 256, 0, s>>>(tris, n, models, perm, node_box, clusters, xtri_sorted, it, err);
 }
 
 void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint4* node_kids, uint2* it,
@@ -1000,10 +1017,10 @@ void launch_layout_level(const uint4* node_kids, uint2* pf, uint32_t id_begin,
 
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
                         const uint32_t* dfs, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                        const SceneState* st, uint32_t* err, cudaStream_t s) {
+                        LeafOut lv, const SceneState* st, uint32_t* err, cudaStream_t s) {
     const uint32_t cnt = 2 * N - 1;
     layout_emit_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd,
-                                                         st, err);
+                                                         lv, st, err);
 }
 
 int ploc_persistent_grid() {
@@ -1027,18 +1044,18 @@ int ploc_persistent_grid() {
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
                                    uint2* pf, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                                   const SceneState* st, unsigned int* bar, uint32_t* iters_out, uint32_t* err,
-                                   uint32_t spin_limit, cudaStream_t s) {
+                                   LeafOut lv, const SceneState* st, unsigned int* bar, uint32_t* iters_out,
+                                   uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
     const int grid = ploc_persistent_grid();
     if (grid <= 0) return cudaErrorNotSupported;
     void* args[] = {&ca, &cb, &node_box, &node_kids, &it, &N, &radius, &lookback, &tickets, &n_tiles_cap, &pf, &out,
-                    &wide, &wide_wt, &depth_odd, &st, &bar, &iters_out, &err, &spin_limit};
+                    &wide, &wide_wt, &depth_odd, &lv, &st, &bar, &iters_out, &err, &spin_limit};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(ploc_persistent_kernel<kPlocSpan, 256, kPlocMaxRadius>),
                                        dim3(grid), dim3(256), args, 0, s);
 }
 
-void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s) {
-    single_leaf_kernel<<<1, 1, 0, s>>>(node_box, out);
+void launch_single_leaf(const float4* node_box, crt_bvh_node* out, LeafOut lv, cudaStream_t s) {
+    single_leaf_kernel<<<1, 1, 0, s>>>(node_box, out, lv);
 }
 
 }  // namespace crt

@@ -1,5 +1,6 @@
-// Internal interface between the build kernels (crt_build.cu), the trace
-// kernels (crt_trace.cu) and the C ABI (crt_api.cu).
+// Internal interface between the build kernels (crt_build.cu), the refit
+// (crt_refit.cu), the trace and frame kernels (crt_trace.cu, crt_frame.cu)
+// and the C ABI (crt_api.cu).
 #pragma once
 
 #include <cstdint>
@@ -61,12 +62,22 @@ void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t*
 void launch_onesweep_segments(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                               uint32_t n, const uint32_t* seg_off, uint32_t n_seg, const uint32_t* seg_hist,
                               uint32_t* lookback, uint32_t* ticket, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
+// xtri_sorted: the leaves' transformed triangles in sorted (Morton) order;
+// the layout moves them into tree order.
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,
-                      float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, uint32_t* err, cudaStream_t s);
+                      float4* clusters, float4* xtri_sorted, uint2* it, uint32_t* err, cudaStream_t s);
 void launch_ploc_iteration(const float4* cin, float4* cout, float4* node_box, uint4* node_kids, uint2* it,
                            int iter, uint32_t N, int radius, uint32_t n_upper,
                            unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap, uint32_t* err,
                            uint32_t spin_limit, cudaStream_t s);
+// Leaf records moved by the layout: leaf L (sorted position) goes to its
+// position in the tree's left-to-right (DFS) leaf order, leaf_of_tri
+// receives triangle -> that position.
+struct LeafOut {
+    const float4* xtri_sorted;
+    float4* xtri;
+    uint32_t* leaf_of_tri;
+};
 // DFS layout as separate launches: one top-down level (nodes [id_begin,
 // id_end)) recording dfs[position] = node, then the emit pass over all
 // positions.
@@ -74,36 +85,39 @@ void launch_layout_level(const uint4* node_kids, uint2* pf, uint32_t id_begin,
                          uint32_t id_end, uint32_t N, uint32_t* dfs, uint32_t* err, cudaStream_t s);
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
                         const uint32_t* dfs, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                        const SceneState* st, uint32_t* err, cudaStream_t s);
+                        LeafOut leaves, const SceneState* st, uint32_t* err, cudaStream_t s);
 void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s);
-void launch_single_leaf(const float4* node_box, crt_bvh_node* out, cudaStream_t s);
+void launch_single_leaf(const float4* node_box, crt_bvh_node* out, LeafOut leaves, cudaStream_t s);
 // All PLOC iterations and the DFS layout in one cooperative launch; returns
 // cudaErrorNotSupported when a cooperative launch is unavailable.
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
                                    uint2* pf, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                                   const SceneState* st, unsigned int* bar, uint32_t* iters_out, uint32_t* err,
-                                   uint32_t spin_limit, cudaStream_t s);
+                                   LeafOut leaves, const SceneState* st, unsigned int* bar, uint32_t* iters_out,
+                                   uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 
-// Refit (crt_refit.cu).  State zeroed before each refit: the scene box of
-// the moved triangles as order-preserving keys, and the resulting slack.
+// Refit (crt_refit.cu).  The slack of the refit tree's root box goes to
+// abs_eps for the host.
 struct RefitState {
-    unsigned int key_max[3];
-    unsigned int key_min_inv[3];  // complemented keys, so that atomicMax finds the minimum
     float abs_eps;
-    unsigned int pad;
+    unsigned int pad[3];
 };
 uint32_t refit_topo_blocks(uint32_t N);
-// Once per build: parent of every node (DFS index), DFS index of every leaf,
-// traversal-node rank of every internal node.  block_count: refit_topo_blocks(N) words.
-void launch_refit_topology(const crt_bvh_node* nodes, const uint32_t* inv_perm, uint32_t N, uint32_t* parent,
-                           uint32_t* leaf_dfs, uint32_t* rank, uint32_t* block_count, uint32_t* err, cudaStream_t s);
-// New leaf records and every box of the node array and both traversal node
-// arrays; cnt (N - 1 words) and st zeroed before.
-void launch_refit(const crt_triangle* tris, uint32_t N, const float* models, const uint32_t* perm,
-                  const uint32_t* leaf_dfs, const uint32_t* parent, const uint32_t* rank, uint32_t* cnt,
-                  crt_bvh_node* nodes, float4* xtri, float4* wide, float4* wide_wt, RefitState* st, uint32_t* err,
-                  cudaStream_t s);
+// Once per build: links to the parent (parent's rank << 1 | child slot,
+// parent's leaf range [first, end)) for every leaf (leaf_link, by place in
+// the tree's leaf order, N entries) and internal node (int_link, by rank,
+// N - 1 entries), and every internal node's DFS position (int_dfs).
+// block_count: refit_topo_blocks(N) words of scratch.
+void launch_refit_topology(const crt_bvh_node* nodes, const float4* wide, uint32_t N, uint4* leaf_link, uint4* int_link,
+                           uint32_t* int_dfs, uint32_t* block_count, uint32_t* err, cudaStream_t s);
+// New leaf records, both traversal node arrays and the root box of the node
+// array; cnt (N - 1 words) zeroed before.
+void launch_refit(const crt_triangle* tris, uint32_t N, const float* models, const uint4* leaf_link,
+                  const uint4* int_link, uint32_t* cnt, crt_bvh_node* nodes, float4* xtri, float4* wide,
+                  float4* wide_wt, RefitState* st, uint32_t* err, cudaStream_t s);
+// The other boxes of the node array, from the traversal nodes.
+void launch_refit_nodes(const float4* wide, const uint32_t* int_dfs, uint32_t N, crt_bvh_node* nodes, uint32_t* err,
+                        cudaStream_t s);
 
 // Trace side (crt_trace.cu).
 struct TraceParams {
@@ -111,7 +125,7 @@ struct TraceParams {
     const float4* wide;      // 64-B traversal nodes: child boxes + child references (watertight
                              // traces: boxes already grown by abs_eps)
     const float4* wide4;     // 128-B 4-wide traversal nodes (even-depth internal nodes)
-    const float4* xtri;      // 3 float4 per leaf (sorted order): transformed p0 | tri id, p1, p2
+    const float4* xtri;      // 3 float4 per leaf (tree order): transformed p0 | tri id, p1 | model id, p2
     const crt_ray* rays;
     crt_hit* hits;
     uint32_t n_rays;
@@ -140,7 +154,7 @@ struct ShadeParams {
     uint32_t n_materials = 0;
     uint32_t flags = 0;                   // CRT_SHADE_*
     uint32_t bvh_depth = 0;
-    const uint32_t* inv_perm = nullptr;   // triangle -> leaf position (its xtri record holds the model id)
+    const uint32_t* inv_perm = nullptr;   // triangle -> leaf position in tree order (its xtri record holds the model id)
     uint32_t n_tris = 0;
     float4* image = nullptr;              // RGBA32F texels
 };
@@ -190,12 +204,12 @@ void launch_batch_morton(const crt_triangle* tris, const void* chunks, uint32_t 
                          const void* states, uint32_t* codes, uint32_t* hist, int bits, cudaStream_t s);
 void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchScene* scenes, uint32_t n_scenes,
                             const float* models, const uint32_t* perm_global, uint32_t* perm_local, float4* node_box,
-                            float4* clusters, float4* xtri, uint32_t* inv_perm, uint2* it, crt_bvh_node* nodes,
-                            uint32_t* err, cudaStream_t s);
+                            float4* clusters, float4* xtri_sorted, float4* xtri, uint32_t* leaf_of_tri, uint2* it,
+                            crt_bvh_node* nodes, uint32_t* err, cudaStream_t s);
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
                               uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
-                              uint8_t* depth_odd, unsigned int* bar, uint32_t max_iters, uint32_t* err,
+                              uint8_t* depth_odd, LeafOut leaves, unsigned int* bar, uint32_t max_iters, uint32_t* err,
                               uint32_t spin_limit, cudaStream_t s);
 // Sets the message crt_last_error_string() returns on the calling thread.
 void set_last_error(const char* msg);

@@ -104,6 +104,15 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Atomic add with acquire-release semantics at gpu scope: the caller's
+// earlier writes are visible to a thread that later observes this add, and
+// writes released before any add this one observes are visible afterwards.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel_u32(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 // Nanoseconds of the GPU's global timer.
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;

@@ -597,8 +597,9 @@ __global__ void treelet_cut_kernel(const crt_bvh_node* nodes, const float4* wide
     *n_out = cnt;
 }
 
-// Class of every triangle: the treelet whose leaf range holds its leaf.
-__global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, const uint32_t* perm, uint32_t n_leaves,
+// Class of every triangle: the treelet whose leaf range (in the tree's
+// left-to-right leaf order, the order of the leaf records) holds its leaf.
+__global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, const float4* xtri, uint32_t n_leaves,
                                      uint8_t* tri_class) {
     const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
     if (L >= n_leaves) return;
@@ -608,7 +609,7 @@ __global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, co
         const int mid = (lo + hi + 1) / 2;
         if (tl[mid].first <= L) lo = mid; else hi = mid - 1;
     }
-    const uint32_t tri = perm[L];
+    const uint32_t tri = __float_as_uint(xtri[3 * static_cast<size_t>(L)].w);
     if (tri < n_leaves) tri_class[tri] = static_cast<uint8_t>(lo);
 }
 
@@ -815,10 +816,10 @@ void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s) {
     pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
 }
 
-void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t* perm, uint32_t n_leaves,
+void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const float4* xtri, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s) {
     pred::treelet_cut_kernel<<<1, 1, 0, s>>>(nodes, wide, n_leaves, tl, n_tl);
-    pred::treelet_label_kernel<<<(n_leaves + 255) / 256, 256, 0, s>>>(tl, n_tl, perm, n_leaves, tri_class);
+    pred::treelet_label_kernel<<<(n_leaves + 255) / 256, 256, 0, s>>>(tl, n_tl, xtri, n_leaves, tri_class);
 }
 
 size_t bounce_scratch_bytes(uint32_t n_prim) {

@@ -83,7 +83,7 @@ void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s);
 size_t pred_order_scratch_bytes(uint32_t n);
 void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes, uint32_t n, uint32_t* order,
                 void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
-void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const uint32_t* perm, uint32_t n_leaves,
+void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const float4* xtri, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
 size_t bounce_scratch_bytes(uint32_t n_prim);
 void launch_bounce(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,

@@ -8,14 +8,21 @@
 // reproduces the built node array bit for bit.  Compiled with -fmad=false.
 //
 // Kernels:
-//   refit_topo / refit_scan / refit_rank  once per build: parent of every
-//       node, DFS index of every leaf, and the rank of every internal node
-//       among internal nodes in DFS order (its traversal-node index);
-//   refit_leaves  new transformed triangles (traversal leaf records) and the
-//       scene box, for the traversal slack;
-//   refit_up      one thread per leaf walks up; at each parent the second
-//       child to arrive (an atomic counter per node) merges both boxes and
-//       continues, so every node is finished once, after both children.
+//   refit_count / refit_scan / refit_link  once per build: for every leaf
+//       (indexed by its place in the tree's left-to-right leaf order) and
+//       every internal node (indexed by its rank among internal nodes in DFS
+//       order, which is also its traversal-node index) a link to its parent:
+//       the parent's rank, which child it is, and the parent's leaf range;
+//       plus the DFS position of every internal node;
+//   refit_up      one thread per leaf: the moved triangle (traversal leaf
+//       record) and its box, then up the tree: at each parent the two
+//       children count in and the second to arrive merges both boxes, writes
+//       the parent's traversal node and goes on, so every node is finished
+//       once, after both children;
+//   refit_grow    the watertight copy of the traversal nodes, every box grown
+//       by the slack of the new root box (coalesced, one float4 per thread);
+//   refit_nodes   on demand (copy-out, box display): the boxes of the
+//       reference-layout node array from the traversal nodes.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -26,33 +33,15 @@ namespace crt {
 
 constexpr uint32_t kNoParent = 0xFFFFFFFFu;
 
-__device__ __forceinline__ float from_ordered_key(uint32_t k) {
-    return __uint_as_float((k & 0x80000000u) ? (k ^ 0x80000000u) : ~k);
+__device__ __forceinline__ bool is_internal_node(const crt_bvh_node* nodes, uint32_t d) {
+    const uint4 k = __ldg(reinterpret_cast<const uint4*>(nodes + d) + 2);  // tri, left, right, pad
+    return (k.y | k.z) != 0u;
 }
 
-__global__ void __launch_bounds__(256) refit_topo_kernel(const crt_bvh_node* __restrict__ nodes, uint32_t n_nodes,
-                                                         const uint32_t* __restrict__ inv_perm, uint32_t N,
-                                                         uint32_t* __restrict__ parent, uint32_t* __restrict__ leaf_dfs,
-                                                         uint32_t* __restrict__ block_count, uint32_t* err) {
+__global__ void __launch_bounds__(256) refit_count_kernel(const crt_bvh_node* __restrict__ nodes, uint32_t n_nodes,
+                                                          uint32_t* __restrict__ block_count) {
     const uint32_t d = blockIdx.x * 256 + threadIdx.x;
-    bool internal = false;
-    if (d < n_nodes) {
-        const uint4 k = __ldg(reinterpret_cast<const uint4*>(nodes + d) + 2);  // tri, left, right, pad
-        internal = (k.y | k.z) != 0u;
-        if (d == 0) parent[0] = kNoParent;
-        if (internal) {
-            // DFS pre-order: the left child follows its parent
-            if (k.y != d + 1 || k.z <= k.y || k.z >= n_nodes) raise_corrupt(err, 12, d, k.z);
-            else {
-                parent[k.y] = d;
-                parent[k.z] = d;
-            }
-        } else {
-            const uint32_t L = k.x < N ? __ldg(inv_perm + k.x) : 0xFFFFFFFFu;
-            if (L >= N) raise_corrupt(err, 12, d, k.x);
-            else leaf_dfs[L] = d;
-        }
-    }
+    const bool internal = d < n_nodes && is_internal_node(nodes, d);
     const uint32_t c = static_cast<uint32_t>(__syncthreads_count(internal));
     if (threadIdx.x == 0) block_count[blockIdx.x] = c;
 }
@@ -93,153 +82,241 @@ __global__ void __launch_bounds__(1024) refit_scan_kernel(uint32_t* __restrict__
     }
 }
 
-__global__ void __launch_bounds__(256) refit_rank_kernel(const crt_bvh_node* __restrict__ nodes, uint32_t n_nodes,
+// For internal node d of rank k: its first leaf is the number of leaves
+// before it in DFS order (d - k) and its children's leaf counts are in its
+// traversal node; its left child sits at d + 1 (rank k + 1 if internal, leaf
+// index first if a leaf), its right child at the node's right index (rank
+// right - (first + left count) if internal, leaf index first + left count if
+// a leaf).  Links are (parent rank << 1 | child slot, parent's first leaf,
+// parent's leaf end, 0); the root's is (kNoParent, 0, N, 0).
+__global__ void __launch_bounds__(256) refit_link_kernel(const crt_bvh_node* __restrict__ nodes, uint32_t n_nodes,
                                                          const uint32_t* __restrict__ block_offset,
-                                                         uint32_t* __restrict__ rank) {
+                                                         const float4* __restrict__ wide, uint4* __restrict__ leaf_link,
+                                                         uint4* __restrict__ int_link, uint32_t* __restrict__ int_dfs,
+                                                         uint32_t* err) {
     __shared__ uint32_t s_w[8];
     const uint32_t d = blockIdx.x * 256 + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    bool internal = false;
-    if (d < n_nodes) {
-        const uint4 k = __ldg(reinterpret_cast<const uint4*>(nodes + d) + 2);
-        internal = (k.y | k.z) != 0u;
-    }
+    uint4 k = make_uint4(0u, 0u, 0u, 0u);
+    if (d < n_nodes) k = __ldg(reinterpret_cast<const uint4*>(nodes + d) + 2);
+    const bool internal = d < n_nodes && (k.y | k.z) != 0u;
     const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, internal);
     if (lane == 0) s_w[warp] = __popc(ballot);
     __syncthreads();
-    uint32_t before = __ldg(block_offset + blockIdx.x) + __popc(ballot & ((1u << lane) - 1u));
-    for (uint32_t w = 0; w < warp; ++w) before += s_w[w];
-    if (d < n_nodes) rank[d] = internal ? before : 0xFFFFFFFFu;
-}
-
-// New leaf records (sorted order: transformed p0 | triangle id, p1 | model
-// id, p2) and the scene box of the moved triangles.
-__global__ void __launch_bounds__(256) refit_leaves_kernel(const crt_triangle* __restrict__ tris, uint32_t N,
-                                                           const float* __restrict__ models,
-                                                           const uint32_t* __restrict__ perm, float4* __restrict__ xtri,
-                                                           RefitState* st, uint32_t* err) {
-    uint32_t kmax[3] = {0u, 0u, 0u}, kmin_inv[3] = {0u, 0u, 0u};  // max of keys, max of complemented keys
-    bool bad = false;
-    for (uint32_t L = blockIdx.x * blockDim.x + threadIdx.x; L < N; L += gridDim.x * blockDim.x) {
-        const uint32_t ti = __ldg(perm + L);
-        if (ti >= N) { raise_corrupt(err, 13, L, ti); continue; }
-        const TriRec t = load_tri(tris, ti);
-        bad |= t.model >= kMaxModels;
-        const float* M = models + 16 * (t.model & (kMaxModels - 1));
-        const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
-        xtri[3 * static_cast<size_t>(L) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(ti));
-        xtri[3 * static_cast<size_t>(L) + 1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
-        xtri[3 * static_cast<size_t>(L) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
-        const float lo[3] = {min_std(p0.x, min_std(p1.x, p2.x)), min_std(p0.y, min_std(p1.y, p2.y)),
-                             min_std(p0.z, min_std(p1.z, p2.z))};
-        const float hi[3] = {max_std(p0.x, max_std(p1.x, p2.x)), max_std(p0.y, max_std(p1.y, p2.y)),
-                             max_std(p0.z, max_std(p1.z, p2.z))};
+    uint32_t rank = __ldg(block_offset + blockIdx.x) + __popc(ballot & ((1u << lane) - 1u));
+    for (uint32_t w = 0; w < warp; ++w) rank += s_w[w];
+    const uint32_t N = (n_nodes + 1) / 2;
+    if (d == 0) {
+        if (internal) int_link[0] = make_uint4(kNoParent, 0u, N, 0u);
+        else leaf_link[0] = make_uint4(kNoParent, 0u, N, 0u);
+    }
+    if (!internal) return;
+    // DFS pre-order: the left child follows its parent
+    if (k.y != d + 1 || k.z <= k.y || k.z >= n_nodes || rank >= N - 1 || d < rank) {
+        raise_corrupt(err, 12, d, k.z);
+        return;
+    }
+    const uint32_t first = d - rank;
+    const uint32_t lca = __float_as_uint(__ldg(wide + 4 * static_cast<size_t>(rank) + 2).w);
+    const uint32_t lcb = __float_as_uint(__ldg(wide + 4 * static_cast<size_t>(rank) + 3).w);
+    if (first >= N || lca == 0u || lcb == 0u || static_cast<uint64_t>(first) + lca + lcb > N) {
+        raise_corrupt(err, 12, d, lca);
+        return;
+    }
+    int_dfs[rank] = d;
+    const uint32_t end = first + lca + lcb;
+    const uint32_t ch[2] = {k.y, k.z}, chf[2] = {first, first + lca};
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (hi[a] == hi[a]) kmax[a] = max(kmax[a], ordered_key(hi[a]));
-            if (lo[a] == lo[a]) kmin_inv[a] = max(kmin_inv[a], ~ordered_key(lo[a]));
+    for (uint32_t slot = 0; slot < 2; ++slot) {
+        const uint4 l = make_uint4((rank << 1) | slot, first, end, 0u);
+        if (is_internal_node(nodes, ch[slot])) {
+            if (ch[slot] < chf[slot] || ch[slot] - chf[slot] >= N - 1) { raise_corrupt(err, 12, d, ch[slot]); continue; }
+            int_link[ch[slot] - chf[slot]] = l;  // the child's rank
+        } else {
+            leaf_link[chf[slot]] = l;
         }
     }
-    if (bad) raise_error(err, kDevBadModel);
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        for (int o = 16; o > 0; o >>= 1) {
-            kmax[a] = max(kmax[a], __shfl_xor_sync(0xFFFFFFFFu, kmax[a], o));
-            kmin_inv[a] = max(kmin_inv[a], __shfl_xor_sync(0xFFFFFFFFu, kmin_inv[a], o));
-        }
-    if ((threadIdx.x & 31u) == 0u)
-        for (int a = 0; a < 3; ++a) {
-            if (kmax[a]) atomicMax(&st->key_max[a], kmax[a]);
-            if (kmin_inv[a]) atomicMax(&st->key_min_inv[a], kmin_inv[a]);
-        }
 }
 
-__global__ void __launch_bounds__(256) refit_up_kernel(const float4* __restrict__ xtri, uint32_t N,
-                                                       const uint32_t* __restrict__ leaf_dfs,
-                                                       const uint32_t* __restrict__ parent,
-                                                       const uint32_t* __restrict__ rank, uint32_t* __restrict__ cnt,
-                                                       crt_bvh_node* __restrict__ nodes, float4* __restrict__ wide,
-                                                       float4* __restrict__ wide_wt, RefitState* st, uint32_t* err) {
+__device__ __forceinline__ void store_xyz(float4* p, float x, float y, float z) {
+    reinterpret_cast<float2*>(p)[0] = make_float2(x, y);
+    reinterpret_cast<float*>(p)[2] = z;
+}
+
+// One block per kRefitLeaves consecutive leaves of the tree's left-to-right
+// leaf order (the order of the leaf records), in which every subtree's
+// leaves form one range.  A parent whose whole leaf range lies in the
+// block's range has both arriving threads in the block: they meet in shared
+// memory (box and reference per side, slot indexed by the parent's split
+// leaf — the first leaf of its right subtree, unique per internal node — and
+// a counter) with block-scope fences, and the second writes the parent's
+// whole traversal node (boxes, references, leaf counts: 64 full bytes).
+// Parents spanning blocks meet in global memory: each child writes its box
+// into its half of the parent's traversal node (whose references and leaf
+// counts stay as the build wrote them), then counts in with an
+// acquire-release atomic.
+constexpr int kRefitLeaves = 512;
+
+__global__ void __launch_bounds__(kRefitLeaves) refit_up_kernel(const crt_triangle* __restrict__ tris, uint32_t N,
+                                                                const float* __restrict__ models,
+                                                                const uint4* __restrict__ leaf_link,
+                                                                const uint4* __restrict__ int_link,
+                                                                uint32_t* __restrict__ cnt,
+                                                                crt_bvh_node* __restrict__ nodes,
+                                                                float4* __restrict__ xtri, float4* __restrict__ wide,
+                                                                uint32_t* err) {
+    __shared__ uint32_t s_cnt[kRefitLeaves];
+    __shared__ float s_box[kRefitLeaves][2][6];
+    __shared__ uint32_t s_ref[kRefitLeaves][2];
+    s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t lo = blockIdx.x * kRefitLeaves;
+    const uint32_t hi = min(lo + kRefitLeaves, N);
+    const uint32_t L = lo + threadIdx.x;
+    if (L >= N) return;
+    const uint32_t ti = __float_as_uint(xtri[3 * static_cast<size_t>(L)].w);  // the leaf's triangle stays
+    if (ti >= N) { raise_corrupt(err, 13, L, ti); return; }
+    // the moved triangle: leaf record (p0 | triangle id, p1 | model id, p2) and box
+    const TriRec t = load_tri(tris, ti);
+    if (t.model >= kMaxModels) raise_error(err, kDevBadModel);
+    const float* M = models + 16 * (t.model & (kMaxModels - 1));
+    const float4 p0 = mat_vec(M, t.p0), p1 = mat_vec(M, t.p1), p2 = mat_vec(M, t.p2);
+    xtri[3 * static_cast<size_t>(L) + 0] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(ti));
+    xtri[3 * static_cast<size_t>(L) + 1] = make_float4(p1.x, p1.y, p1.z, __uint_as_float(t.model));
+    xtri[3 * static_cast<size_t>(L) + 2] = make_float4(p2.x, p2.y, p2.z, 0.f);
+    float b[6] = {min_std(p0.x, min_std(p1.x, p2.x)), min_std(p0.y, min_std(p1.y, p2.y)),
+                  min_std(p0.z, min_std(p1.z, p2.z)), max_std(p0.x, max_std(p1.x, p2.x)),
+                  max_std(p0.y, max_std(p1.y, p2.y)), max_std(p0.z, max_std(p1.z, p2.z))};
+    uint32_t ref = kLeafRef | L;            // this node's reference in its parent's traversal node
+    uint32_t my_first = L, my_end = L + 1;  // its leaf range
+    uint4 up = __ldg(leaf_link + L);
+    for (uint32_t guard = 0; guard < N; ++guard) {
+        if (up.x == kNoParent) {  // the root: its box goes to the node array (the slack is read from it)
+            float4* nb = reinterpret_cast<float4*>(nodes);
+            nb[0] = make_float4(b[0], b[1], b[2], 0.f);
+            nb[1] = make_float4(b[3], b[4], b[5], 0.f);
+            return;
+        }
+        const uint32_t k = up.x >> 1, slot = up.x & 1u;
+        if (k >= N - 1) { raise_corrupt(err, 14, L, k); return; }
+        float4* w = wide + 4 * static_cast<size_t>(k);
+        float sb[6];
+        uint32_t sref = 0;
+        const bool in_block = up.y >= lo && up.z <= hi;
+        if (in_block) {
+            const uint32_t j = (slot == 0u ? my_end : my_first) - lo;  // the parent's split leaf, in [1, hi - lo)
+            if (j == 0u || j >= kRefitLeaves) { raise_corrupt(err, 14, L, j); return; }
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s_box[j][slot][c] = b[c];
+            s_ref[j][slot] = ref;
+            __threadfence_block();
+            if (atomicAdd(&s_cnt[j], 1u) == 0u) return;  // the sibling's thread finishes the parent
+            __threadfence_block();
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sb[c] = s_box[j][slot ^ 1u][c];
+            sref = s_ref[j][slot ^ 1u];
+        } else {
+            store_xyz(w + 2 * slot, b[0], b[1], b[2]);
+            store_xyz(w + 2 * slot + 1, b[3], b[4], b[5]);
+            if (atomic_add_acq_rel_u32(cnt + k, 1u) == 0u) return;
+            const float4 smn = __ldcg(w + 2 * (slot ^ 1u)), smx = __ldcg(w + 2 * (slot ^ 1u) + 1);
+            sb[0] = smn.x; sb[1] = smn.y; sb[2] = smn.z;
+            sb[3] = smx.x; sb[4] = smx.y; sb[5] = smx.z;
+        }
+        float lb[6], rb[6];  // left and right child's boxes
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            lb[c] = slot == 0u ? b[c] : sb[c];
+            rb[c] = slot == 0u ? sb[c] : b[c];
+        }
+        if (in_block) {
+            const uint32_t lref = slot == 0u ? ref : sref, rref = slot == 0u ? sref : ref;
+            const uint32_t mine = my_end - my_first, other = (up.z - up.y) - mine;
+            const uint32_t lcnt = slot == 0u ? mine : other, rcnt = slot == 0u ? other : mine;
+            w[0] = make_float4(lb[0], lb[1], lb[2], __uint_as_float(lref));
+            w[1] = make_float4(lb[3], lb[4], lb[5], __uint_as_float(rref));
+            w[2] = make_float4(rb[0], rb[1], rb[2], __uint_as_float(lcnt));
+            w[3] = make_float4(rb[3], rb[4], rb[5], __uint_as_float(rcnt));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {  // AABB::merge(left, right)
+            b[c] = min_std(lb[c], rb[c]);
+            b[3 + c] = max_std(lb[3 + c], rb[3 + c]);
+        }
+        ref = k;
+        my_first = up.y;
+        my_end = up.z;
+        up = __ldg(int_link + k);
+    }
+    raise_corrupt(err, 14, L, ref);
+}
+
+// wide_wt = wide with every box grown by the slack of the new root box
+// (min - grow, max + grow, as the build's layout pass rounds them).
+__global__ void __launch_bounds__(256) refit_grow_kernel(const crt_bvh_node* __restrict__ nodes,
+                                                         const float4* __restrict__ wide, uint32_t n_vec,
+                                                         float4* __restrict__ wide_wt, RefitState* st) {
     __shared__ float s_grow;
     if (threadIdx.x == 0) {
-        float smin[3], smax[3];
-        for (int a = 0; a < 3; ++a) {
-            smax[a] = from_ordered_key(st->key_max[a]);
-            smin[a] = from_ordered_key(~st->key_min_inv[a]);
-        }
-        const float g = scene_abs_eps(smin, smax);
-        s_grow = g;
-        if (blockIdx.x == 0) st->abs_eps = g;
+        const float4 a = __ldg(reinterpret_cast<const float4*>(nodes)), b = __ldg(reinterpret_cast<const float4*>(nodes) + 1);
+        const float smin[3] = {a.x, a.y, a.z}, smax[3] = {b.x, b.y, b.z};
+        s_grow = scene_abs_eps(smin, smax);
+        if (blockIdx.x == 0) st->abs_eps = s_grow;
     }
     __syncthreads();
-    const float grow = s_grow;
-    const uint32_t L = blockIdx.x * 256 + threadIdx.x;
-    if (L >= N) return;
+    const uint32_t i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n_vec) return;
+    const float g = (i & 1u) ? s_grow : -s_grow;  // float4s alternate min, max
+    const float4 v = __ldg(wide + i);
+    wide_wt[i] = make_float4(v.x + g, v.y + g, v.z + g, v.w);
+}
+
+// Node-array boxes from the traversal nodes: internal node k (DFS position
+// int_dfs[k]) holds its children's boxes; its left child sits right after
+// it, its right child at its right index.  The root's box is already there.
+__global__ void __launch_bounds__(256) refit_nodes_kernel(const float4* __restrict__ wide,
+                                                          const uint32_t* __restrict__ int_dfs, uint32_t N,
+                                                          crt_bvh_node* __restrict__ nodes, uint32_t* err) {
+    const uint32_t k = blockIdx.x * 256 + threadIdx.x;
+    if (k + 1 >= N) return;
     const uint32_t n_nodes = 2 * N - 1;
-    uint32_t cur = __ldg(leaf_dfs + L);
-    if (cur >= n_nodes) { raise_corrupt(err, 14, L, cur); return; }
-    const float4 a = __ldg(xtri + 3 * static_cast<size_t>(L)), b = __ldg(xtri + 3 * static_cast<size_t>(L) + 1),
-                 c = __ldg(xtri + 3 * static_cast<size_t>(L) + 2);
-    float3 mn = make_float3(min_std(a.x, min_std(b.x, c.x)), min_std(a.y, min_std(b.y, c.y)), min_std(a.z, min_std(b.z, c.z)));
-    float3 mx = make_float3(max_std(a.x, max_std(b.x, c.x)), max_std(a.y, max_std(b.y, c.y)), max_std(a.z, max_std(b.z, c.z)));
-    float4* nb = reinterpret_cast<float4*>(nodes + cur);
-    nb[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
-    nb[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
-    for (uint32_t guard = 0; guard < n_nodes; ++guard) {
-        const uint32_t p = __ldg(parent + cur);
-        if (p == kNoParent) return;  // cur is the root
-        const uint32_t k = p < n_nodes ? __ldg(rank + p) : 0xFFFFFFFFu;
-        if (k >= N - 1) { raise_corrupt(err, 14, cur, p); return; }
-        const uint32_t slot = (cur == p + 1) ? 0u : 1u;  // left child follows its parent
-        // this child's box in the parent's traversal record; the .w words
-        // (child references, leaf counts) stay as the build wrote them
-        float4* w = wide + 4 * static_cast<size_t>(k) + 2 * slot;
-        float4* g = wide_wt + 4 * static_cast<size_t>(k) + 2 * slot;
-        const float w0 = w[0].w, w1 = w[1].w;
-        w[0] = make_float4(mn.x, mn.y, mn.z, w0);
-        w[1] = make_float4(mx.x, mx.y, mx.z, w1);
-        g[0] = make_float4(mn.x - grow, mn.y - grow, mn.z - grow, w0);
-        g[1] = make_float4(mx.x + grow, mx.y + grow, mx.z + grow, w1);
-        __threadfence();
-        if (atomicAdd(cnt + k, 1u) == 0u) return;  // the sibling's thread finishes the parent
-        __threadfence();
-        const uint32_t sib = slot == 0u ? __ldg(reinterpret_cast<const uint4*>(nodes + p) + 2).z : p + 1;
-        if (sib >= n_nodes) { raise_corrupt(err, 14, p, sib); return; }
-        const float4 smn = __ldcg(reinterpret_cast<const float4*>(nodes + sib));
-        const float4 smx = __ldcg(reinterpret_cast<const float4*>(nodes + sib) + 1);
-        if (slot == 0u) {  // AABB::merge(left = this, right = sibling)
-            mn = make_float3(min_std(mn.x, smn.x), min_std(mn.y, smn.y), min_std(mn.z, smn.z));
-            mx = make_float3(max_std(mx.x, smx.x), max_std(mx.y, smx.y), max_std(mx.z, smx.z));
-        } else {           // AABB::merge(left = sibling, right = this)
-            mn = make_float3(min_std(smn.x, mn.x), min_std(smn.y, mn.y), min_std(smn.z, mn.z));
-            mx = make_float3(max_std(smx.x, mx.x), max_std(smx.y, mx.y), max_std(smx.z, mx.z));
-        }
-        float4* pb = reinterpret_cast<float4*>(nodes + p);
-        pb[0] = make_float4(mn.x, mn.y, mn.z, 0.f);
-        pb[1] = make_float4(mx.x, mx.y, mx.z, 0.f);
-        cur = p;
-    }
-    raise_corrupt(err, 14, L, cur);
+    const uint32_t d = __ldg(int_dfs + k);
+    if (d + 1 >= n_nodes) { raise_corrupt(err, 15, k, d); return; }
+    const uint32_t right = __ldg(reinterpret_cast<const uint4*>(nodes + d) + 2).z;
+    if (right >= n_nodes) { raise_corrupt(err, 15, k, right); return; }
+    const float4* w = wide + 4 * static_cast<size_t>(k);
+    const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2), w3 = __ldg(w + 3);
+    float4* l = reinterpret_cast<float4*>(nodes + d + 1);
+    float4* r = reinterpret_cast<float4*>(nodes + right);
+    l[0] = make_float4(w0.x, w0.y, w0.z, 0.f);
+    l[1] = make_float4(w1.x, w1.y, w1.z, 0.f);
+    r[0] = make_float4(w2.x, w2.y, w2.z, 0.f);
+    r[1] = make_float4(w3.x, w3.y, w3.z, 0.f);
 }
 
 uint32_t refit_topo_blocks(uint32_t N) { return (2 * N - 1 + 255) / 256; }
 
-void launch_refit_topology(const crt_bvh_node* nodes, const uint32_t* inv_perm, uint32_t N, uint32_t* parent,
-                           uint32_t* leaf_dfs, uint32_t* rank, uint32_t* block_count, uint32_t* err, cudaStream_t s) {
+void launch_refit_topology(const crt_bvh_node* nodes, const float4* wide, uint32_t N, uint4* leaf_link, uint4* int_link,
+                           uint32_t* int_dfs, uint32_t* block_count, uint32_t* err, cudaStream_t s) {
     const uint32_t n_nodes = 2 * N - 1, blocks = refit_topo_blocks(N);
-    refit_topo_kernel<<<blocks, 256, 0, s>>>(nodes, n_nodes, inv_perm, N, parent, leaf_dfs, block_count, err);
+    refit_count_kernel<<<blocks, 256, 0, s>>>(nodes, n_nodes, block_count);
     refit_scan_kernel<<<1, 1024, 0, s>>>(block_count, blocks);
-    refit_rank_kernel<<<blocks, 256, 0, s>>>(nodes, n_nodes, block_count, rank);
+    refit_link_kernel<<<blocks, 256, 0, s>>>(nodes, n_nodes, block_count, wide, leaf_link, int_link, int_dfs, err);
 }
 
-void launch_refit(const crt_triangle* tris, uint32_t N, const float* models, const uint32_t* perm,
-                  const uint32_t* leaf_dfs, const uint32_t* parent, const uint32_t* rank, uint32_t* cnt,
-                  crt_bvh_node* nodes, float4* xtri, float4* wide, float4* wide_wt, RefitState* st, uint32_t* err,
-                  cudaStream_t s) {
-    const uint32_t want = (N + 255) / 256;
-    const uint32_t grid = want < static_cast<uint32_t>(kNumSms * 8) ? want : kNumSms * 8;
-    refit_leaves_kernel<<<grid, 256, 0, s>>>(tris, N, models, perm, xtri, st, err);
-    refit_up_kernel<<<want, 256, 0, s>>>(xtri, N, leaf_dfs, parent, rank, cnt, nodes, wide, wide_wt, st, err);
+void launch_refit(const crt_triangle* tris, uint32_t N, const float* models, const uint4* leaf_link,
+                  const uint4* int_link, uint32_t* cnt, crt_bvh_node* nodes, float4* xtri, float4* wide,
+                  float4* wide_wt, RefitState* st, uint32_t* err, cudaStream_t s) {
+    refit_up_kernel<<<(N + kRefitLeaves - 1) / kRefitLeaves, kRefitLeaves, 0, s>>>(tris, N, models, leaf_link, int_link,
+                                                                                  cnt, nodes, xtri, wide, err);
+    const uint32_t n_vec = 4 * (N - 1);
+    refit_grow_kernel<<<n_vec ? (n_vec + 255) / 256 : 1u, 256, 0, s>>>(nodes, wide, n_vec, wide_wt, st);
+}
+
+void launch_refit_nodes(const float4* wide, const uint32_t* int_dfs, uint32_t N, crt_bvh_node* nodes, uint32_t* err,
+                        cudaStream_t s) {
+    if (N < 2) return;
+    refit_nodes_kernel<<<(N - 1 + 255) / 256, 256, 0, s>>>(wide, int_dfs, N, nodes, err);
 }
 
 }  // namespace crt
