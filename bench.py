@@ -250,6 +250,30 @@ def run_ours(args):
     torch.cuda.synchronize()
     p_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
 
+    # ---- mesh input: the scene's indexed mesh to TriangleGPU records on the GPU
+    from realtimeraytracing_gb300 import scenes as S
+    mv, mf = S.displaced_icosphere(8, 0.05, 0)
+    d_mv = torch.from_numpy(np.ascontiguousarray(mv, np.float32)).to(dev)
+    d_mf = torch.from_numpy(np.ascontiguousarray(mf, np.uint32).view(np.int32)).to(dev)
+    d_mt = torch.empty((mf.shape[0], 16), dtype=torch.float32, device=dev)
+    for _ in range(2):
+        ctx.triangles_from_indexed(d_mv, d_mf, 0, out=d_mt)
+    mev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            l2_flush.zero_()
+            mev[k][0].record(stream)
+            ctx.triangles_from_indexed(d_mv, d_mf, 0, out=d_mt)
+            mev[k][1].record(stream)
+    torch.cuda.synchronize()
+    m_ms = statistics.mean(a.elapsed_time(b) for a, b in mev)
+    mesh_upload = {"triangles": int(mf.shape[0]), "ms": round(m_ms, 4),
+                   "gbs": round((12 + 36 + 64) * mf.shape[0] / (m_ms * 1e-3) / 1e9, 1),
+                   "identical_to_scene_records": bool(torch.equal(d_mt.cpu(), torch.from_numpy(tris))),
+                   "note": "crt_triangles_from_indexed on device arrays: 12 B indices + 36 B gathered vertices + "
+                           "64 B record per triangle, L2 flushed before each call"}
+    del d_mv, d_mf, d_mt
+
     # ---- the reference's whole compute pass (getRay, closest hit, getColor,
     # imageStore) into a device RGBA32F image: crt_render_frame, one launch
     img = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
@@ -341,6 +365,7 @@ def run_ours(args):
             "primary_trace_kernel": {"ms": round(p_ms, 4), "mrays_s": round(n_rays / (p_ms * 1e-3) / 1e6, 1),
                                      "node_fetches_per_ray": round(p_visited / n_rays, 2),
                                      "tris_per_ray": round(p_tested / n_rays, 2)},
+            "mesh_upload": mesh_upload,
             "shaded_frame": dict(shaded, note="crt_render_frame: camera ray, closest hit, getColor and "
                                               "imageStore per texel into a device RGBA32F image, no shadow rays"),
             "cpu_baseline": cpu,

@@ -159,6 +159,24 @@ const char* crt_last_error_string(void);
 /* The CUDA stream (cudaStream_t) the context orders its work on. */
 void* crt_stream(crt_ctx* ctx);
 
+/* ---- mesh input: replaces Mesh::load (srcCommon/scene/geometry/mesh.cpp:186-263) and
+ * the TriangleGPU assembly of Scene::getTriangleToGPUData (srcOpenGL/scene/scene.cpp:26-40).
+ * crt_obj_parse reads Wavefront OBJ text (len bytes) on the host: "v x y z" vertices and
+ * "f" faces ("v", "v/vt", "v//vn", "v/vt/vn" corners, 1-based or negative relative
+ * indices; faces of more than 3 corners become the fan (0, i, i+1)); everything else is
+ * skipped.  It writes up to vert_cap vertices (3 floats each) and tri_cap triangles (3
+ * vertex indices each) — pass NULL / 0 to count only — and returns the full counts in
+ * counts[0] (vertices) and counts[1] (triangles).  Malformed lines give CRT_ERR_BAD_INPUT
+ * naming the line. */
+crt_status crt_obj_parse(const char* text, size_t len, float* vertices, uint32_t vert_cap, uint32_t* indices,
+                         uint32_t tri_cap, uint32_t counts[2]);
+/* TriangleGPU records of an indexed mesh on the GPU: out[i] holds the vertices of
+ * indices[3i..3i+2] as (x, y, z, 1) and model_id (Triangle's constructor,
+ * triangle.cpp:18-25).  Several meshes form one scene buffer by writing to out + offset
+ * with each mesh's id.  Indices past n_vertices give CRT_ERR_BAD_INPUT. */
+crt_status crt_triangles_from_indexed(crt_ctx* ctx, const float* vertices, uint32_t n_vertices, const uint32_t* indices,
+                                      uint32_t n_triangles, uint32_t model_id, crt_triangle* out);
+
 /* ---- build: replaces cr::BVH::BVH (bvh.cpp:11-24) + Scene::getBVH_NodesToGPUData
  * (scene.cpp:203-208).
  *   tris      n_buffer triangles; the reference scans all n_buffer of them for

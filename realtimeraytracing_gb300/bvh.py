@@ -30,6 +30,19 @@ def default_context() -> crt.Context:
     return _default_ctx
 
 
+class Mesh:
+    """cr::Mesh::load (srcCommon/scene/geometry/mesh.cpp:186-263): an OBJ
+    file's faces as TriangleGPU records of model `meshId`, read on the host
+    and assembled on the GPU.  Scenes concatenate meshes' records, as
+    Scene::getTriangleToGPUData does (srcOpenGL/scene/scene.cpp:26-40)."""
+
+    @staticmethod
+    def load(path: str, meshId: int = 0, ctx: crt.Context | None = None, out=None):
+        ctx = ctx or default_context()
+        vertices, indices = crt.parse_obj(path)
+        return ctx.triangles_from_indexed(vertices, indices, meshId, out)
+
+
 class BVH:
     """cr::BVH.  `unsortedTriangles` is the (n_buffer, 16) float32 TriangleGPU
     buffer — the reference scans every entry of it for the scene box

@@ -48,7 +48,8 @@ EXPORTS = [
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
-    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit",
+    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_obj_parse",
+    "crt_triangles_from_indexed",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -137,6 +138,8 @@ def lib():
             "crt_shade": ([vp, vp, vp, vp, u32, vp, vp], i32),
             "crt_render_frame": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
             "crt_refit": ([vp, vp, vp, u32, vp, u32], i32),
+            "crt_obj_parse": ([C.c_char_p, C.c_size_t, vp, u32, vp, u32, vp], i32),
+            "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -188,6 +191,22 @@ def _shading(models, materials, flags, bvh_depth):
     sh.n_materials = 0 if materials is None else _rows(materials)
     sh.flags, sh.bvh_depth = flags, bvh_depth
     return sh, (models, materials)
+
+
+def parse_obj(source):
+    """crt_obj_parse on OBJ text (str / bytes) or a file path: (vertices (n, 3)
+    float32, indices (m, 3) uint32).  Host-side parsing, as Mesh::load's."""
+    if isinstance(source, str) and "\n" not in source and os.path.exists(source):
+        with open(source, "rb") as f:
+            data = f.read()
+    else:
+        data = source.encode() if isinstance(source, str) else bytes(source)
+    counts = np.zeros(2, np.uint32)
+    _check(lib().crt_obj_parse(data, len(data), None, 0, None, 0, _ptr(counts)))
+    verts = np.empty((int(counts[0]), 3), np.float32)
+    idx = np.empty((int(counts[1]), 3), np.uint32)
+    _check(lib().crt_obj_parse(data, len(data), _ptr(verts), verts.shape[0], _ptr(idx), idx.shape[0], _ptr(counts)))
+    return verts, idx
 
 
 class PredictorConfig(C.Structure):
@@ -538,6 +557,20 @@ class Context:
         _check(lib().crt_trace_frame(self.handle, bvh.handle, _ptr(cam), width, height, lp, flags, _ptr(hp),
                                      _ptr(hs)))
         return hp, hs
+
+    def triangles_from_indexed(self, vertices, indices, model_id: int = 0, out=None):
+        """crt_triangles_from_indexed: (m, 16) float32 TriangleGPU records of an
+        indexed mesh, built on the GPU."""
+        self._after_torch()
+        if isinstance(vertices, np.ndarray):
+            vertices = np.ascontiguousarray(vertices, np.float32)
+        if isinstance(indices, np.ndarray):
+            indices = np.ascontiguousarray(indices, np.uint32)
+        n_tri = _rows(indices)
+        out = np.empty((n_tri, 16), np.float32) if out is None else out
+        _check(lib().crt_triangles_from_indexed(self.handle, _ptr(vertices), _rows(vertices), _ptr(indices), n_tri,
+                                                model_id, _ptr(out)))
+        return out
 
     def shade(self, bvh: Bvh, rays, hits, models=None, materials=None, shade_flags: int = 0, bvh_depth: int = 0,
               out=None):

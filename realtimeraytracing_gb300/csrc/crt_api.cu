@@ -183,6 +183,7 @@ struct crt_ctx {
         const uint32_t e = ew[0];
         if (e & crt::kDevTimeout) return fail(CRT_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up (err=0x%x)", e);
         if (e & crt::kDevBadModel) return fail(CRT_ERR_BAD_INPUT, "a triangle references model id >= 64");
+        if (e & crt::kDevBadIndex) return fail(CRT_ERR_BAD_INPUT, "a triangle references a vertex past the end");
         if (e & crt::kDevStackOverflow) return fail(CRT_ERR_STACK_OVERFLOW, "a ray overflowed its traversal stack");
         if (e & crt::kDevCorrupt)
             return fail(CRT_ERR_CUDA, "a device index check failed (err=0x%x site=%u iter=%u values=%u,%u)", e,
@@ -1797,6 +1798,54 @@ crt_status crt_render_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam,
     CRT_TRY(x->check_device_error());
     if (flags & CRT_TRACE_STATS) CRT_CUDA(cudaMemcpy(x->last_trace_stats, x->trace_stats.p, 16, cudaMemcpyDeviceToHost));
     return CRT_OK;
+}
+
+}  // extern "C"
+
+// ===================================================================== mesh input
+extern "C" {
+
+crt_status crt_obj_parse(const char* text, size_t len, float* vertices, uint32_t vert_cap, uint32_t* indices,
+                         uint32_t tri_cap, uint32_t counts[2]) {
+    if (!text || !counts) return fail(CRT_ERR_INVALID_ARG, "crt_obj_parse: null text or counts");
+    uint64_t nv = 0, nt = 0;
+    std::string err;
+    if (!crt::obj_parse(text, len, vertices, vertices ? vert_cap : 0, indices, indices ? tri_cap : 0, &nv, &nt, &err))
+        return fail(CRT_ERR_BAD_INPUT, "crt_obj_parse: %s", err.c_str());
+    if (nv > 0xFFFFFFFFull || nt > 0xFFFFFFFFull) return fail(CRT_ERR_BAD_INPUT, "crt_obj_parse: more than 2^32 elements");
+    counts[0] = static_cast<uint32_t>(nv);
+    counts[1] = static_cast<uint32_t>(nt);
+    return CRT_OK;
+}
+
+crt_status crt_triangles_from_indexed(crt_ctx* x, const float* vertices, uint32_t n_vertices, const uint32_t* indices,
+                                      uint32_t n_triangles, uint32_t model_id, crt_triangle* out) {
+    if (!x || !out || (n_triangles && (!vertices || !indices)))
+        return fail(CRT_ERR_INVALID_ARG, "crt_triangles_from_indexed: null argument");
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n_triangles == 0) return CRT_OK;
+    const void* d_v = nullptr;
+    const void* d_i = nullptr;
+    CRT_TRY(stage_in(x, x->rays_in, vertices, 12ull * n_vertices, &d_v));
+    CRT_TRY(stage_in(x, x->hits_out, indices, 12ull * n_triangles, &d_i));
+    if (!aligned(d_v, 4) || !aligned(d_i, 4))
+        return fail(CRT_ERR_INVALID_ARG, "crt_triangles_from_indexed: vertices and indices must be 4-byte aligned");
+    const bool dev_out = is_device_ptr(out);
+    crt_triangle* d_out = out;
+    if (!dev_out) {
+        CRT_TRY(x->tris_in.reserve(sizeof(crt_triangle) * static_cast<size_t>(n_triangles)));
+        d_out = x->tris_in.as<crt_triangle>();
+    } else if (!aligned(out, 16)) {
+        return fail(CRT_ERR_INVALID_ARG, "crt_triangles_from_indexed: out must be 16-byte aligned");
+    }
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    crt::launch_indexed(static_cast<const float*>(d_v), n_vertices, static_cast<const uint32_t*>(d_i), n_triangles,
+                        model_id, d_out, x->err.as<uint32_t>(), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out)
+        CRT_CUDA(cudaMemcpyAsync(out, d_out, sizeof(crt_triangle) * static_cast<size_t>(n_triangles),
+                                 cudaMemcpyDeviceToHost, x->stream));
+    return x->check_device_error();
 }
 
 }  // extern "C"

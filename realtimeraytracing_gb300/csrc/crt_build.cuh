@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <string>
 
 #include "crt.h"
 #include "crt_predictor.cuh"
@@ -211,6 +212,16 @@ cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
                               uint8_t* depth_odd, LeafOut leaves, unsigned int* bar, uint32_t max_iters, uint32_t* err,
                               uint32_t spin_limit, cudaStream_t s);
+// Mesh input (crt_mesh.cu).  obj_parse reads OBJ text into at most vert_cap
+// vertices (3 floats each) and tri_cap triangles (3 vertex indices each) —
+// either may be null to count only — and returns the full counts, or false
+// with *error set.
+bool obj_parse(const char* text, size_t len, float* vertices, uint64_t vert_cap, uint32_t* indices, uint64_t tri_cap,
+               uint64_t* n_vertices, uint64_t* n_triangles, std::string* error);
+// TriangleGPU records of an indexed mesh (vertices: 3 floats each).
+void launch_indexed(const float* vertices, uint32_t n_vertices, const uint32_t* indices, uint32_t n_triangles,
+                    uint32_t model_id, crt_triangle* out, uint32_t* err, cudaStream_t s);
+
 // Sets the message crt_last_error_string() returns on the calling thread.
 void set_last_error(const char* msg);
 

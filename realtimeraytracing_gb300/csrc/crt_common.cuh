@@ -129,6 +129,7 @@ enum DevError : uint32_t {
     kDevStackOverflow = 1u << 2,
     kDevIterLimit = 1u << 3,
     kDevCorrupt = 1u << 4,   // an index check failed; the access was skipped
+    kDevBadIndex = 1u << 5,  // an input triangle names a vertex past the end
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) { atomicOr(err, code); }
