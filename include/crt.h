@@ -122,6 +122,9 @@ typedef struct crt_camera {
 #define CRT_TRACE_WIDE        0x10u /* walk the 4-wide nodes instead of the binary ones (same hits) */
 #define CRT_TRACE_PREDICTOR_ORDER 0x20u /* trace the rays grouped by their predicted treelet (same hits) */
 #define CRT_TRACE_SORT_RAYS   0x40u /* trace the rays ordered by origin cell and direction (same hits) */
+#define CRT_TRACE_COMPRESSED  0x80u /* walk 64-byte compressed 4-wide nodes: 8-bit child boxes rounded
+                                       outward, exact leaf boxes re-checked (same hits); the reference
+                                       layout stays the export format */
 
 typedef struct crt_config {
     int device;                 /* CUDA device ordinal, default 0 */

@@ -105,12 +105,13 @@ struct crt_bvh {
     // wide_wt: boxes grown by abs_eps; xtri: transformed triangles in the tree's
     // left-to-right leaf order; inv_perm: triangle -> its position in that order
     DevBuf nodes, wide, wide_wt, depth_odd, xtri, codes, perm, inv_perm;
-    mutable DevBuf wide4;
+    mutable DevBuf wide4, cwide;
     crt_predictor* predictor = nullptr;
     // The 4-wide traversal nodes are derived on the first CRT_TRACE_WIDE
     // trace after a build, so builds whose trees are never walked 4-wide
     // neither compute nor store them.
     mutable bool wide4_ready = false;
+    mutable bool cwide_ready = false;  // the compressed 4-wide nodes, derived likewise
     // Refit topology of the last build (crt_refit, derived on its first call).
     DevBuf refit_link, refit_leaf, refit_dfs, refit_cnt;
     bool refit_ready = false;
@@ -364,6 +365,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     CRT_TRY(b->wide.reserve(64ull * N));
     CRT_TRY(b->wide_wt.reserve(64ull * N));
     b->wide4_ready = false;
+    b->cwide_ready = false;
     b->refit_ready = false;
     b->node_boxes_stale = false;
     CRT_TRY(b->depth_odd.reserve(N));
@@ -540,7 +542,7 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
 
 crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
     if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS | CRT_TRACE_WIDE |
-                  CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_SORT_RAYS))
+                  CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_SORT_RAYS | CRT_TRACE_COMPRESSED))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
     if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && !b->predictor)
         return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor bound to this bvh (crt_predictor_create)");
@@ -559,16 +561,30 @@ crt_status ensure_wide4(crt_ctx* x, const crt_bvh* b) {
     return CRT_OK;
 }
 
+// Derives the compressed 4-wide traversal nodes of b on x's stream if the
+// last build (or refit) has not yet done so.
+crt_status ensure_cwide(crt_ctx* x, const crt_bvh* b) {
+    if (b->cwide_ready || b->n <= 1) return CRT_OK;
+    CRT_TRY(b->cwide.reserve(64ull * b->n));
+    crt::launch_cwide(b->wide.as<float4>(), b->depth_odd.as<uint8_t>(), b->n - 1, b->cwide.as<uint4>(),
+                      x->err.as<uint32_t>(), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    b->cwide_ready = true;
+    return CRT_OK;
+}
+
 // Enqueues one traversal launch on device-resident rays/hits (no sync).
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
                         crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0) {
     if (n_rays == 0) return CRT_OK;
     if (flags & CRT_TRACE_WIDE) CRT_TRY(ensure_wide4(x, b));
+    if (flags & CRT_TRACE_COMPRESSED) CRT_TRY(ensure_cwide(x, b));
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
     p.xtri = b->xtri.as<float4>();
     p.wide = (flags & CRT_TRI_WATERTIGHT) ? b->wide_wt.as<float4>() : b->wide.as<float4>();
     p.wide4 = (b->n > 1) ? b->wide4.as<float4>() : nullptr;
+    p.cwide = (b->n > 1 && (flags & CRT_TRACE_COMPRESSED)) ? b->cwide.as<uint4>() : nullptr;
     p.rays = d_rays;
     p.hits = d_hits;
     p.n_rays = n_rays;
@@ -615,7 +631,8 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     }
     // binary walk: stack <= tree height <= PLOC iterations + 1; 4-wide walk: <= 3 per two levels
     const bool deep = (b->iterations + 2 > 64) || (3 * ((b->iterations + 2) / 2) + 3 > 96);
-    const uint32_t launch_flags = (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_WIDE)) | (deep ? (1u << 16) : 0u);
+    const uint32_t launch_flags =
+        (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED)) | (deep ? (1u << 16) : 0u);
     crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
@@ -697,6 +714,7 @@ crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t 
     CRT_CUDA(cudaMemcpyAsync(h_eps, &x->refit_state.as<crt::RefitState>()->abs_eps, sizeof(float),
                              cudaMemcpyDeviceToHost, s));
     b->wide4_ready = false;
+    b->cwide_ready = false;
     b->node_boxes_stale = N > 1;
     const crt_status st = x->check_device_error();
     if (st != CRT_OK) {
@@ -714,6 +732,7 @@ crt_status crt_bvh_free(crt_bvh* b) {
     b->wide.release();
     b->wide_wt.release();
     b->wide4.release();
+    b->cwide.release();
     b->depth_odd.release();
     b->inv_perm.release();
     if (b->predictor) b->predictor->bvh = nullptr;
@@ -874,7 +893,7 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     if (flags & CRT_TRACE_ANY) return fail(CRT_ERR_INVALID_ARG, "crt_trace_frame: primary rays are closest-hit");
     CRT_CUDA(cudaSetDevice(x->device));
     const uint32_t n = width * height;
-    const bool fused = !(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE));
+    const bool fused = !(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED));
     bool dev_p = is_device_ptr(hits_primary);
     crt_hit* d_hp = hits_primary;
     if (!dev_p && fused) {  // page-locked host output: the frame kernel writes it over the CPU-GPU link
@@ -1766,7 +1785,7 @@ crt_status crt_render_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam,
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
-    if (!(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE))) {
+    if (!(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED))) {
         // one launch: camera ray, closest hit and texel per pixel
         crt::TraceParams p = bvh_params(x, b, flags);
         p.n_rays = n;

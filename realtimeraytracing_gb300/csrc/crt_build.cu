@@ -951,6 +951,104 @@ __global__ void __launch_bounds__(256) wide4_kernel(const float4* __restrict__ w
     o[7] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// ================================= K4c: compressed 4-wide traversal nodes
+// The same four children as wide4_kernel, in 64 bytes: the node's origin
+// (the minimum corner over its children), one power-of-two step per axis
+// (the least with 255 steps covering the node's extent, biased exponent in a
+// byte) and each child box as 8-bit step counts, the minimum rounded down
+// and the maximum up.  The traversal decodes origin + q * step; rounding to
+// nearest is monotone, so the decoded box encloses the exact one.  Record:
+// (origin xyz, exponents | child count << 24), (qlo x, y, z, qhi x), (qhi y,
+// z, 0, 0), four child references; byte c of each q word belongs to child c.
+__device__ __forceinline__ uint32_t quant_step_exp(double extent) {
+    int e = -126;
+    if (extent > 0.0) {
+        int k = 0;
+        frexp(extent / 255.0, &k);  // extent / 255 < 2^k
+        e = k < -126 ? -126 : k;
+    }
+    return static_cast<uint32_t>(e + 127);
+}
+
+__global__ void __launch_bounds__(256) cwide_kernel(const float4* __restrict__ wide, const uint8_t* __restrict__ depth_odd,
+                                                    uint32_t n_internal, uint4* __restrict__ cwide, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_internal || depth_odd[i]) return;
+    float mn[4][3], mx[4][3];
+    uint32_t ref[4];
+    int k = 0;
+    const float4* w = wide + 4 * static_cast<size_t>(i);
+    const float4 w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3];
+    const float4 cmn[2] = {w0, w2}, cmx[2] = {w1, w3};
+    const uint32_t cref[2] = {__float_as_uint(w0.w), __float_as_uint(w1.w)};
+    auto put = [&](float4 a, float4 b, uint32_t r) {
+        mn[k][0] = a.x; mn[k][1] = a.y; mn[k][2] = a.z;
+        mx[k][0] = b.x; mx[k][1] = b.y; mx[k][2] = b.z;
+        ref[k++] = r;
+    };
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        if (cref[c] & kLeafRef) {
+            put(cmn[c], cmx[c], cref[c]);
+        } else {
+            const float4* g = wide + 4 * static_cast<size_t>(cref[c]);
+            const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3];
+            put(g0, g1, __float_as_uint(g0.w));
+            put(g2, g3, __float_as_uint(g1.w));
+        }
+    }
+    const int n = k;
+    float o[3];
+    uint32_t ex[3];
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float lo = mn[0][a], hi = mx[0][a];
+        for (int c = 1; c < n; ++c) {
+            lo = min_std(lo, mn[c][a]);
+            hi = max_std(hi, mx[c][a]);
+        }
+        ok = ok && isfinite(lo) && isfinite(hi) && lo <= hi;
+        o[a] = lo;
+        ex[a] = quant_step_exp(static_cast<double>(hi) - static_cast<double>(lo));
+        ok = ok && ex[a] <= 254u;
+    }
+    uint32_t q[6] = {0u, 0u, 0u, 0u, 0u, 0u};  // lo x, y, z, hi x, y, z; byte c = child c
+    if (ok) {
+        for (int c = 0; c < n; ++c)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const double step = ldexp(1.0, static_cast<int>(ex[a]) - 127);
+                const float fstep = __uint_as_float(ex[a] << 23);
+                double dl = floor((static_cast<double>(mn[c][a]) - o[a]) / step);
+                double dh = ceil((static_cast<double>(mx[c][a]) - o[a]) / step);
+                int ql = dl < 0.0 ? 0 : (dl > 255.0 ? 255 : static_cast<int>(dl));
+                int qh = dh < 0.0 ? 0 : (dh > 255.0 ? 255 : static_cast<int>(dh));
+                // settle the counts against the decoder's own float arithmetic
+                while (ql > 0 && o[a] + static_cast<float>(ql) * fstep > mn[c][a]) --ql;
+                while (qh < 255 && o[a] + static_cast<float>(qh) * fstep < mx[c][a]) ++qh;
+                ok = ok && !(o[a] + static_cast<float>(ql) * fstep > mn[c][a]) &&
+                     !(o[a] + static_cast<float>(qh) * fstep < mx[c][a]);
+                q[a] |= static_cast<uint32_t>(ql) << (8 * c);
+                q[3 + a] |= static_cast<uint32_t>(qh) << (8 * c);
+            }
+    }
+    if (!ok) raise_corrupt(err, 16, i, 0u);
+    for (int c = n; c < 4; ++c) ref[c] = kNoChild;
+    uint4* out = cwide + 4 * static_cast<size_t>(i);
+    out[0] = make_uint4(__float_as_uint(o[0]), __float_as_uint(o[1]), __float_as_uint(o[2]),
+                        ex[0] | (ex[1] << 8) | (ex[2] << 16) | (static_cast<uint32_t>(n) << 24));
+    out[1] = make_uint4(q[0], q[1], q[2], q[3]);
+    out[2] = make_uint4(q[4], q[5], 0u, 0u);
+    out[3] = make_uint4(ref[0], ref[1], ref[2], ref[3]);
+}
+
+void launch_cwide(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, uint4* cwide, uint32_t* err,
+                  cudaStream_t s) {
+    if (n_internal == 0) return;
+    cwide_kernel<<<(n_internal + 255) / 256, 256, 0, s>>>(wide, depth_odd, n_internal, cwide, err);
+}
+
 void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s) {
     if (n_internal == 0) return;
     wide4_kernel<<<(n_internal + 255) / 256, 256, 0, s>>>(wide, depth_odd, n_internal, wide4);

@@ -88,6 +88,11 @@ void launch_layout_emit(const float4* node_box, const uint4* node_kids, const ui
                         const uint32_t* dfs, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
                         LeafOut leaves, const SceneState* st, uint32_t* err, cudaStream_t s);
 void launch_wide4(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, float4* wide4, cudaStream_t s);
+// 64-byte compressed 4-wide nodes (CRT_TRACE_COMPRESSED) from the binary
+// traversal nodes; raises kDevCorrupt where a box cannot be quantized
+// (non-finite coordinates).
+void launch_cwide(const float4* wide, const uint8_t* depth_odd, uint32_t n_internal, uint4* cwide, uint32_t* err,
+                  cudaStream_t s);
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, LeafOut leaves, cudaStream_t s);
 // All PLOC iterations and the DFS layout in one cooperative launch; returns
 // cudaErrorNotSupported when a cooperative launch is unavailable.
@@ -126,6 +131,7 @@ struct TraceParams {
     const float4* wide;      // 64-B traversal nodes: child boxes + child references (watertight
                              // traces: boxes already grown by abs_eps)
     const float4* wide4;     // 128-B 4-wide traversal nodes (even-depth internal nodes)
+    const uint4* cwide = nullptr;  // 64-B compressed 4-wide traversal nodes (same indices)
     const float4* xtri;      // 3 float4 per leaf (tree order): transformed p0 | tri id, p1 | model id, p2
     const crt_ray* rays;
     crt_hit* hits;

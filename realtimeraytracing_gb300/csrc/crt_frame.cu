@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(BLOCK) frame_kernel(TraceParams p, const crt_c
     const uint32_t y = i / width, x = i - y * width;
     float4 r0, r1;
     camera_ray(cam, x, y, width, height, r0, r1);
-    const uint4 h = trace_one<false, WT, STACK, false, false>(p, i, r0, r1);
+    const uint4 h = trace_one<false, WT, STACK, false, 0>(p, i, r0, r1);
     if (!SHADE || p.hits) reinterpret_cast<uint4*>(p.hits)[i] = h;
     if (SHADE) sp.image[i] = shade_texel(p, sp, h, r0, r1);
     if (!shadows) return;
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(BLOCK) frame_kernel(TraceParams p, const crt_c
     if (h.x != CRT_MISS) {
         float4 s0, s1;
         shadow_ray(r0, r1, h, lx, ly, lz, s0, s1);
-        hs = trace_one<true, WT, STACK, false, false>(p, i, s0, s1);
+        hs = trace_one<true, WT, STACK, false, 0>(p, i, s0, s1);
     }
     reinterpret_cast<uint4*>(hits_shadow)[i] = hs;
 }

@@ -12,13 +12,13 @@
 
 namespace crt {
 
-template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE, int BLOCK>
+template <bool ANY, bool WT, int STACK, bool SEED, int WALK, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) trace_kernel(TraceParams p) {
     const uint32_t t_id = blockIdx.x * BLOCK + threadIdx.x;
     if (t_id >= p.n_rays) return;
     const uint32_t i = p.order ? __ldg(p.order + t_id) : ray_of_thread(t_id, p.tile_width);
     if (i >= p.n_rays) { raise_corrupt(p.err, 7, t_id, i); return; }
-    trace_ray<ANY, WT, STACK, SEED, WIDE>(p, i);
+    trace_ray<ANY, WT, STACK, SEED, WALK>(p, i);
 }
 
 // Many scenes in one launch: ray i belongs to the scene whose ray range holds
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, co
     p.xtri = base.xtri + 3 * static_cast<size_t>(sc.tri_off);
     p.n_nodes = 2 * sc.n_tris - 1;
     p.abs_eps = sc.abs_eps;
-    trace_ray<ANY, WT, STACK, false, false>(p, i);
+    trace_ray<ANY, WT, STACK, false, 0>(p, i);
 }
 
 // ------------------------------------------------------ ray ordering
@@ -161,37 +161,40 @@ __global__ void __launch_bounds__(256) shadow_kernel(const crt_ray* __restrict__
 
 
 template <bool ANY, bool WT, int BLOCK>
-static void launch_trace_b(const TraceParams& p, bool deep, bool seed, bool wide, cudaStream_t s) {
+static void launch_trace_b(const TraceParams& p, bool deep, bool seed, int walk, cudaStream_t s) {
     const uint32_t grid = (p.n_rays + BLOCK - 1) / BLOCK;
     if (grid == 0) return;
     if (seed) {
-        if (deep) trace_kernel<ANY, WT, 1024, true, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 64, true, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
-    } else if (wide) {
-        if (deep) trace_kernel<ANY, WT, 1024, false, true, BLOCK><<<grid, BLOCK, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 96, false, true, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, true, 0, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, true, 0, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+    } else if (walk == 1) {
+        if (deep) trace_kernel<ANY, WT, 1024, false, 1, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 96, false, 1, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+    } else if (walk == 2) {
+        if (deep) trace_kernel<ANY, WT, 1024, false, 2, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 96, false, 2, BLOCK><<<grid, BLOCK, 0, s>>>(p);
     } else {
-        if (deep) trace_kernel<ANY, WT, 1024, false, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
-        else trace_kernel<ANY, WT, 64, false, false, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        if (deep) trace_kernel<ANY, WT, 1024, false, 0, BLOCK><<<grid, BLOCK, 0, s>>>(p);
+        else trace_kernel<ANY, WT, 64, false, 0, BLOCK><<<grid, BLOCK, 0, s>>>(p);
     }
 }
 
 template <bool ANY, bool WT>
-static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, bool wide, cudaStream_t s) {
-    if (block == 256) launch_trace_b<ANY, WT, 256>(p, deep, seed, wide, s);
-    else if (block == 64) launch_trace_b<ANY, WT, 64>(p, deep, seed, wide, s);
-    else launch_trace_b<ANY, WT, 128>(p, deep, seed, wide, s);
+static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed, int walk, cudaStream_t s) {
+    if (block == 256) launch_trace_b<ANY, WT, 256>(p, deep, seed, walk, s);
+    else if (block == 64) launch_trace_b<ANY, WT, 64>(p, deep, seed, walk, s);
+    else launch_trace_b<ANY, WT, 128>(p, deep, seed, walk, s);
 }
 
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s) {
     const bool any = flags & CRT_TRACE_ANY, wt = flags & CRT_TRI_WATERTIGHT;
     const bool deep = (flags >> 16) != 0;  // set by the host when the tree may be deeper than the stacks allow
     const bool seed = p.pred_class != nullptr;
-    const bool wide = (flags & CRT_TRACE_WIDE) && p.wide4 != nullptr;
-    if (any && wt) launch_trace_t<true, true>(p, block, deep, seed, wide, s);
-    else if (any) launch_trace_t<true, false>(p, block, deep, seed, wide, s);
-    else if (wt) launch_trace_t<false, true>(p, block, deep, seed, wide, s);
-    else launch_trace_t<false, false>(p, block, deep, seed, wide, s);
+    const int walk = ((flags & CRT_TRACE_COMPRESSED) && p.cwide) ? 2 : ((flags & CRT_TRACE_WIDE) && p.wide4) ? 1 : 0;
+    if (any && wt) launch_trace_t<true, true>(p, block, deep, seed, walk, s);
+    else if (any) launch_trace_t<true, false>(p, block, deep, seed, walk, s);
+    else if (wt) launch_trace_t<false, true>(p, block, deep, seed, walk, s);
+    else launch_trace_t<false, false>(p, block, deep, seed, walk, s);
 }
 
 template <bool ANY, bool WT, int BLOCK>

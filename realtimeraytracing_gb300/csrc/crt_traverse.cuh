@@ -8,8 +8,9 @@
 //
 // Traversal (one thread per ray, stack in local memory) over the 64-byte
 // binary nodes the layout pass writes (both child boxes + references), or
-// with CRT_TRACE_WIDE over 128-byte 4-wide nodes (half the fetches, more
-// work per fetch — slower on GB300 today, kept for comparison):
+// with CRT_TRACE_WIDE over 128-byte 4-wide nodes or with CRT_TRACE_COMPRESSED
+// over 64-byte compressed 4-wide nodes (half the fetches, more work per
+// fetch — slower on GB300 today, kept for comparison):
 //   * children are box-tested at their parent, leaves tested at once, the
 //     nearer internal child entered without a stack round trip;
 //   * a subtree is skipped when its entry distance exceeds the best hit by
@@ -185,7 +186,8 @@ __device__ __forceinline__ uint32_t ray_of_thread(uint32_t t, uint32_t width) {
 
 // Closest hit (or any hit) of the ray r0 = (o, tmin), r1 = (d, tmax) as a
 // crt_hit; i is the ray's index (its predicted treelet with SEED).
-template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE>
+// WALK: 0 = binary traversal nodes, 1 = 4-wide nodes, 2 = compressed 4-wide nodes.
+template <bool ANY, bool WT, int STACK, bool SEED, int WALK>
 __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t i, const float4 r0, const float4 r1) {
     RayCtx r;
     r.o = make_float3(r0.x, r0.y, r0.z);
@@ -285,22 +287,66 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
             }
         }
     };
+    // A leaf reached through a compressed node, whose box there only
+    // encloses the exact one: with the shader's predicate the leaf's exact box
+    // (from its triangle) must pass the shader's slab test first, so that the
+    // tested triangles are the shader's.
+    auto test_leaf_exact = [&](uint32_t L) {
+        if (L >= n_leaves) { corrupt = true; return; }
+        const float4* t = p.xtri + 3 * static_cast<size_t>(L);
+        const float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
+        const float4 mn = make_float4(min_std(a.x, min_std(b.x, c.x)), min_std(a.y, min_std(b.y, c.y)),
+                                      min_std(a.z, min_std(b.z, c.z)), 0.f);
+        const float4 mx = make_float4(max_std(a.x, max_std(b.x, c.x)), max_std(a.y, max_std(b.y, c.y)),
+                                      max_std(a.z, max_std(b.z, c.z)), 0.f);
+        float te;
+        if (!slab<false>(r, mn, mx, 0.f, te) || te > bound) return;
+        test_leaf(L);
+    };
     // Same walk over the 4-wide nodes: up to four children tested per fetch,
     // leaves tested at once, internal hits ordered by entry distance with a
     // 4-input sorting network; the nearest is entered, the rest pushed.
+    // Compressed nodes (WALK 2, 64 bytes) hold each child box as 8-bit
+    // offsets from the node's origin in steps of a power of two per axis,
+    // rounded outward, decoded as origin + q * step (both exact but the add).
     auto walk4 = [&](uint32_t cur) {
         int sp = 0;
         while (cur != 0xFFFFFFFFu) {
             if (cur >= n_leaves - 1) { corrupt = true; break; }
             ++fetched;
-            const float4* nd = p.wide4 + 8 * static_cast<size_t>(cur);
-            const float4 qnx = __ldg(nd), qny = __ldg(nd + 1), qnz = __ldg(nd + 2);
-            const float4 qxx = __ldg(nd + 3), qxy = __ldg(nd + 4), qxz = __ldg(nd + 5);
-            const uint4 qr = __ldg(reinterpret_cast<const uint4*>(nd + 6));
-            const float nx[4] = {qnx.x, qnx.y, qnx.z, qnx.w}, ny[4] = {qny.x, qny.y, qny.z, qny.w};
-            const float nz[4] = {qnz.x, qnz.y, qnz.z, qnz.w}, xx[4] = {qxx.x, qxx.y, qxx.z, qxx.w};
-            const float xy[4] = {qxy.x, qxy.y, qxy.z, qxy.w}, xz[4] = {qxz.x, qxz.y, qxz.z, qxz.w};
-            const uint32_t rf[4] = {qr.x, qr.y, qr.z, qr.w};
+            float nx[4], ny[4], nz[4], xx[4], xy[4], xz[4];
+            uint32_t rf[4];
+            if (WALK == 2) {
+                const uint4* nd = p.cwide + 4 * static_cast<size_t>(cur);
+                const uint4 h = __ldg(nd), q0 = __ldg(nd + 1), q1 = __ldg(nd + 2), qr = __ldg(nd + 3);
+                const float ox = __uint_as_float(h.x), oy = __uint_as_float(h.y), oz = __uint_as_float(h.z);
+                // step 2^e per axis, e biased by 127 in the low three bytes of h.w
+                const float sx = __uint_as_float((h.w & 0xFFu) << 23), sy = __uint_as_float(((h.w >> 8) & 0xFFu) << 23);
+                const float sz = __uint_as_float(((h.w >> 16) & 0xFFu) << 23);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int sh = 8 * c;
+                    nx[c] = ox + static_cast<float>((q0.x >> sh) & 0xFFu) * sx;
+                    ny[c] = oy + static_cast<float>((q0.y >> sh) & 0xFFu) * sy;
+                    nz[c] = oz + static_cast<float>((q0.z >> sh) & 0xFFu) * sz;
+                    xx[c] = ox + static_cast<float>((q0.w >> sh) & 0xFFu) * sx;
+                    xy[c] = oy + static_cast<float>((q1.x >> sh) & 0xFFu) * sy;
+                    xz[c] = oz + static_cast<float>((q1.y >> sh) & 0xFFu) * sz;
+                }
+                rf[0] = qr.x; rf[1] = qr.y; rf[2] = qr.z; rf[3] = qr.w;
+            } else {
+                const float4* nd = p.wide4 + 8 * static_cast<size_t>(cur);
+                const float4 qnx = __ldg(nd), qny = __ldg(nd + 1), qnz = __ldg(nd + 2);
+                const float4 qxx = __ldg(nd + 3), qxy = __ldg(nd + 4), qxz = __ldg(nd + 5);
+                const uint4 qr = __ldg(reinterpret_cast<const uint4*>(nd + 6));
+                nx[0] = qnx.x; nx[1] = qnx.y; nx[2] = qnx.z; nx[3] = qnx.w;
+                ny[0] = qny.x; ny[1] = qny.y; ny[2] = qny.z; ny[3] = qny.w;
+                nz[0] = qnz.x; nz[1] = qnz.y; nz[2] = qnz.z; nz[3] = qnz.w;
+                xx[0] = qxx.x; xx[1] = qxx.y; xx[2] = qxx.z; xx[3] = qxx.w;
+                xy[0] = qxy.x; xy[1] = qxy.y; xy[2] = qxy.z; xy[3] = qxy.w;
+                xz[0] = qxz.x; xz[1] = qxz.y; xz[2] = qxz.z; xz[3] = qxz.w;
+                rf[0] = qr.x; rf[1] = qr.y; rf[2] = qr.z; rf[3] = qr.w;
+            }
             const float kInf = __int_as_float(0x7F800000);
             float ht[4];
             uint32_t hr[4];
@@ -314,7 +360,8 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
                     continue;
                 if (te > bound) continue;
                 if (rf[c] & kLeafRef) {
-                    test_leaf(rf[c] & ~kLeafRef);
+                    if (WALK == 2 && !WT) test_leaf_exact(rf[c] & ~kLeafRef);
+                    else test_leaf(rf[c] & ~kLeafRef);
                 } else {
                     ht[c] = te;
                     hr[c] = rf[c];
@@ -358,7 +405,7 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
         float te;
         if (ref == skip || !slab<WT>(r, mn, mx, grow, te) || te > bound) return;
         if (ref & kLeafRef) test_leaf(ref & ~kLeafRef);
-        else if (WIDE) walk4(ref);   // the root has depth 0, so it is a 4-wide node
+        else if (WALK != 0) walk4(ref);   // the root has depth 0, so it is a 4-wide node
         else walk(ref, skip);
     };
     constexpr uint32_t kNoSkip = 0xFFFFFFFFu;  // never a reference: leaf indices stay below 2^30
@@ -394,11 +441,11 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
 }
 
 // Ray i of p.rays into p.hits[i].
-template <bool ANY, bool WT, int STACK, bool SEED, bool WIDE>
+template <bool ANY, bool WT, int STACK, bool SEED, int WALK>
 __device__ __forceinline__ void trace_ray(const TraceParams& p, const uint32_t i) {
     const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
     const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
-    reinterpret_cast<uint4*>(p.hits)[i] = trace_one<ANY, WT, STACK, SEED, WIDE>(p, i, r0, r1);
+    reinterpret_cast<uint4*>(p.hits)[i] = trace_one<ANY, WT, STACK, SEED, WALK>(p, i, r0, r1);
 }
 
 // getRay (raytracer.glsl:92-100): pos = texel / size, direction =
