@@ -249,6 +249,24 @@ def run_ours(args):
             kev[k][1].record(stream)
     torch.cuda.synchronize()
     p_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+    # the same primary trace over the other node formats (same hits)
+    node_formats = {"binary_64B": {"ms": round(p_ms, 4), "node_fetches_per_ray": round(p_visited / n_rays, 2)}}
+    hp_alt = torch.empty_like(hp)
+    for fname, fflag in (("wide4_128B", crt.TRACE_WIDE), ("compressed4_64B", crt.TRACE_COMPRESSED)):
+        ctx.trace(bvh, rays, flags | fflag | crt.TRACE_STATS, out=hp_alt)
+        f_visited, _ = ctx.last_trace_stats()
+        fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                l2_flush.zero_()
+                fev[k][0].record(stream)
+                ctx.trace(bvh, rays, flags | fflag, out=hp_alt)
+                fev[k][1].record(stream)
+        torch.cuda.synchronize()
+        node_formats[fname] = {"ms": round(statistics.mean(a.elapsed_time(b) for a, b in fev), 4),
+                               "node_fetches_per_ray": round(f_visited / n_rays, 2),
+                               "identical_hits": bool(torch.equal(hp_alt.view(torch.int32), hp.view(torch.int32)))}
+    del hp_alt
 
     # ---- mesh input: the scene's indexed mesh to TriangleGPU records on the GPU
     from realtimeraytracing_gb300 import scenes as S
@@ -362,6 +380,7 @@ def run_ours(args):
                          "alg_bytes_per_launch": int(alg_bytes),
                          "node_fetches_per_pixel": round(visited / n_rays, 2),
                          "tris_per_pixel": round(tested / n_rays, 2)},
+            "primary_trace_node_formats": node_formats,
             "primary_trace_kernel": {"ms": round(p_ms, 4), "mrays_s": round(n_rays / (p_ms * 1e-3) / 1e6, 1),
                                      "node_fetches_per_ray": round(p_visited / n_rays, 2),
                                      "tris_per_ray": round(p_tested / n_rays, 2)},
@@ -630,6 +649,12 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
     t_plain = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=plain), reps)
     ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=plain)
     f_plain, _ = ctx.last_trace_stats()
+    # the other node formats on the same incoherent rays (same hits)
+    incoherent_formats = {}
+    for fname, fflag in (("wide4_128B", crt.TRACE_WIDE), ("compressed4_64B", crt.TRACE_COMPRESSED)):
+        t_f = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | fflag, out=seeded), reps)
+        incoherent_formats[fname] = {"mrays_s": round(n / (t_f * 1e-3) / 1e6, 1), "vs_binary": round(t_plain / t_f, 3),
+                                     "identical_hits": bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))}
     pred = crt.Predictor(ctx, bvh, seed=1, miss_threshold=0.9)
     truth = pred.classes_of_hits(plain)
     hit = truth != 127
@@ -680,6 +705,7 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
         "workload": "clustered soup 4,194,304 tris (256 clusters); 8,388,608 cosine bounce rays from 2048x2048 primary hits",
         "build_ms": round(build_ms, 3),
         "plain_mrays_s": round(n / t_plain / 1e3, 1),
+        "node_formats": incoherent_formats,
         "seeded_mrays_s": round(n / t_seeded / 1e3, 1),
         "speedup": round(t_plain / t_seeded, 3),
         "infer_ms": round(t_infer, 3),
