@@ -852,9 +852,11 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     unsigned long long* stamp = reinterpret_cast<unsigned long long*>(iters_out + 2);
     if (blockIdx.x == 0 && threadIdx.x == 0) stamp[0] = global_ns();
     int iter = 0;
+    bool tail = false;
     for (;; ++iter) {
         const uint2 cur = __ldcg(it + iter);
         if (cur.x <= 1u) break;
+        if (cur.x <= ploc_own(R)) { tail = true; break; }  // every block reads the same record
         const float4* cin = (iter & 1) ? cb : ca;
         float4* cout = (iter & 1) ? ca : cb;
         unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
@@ -872,14 +874,53 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
         if (!grid_barrier(bar, err, spin_limit)) return;
         if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
     }
+    if (tail) {
+        // The remaining iterations fit in one tile each (the last few hundred
+        // clusters, which merge a few pairs per iteration): block 0 runs them
+        // alone, with block barriers only, while the others wait once.
+        if (blockIdx.x == 0) {
+            for (;; ++iter) {
+                __syncthreads();  // the previous iteration's clusters and record are written
+                const uint2 cur = __ldcg(it + iter);
+                if (cur.x <= 1u) break;
+                if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); break; }
+                const float4* cin = (iter & 1) ? cb : ca;
+                float4* cout = (iter & 1) ? ca : cb;
+                unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
+                unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
+                ploc_tile<TILE, BLOCK, MAXR>(S, 0u, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur,
+                                             lb_next, err, spin_limit);
+            }
+            if (threadIdx.x == 0) iters_out[0] = static_cast<uint32_t>(iter);
+        }
+        if (!grid_barrier(bar, err, spin_limit)) return;
+        iter = static_cast<int>(__ldcg(iters_out));
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         iters_out[0] = static_cast<uint32_t>(iter);
         stamp[1] = global_ns();
     }
     // DFS layout: top-down levels, last iteration's nodes first, into dfs
     // (the first cluster buffer, free now), then every position in order.
+    // The top levels hold a few nodes each: block 0 lays them out alone, with
+    // block barriers between levels, and one grid barrier ends that part.
     uint32_t* dfs = reinterpret_cast<uint32_t*>(ca);
-    for (int k = iter - 1; k >= 0; --k) {
+    constexpr uint32_t kSmallLevel = 4 * BLOCK;
+    int k = iter - 1;
+    int k_small = k;
+    while (k_small >= 0 && __ldcg(it + k_small + 1).y - __ldcg(it + k_small).y <= kSmallLevel) --k_small;
+    if (k_small < k) {
+        if (blockIdx.x == 0) {
+            for (int kk = k; kk > k_small; --kk) {
+                const uint32_t lo = __ldcg(it + kk).y, hi = __ldcg(it + kk + 1).y;
+                for (uint32_t X = lo + threadIdx.x; X < hi; X += BLOCK) layout_down(X, node_kids, pf, N, dfs, err);
+                __syncthreads();
+            }
+        }
+        if (!grid_barrier(bar, err, spin_limit)) return;
+        k = k_small;
+    }
+    for (; k >= 0; --k) {
         const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
         for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
             layout_down(X, node_kids, pf, N, dfs, err);
