@@ -159,6 +159,7 @@ struct crt_ctx {
     DevBuf shade_models, shade_materials, shade_rays, shade_hits, image;  // crt_shade / crt_render_frame
     DevBuf refit_state;  // crt::RefitState
     DevBuf xtri_sorted;  // leaf records in sorted order until the layout moves them
+    DevBuf mesh_vertices, mesh_indices, mesh_out;  // crt_triangles_from_indexed staging
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -272,7 +273,8 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->clus_b, &x->iters, &x->ploc_lb, &x->cam, &x->rays_in, &x->hits_out, &x->rays_out,
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
                       &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
-                      &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state, &x->xtri_sorted};
+                      &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state, &x->xtri_sorted,
+                      &x->mesh_vertices, &x->mesh_indices, &x->mesh_out};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -1845,15 +1847,15 @@ crt_status crt_triangles_from_indexed(crt_ctx* x, const float* vertices, uint32_
     if (n_triangles == 0) return CRT_OK;
     const void* d_v = nullptr;
     const void* d_i = nullptr;
-    CRT_TRY(stage_in(x, x->rays_in, vertices, 12ull * n_vertices, &d_v));
-    CRT_TRY(stage_in(x, x->hits_out, indices, 12ull * n_triangles, &d_i));
+    CRT_TRY(stage_in(x, x->mesh_vertices, vertices, 12ull * n_vertices, &d_v));
+    CRT_TRY(stage_in(x, x->mesh_indices, indices, 12ull * n_triangles, &d_i));
     if (!aligned(d_v, 4) || !aligned(d_i, 4))
         return fail(CRT_ERR_INVALID_ARG, "crt_triangles_from_indexed: vertices and indices must be 4-byte aligned");
     const bool dev_out = is_device_ptr(out);
     crt_triangle* d_out = out;
     if (!dev_out) {
-        CRT_TRY(x->tris_in.reserve(sizeof(crt_triangle) * static_cast<size_t>(n_triangles)));
-        d_out = x->tris_in.as<crt_triangle>();
+        CRT_TRY(x->mesh_out.reserve(sizeof(crt_triangle) * static_cast<size_t>(n_triangles)));
+        d_out = x->mesh_out.as<crt_triangle>();
     } else if (!aligned(out, 16)) {
         return fail(CRT_ERR_INVALID_ARG, "crt_triangles_from_indexed: out must be 16-byte aligned");
     }
