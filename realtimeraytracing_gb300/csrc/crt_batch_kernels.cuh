@@ -280,6 +280,39 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
         __syncthreads();
         if (s_running == 0) break;
         if (static_cast<uint32_t>(iter) >= max_iters) { raise_error(err, kDevIterLimit); return; }
+        // Once every running scene fits in one tile, each block finishes whole
+        // scenes alone (their remaining iterations, one tile each, with block
+        // barriers only) and one grid barrier ends the PLOC phase.
+        if (threadIdx.x == 0) {
+            uint32_t big = 0;
+            for (uint32_t k = 0; k < n_scenes; ++k) big += s_n[k] > ploc_own(R) ? 1u : 0u;
+            s_tile = big;
+        }
+        __syncthreads();
+        if (s_tile == 0u) {
+            for (uint32_t sc = blockIdx.x; sc < n_scenes; sc += gridDim.x) {
+                if (s_n[sc] <= 1u) continue;  // finished before this iteration
+                const BatchScene B = scenes[sc];
+                for (uint32_t k = static_cast<uint32_t>(iter);; ++k) {
+                    __syncthreads();  // the previous iteration's clusters and record are written
+                    const uint2 cur = __ldcg(it + B.it_off + k);
+                    if (cur.x <= 1u) {
+                        if (threadIdx.x == 0) scenes[sc].iters = k;
+                        break;
+                    }
+                    if (k >= max_iters) { raise_error(err, kDevIterLimit); break; }
+                    float4* cin = ((k & 1) ? cb : ca) + 2 * static_cast<size_t>(B.tri_off);
+                    float4* cout = ((k & 1) ? ca : cb) + 2 * static_cast<size_t>(B.tri_off);
+                    unsigned long long* lb_cur = lookback + static_cast<size_t>(k & 1) * lb_cap + B.lb_off;
+                    unsigned long long* lb_next = lookback + static_cast<size_t>((k + 1) & 1) * lb_cap + B.lb_off;
+                    ploc_tile<TILE, BLOCK, MAXR>(S, 0u, cur, static_cast<int>(k), cin, cout,
+                                                 node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off,
+                                                 it + B.it_off, B.n_tris, R, lb_cur, lb_next, err, spin_limit);
+                }
+            }
+            if (!grid_barrier(bar, err, spin_limit)) return;
+            break;
+        }
         if (threadIdx.x == 0) {
             uint32_t run = 0;
             for (uint32_t k = 0; k < n_scenes; ++k) {
