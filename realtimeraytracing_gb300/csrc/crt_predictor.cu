@@ -137,13 +137,18 @@ __device__ __forceinline__ uint32_t lane_addr(uint32_t tbase, uint32_t col) {
 
 // ---------------------------------------------------------- inference
 // Persistent: each CTA (128 threads, one ray per thread) loads the weights
-// once and walks 128-ray tiles.  TMEM: D1 cols 0-63, D2 64-127, logits 128-255.
-constexpr int kInferSmemUsed = 64 * 32 * 2 + 64 * 64 * 2 + 128 * 64 * 2 + 128 * 32 * 2 + 2 * 128 * 64 * 2 +
+// once and walks 128-ray tiles.  TMEM (128 columns): D1 cols 0-63, D2 64-127,
+// then the logits over both once H2 is out of D2.  Shared memory: weights, X,
+// and one activation buffer that holds H1 and then H2 (H1 is dead once the
+// second GEMM has completed).
+constexpr int kInferSmemUsed = 64 * 32 * 2 + 64 * 64 * 2 + 128 * 64 * 2 + 128 * 32 * 2 + 128 * 64 * 2 +
                                (64 + 64 + 128) * 4 + 64;
-// Requested size caps residency at two CTAs per SM, the number whose
-// 256-column TMEM allocations fit the SM's 512 columns together.
-constexpr int kInferSmem = 100 * 1024;
-static_assert(kInferSmemUsed <= kInferSmem, "inference tile layout");
+// Requested size caps residency at four CTAs per SM, the number whose
+// 128-column TMEM allocations fit the SM's 512 columns together.
+constexpr int kInferSmem = 54 * 1024;
+constexpr int kInferCtasPerSm = 4;
+static_assert(kInferSmemUsed <= kInferSmem && kInferCtasPerSm * kInferSmem <= 228 * 1024 &&
+              (kInferCtasPerSm + 1) * kInferSmem > 228 * 1024, "inference tile layout and residency");
 
 __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bvh_node* nodes, const crt_ray* rays,
                                                     uint32_t n, uint16_t* classes, float miss_threshold, uint32_t* err) {
@@ -153,8 +158,8 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
     unsigned char* sW3 = sW2 + 64 * 64 * 2;
     unsigned char* sX = sW3 + 128 * 64 * 2;
     unsigned char* sH1 = sX + 128 * 32 * 2;
-    unsigned char* sH2 = sH1 + 128 * 64 * 2;
-    float* sB = reinterpret_cast<float*>(sH2 + 128 * 64 * 2);
+    unsigned char* sH2 = sH1;  // H1 is dead once the second GEMM has completed
+    float* sB = reinterpret_cast<float*>(sH1 + 128 * 64 * 2);
     uint32_t* sT = reinterpret_cast<uint32_t*>(sB + 256);
     uint64_t* sM = reinterpret_cast<uint64_t*>(sT + 2);
 
@@ -165,7 +170,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         const float b = i < 64 ? P.master[oB1 + i] : (i < 128 ? P.master[oB2 + i - 64] : P.master[oB3 + i - 128]);
         sB[i] = b;
     }
-    if (threadIdx.x < 32) { tc::tmem_alloc(sT, 256); tc::tmem_relinquish(); }
+    if (threadIdx.x < 32) { tc::tmem_alloc(sT, 128); tc::tmem_relinquish(); }
     if (threadIdx.x == 0) tc::mbar_init(sM, 1);
     Sync sy{sM, 0, err};
     sy.before_mma();
@@ -211,7 +216,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
             store_row8(sH2, 64, tid, c + 8, v + 8);
         }
         sy.before_mma();
-        if (tid == 0) gemm(tb + 128, sH2, sW3, 64, 128, 128);
+        if (tid == 0) gemm(tb + 0, sH2, sW3, 64, 128, 128);  // logits over D1 and D2, both read out
         sy.commit_and_wait();
         // Seed the most likely treelet unless the miss class holds at least
         // `miss_threshold` of the probability mass.
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         int bc = 0;
         for (int c = 0; c < 128; c += 16) {
             float v[16];
-            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+            tc::tmem_ld16(lane_addr(tb, c), v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const float l = v[j] + sB[128 + c + j];
@@ -231,7 +236,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         float sum = 0.f;
         for (int c = 0; c < 128; c += 16) {
             float v[16];
-            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+            tc::tmem_ld16(lane_addr(tb, c), v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - lmax);
         }
@@ -242,7 +247,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x < 32) tc::tmem_dealloc(tb, 256);
+    if (threadIdx.x < 32) tc::tmem_dealloc(tb, 128);
 }
 
 // ------------------------------------------------------------ training
@@ -782,7 +787,8 @@ cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const c
         attr = true;
     }
     const uint32_t tiles = (n + 127) / 128;
-    const uint32_t grid = tiles < 2u * kNumSms ? tiles : 2u * kNumSms;
+    const uint32_t cap = static_cast<uint32_t>(pred::kInferCtasPerSm) * kNumSms;
+    const uint32_t grid = tiles < cap ? tiles : cap;
     if (grid == 0) return cudaSuccess;
     pred::infer_kernel<<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold, err);
     return cudaGetLastError();
