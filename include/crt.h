@@ -217,6 +217,14 @@ crt_status crt_bvh_copy_codes(crt_ctx* ctx, const crt_bvh* bvh, uint32_t* dst);
 crt_status crt_bvh_copy_perm(crt_ctx* ctx, const crt_bvh* bvh, uint32_t* dst);
 crt_status crt_last_build_stats(crt_ctx* ctx, crt_build_stats* stats);
 
+/* Failure detection check: one bounded device-side wait on a flag in context
+ * memory, the same bounded spin every look-back and grid barrier uses.  With
+ * set_flag != 0 the flag is set before the wait (CRT_OK); with set_flag == 0
+ * nothing sets it and the wait gives up after spin_limit rounds
+ * (CRT_ERR_DEVICE_TIMEOUT, the context stays usable).  spin_limit 0 = the
+ * context's limit. */
+crt_status crt_selftest_wait(crt_ctx* ctx, int set_flag, uint32_t spin_limit);
+
 /* ---- rays ------------------------------------------------------------- */
 /* Primary rays of getRay (raytracer.glsl:92-100) for a width x height image:
  * ray (x, y) is stored at y * width + x and uses pos = (x / width, y / height). */

@@ -50,7 +50,7 @@ EXPORTS = [
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
     "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_obj_parse",
-    "crt_triangles_from_indexed",
+    "crt_triangles_from_indexed", "crt_selftest_wait",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -141,6 +141,7 @@ def lib():
             "crt_refit": ([vp, vp, vp, u32, vp, u32], i32),
             "crt_obj_parse": ([C.c_char_p, C.c_size_t, vp, u32, vp, u32, vp], i32),
             "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
+            "crt_selftest_wait": ([vp, i32, u32], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -482,6 +483,10 @@ class Context:
 
     def sync(self):
         _check(lib().crt_sync(self.handle))
+
+    def selftest_wait(self, set_flag: bool, spin_limit: int = 0):
+        """crt_selftest_wait: one bounded device wait on a flag (set or never set)."""
+        _check(lib().crt_selftest_wait(self.handle, 1 if set_flag else 0, spin_limit))
 
     def build(self, tris, n_tris=None, models=None, n_buffer=None) -> Bvh:
         """cr::BVH::BVH(nbTriangles, unsortedTriangles, meshesInTheScene)."""

@@ -160,6 +160,7 @@ struct crt_ctx {
     DevBuf refit_state;  // crt::RefitState
     DevBuf xtri_sorted;  // leaf records in sorted order until the layout moves them
     DevBuf mesh_vertices, mesh_indices, mesh_out;  // crt_triangles_from_indexed staging
+    DevBuf probe_flag;                             // crt_selftest_wait
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -274,7 +275,7 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
                       &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
                       &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state, &x->xtri_sorted,
-                      &x->mesh_vertices, &x->mesh_indices, &x->mesh_out};
+                      &x->mesh_vertices, &x->mesh_indices, &x->mesh_out, &x->probe_flag};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -282,6 +283,18 @@ crt_status crt_destroy(crt_ctx* x) {
     if (x->stream) cudaStreamDestroy(x->stream);
     delete x;
     return CRT_OK;
+}
+
+crt_status crt_selftest_wait(crt_ctx* x, int set_flag, uint32_t spin_limit) {
+    if (!x) return fail(CRT_ERR_INVALID_ARG, "null context");
+    CRT_CUDA(cudaSetDevice(x->device));
+    CRT_TRY(x->probe_flag.reserve(4));
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    CRT_CUDA(cudaMemsetAsync(x->probe_flag.p, set_flag ? 0xFF : 0, 4, x->stream));
+    crt::launch_wait_probe(x->probe_flag.as<unsigned int>(), spin_limit ? spin_limit : x->cfg.spin_limit,
+                           x->err.as<uint32_t>(), x->stream);
+    CRT_CUDA(cudaGetLastError());
+    return x->check_device_error();
 }
 
 crt_status crt_sync(crt_ctx* x) {

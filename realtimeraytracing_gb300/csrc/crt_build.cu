@@ -1193,6 +1193,19 @@ cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uin
                                        dim3(grid), dim3(256), args, 0, s);
 }
 
+// A wait on a flag, bounded like every look-back and grid-barrier wait: on
+// exhaustion the error word records the timeout and the kernel returns.
+__global__ void wait_probe_kernel(const unsigned int* flag, uint32_t spin_limit, uint32_t* err) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    SpinBound spin(spin_limit);
+    while (ld_acquire_u32(flag) == 0u)
+        if (!spin.step()) { raise_error(err, kDevTimeout); return; }
+}
+
+void launch_wait_probe(const unsigned int* flag, uint32_t spin_limit, uint32_t* err, cudaStream_t s) {
+    wait_probe_kernel<<<1, 32, 0, s>>>(flag, spin_limit, err);
+}
+
 void launch_single_leaf(const float4* node_box, crt_bvh_node* out, LeafOut lv, cudaStream_t s) {
     single_leaf_kernel<<<1, 1, 0, s>>>(node_box, out, lv);
 }

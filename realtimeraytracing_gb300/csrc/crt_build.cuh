@@ -228,6 +228,9 @@ bool obj_parse(const char* text, size_t len, float* vertices, uint64_t vert_cap,
 void launch_indexed(const float* vertices, uint32_t n_vertices, const uint32_t* indices, uint32_t n_triangles,
                     uint32_t model_id, crt_triangle* out, uint32_t* err, cudaStream_t s);
 
+// One bounded wait on *flag (crt_selftest_wait); a timeout sets kDevTimeout.
+void launch_wait_probe(const unsigned int* flag, uint32_t spin_limit, uint32_t* err, cudaStream_t s);
+
 // Sets the message crt_last_error_string() returns on the calling thread.
 void set_last_error(const char* msg);
 

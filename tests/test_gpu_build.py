@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from realtimeraytracing_gb300 import crt
 from realtimeraytracing_gb300 import scenes as S
 
 pytestmark = pytest.mark.gpu
@@ -136,3 +137,23 @@ def test_multi_launch_build_matches(ctx, n):
     tris = S.uniform_soup(n, seed=60 + n)
     _check_build(c, tris, n, S.identity_models(1))
     c.close()
+
+
+def test_bounded_wait_times_out_and_the_context_stays_usable(ctx):
+    """A device wait on a flag that nothing sets gives up after its bound and
+    reports CRT_ERR_DEVICE_TIMEOUT (no trap, no hang); the same wait on a set
+    flag passes; builds and traces on the context still match the oracle."""
+    ctx.selftest_wait(True, spin_limit=1 << 12)
+    with pytest.raises(crt.CrtError) as e:
+        ctx.selftest_wait(False, spin_limit=1 << 12)
+    assert e.value.status == 4  # CRT_ERR_DEVICE_TIMEOUT
+    tris = S.uniform_soup(3000, seed=17)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    ref = O.build_bvh(tris, 3000, models)
+    assert np.array_equal(bvh.nodes().view(np.uint32), ref["nodes"].view(np.uint32))
+    rays = S.sphere_rays(2000, seed=8)
+    h = ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)
+    rh, _ = O.trace(ref["nodes"], tris, models, rays, crt.TRI_WATERTIGHT)
+    assert np.array_equal(h.view(np.uint32), rh.view(np.uint32))
+    bvh.free()

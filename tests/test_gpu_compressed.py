@@ -77,3 +77,15 @@ def test_compressed_frame(ctx):
     np.testing.assert_array_equal(cp.view(np.uint32), hp.view(np.uint32))
     np.testing.assert_array_equal(cs.view(np.uint32)[:, 0] == crt.MISS, hs.view(np.uint32)[:, 0] == crt.MISS)
     bvh.free()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 33, 1025])
+def test_compressed_small_trees(ctx, n):
+    tris = S.uniform_soup(n, seed=40 + n, edge_lo=0.05, edge_hi=0.3)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    rays = S.sphere_rays(4096, seed=n)
+    for flags in (crt.TRI_REFERENCE, crt.TRI_WATERTIGHT):
+        ref, _ = O.trace(bvh.nodes(), tris, models, rays, flags)
+        _cmp_hits(ctx.trace(bvh, rays, flags | crt.TRACE_COMPRESSED), ref)
+    bvh.free()
