@@ -227,9 +227,13 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
     __shared__ unsigned long long s_wsum[WARPS];
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_seg[SEG ? RADIX + 1 : 1];
+    __shared__ uint32_t s_timeout;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    if (threadIdx.x == 0) {
+        s_tile = atomicAdd(ticket, 1u);
+        s_timeout = 0u;
+    }
     for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) (&s_whist[0][0])[i] = 0u;
     if (SEG)
         for (int i = threadIdx.x; i <= RADIX; i += BLOCK) s_seg[i] = (static_cast<uint32_t>(i) <= n_seg) ? seg_off[i] : 0xFFFFFFFFu;
@@ -327,7 +331,11 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
                 }
                 if (done) break;
                 k -= q;
-                if (q < kLbWindow && !spin.step()) { raise_error(err, kDevTimeout); break; }
+                if (q < kLbWindow && !spin.step()) {
+                    raise_error(err, kDevTimeout);
+                    s_timeout = 1u;
+                    break;
+                }
             }
             st_relaxed_u32(lookback + static_cast<size_t>(tile) * RADIX + d, kLbPrefix | (excl + total));
         }
@@ -337,6 +345,7 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
         s_adj[d] = (incl_g - gh) + excl - (incl_a - a);
     }
     __syncthreads();
+    if (s_timeout) return;  // the prefix is incomplete: write nothing
     // Tile-local sorted slot of each element.
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
@@ -353,6 +362,11 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
         if (i < tile_n) {
             const uint32_t x = s_buf[i];
             dst[k] = s_adj[SEG ? digit_of(0u, x) : digit_of(x, 0u)] + i;
+            if (dst[k] >= n) {  // only a corrupt histogram gets here
+                raise_corrupt(err, 17, tile, dst[k]);
+                dst[k] = 0xFFFFFFFFu;
+                continue;
+            }
             if (SEG) vals_out[dst[k]] = x;
             else keys_out[dst[k]] = x;
         }
@@ -365,7 +379,7 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
 #pragma unroll
     for (int k = 0; k < KPT; ++k) {
         const uint32_t i = k * BLOCK + threadIdx.x;
-        if (i < tile_n) {
+        if (i < tile_n && dst[k] != 0xFFFFFFFFu) {
             if (SEG) keys_out[dst[k]] = s_buf[i];
             else vals_out[dst[k]] = s_buf[i];
         }
