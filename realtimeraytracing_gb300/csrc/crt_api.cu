@@ -850,9 +850,17 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
     if (n_rays == 0) return CRT_OK;
     const crt_ray* d_rays = rays;
     if (!is_device_ptr(rays)) {
-        CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
-        CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, rays, sizeof(crt_ray) * n_rays, cudaMemcpyHostToDevice, x->stream));
-        d_rays = x->rays_in.as<crt_ray>();
+        // Page-locked host rays are read in place by the trace kernel when it
+        // reads each ray once, in order; reordered or predicted traces read
+        // them more than once and out of order, so those copy them in first.
+        const bool once = !(flags & (CRT_TRACE_SORT_RAYS | CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_USE_PREDICTOR));
+        if (void* m = once ? mapped_host_ptr(const_cast<crt_ray*>(rays)) : nullptr) {
+            d_rays = static_cast<const crt_ray*>(m);
+        } else {
+            CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
+            CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, rays, sizeof(crt_ray) * n_rays, cudaMemcpyHostToDevice, x->stream));
+            d_rays = x->rays_in.as<crt_ray>();
+        }
     }
     bool dev_out = is_device_ptr(hits);
     crt_hit* d_hits = hits;

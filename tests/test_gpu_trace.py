@@ -215,3 +215,18 @@ def test_trace_into_page_locked_host_memory(ctx, config0):
     ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=pinned)
     _cmp_hits(pinned.numpy(), ref)
     _cmp_hits(ctx.trace(bvh, rays, crt.TRI_WATERTIGHT), ref)
+
+
+@pytest.mark.parametrize("flags", [crt.TRI_REFERENCE, crt.TRI_WATERTIGHT | crt.TRACE_ANY,
+                                   crt.TRI_WATERTIGHT | crt.SORT_RAYS])
+def test_trace_from_page_locked_host_rays(ctx, config0, flags):
+    """Page-locked host rays are read in place by the trace kernel (in-order
+    traces) or copied in first (reordered traces): the oracle's hits either way."""
+    torch = pytest.importorskip("torch")
+    tris, models, cam, w, h, bvh = config0
+    rays = O.raygen(cam, w, h)
+    ref, _ = O.trace(bvh.nodes(), tris, models, rays, flags & (crt.TRI_WATERTIGHT | crt.TRACE_ANY))
+    pinned_rays = torch.from_numpy(rays).pin_memory()
+    pinned_hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, pin_memory=True)
+    ctx.trace(bvh, pinned_rays, flags, out=pinned_hits)
+    _cmp_hits(pinned_hits.numpy(), ref, any_hit=bool(flags & crt.TRACE_ANY))
