@@ -1023,6 +1023,18 @@ crt_status stage_in(crt_ctx* x, DevBuf& buf, const void* src, size_t bytes, cons
     return CRT_OK;
 }
 
+// As stage_in, for inputs a kernel reads once, in order: page-locked host
+// memory is then read in place over the CPU-GPU link instead of copied.
+crt_status stage_in_once(crt_ctx* x, DevBuf& buf, const void* src, size_t bytes, const void** dev) {
+    if (!is_device_ptr(src)) {
+        if (void* m = mapped_host_ptr(const_cast<void*>(src))) {
+            *dev = m;
+            return CRT_OK;
+        }
+    }
+    return stage_in(x, buf, src, bytes, dev);
+}
+
 crt_status predictor_targets(crt_ctx* x, crt_predictor* pr) {
     crt_bvh* b = pr->bvh;
     CRT_TRY(pr->tri_class.reserve(b->n));
@@ -1770,9 +1782,9 @@ crt_status crt_shade(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, const cr
     CRT_TRY(shade_setup(x, b, sh, &sp));
     if (n == 0) return CRT_OK;
     const void* d_hits = nullptr;
-    CRT_TRY(stage_in(x, x->shade_hits, hits, sizeof(crt_hit) * n, &d_hits));
+    CRT_TRY(stage_in_once(x, x->shade_hits, hits, sizeof(crt_hit) * n, &d_hits));
     const void* d_rays = nullptr;
-    if (sp.flags & CRT_SHADE_BVH) CRT_TRY(stage_in(x, x->shade_rays, rays, sizeof(crt_ray) * n, &d_rays));
+    if (sp.flags & CRT_SHADE_BVH) CRT_TRY(stage_in_once(x, x->shade_rays, rays, sizeof(crt_ray) * n, &d_rays));
     if (!aligned(d_hits, 16) || !aligned(d_rays, 16))
         return fail(CRT_ERR_INVALID_ARG, "crt_shade: rays and hits must be 16-byte aligned");
     bool copy_out = false;

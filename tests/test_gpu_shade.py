@@ -90,6 +90,9 @@ def test_render_paths_and_outputs_agree(ctx, scene):
     hits = ctx.trace(bvh, rays)
     _eq(ctx.shade(bvh, rays, hits, models=models, materials=MATERIALS, shade_flags=flags, bvh_depth=3), ref,
         "crt_shade")
+    # page-locked host rays and hits, read in place
+    _eq(ctx.shade(bvh, torch.from_numpy(rays).pin_memory(), torch.from_numpy(hits).pin_memory(), models=models,
+                  materials=MATERIALS, shade_flags=flags, bvh_depth=3), ref, "crt_shade, page-locked inputs")
 
 
 def test_no_models_or_materials(ctx, scene):
