@@ -33,6 +33,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -81,7 +82,9 @@ class ClockSampler:
         self.path = None
 
     def start(self):
-        out_dir = os.path.join(ROOT, "gpurun_out")
+        # the raw samples go to CRT_CLOCKS_DIR (kept beside the run's other
+        # outputs when set), else to the temporary directory
+        out_dir = os.environ.get("CRT_CLOCKS_DIR") or tempfile.gettempdir()
         os.makedirs(out_dir, exist_ok=True)
         self.path = os.path.join(out_dir, f"clocks_bench_{os.getpid()}.csv")
         try:

@@ -81,11 +81,18 @@ int main(void) {
     assert C.sizeof(crt.Shading) == 40 and crt.Shading.bvh_depth.offset == 32
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/srcCommon"), reason="reference checkout not present")
+def _reference_dir():
+    from oracle import oracle as O
+    return O.REFERENCE_DIR
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(_reference_dir(), "srcCommon")),
+                    reason="reference checkout not present")
 def test_adapter_compiles_and_links_against_reference_header(lib, tmp_path):
     gxx = shutil.which("g++")
     tmp = str(tmp_path)
-    inc = ["-I", os.path.join(ROOT, "oracle", "glm_shim"), "-I", "/root/reference/srcCommon/scene/geometry",
+    inc = ["-I", os.path.join(ROOT, "oracle", "glm_shim"), "-I",
+           os.path.join(_reference_dir(), "srcCommon", "scene", "geometry"),
            "-I", os.path.join(ROOT, "include")]
     obj = os.path.join(tmp, "bvh_cuda.o")
     subprocess.run([gxx, "-std=gnu++20", "-O2", "-c", os.path.join(ROOT, "adapter", "bvh_cuda.cpp"), *inc, "-o", obj],

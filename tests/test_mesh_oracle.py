@@ -11,7 +11,9 @@ from oracle import obj_oracle as OO
 from realtimeraytracing_gb300 import crt
 from realtimeraytracing_gb300 import scenes as S
 
-MODELS = "/root/reference/resources/models"
+from oracle import oracle as O
+
+MODELS = os.path.join(O.REFERENCE_DIR, "resources", "models")
 
 
 @pytest.fixture(scope="module", autouse=True)
