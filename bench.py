@@ -703,6 +703,20 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
     keysort_identical = bool(torch.equal(sh.view(torch.int32), plain.index_select(0, sorder).view(torch.int32)))
     info = pred.info()
     pred.free()
+    # the same rays over the treelet-restructured tree (crt_optimize, 2 passes; one call timed)
+    nodes_before = bvh.nodes()
+    oa, ob = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    oa.record(stream)
+    bvh.optimize(2)
+    ob.record(stream)
+    torch.cuda.synchronize()
+    t_optimize = oa.elapsed_time(ob)
+    t_opt_trace = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=seeded), reps)
+    opt_identical = bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
+    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=seeded)
+    f_opt, _ = ctx.last_trace_stats()
+    sah_before, sah_after = sah_cost(nodes_before), sah_cost(bvh.nodes())
     bvh.free()
     return {
         "workload": "clustered soup 4,194,304 tris (256 clusters); 8,388,608 cosine bounce rays from 2048x2048 primary hits",
@@ -732,10 +746,26 @@ def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
                                   "speedup_trace_only": round(t_plain / t_keytrace, 3),
                                   "speedup_with_sort": round(t_plain / (t_keysort + t_keytrace), 3),
                                   "identical_hits": keysort_identical},
+        "treelet_optimized_tree": {"optimize_ms": round(t_optimize, 3), "passes": 2,
+                                   "sah_cost": [round(sah_before, 2), round(sah_after, 2)],
+                                   "mrays_s": round(n / t_opt_trace / 1e3, 1), "vs_built_tree": round(t_plain / t_opt_trace, 3),
+                                   "node_fetches_per_ray": round(f_opt / n, 2), "identical_hits": opt_identical,
+                                   "note": "crt_optimize: treelet restructuring of the built tree (SAH cost = sum of "
+                                           "1.2 x internal + leaf box areas over the root area), then the plain trace"},
         "training": {"passes": passes, "adam_steps": info["steps"], "loss_first": round(losses[0], 4),
                      "loss_last": round(losses[-1], 4), "ms_per_pass": round(train_ms, 2),
                      "samples_per_pass": n // 20},
     }
+
+
+def sah_cost(nodes, ci=1.2):
+    """Surface-area cost of a node array as crt_optimize counts it (internal
+    nodes ci x area, leaves 1 x area), relative to the root's area."""
+    d = nodes[:, 4:7].astype(np.float64) - nodes[:, 0:3]
+    a = 2.0 * (d[:, 0] * d[:, 1] + d[:, 1] * d[:, 2] + d[:, 2] * d[:, 0])
+    u = np.ascontiguousarray(nodes).view(np.uint32)
+    leaf = (u[:, 9] == 0) & (u[:, 10] == 0)
+    return float((np.where(leaf, 1.0, ci) * a).sum() / a[0])
 
 
 def ray_input_keys(torch, rays, box):

@@ -206,6 +206,23 @@ crt_status crt_rebuild(crt_ctx* ctx, crt_bvh* bvh, const crt_triangle* tris, uin
  * crt_predictor_retarget afterwards, as after a rebuild. */
 crt_status crt_refit(crt_ctx* ctx, crt_bvh* bvh, const crt_triangle* tris, uint32_t n_tris,
                      const crt_mesh_model* models, uint32_t n_models);
+/* Treelet restructuring of a built or refit tree (no counterpart in the
+ * reference; Karras & Aila, "Fast Parallel Construction of High-Quality
+ * BVHs", HPG 2013): the same leaves under a tree of lower surface-area cost
+ * (a leaf costs its box area, an internal node 1.2 x its area plus its
+ * children's costs), for faster traces of a tree that is traced many times,
+ * or of a refit tree whose boxes have grown.  Each pass visits every internal
+ * node after its children and rebuilds the 7-leaf treelet under each node
+ * with at least 7 leaves optimally when that lowers its cost; every box is
+ * recomputed with AABB::merge (bvh.cpp:401-413), so the result is one exact
+ * function of the input tree.  passes = 0 only recomputes the boxes and lays
+ * the tree out again.  The node array and the traversal nodes are rewritten
+ * in DFS order (leaf positions change; crt_bvh_copy_perm keeps the build's
+ * sorted order); with CRT_TRI_REFERENCE equal-t ties follow the new tree's
+ * DFS order, watertight hits are unchanged.  A bound predictor needs
+ * crt_predictor_retarget afterwards. */
+#define CRT_OPTIMIZE_MAX_PASSES 16u
+crt_status crt_optimize(crt_ctx* ctx, crt_bvh* bvh, uint32_t passes);
 crt_status crt_bvh_free(crt_bvh* bvh);
 uint32_t crt_bvh_node_count(const crt_bvh* bvh);       /* 2 * n_tris - 1 */
 uint32_t crt_bvh_triangle_count(const crt_bvh* bvh);

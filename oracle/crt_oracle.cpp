@@ -749,3 +749,232 @@ void oracle_refit(crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tri
 }
 
 }  // extern "C"
+
+// ==================================================== treelet restructuring
+// The product's crt_optimize, restated serially: treelet restructuring after
+// Karras & Aila, "Fast Parallel Construction of High-Quality Bounding Volume
+// Hierarchies" (HPG 2013), with the product's fixed rules so that the result
+// is one exact tree.  No counterpart in the reference.
+//
+// Ids: leaves 0..N-1 in DFS order, internal nodes N + their rank in DFS order
+// (the root is N).  Cost model: a leaf costs its box area, an internal node
+// kCi * area + (cost(left) + cost(right)).  One pass visits every internal
+// node children first; at node R it sets R's box (AABB::merge(left, right)),
+// leaf count, height and cost, and if R has at least 7 leaves it forms R's
+// treelet and rebuilds it optimally:
+//   * treelet leaves start as [left, right]; 5 times the one with the largest
+//     area (ordered-key compare; ties: the lowest index) among those that are
+//     internal nodes is replaced in place by its left child and its right
+//     child appended; the replaced nodes (R first) are the treelet's ids;
+//   * area of each subset s of the 7: the union of its members' boxes taken
+//     in increasing index, as AABB::merge(union, member);
+//   * C[{k}] = cost of member k; C[s] = kCi * A[s] + min over p (C[p] +
+//     C[s ^ p]) for p containing the lowest member of s, p != s; the minimum
+//     by (ordered key of the sum, p), so the smallest p wins ties; p is the
+//     left child;
+//   * if C[all] < cost(R) the treelet is rebuilt: internal subsets take the
+//     treelet's ids in pre-order (left first), each gets its union box, C[s],
+//     leaf count and height.
+// Passes repeat over the current tree; the result is laid out in DFS
+// pre-order, left first, as the build lays out its tree.
+namespace {
+
+constexpr float kOptCi = 1.2f;
+
+inline uint32_t ordered_key_f(float v) {
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    if ((b & 0x7FFFFFFFu) == 0u) b = 0u;
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+struct OptTree {
+    uint32_t N = 0;
+    std::vector<Box> box;           // per id
+    std::vector<uint32_t> tri;      // per leaf
+    std::vector<float> cost;        // per id
+    std::vector<uint32_t> nl, height, parent;
+    std::vector<uint32_t> kl, kr;   // per internal id - N
+};
+
+void opt_treelet(OptTree& t, uint32_t R) {
+    const uint32_t N = t.N;
+    uint32_t L[7], I[6];
+    int n = 2;
+    L[0] = t.kl[R - N];
+    L[1] = t.kr[R - N];
+    I[0] = R;
+    for (int e = 0; e < 5; ++e) {
+        int best = -1;
+        uint32_t bk = 0;
+        for (int j = 0; j < n; ++j) {
+            if (L[j] < N) continue;
+            const uint32_t k = ordered_key_f(surface_area(t.box[L[j]]));
+            if (best < 0 || k > bk) { best = j; bk = k; }
+        }
+        const uint32_t X = L[best];
+        L[best] = t.kl[X - N];
+        L[n++] = t.kr[X - N];
+        I[e + 1] = X;
+    }
+    Box U[128];
+    float A[128], Cs[128];
+    uint8_t P[128] = {};
+    for (uint32_t s = 1; s < 128; ++s) {
+        int k0 = 0;
+        while (!((s >> k0) & 1u)) ++k0;
+        Box u = t.box[L[k0]];
+        for (int k = k0 + 1; k < 7; ++k)
+            if ((s >> k) & 1u) u = merge(u, t.box[L[k]]);
+        U[s] = u;
+        A[s] = surface_area(u);
+    }
+    for (int k = 0; k < 7; ++k) Cs[1u << k] = t.cost[L[k]];
+    for (int size = 2; size <= 7; ++size) {
+        for (uint32_t s = 1; s < 128; ++s) {
+            if (__builtin_popcount(s) != size) continue;
+            const uint32_t low = s & (0u - s), rest = s ^ low;
+            uint32_t bp = 0, bkey = 0;
+            float bv = 0.f;
+            bool first = true;
+            for (uint32_t q = 0;; q = (q - rest) & rest) {  // subsets of rest in increasing order
+                if (q == rest) break;
+                const uint32_t p = low | q;
+                const float v = Cs[p] + Cs[s ^ p];
+                const uint32_t key = ordered_key_f(v);
+                if (first || key < bkey) { bp = p; bkey = key; bv = v; first = false; }
+            }
+            P[s] = static_cast<uint8_t>(bp);
+            Cs[s] = kOptCi * A[s] + bv;
+        }
+    }
+    if (!(Cs[127] < t.cost[R])) return;
+    // ids in pre-order, left first
+    uint32_t sid[128];
+    for (int k = 0; k < 7; ++k) sid[1u << k] = L[k];
+    uint32_t order[6];
+    int n_int = 0, next = 0;
+    uint32_t stack[8];
+    int sp = 0;
+    stack[sp++] = 127;
+    while (sp > 0) {
+        const uint32_t s = stack[--sp];
+        if (__builtin_popcount(s) < 2) continue;
+        sid[s] = I[next++];
+        order[n_int++] = s;
+        stack[sp++] = s ^ P[s];
+        stack[sp++] = P[s];
+    }
+    for (int j = n_int - 1; j >= 0; --j) {  // children before parents
+        const uint32_t s = order[j], p = P[s], id = sid[s];
+        const uint32_t a = sid[p], b = sid[s ^ p];
+        t.kl[id - N] = a;
+        t.kr[id - N] = b;
+        t.parent[a] = id;
+        t.parent[b] = id;
+        t.box[id] = U[s];
+        t.cost[id] = Cs[s];
+        t.nl[id] = t.nl[a] + t.nl[b];
+        t.height[id] = 1 + std::max(t.height[a], t.height[b]);
+    }
+}
+
+void opt_process(OptTree& t, uint32_t R, bool treelets) {
+    const uint32_t N = t.N, a = t.kl[R - N], b = t.kr[R - N];
+    t.box[R] = merge(t.box[a], t.box[b]);
+    t.nl[R] = t.nl[a] + t.nl[b];
+    t.height[R] = 1 + std::max(t.height[a], t.height[b]);
+    t.cost[R] = kOptCi * surface_area(t.box[R]) + (t.cost[a] + t.cost[b]);
+    if (treelets && t.nl[R] >= 7) opt_treelet(t, R);
+}
+
+}  // namespace
+
+extern "C" {
+
+// nodes_in: a DFS node array (crt_bvh_node, 2N-1); nodes_out receives the
+// restructured tree in the same layout.  Returns the root's height.
+uint32_t oracle_optimize(const crt_bvh_node* nodes_in, uint32_t n_nodes, uint32_t passes, crt_bvh_node* nodes_out) {
+    if (n_nodes == 0) return 0;
+    const uint32_t N = (n_nodes + 1) / 2;
+    if (N == 1) {
+        nodes_out[0] = nodes_in[0];
+        return 0;
+    }
+    OptTree t;
+    t.N = N;
+    t.box.resize(2 * N - 1);
+    t.tri.resize(N);
+    t.cost.assign(2 * N - 1, 0.f);
+    t.nl.assign(2 * N - 1, 0);
+    t.height.assign(2 * N - 1, 0);
+    t.parent.assign(2 * N - 1, 0xFFFFFFFFu);
+    t.kl.resize(N - 1);
+    t.kr.resize(N - 1);
+    std::vector<uint32_t> id_of(n_nodes);
+    uint32_t n_leaf = 0, n_int = 0;
+    for (uint32_t d = 0; d < n_nodes; ++d) {
+        const crt_bvh_node& nd = nodes_in[d];
+        const bool leaf = nd.left == 0 && nd.right == 0;
+        id_of[d] = leaf ? n_leaf++ : N + n_int++;
+        const uint32_t id = id_of[d];
+        t.box[id] = Box{{nd.mn[0], nd.mn[1], nd.mn[2]}, {nd.mx[0], nd.mx[1], nd.mx[2]}};
+        if (leaf) {
+            t.tri[id] = nd.tri;
+            t.cost[id] = surface_area(t.box[id]);
+            t.nl[id] = 1;
+        }
+    }
+    for (uint32_t d = 0; d < n_nodes; ++d) {
+        const crt_bvh_node& nd = nodes_in[d];
+        if (nd.left == 0 && nd.right == 0) continue;
+        const uint32_t id = id_of[d];
+        t.kl[id - N] = id_of[nd.left];
+        t.kr[id - N] = id_of[nd.right];
+        t.parent[id_of[nd.left]] = id;
+        t.parent[id_of[nd.right]] = id;
+    }
+    for (uint32_t pass = 0; pass <= passes; ++pass) {
+        const bool treelets = pass < passes;  // a last pass without treelets only sets heights
+        if (!treelets && passes > 0) break;
+        // post-order, iterative: (node, children pushed)
+        std::vector<std::pair<uint32_t, bool>> st;
+        st.emplace_back(N, false);
+        while (!st.empty()) {
+            auto [X, expanded] = st.back();
+            st.pop_back();
+            if (X < N) continue;
+            if (expanded) {
+                opt_process(t, X, treelets);
+                continue;
+            }
+            st.emplace_back(X, true);
+            st.emplace_back(t.kr[X - N], false);
+            st.emplace_back(t.kl[X - N], false);
+        }
+    }
+    // DFS pre-order layout, left first
+    uint32_t pos = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> st;  // (id, position)
+    st.emplace_back(N, pos++);
+    while (!st.empty()) {
+        const auto [X, p] = st.back();
+        st.pop_back();
+        crt_bvh_node& o = nodes_out[p];
+        std::memset(&o, 0, sizeof(o));
+        o.mn[0] = t.box[X].mn.x; o.mn[1] = t.box[X].mn.y; o.mn[2] = t.box[X].mn.z;
+        o.mx[0] = t.box[X].mx.x; o.mx[1] = t.box[X].mx.y; o.mx[2] = t.box[X].mx.z;
+        if (X < N) {
+            o.tri = t.tri[X];
+            continue;
+        }
+        const uint32_t a = t.kl[X - N], b = t.kr[X - N];
+        o.left = p + 1;
+        o.right = p + 2 * t.nl[a];
+        st.emplace_back(b, o.right);
+        st.emplace_back(a, o.left);
+    }
+    return t.height[N];
+}
+
+}  // extern "C"

@@ -59,6 +59,8 @@ def lib():
         L.oracle_trace_brute.argtypes = [vp, u32, vp, u32, vp, u32, u32, vp]
         L.oracle_shade.argtypes = [vp, u32, vp, u32, vp, u32, vp, u32, vp, vp, u32, u32, u32, vp]
         L.oracle_refit.argtypes = [vp, u32, vp, u32, vp, u32]
+        L.oracle_optimize.argtypes = [vp, u32, u32, vp]
+        L.oracle_optimize.restype = u32
         _lib = L
     return _lib
 
@@ -175,3 +177,12 @@ def refit(nodes, tris, models):
     tris, models = _f32(tris, 16), _f32(models, 17)
     lib().oracle_refit(_p(out), out.shape[0], _p(tris), tris.shape[0], _p(models), models.shape[0])
     return out
+
+
+def optimize(nodes, passes=1):
+    """Treelet-restructured node array (the product's crt_optimize) and the
+    new root height."""
+    nodes = _f32(nodes, 12)
+    out = np.zeros_like(nodes)
+    h = lib().oracle_optimize(_p(nodes), nodes.shape[0], passes, _p(out))
+    return out, int(h)

@@ -28,6 +28,7 @@ UNITS = [
     ("crt_trace.cu", ["-fmad=false"]),
     ("crt_frame.cu", ["-fmad=false"]),
     ("crt_refit.cu", ["-fmad=false"]),
+    ("crt_optimize.cu", ["-fmad=false"]),
     ("crt_mesh.cu", []),
     ("crt_api.cu", ["-fmad=false"]),
     ("crt_noalloc.cu", ["-fmad=false"]),

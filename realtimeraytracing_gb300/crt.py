@@ -37,6 +37,7 @@ MISS = 0xFFFFFFFF
 SHADE_WIREFRAME = 0x1  # CRT_SHADE_WIREFRAME: uIsWireframeModeOn
 SHADE_BVH = 0x2  # CRT_SHADE_BVH: uIsBVHDisplayed
 SHADE_MAX_BVH_DEPTH = 63
+OPTIMIZE_MAX_PASSES = 16  # CRT_OPTIMIZE_MAX_PASSES
 
 # Every symbol include/crt.h declares.
 EXPORTS = [
@@ -49,7 +50,7 @@ EXPORTS = [
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
-    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_obj_parse",
+    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_obj_parse",
     "crt_triangles_from_indexed", "crt_selftest_wait",
 ]
 
@@ -139,6 +140,7 @@ def lib():
             "crt_shade": ([vp, vp, vp, vp, u32, vp, vp], i32),
             "crt_render_frame": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
             "crt_refit": ([vp, vp, vp, u32, vp, u32], i32),
+            "crt_optimize": ([vp, vp, u32], i32),
             "crt_obj_parse": ([C.c_char_p, C.c_size_t, vp, u32, vp, u32, vp], i32),
             "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
             "crt_selftest_wait": ([vp, i32, u32], i32),
@@ -412,6 +414,13 @@ class Bvh:
         models = _models(models)
         _check(lib().crt_refit(self.ctx.handle, self.handle, _ptr(tris), self.n_tris, _ptr(models),
                                0 if models is None else _rows(models)))
+        return self
+
+    def optimize(self, passes: int = 2):
+        """crt_optimize: treelet restructuring, `passes` passes (0 = boxes
+        recomputed and the tree laid out again)."""
+        self.ctx._after_torch()
+        _check(lib().crt_optimize(self.ctx.handle, self.handle, passes))
         return self
 
     def free(self):

@@ -100,7 +100,9 @@ void set_last_error(const char* msg) { std::snprintf(g_err, sizeof(g_err), "%s",
 struct crt_bvh {
     crt_ctx* ctx = nullptr;
     uint32_t n = 0;
-    uint32_t iterations = 0;
+    // Bound on the traversal stack's depth: the PLOC iteration count after a
+    // build (tree height <= iterations + 1), the tree's height after crt_optimize.
+    uint32_t depth_bound = 0;
     float abs_eps = 0.f;
     // wide_wt: boxes grown by abs_eps; xtri: transformed triangles in the tree's
     // left-to-right leaf order; inv_perm: triangle -> its position in that order
@@ -161,6 +163,7 @@ struct crt_ctx {
     DevBuf xtri_sorted;  // leaf records in sorted order until the layout moves them
     DevBuf mesh_vertices, mesh_indices, mesh_out;  // crt_triangles_from_indexed staging
     DevBuf probe_flag;                             // crt_selftest_wait
+    DevBuf opt_scratch;                            // crt_optimize
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
     void* pinned = nullptr;
@@ -541,7 +544,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         x->stats.scene_box[3 + a] = hs.scene_max[a];
     }
     b->n = N;
-    b->iterations = iters;
+    b->depth_bound = iters;
     b->abs_eps = hs.abs_eps;  // the value the layout grew the watertight nodes by
     b->ctx = x;
     return CRT_OK;
@@ -645,7 +648,7 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
         p.order = x->ray_order.as<uint32_t>();
     }
     // binary walk: stack <= tree height <= PLOC iterations + 1; 4-wide walk: <= 3 per two levels
-    const bool deep = (b->iterations + 2 > 64) || (3 * ((b->iterations + 2) / 2) + 3 > 96);
+    const bool deep = (b->depth_bound + 2 > 64) || (3 * ((b->depth_bound + 2) / 2) + 3 > 96);
     const uint32_t launch_flags =
         (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED)) | (deep ? (1u << 16) : 0u);
     crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
@@ -738,6 +741,86 @@ crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t 
     }
     b->abs_eps = *h_eps;
     return CRT_OK;
+}
+
+crt_status crt_optimize(crt_ctx* x, crt_bvh* b, uint32_t passes) {
+    if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "crt_optimize: null context or bvh");
+    if (b->n == 0) return fail(CRT_ERR_INVALID_ARG, "crt_optimize: empty bvh");
+    if (passes > CRT_OPTIMIZE_MAX_PASSES)
+        return fail(CRT_ERR_INVALID_ARG, "crt_optimize: %u passes (at most %u)", passes, CRT_OPTIMIZE_MAX_PASSES);
+    const uint32_t N = b->n;
+    if (N < 2) return CRT_OK;
+    CRT_CUDA(cudaSetDevice(x->device));
+    cudaStream_t s = x->stream;
+    uint32_t* err = x->err.as<uint32_t>();
+    // scratch: per id (2N-1) two boxes, cost, leaf count, height, parent; per
+    // internal node (N-1) children twice, child areas, counter, new id, layout position;
+    // DFS table (2N-1); leaf records (N); scene slack
+    const size_t n_id = 2ull * N - 1, n_int = N - 1;
+    size_t off = 0;
+    auto carve = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+    const size_t o_box = carve(32 * n_id), o_box2 = carve(32 * n_id), o_cost = carve(4 * n_id), o_nl = carve(4 * n_id),
+                 o_h = carve(4 * n_id), o_par = carve(4 * n_id), o_kids = carve(16 * n_int), o_kids2 = carve(16 * n_int),
+                 o_karea = carve(8 * n_int), o_cnt = carve(4 * n_int), o_new = carve(4 * n_int), o_pf = carve(8 * n_int),
+                 o_dfs = carve(4 * n_id), o_xtri = carve(48ull * N), o_st = carve(sizeof(crt::SceneState)),
+                 o_hist = carve(4 * (n_id + 1));
+    CRT_TRY(x->opt_scratch.reserve(off));
+    char* base = x->opt_scratch.as<char>();
+    crt::OptView v;
+    v.box = reinterpret_cast<float4*>(base + o_box);
+    v.cost = reinterpret_cast<float*>(base + o_cost);
+    v.nl = reinterpret_cast<uint32_t*>(base + o_nl);
+    v.height = reinterpret_cast<uint32_t*>(base + o_h);
+    v.parent = reinterpret_cast<uint32_t*>(base + o_par);
+    v.kids = reinterpret_cast<uint4*>(base + o_kids);
+    v.karea = reinterpret_cast<float2*>(base + o_karea);
+    v.cnt = reinterpret_cast<uint32_t*>(base + o_cnt);
+    v.N = N;
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, s));
+    crt::launch_opt_init(b->wide.as<float4>(), b->xtri.as<float4>(), v, err, s);
+    for (uint32_t k = 0; k < passes; ++k) crt::launch_opt_pass(v, true, err, s);
+    if (passes == 0) crt::launch_opt_pass(v, false, err, s);
+    CRT_CUDA(cudaGetLastError());
+    uint32_t H = 0;
+    CRT_CUDA(cudaMemcpyAsync(&H, v.height + N, 4, cudaMemcpyDeviceToHost, s));
+    CRT_TRY(x->check_device_error());  // synchronises: H is read
+    if (H == 0 || H > N - 1) return fail(CRT_ERR_CUDA, "crt_optimize: root height %u for %u leaves", H, N);
+    // internal nodes bucketed by height, the root (unique at height H) last
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base + o_hist);
+    CRT_CUDA(cudaMemsetAsync(hist, 0, 4ull * (H + 1), s));
+    crt::launch_opt_hist(v, H, hist, err, s);
+    std::vector<uint32_t> h_hist(H + 2, 0);
+    CRT_CUDA(cudaMemcpyAsync(h_hist.data(), hist, 4ull * (H + 1), cudaMemcpyDeviceToHost, s));
+    CRT_TRY(x->check_device_error());
+    std::vector<uint32_t> h_off(H + 2, 0);
+    for (uint32_t h = 1; h <= H + 1; ++h) h_off[h] = h_off[h - 1] + h_hist[h - 1];
+    if (h_off[H + 1] != N - 1 || h_hist[H] != 1u || h_hist[0] != 0u)
+        return fail(CRT_ERR_CUDA, "crt_optimize: height histogram inconsistent (%u of %u nodes)", h_off[H + 1], N - 1);
+    CRT_CUDA(cudaMemcpyAsync(hist, h_off.data(), 4ull * (H + 1), cudaMemcpyHostToDevice, s));
+    uint4* kids2 = reinterpret_cast<uint4*>(base + o_kids2);
+    float4* box2 = reinterpret_cast<float4*>(base + o_box2);
+    crt::launch_opt_relabel(v, H, hist, reinterpret_cast<uint32_t*>(base + o_new), kids2, box2, err, s);
+    // the leaf records move from the current tree order to the new one
+    float4* xtri_old = reinterpret_cast<float4*>(base + o_xtri);
+    CRT_CUDA(cudaMemcpyAsync(xtri_old, b->xtri.p, 48ull * N, cudaMemcpyDeviceToDevice, s));
+    crt::SceneState hst{};
+    hst.abs_eps = b->abs_eps;  // the slack the watertight nodes are grown by stays the tree's own
+    crt::SceneState* st = reinterpret_cast<crt::SceneState*>(base + o_st);
+    CRT_CUDA(cudaMemcpyAsync(st, &hst, sizeof(hst), cudaMemcpyHostToDevice, s));
+    uint2* pf = reinterpret_cast<uint2*>(base + o_pf);
+    uint32_t* dfs = reinterpret_cast<uint32_t*>(base + o_dfs);
+    for (uint32_t h = H; h >= 1; --h)
+        crt::launch_layout_level(kids2, pf, N + h_off[h], N + h_off[h + 1], N, dfs, err, s);
+    crt::LeafOut leaves{xtri_old, b->xtri.as<float4>(), b->inv_perm.as<uint32_t>()};
+    crt::launch_layout_emit(box2, kids2, pf, N, dfs, b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(),
+                            b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves, st, err, s);
+    CRT_CUDA(cudaGetLastError());
+    b->wide4_ready = false;
+    b->cwide_ready = false;
+    b->refit_ready = false;
+    b->node_boxes_stale = false;
+    b->depth_bound = H;
+    return x->check_device_error();  // also keeps the host staging alive until the copies ran
 }
 
 crt_status crt_bvh_free(crt_bvh* b) {
@@ -969,7 +1052,7 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
             CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
             p.stats = x->trace_stats.as<unsigned long long>();
         }
-        const bool deep = b->iterations + 2 > 64;
+        const bool deep = b->depth_bound + 2 > 64;
         const uint32_t kflags = (flags & CRT_TRI_WATERTIGHT) | (deep ? (1u << 16) : 0u);
         // One launch for the whole image.  Splitting it into row bands whose
         // hits are copied out on a second stream while the next band runs was
@@ -1829,7 +1912,7 @@ crt_status crt_render_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam,
             CRT_CUDA(cudaMemsetAsync(x->trace_stats.p, 0, 16, x->stream));
             p.stats = x->trace_stats.as<unsigned long long>();
         }
-        const bool deep = b->iterations + 2 > 64;
+        const bool deep = b->depth_bound + 2 > 64;
         const uint32_t kflags = (flags & CRT_TRI_WATERTIGHT) | (deep ? (1u << 16) : 0u);
         crt::launch_frame(p, d_cam, width, height, 0, height, nullptr, nullptr, kflags,
                           static_cast<int>(x->cfg.trace_block), &sp, x->stream);

@@ -218,6 +218,29 @@ cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
                               uint8_t* depth_odd, LeafOut leaves, unsigned int* bar, uint32_t max_iters, uint32_t* err,
                               uint32_t spin_limit, cudaStream_t s);
+// Treelet restructuring (crt_optimize.cu).  Ids: leaves 0..N-1 in tree
+// leaf order, internal nodes N + DFS rank (root N).
+struct OptView {
+    float4* box;  // 2 per id: (min | triangle id for leaves), (max | 0)
+    float* cost;
+    uint32_t* nl;      // leaves below
+    uint32_t* height;  // leaves 0
+    uint32_t* parent;
+    uint4* kids;  // per internal node: left id, right id, leaves(left), leaves(right)
+    float2* karea;  // per internal node: its children's box areas
+    uint32_t* cnt;
+    uint32_t N;
+};
+void launch_opt_init(const float4* wide, const float4* xtri, const OptView& t, uint32_t* err, cudaStream_t s);
+// One bottom-up pass: every internal node's box, cost, leaf count and height;
+// with treelets, the treelet step at nodes with at least 7 leaves.
+void launch_opt_pass(const OptView& t, bool treelets, uint32_t* err, cudaStream_t s);
+// hist[h] += internal nodes of height h (1 <= h <= H)
+void launch_opt_hist(const OptView& t, uint32_t H, uint32_t* hist, uint32_t* err, cudaStream_t s);
+// cursor: exclusive offsets per height; new ids N + offset (root last), then
+// children and boxes (leaves too) moved to kids2 / box2 under the new ids.
+void launch_opt_relabel(const OptView& t, uint32_t H, uint32_t* cursor, uint32_t* newid, uint4* kids2, float4* box2,
+                        uint32_t* err, cudaStream_t s);
 // Mesh input (crt_mesh.cu).  obj_parse reads OBJ text into at most vert_cap
 // vertices (3 floats each) and tri_cap triangles (3 vertex indices each) —
 // either may be null to count only — and returns the full counts, or false

@@ -114,6 +114,10 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel_u32(unsigned int* p, unsi
 }
 
 // Nanoseconds of the GPU's global timer.
+// Acquire-release fence at device scope (lighter than __threadfence's
+// sequentially consistent one).
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
