@@ -177,10 +177,11 @@ __global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restr
 // ============================================== K2: Onesweep digit binning
 // One stable counting pass over digit (key >> shift) & (RADIX-1) of a tile
 // of BLOCK*KPT keys (Adinets & Merrill, "Onesweep", 2022):
-//  * warp multisplit: the lanes holding the same digit are found with BITS
-//    ballots (cheaper than match.any on this part), the highest of them adds
-//    the group's size to the warp's shared-memory digit counter and
-//    broadcasts the old count;
+//  * warp multisplit: each lane ORs its bit into the warp's shared-memory
+//    mask of its digit, so the lanes holding the same digit read their group
+//    back (fewer instructions than BITS ballots, and than match.any, on this
+//    part); the highest of them adds the group's size to the warp's digit
+//    counter and broadcasts the old count;
 //  * chained-scan decoupled look-back across tiles for the global digit
 //    offsets; each digit's thread reads a window of LB_WIN predecessor tiles
 //    per round trip with relaxed loads (flag and count share one word);
@@ -191,19 +192,6 @@ __global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restr
 // reference's std::sort of (code, index) pairs (bvh.cpp:214-232).
 constexpr uint32_t kLbAgg = 1u << 30, kLbPrefix = 2u << 30, kLbMask = (1u << 30) - 1u;
 constexpr int kLbWindow = 4;
-
-template <int BITS>
-__device__ __forceinline__ uint32_t ballot_peers(uint32_t d, bool ok) {
-    uint32_t peers = __ballot_sync(0xFFFFFFFFu, ok);
-    if (!ok) peers = ~peers;
-#pragma unroll
-    for (int b = 0; b < BITS; ++b) {
-        const bool bit = (d >> b) & 1u;
-        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, bit);
-        peers &= bit ? bal : ~bal;
-    }
-    return peers;
-}
 
 // SEG: the digit is not taken from the key but is the segment (scene) whose
 // range [seg_off[d], seg_off[d+1]) holds the value — one extra stable pass
@@ -222,6 +210,7 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
     static_assert(BLOCK >= RADIX, "one thread per digit");
     __shared__ uint32_t s_buf[TILE];            // staging for the scatter
     __shared__ uint32_t s_whist[WARPS][RADIX];  // per-warp digit counters, then per-warp offsets
+    __shared__ uint32_t s_match[WARPS][RADIX];  // per-warp lane masks of the key being ranked
     __shared__ uint32_t s_start[RADIX];         // block-local exclusive digit start
     __shared__ uint32_t s_adj[RADIX];           // global destination of sorted slot i is s_adj[d] + i
     __shared__ unsigned long long s_wsum[WARPS];
@@ -234,7 +223,10 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
         s_tile = atomicAdd(ticket, 1u);
         s_timeout = 0u;
     }
-    for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) (&s_whist[0][0])[i] = 0u;
+    for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) {
+        (&s_whist[0][0])[i] = 0u;
+        (&s_match[0][0])[i] = 0u;
+    }
     if (SEG)
         for (int i = threadIdx.x; i <= RADIX; i += BLOCK) s_seg[i] = (static_cast<uint32_t>(i) <= n_seg) ? seg_off[i] : 0xFFFFFFFFu;
     __syncthreads();
@@ -267,14 +259,23 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
     }
     const uint32_t lt_mask = (1u << lane) - 1u;
     uint32_t* my_hist = &s_whist[warp][0];
+    uint32_t* my_match = &s_match[warp][0];
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
         const bool ok = wofs + j * 32u < tile_n;
         const uint32_t d = ok ? digit_of(key[j], val[j]) : 0u;
-        const uint32_t peers = ballot_peers<BITS>(d, ok);
-        const int leader = 31 - __clz(peers);
+        // the lanes holding digit d: each sets its bit in the warp's mask of d
+        if (ok) atomicOr(my_match + d, 1u << lane);
+        __syncwarp();
+        const uint32_t peers = ok ? my_match[d] : 0u;
+        __syncwarp();
+        const int leader = 31 - __clz(peers | 1u);  // the highest peer; lanes without a key read lane 0
         uint32_t base = 0;
-        if (lane == leader && ok) base = atomicAdd(my_hist + d, static_cast<uint32_t>(__popc(peers)));
+        if (ok && lane == static_cast<uint32_t>(leader)) {  // one leader per digit: plain updates
+            base = my_hist[d];
+            my_hist[d] = base + static_cast<uint32_t>(__popc(peers));
+            my_match[d] = 0u;
+        }
         pos[j] = __shfl_sync(0xFFFFFFFFu, base, leader) + __popc(peers & lt_mask);
         __syncwarp();
     }
