@@ -18,9 +18,10 @@
 //                from the traversal nodes, leaf costs;
 //   opt_pass     one thread per leaf climbing to the root; at each internal
 //                node the second child to arrive (acquire-release counter)
-//                finishes it: box, leaf count, height, cost, and — for nodes
-//                with at least 7 leaves, when treelets are on — the treelet
-//                step, done by the whole warp for one node at a time:
+//                finishes it: box, leaf count, height, cost — in its own
+//                lane, unless the node has at least 7 leaves and treelets are
+//                on: then the whole warp takes it, one node at a time, and
+//                runs the treelet step:
 //                  formation: treelet leaves [left, right]; 5 times the
 //                    internal one of largest area (ordered-key compare, ties
 //                    to the lowest index) is replaced by its left child and
@@ -351,6 +352,35 @@ __device__ __forceinline__ void opt_node(const OptView& t, uint32_t R, TreeletSm
     }
 }
 
+// Finish internal node R in the calling lane alone when it gets no treelet
+// step (fewer than 7 leaves, or treelets off); false leaves it to the warp.
+template <bool TREELETS>
+__device__ __forceinline__ bool opt_finish_lane(const OptView& t, uint32_t R, uint32_t* err) {
+    const uint32_t N = t.N;
+    const uint4 kd = __ldcg(t.kids + (R - N));
+    const uint32_t a = kd.x, b = kd.y;
+    if (a >= 2 * N - 1 || b >= 2 * N - 1) {
+        raise_corrupt(err, 21, R, a);
+        return true;
+    }
+    const uint32_t nla = __ldcg(t.nl + a), nlb = __ldcg(t.nl + b);
+    if (TREELETS && nla + nlb >= 7u) return false;
+    float4 mn = __ldcg(t.box + 2 * static_cast<size_t>(a)), mx = __ldcg(t.box + 2 * static_cast<size_t>(a) + 1);
+    const float4 bmn = __ldcg(t.box + 2 * static_cast<size_t>(b)), bmx = __ldcg(t.box + 2 * static_cast<size_t>(b) + 1);
+    const float area_a = box_area(mn, mx), area_b = box_area(bmn, bmx);
+    box_merge(mn, mx, bmn, bmx);
+    mn.w = 0.f;
+    mx.w = 0.f;
+    t.box[2 * static_cast<size_t>(R)] = mn;
+    t.box[2 * static_cast<size_t>(R) + 1] = mx;
+    t.cost[R] = kOptCi * box_area(mn, mx) + (__ldcg(t.cost + a) + __ldcg(t.cost + b));
+    t.nl[R] = nla + nlb;
+    t.height[R] = 1u + max(__ldcg(t.height + a), __ldcg(t.height + b));
+    t.kids[R - N] = make_uint4(a, b, nla, nlb);
+    t.karea[R - N] = make_float2(area_a, area_b);
+    return true;
+}
+
 template <bool TREELETS>
 __global__ void __launch_bounds__(kOptBlock, 4) opt_pass_kernel(OptView t, uint32_t* err) {
     __shared__ TreeletSmem s_tree[TREELETS ? kOptWarps : 1];
@@ -381,7 +411,10 @@ __global__ void __launch_bounds__(kOptBlock, 4) opt_pass_kernel(OptView t, uint3
                 proc = true;
             }
         }
-        uint32_t todo = __ballot_sync(0xFFFFFFFFu, proc);
+        // small nodes: each lane finishes its own (its acquire covers its reads,
+        // its next acquire-release atomic releases its writes)
+        const bool coop = proc && !opt_finish_lane<TREELETS>(t, node, err);
+        uint32_t todo = __ballot_sync(0xFFFFFFFFu, coop);
         if (todo) {
             fence_acq_rel_gpu();  // every lane reads what the acquiring lanes acquired
             while (todo) {
