@@ -6,7 +6,9 @@ oracle's; the one-launch frame (crt_trace_frame: camera ray, closest hit,
 shadow ray, any hit per pixel) must give the oracle's closest hits for every
 pixel (both triangle predicates) and the oracle's occlusion for every shadow
 ray; the shaded frame must equal the oracle's texels; and the treelet-
-restructured tree (crt_optimize) must equal the oracle's at this size.
+restructured tree (crt_optimize) must equal the oracle's at this size.  The
+incoherent-bounce workload (4,194,304 clustered triangles, 8,388,608 bounce
+rays) is checked the same way on a sample of its rays.
 """
 import numpy as np
 import pytest
@@ -78,3 +80,29 @@ def test_config1_optimized_tree(ctx, config1):
     rays = O.raygen(cam, 480, 270)
     _cmp_hits(ctx.trace(b, rays, crt.TRI_WATERTIGHT), O.trace(want, tris, models, rays, crt.TRI_WATERTIGHT)[0])
     b.free()
+
+
+def test_config3_build_and_bounce_rays(ctx):
+    """The incoherent-bounce workload: the 4,194,304-triangle clustered soup
+    built bit for bit, 2048x2048 primary hits, 8,388,608 cosine bounce rays;
+    the plain trace matches the oracle's closest hits (every 8th ray), and the
+    rays traced in sorted order and over the restructured tree give the plain
+    trace's hits for every ray."""
+    tris, models = S.config3_scene(seed=0)
+    ref = O.build_bvh(tris, tris.shape[0], models)
+    bvh = ctx.build(tris, models=models)
+    bad = np.nonzero((_u(bvh.nodes()) != _u(ref["nodes"])).any(axis=1))[0]
+    assert bad.size == 0, f"{bad.size} node records differ, first at {bad[:5]}"
+    cam = S.camera_gpu_data((0.5, 0.5, -1.5))
+    prim = ctx.raygen(cam, 2048, 2048)
+    ph = ctx.trace(bvh, prim, crt.TRI_WATERTIGHT)
+    rays = ctx.bounce_rays(bvh, prim, ph, 8 * 1024 * 1024, seed=11)
+    sample = rays[::8].copy()
+    want, _ = O.trace(ref["nodes"], tris, models, sample, crt.TRI_WATERTIGHT)
+    plain = ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)
+    _cmp_hits(plain[::8], want)
+    assert float((_u(plain)[:, 0] != crt.MISS).mean()) > 0.3
+    np.testing.assert_array_equal(_u(ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.SORT_RAYS)), _u(plain))
+    bvh.optimize(1)
+    np.testing.assert_array_equal(_u(ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)), _u(plain))
+    bvh.free()
