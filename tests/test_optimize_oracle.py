@@ -96,3 +96,35 @@ def test_passes_lower_the_cost_and_keep_the_hits(kind):
     a, _ = O.trace(nodes, tris, models, rays, crt.TRI_REFERENCE)
     b, _ = O.trace(prev, tris, models, rays, crt.TRI_REFERENCE)
     np.testing.assert_array_equal(a[:, 1], b[:, 1])
+
+
+def _height(nodes):
+    u = nodes.view(np.uint32)
+    depth = np.zeros(nodes.shape[0], np.int64)
+    for d in range(nodes.shape[0]):
+        if u[d, 9] or u[d, 10]:
+            depth[u[d, 9]] = depth[d] + 1
+            depth[u[d, 10]] = depth[d] + 1
+    return int(depth.max())
+
+
+def test_reported_height_and_refit_trees():
+    """The returned height is the tree's; a refit tree restructured keeps the
+    moved triangles' watertight hits (those of the brute force)."""
+    from test_refit_oracle import moved
+    n = 4000
+    tris = S.uniform_soup(n, seed=12)
+    models = S.identity_models(1)
+    nodes = O.build_bvh(tris, n, models)["nodes"]
+    for p in (0, 1, 2):
+        out, h = O.optimize(nodes, p)
+        assert h == _height(out)
+    new = moved(tris, 2.2, amp=0.2)
+    refit = O.refit(nodes, new, models)
+    out, _ = O.optimize(refit, 2)
+    check_tree(out, n)
+    assert sah(out) < sah(refit)
+    rays = S.sphere_rays(3000, seed=13)
+    got, _ = O.trace(out, new, models, rays, crt.TRI_WATERTIGHT)
+    want = O.trace_brute(new, models, rays, crt.TRI_WATERTIGHT)
+    np.testing.assert_array_equal(got.view(np.uint32)[:, 0], want.view(np.uint32)[:, 0])
