@@ -223,6 +223,21 @@ crt_status crt_refit(crt_ctx* ctx, crt_bvh* bvh, const crt_triangle* tris, uint3
  * crt_predictor_retarget afterwards. */
 #define CRT_OPTIMIZE_MAX_PASSES 16u
 crt_status crt_optimize(crt_ctx* ctx, crt_bvh* bvh, uint32_t passes);
+/* A BVH from a node array the caller already has: the reference's own
+ * Scene::getBVH_NodesToGPUData output (scene.cpp:203-208; BVH_NodeGPU in DFS
+ * pre-order, left child first, leaves with both children 0 — the array
+ * raytracer.glsl reads from binding 5) and the n_tris triangles it indexes,
+ * with their models.  Keeps the caller's tree (for example the reference's
+ * own CPU build) and makes it traceable here: crt_trace, crt_trace_frame,
+ * crt_shade, crt_render_frame, crt_refit and crt_optimize accept the result;
+ * crt_bvh_copy_codes / _perm do not (there is no Morton sort).  nodes and
+ * tris may be host or device memory.  The array must have 2 n_tris - 1
+ * records in that order, each triangle in exactly one leaf; anything else is
+ * CRT_ERR_INVALID_ARG.  Boxes are used as given and must contain their
+ * triangles (AABB::buildFromTriangle, bvh.cpp:383-399, makes such boxes); the
+ * watertight slack is derived from the root box. */
+crt_status crt_bvh_from_nodes(crt_ctx* ctx, const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris,
+                              uint32_t n_tris, const crt_mesh_model* models, uint32_t n_models, crt_bvh** out);
 crt_status crt_bvh_free(crt_bvh* bvh);
 uint32_t crt_bvh_node_count(const crt_bvh* bvh);       /* 2 * n_tris - 1 */
 uint32_t crt_bvh_triangle_count(const crt_bvh* bvh);

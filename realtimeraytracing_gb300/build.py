@@ -29,6 +29,7 @@ UNITS = [
     ("crt_frame.cu", ["-fmad=false"]),
     ("crt_refit.cu", ["-fmad=false"]),
     ("crt_optimize.cu", ["-fmad=false"]),
+    ("crt_import.cu", ["-fmad=false"]),
     ("crt_mesh.cu", []),
     ("crt_api.cu", ["-fmad=false"]),
     ("crt_noalloc.cu", ["-fmad=false"]),

@@ -50,7 +50,8 @@ EXPORTS = [
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
-    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_obj_parse",
+    "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_bvh_from_nodes",
+    "crt_obj_parse",
     "crt_triangles_from_indexed", "crt_selftest_wait",
 ]
 
@@ -141,6 +142,7 @@ def lib():
             "crt_render_frame": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
             "crt_refit": ([vp, vp, vp, u32, vp, u32], i32),
             "crt_optimize": ([vp, vp, u32], i32),
+            "crt_bvh_from_nodes": ([vp, vp, u32, vp, u32, vp, u32, C.POINTER(vp)], i32),
             "crt_obj_parse": ([C.c_char_p, C.c_size_t, vp, u32, vp, u32, vp], i32),
             "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
             "crt_selftest_wait": ([vp, i32, u32], i32),
@@ -506,6 +508,18 @@ class Context:
         h = C.c_void_p()
         _check(lib().crt_build(self.handle, _ptr(tris), n_buffer, n_tris, _ptr(models),
                                0 if models is None else _rows(models), C.byref(h)))
+        return Bvh(self, h)
+
+    def bvh_from_nodes(self, nodes, tris, models=None) -> Bvh:
+        """crt_bvh_from_nodes: a traceable BVH from a DFS node array in the
+        reference's layout ((2n-1, 12) float32 records) and its n triangles."""
+        self._after_torch()
+        models = _models(models)
+        if isinstance(nodes, np.ndarray):
+            nodes = np.ascontiguousarray(nodes, np.float32)
+        h = C.c_void_p()
+        _check(lib().crt_bvh_from_nodes(self.handle, _ptr(nodes), _rows(nodes), _ptr(tris), _rows(tris), _ptr(models),
+                                        0 if models is None else _rows(models), C.byref(h)))
         return Bvh(self, h)
 
     def last_build_stats(self) -> dict:

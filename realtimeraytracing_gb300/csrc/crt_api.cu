@@ -86,7 +86,27 @@ void* mapped_host_ptr(void* ptr) {
         cudaGetLastError();
         return nullptr;
     }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    // the kernels read and write records as 16-byte vectors: other page-locked
+    // buffers take the copy path
+    if (a.type != cudaMemoryTypeHost || (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u) != 0) return nullptr;
+    return a.devicePointer;
+}
+
+// A caller's device buffer the kernels read or write as 16-byte vectors.
+crt_status check_aligned16(const void* p, const char* what) {
+    if ((reinterpret_cast<uintptr_t>(p) & 15u) != 0)
+        return fail(CRT_ERR_INVALID_ARG, "%s: device memory must be 16-byte aligned", what);
+    return CRT_OK;
+}
+
+// The batch pipeline reads its triangles and rays and writes its hits in
+// device memory only (graph replays reuse the pointers).
+crt_status check_batch_buffers(const void* tris, const void* rays, const void* hits, const char* fn) {
+    if (!is_device_ptr(tris) || !is_device_ptr(rays) || !is_device_ptr(hits))
+        return fail(CRT_ERR_INVALID_ARG, "%s: triangles, rays and hits must be device memory", fn);
+    if (((reinterpret_cast<uintptr_t>(tris) | reinterpret_cast<uintptr_t>(rays) | reinterpret_cast<uintptr_t>(hits)) & 15u) != 0)
+        return fail(CRT_ERR_INVALID_ARG, "%s: device memory must be 16-byte aligned", fn);
+    return CRT_OK;
 }
 
 constexpr uint32_t kDefaultSpin = 1u << 22;   // ~0.3 s with back-off; far above any normal wait
@@ -120,6 +140,8 @@ struct crt_bvh {
     // After a refit only the root box of the node array is current; the
     // others are derived from the traversal nodes when the array is read.
     mutable bool node_boxes_stale = false;
+    // Sorted Morton codes and permutation exist (a tree from crt_bvh_from_nodes has none).
+    bool has_sort = false;
 };
 
 struct crt_predictor {
@@ -360,6 +382,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         CRT_CUDA(cudaMemcpyAsync(x->tris_in.p, tris, sizeof(crt_triangle) * static_cast<size_t>(n_buffer),
                                  cudaMemcpyHostToDevice, s));
         d_tris = x->tris_in.as<crt_triangle>();
+    } else {
+        CRT_TRY(check_aligned16(tris, "crt_build: triangles"));
     }
     const size_t hist_words = static_cast<size_t>(passes) * radix;
     const size_t sort_lb_words = static_cast<size_t>(passes) * (sort_tiles * radix + 1);  // + ticket per pass
@@ -545,6 +569,7 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     }
     b->n = N;
     b->depth_bound = iters;
+    b->has_sort = true;
     b->abs_eps = hs.abs_eps;  // the value the layout grew the watertight nodes by
     b->ctx = x;
     return CRT_OK;
@@ -705,6 +730,8 @@ crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t 
         CRT_TRY(x->tris_in.reserve(sizeof(crt_triangle) * static_cast<size_t>(N)));
         CRT_CUDA(cudaMemcpyAsync(x->tris_in.p, tris, sizeof(crt_triangle) * static_cast<size_t>(N), cudaMemcpyHostToDevice, s));
         d_tris = x->tris_in.as<crt_triangle>();
+    } else {
+        CRT_TRY(check_aligned16(tris, "crt_refit: triangles"));
     }
     CRT_TRY(stage_model_matrices(x, models, n_models));
     CRT_TRY(x->refit_state.reserve(sizeof(crt::RefitState)));
@@ -740,6 +767,134 @@ crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t 
         return st;
     }
     b->abs_eps = *h_eps;
+    return CRT_OK;
+}
+
+crt_status crt_bvh_from_nodes(crt_ctx* x, const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris,
+                              uint32_t n_tris, const crt_mesh_model* models, uint32_t n_models, crt_bvh** out) {
+    if (!x || !nodes || !tris || !out) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: null argument");
+    *out = nullptr;
+    if (n_tris == 0 || n_tris > (1u << 30))
+        return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: n_tris must be in [1, 2^30]");
+    if (n_nodes != 2 * n_tris - 1)
+        return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: %u nodes for %u triangles (need 2n-1)", n_nodes, n_tris);
+    if (n_models > crt::kMaxModels) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: more than 64 models");
+    if (n_models > 0 && !models) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: null models");
+    CRT_CUDA(cudaSetDevice(x->device));
+    cudaStream_t s = x->stream;
+    const uint32_t N = n_tris;
+    if (is_device_ptr(tris)) CRT_TRY(check_aligned16(tris, "crt_bvh_from_nodes: triangles"));
+    // the array on the host, for the structure check and the numbering
+    std::vector<crt_bvh_node> h(n_nodes);
+    if (is_device_ptr(nodes)) {
+        CRT_CUDA(cudaMemcpy(h.data(), nodes, sizeof(crt_bvh_node) * n_nodes, cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(h.data(), nodes, sizeof(crt_bvh_node) * n_nodes);
+    }
+    // DFS pre-order, left child first (scene.cpp:189-208): an internal node at d
+    // has its left child at d + 1 and its right child after the left subtree;
+    // a leaf (both children 0, raytracer.glsl:239-244) names one triangle, each
+    // triangle once.  Numbering: leaves and internal nodes in order of position.
+    std::vector<uint32_t> idx(n_nodes), leaves(n_nodes), int_pos(N > 1 ? N - 1 : 1), leaf_pos(N);
+    std::vector<uint2> lc(N > 1 ? N - 1 : 1);
+    std::vector<uint8_t> seen(N, 0), odd(N > 1 ? N - 1 : 1, 0);
+    std::vector<uint8_t> referenced(n_nodes, 0);
+    uint32_t n_leaf = 0, n_int = 0, max_depth = 0;
+    std::vector<uint32_t> dep(n_nodes, 0);
+    for (uint32_t d = 0; d < n_nodes; ++d) {
+        const crt_bvh_node& nd = h[d];
+        if (d > 0 && !referenced[d])
+            return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: node %u is no node's child", d);
+        if (nd.left == 0 && nd.right == 0) {
+            if (nd.tri >= N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: leaf %u names triangle %u", d, nd.tri);
+            if (seen[nd.tri]) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: triangle %u in two leaves", nd.tri);
+            seen[nd.tri] = 1;
+            if (n_leaf >= N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: more than %u leaves", N);
+            idx[d] = n_leaf;
+            leaf_pos[n_leaf++] = d;
+        } else {
+            if (nd.left != d + 1 || nd.right <= nd.left || nd.right >= n_nodes || referenced[nd.left] ||
+                referenced[nd.right])
+                return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: node %u is not in DFS pre-order (children %u, %u)",
+                            d, nd.left, nd.right);
+            if (n_int + 1 >= N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: more than %u internal nodes", N - 1);
+            referenced[nd.left] = referenced[nd.right] = 1;
+            dep[nd.left] = dep[nd.right] = dep[d] + 1;
+            max_depth = std::max(max_depth, dep[d] + 1);
+            idx[d] = n_int;
+            int_pos[n_int++] = d;
+        }
+    }
+    if (n_leaf != N || n_int != N - 1)
+        return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: %u leaves and %u internal nodes for %u triangles", n_leaf,
+                    n_int, N);
+    for (uint32_t d = n_nodes; d-- > 0;) {  // children follow their parent: a reverse sweep counts leaves
+        const crt_bvh_node& nd = h[d];
+        if (nd.left == 0 && nd.right == 0) {
+            leaves[d] = 1;
+            continue;
+        }
+        leaves[d] = leaves[nd.left] + leaves[nd.right];
+        if (nd.right != nd.left + 2 * leaves[nd.left] - 1)
+            return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: node %u's right child does not follow its left subtree", d);
+        lc[idx[d]] = make_uint2(leaves[nd.left], leaves[nd.right]);
+        odd[idx[d]] = static_cast<uint8_t>(dep[d] & 1u);
+    }
+    if (leaves[0] != N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: the root holds %u of %u leaves", leaves[0], N);
+
+    crt_bvh* b = new crt_bvh();
+    auto fail_free = [&](crt_status st) {
+        crt_bvh_free(b);
+        return st;
+    };
+    const size_t n_int_alloc = std::max<size_t>(N - 1, 1);
+    crt_status st = CRT_OK;
+    if ((st = b->nodes.reserve(sizeof(crt_bvh_node) * n_nodes)) != CRT_OK || (st = b->xtri.reserve(48ull * N)) != CRT_OK ||
+        (st = b->wide.reserve(64ull * n_int_alloc)) != CRT_OK || (st = b->wide_wt.reserve(64ull * n_int_alloc)) != CRT_OK ||
+        (st = b->depth_odd.reserve(n_int_alloc)) != CRT_OK || (st = b->inv_perm.reserve(4ull * N)) != CRT_OK)
+        return fail_free(st);
+    // staging: idx (n_nodes) | int_pos (N-1) | leaf counts (N-1, uint2) | leaf_pos (N), each part
+    // starting on a 256-byte boundary (the uint2 loads need 8-byte alignment)
+    auto up256 = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t o_int = up256(4ull * n_nodes), o_lc = up256(o_int + 4ull * n_int_alloc),
+                 o_leaf = up256(o_lc + 8ull * n_int_alloc), bytes = o_leaf + 4ull * N;
+    if ((st = x->opt_scratch.reserve(bytes)) != CRT_OK) return fail_free(st);
+    char* base = x->opt_scratch.as<char>();
+    if ((st = stage_model_matrices(x, models, n_models)) != CRT_OK) return fail_free(st);
+    const crt_triangle* d_tris = tris;
+    if (!is_device_ptr(tris)) {
+        if ((st = x->tris_in.reserve(sizeof(crt_triangle) * static_cast<size_t>(N))) != CRT_OK) return fail_free(st);
+        if (cudaMemcpyAsync(x->tris_in.p, tris, sizeof(crt_triangle) * static_cast<size_t>(N), cudaMemcpyHostToDevice, s) !=
+            cudaSuccess)
+            return fail_free(fail(CRT_ERR_CUDA, "crt_bvh_from_nodes: triangle upload failed"));
+        d_tris = x->tris_in.as<crt_triangle>();
+    }
+    const cudaError_t ce[6] = {
+        cudaMemcpyAsync(b->nodes.p, h.data(), sizeof(crt_bvh_node) * n_nodes, cudaMemcpyHostToDevice, s),
+        cudaMemcpyAsync(base, idx.data(), 4ull * n_nodes, cudaMemcpyHostToDevice, s),
+        cudaMemcpyAsync(base + o_int, int_pos.data(), 4ull * n_int_alloc, cudaMemcpyHostToDevice, s),
+        cudaMemcpyAsync(base + o_lc, lc.data(), 8ull * n_int_alloc, cudaMemcpyHostToDevice, s),
+        cudaMemcpyAsync(base + o_leaf, leaf_pos.data(), 4ull * N, cudaMemcpyHostToDevice, s),
+        cudaMemcpyAsync(b->depth_odd.p, odd.data(), n_int_alloc, cudaMemcpyHostToDevice, s)};
+    for (cudaError_t e : ce)
+        if (e != cudaSuccess) return fail_free(fail(CRT_ERR_CUDA, "crt_bvh_from_nodes: upload failed: %s", cudaGetErrorString(e)));
+    // the traversal slack of the root box, as a refit derives it
+    const float smin[3] = {h[0].mn[0], h[0].mn[1], h[0].mn[2]}, smax[3] = {h[0].mx[0], h[0].mx[1], h[0].mx[2]};
+    const float grow = crt::scene_abs_eps(smin, smax);
+    if (cudaMemsetAsync(x->err.p, 0, 16, s) != cudaSuccess) return fail_free(fail(CRT_ERR_CUDA, "crt_bvh_from_nodes: memset"));
+    crt::launch_import(b->nodes.as<crt_bvh_node>(), N, reinterpret_cast<const uint32_t*>(base),
+                       reinterpret_cast<const uint32_t*>(base + o_int), reinterpret_cast<const uint2*>(base + o_lc),
+                       reinterpret_cast<const uint32_t*>(base + o_leaf), d_tris, x->models.as<float>(), grow,
+                       b->wide.as<float4>(), b->wide_wt.as<float4>(), b->xtri.as<float4>(), b->inv_perm.as<uint32_t>(),
+                       x->err.as<uint32_t>(), s);
+    if (cudaGetLastError() != cudaSuccess) return fail_free(fail(CRT_ERR_CUDA, "crt_bvh_from_nodes: launch failed"));
+    if ((st = x->check_device_error()) != CRT_OK) return fail_free(st);  // synchronises: the host arrays may go
+    b->n = N;
+    b->depth_bound = max_depth;
+    b->abs_eps = grow;
+    b->has_sort = false;
+    b->ctx = x;
+    *out = b;
     return CRT_OK;
 }
 
@@ -860,10 +1015,12 @@ crt_status crt_bvh_copy_nodes(crt_ctx* x, const crt_bvh* b, crt_bvh_node* dst) {
 }
 crt_status crt_bvh_copy_codes(crt_ctx* x, const crt_bvh* b, uint32_t* dst) {
     if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "null context or bvh");
+    if (!b->has_sort) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_copy_codes: this tree was not built here (no Morton sort)");
     return copy_out(x, dst, b->codes.p, 4ull * b->n);
 }
 crt_status crt_bvh_copy_perm(crt_ctx* x, const crt_bvh* b, uint32_t* dst) {
     if (!x || !b) return fail(CRT_ERR_INVALID_ARG, "null context or bvh");
+    if (!b->has_sort) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_copy_perm: this tree was not built here (no Morton sort)");
     return copy_out(x, dst, b->perm.p, 4ull * b->n);
 }
 
@@ -882,8 +1039,11 @@ crt_status crt_raygen_pinhole(crt_ctx* x, const crt_camera* cam, uint32_t width,
     if (!is_device_ptr(cam)) {
         CRT_CUDA(cudaMemcpyAsync(x->cam.p, cam, sizeof(crt_camera), cudaMemcpyHostToDevice, x->stream));
         d_cam = x->cam.as<crt_camera>();
+    } else {
+        CRT_TRY(check_aligned16(cam, "crt_raygen_pinhole: camera"));
     }
     const bool dev_out = is_device_ptr(rays);
+    if (dev_out) CRT_TRY(check_aligned16(rays, "crt_raygen_pinhole: rays"));
     crt_ray* d_rays = rays;
     if (!dev_out) {
         CRT_TRY(x->rays_out.reserve(sizeof(crt_ray) * n));
@@ -903,6 +1063,9 @@ crt_status crt_shadow_rays(crt_ctx* x, const crt_ray* primary, const crt_hit* hi
     if (n == 0) return CRT_OK;
     const crt_ray* d_prim = primary;
     const crt_hit* d_hits = hits;
+    if (is_device_ptr(primary)) CRT_TRY(check_aligned16(primary, "crt_shadow_rays: primary rays"));
+    if (is_device_ptr(hits)) CRT_TRY(check_aligned16(hits, "crt_shadow_rays: hits"));
+    if (is_device_ptr(shadow)) CRT_TRY(check_aligned16(shadow, "crt_shadow_rays: shadow rays"));
     if (!is_device_ptr(primary)) {
         CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n));
         CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, primary, sizeof(crt_ray) * n, cudaMemcpyHostToDevice, x->stream));
@@ -931,6 +1094,8 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
     CRT_TRY(check_trace_flags(b, flags));
     CRT_CUDA(cudaSetDevice(x->device));
     if (n_rays == 0) return CRT_OK;
+    if (is_device_ptr(rays)) CRT_TRY(check_aligned16(rays, "crt_trace: rays"));
+    if (is_device_ptr(hits)) CRT_TRY(check_aligned16(hits, "crt_trace: hits"));
     const crt_ray* d_rays = rays;
     if (!is_device_ptr(rays)) {
         // Page-locked host rays are read in place by the trace kernel when it
@@ -975,6 +1140,10 @@ crt_status crt_trace_seeded(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, u
     if (n_rays == 0) return CRT_OK;
     if (!is_device_ptr(rays) || !is_device_ptr(hits) || !is_device_ptr(classes))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace_seeded: rays, classes and hits must be device memory");
+    CRT_TRY(check_aligned16(rays, "crt_trace_seeded: rays"));
+    CRT_TRY(check_aligned16(hits, "crt_trace_seeded: hits"));
+    if (reinterpret_cast<uintptr_t>(classes) & 1u)
+        return fail(CRT_ERR_INVALID_ARG, "crt_trace_seeded: classes must be 2-byte aligned");
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     CRT_TRY(trace_device(x, b, rays, n_rays, flags & ~CRT_TRACE_USE_PREDICTOR, hits, classes));
     CRT_TRY(x->check_device_error());
@@ -1001,6 +1170,9 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     const uint32_t n = width * height;
     const bool fused = !(flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED));
     bool dev_p = is_device_ptr(hits_primary);
+    if (dev_p) CRT_TRY(check_aligned16(hits_primary, "crt_trace_frame: primary hits"));
+    if (light && hits_shadow && is_device_ptr(hits_shadow))
+        CRT_TRY(check_aligned16(hits_shadow, "crt_trace_frame: shadow hits"));
     crt_hit* d_hp = hits_primary;
     if (!dev_p && fused) {  // page-locked host output: the frame kernel writes it over the CPU-GPU link
         if (void* m = mapped_host_ptr(hits_primary)) {
@@ -1016,6 +1188,8 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
     if (!is_device_ptr(cam)) {
         CRT_CUDA(cudaMemcpyAsync(x->cam.p, cam, sizeof(crt_camera), cudaMemcpyHostToDevice, x->stream));
         d_cam = x->cam.as<crt_camera>();
+    } else {
+        CRT_TRY(check_aligned16(cam, "camera"));
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp
@@ -1099,7 +1273,11 @@ crt_status crt_trace_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam, 
 namespace {
 
 crt_status stage_in(crt_ctx* x, DevBuf& buf, const void* src, size_t bytes, const void** dev) {
-    if (is_device_ptr(src)) { *dev = src; return CRT_OK; }
+    if (is_device_ptr(src)) {
+        CRT_TRY(check_aligned16(src, "ray or hit input"));
+        *dev = src;
+        return CRT_OK;
+    }
     CRT_TRY(buf.reserve(bytes));
     CRT_CUDA(cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, x->stream));
     *dev = buf.p;
@@ -1328,6 +1506,7 @@ crt_status crt_bounce_rays(crt_ctx* x, const crt_bvh* b, const crt_ray* primary,
     CRT_TRY(stage_in(x, x->rays_in, primary, sizeof(crt_ray) * static_cast<size_t>(n_primary), &d_prim));
     CRT_TRY(stage_in(x, x->hits_out, hits, sizeof(crt_hit) * static_cast<size_t>(n_primary), &d_hits));
     const bool dev_out = is_device_ptr(out);
+    if (dev_out) CRT_TRY(check_aligned16(out, "crt_bounce_rays: rays"));
     crt_ray* d_out = out;
     if (!dev_out) {
         CRT_TRY(x->rays_out.reserve(sizeof(crt_ray) * static_cast<size_t>(n_out)));
@@ -1628,6 +1807,7 @@ crt_status crt_batch_get_config(const crt_batch* bt, crt_config* cfg) {
 crt_status crt_batch_build(crt_ctx* x, crt_batch* bt, const crt_triangle* tris) {
     if (!x || !bt || !tris) return fail(CRT_ERR_INVALID_ARG, "crt_batch_build: null argument");
     if (!is_device_ptr(tris)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_build: triangles must be device memory");
+    CRT_TRY(check_aligned16(tris, "crt_batch_build: triangles"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_enqueue(x, bt, tris, nullptr, 0, nullptr, nullptr));
     return batch_check(x, bt);
@@ -1638,6 +1818,8 @@ crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint3
     if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS))
         return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: unsupported flags");
     if (!is_device_ptr(rays) || !is_device_ptr(hits)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: device memory only");
+    CRT_TRY(check_aligned16(rays, "crt_batch_trace: rays"));
+    CRT_TRY(check_aligned16(hits, "crt_batch_trace: hits"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_order_buffers(bt, flags));
     CRT_CUDA(cudaMemsetAsync(bt->err.p, 0, 16, x->stream));
@@ -1668,6 +1850,7 @@ crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
     if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: null argument");
     if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS))
         return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: unsupported flags");
+    CRT_TRY(check_batch_buffers(tris, rays, hits, "crt_batch_run"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_order_buffers(bt, flags));  // before any graph capture: no allocation inside it
     if (graph_used) *graph_used = 0;
@@ -1721,6 +1904,7 @@ crt_status crt_batch_scene_info(const crt_batch* bt, uint32_t scene, uint32_t in
 crt_status crt_batch_autotune(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
                               crt_hit* hits, crt_config* best, float* best_ms) {
     if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_autotune: null argument");
+    CRT_TRY(check_batch_buffers(tris, rays, hits, "crt_batch_autotune"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_order_buffers(bt, flags));
     cudaEvent_t e0, e1, e2;
@@ -1900,6 +2084,8 @@ crt_status crt_render_frame(crt_ctx* x, const crt_bvh* b, const crt_camera* cam,
     if (!is_device_ptr(cam)) {
         CRT_CUDA(cudaMemcpyAsync(x->cam.p, cam, sizeof(crt_camera), cudaMemcpyHostToDevice, x->stream));
         d_cam = x->cam.as<crt_camera>();
+    } else {
+        CRT_TRY(check_aligned16(cam, "camera"));
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     const uint32_t tw = (width % 8 == 0 && height % 4 == 0) ? width : 0u;  // 8x4 pixel tiles per warp

@@ -241,6 +241,13 @@ void launch_opt_hist(const OptView& t, uint32_t H, uint32_t* hist, uint32_t* err
 // children and boxes (leaves too) moved to kids2 / box2 under the new ids.
 void launch_opt_relabel(const OptView& t, uint32_t H, uint32_t* cursor, uint32_t* newid, uint4* kids2, float4* box2,
                         uint32_t* err, cudaStream_t s);
+// A BVH from a caller's DFS node array (crt_import.cu): idx[d] = leaf index
+// or internal rank of position d; int_pos[k] = position of internal rank k;
+// leaf_counts[k] = leaves under its children; leaf_pos[l] = position of leaf l.
+void launch_import(const crt_bvh_node* nodes, uint32_t N, const uint32_t* idx, const uint32_t* int_pos,
+                   const uint2* leaf_counts, const uint32_t* leaf_pos, const crt_triangle* tris, const float* models,
+                   float grow, float4* wide, float4* wide_wt, float4* xtri, uint32_t* leaf_of_tri, uint32_t* err,
+                   cudaStream_t s);
 // Mesh input (crt_mesh.cu).  obj_parse reads OBJ text into at most vert_cap
 // vertices (3 floats each) and tri_cap triangles (3 vertex indices each) —
 // either may be null to count only — and returns the full counts, or false
