@@ -1411,6 +1411,8 @@ crt_status crt_predictor_infer(crt_ctx* x, crt_predictor* pr, const crt_ray* ray
     const void* d_rays;
     CRT_TRY(stage_in(x, pr->rays_in, rays, sizeof(crt_ray) * static_cast<size_t>(n), &d_rays));
     const bool dev_out = is_device_ptr(classes);
+    if (dev_out && (reinterpret_cast<uintptr_t>(classes) & 1u))
+        return fail(CRT_ERR_INVALID_ARG, "classes: device memory must be 2-byte aligned");
     uint16_t* d_out = classes;
     if (!dev_out) {
         CRT_TRY(pr->classes.reserve(2ull * n));
@@ -1431,6 +1433,8 @@ crt_status crt_predictor_classes_of_hits(crt_ctx* x, crt_predictor* pr, const cr
     const void* d_hits;
     CRT_TRY(stage_in(x, pr->hits_in, hits, sizeof(crt_hit) * static_cast<size_t>(n), &d_hits));
     const bool dev_out = is_device_ptr(classes);
+    if (dev_out && (reinterpret_cast<uintptr_t>(classes) & 1u))
+        return fail(CRT_ERR_INVALID_ARG, "classes: device memory must be 2-byte aligned");
     uint16_t* d_out = classes;
     if (!dev_out) {
         CRT_TRY(pr->targets_in.reserve(2ull * n));
