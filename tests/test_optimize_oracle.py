@@ -128,3 +128,29 @@ def test_reported_height_and_refit_trees():
     got, _ = O.trace(out, new, models, rays, crt.TRI_WATERTIGHT)
     want = O.trace_brute(new, models, rays, crt.TRI_WATERTIGHT)
     np.testing.assert_array_equal(got.view(np.uint32)[:, 0], want.view(np.uint32)[:, 0])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_small_scenes(seed):
+    """Random sizes 1..300 and pass counts 0..3: always a valid tree over the
+    same triangles, never a higher cost, zero passes the identity."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(1, 301))
+    kind = seed % 3
+    if kind == 0:
+        tris = S.uniform_soup(n, seed=100 + seed)
+    elif kind == 1:
+        tris = S.clustered_soup(n, 3, 0.05, 0.01, 0.5, seed=100 + seed)
+    else:  # a few distinct triangles repeated: equal boxes and costs
+        base = S.uniform_soup(max(1, n // 5), seed=100 + seed)
+        tris = np.concatenate([base] * 6)[:n].copy()
+    models = S.identity_models(1)
+    nodes = O.build_bvh(tris, n, models)["nodes"]
+    out0, _ = O.optimize(nodes, 0)
+    np.testing.assert_array_equal(out0.view(np.uint32), nodes.view(np.uint32))
+    passes = int(rng.integers(1, 4))
+    out, h = O.optimize(nodes, passes)
+    if n > 1:
+        check_tree(out, n)
+    assert h == _height(out)
+    assert sah(out) <= sah(nodes) * (1 + 1e-6)
