@@ -238,6 +238,12 @@ crt_status crt_optimize(crt_ctx* ctx, crt_bvh* bvh, uint32_t passes);
  * watertight slack is derived from the root box. */
 crt_status crt_bvh_from_nodes(crt_ctx* ctx, const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris,
                               uint32_t n_tris, const crt_mesh_model* models, uint32_t n_models, crt_bvh** out);
+/* The structure check of crt_bvh_from_nodes alone, on the host, without a
+ * context (nodes in host memory, or device memory when a GPU is present):
+ * CRT_OK for a well-formed array, with info[0] = leaves, [1] = internal nodes,
+ * [2] = height (edges on the longest root-leaf path), [3] = 0; otherwise
+ * CRT_ERR_INVALID_ARG, and crt_last_error_string() names the first problem. */
+crt_status crt_validate_nodes(const crt_bvh_node* nodes, uint32_t n_nodes, uint32_t n_tris, uint32_t info[4]);
 crt_status crt_bvh_free(crt_bvh* bvh);
 uint32_t crt_bvh_node_count(const crt_bvh* bvh);       /* 2 * n_tris - 1 */
 uint32_t crt_bvh_triangle_count(const crt_bvh* bvh);

@@ -51,7 +51,7 @@ EXPORTS = [
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
     "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_bvh_from_nodes",
-    "crt_obj_parse",
+    "crt_validate_nodes", "crt_obj_parse",
     "crt_triangles_from_indexed", "crt_selftest_wait",
 ]
 
@@ -143,6 +143,7 @@ def lib():
             "crt_refit": ([vp, vp, vp, u32, vp, u32], i32),
             "crt_optimize": ([vp, vp, u32], i32),
             "crt_bvh_from_nodes": ([vp, vp, u32, vp, u32, vp, u32, C.POINTER(vp)], i32),
+            "crt_validate_nodes": ([vp, u32, u32, vp], i32),
             "crt_obj_parse": ([C.c_char_p, C.c_size_t, vp, u32, vp, u32, vp], i32),
             "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
             "crt_selftest_wait": ([vp, i32, u32], i32),
@@ -197,6 +198,16 @@ def _shading(models, materials, flags, bvh_depth):
     sh.n_materials = 0 if materials is None else _rows(materials)
     sh.flags, sh.bvh_depth = flags, bvh_depth
     return sh, (models, materials)
+
+
+def validate_nodes(nodes, n_tris=None) -> dict:
+    """crt_validate_nodes: the structure check of a DFS node array ((2n-1, 12)
+    float32 records) on the host; raises CrtError naming the first problem."""
+    nodes = np.ascontiguousarray(nodes, np.float32)
+    n_tris = (nodes.shape[0] + 1) // 2 if n_tris is None else n_tris
+    info = np.zeros(4, np.uint32)
+    _check(lib().crt_validate_nodes(_ptr(nodes), nodes.shape[0], n_tris, _ptr(info)))
+    return {"leaves": int(info[0]), "internal": int(info[1]), "height": int(info[2])}
 
 
 def parse_obj(source):

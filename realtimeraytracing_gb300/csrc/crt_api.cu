@@ -770,6 +770,102 @@ crt_status crt_refit(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t 
     return CRT_OK;
 }
 
+// The structure check and numbering of a caller's DFS node array (host copy
+// h of n_nodes records over N triangles), shared by crt_validate_nodes and
+// crt_bvh_from_nodes.  DFS pre-order, left child first (scene.cpp:189-208):
+// an internal node at d has its left child at d + 1 and its right child
+// after the left subtree; a leaf (both children 0, raytracer.glsl:239-244)
+// names one triangle, each triangle once.  Leaves and internal nodes are
+// numbered in order of position.
+struct NodeNumbering {
+    std::vector<uint32_t> idx, int_pos, leaf_pos;
+    std::vector<uint2> lc;
+    std::vector<uint8_t> odd;
+    uint32_t max_depth = 0;
+};
+
+static crt_status number_nodes(const crt_bvh_node* h, uint32_t n_nodes, uint32_t N, const char* fn, NodeNumbering* out) {
+    if (N == 0 || N > (1u << 30)) return fail(CRT_ERR_INVALID_ARG, "%s: n_tris must be in [1, 2^30]", fn);
+    if (n_nodes != 2 * N - 1) return fail(CRT_ERR_INVALID_ARG, "%s: %u nodes for %u triangles (need 2n-1)", fn, n_nodes, N);
+    NodeNumbering& o = *out;
+    o.idx.assign(n_nodes, 0);
+    o.int_pos.assign(N > 1 ? N - 1 : 1, 0);
+    o.leaf_pos.assign(N, 0);
+    o.lc.assign(N > 1 ? N - 1 : 1, make_uint2(0u, 0u));
+    o.odd.assign(N > 1 ? N - 1 : 1, 0);
+    o.max_depth = 0;
+    std::vector<uint32_t> leaves(n_nodes, 0), dep(n_nodes, 0);
+    std::vector<uint8_t> seen(N, 0), referenced(n_nodes, 0);
+    uint32_t n_leaf = 0, n_int = 0;
+    for (uint32_t d = 0; d < n_nodes; ++d) {
+        const crt_bvh_node& nd = h[d];
+        if (d > 0 && !referenced[d]) return fail(CRT_ERR_INVALID_ARG, "%s: node %u is no node's child", fn, d);
+        if (nd.left == 0 && nd.right == 0) {
+            if (nd.tri >= N) return fail(CRT_ERR_INVALID_ARG, "%s: leaf %u names triangle %u", fn, d, nd.tri);
+            if (seen[nd.tri]) return fail(CRT_ERR_INVALID_ARG, "%s: triangle %u in two leaves", fn, nd.tri);
+            seen[nd.tri] = 1;
+            if (n_leaf >= N) return fail(CRT_ERR_INVALID_ARG, "%s: more than %u leaves", fn, N);
+            o.idx[d] = n_leaf;
+            o.leaf_pos[n_leaf++] = d;
+        } else {
+            if (nd.left != d + 1 || nd.right <= nd.left || nd.right >= n_nodes || referenced[nd.left] ||
+                referenced[nd.right])
+                return fail(CRT_ERR_INVALID_ARG, "%s: node %u is not in DFS pre-order (children %u, %u)", fn, d, nd.left,
+                            nd.right);
+            if (n_int + 1 >= N) return fail(CRT_ERR_INVALID_ARG, "%s: more than %u internal nodes", fn, N - 1);
+            referenced[nd.left] = referenced[nd.right] = 1;
+            dep[nd.left] = dep[nd.right] = dep[d] + 1;
+            o.max_depth = std::max(o.max_depth, dep[d] + 1);
+            o.idx[d] = n_int;
+            o.int_pos[n_int++] = d;
+        }
+    }
+    if (n_leaf != N || n_int != N - 1)
+        return fail(CRT_ERR_INVALID_ARG, "%s: %u leaves and %u internal nodes for %u triangles", fn, n_leaf, n_int, N);
+    for (uint32_t d = n_nodes; d-- > 0;) {  // children follow their parent: a reverse sweep counts leaves
+        const crt_bvh_node& nd = h[d];
+        if (nd.left == 0 && nd.right == 0) {
+            leaves[d] = 1;
+            continue;
+        }
+        leaves[d] = leaves[nd.left] + leaves[nd.right];
+        if (nd.right != nd.left + 2 * leaves[nd.left] - 1)
+            return fail(CRT_ERR_INVALID_ARG, "%s: node %u's right child does not follow its left subtree", fn, d);
+        o.lc[o.idx[d]] = make_uint2(leaves[nd.left], leaves[nd.right]);
+        o.odd[o.idx[d]] = static_cast<uint8_t>(dep[d] & 1u);
+    }
+    if (leaves[0] != N) return fail(CRT_ERR_INVALID_ARG, "%s: the root holds %u of %u leaves", fn, leaves[0], N);
+    return CRT_OK;
+}
+
+// A host copy of the caller's node array (host or device memory).
+static crt_status host_nodes(const crt_bvh_node* nodes, uint32_t n_nodes, std::vector<crt_bvh_node>* h) {
+    h->resize(n_nodes);
+    if (is_device_ptr(nodes)) {
+        CRT_CUDA(cudaMemcpy(h->data(), nodes, sizeof(crt_bvh_node) * n_nodes, cudaMemcpyDeviceToHost));
+    } else {
+        std::memcpy(h->data(), nodes, sizeof(crt_bvh_node) * n_nodes);
+    }
+    return CRT_OK;
+}
+
+crt_status crt_validate_nodes(const crt_bvh_node* nodes, uint32_t n_nodes, uint32_t n_tris, uint32_t info[4]) {
+    if (!nodes) return fail(CRT_ERR_INVALID_ARG, "crt_validate_nodes: null nodes");
+    if (n_tris == 0 || n_nodes != 2 * n_tris - 1)
+        return fail(CRT_ERR_INVALID_ARG, "crt_validate_nodes: %u nodes for %u triangles (need 2n-1)", n_nodes, n_tris);
+    std::vector<crt_bvh_node> h;
+    CRT_TRY(host_nodes(nodes, n_nodes, &h));
+    NodeNumbering num;
+    CRT_TRY(number_nodes(h.data(), n_nodes, n_tris, "crt_validate_nodes", &num));
+    if (info) {
+        info[0] = n_tris;
+        info[1] = n_tris - 1;
+        info[2] = num.max_depth;
+        info[3] = 0;
+    }
+    return CRT_OK;
+}
+
 crt_status crt_bvh_from_nodes(crt_ctx* x, const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris,
                               uint32_t n_tris, const crt_mesh_model* models, uint32_t n_models, crt_bvh** out) {
     if (!x || !nodes || !tris || !out) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: null argument");
@@ -785,62 +881,16 @@ crt_status crt_bvh_from_nodes(crt_ctx* x, const crt_bvh_node* nodes, uint32_t n_
     const uint32_t N = n_tris;
     if (is_device_ptr(tris)) CRT_TRY(check_aligned16(tris, "crt_bvh_from_nodes: triangles"));
     // the array on the host, for the structure check and the numbering
-    std::vector<crt_bvh_node> h(n_nodes);
-    if (is_device_ptr(nodes)) {
-        CRT_CUDA(cudaMemcpy(h.data(), nodes, sizeof(crt_bvh_node) * n_nodes, cudaMemcpyDeviceToHost));
-    } else {
-        std::memcpy(h.data(), nodes, sizeof(crt_bvh_node) * n_nodes);
-    }
-    // DFS pre-order, left child first (scene.cpp:189-208): an internal node at d
-    // has its left child at d + 1 and its right child after the left subtree;
-    // a leaf (both children 0, raytracer.glsl:239-244) names one triangle, each
-    // triangle once.  Numbering: leaves and internal nodes in order of position.
-    std::vector<uint32_t> idx(n_nodes), leaves(n_nodes), int_pos(N > 1 ? N - 1 : 1), leaf_pos(N);
-    std::vector<uint2> lc(N > 1 ? N - 1 : 1);
-    std::vector<uint8_t> seen(N, 0), odd(N > 1 ? N - 1 : 1, 0);
-    std::vector<uint8_t> referenced(n_nodes, 0);
-    uint32_t n_leaf = 0, n_int = 0, max_depth = 0;
-    std::vector<uint32_t> dep(n_nodes, 0);
-    for (uint32_t d = 0; d < n_nodes; ++d) {
-        const crt_bvh_node& nd = h[d];
-        if (d > 0 && !referenced[d])
-            return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: node %u is no node's child", d);
-        if (nd.left == 0 && nd.right == 0) {
-            if (nd.tri >= N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: leaf %u names triangle %u", d, nd.tri);
-            if (seen[nd.tri]) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: triangle %u in two leaves", nd.tri);
-            seen[nd.tri] = 1;
-            if (n_leaf >= N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: more than %u leaves", N);
-            idx[d] = n_leaf;
-            leaf_pos[n_leaf++] = d;
-        } else {
-            if (nd.left != d + 1 || nd.right <= nd.left || nd.right >= n_nodes || referenced[nd.left] ||
-                referenced[nd.right])
-                return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: node %u is not in DFS pre-order (children %u, %u)",
-                            d, nd.left, nd.right);
-            if (n_int + 1 >= N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: more than %u internal nodes", N - 1);
-            referenced[nd.left] = referenced[nd.right] = 1;
-            dep[nd.left] = dep[nd.right] = dep[d] + 1;
-            max_depth = std::max(max_depth, dep[d] + 1);
-            idx[d] = n_int;
-            int_pos[n_int++] = d;
-        }
-    }
-    if (n_leaf != N || n_int != N - 1)
-        return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: %u leaves and %u internal nodes for %u triangles", n_leaf,
-                    n_int, N);
-    for (uint32_t d = n_nodes; d-- > 0;) {  // children follow their parent: a reverse sweep counts leaves
-        const crt_bvh_node& nd = h[d];
-        if (nd.left == 0 && nd.right == 0) {
-            leaves[d] = 1;
-            continue;
-        }
-        leaves[d] = leaves[nd.left] + leaves[nd.right];
-        if (nd.right != nd.left + 2 * leaves[nd.left] - 1)
-            return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: node %u's right child does not follow its left subtree", d);
-        lc[idx[d]] = make_uint2(leaves[nd.left], leaves[nd.right]);
-        odd[idx[d]] = static_cast<uint8_t>(dep[d] & 1u);
-    }
-    if (leaves[0] != N) return fail(CRT_ERR_INVALID_ARG, "crt_bvh_from_nodes: the root holds %u of %u leaves", leaves[0], N);
+    std::vector<crt_bvh_node> h;
+    CRT_TRY(host_nodes(nodes, n_nodes, &h));
+    NodeNumbering num;
+    CRT_TRY(number_nodes(h.data(), n_nodes, N, "crt_bvh_from_nodes", &num));
+    const std::vector<uint32_t>& idx = num.idx;
+    const std::vector<uint32_t>& int_pos = num.int_pos;
+    const std::vector<uint32_t>& leaf_pos = num.leaf_pos;
+    const std::vector<uint2>& lc = num.lc;
+    const std::vector<uint8_t>& odd = num.odd;
+    const uint32_t max_depth = num.max_depth;
 
     crt_bvh* b = new crt_bvh();
     auto fail_free = [&](crt_status st) {
