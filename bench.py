@@ -295,6 +295,36 @@ def run_ours(args):
                            "64 B record per triangle, L2 flushed before each call"}
     del d_mv, d_mf, d_mt
 
+    # ---- the trace side alone over a node array built elsewhere: the reference's
+    # CPU build hands its shader this same DFS array (host memory), which
+    # crt_bvh_from_nodes makes traceable; the frame over it must equal the frame
+    # over the built handle
+    nodes_h = bvh.nodes()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    imp = ctx.bvh_from_nodes(nodes_h, tris, models=models)
+    import_ms = (time.perf_counter() - t0) * 1e3
+    hp_i, hs_i = torch.empty_like(hp), torch.empty_like(hs)
+    ctx.trace_frame(bvh, d_cam, W, H, light, flags, hits_primary=hp, hits_shadow=hs)
+    iev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ctx.trace_frame(imp, d_cam, W, H, light, flags, hits_primary=hp_i, hits_shadow=hs_i)
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            l2_flush.zero_()
+            iev[k][0].record(stream)
+            ctx.trace_frame(imp, d_cam, W, H, light, flags, hits_primary=hp_i, hits_shadow=hs_i)
+            iev[k][1].record(stream)
+    torch.cuda.synchronize()
+    imported_tree = {
+        "import_ms": round(import_ms, 3),
+        "frame_ms": round(statistics.mean(a.elapsed_time(b) for a, b in iev), 4),
+        "identical_hits": bool(torch.equal(hp_i.view(torch.int32), hp.view(torch.int32)) and
+                               torch.equal(hs_i[:, 0].view(torch.int32) == -1, hs[:, 0].view(torch.int32) == -1)),
+        "note": "crt_bvh_from_nodes from the 2,621,439-record node array in host memory (structure check, "
+                "upload, traversal records; host-timed), then the one-launch frame over the imported tree"}
+    imp.free()
+    del hp_i, hs_i
+
     # ---- the reference's whole compute pass (getRay, closest hit, getColor,
     # imageStore) into a device RGBA32F image: crt_render_frame, one launch
     img = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
@@ -388,6 +418,7 @@ def run_ours(args):
                                      "node_fetches_per_ray": round(p_visited / n_rays, 2),
                                      "tris_per_ray": round(p_tested / n_rays, 2)},
             "mesh_upload": mesh_upload,
+            "imported_tree": imported_tree,
             "shaded_frame": dict(shaded, note="crt_render_frame: camera ray, closest hit, getColor and "
                                               "imageStore per texel into a device RGBA32F image, no shadow rays"),
             "cpu_baseline": cpu,
