@@ -13,9 +13,12 @@
  * Every stage runs as hand-written CUDA kernels for sm_103a on one GPU.
  *
  * Conventions
- *   - Plain pointers and sizes only.  Every pointer argument may point to host
- *     or device memory; the library checks with cudaPointerGetAttributes and
- *     copies host data in and out on the context's stream.
+ *   - Plain pointers and sizes only.  The single-scene calls accept each
+ *     pointer in host or device memory; the library checks with
+ *     cudaPointerGetAttributes and copies host data in and out on the
+ *     context's stream.  The batched calls (crt_batch_*) and
+ *     crt_morton_sort_noalloc take device memory for their triangles, rays,
+ *     hits and outputs and refuse host pointers (CRT_ERR_INVALID_ARG).
  *   - Calls are ordered on the context's stream.  Functions that return data
  *     to host memory synchronise that stream before returning.
  *   - Errors come back as crt_status; crt_last_error_string() describes the
@@ -262,6 +265,15 @@ crt_status crt_last_build_stats(crt_ctx* ctx, crt_build_stats* stats);
  * (CRT_ERR_DEVICE_TIMEOUT, the context stays usable).  spin_limit 0 = the
  * context's limit. */
 crt_status crt_selftest_wait(crt_ctx* ctx, int set_flag, uint32_t spin_limit);
+/* Failure detection check of the tensor-core wait the predictor kernels use
+ * (an mbarrier that an MMA commit completes): one CTA allocates tensor
+ * memory, then with complete != 0 issues and commits one MMA and reads the
+ * result back (CRT_OK when it is right); with complete == 0 it waits on a
+ * phase nothing completes, gives up after spin_limit rounds
+ * (CRT_ERR_DEVICE_TIMEOUT), frees its tensor memory without reading it and
+ * returns, so the context and later predictor calls stay usable.  spin_limit
+ * 0 = the predictor kernels' own limit. */
+crt_status crt_selftest_tc_wait(crt_ctx* ctx, int complete, uint32_t spin_limit);
 
 /* ---- rays ------------------------------------------------------------- */
 /* Primary rays of getRay (raytracer.glsl:92-100) for a width x height image:

@@ -22,7 +22,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_bvh.so")
-REFERENCE_DIR = "/root/reference"
+# The reference checkout: CRT_REFERENCE_DIR, else a directory named
+# "reference" beside the repository.
+REFERENCE_DIR = os.environ.get("CRT_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 _lib = None
 _ref = None
@@ -36,7 +38,7 @@ def build(ref: bool | None = None) -> None:
         ref = os.path.isdir(os.path.join(REFERENCE_DIR, "srcCommon"))
     if ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, *targets], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"REFERENCE_DIR={REFERENCE_DIR}", *targets], check=True)
 
 
 def _p(a):

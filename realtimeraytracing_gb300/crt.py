@@ -52,7 +52,7 @@ EXPORTS = [
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
     "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_bvh_from_nodes",
     "crt_validate_nodes", "crt_obj_parse",
-    "crt_triangles_from_indexed", "crt_selftest_wait",
+    "crt_triangles_from_indexed", "crt_selftest_wait", "crt_selftest_tc_wait",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -147,6 +147,7 @@ def lib():
             "crt_obj_parse": ([C.c_char_p, C.c_size_t, vp, u32, vp, u32, vp], i32),
             "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
             "crt_selftest_wait": ([vp, i32, u32], i32),
+            "crt_selftest_tc_wait": ([vp, i32, u32], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -509,6 +510,10 @@ class Context:
     def selftest_wait(self, set_flag: bool, spin_limit: int = 0):
         """crt_selftest_wait: one bounded device wait on a flag (set or never set)."""
         _check(lib().crt_selftest_wait(self.handle, 1 if set_flag else 0, spin_limit))
+
+    def selftest_tc_wait(self, complete: bool, spin_limit: int = 0):
+        """crt_selftest_tc_wait: one MMA commit wait (completed, or never completed)."""
+        _check(lib().crt_selftest_tc_wait(self.handle, 1 if complete else 0, spin_limit))
 
     def build(self, tris, n_tris=None, models=None, n_buffer=None) -> Bvh:
         """cr::BVH::BVH(nbTriangles, unsortedTriangles, meshesInTheScene)."""

@@ -322,6 +322,23 @@ crt_status crt_selftest_wait(crt_ctx* x, int set_flag, uint32_t spin_limit) {
     return x->check_device_error();
 }
 
+crt_status crt_selftest_tc_wait(crt_ctx* x, int complete, uint32_t spin_limit) {
+    if (!x) return fail(CRT_ERR_INVALID_ARG, "null context");
+    CRT_CUDA(cudaSetDevice(x->device));
+    CRT_TRY(x->probe_flag.reserve(128 * sizeof(float)));
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
+    CRT_CUDA(cudaMemsetAsync(x->probe_flag.p, 0, 128 * sizeof(float), x->stream));
+    CRT_CUDA(crt::tc_wait_probe(complete, spin_limit, x->err.as<uint32_t>(), x->probe_flag.as<float>(), x->stream));
+    const crt_status st = x->check_device_error();
+    if (st != CRT_OK || !complete) return st;
+    float got[128];
+    CRT_CUDA(cudaMemcpyAsync(got, x->probe_flag.p, sizeof(got), cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    for (int i = 0; i < 128; ++i)
+        if (got[i] != 16.f) return fail(CRT_ERR_CUDA, "MMA probe: lane %d read %g, expected 16", i, got[i]);
+    return CRT_OK;
+}
+
 crt_status crt_sync(crt_ctx* x) {
     if (!x) return fail(CRT_ERR_INVALID_ARG, "null context");
     CRT_CUDA(cudaStreamSynchronize(x->stream));

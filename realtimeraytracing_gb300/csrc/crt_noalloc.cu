@@ -21,9 +21,15 @@
 // Host code cannot use the array's name as a device address, so the first
 // call on each device looks the address up with cudaGetSymbolAddress while
 // that device is current; make that first call before any stream capture.
+// The address is kept per device together with the unique id of the CUDA
+// context it was looked up in (cuCtxGetId): after cudaDeviceReset the device
+// gets a new primary context, the library's device code is loaded again and
+// the array may move, so a call that finds a different context id looks the
+// address up again instead of using the stale one.
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <mutex>
 
@@ -75,7 +81,42 @@ __global__ void noalloc_clear_kernel(unsigned char* scratch) {
 }
 
 std::mutex g_setup_mu;
-void* g_scratch_addr[64] = {};
+// Per device ordinal: the scratch array's device address and the id of the
+// context it belongs to (0 = not looked up yet).
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    void* addr;
+};
+ScratchSlot g_scratch_slot[64] = {};
+
+// Unique id of the calling thread's current CUDA context (never reused
+// within a process), through the driver entry points the runtime exposes, so
+// that the library needs no link to the driver library.  False when the
+// driver cannot tell (no current context yet, or an old driver).
+bool current_context_id(unsigned long long* id) {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+        cudaGetLastError();
+        resolved = true;
+    }
+    if (!get_current || !get_id) return false;
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || c == nullptr) return false;
+    return get_id(c, id) == CUDA_SUCCESS && *id != 0;
+}
 
 crt_status nerr(crt_status s, const char* msg, cudaError_t e = cudaSuccess) {
     char buf[256];
@@ -87,7 +128,19 @@ crt_status nerr(crt_status s, const char* msg, cudaError_t e = cudaSuccess) {
     return s;
 }
 
-bool on_device(const void* p) {
+// Device (or managed) memory of device `dev`: every launch runs on the
+// current device, so buffers of another GPU are refused rather than reached
+// through peer access.
+bool on_device(const void* p, int dev) {
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev;
+}
+
+bool is_device_memory(const void* p) {
     cudaPointerAttributes a;
     if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
@@ -113,25 +166,32 @@ crt_status crt_morton_sort_noalloc(const crt_triangle* tris, uint32_t n_buffer, 
     if (n_buffer < n_tris) return nerr(CRT_ERR_INVALID_ARG, "crt_morton_sort_noalloc: n_buffer < n_tris");
     if (n_models > kMaxModels) return nerr(CRT_ERR_INVALID_ARG, "crt_morton_sort_noalloc: more than 64 models");
     if (n_models > 0 && !models) return nerr(CRT_ERR_INVALID_ARG, "crt_morton_sort_noalloc: null models");
-    if (!on_device(tris) || !on_device(codes_out) || !on_device(perm_out))
-        return nerr(CRT_ERR_INVALID_ARG, "crt_morton_sort_noalloc: tris, codes_out and perm_out must be device memory");
-    if (n_models > 0 && on_device(models))
-        return nerr(CRT_ERR_INVALID_ARG, "crt_morton_sort_noalloc: models must be host memory");
-
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return nerr(CRT_ERR_CUDA, "cudaGetDevice", e);
     if (dev < 0 || dev >= 64) return nerr(CRT_ERR_UNSUPPORTED, "crt_morton_sort_noalloc: device ordinal above 63");
+    if (!on_device(tris, dev) || !on_device(codes_out, dev) || !on_device(perm_out, dev))
+        return nerr(CRT_ERR_INVALID_ARG,
+                    "crt_morton_sort_noalloc: tris, codes_out and perm_out must be device memory of the current device");
+    if (n_models > 0 && is_device_memory(models))
+        return nerr(CRT_ERR_INVALID_ARG, "crt_morton_sort_noalloc: models must be host memory");
+
     unsigned char* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_setup_mu);
-        if (!g_scratch_addr[dev]) {
+        ScratchSlot& slot = g_scratch_slot[dev];
+        unsigned long long id = 0;
+        const bool have_id = current_context_id(&id);
+        if (!slot.addr || !have_id || slot.ctx_id != id) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess || !p) return nerr(CRT_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch)", e);
-            g_scratch_addr[dev] = p;
+            // the lookup makes the device's primary context current if it was not yet
+            if (!have_id && !current_context_id(&id)) id = 0;
+            slot.addr = p;
+            slot.ctx_id = id;
         }
-        scratch = static_cast<unsigned char*>(g_scratch_addr[dev]);
+        scratch = static_cast<unsigned char*>(slot.addr);
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 

@@ -111,10 +111,13 @@ __device__ __forceinline__ void gemm(uint32_t d_tmem, const unsigned char* A, co
                     id, kk > 0);
 }
 
+constexpr uint32_t kMmaWaitLimit = 1u << 26;  // try_wait rounds before a tile gives up
+
 struct Sync {
     uint64_t* mbar;
     uint32_t phase = 0;
     uint32_t* err;
+    uint32_t limit = kMmaWaitLimit;
     // Publish generic smem writes to the tensor core and order tcgen05 work.
     __device__ __forceinline__ void before_mma() {
         tc::fence_async_smem();
@@ -122,11 +125,26 @@ struct Sync {
         __syncthreads();
         tc::fence_after_sync();
     }
-    __device__ __forceinline__ void commit_and_wait() {
-        if (threadIdx.x == 0) tc::mma_commit(mbar);
-        if (!tc::mbar_wait(mbar, phase, 1u << 26)) raise_error(err, kDevTimeout);
-        phase ^= 1u;
+    // Commit the MMAs thread 0 issued and wait for them (issue = false waits
+    // on a phase nothing will complete: the self-test's way to make the wait
+    // run out).  Block-uniform result: false when any thread's bounded wait
+    // gave up.  Then the error word is set and every thread waits once more,
+    // again bounded, so that MMAs still in flight finish writing TMEM before
+    // the caller frees it; the caller must leave its tile loop without
+    // reading TMEM or issuing more MMAs.
+    __device__ __forceinline__ bool commit_and_wait(bool issue = true) {
+        if (issue && threadIdx.x == 0) tc::mma_commit(mbar);
+        const bool ok = tc::mbar_wait(mbar, phase, limit);
+        if (__syncthreads_and(ok)) {
+            phase ^= 1u;
+            tc::fence_after_sync();
+            return true;
+        }
+        if (threadIdx.x == 0) raise_error(err, kDevTimeout);
+        tc::mbar_wait(mbar, phase, limit);
         tc::fence_after_sync();
+        __syncthreads();
+        return false;
     }
 };
 
@@ -195,7 +213,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         for (int c = 0; c < 4; ++c) *reinterpret_cast<uint4*>(sX + kmajor_offset(tid, 8 * c, 32)) = e[c];
         sy.before_mma();
         if (tid == 0) gemm(tb + 0, sX, sW1, 32, 128, 64);
-        sy.commit_and_wait();
+        if (!sy.commit_and_wait()) break;
         for (int c = 0; c < 64; c += 16) {
             float v[16];
             tc::tmem_ld16(lane_addr(tb, c), v);
@@ -206,7 +224,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         }
         sy.before_mma();
         if (tid == 0) gemm(tb + 64, sH1, sW2, 64, 128, 64);
-        sy.commit_and_wait();
+        if (!sy.commit_and_wait()) break;
         for (int c = 0; c < 64; c += 16) {
             float v[16];
             tc::tmem_ld16(lane_addr(tb, 64 + c), v);
@@ -217,7 +235,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         }
         sy.before_mma();
         if (tid == 0) gemm(tb + 0, sH2, sW3, 64, 128, 128);  // logits over D1 and D2, both read out
-        sy.commit_and_wait();
+        if (!sy.commit_and_wait()) break;
         // Seed the most likely treelet unless the miss class holds at least
         // `miss_threshold` of the probability mass.
         float best = -INFINITY, lmax = -INFINITY, lmiss = 0.f;
@@ -332,165 +350,199 @@ __global__ void __launch_bounds__(128) train_kernel(PredictorDev P, const crt_bv
     sy.before_mma();
     const uint32_t tb = *sT;
 
-    // ---- forward
-    if (tid == 0) gemm(tb + 0, sX, sW1, 32, 128, 64);
-    sy.commit_and_wait();
-    for (int c = 0; c < 64; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, c), v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            v[j] = __half2float(__float2half_rn(fmaxf(v[j] + sB[c + j], 0.f)));
-            store_h(sH1T, 128, c + j, tid, v[j]);
-        }
-        store_row8(sH1, 64, tid, c, v);
-        store_row8(sH1, 64, tid, c + 8, v + 8);
-    }
-    sy.before_mma();
-    if (tid == 0) gemm(tb + 64, sH1, sW2, 64, 128, 64);
-    sy.commit_and_wait();
-    for (int c = 0; c < 64; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, 64 + c), v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            v[j] = __half2float(__float2half_rn(fmaxf(v[j] + sB[64 + c + j], 0.f)));
-            store_h(sH2T, 128, c + j, tid, v[j]);
-        }
-        store_row8(sH2, 64, tid, c, v);
-        store_row8(sH2, 64, tid, c + 8, v + 8);
-    }
-    sy.before_mma();
-    if (tid == 0) gemm(tb + 128, sH2, sW3, 64, 128, 128);
-    sy.commit_and_wait();
-
-    // ---- softmax cross-entropy: G3 = p - onehot(target)
-    float mx = -INFINITY;
-    for (int c = 0; c < 128; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) mx = fmaxf(mx, v[j] + sB[128 + c + j]);
-    }
-    float sum = 0.f;
-    for (int c = 0; c < 128; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - mx);
-    }
-    const float inv = 1.f / sum;
-    for (int c = 0; c < 128; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const float l = v[j] + sB[128 + c + j];
-            const float p = __expf(l - mx) * inv;
-            float g = p - ((c + j) == target ? 1.f : 0.f);
-            if (!valid) g = 0.f;
-            if (valid && (c + j) == target) atomicAdd(loss_sum, -(l - mx - __logf(sum)));
-            v[j] = __half2float(__float2half_rn(g));
-            store_h(sG3T, 128, c + j, tid, v[j]);
-        }
-        store_row8(sG3, 128, tid, c, v);
-        store_row8(sG3, 128, tid, c + 8, v + 8);
-    }
-    // ---- dW3 = G3^T H2 and dH2 = G3 W3
-    sy.before_mma();
-    if (tid == 0) {
-        gemm(tb + 0, sG3T, sH2T, 128, 128, 64);
-        gemm(tb + 64, sG3, sW3T, 128, 128, 64);
-    }
-    sy.commit_and_wait();
-    {
-        float acc = 0.f;  // db3[tid] = sum over samples of G3[:, tid]
-        for (int b = 0; b < 128; ++b) acc += load_h(sG3T, 128, tid, b);
-        atomicAdd(grad + oB3 + tid, acc);
-    }
-    for (int c = 0; c < 64; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, c), v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) atomicAdd(grad + oW3 + tid * 64 + c + j, v[j]);
-    }
-    float dh[64];
-    for (int c = 0; c < 64; c += 16) tc::tmem_ld16(lane_addr(tb, 64 + c), dh + c);
-    tc::fence_before_sync();
-    __syncthreads();  // G3 / G3T fully consumed
-    zero_bytes(sGT + 64 * 128 * 2, 64 * 128 * 2);  // padding rows 64..127 of G2T
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-        dh[j] = (load_h(sH2, 64, tid, j) > 0.f) ? __half2float(__float2half_rn(dh[j])) : 0.f;
-        store_h(sGT, 128, j, tid, dh[j]);
-    }
-    for (int c = 0; c < 64; c += 8) store_row8(sG, 64, tid, c, dh + c);
-    // ---- dW2 = G2^T H1 and dH1 = G2 W2
-    sy.before_mma();
-    if (tid == 0) {
-        gemm(tb + 128, sGT, sH1T, 128, 128, 64);
-        gemm(tb + 192, sG, sW2T, 64, 128, 64);
-    }
-    sy.commit_and_wait();
-    if (tid < 64) {
-        float acc = 0.f;
-        for (int b = 0; b < 128; ++b) acc += load_h(sGT, 128, tid, b);
-        atomicAdd(grad + oB2 + tid, acc);
-    }
-    for (int c = 0; c < 64; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, 128 + c), v);
-        if (tid < 64) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) atomicAdd(grad + oW2 + tid * 64 + c + j, v[j]);
-        }
-    }
-    for (int c = 0; c < 64; c += 16) tc::tmem_ld16(lane_addr(tb, 192 + c), dh + c);
-    tc::fence_before_sync();
-    __syncthreads();
-    zero_bytes(sGT + 64 * 128 * 2, 64 * 128 * 2);
-#pragma unroll
-    for (int j = 0; j < 64; ++j) {
-        dh[j] = (load_h(sH1, 64, tid, j) > 0.f) ? __half2float(__float2half_rn(dh[j])) : 0.f;
-        store_h(sGT, 128, j, tid, dh[j]);
-    }
-    for (int c = 0; c < 64; c += 8) store_row8(sG, 64, tid, c, dh + c);
-    // ---- dW1 = G1^T X and dX = G1 W1
-    sy.before_mma();
-    if (tid == 0) {
-        gemm(tb + 0, sGT, sXT, 128, 128, 32);
-        gemm(tb + 32, sG, sW1T, 64, 128, 32);
-    }
-    sy.commit_and_wait();
-    if (tid < 64) {
-        float acc = 0.f;
-        for (int b = 0; b < 128; ++b) acc += load_h(sGT, 128, tid, b);
-        atomicAdd(grad + oB1 + tid, acc);
-    }
-    for (int c = 0; c < 32; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, c), v);
-        if (tid < 64) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) atomicAdd(grad + oW1 + tid * 32 + c + j, v[j]);
-        }
-    }
-    for (int c = 0; c < 32; c += 16) {
-        float v[16];
-        tc::tmem_ld16(lane_addr(tb, 32 + c), v);
-        if (valid) {
+    // One pass through the tile; a timed-out MMA wait leaves it (break) to
+    // the TMEM release below.
+    do {
+        // ---- forward
+        if (tid == 0) gemm(tb + 0, sX, sW1, 32, 128, 64);
+        if (!sy.commit_and_wait()) break;
+        for (int c = 0; c < 64; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, c), v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-                const int ee = c + j;
-                float* dst = ee < kEmb ? grad + oEo + static_cast<size_t>(cell) * kEmb + ee
-                                       : grad + oEd + static_cast<size_t>(bin) * kEmb + (ee - kEmb);
-                atomicAdd(dst, v[j]);
+                v[j] = __half2float(__float2half_rn(fmaxf(v[j] + sB[c + j], 0.f)));
+                store_h(sH1T, 128, c + j, tid, v[j]);
+            }
+            store_row8(sH1, 64, tid, c, v);
+            store_row8(sH1, 64, tid, c + 8, v + 8);
+        }
+        sy.before_mma();
+        if (tid == 0) gemm(tb + 64, sH1, sW2, 64, 128, 64);
+        if (!sy.commit_and_wait()) break;
+        for (int c = 0; c < 64; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 64 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                v[j] = __half2float(__float2half_rn(fmaxf(v[j] + sB[64 + c + j], 0.f)));
+                store_h(sH2T, 128, c + j, tid, v[j]);
+            }
+            store_row8(sH2, 64, tid, c, v);
+            store_row8(sH2, 64, tid, c + 8, v + 8);
+        }
+        sy.before_mma();
+        if (tid == 0) gemm(tb + 128, sH2, sW3, 64, 128, 128);
+        if (!sy.commit_and_wait()) break;
+
+        // ---- softmax cross-entropy: G3 = p - onehot(target)
+        float mx = -INFINITY;
+        for (int c = 0; c < 128; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) mx = fmaxf(mx, v[j] + sB[128 + c + j]);
+        }
+        float sum = 0.f;
+        for (int c = 0; c < 128; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - mx);
+        }
+        const float inv = 1.f / sum;
+        for (int c = 0; c < 128; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float l = v[j] + sB[128 + c + j];
+                const float p = __expf(l - mx) * inv;
+                float g = p - ((c + j) == target ? 1.f : 0.f);
+                if (!valid) g = 0.f;
+                if (valid && (c + j) == target) atomicAdd(loss_sum, -(l - mx - __logf(sum)));
+                v[j] = __half2float(__float2half_rn(g));
+                store_h(sG3T, 128, c + j, tid, v[j]);
+            }
+            store_row8(sG3, 128, tid, c, v);
+            store_row8(sG3, 128, tid, c + 8, v + 8);
+        }
+        // ---- dW3 = G3^T H2 and dH2 = G3 W3
+        sy.before_mma();
+        if (tid == 0) {
+            gemm(tb + 0, sG3T, sH2T, 128, 128, 64);
+            gemm(tb + 64, sG3, sW3T, 128, 128, 64);
+        }
+        if (!sy.commit_and_wait()) break;
+        {
+            float acc = 0.f;  // db3[tid] = sum over samples of G3[:, tid]
+            for (int b = 0; b < 128; ++b) acc += load_h(sG3T, 128, tid, b);
+            atomicAdd(grad + oB3 + tid, acc);
+        }
+        for (int c = 0; c < 64; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, c), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) atomicAdd(grad + oW3 + tid * 64 + c + j, v[j]);
+        }
+        float dh[64];
+        for (int c = 0; c < 64; c += 16) tc::tmem_ld16(lane_addr(tb, 64 + c), dh + c);
+        tc::fence_before_sync();
+        __syncthreads();  // G3 / G3T fully consumed
+        zero_bytes(sGT + 64 * 128 * 2, 64 * 128 * 2);  // padding rows 64..127 of G2T
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+            dh[j] = (load_h(sH2, 64, tid, j) > 0.f) ? __half2float(__float2half_rn(dh[j])) : 0.f;
+            store_h(sGT, 128, j, tid, dh[j]);
+        }
+        for (int c = 0; c < 64; c += 8) store_row8(sG, 64, tid, c, dh + c);
+        // ---- dW2 = G2^T H1 and dH1 = G2 W2
+        sy.before_mma();
+        if (tid == 0) {
+            gemm(tb + 128, sGT, sH1T, 128, 128, 64);
+            gemm(tb + 192, sG, sW2T, 64, 128, 64);
+        }
+        if (!sy.commit_and_wait()) break;
+        if (tid < 64) {
+            float acc = 0.f;
+            for (int b = 0; b < 128; ++b) acc += load_h(sGT, 128, tid, b);
+            atomicAdd(grad + oB2 + tid, acc);
+        }
+        for (int c = 0; c < 64; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 128 + c), v);
+            if (tid < 64) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) atomicAdd(grad + oW2 + tid * 64 + c + j, v[j]);
             }
         }
-    }
+        for (int c = 0; c < 64; c += 16) tc::tmem_ld16(lane_addr(tb, 192 + c), dh + c);
+        tc::fence_before_sync();
+        __syncthreads();
+        zero_bytes(sGT + 64 * 128 * 2, 64 * 128 * 2);
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+            dh[j] = (load_h(sH1, 64, tid, j) > 0.f) ? __half2float(__float2half_rn(dh[j])) : 0.f;
+            store_h(sGT, 128, j, tid, dh[j]);
+        }
+        for (int c = 0; c < 64; c += 8) store_row8(sG, 64, tid, c, dh + c);
+        // ---- dW1 = G1^T X and dX = G1 W1
+        sy.before_mma();
+        if (tid == 0) {
+            gemm(tb + 0, sGT, sXT, 128, 128, 32);
+            gemm(tb + 32, sG, sW1T, 64, 128, 32);
+        }
+        if (!sy.commit_and_wait()) break;
+        if (tid < 64) {
+            float acc = 0.f;
+            for (int b = 0; b < 128; ++b) acc += load_h(sGT, 128, tid, b);
+            atomicAdd(grad + oB1 + tid, acc);
+        }
+        for (int c = 0; c < 32; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, c), v);
+            if (tid < 64) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) atomicAdd(grad + oW1 + tid * 32 + c + j, v[j]);
+            }
+        }
+        for (int c = 0; c < 32; c += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 32 + c), v);
+            if (valid) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int ee = c + j;
+                    float* dst = ee < kEmb ? grad + oEo + static_cast<size_t>(cell) * kEmb + ee
+                                           : grad + oEd + static_cast<size_t>(bin) * kEmb + (ee - kEmb);
+                    atomicAdd(dst, v[j]);
+                }
+            }
+        }
+    } while (false);
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x < 32) tc::tmem_dealloc(tb, 256);
+}
+
+// ---------------------------------------------- failure-detection probe
+// The MMA wait of the kernels above, alone: one CTA allocates 32 TMEM
+// columns, then either issues one 128 x 32 x 16 MMA of all-ones tiles and
+// commits it (complete != 0; every output is 16) or waits on a phase that
+// nothing completes.  In the second case the bounded wait gives up, the error
+// word gets kDevTimeout, TMEM is not read, and the CTA still frees its TMEM
+// and returns, so later tcgen05 kernels on the device can allocate again.
+__global__ void __launch_bounds__(128) tc_wait_probe_kernel(int complete, uint32_t limit, uint32_t* err, float* out) {
+    __shared__ __align__(1024) unsigned char sA[128 * 16 * 2];
+    __shared__ __align__(1024) unsigned char sB[32 * 16 * 2];
+    __shared__ uint32_t sT[2];
+    __shared__ __align__(8) uint64_t sM[1];
+    for (int i = threadIdx.x; i < 128 * 16; i += 128) reinterpret_cast<__half*>(sA)[i] = __float2half_rn(1.f);
+    for (int i = threadIdx.x; i < 32 * 16; i += 128) reinterpret_cast<__half*>(sB)[i] = __float2half_rn(1.f);
+    if (threadIdx.x < 32) { tc::tmem_alloc(sT, 32); tc::tmem_relinquish(); }
+    if (threadIdx.x == 0) tc::mbar_init(sM, 1);
+    Sync sy{sM, 0, err, limit};
+    sy.before_mma();
+    const uint32_t tb = *sT;
+    if (complete && threadIdx.x == 0) gemm(tb, sA, sB, 16, 128, 32);
+    if (sy.commit_and_wait(complete != 0)) {
+        float v[16];
+        tc::tmem_ld16(lane_addr(tb, 0), v);
+        out[threadIdx.x] = v[0];
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_dealloc(tb, 32);
 }
 
 // ------------------------------------------------------------ optimiser
@@ -772,6 +824,11 @@ void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* 
         launch_onesweep(kin[p], vin[p], kout[p], vout[p], n, 8 * p, 8, hist + 256 * p, l + 1, l, err, spin_limit, s);
     }
 }
+cudaError_t tc_wait_probe(int complete, uint32_t limit, uint32_t* err, float* out, cudaStream_t s) {
+    pred::tc_wait_probe_kernel<<<1, 128, 0, s>>>(complete, limit ? limit : pred::kMmaWaitLimit, err, out);
+    return cudaGetLastError();
+}
+
 void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s) {
     pred::init_kernel<<<kNumSms * 8, 256, 0, s>>>(P, seed);
     pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);

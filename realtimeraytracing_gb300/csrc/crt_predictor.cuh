@@ -85,6 +85,9 @@ void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* 
                 void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const float4* xtri, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
+// Failure-detection probe of the predictor kernels' MMA wait (one CTA, one
+// MMA or none): out[128] receives 16.0 per thread when complete != 0.
+cudaError_t tc_wait_probe(int complete, uint32_t limit, uint32_t* err, float* out, cudaStream_t s);
 size_t bounce_scratch_bytes(uint32_t n_prim);
 void launch_bounce(const crt_ray* prim, const crt_hit* hits, uint32_t n_prim, const float4* xtri,
                    const uint32_t* inv_perm, uint32_t n_tris, uint32_t n_out, uint32_t seed, crt_ray* out,

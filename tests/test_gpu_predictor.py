@@ -162,3 +162,28 @@ def test_predictor_ordered_traversal_is_exact(ctx, scene, flags):
         torch.equal(_i32(got)[:, 0] == -1, _i32(plain)[:, 0] == -1)
     assert ok
     pred.free()
+
+
+def test_mma_wait_times_out_frees_tensor_memory_and_the_context_stays_usable(ctx):
+    """The predictor kernels' MMA wait: a commit that completes passes and
+    reads the right product; a phase nothing completes gives up after a short
+    bound with CRT_ERR_DEVICE_TIMEOUT, without reading tensor memory, and the
+    CTA still frees it — so the next tcgen05 kernels (the predictor's own
+    inference and training) allocate and run as before."""
+    ctx.selftest_tc_wait(True)
+    with pytest.raises(crt.CrtError) as e:
+        ctx.selftest_tc_wait(False, spin_limit=1 << 10)
+    assert e.value.status == 4  # CRT_ERR_DEVICE_TIMEOUT
+    ctx.selftest_tc_wait(True)
+    tris = S.uniform_soup(20000, seed=91)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    rays = S.sphere_rays(4096, seed=92)
+    hits = ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)
+    pred = crt.Predictor(ctx, bvh, seed=5)
+    loss = pred.train(rays, hits, offset=0)
+    assert np.isfinite(loss)
+    seeded = ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR)
+    assert np.array_equal(seeded.view(np.uint32), hits.view(np.uint32))
+    pred.free()
+    bvh.free()
