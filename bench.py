@@ -1,33 +1,47 @@
 #!/usr/bin/env python
 """Throughput benchmark of the GB300 ray-tracing core.
 
-Workload (one "step" = one frame of the reference's compute pass,
-Application::drawOneFrame in srcOpenGL/application.cpp:220-262, minus shading):
-  scene   1,310,720-triangle displaced icosphere (subdivision 8, radius 1,
-          3-octave value noise of amplitude 0.05), seeded synthetic data;
-          the BVH is built by the CUDA PLOC path (build time reported apart
-          as build_ms, as the reference builds once at scene load)
-  frame   1920x1080 primary rays (getRay) -> closest hit (watertight
-          predicate) -> one any-hit shadow ray per hit toward (2, 2, -2);
-          crt_trace_frame runs it as one kernel launch (frame_kernel)
-  value   rays traced per second (primary + shadow rays of hits), Mrays/s,
-          inputs resident in HBM, CUDA events on the library's stream
-  e2e     the same frame through the public C ABI call crt_trace_frame with
-          the camera in from pinned host memory and both hit buffers out to
-          pinned host memory (the frame kernel writes them there directly),
-          timed on the host clock around the call
+Headline workload (the hit-predictor metric's own scene): one "step" traces
+a batch of incoherent rays with the learned hit predictor.
+  scene   4,194,304-triangle clustered soup (256 Gaussian clusters, sigma
+          0.02, edges lognormal(ln 0.003, 0.6)), seeded synthetic data, BVH
+          built by the CUDA PLOC path (build ms reported apart)
+  rays    8,388,608 cosine-weighted diffuse bounce rays from the closest hits
+          of 2048x2048 primary rays from (0.5, 0.5, -1.5) toward +z, made on
+          the host from the seed (scenes.bounce_rays: IEEE-exact float64
+          arithmetic, so every run and both arms get the same bytes)
+  step    crt_trace with CRT_TRACE_PREDICTOR_ORDER: predictor inference (FP16
+          MLP on tcgen05, trained online on the tracer's own hits), rays
+          ordered by (predicted treelet, origin cell, direction bin), closest
+          hit with the watertight predicate; the hits must equal the plain
+          traversal's bit for bit
+  value   rays per second of that step, Mrays/s, rays resident in HBM, L2
+          flushed before each step, CUDA events on the library's stream
+  e2e     the same step through the public C ABI call crt_trace with the
+          rays in page-locked host memory and the hits written back to it,
+          host-timed around the call
+The plain traversal (rays in caller order), the no-network ordering
+(CRT_TRACE_SORT_RAYS) and the other learned modes are timed beside it on
+the same rays.  The 1,310,720-triangle icosphere frame (primary + shadow
+rays, one launch), the 65,536-triangle soup under the shader's own triangle
+predicate, the 64-scene batch and the 16M-triangle animation are reported as
+extra keys.
 
---impl reference times the reference's CPU path on the host cores instead:
-its PLOC build (bvh.cpp restated for N > 65,536, the reference's own cap)
-and its shader traversal restated in C++ (right-child-first DFS without
-t pruning, the shader's triangle predicate), on a bounded sample of rays.
+--impl reference times the reference's CPU path on the host cores instead,
+on the same rays: the shader's traversal (raytracer.glsl:246-295: DFS, right
+child popped first, every box the ray crosses entered, no t pruning) restated
+in C++ with the watertight triangle predicate the GPU arm uses, over the same
+BVH (its PLOC build restated from bvh.cpp), on a bounded rotating 1/64
+sample of the rays per step.  Both arms print a digest of the rays and of the
+hits on that sample, which must agree.
 
-Multi-GPU: replicas (each rank traces its own full frame); value is the
-total over ranks divided by the slowest rank's time (weak scaling).
+Multi-GPU: replicas (each rank traces its own copy of the batch); value is
+the total over ranks divided by the slowest rank's time (weak scaling).
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -42,8 +56,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s closest-hit: hit-predictor vs plain, 1 GB300, exact hits; BVH build ms"
-WORKLOAD = "displaced icosphere 1,310,720 tris; 1920x1080 primary closest-hit + shadow any-hit to (2,2,-2)"
-W, H = 1920, 1080
+WORKLOAD = ("clustered soup 4,194,304 tris (256 clusters); 8,388,608 cosine bounce rays from the closest hits of "
+            "2048x2048 primary rays; closest hit (watertight)")
+N_BOUNCE = 8 * 1024 * 1024   # --rays: smaller copies of the batch for profilers
+BOUNCE_SEED = 11
+REF_STRIDE = 64        # the reference arm traces rays k % 64, k % 64 + 64, ... in step k
+TRI_WATERTIGHT = 0x2   # crt.h flags, also understood by the oracle
+TRI_REFERENCE = 0x0
+W1, H1 = 1920, 1080    # the icosphere frame
 
 
 def load_peaks():
@@ -55,18 +75,38 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def read_profile_traffic():
-    """Per-launch DRAM bytes of the frame kernel from the committed ncu
-    summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", "frame_kernel_config1.md")
+def read_profile_value(name, key):
+    """A number from a committed ncu summary (a line 'key: value ...')."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             for line in f:
-                if line.strip().startswith("traffic_bytes_per_launch:"):
+                if line.strip().startswith(key + ":"):
                     return float(line.split(":", 1)[1].split()[0])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
+
+
+def digest(a) -> str:
+    """Short SHA-256 of an array's bytes."""
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()[:16]
+
+
+def ref_sample(k: int, n: int) -> np.ndarray:
+    """Indices of the rays the reference arm traces in step k."""
+    return np.arange(k % REF_STRIDE, n, REF_STRIDE)
+
+
+def edge_hits(hits) -> int:
+    """Closest hits within about one float ulp of a triangle edge: a
+    barycentric coordinate (u, v or 1 - u - v) below 2^-22.  Such rays may
+    take either neighbour of a shared edge; both predicates report them."""
+    u32 = np.ascontiguousarray(hits).view(np.uint32)
+    hit = u32[:, 0] != 0xFFFFFFFF
+    u, v = hits[hit, 2].astype(np.float64), hits[hit, 3].astype(np.float64)
+    w = 1.0 - u - v
+    return int((np.minimum(np.minimum(u, v), w) < 2.0 ** -22).sum())
 
 
 class ClockSampler:
@@ -150,11 +190,39 @@ def whole_job_mrays(world: int, rays_per_replica: int, t_ms: float) -> float:
     return world * rays_per_replica / (t_ms * 1e-3) / 1e6
 
 
-def make_scene():
+def headline_config():
+    """The workload description both arms put in `config`."""
+    wl = WORKLOAD if N_BOUNCE == 8 * 1024 * 1024 else WORKLOAD.replace("8,388,608", f"{N_BOUNCE:,}")
+    return {"workload": wl, "triangles": 4194304, "rays_per_step": N_BOUNCE, "predicate": "watertight",
+            "rays": "host-generated from seed 11 (scenes.bounce_rays), identical bytes in both arms",
+            "l2": "rays, nodes and triangles (1.2 GB) exceed L2; a 256 MB buffer is also written before every timed step",
+            "parallelism": "single GPU"}
+
+
+def config3_inputs(primary_hits_fn):
+    """(triangles, models, bounce rays) of the headline workload; the primary
+    hits come from primary_hits_fn(rays) (the GPU in the product arm, the
+    CPU oracle in the reference arm: the same hits bit for bit)."""
     from realtimeraytracing_gb300 import scenes as S
-    tris, models, cam, (w, h), light = S.config1_scene(seed=0)
-    assert (w, h) == (W, H)
-    return tris, models, cam, light
+    tris, models = S.config3_scene(seed=0)
+    _, _, rays = S.config3_rays(tris, models, primary_hits_fn, seed=BOUNCE_SEED, n_out=N_BOUNCE)
+    return tris, models, rays
+
+
+def l2_read_gbs(torch, dev, stream) -> float:
+    """Read bandwidth of an L2-resident buffer (48 MB, summed 50 times by
+    torch), the ceiling for traversal fetches that hit L2."""
+    x = torch.ones(12 * 1024 * 1024, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            x.sum()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(50):
+            x.sum()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return 50 * x.numel() * 4 / (a.elapsed_time(b) * 1e-3) / 1e9
 
 
 # --------------------------------------------------------------- our arm
@@ -167,216 +235,177 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from realtimeraytracing_gb300 import crt
 
-    tris, models, cam, light = make_scene()
-    n_tris = tris.shape[0]
-    ctx = crt.Context(device=local)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     dev = torch.device("cuda", local)
+    ctx = crt.Context(device=local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    WT = crt.TRI_WATERTIGHT
+
+    # ---- scene, BVH build (scene load; device-timed inside the library)
+    from realtimeraytracing_gb300 import scenes as S
+    tris, models = S.config3_scene(seed=0)
+    n_tris = tris.shape[0]
     d_tris = torch.from_numpy(tris).to(dev)
     d_models = torch.from_numpy(models).to(dev)
-    d_cam = torch.from_numpy(cam).to(dev)
-    torch.cuda.synchronize()
-
-    # ---- BVH build (scene load), device-timed inside the library
     bvh = ctx.build(d_tris, models=d_models)
-    build_ms = []
+    builds = []
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         bvh.rebuild(d_tris, models=d_models)
         wall = (time.perf_counter() - t0) * 1e3
-        st = ctx.last_build_stats()
         if i >= args.warmup:
-            build_ms.append((st["ms_total"], wall, st))
-    build_dev = statistics.median(b[0] for b in build_ms)
-    build_wall = statistics.median(b[1] for b in build_ms)
-    stages = {k: round(statistics.median(b[2][k] for b in build_ms), 4)
+            builds.append((ctx.last_build_stats(), wall))
+    build_ms = statistics.median(b[0]["ms_total"] for b in builds)
+    stages = {k: round(statistics.median(b[0][k] for b in builds), 4)
               for k in ("ms_morton", "ms_sort", "ms_ploc", "ms_layout")}
-    iters = build_ms[-1][2]["ploc_iterations"]
 
-    n_rays = W * H
-    hp = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
-    hs = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
-    flags = crt.TRI_WATERTIGHT
-    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    # ---- the rays: primary hits on the GPU, bounce rays on the host
+    def primary_hits(prim):
+        dp = torch.from_numpy(prim).to(dev)
+        h = torch.empty((prim.shape[0], 4), dtype=torch.float32, device=dev)
+        ctx.trace(bvh, dp, WT, out=h)
+        torch.cuda.synchronize()
+        return h.cpu().numpy()
 
-    def frame():
-        ctx.trace_frame(bvh, d_cam, W, H, light, flags, hits_primary=hp, hits_shadow=hs)
-
-    for _ in range(args.warmup):
-        frame()
+    _, _, rays_h = S.config3_rays(tris, models, primary_hits, seed=BOUNCE_SEED, n_out=N_BOUNCE)
+    n = N_BOUNCE
+    d_rays = torch.from_numpy(rays_h).to(dev)
+    plain = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    out = torch.empty_like(plain)
+    ctx.trace(bvh, d_rays, WT, out=plain)
     torch.cuda.synchronize()
-    n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
-    rays_per_frame = n_rays + n_hits
 
-    # ---- timed frames (device resident), L2 flushed before each frame
+    # ---- the learned part: trained online on the tracer's own exact hits
+    # (every 20th ray = 5% per pass, rotating offset), then deployed
+    pred = crt.Predictor(ctx, bvh, seed=1, miss_threshold=0.9)
+    passes = 20
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = [pred.train(d_rays, plain, offset=k % 20) for k in range(passes)]
+    torch.cuda.synchronize()
+    train_ms = (time.perf_counter() - t0) * 1e3 / passes
+    LEARNED = WT | crt.PREDICTOR_ORDER
+
+    def run_steps(flags, steps, warmup, hits_out):
+        for _ in range(warmup):
+            ctx.trace(bvh, d_rays, flags, out=hits_out)
+        torch.cuda.synchronize()
+        evs, kern = [], []
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                l2_flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.trace(bvh, d_rays, flags, out=hits_out)
+                b.record(stream)
+                kern.append(ctx.last_trace_timing())
+                evs.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs], kern
+
+    def same(h):
+        return bool(torch.equal(h.view(torch.int32), plain.view(torch.int32)))
+
+    # ---- timed steps of the headline (learned) mode
     clocks = ClockSampler(local)
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            l2_flush.zero_()
-            ev[k][0].record(stream)
-            frame()
-            ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    frame_ms = [a.elapsed_time(b) for a, b in ev]
+    step_ms, kern = run_steps(LEARNED, args.steps, args.warmup, out)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    t_frame = slowest_ms(sum(frame_ms) / len(frame_ms), world, dev)
-    value = whole_job_mrays(world, rays_per_frame, t_frame)
+    t_step = slowest_ms(statistics.mean(step_ms), world, dev)
+    value = whole_job_mrays(world, n, t_step)
+    identical = same(out)
 
-    # ---- the dominant kernel: the frame is one frame_kernel launch; its node
-    # fetches and triangle tests (primary + shadow) from a CRT_TRACE_STATS frame
-    ctx.trace_frame(bvh, d_cam, W, H, light, flags | crt.TRACE_STATS, hits_primary=hp, hits_shadow=hs)
-    visited, tested = ctx.last_trace_stats()
-    k_ms = statistics.mean(frame_ms)  # this rank's frame_kernel launch, L2 flushed before it
-    alg_bytes = 64.0 * visited + 48.0 * tested + 2 * 16.0 * n_rays  # nodes, triangles, both hit buffers
+    # ---- the same rays plain, sorted without the network, seeded
+    reps = max(3, min(args.steps, 10))
+    t_plain = statistics.mean(run_steps(WT, reps, 2, out)[0])
+    identical = identical and same(out)
+    t_sorted = statistics.mean(run_steps(WT | crt.SORT_RAYS, reps, 2, out)[0])
+    identical = identical and same(out)
+    t_seeded = statistics.mean(run_steps(WT | crt.USE_PREDICTOR, reps, 2, out)[0])
+    identical = identical and same(out)
+    # online training inside the step: trace + one 5% training pass
+    ev_t = []
+    with torch.cuda.stream(stream):
+        for k in range(reps):
+            l2_flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.trace(bvh, d_rays, LEARNED, out=out)
+            pred.train(d_rays, out, offset=k % 20)
+            b.record(stream)
+            ev_t.append((a, b))
+    torch.cuda.synchronize()
+    t_online = statistics.mean(a.elapsed_time(b) for a, b in ev_t)
+    identical = identical and same(out)
+
+    # node fetches and triangle tests per ray
+    ctx.trace(bvh, d_rays, WT | crt.TRACE_STATS, out=out)
+    f_plain, tt_plain = ctx.last_trace_stats()
+    ctx.trace(bvh, d_rays, LEARNED | crt.TRACE_STATS, out=out)
+    f_learned, tt_learned = ctx.last_trace_stats()
+    # prediction quality: treelet hit rate on hitting rays
+    cls = torch.empty((n,), dtype=torch.int16, device=dev)
+    pred.infer(d_rays, out=cls)
+    truth = pred.classes_of_hits(plain)
+    pc = cls.cpu().numpy().view(np.uint16)
+    hit = truth != 127
+    hit_rate = float((pc[hit] == truth[hit]).mean()) if hit.any() else 0.0
+
+    # ---- the dominant kernel (trace_kernel in the learned step), timed by
+    # the library's CUDA events on its stream around that launch
+    k_ms = statistics.mean(k[1] for k in kern)
+    order_ms = statistics.mean(k[0] for k in kern)
+    alg_bytes = 64.0 * f_learned + 48.0 * tt_learned + (32.0 + 16.0 + 4.0) * n  # nodes, triangles, ray, hit, order
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-    traffic = read_profile_traffic()
-    # the primary closest-hit trace alone (crt_trace over stored rays), for reference
-    rays = torch.empty((n_rays, 8), dtype=torch.float32, device=dev)
-    ctx.raygen(d_cam, W, H, out=rays)
-    ctx.trace(bvh, rays, flags | crt.TRACE_STATS, out=hp)
-    p_visited, p_tested = ctx.last_trace_stats()
-    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            l2_flush.zero_()
-            kev[k][0].record(stream)
-            ctx.trace(bvh, rays, flags, out=hp)
-            kev[k][1].record(stream)
-    torch.cuda.synchronize()
-    p_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
-    # the same primary trace over the other node formats (same hits)
-    node_formats = {"binary_64B": {"ms": round(p_ms, 4), "node_fetches_per_ray": round(p_visited / n_rays, 2)}}
-    hp_alt = torch.empty_like(hp)
-    for fname, fflag in (("wide4_128B", crt.TRACE_WIDE), ("compressed4_64B", crt.TRACE_COMPRESSED)):
-        ctx.trace(bvh, rays, flags | fflag | crt.TRACE_STATS, out=hp_alt)
-        f_visited, _ = ctx.last_trace_stats()
-        fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        with torch.cuda.stream(stream):
-            for k in range(args.steps):
-                l2_flush.zero_()
-                fev[k][0].record(stream)
-                ctx.trace(bvh, rays, flags | fflag, out=hp_alt)
-                fev[k][1].record(stream)
-        torch.cuda.synchronize()
-        node_formats[fname] = {"ms": round(statistics.mean(a.elapsed_time(b) for a, b in fev), 4),
-                               "node_fetches_per_ray": round(f_visited / n_rays, 2),
-                               "identical_hits": bool(torch.equal(hp_alt.view(torch.int32), hp.view(torch.int32)))}
-    del hp_alt
+    traffic = read_profile_value("trace_kernel_bounce_config3.md", "traffic_bytes_per_launch")
+    l2_gbs = l2_read_gbs(torch, dev, stream)
 
-    # ---- mesh input: the scene's indexed mesh to TriangleGPU records on the GPU
-    from realtimeraytracing_gb300 import scenes as S
-    mv, mf = S.displaced_icosphere(8, 0.05, 0)
-    d_mv = torch.from_numpy(np.ascontiguousarray(mv, np.float32)).to(dev)
-    d_mf = torch.from_numpy(np.ascontiguousarray(mf, np.uint32).view(np.int32)).to(dev)
-    d_mt = torch.empty((mf.shape[0], 16), dtype=torch.float32, device=dev)
+    # ---- end to end through the public API: host rays in, host hits out
+    rays_pin = torch.from_numpy(rays_h).pin_memory()
+    hits_pin = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
     for _ in range(2):
-        ctx.triangles_from_indexed(d_mv, d_mf, 0, out=d_mt)
-    mev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            l2_flush.zero_()
-            mev[k][0].record(stream)
-            ctx.triangles_from_indexed(d_mv, d_mf, 0, out=d_mt)
-            mev[k][1].record(stream)
-    torch.cuda.synchronize()
-    m_ms = statistics.mean(a.elapsed_time(b) for a, b in mev)
-    mesh_upload = {"triangles": int(mf.shape[0]), "ms": round(m_ms, 4),
-                   "gbs": round((12 + 36 + 64) * mf.shape[0] / (m_ms * 1e-3) / 1e9, 1),
-                   "identical_to_scene_records": bool(torch.equal(d_mt.cpu(), torch.from_numpy(tris))),
-                   "note": "crt_triangles_from_indexed on device arrays: 12 B indices + 36 B gathered vertices + "
-                           "64 B record per triangle, L2 flushed before each call"}
-    del d_mv, d_mf, d_mt
-
-    # ---- the trace side alone over a node array built elsewhere: the reference's
-    # CPU build hands its shader this same DFS array (host memory), which
-    # crt_bvh_from_nodes makes traceable; the frame over it must equal the frame
-    # over the built handle
-    nodes_h = bvh.nodes()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    imp = ctx.bvh_from_nodes(nodes_h, tris, models=models)
-    import_ms = (time.perf_counter() - t0) * 1e3
-    hp_i, hs_i = torch.empty_like(hp), torch.empty_like(hs)
-    ctx.trace_frame(bvh, d_cam, W, H, light, flags, hits_primary=hp, hits_shadow=hs)
-    iev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    ctx.trace_frame(imp, d_cam, W, H, light, flags, hits_primary=hp_i, hits_shadow=hs_i)
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            l2_flush.zero_()
-            iev[k][0].record(stream)
-            ctx.trace_frame(imp, d_cam, W, H, light, flags, hits_primary=hp_i, hits_shadow=hs_i)
-            iev[k][1].record(stream)
-    torch.cuda.synchronize()
-    imported_tree = {
-        "import_ms": round(import_ms, 3),
-        "frame_ms": round(statistics.mean(a.elapsed_time(b) for a, b in iev), 4),
-        "identical_hits": bool(torch.equal(hp_i.view(torch.int32), hp.view(torch.int32)) and
-                               torch.equal(hs_i[:, 0].view(torch.int32) == -1, hs[:, 0].view(torch.int32) == -1)),
-        "note": "crt_bvh_from_nodes from the 2,621,439-record node array in host memory (structure check, "
-                "upload, traversal records; host-timed), then the one-launch frame over the imported tree"}
-    imp.free()
-    del hp_i, hs_i
-
-    # ---- the reference's whole compute pass (getRay, closest hit, getColor,
-    # imageStore) into a device RGBA32F image: crt_render_frame, one launch
-    img = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
-    d_mats = torch.tensor([[0.8, 0.7, 0.6, 1.0]], dtype=torch.float32, device=dev)
-    shaded = {}
-    for name, sflags, depth in (("plain", 0, 0), ("wireframe_bvh_depth3", crt.SHADE_WIREFRAME | crt.SHADE_BVH, 3)):
-        def render():
-            ctx.render_frame(bvh, d_cam, W, H, models=d_models, materials=d_mats, shade_flags=sflags,
-                             bvh_depth=depth, flags=flags, out=img)
-        for _ in range(2):
-            render()
-        sev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        with torch.cuda.stream(stream):
-            for k in range(args.steps):
-                l2_flush.zero_()
-                sev[k][0].record(stream)
-                render()
-                sev[k][1].record(stream)
-        torch.cuda.synchronize()
-        s_ms = statistics.mean(a.elapsed_time(b) for a, b in sev)
-        shaded[name] = {"ms": round(s_ms, 4), "mrays_s": round(n_rays / (s_ms * 1e-3) / 1e6, 1)}
-
-    # ---- end to end through the public API: camera in, hits out (pinned host)
-    hp_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
-    hs_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
-    cam_h = torch.from_numpy(cam.copy()).pin_memory()
-    for _ in range(2):
-        ctx.trace_frame(bvh, cam_h, W, H, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
+        ctx.trace(bvh, rays_pin, LEARNED, out=hits_pin)
     e2e_ms = []
     for _ in range(args.steps):
         l2_flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ctx.trace_frame(bvh, cam_h, W, H, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
+        ctx.trace(bvh, rays_pin, LEARNED, out=hits_pin)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_t = slowest_ms(statistics.mean(e2e_ms), world, dev)
-    e2e_value = whole_job_mrays(world, rays_per_frame, e2e_t)
+    e2e_value = whole_job_mrays(world, n, e2e_t)
+    plain_h = plain.cpu().numpy()
+    identical = identical and bool(np.array_equal(hits_pin.numpy().view(np.uint32), plain_h.view(np.uint32)))
+
+    # the hits on the reference arm's timed samples, for comparison with its digest
+    ref_hits = np.concatenate([plain_h[ref_sample(k, n)] for k in range(args.warmup, args.warmup + args.steps)])
+    nodes_h = bvh.nodes()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(tris, models, cam)
-    batch = None
+        cpu = cpu_baseline(nodes_h, tris, models, rays_h, plain_h)
+    del rays_pin, hits_pin
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras["treelet_optimized_tree"] = optimized_tree_experiment(ctx, torch, crt, bvh, d_rays, plain, out,
+                                                                     run_steps, t_plain)
+    pred.free()
+    bvh.free()
+    del d_tris, d_rays, plain, out, cls
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_extras:
+        extras["config0_shader_predicate"] = run_config0(ctx, torch, crt, dev, stream, args)
+        extras["frame"] = run_frame_experiment(ctx, torch, crt, dev, stream, l2_flush, args)
     if rank == 0 and not args.no_batch:
-        batch = run_batch_experiment(ctx, torch, crt, dev, args)
-    dynamic = None
+        extras["batch"] = run_batch_experiment(ctx, torch, crt, dev, args)
     if rank == 0 and not args.no_dynamic:
-        dynamic = run_dynamic_experiment(ctx, torch, crt, dev, args)
-    predictor = None
-    if rank == 0 and not args.no_predictor:
-        del d_tris, bvh
-        torch.cuda.empty_cache()
-        predictor = run_predictor_experiment(ctx, torch, crt, dev, stream, args)
+        extras["dynamic"] = run_dynamic_experiment(ctx, torch, crt, dev, args)
 
     if rank == 0:
         line = {
@@ -386,50 +415,263 @@ def run_ours(args):
             "n_gpus": world,
             "steps": args.steps,
             "warmup": args.warmup,
-            "ms_per_step": round(t_frame, 4),
+            "ms_per_step": round(t_step, 4),
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f32",
-            "data": "synthetic (seeded displaced icosphere)",
-            "config": {"workload": WORKLOAD, "triangles": n_tris, "image": [W, H],
-                       "rays_per_step": rays_per_frame, "primary_hits": n_hits,
-                       "predicate": "watertight", "ploc_radius": 16, "sort_digit_bits": 8,
-                       "l2": "flushed (256 MB write) before every timed step",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "build_ms": round(build_dev, 4),
-            "build_ms_wall": round(build_wall, 4),
+            "data": "synthetic (seeded clustered soup and host-generated bounce rays)",
+            "config": headline_config(),
+            "learned_vs_plain": {
+                "learned_mrays_s": round(value / world, 2), "plain_mrays_s": round(n / t_plain / 1e3, 2),
+                "speedup": round(t_plain / t_step, 3), "identical_hits": identical,
+                "no_network_sorted_mrays_s": round(n / t_sorted / 1e3, 2),
+                "no_network_speedup": round(t_plain / t_sorted, 3),
+                "learned_vs_no_network": round(t_sorted / t_step, 3),
+                "seeded_tmax_mrays_s": round(n / t_seeded / 1e3, 2), "seeded_speedup": round(t_plain / t_seeded, 3),
+                "with_online_training_mrays_s": round(n / t_online / 1e3, 2),
+                "with_online_training_speedup": round(t_plain / t_online, 3),
+                "ordering_ms": round(order_ms, 4), "trace_kernel_ms": round(k_ms, 4),
+                "node_fetches_per_ray": {"plain": round(f_plain / n, 2), "learned": round(f_learned / n, 2)},
+                "tris_per_ray": {"plain": round(tt_plain / n, 2), "learned": round(tt_learned / n, 2)},
+                "treelet_hit_rate": round(hit_rate, 4), "rays_hitting": round(float(hit.mean()), 4),
+                "training": {"passes": passes, "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4),
+                             "ms_per_pass": round(train_ms, 3), "samples_per_pass": n // 20},
+                "modes": "learned = CRT_TRACE_PREDICTOR_ORDER (inference + order by predicted treelet, origin "
+                         "cell, direction bin + trace); no network = CRT_TRACE_SORT_RAYS (order by origin cell and "
+                         "direction bin + trace); seeded = CRT_TRACE_USE_PREDICTOR (t_max from an exact search of "
+                         "the predicted treelet)"},
+            "build_ms": round(build_ms, 4),
+            "build_ms_wall": round(statistics.median(b[1] for b in builds), 4),
             "build_stages_ms": stages,
-            "ploc_iterations": iters,
-            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(cam.nbytes),
-                    "d2h_bytes_per_step": int(2 * n_rays * 16), "ms_per_step": round(e2e_t, 4),
-                    "transfer": "camera in by cudaMemcpyAsync; both hit buffers (page-locked host memory) written by "
-                                "the frame kernel over the CPU-GPU link, host-timed around crt_trace_frame"},
-            "gpu_launches": args.steps,
-            "roofline": {"kernel": "frame_kernel (camera ray, closest hit, shadow ray, any hit)", "bound": "hbm",
-                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "peak_source": peak_kind, "ms_per_launch": round(k_ms, 4),
-                         "alg_bytes_per_launch": int(alg_bytes),
-                         "node_fetches_per_pixel": round(visited / n_rays, 2),
-                         "tris_per_pixel": round(tested / n_rays, 2)},
-            "primary_trace_node_formats": node_formats,
-            "primary_trace_kernel": {"ms": round(p_ms, 4), "mrays_s": round(n_rays / (p_ms * 1e-3) / 1e6, 1),
-                                     "node_fetches_per_ray": round(p_visited / n_rays, 2),
-                                     "tris_per_ray": round(p_tested / n_rays, 2)},
-            "mesh_upload": mesh_upload,
-            "imported_tree": imported_tree,
-            "shaded_frame": dict(shaded, note="crt_render_frame: camera ray, closest hit, getColor and "
-                                              "imageStore per texel into a device RGBA32F image, no shadow rays"),
+            "ploc_iterations": builds[-1][0]["ploc_iterations"],
+            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(n * 32),
+                    "d2h_bytes_per_step": int(n * 16), "ms_per_step": round(e2e_t, 4),
+                    "transfer": "crt_trace on page-locked host rays (copied in on the library stream) and host hits "
+                                "(written by the trace kernel over the CPU-GPU link), host-timed around the call"},
+            "gpu_launches": 7 * args.steps,
+            "gpu_launches_note": "per step: infer_kernel, order_keys_kernel, 4 onesweep_kernel passes, trace_kernel",
+            "roofline": {"kernel": "trace_kernel (learned step: rays in predicted order, closest hit, watertight)",
+                         "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                         "ms_per_launch": round(k_ms, 4), "alg_bytes_per_launch": int(alg_bytes),
+                         "alg_bytes_model": "64 B per node fetched + 48 B per triangle tested + 32 B ray + 16 B hit "
+                                            "+ 4 B order index per ray (fetched bytes; most are L1/L2 hits)",
+                         "l2": {"read_gbs": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4),
+                                "how": "torch sum over a 48 MB L2-resident buffer, 50 passes, CUDA events"}},
+            "rays_sha256": digest(rays_h),
+            "reference_sample_hits_sha256": digest(ref_hits),
+            "reference_sample_hits": int((ref_hits[:, 0].view(np.uint32) != 0xFFFFFFFF).sum()),
+            "edge_hits": edge_hits(plain_h),
             "cpu_baseline": cpu,
             "clocks": clk,
-            "batch": batch,
-            "dynamic": dynamic,
-            "predictor": predictor,
         }
+        line.update(extras)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def optimized_tree_experiment(ctx, torch, crt, bvh, d_rays, plain, out, run_steps, t_plain):
+    """The same rays over the treelet-restructured tree (crt_optimize, 2
+    passes; the build's tree is replaced)."""
+    n = d_rays.shape[0]
+    nodes_before = bvh.nodes()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bvh.optimize(2)
+    torch.cuda.synchronize()
+    t_opt = (time.perf_counter() - t0) * 1e3
+    t_tr = statistics.mean(run_steps(crt.TRI_WATERTIGHT, 5, 1, out)[0])
+    ident = bool(torch.equal(out.view(torch.int32), plain.view(torch.int32)))
+    return {"optimize_ms_wall": round(t_opt, 2), "passes": 2,
+            "sah_cost": [round(sah_cost(nodes_before), 2), round(sah_cost(bvh.nodes()), 2)],
+            "plain_mrays_s": round(n / t_tr / 1e3, 1), "vs_built_tree": round(t_plain / t_tr, 3),
+            "identical_hits": ident}
+
+
+def run_config0(ctx, torch, crt, dev, stream, args):
+    """The 65,536-triangle soup (512x512 primary rays) under the shader's own
+    triangle predicate (raytracer.glsl:102-147), the one scene of the set
+    where that predicate finds hits: GPU and CPU oracle on the same rays,
+    and how the watertight predicate differs on them."""
+    from oracle import oracle as O
+    from realtimeraytracing_gb300 import scenes as S
+    tris, models, cam, (w, h) = S.config0_scene(seed=0)
+    bvh = ctx.build(tris, models=models)
+    rays = S.pinhole_rays(cam, w, h)
+    d_rays = torch.from_numpy(rays).to(dev)
+    out = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+    res = {}
+    for name, fl in (("reference", crt.TRI_REFERENCE), ("watertight", crt.TRI_WATERTIGHT)):
+        for _ in range(3):
+            ctx.trace(bvh, d_rays, fl, out=out)
+        torch.cuda.synchronize()
+        evs = []
+        with torch.cuda.stream(stream):
+            for _ in range(10):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.trace(bvh, d_rays, fl, out=out)
+                b.record(stream)
+                evs.append((a, b))
+        torch.cuda.synchronize()
+        ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+        res[name] = (out.cpu().numpy(), ms)
+    gh, g_ms = res["reference"]
+    wh, w_ms = res["watertight"]
+    nodes = bvh.nodes()
+    bvh.free()
+    t0 = time.perf_counter()
+    oh, _ = O.trace(nodes, tris, models, rays, TRI_REFERENCE)
+    o_ms = (time.perf_counter() - t0) * 1e3
+    gt, wt = gh[:, 0].view(np.uint32), wh[:, 0].view(np.uint32)
+    both = (gt != 0xFFFFFFFF) & (wt != 0xFFFFFFFF)
+    return {
+        "workload": "uniform soup 65,536 tris, 512x512 primary rays from (0.5, 0.5, -1.5), closest hit",
+        "gpu_reference_predicate_mrays_s": round(rays.shape[0] / g_ms / 1e3, 1),
+        "gpu_watertight_mrays_s": round(rays.shape[0] / w_ms / 1e3, 1),
+        "cpu_reference_predicate_mrays_s": round(rays.shape[0] / o_ms / 1e3, 3),
+        "cpu_cores": os.cpu_count(),
+        "hits": int((gt != 0xFFFFFFFF).sum()),
+        "gpu_equals_cpu": bool(np.array_equal(gh.view(np.uint32), oh.view(np.uint32))),
+        "hits_sha256": digest(gh),
+        "predicates_disagree": {"rays": int((gt != wt).sum()), "hit_by_reference_only": int(((gt != 0xFFFFFFFF) & (wt == 0xFFFFFFFF)).sum()),
+                                "hit_by_watertight_only": int(((gt == 0xFFFFFFFF) & (wt != 0xFFFFFFFF)).sum()),
+                                "different_triangle": int((both & (gt != wt)).sum())},
+        "edge_hits": {"reference": edge_hits(gh), "watertight": edge_hits(wh)},
+        "note": "reference = CRT_TRI_REFERENCE (|a| < 1e-4 rejected, back faces culled); the shader's predicate "
+                "rejects every triangle of the larger scenes (their |a| is below 1e-4)",
+    }
+
+
+def run_frame_experiment(ctx, torch, crt, dev, stream, l2_flush, args):
+    """The 1,310,720-triangle displaced icosphere: 1920x1080 primary rays,
+    closest hit, one any-hit shadow ray per hit toward (2, 2, -2), one
+    frame_kernel launch (crt_trace_frame); plus the shaded frame, mesh upload
+    and a tree imported from its node array."""
+    from realtimeraytracing_gb300 import scenes as S
+    tris, models, cam, (w, h), light = S.config1_scene(seed=0)
+    d_tris = torch.from_numpy(tris).to(dev)
+    d_models = torch.from_numpy(models).to(dev)
+    d_cam = torch.from_numpy(cam).to(dev)
+    bvh = ctx.build(d_tris, models=d_models)
+    builds = []
+    for i in range(args.warmup + args.steps):
+        bvh.rebuild(d_tris, models=d_models)
+        if i >= args.warmup:
+            builds.append(ctx.last_build_stats())
+    n_rays = w * h
+    hp = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+    hs = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+    flags = crt.TRI_WATERTIGHT
+
+    def frame():
+        ctx.trace_frame(bvh, d_cam, w, h, light, flags, hits_primary=hp, hits_shadow=hs)
+
+    def timed(fn, steps):
+        evs = []
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                l2_flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                evs.append((a, b))
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
+    rays_per_frame = n_rays + n_hits
+    f_ms = timed(frame, args.steps)
+    ctx.trace_frame(bvh, d_cam, w, h, light, flags | crt.TRACE_STATS, hits_primary=hp, hits_shadow=hs)
+    visited, tested = ctx.last_trace_stats()
+    alg_bytes = 64.0 * visited + 48.0 * tested + 2 * 16.0 * n_rays
+    # the primary trace alone over the three node formats (same hits)
+    rays = torch.empty((n_rays, 8), dtype=torch.float32, device=dev)
+    ctx.raygen(d_cam, w, h, out=rays)
+    ctx.trace(bvh, rays, flags, out=hp)
+    formats = {}
+    hp_alt = torch.empty_like(hp)
+    for fname, fflag in (("binary_64B", 0), ("wide4_128B", crt.TRACE_WIDE), ("compressed4_64B", crt.TRACE_COMPRESSED)):
+        ctx.trace(bvh, rays, flags | fflag | crt.TRACE_STATS, out=hp_alt)
+        fv, _ = ctx.last_trace_stats()
+        ms = timed(lambda: ctx.trace(bvh, rays, flags | fflag, out=hp_alt), args.steps)
+        formats[fname] = {"ms": round(ms, 4), "node_fetches_per_ray": round(fv / n_rays, 2),
+                          "identical_hits": bool(torch.equal(hp_alt.view(torch.int32), hp.view(torch.int32)))}
+    # mesh upload: the indexed icosphere to TriangleGPU records on the GPU
+    mv, mf = S.displaced_icosphere(8, 0.05, 0)
+    d_mv = torch.from_numpy(np.ascontiguousarray(mv, np.float32)).to(dev)
+    d_mf = torch.from_numpy(np.ascontiguousarray(mf, np.uint32).view(np.int32)).to(dev)
+    d_mt = torch.empty((mf.shape[0], 16), dtype=torch.float32, device=dev)
+    ctx.triangles_from_indexed(d_mv, d_mf, 0, out=d_mt)
+    m_ms = timed(lambda: ctx.triangles_from_indexed(d_mv, d_mf, 0, out=d_mt), args.steps)
+    mesh = {"triangles": int(mf.shape[0]), "ms": round(m_ms, 4),
+            "gbs": round((12 + 36 + 64) * mf.shape[0] / (m_ms * 1e-3) / 1e9, 1),
+            "identical_to_scene_records": bool(torch.equal(d_mt.cpu(), torch.from_numpy(tris)))}
+    del d_mv, d_mf, d_mt
+    # the trace side alone over a node array built elsewhere (host memory)
+    frame()
+    nodes_h = bvh.nodes()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    imp = ctx.bvh_from_nodes(nodes_h, tris, models=models)
+    import_ms = (time.perf_counter() - t0) * 1e3
+    hp_i, hs_i = torch.empty_like(hp), torch.empty_like(hs)
+    i_ms = timed(lambda: ctx.trace_frame(imp, d_cam, w, h, light, flags, hits_primary=hp_i, hits_shadow=hs_i),
+                 args.steps)
+    imported = {"import_ms": round(import_ms, 3), "frame_ms": round(i_ms, 4),
+                "identical_hits": bool(torch.equal(hp_i.view(torch.int32), hp.view(torch.int32)) and
+                                       torch.equal(hs_i[:, 0].view(torch.int32) == -1, hs[:, 0].view(torch.int32) == -1))}
+    imp.free()
+    # the reference's whole compute pass into a device RGBA32F image
+    img = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+    d_mats = torch.tensor([[0.8, 0.7, 0.6, 1.0]], dtype=torch.float32, device=dev)
+    shaded = {}
+    for name, sflags, depth in (("plain", 0, 0), ("wireframe_bvh_depth3", crt.SHADE_WIREFRAME | crt.SHADE_BVH, 3)):
+        def render():
+            ctx.render_frame(bvh, d_cam, w, h, models=d_models, materials=d_mats, shade_flags=sflags,
+                             bvh_depth=depth, flags=flags, out=img)
+        render()
+        s_ms = timed(render, args.steps)
+        shaded[name] = {"ms": round(s_ms, 4), "mrays_s": round(n_rays / (s_ms * 1e-3) / 1e6, 1)}
+    # end to end: camera in, both hit buffers out to page-locked host memory
+    hp_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
+    hs_h = torch.empty((n_rays, 4), dtype=torch.float32, pin_memory=True)
+    cam_h = torch.from_numpy(cam.copy()).pin_memory()
+    for _ in range(2):
+        ctx.trace_frame(bvh, cam_h, w, h, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
+    e2e = []
+    for _ in range(args.steps):
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.trace_frame(bvh, cam_h, w, h, light, flags, hits_primary=hp_h, hits_shadow=hs_h)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    bvh.free()
+    return {
+        "workload": "displaced icosphere 1,310,720 tris; 1920x1080 primary closest-hit + shadow any-hit to (2,2,-2)",
+        "rays_per_frame": rays_per_frame, "primary_hits": n_hits,
+        "frame_ms": round(f_ms, 4), "mrays_s": round(rays_per_frame / (f_ms * 1e-3) / 1e6, 2),
+        "e2e_mrays_s": round(rays_per_frame / (statistics.mean(e2e) * 1e-3) / 1e6, 2),
+        "build_ms": round(statistics.median(b["ms_total"] for b in builds), 4),
+        "build_stages_ms": {k: round(statistics.median(b[k] for b in builds), 4)
+                            for k in ("ms_morton", "ms_sort", "ms_ploc", "ms_layout")},
+        "ploc_iterations": builds[-1]["ploc_iterations"],
+        "frame_kernel": {"fetched_bytes_gbs": round(alg_bytes / (f_ms * 1e-3) / 1e9, 1),
+                         "node_fetches_per_pixel": round(visited / n_rays, 2),
+                         "tris_per_pixel": round(tested / n_rays, 2),
+                         "dram_bytes_per_launch": read_profile_value("frame_kernel_config1.md",
+                                                                     "traffic_bytes_per_launch")},
+        "primary_trace_node_formats": formats,
+        "mesh_upload": mesh,
+        "imported_tree": imported,
+        "shaded_frame": shaded,
+    }
 
 
 def run_batch_experiment(ctx, torch, crt, dev, args):
@@ -636,159 +878,6 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
     })
 
 
-def run_predictor_experiment(ctx, torch, crt, dev, stream, args):
-    """Learned hit predictor vs plain traversal on the incoherent-bounce
-    workload: 4,194,304-triangle clustered soup (256 Gaussian clusters,
-    sigma 0.02, edges lognormal(ln 0.003, 0.6)), 2048x2048 primary rays from
-    (0.5, 0.5, -1.5) toward +z, 8,388,608 cosine-weighted bounce rays from
-    their first hits.  The network trains online on every 20th traced ray
-    (5%) for `passes` passes, then plain and seeded traversal are timed on
-    the same rays; the hits must be identical."""
-    from realtimeraytracing_gb300 import scenes as S
-    tris, models = S.config3_scene(seed=0)
-    d_tris = torch.from_numpy(tris).to(dev)
-    bvh = ctx.build(d_tris, models=torch.from_numpy(models).to(dev))
-    bst = ctx.last_build_stats()
-    build_ms, scene_box = bst["ms_total"], bst["scene_box"]  # scene box = root box (no padding)
-    del d_tris
-    cam = torch.from_numpy(S.camera_gpu_data((0.5, 0.5, -1.5))).to(dev)
-    w = 2048
-    prim = torch.empty((w * w, 8), dtype=torch.float32, device=dev)
-    ctx.raygen(cam, w, w, out=prim)
-    ph = torch.empty((w * w, 4), dtype=torch.float32, device=dev)
-    ctx.trace(bvh, prim, crt.TRI_WATERTIGHT, out=ph)
-    n = 8 * 1024 * 1024
-    rays = torch.empty((n, 8), dtype=torch.float32, device=dev)
-    ctx.bounce_rays(bvh, prim, ph, n, seed=11, out=rays)
-    del prim, ph
-    plain = torch.empty((n, 4), dtype=torch.float32, device=dev)
-    seeded = torch.empty_like(plain)
-    cls = torch.empty((n,), dtype=torch.int16, device=dev)
-
-    def timed(fn, reps):
-        # every call, the warm-up included, on the library's stream: torch work
-        # inside fn is then ordered with the library's kernels
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-        with torch.cuda.stream(stream):
-            fn()
-            torch.cuda.synchronize()
-            for a, b in evs:
-                a.record(stream)
-                fn()
-                b.record(stream)
-        torch.cuda.synchronize()
-        return statistics.mean(a.elapsed_time(b) for a, b in evs)
-
-    reps = max(3, min(args.steps, 10))
-    t_plain = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=plain), reps)
-    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=plain)
-    f_plain, _ = ctx.last_trace_stats()
-    # the other node formats on the same incoherent rays (same hits)
-    incoherent_formats = {}
-    for fname, fflag in (("wide4_128B", crt.TRACE_WIDE), ("compressed4_64B", crt.TRACE_COMPRESSED)):
-        t_f = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | fflag, out=seeded), reps)
-        incoherent_formats[fname] = {"mrays_s": round(n / (t_f * 1e-3) / 1e6, 1), "vs_binary": round(t_plain / t_f, 3),
-                                     "identical_hits": bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))}
-    pred = crt.Predictor(ctx, bvh, seed=1, miss_threshold=0.9)
-    truth = pred.classes_of_hits(plain)
-    hit = truth != 127
-    passes = 20
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    losses = [pred.train(rays, plain, offset=k % 20) for k in range(passes)]
-    train_ms = (time.perf_counter() - t0) * 1e3 / passes
-    t_infer = timed(lambda: pred.infer(rays, out=cls), reps)
-    t_seeded = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR, out=seeded), reps)
-    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.USE_PREDICTOR | crt.TRACE_STATS, out=seeded)
-    f_seeded, _ = ctx.last_trace_stats()
-    identical = bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
-    pc = cls.cpu().numpy().view(np.uint16)
-    hit_rate = float((pc[hit] == truth[hit]).mean()) if hit.any() else 0.0
-    tcls = torch.from_numpy(truth.astype(np.int16)).to(dev)
-    t_perfect = timed(lambda: ctx.trace_seeded(bvh, rays, tcls, crt.TRI_WATERTIGHT, out=seeded), reps)
-    ctx.trace_seeded(bvh, rays, tcls, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=seeded)
-    f_perfect, _ = ctx.last_trace_stats()
-    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
-    # rays grouped by predicted treelet (inference + one radix pass + trace), alone and with seeding
-    t_ordered = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER, out=seeded), reps)
-    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
-    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER | crt.TRACE_STATS, out=seeded)
-    f_ordered, _ = ctx.last_trace_stats()
-    t_ord_seed = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER | crt.USE_PREDICTOR,
-                                         out=seeded), reps)
-    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
-    # no network: rays sorted by the network's own input key (origin cell on the 64^3 grid of the scene
-    # box, octahedral direction bin 32x32), gathered, traced; the sort + gather is timed apart
-    key = ray_input_keys(torch, rays, scene_box)
-    def key_sort():
-        order = torch.argsort(key)
-        return rays.index_select(0, order), order
-    t_keysort = timed(key_sort, reps)
-    with torch.cuda.stream(stream):
-        srays, sorder = key_sort()
-        sh = torch.empty_like(plain)
-    torch.cuda.synchronize()
-    t_keytrace = timed(lambda: ctx.trace(bvh, srays, crt.TRI_WATERTIGHT, out=sh), reps)
-    t_native_sort = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.SORT_RAYS, out=seeded), reps)
-    identical = identical and bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
-    keysort_identical = bool(torch.equal(sh.view(torch.int32), plain.index_select(0, sorder).view(torch.int32)))
-    info = pred.info()
-    pred.free()
-    # the same rays over the treelet-restructured tree (crt_optimize, 2 passes; one call timed)
-    nodes_before = bvh.nodes()
-    oa, ob = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    oa.record(stream)
-    bvh.optimize(2)
-    ob.record(stream)
-    torch.cuda.synchronize()
-    t_optimize = oa.elapsed_time(ob)
-    t_opt_trace = timed(lambda: ctx.trace(bvh, rays, crt.TRI_WATERTIGHT, out=seeded), reps)
-    opt_identical = bool(torch.equal(seeded.view(torch.int32), plain.view(torch.int32)))
-    ctx.trace(bvh, rays, crt.TRI_WATERTIGHT | crt.TRACE_STATS, out=seeded)
-    f_opt, _ = ctx.last_trace_stats()
-    sah_before, sah_after = sah_cost(nodes_before), sah_cost(bvh.nodes())
-    bvh.free()
-    return {
-        "workload": "clustered soup 4,194,304 tris (256 clusters); 8,388,608 cosine bounce rays from 2048x2048 primary hits",
-        "build_ms": round(build_ms, 3),
-        "plain_mrays_s": round(n / t_plain / 1e3, 1),
-        "node_formats": incoherent_formats,
-        "seeded_mrays_s": round(n / t_seeded / 1e3, 1),
-        "speedup": round(t_plain / t_seeded, 3),
-        "infer_ms": round(t_infer, 3),
-        "overhead_frac": round(t_infer / t_seeded, 3),
-        "identical_hits": identical,
-        "treelet_hit_rate": round(hit_rate, 4),
-        "rays_hitting": round(float(hit.mean()), 4),
-        "treelets": info["treelets"],
-        "node_fetches_per_ray": {"plain": round(f_plain / n, 2), "seeded": round(f_seeded / n, 2),
-                                 "perfect_prediction": round(f_perfect / n, 2)},
-        "perfect_prediction_speedup": round(t_plain / t_perfect, 3),
-        "predictor_ordered": {"mrays_s": round(n / t_ordered / 1e3, 1), "speedup": round(t_plain / t_ordered, 3),
-                              "node_fetches_per_ray": round(f_ordered / n, 2),
-                              "note": "CRT_TRACE_PREDICTOR_ORDER: inference + order by (predicted treelet, origin-cell Morton code, direction bin) + trace"},
-        "predictor_ordered_seeded": {"mrays_s": round(n / t_ord_seed / 1e3, 1),
-                                     "speedup": round(t_plain / t_ord_seed, 3)},
-        "sorted_rays_no_network": {"mrays_s": round(n / t_native_sort / 1e3, 1),
-                                   "speedup": round(t_plain / t_native_sort, 3),
-                                   "note": "CRT_TRACE_SORT_RAYS: order by (origin-cell Morton code, direction bin) + trace"},
-        "key_sorted_no_network": {"sort_gather_ms": round(t_keysort, 3), "trace_ms": round(t_keytrace, 3),
-                                  "speedup_trace_only": round(t_plain / t_keytrace, 3),
-                                  "speedup_with_sort": round(t_plain / (t_keysort + t_keytrace), 3),
-                                  "identical_hits": keysort_identical},
-        "treelet_optimized_tree": {"optimize_ms": round(t_optimize, 3), "passes": 2,
-                                   "sah_cost": [round(sah_before, 2), round(sah_after, 2)],
-                                   "mrays_s": round(n / t_opt_trace / 1e3, 1), "vs_built_tree": round(t_plain / t_opt_trace, 3),
-                                   "node_fetches_per_ray": round(f_opt / n, 2), "identical_hits": opt_identical,
-                                   "note": "crt_optimize: treelet restructuring of the built tree (SAH cost = sum of "
-                                           "1.2 x internal + leaf box areas over the root area), then the plain trace"},
-        "training": {"passes": passes, "adam_steps": info["steps"], "loss_first": round(losses[0], 4),
-                     "loss_last": round(losses[-1], 4), "ms_per_pass": round(train_ms, 2),
-                     "samples_per_pass": n // 20},
-    }
-
-
 def sah_cost(nodes, ci=1.2):
     """Surface-area cost of a node array as crt_optimize counts it (internal
     nodes ci x area, leaves 1 x area), relative to the root's area."""
@@ -799,109 +888,109 @@ def sah_cost(nodes, ci=1.2):
     return float((np.where(leaf, 1.0, ci) * a).sum() / a[0])
 
 
-def ray_input_keys(torch, rays, box):
-    """The predictor's input key of each ray without the network: origin cell
-    on the 64^3 grid of the scene box (min xyz, max xyz; x-major) * 1024 +
-    octahedral direction bin on 32x32, as int64 (the quantisation the
-    network's embeddings use)."""
-    mn = torch.tensor(list(box[0:3]), dtype=torch.float32, device=rays.device)
-    mx = torch.tensor(list(box[3:6]), dtype=torch.float32, device=rays.device)
-    ext = torch.clamp(mx - mn, min=1e-20)
-    c = torch.clamp(((rays[:, 0:3] - mn) * (64.0 / ext)).floor().long(), 0, 63)
-    cell = (c[:, 0] * 64 + c[:, 1]) * 64 + c[:, 2]
-    d = rays[:, 4:7]
-    a = d.abs().sum(dim=1).clamp(min=1e-30)
-    px, py = d[:, 0] / a, d[:, 1] / a
-    neg = d[:, 2] < 0
-    qx = (1 - py.abs()) * torch.where(px >= 0, 1.0, -1.0)
-    qy = (1 - px.abs()) * torch.where(py >= 0, 1.0, -1.0)
-    px, py = torch.where(neg, qx, px), torch.where(neg, qy, py)
-    bu = torch.clamp(((px + 1) * 16).long(), 0, 31)
-    bv = torch.clamp(((py + 1) * 16).long(), 0, 31)
-    return cell * 1024 + bu * 32 + bv
-
-
-def cpu_baseline(tris, models, cam, sample_stride=8):
-    """The reference's CPU path on the host cores: the shader traversal
-    restated in C++ (oracle), every `sample_stride`-th ray of the frame."""
+def cpu_baseline(nodes, tris, models, rays, gpu_hits):
+    """The reference's traversal on the host cores: the shader's walk
+    (raytracer.glsl:246-295, right child popped first, no t pruning)
+    restated in C++ (oracle) with the watertight predicate, on the reference
+    arm's step-0 sample of the same rays; its hits are compared with the GPU's."""
     from oracle import oracle as O
-    n = tris.shape[0]
-    nb = O.build_bvh(tris, n, models, faithful=True)
-    rays = O.raygen(cam, W, H)[::sample_stride].copy()
-    O.trace(nb["nodes"], tris, models, rays[:4096], 0)
+    idx = ref_sample(0, rays.shape[0])
+    sub = np.ascontiguousarray(rays[idx])
+    O.trace(nodes, tris, models, sub[:2048], TRI_WATERTIGHT)
     t0 = time.perf_counter()
-    reps = 0
-    while True:
-        hits, _ = O.trace(nb["nodes"], tris, models, rays, 0)
-        reps += 1
-        if time.perf_counter() - t0 > 2.0:
-            break
-    dt = (time.perf_counter() - t0) / reps
-    cores = os.cpu_count()
-    return {"value": round(rays.shape[0] / dt / 1e6, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
-            "sample": f"every {sample_stride}th primary ray of the 1920x1080 frame ({rays.shape[0]} rays), "
-                      f"shader predicate, no t pruning; shadow rays: none (the shader predicate hits nothing "
-                      f"on this mesh)",
-            "build_ms": round(float(sum(nb["ms"])), 2)}
+    hits, _ = O.trace(nodes, tris, models, sub, TRI_WATERTIGHT)
+    dt = time.perf_counter() - t0
+    return {"value": round(sub.shape[0] / dt / 1e6, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"every {REF_STRIDE}th ray of the same 8,388,608 bounce rays ({sub.shape[0]} rays), watertight "
+                      f"predicate, the shader's DFS without t pruning, OpenMP over rays",
+            "hits_equal_gpu": bool(np.array_equal(hits.view(np.uint32), gpu_hits[idx].view(np.uint32))),
+            "hits": int((hits[:, 0].view(np.uint32) != 0xFFFFFFFF).sum())}
 
 
 # --------------------------------------------------------- reference arm
 def run_reference(args):
+    """The reference's path on the host cores, on the headline workload:
+    its PLOC build (bvh.cpp restated for N > 65,536, the reference's own cap)
+    and its shader traversal restated in C++, a rotating 1/64 sample of the
+    same bounce rays per step."""
     world, rank, local = dist_setup()
     if rank != 0:
         return
     from oracle import oracle as O
+    from realtimeraytracing_gb300 import scenes as S
     O.build()
-    tris, models, cam, light = make_scene()
-    n = tris.shape[0]
+    tris, models = S.config3_scene(seed=0)
+    n_tris = tris.shape[0]
     t0 = time.perf_counter()
-    nb = O.build_bvh(tris, n, models, faithful=True)
+    nb = O.build_bvh(tris, n_tris, models, faithful=True)
     build_ms = (time.perf_counter() - t0) * 1e3
-    rays_all = O.raygen(cam, W, H)
-    stride = 8
-    times, counted = [], []
+    nodes = nb["nodes"]
+
+    def primary_hits(prim):  # input generation only: the pruned walk, same hits
+        h, _ = O.trace(nodes, tris, models, prim, TRI_WATERTIGHT | O.PRUNED)
+        return h
+
+    _, _, rays = S.config3_rays(tris, models, primary_hits, seed=BOUNCE_SEED, n_out=N_BOUNCE)
+    times, counted, parts = [], [], []
     for k in range(args.warmup + args.steps):
-        sub = rays_all[(k % stride)::stride].copy()
+        sub = np.ascontiguousarray(rays[ref_sample(k, N_BOUNCE)])
         t0 = time.perf_counter()
-        hits, _ = O.trace(nb["nodes"], tris, models, sub, 0)
-        nh = int((hits[:, 0].view(np.uint32) != 0xFFFFFFFF).sum())
-        if nh:
-            sh = O.shadow_rays(sub, hits, light)
-            O.trace(nb["nodes"], tris, models, sh, 1)
+        hits, _ = O.trace(nodes, tris, models, sub, TRI_WATERTIGHT)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(dt)
-            counted.append(sub.shape[0] + nh)
+            counted.append(sub.shape[0])
+            parts.append(hits)
     value = sum(counted) / sum(times) / 1e6
+    allh = np.concatenate(parts)
     cores = os.cpu_count()
+    # the 65,536-triangle soup under the shader's own triangle predicate
+    t0s, m0, cam0, (w0, h0) = S.config0_scene(seed=0)
+    nb0 = O.build_bvh(t0s, t0s.shape[0], m0, faithful=True)
+    r0 = S.pinhole_rays(cam0, w0, h0)
+    t0 = time.perf_counter()
+    h0, _ = O.trace(nb0["nodes"], t0s, m0, r0, TRI_REFERENCE)
+    c0_ms = (time.perf_counter() - t0) * 1e3
+    sample = (f"every {REF_STRIDE}th bounce ray per step, offset rotating with the step ({N_BOUNCE // REF_STRIDE} rays); "
+              f"watertight predicate, the shader's DFS (raytracer.glsl:246-295) without t pruning, OpenMP over rays")
     line = {
         "metric": METRIC, "impl": "reference", "value": round(value, 4), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(times), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded displaced icosphere)",
-        "config": {"workload": WORKLOAD, "triangles": n, "image": [W, H], "sample": f"1/{stride} of the frame per step"},
+        "data": "synthetic (seeded clustered soup and host-generated bounce rays)",
+        "config": headline_config(),
         "build_ms": round(build_ms, 2),
+        "rays_sha256": digest(rays),
+        "sample_hits_sha256": digest(allh),
+        "sample_hits": int((allh[:, 0].view(np.uint32) != 0xFFFFFFFF).sum()),
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                         "sample": f"every {stride}th primary ray per step (rotating offset), shader predicate, "
-                                   f"right-child-first DFS without t pruning; shadow rays for its hits"},
+                         "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config0_shader_predicate": {"cpu_reference_predicate_mrays_s": round(r0.shape[0] / c0_ms / 1e3, 3),
+                                     "hits": int((h0[:, 0].view(np.uint32) != 0xFFFFFFFF).sum()),
+                                     "hits_sha256": digest(h0)},
     }
     print(json.dumps(line))
 
 
 def main():
+    global N_BOUNCE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-predictor", action="store_true", help="skip the learned-predictor (4M-triangle) experiment")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the restructured tree, the shader-predicate soup and the icosphere frame")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched experiment")
     ap.add_argument("--no-dynamic", action="store_true", help="skip the 16M-triangle 60-frame dynamic experiment")
+    ap.add_argument("--rays", type=int, default=N_BOUNCE,
+                    help="bounce rays per step (default 8,388,608; smaller batches for profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    N_BOUNCE = args.rays
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -293,6 +293,12 @@ crt_status crt_trace(crt_ctx* ctx, const crt_bvh* bvh, const crt_ray* rays, uint
  * out[0] = traversal nodes fetched (64-byte binary, or 128-byte 4-wide with
  * CRT_TRACE_WIDE), out[1] = triangles tested. */
 crt_status crt_last_trace_stats(crt_ctx* ctx, uint64_t out[2]);
+/* Device time of the last traversal issued through crt_trace,
+ * crt_trace_seeded or the multi-launch frame paths, from CUDA events on the
+ * context's stream: ms[0] = the work before the traversal kernel (predictor
+ * inference, ray keys and their radix sort; 0 for a plain trace), ms[1] =
+ * the traversal kernel itself.  Waits for that work to finish. */
+crt_status crt_last_trace_timing(crt_ctx* ctx, float ms[2]);
 
 /* One frame of the reference's compute pass (Application::drawOneFrame,
  * srcOpenGL/application.cpp:220-262, minus shading): getRay for every texel

@@ -490,7 +490,8 @@ inline bool slab_reference(const crt_ray& r, const crt_bvh_node& n) {
 
 // Generous box test for the watertight oracle: double precision, box grown
 // by 1e-5 of its own scale, so every triangle the float test can hit is reached.
-inline bool slab_loose(const crt_ray& r, const crt_bvh_node& n) {
+// *enter (optional) receives the entry distance along d.
+inline bool slab_loose(const crt_ray& r, const crt_bvh_node& n, double* enter = nullptr) {
     double t0 = -1e300, t1 = 1e300;
     for (int k = 0; k < 3; ++k) {
         const double pad = 1e-5 * (1.0 + std::fabs(static_cast<double>(n.mn[k])) + std::fabs(static_cast<double>(n.mx[k])));
@@ -503,9 +504,17 @@ inline bool slab_loose(const crt_ray& r, const crt_bvh_node& n) {
         if (a > b) std::swap(a, b);
         t0 = std::max(t0, a); t1 = std::min(t1, b);
     }
+    if (enter) *enter = t0;
     return t1 >= std::min(0.0, static_cast<double>(r.tmin)) - 1e-6 && t0 <= t1 &&
            t0 <= static_cast<double>(r.tmax) * (1.0 + 1e-5) + 1e-6;
 }
+
+// Pruned walk of oracle_trace (ORACLE_PRUNED): the nearer child first, and a
+// box only when it can hold a hit at t <= the best t so far (the box test
+// with tmax = best t keeps every box a tying hit could lie in).  It finds the
+// same closest hit (same tie rule) as the full walk; tests pin that, and it
+// serves only to make large test inputs (the hits a bounce ray starts from).
+constexpr uint32_t kOraclePruned = 0x100u;
 
 }  // namespace
 
@@ -556,6 +565,8 @@ void oracle_shadow_rays(const crt_ray* prim, const crt_hit* hits, uint32_t n, co
 //     replaces a hit (the shader's :279 compares an unset t there).
 //   CRT_TRI_WATERTIGHT: every triangle reachable through a generously grown
 //     box is tested; equal t keeps the lower triangle index.
+//   0x100 (with CRT_TRI_WATERTIGHT, closest hit): the pruned walk above, for
+//     making large test inputs only; same hits, far fewer boxes.
 // stats (optional, 2 x uint64): nodes whose box was tested, triangles tested.
 void oracle_trace(const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangle* tris, uint32_t n_tris,
                   const crt_mesh_model* models, uint32_t n_models, const crt_ray* rays, uint32_t n_rays,
@@ -565,6 +576,7 @@ void oracle_trace(const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangl
     for (uint32_t i = 0; i < n_tris; ++i) xt[i] = xform(tris[i], M);
     const bool any = (flags & CRT_TRACE_ANY) != 0;
     const bool wt = (flags & CRT_TRI_WATERTIGHT) != 0;
+    const bool pruned = wt && !any && (flags & kOraclePruned) != 0;
     uint64_t visited = 0, tested = 0;
 #pragma omp parallel for schedule(dynamic, 256) reduction(+ : visited, tested)
     for (int64_t ri = 0; ri < static_cast<int64_t>(n_rays); ++ri) {
@@ -575,22 +587,45 @@ void oracle_trace(const crt_bvh_node* nodes, uint32_t n_nodes, const crt_triangl
         bool have = false;
         float bt = 0.f;
         uint32_t bid = 0;
-        std::vector<uint32_t> stack;
-        stack.reserve(128);
+        // one stack per thread, reused across its rays
+        static thread_local std::vector<uint32_t> stack;
+        stack.clear();
         stack.push_back(0);
+        crt_ray rb = r;  // the pruned walk's box-test ray: tmax = best t
         while (!stack.empty()) {
             const uint32_t ni = stack.back();
             stack.pop_back();
             const crt_bvh_node& nd = nodes[ni];
             ++visited;
-            if (!(wt ? slab_loose(r, nd) : slab_reference(r, nd))) continue;
+            if (pruned) {
+                if (!slab_loose(rb, nd)) continue;
+                if (!(nd.left == 0 && nd.right == 0)) {
+                    double el = 0.0, er = 0.0;
+                    const bool hl = slab_loose(rb, nodes[nd.left], &el);
+                    const bool hr = slab_loose(rb, nodes[nd.right], &er);
+                    if (hl && hr) {
+                        stack.push_back(el <= er ? nd.right : nd.left);
+                        stack.push_back(el <= er ? nd.left : nd.right);
+                    } else if (hl) {
+                        stack.push_back(nd.left);
+                    } else if (hr) {
+                        stack.push_back(nd.right);
+                    }
+                    continue;
+                }
+            } else if (!(wt ? slab_loose(r, nd) : slab_reference(r, nd))) {
+                continue;
+            }
             if (nd.left == 0 && nd.right == 0) {
                 ++tested;
                 const Hit h = wt ? tri_watertight(r, w, xt[nd.tri]) : tri_reference(r, xt[nd.tri]);
                 if (!h.did) continue;
                 if (any) { have = true; bid = nd.tri; bt = h.t; out.u = h.u; out.v = h.v; break; }
                 const bool better = !have || h.t < bt || (wt && h.t == bt && nd.tri < bid);
-                if (better) { have = true; bt = h.t; bid = nd.tri; out.u = h.u; out.v = h.v; }
+                if (better) {
+                    have = true; bt = h.t; bid = nd.tri; out.u = h.u; out.v = h.v;
+                    rb.tmax = bt;
+                }
             } else {
                 stack.push_back(nd.left);
                 stack.push_back(nd.right);

@@ -29,6 +29,10 @@ REFERENCE_DIR = os.environ.get("CRT_REFERENCE_DIR") or os.path.join(os.path.dirn
 _lib = None
 _ref = None
 
+# oracle_trace flag (with CRT_TRI_WATERTIGHT, closest hit): the pruned
+# near-first walk, same hits as the full walk; for making large test inputs.
+PRUNED = 0x100
+
 
 def build(ref: bool | None = None) -> None:
     """Compile the restatement (always) and the reference library (when the

@@ -52,7 +52,7 @@ EXPORTS = [
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
     "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_bvh_from_nodes",
     "crt_validate_nodes", "crt_obj_parse",
-    "crt_triangles_from_indexed", "crt_selftest_wait", "crt_selftest_tc_wait",
+    "crt_triangles_from_indexed", "crt_selftest_wait", "crt_selftest_tc_wait", "crt_last_trace_timing",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -148,6 +148,7 @@ def lib():
             "crt_triangles_from_indexed": ([vp, vp, u32, vp, u32, u32, vp], i32),
             "crt_selftest_wait": ([vp, i32, u32], i32),
             "crt_selftest_tc_wait": ([vp, i32, u32], i32),
+            "crt_last_trace_timing": ([vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -584,6 +585,12 @@ class Context:
         out = np.zeros(2, np.uint64)
         _check(lib().crt_last_trace_stats(self.handle, _ptr(out)))
         return int(out[0]), int(out[1])
+
+    def last_trace_timing(self):
+        """(ms before the traversal kernel, traversal kernel ms) of the last trace, from CUDA events."""
+        out = np.zeros(2, np.float32)
+        _check(lib().crt_last_trace_timing(self.handle, _ptr(out)))
+        return float(out[0]), float(out[1])
 
     def trace_frame(self, bvh: Bvh, cam, width: int, height: int, light=None, flags: int = 0,
                     hits_primary=None, hits_shadow=None):

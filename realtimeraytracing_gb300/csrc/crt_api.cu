@@ -191,6 +191,9 @@ struct crt_ctx {
     void* pinned = nullptr;
     size_t pinned_cap = 0;
     cudaEvent_t ev[6] = {};
+    // crt_trace timing: start, traversal kernel launch, end (on the stream)
+    cudaEvent_t tev[3] = {};
+    bool tev_valid = false;
     crt_build_stats stats{};
     std::vector<uint2> it_host;
     bool force_multi_launch = false;  // testing: run PLOC/layout as one launch per iteration
@@ -270,6 +273,8 @@ crt_status crt_create(crt_ctx** out, const crt_config* cfg) {
     if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) s = fail(CRT_ERR_CUDA, "stream");
     for (auto& e : x->ev)
         if (s == CRT_OK && cudaEventCreate(&e) != cudaSuccess) s = fail(CRT_ERR_CUDA, "event");
+    for (auto& e : x->tev)
+        if (s == CRT_OK && cudaEventCreate(&e) != cudaSuccess) s = fail(CRT_ERR_CUDA, "event");
     if (s == CRT_OK) s = x->scene_state.reserve(sizeof(crt::SceneState));
     if (s == CRT_OK) s = x->err.reserve(16);
     if (s == CRT_OK) s = x->models.reserve(2 * 64 * 16 * sizeof(float));
@@ -303,6 +308,8 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->mesh_vertices, &x->mesh_indices, &x->mesh_out, &x->probe_flag};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : x->tev)
         if (e) cudaEventDestroy(e);
     if (x->pinned) cudaFreeHost(x->pinned);
     if (x->stream) cudaStreamDestroy(x->stream);
@@ -639,6 +646,8 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     if (n_rays == 0) return CRT_OK;
     if (flags & CRT_TRACE_WIDE) CRT_TRY(ensure_wide4(x, b));
     if (flags & CRT_TRACE_COMPRESSED) CRT_TRY(ensure_cwide(x, b));
+    x->tev_valid = false;
+    CRT_CUDA(cudaEventRecord(x->tev[0], x->stream));
     crt::TraceParams p{};
     p.nodes = b->nodes.as<crt_bvh_node>();
     p.xtri = b->xtri.as<float4>();
@@ -693,8 +702,11 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     const bool deep = (b->depth_bound + 2 > 64) || (3 * ((b->depth_bound + 2) / 2) + 3 > 96);
     const uint32_t launch_flags =
         (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED)) | (deep ? (1u << 16) : 0u);
+    CRT_CUDA(cudaEventRecord(x->tev[1], x->stream));
     crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
     CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaEventRecord(x->tev[2], x->stream));
+    x->tev_valid = true;
     return CRT_OK;
 }
 
@@ -1216,6 +1228,15 @@ crt_status crt_trace_seeded(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, u
     CRT_TRY(x->check_device_error());
     if (flags & CRT_TRACE_STATS)
         CRT_CUDA(cudaMemcpy(x->last_trace_stats, x->trace_stats.p, 16, cudaMemcpyDeviceToHost));
+    return CRT_OK;
+}
+
+crt_status crt_last_trace_timing(crt_ctx* x, float ms[2]) {
+    if (!x || !ms) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    if (!x->tev_valid) return fail(CRT_ERR_INVALID_ARG, "crt_last_trace_timing: no traversal recorded yet");
+    CRT_CUDA(cudaEventSynchronize(x->tev[2]));
+    CRT_CUDA(cudaEventElapsedTime(&ms[0], x->tev[0], x->tev[1]));
+    CRT_CUDA(cudaEventElapsedTime(&ms[1], x->tev[1], x->tev[2]));
     return CRT_OK;
 }
 

@@ -267,6 +267,103 @@ def sphere_rays(n: int, seed: int = 0, radius: float = 2.0, center=(0.5, 0.5, 0.
     return r
 
 
+def bounce_rays(prim: np.ndarray, hits: np.ndarray, tris: np.ndarray, n_out: int, seed: int = 0,
+                chunk: int = 1 << 20) -> np.ndarray:
+    """Cosine-weighted diffuse bounce rays from closest hits, on the host.
+
+    Ray j leaves hit number (j * 2654435761 + seed) mod n_hits of the
+    primary hits in ray order (so consecutive rays come from scattered
+    pixels: an incoherent batch).  Its origin is the hit point o + t d, its
+    direction normalize(n + u) with n the hit triangle's unit geometric
+    normal turned toward the incoming ray and u uniform on S^2 (a
+    cosine-weighted direction about n), and [tmin, tmax] = [1e-4, inf].
+    Only IEEE-exact float64 arithmetic (+, -, *, /, sqrt) and the SplitMix64
+    stream, so equal inputs give equal rays on every machine.  Triangles are
+    (n, 16) records with identity models (their vertices as stored)."""
+    tri = np.ascontiguousarray(hits[:, 0]).view(np.uint32)
+    src = np.nonzero(tri != 0xFFFFFFFF)[0]
+    out = np.zeros((n_out, 8), np.float32)
+    if src.size == 0:
+        out[:, 3] = 1.0  # empty rays: tmin 1 > tmax 0
+        return out
+    j = np.arange(n_out, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        pick = ((j * np.uint64(2654435761) + np.uint64(seed)) % np.uint64(src.size)).astype(np.int64)
+    for c0 in range(0, n_out, chunk):
+        c1 = min(n_out, c0 + chunk)
+        k = src[pick[c0:c1]]
+        o = prim[k, 0:3].astype(np.float64)
+        d = prim[k, 4:7].astype(np.float64)
+        t = hits[k, 1].astype(np.float64)
+        p = (o + t[:, None] * d).astype(np.float32).astype(np.float64)
+        tv = tris[tri[k]]
+        a, b, cc = tv[:, 0:3].astype(np.float64), tv[:, 4:7].astype(np.float64), tv[:, 8:11].astype(np.float64)
+        e1, e2 = b - a, cc - a
+        nrm = np.stack([e1[:, 1] * e2[:, 2] - e1[:, 2] * e2[:, 1],
+                        e1[:, 2] * e2[:, 0] - e1[:, 0] * e2[:, 2],
+                        e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]], axis=1)
+        ln = np.sqrt((nrm ** 2).sum(1))
+        nrm /= np.where(ln > 0.0, ln, 1.0)[:, None]
+        flip = (nrm * d).sum(1) > 0.0
+        nrm[flip] = -nrm[flip]
+        u = _unit_vectors(seed, 5000 + 8 * (c0 // chunk), c1 - c0)
+        v = nrm + u
+        lv = np.sqrt((v ** 2).sum(1))
+        bad = lv < 1e-9
+        v[bad] = nrm[bad]
+        lv[bad] = 1.0
+        v /= lv[:, None]
+        out[c0:c1, 0:3] = p
+        out[c0:c1, 3] = 1e-4
+        out[c0:c1, 4:7] = v
+        out[c0:c1, 7] = np.inf
+    return out
+
+
+def config3_rays(tris, models, primary_hits_fn, seed: int = 11, width: int = 2048, n_out: int = 8 * 1024 * 1024):
+    """The incoherent-bounce rays of the hit-predictor workload: 2048x2048
+    primary rays from (0.5, 0.5, -1.5) toward +z, their closest hits
+    (watertight) from primary_hits_fn(rays) -> (n, 4) hits, then n_out
+    cosine bounce rays (bounce_rays).  Returns (primary rays, primary hits,
+    bounce rays)."""
+    cam = camera_gpu_data((0.5, 0.5, -1.5))
+    prim = pinhole_rays(cam, width, width)
+    ph = primary_hits_fn(prim)
+    return prim, ph, bounce_rays(prim, ph, tris, n_out, seed)
+
+
+def pinhole_rays(cam: np.ndarray, width: int, height: int) -> np.ndarray:
+    """getRay (raytracer.glsl:92-100) on the host in float32, operation for
+    operation as the library's raygen (float32 division, glm mat*vec order,
+    1/sqrt): ray (x, y) at row y * width + x."""
+    f = np.float32
+    cam = np.asarray(cam, np.float32)
+    m = cam[0:16]
+    eye = cam[16:20]
+    pw_, ph_, pn_ = cam[20], cam[21], cam[22]
+    xs = np.arange(width, dtype=np.float32) / f(width)
+    ys = np.arange(height, dtype=np.float32) / f(height)
+    px, py = np.meshgrid(xs, ys)
+    v0 = (px - f(0.5)) * pw_
+    v1 = (py - f(0.5)) * ph_
+    v2 = np.full_like(v0, f(1.0) * pn_)
+    v3 = np.full_like(v0, f(1.0))
+    comp = []
+    for r in range(4):
+        a = m[0 + r] * v0 + m[4 + r] * v1
+        b = m[8 + r] * v2 + m[12 + r] * v3
+        comp.append(a + b)
+    dx, dy, dz, dw = comp[0] - eye[0], comp[1] - eye[1], comp[2] - eye[2], comp[3] - eye[3]
+    inv = f(1.0) / np.sqrt(((dx * dx + dy * dy) + dz * dz) + dw * dw)
+    rays = np.zeros((height * width, 8), np.float32)
+    rays[:, 0:3] = eye[0:3]
+    rays[:, 4] = (dx * inv).reshape(-1)
+    rays[:, 5] = (dy * inv).reshape(-1)
+    rays[:, 6] = (dz * inv).reshape(-1)
+    rays[:, 7] = np.inf
+    return rays
+
+
 def config2_sizes(n_scenes: int = 64, seed: int = 0, tri_range=(1000, 2_000_000), ray_range=(65536, 4_194_304)):
     """Log-uniform triangle and ray counts of the batched workload."""
     u = uniform01(seed, 401, n_scenes)
