@@ -275,6 +275,27 @@ crt_status crt_selftest_wait(crt_ctx* ctx, int set_flag, uint32_t spin_limit);
  * 0 = the predictor kernels' own limit. */
 crt_status crt_selftest_tc_wait(crt_ctx* ctx, int complete, uint32_t spin_limit);
 
+/* The radix sort's two counting steps alone, the parts the reference's GPU
+ * sort shaders implement (srcCommon/shaders/ploc/preprocessing/sort/
+ * histogramOfGlobalDigitCounts.glsl:31-59, prefixSumOfGlobalDigitCounts.glsl:
+ * 24-69) and its sort tests check (tests/testsSortGPU/testHistogramCreation.cpp,
+ * testHistogramCreationHard.cpp, testHistogramPrefixSum.cpp).  Both run the
+ * device functions the sort passes themselves use.  digit_bits: 1, 2, 4 or 8.
+ *   crt_radix_digit_counts: counts[p * 2^digit_bits + d] = keys whose digit p
+ *     (bits p*digit_bits and up) is d, for the ceil(32 / digit_bits) digit
+ *     places of 32-bit keys.  With 1-bit digits, counts[2b + 1] is the
+ *     reference's per-bit histogram entry b.
+ *   crt_radix_digit_offsets: for each of n_places places, the exclusive scan
+ *     of its 2^digit_bits counts (where each digit's keys start in that
+ *     pass's output).  With 2-bit digits this is the reference's scan inside
+ *     each group of 4 histogram entries.
+ * Pointers may be host or device memory; both return after their stream
+ * synchronises. */
+crt_status crt_radix_digit_counts(crt_ctx* ctx, const uint32_t* keys, uint32_t n, uint32_t digit_bits,
+                                  uint32_t* counts);
+crt_status crt_radix_digit_offsets(crt_ctx* ctx, const uint32_t* counts, uint32_t n_places, uint32_t digit_bits,
+                                   uint32_t* offsets);
+
 /* ---- rays ------------------------------------------------------------- */
 /* Primary rays of getRay (raytracer.glsl:92-100) for a width x height image:
  * ray (x, y) is stored at y * width + x and uses pos = (x / width, y / height). */

@@ -7,6 +7,9 @@ ctypes front end of the CPU oracle:
   * _ref/libref_bvh.so — the reference's own bvh.cpp/triangle.cpp compiled in
     place with the project's glm shim (only where the reference checkout is
     present; N <= 65,536).
+  * _ref/libref_shader.so — the reference's own raytracer.glsl compiled as
+    C++ (declarations rewritten by glsl_to_cpp.py, bodies unchanged, the
+    project's GLSL shim), where the reference checkout is present.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module.
@@ -22,12 +25,14 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_bvh.so")
+SHADER_LIB = os.path.join(HERE, "_ref", "libref_shader.so")
 # The reference checkout: CRT_REFERENCE_DIR, else a directory named
 # "reference" beside the repository.
 REFERENCE_DIR = os.environ.get("CRT_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 _lib = None
 _ref = None
+_shader = None
 
 # oracle_trace flag (with CRT_TRI_WATERTIGHT, closest hit): the pruned
 # near-first walk, same hits as the full walk; for making large test inputs.
@@ -85,6 +90,54 @@ def ref_lib():
         L.ref_max_triangles.restype = u32
         _ref = L
     return _ref
+
+
+def shader_available() -> bool:
+    return os.path.exists(SHADER_LIB)
+
+
+def shader_lib():
+    """The reference's raytracer.glsl compiled as C++ (shader_driver.cpp)."""
+    global _shader
+    if _shader is None:
+        L = C.CDLL(SHADER_LIB)
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        L.glsl_closest_hits.argtypes = [vp, vp, u32, vp, u32, vp, u32, vp]
+        L.glsl_all_hits.argtypes = [vp, u32, vp, u32, vp, u32, vp]
+        L.glsl_frame.argtypes = [vp, u32, u32, vp, vp, u32, vp, u32, vp, u32, u32, i32, vp]
+        _shader = L
+    return _shader
+
+
+def shader_closest_hits(nodes, tris, models, rays):
+    """getClosestHitBVH (raytracer.glsl:246-295) of the shader itself, per ray."""
+    nodes = _f32(nodes, 12)
+    tris, models, rays = _f32(tris, 16), _f32(models, 17), _f32(rays, 8)
+    hits = np.zeros((rays.shape[0], 4), np.float32)
+    shader_lib().glsl_closest_hits(_p(nodes), _p(tris), tris.shape[0], _p(models), models.shape[0], _p(rays),
+                                   rays.shape[0], _p(hits))
+    return hits
+
+
+def shader_all_hits(tris, models, rays):
+    """getAllHits (raytracer.glsl:149-157) of the shader itself, per ray."""
+    tris, models, rays = _f32(tris, 16), _f32(models, 17), _f32(rays, 8)
+    hits = np.zeros((rays.shape[0], 4), np.float32)
+    shader_lib().glsl_all_hits(_p(tris), tris.shape[0], _p(models), models.shape[0], _p(rays), rays.shape[0],
+                               _p(hits))
+    return hits
+
+
+def shader_frame(cam, width, height, nodes, tris, models, materials, flags=0, depth=0):
+    """The shader's main (raytracer.glsl:299-331) over (width/16) x
+    (height/16) work groups: RGBA32F texels, row y at y * width."""
+    cam = np.ascontiguousarray(cam, np.float32)
+    nodes = _f32(nodes, 12)
+    tris, models, materials = _f32(tris, 16), _f32(models, 17), _f32(materials, 4)
+    out = np.zeros((width * height, 4), np.float32)
+    shader_lib().glsl_frame(_p(cam), width, height, _p(nodes), _p(tris), tris.shape[0], _p(models), models.shape[0],
+                            _p(materials), materials.shape[0], flags, depth, _p(out))
+    return out
 
 
 def _f32(a, cols):

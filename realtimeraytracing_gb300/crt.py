@@ -53,6 +53,7 @@ EXPORTS = [
     "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_bvh_from_nodes",
     "crt_validate_nodes", "crt_obj_parse",
     "crt_triangles_from_indexed", "crt_selftest_wait", "crt_selftest_tc_wait", "crt_last_trace_timing",
+    "crt_radix_digit_counts", "crt_radix_digit_offsets",
 ]
 
 PREDICTOR_CLASSES = 128
@@ -149,6 +150,8 @@ def lib():
             "crt_selftest_wait": ([vp, i32, u32], i32),
             "crt_selftest_tc_wait": ([vp, i32, u32], i32),
             "crt_last_trace_timing": ([vp, vp], i32),
+            "crt_radix_digit_counts": ([vp, vp, u32, u32, vp], i32),
+            "crt_radix_digit_offsets": ([vp, vp, u32, u32, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -515,6 +518,21 @@ class Context:
     def selftest_tc_wait(self, complete: bool, spin_limit: int = 0):
         """crt_selftest_tc_wait: one MMA commit wait (completed, or never completed)."""
         _check(lib().crt_selftest_tc_wait(self.handle, 1 if complete else 0, spin_limit))
+
+    def radix_digit_counts(self, keys, digit_bits: int):
+        """crt_radix_digit_counts: (places, 2^digit_bits) counts of 32-bit keys."""
+        keys = np.ascontiguousarray(keys, np.uint32) if isinstance(keys, np.ndarray) else keys
+        places = (32 + digit_bits - 1) // digit_bits
+        out = np.zeros((places, 1 << digit_bits), np.uint32)
+        _check(lib().crt_radix_digit_counts(self.handle, _ptr(keys), _rows(keys), digit_bits, _ptr(out)))
+        return out
+
+    def radix_digit_offsets(self, counts, digit_bits: int):
+        """crt_radix_digit_offsets: per place (row), the exclusive scan of its digit counts."""
+        counts = np.ascontiguousarray(counts, np.uint32).reshape(-1, 1 << digit_bits)
+        out = np.zeros_like(counts)
+        _check(lib().crt_radix_digit_offsets(self.handle, _ptr(counts), counts.shape[0], digit_bits, _ptr(out)))
+        return out
 
     def build(self, tris, n_tris=None, models=None, n_buffer=None) -> Bvh:
         """cr::BVH::BVH(nbTriangles, unsortedTriangles, meshesInTheScene)."""

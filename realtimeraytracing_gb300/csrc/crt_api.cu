@@ -185,6 +185,7 @@ struct crt_ctx {
     DevBuf xtri_sorted;  // leaf records in sorted order until the layout moves them
     DevBuf mesh_vertices, mesh_indices, mesh_out;  // crt_triangles_from_indexed staging
     DevBuf probe_flag;                             // crt_selftest_wait
+    DevBuf step_in, step_out;                      // crt_radix_digit_counts / _offsets
     DevBuf opt_scratch;                            // crt_optimize
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
@@ -305,7 +306,8 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->trace_stats, &x->frame_rays, &x->frame_hits, &x->frame_shadow, &x->frame_shits,
                       &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
                       &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state, &x->xtri_sorted,
-                      &x->mesh_vertices, &x->mesh_indices, &x->mesh_out, &x->probe_flag};
+                      &x->mesh_vertices, &x->mesh_indices, &x->mesh_out, &x->probe_flag, &x->step_in,
+                      &x->step_out};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -343,6 +345,61 @@ crt_status crt_selftest_tc_wait(crt_ctx* x, int complete, uint32_t spin_limit) {
     CRT_CUDA(cudaStreamSynchronize(x->stream));
     for (int i = 0; i < 128; ++i)
         if (got[i] != 16.f) return fail(CRT_ERR_CUDA, "MMA probe: lane %d read %g, expected 16", i, got[i]);
+    return CRT_OK;
+}
+
+// The radix sort's counting and digit-offset steps on caller data (host or
+// device memory), each through the library's own device functions.
+crt_status crt_radix_digit_counts(crt_ctx* x, const uint32_t* keys, uint32_t n, uint32_t digit_bits, uint32_t* counts) {
+    if (!x || (!keys && n) || !counts) return fail(CRT_ERR_INVALID_ARG, "crt_radix_digit_counts: null argument");
+    if (digit_bits != 1 && digit_bits != 2 && digit_bits != 4 && digit_bits != 8)
+        return fail(CRT_ERR_INVALID_ARG, "crt_radix_digit_counts: digit_bits must be 1, 2, 4 or 8");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const size_t n_counts = static_cast<size_t>((32 + digit_bits - 1) / digit_bits) << digit_bits;
+    const uint32_t* d_keys = keys;
+    if (n && !is_device_ptr(keys)) {
+        CRT_TRY(x->step_in.reserve(4ull * n));
+        CRT_CUDA(cudaMemcpyAsync(x->step_in.p, keys, 4ull * n, cudaMemcpyHostToDevice, x->stream));
+        d_keys = x->step_in.as<uint32_t>();
+    }
+    const bool dev_out = is_device_ptr(counts);
+    uint32_t* d_counts = counts;
+    if (!dev_out) {
+        CRT_TRY(x->step_out.reserve(4 * n_counts));
+        d_counts = x->step_out.as<uint32_t>();
+    }
+    CRT_CUDA(cudaMemsetAsync(d_counts, 0, 4 * n_counts, x->stream));
+    if (n) crt::launch_digit_counts(d_keys, n, static_cast<int>(digit_bits), d_counts, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(counts, d_counts, 4 * n_counts, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    return CRT_OK;
+}
+
+crt_status crt_radix_digit_offsets(crt_ctx* x, const uint32_t* counts, uint32_t n_places, uint32_t digit_bits,
+                                   uint32_t* offsets) {
+    if (!x || !counts || !offsets) return fail(CRT_ERR_INVALID_ARG, "crt_radix_digit_offsets: null argument");
+    if (digit_bits != 1 && digit_bits != 2 && digit_bits != 4 && digit_bits != 8)
+        return fail(CRT_ERR_INVALID_ARG, "crt_radix_digit_offsets: digit_bits must be 1, 2, 4 or 8");
+    if (n_places == 0 || n_places > 65536) return fail(CRT_ERR_INVALID_ARG, "crt_radix_digit_offsets: bad n_places");
+    CRT_CUDA(cudaSetDevice(x->device));
+    const size_t n_counts = static_cast<size_t>(n_places) << digit_bits;
+    const uint32_t* d_in = counts;
+    if (!is_device_ptr(counts)) {
+        CRT_TRY(x->step_in.reserve(4 * n_counts));
+        CRT_CUDA(cudaMemcpyAsync(x->step_in.p, counts, 4 * n_counts, cudaMemcpyHostToDevice, x->stream));
+        d_in = x->step_in.as<uint32_t>();
+    }
+    const bool dev_out = is_device_ptr(offsets);
+    uint32_t* d_out = offsets;
+    if (!dev_out) {
+        CRT_TRY(x->step_out.reserve(4 * n_counts));
+        d_out = x->step_out.as<uint32_t>();
+    }
+    crt::launch_digit_offsets(d_in, n_places, static_cast<int>(digit_bits), d_out, x->stream);
+    CRT_CUDA(cudaGetLastError());
+    if (!dev_out) CRT_CUDA(cudaMemcpyAsync(offsets, d_out, 4 * n_counts, cudaMemcpyDeviceToHost, x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
     return CRT_OK;
 }
 

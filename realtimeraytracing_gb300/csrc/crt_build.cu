@@ -140,6 +140,40 @@ __device__ __forceinline__ uint32_t to_u10(float x) {  // bvh.cpp:363-367
     return __float2uint_rz(x);  // NaN -> 0, as on the reference's hosts
 }
 
+// The digit histograms of the radix passes: for each of PASSES digit places
+// of BITS bits, one count per digit value, in shared memory (s_hist[p *
+// 2^BITS + d]).  The sort's counting step — with 1-bit digits it is the
+// reference's per-bit histogram (histogramOfGlobalDigitCounts.glsl:31-59).
+template <int BITS, int PASSES>
+__device__ __forceinline__ void add_digit_counts(uint32_t key, uint32_t* s_hist) {
+    constexpr uint32_t RADIX = 1u << BITS;
+#pragma unroll
+    for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p * RADIX + ((key >> (p * BITS)) & (RADIX - 1))], 1u);
+}
+
+// Block-wide inclusive scan, in thread order, of one 64-bit value per thread
+// (the radix passes pack two 32-bit counts into it); s_wsum holds one entry
+// per warp.  Every thread of the block must call it.
+template <int BLOCK>
+__device__ __forceinline__ unsigned long long block_inclusive_scan_u64(unsigned long long v,
+                                                                       unsigned long long* s_wsum) {
+    constexpr int WARPS = BLOCK / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) s_wsum[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long run = 0;
+        for (int w = 0; w < WARPS; ++w) { const unsigned long long t = s_wsum[w]; s_wsum[w] = run; run += t; }
+    }
+    __syncthreads();
+    return v + s_wsum[warp];
+}
+
 // Centroid (triangle.cpp:31-33), normalisation (bvh.cpp:314-328) and code
 // (bvh.cpp:358-372), plus the digit histograms of all radix passes.
 template <int BITS>
@@ -166,8 +200,7 @@ __global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restr
         const float nx = (c.x - cmx) / lx, ny = (c.y - cmy) / ly, nz = (c.z - cmz) / lz;
         const uint32_t code = (expand_bits(to_u10(nx)) << 2) | (expand_bits(to_u10(ny)) << 1) | expand_bits(to_u10(nz));
         codes[i] = code;
-#pragma unroll
-        for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p * RADIX + ((code >> (p * BITS)) & (RADIX - 1))], 1u);
+        add_digit_counts<BITS, PASSES>(code, s_hist);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < PASSES * RADIX; i += blockDim.x)
@@ -296,20 +329,8 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
     // histogram), packed as two 32-bit halves of one 64-bit scan.
     const uint32_t gh = (d < RADIX) ? pass_hist[d] : 0u;
     const uint32_t a = (d < RADIX) ? total : 0u;
-    unsigned long long packed = (static_cast<unsigned long long>(gh) << 32) | a;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, packed, o);
-        if (lane >= o) packed += y;
-    }
-    if (lane == 31) s_wsum[warp] = packed;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long run = 0;
-        for (int w = 0; w < WARPS; ++w) { const unsigned long long t = s_wsum[w]; s_wsum[w] = run; run += t; }
-    }
-    __syncthreads();
-    packed += s_wsum[warp];
+    const unsigned long long packed =
+        block_inclusive_scan_u64<BLOCK>((static_cast<unsigned long long>(gh) << 32) | a, s_wsum);
     if (d < RADIX) {
         if (tile > 0) {
             // Look-back: sum the predecessors' counts of digit d down to the
@@ -1146,6 +1167,63 @@ void launch_onesweep_segments(const uint32_t* keys_in, const uint32_t* vals_in, 
     const uint32_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
     onesweep_kernel<8, 256, 16, true><<<tiles, 256, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, 0, seg_hist,
                                                              lookback, ticket, err, spin_limit, seg_off, n_seg);
+}
+
+// The sort's counting and digit-offset steps alone, on caller keys and
+// counts (the reference's sort-shader known-answer tests drive them).
+template <int BITS>
+__global__ void __launch_bounds__(256) digit_counts_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                           uint32_t* __restrict__ counts) {
+    constexpr int RADIX = 1 << BITS;
+    constexpr int PASSES = (32 + BITS - 1) / BITS;
+    __shared__ uint32_t s_hist[PASSES * RADIX];
+    for (int i = threadIdx.x; i < PASSES * RADIX; i += blockDim.x) s_hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        add_digit_counts<BITS, PASSES>(keys[i], s_hist);
+    __syncthreads();
+    for (int i = threadIdx.x; i < PASSES * RADIX; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&counts[i], s_hist[i]);
+}
+
+// One block per digit place: where each digit's keys start in the pass's
+// output, the exclusive scan over digits that the radix pass takes of its
+// global histogram (the same packed block scan, the global counts in the
+// high half).
+template <int BITS, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) digit_offsets_kernel(const uint32_t* __restrict__ counts,
+                                                              uint32_t* __restrict__ offsets) {
+    constexpr int RADIX = 1 << BITS;
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+    __shared__ unsigned long long s_wsum[BLOCK / 32];
+    const int d = threadIdx.x;
+    const size_t base = static_cast<size_t>(blockIdx.x) * RADIX;
+    const uint32_t gh = d < RADIX ? counts[base + d] : 0u;
+    const unsigned long long incl = block_inclusive_scan_u64<BLOCK>(static_cast<unsigned long long>(gh) << 32, s_wsum);
+    if (d < RADIX) offsets[base + d] = static_cast<uint32_t>(incl >> 32) - gh;
+}
+
+bool launch_digit_counts(const uint32_t* keys, uint32_t n, int bits, uint32_t* counts, cudaStream_t s) {
+    const uint32_t want = (n + 255) / 256;
+    const uint32_t grid = want < static_cast<uint32_t>(kNumSms * 8) ? (want ? want : 1u) : kNumSms * 8;
+    switch (bits) {
+        case 1: digit_counts_kernel<1><<<grid, 256, 0, s>>>(keys, n, counts); return true;
+        case 2: digit_counts_kernel<2><<<grid, 256, 0, s>>>(keys, n, counts); return true;
+        case 4: digit_counts_kernel<4><<<grid, 256, 0, s>>>(keys, n, counts); return true;
+        case 8: digit_counts_kernel<8><<<grid, 256, 0, s>>>(keys, n, counts); return true;
+        default: return false;
+    }
+}
+
+bool launch_digit_offsets(const uint32_t* counts, uint32_t places, int bits, uint32_t* offsets, cudaStream_t s) {
+    if (places == 0) return true;
+    switch (bits) {
+        case 1: digit_offsets_kernel<1, 32><<<places, 32, 0, s>>>(counts, offsets); return true;
+        case 2: digit_offsets_kernel<2, 32><<<places, 32, 0, s>>>(counts, offsets); return true;
+        case 4: digit_offsets_kernel<4, 32><<<places, 32, 0, s>>>(counts, offsets); return true;
+        case 8: digit_offsets_kernel<8, 256><<<places, 256, 0, s>>>(counts, offsets); return true;
+        default: return false;
+    }
 }
 
 void launch_leaf_init(const crt_triangle* tris, uint32_t n, const float* models, const uint32_t* perm, float4* node_box,

@@ -56,6 +56,13 @@ void launch_scene_box(const crt_triangle* tris, uint32_t n_buffer, const float* 
 void launch_morton(const crt_triangle* tris, uint32_t n, const float* models_third, const SceneState* st,
                    uint32_t* codes, uint32_t* hist, int bits, cudaStream_t s);
 uint32_t sort_tile_keys(int bits);
+// The sort's counting step (digit histograms of 32-bit keys, bits in {1, 2,
+// 4, 8}: counts[p * 2^bits + d], counts zeroed by the caller) and its
+// digit-offset step (per place, exclusive scan over its 2^bits counts), for
+// the known-answer tests of the reference's sort shaders.  False on an
+// unsupported width.
+bool launch_digit_counts(const uint32_t* keys, uint32_t n, int bits, uint32_t* counts, cudaStream_t s);
+bool launch_digit_offsets(const uint32_t* counts, uint32_t places, int bits, uint32_t* offsets, cudaStream_t s);
 void launch_onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, uint32_t n,
                      int shift, int bits, const uint32_t* pass_hist, uint32_t* lookback, uint32_t* ticket, uint32_t* err,
                      uint32_t spin_limit, cudaStream_t s);

@@ -6,9 +6,11 @@ oracle/Makefile (target `ref`) into oracle/_ref/libref_bvh.so.  This script
 therefore needs the reference checkout; the fixtures it writes let the oracle
 be pinned on machines without it.
 
-Trace fixtures come from the oracle's restatement of raytracer.glsl (the
-shader itself cannot run without a graphics stack) and only guard that
-restatement against drift.
+Trace and frame fixtures come from the reference's own compute shader,
+srcCommon/shaders/raytracer.glsl compiled as C++ (oracle/glsl_to_cpp.py
+rewrites its declarations, the project's GLSL shim supplies the built-ins;
+oracle/Makefile target `ref` builds oracle/_ref/libref_shader.so), after
+checking that the oracle's restatement gives the same bits.
 
 Inputs are regenerated from seeds by realtimeraytracing_gb300.scenes, whose
 generators use exact arithmetic only; each fixture stores the sha256 of its
@@ -70,11 +72,26 @@ def main():
                         "codes_sha256": sha(r["codes"]), "perm_sha256": sha(r["perm"]),
                         "nodes_sha256": sha(r["nodes"]), "codes_unsorted_sha256": sha(r["codes_unsorted"])}
     rays = O.raygen(cam, w, h)
-    hr, _ = O.trace(r["nodes"], tris, models, rays, 0)
+    hr = O.shader_closest_hits(r["nodes"], tris, models, rays)
+    ho, _ = O.trace(r["nodes"], tris, models, rays, 0)
+    assert sha(hr) == sha(ho), "the oracle's traversal differs from the shader's"
     hw, _ = O.trace(r["nodes"], tris, models, rays, 2)
     index["config0_trace"] = {"camera": [float(x) for x in cam], "rays_sha256": sha(rays),
                               "hits_reference_sha256": sha(hr), "hits_watertight_sha256": sha(hw),
-                              "source": "oracle restatement of raytracer.glsl (shader cannot run here)"}
+                              "source": "reference predicate: the reference's raytracer.glsl compiled as C++ "
+                                        "(getClosestHitBVH); watertight: the oracle's restatement"}
+    # the whole compute pass (main: getRay, closest hit, bvhColor, getColor, imageStore)
+    fw = fh = 128
+    mats = [[0.1, 0.2, 0.3, 1.0], [0.75, 0.5, 0.25, 1.0]]
+    fm = S.models_with_materials([1])
+    img = O.shader_frame(cam, fw, fh, r["nodes"], tris, fm, S.materials(mats), 3, 2)
+    r2 = O.raygen(cam, fw, fh)
+    h2, _ = O.trace(r["nodes"], tris, fm, r2, 0)
+    assert sha(img) == sha(O.shade(r["nodes"], tris, fm, S.materials(mats), r2, h2, 3, 2))
+    index["config0_frame"] = {"width": fw, "height": fh, "flags": 3, "depth": 2, "materials": mats,
+                              "material_ids": [1], "texels_sha256": sha(img),
+                              "source": "the reference's raytracer.glsl main compiled as C++, "
+                                        "wireframe on, BVH boxes of depth 2 displayed"}
     with open(os.path.join(HERE, "index.json"), "w") as f:
         json.dump(index, f, indent=1, sort_keys=True)
     print("wrote", len(index), "fixtures")

@@ -52,6 +52,27 @@ def test_closest_hit_reference_predicate_config0(ctx, config0):
     assert (got[:, 0].view(np.uint32) != crt.MISS).sum() > 10000
 
 
+def test_config0_hits_and_frame_equal_the_shaders(ctx, config0):
+    """Against the reference's own compute shader: tests/golden/index.json
+    holds the digests of what raytracer.glsl (compiled as C++, see
+    tests/test_shader_pin.py) computes on this scene — getClosestHitBVH for
+    all 262,144 primary rays, and main's texels for a 128x128 frame with the
+    wireframe and the depth-2 BVH boxes shown."""
+    import hashlib
+    import json
+    import os
+    tris, models, cam, w, h, bvh = config0
+    with open(os.path.join(os.path.dirname(__file__), "golden", "index.json")) as f:
+        index = json.load(f)
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    hits, _ = ctx.trace_frame(bvh, cam, w, h, None, crt.TRI_REFERENCE)
+    assert sha(hits) == index["config0_trace"]["hits_reference_sha256"]
+    fr = index["config0_frame"]
+    img = ctx.render_frame(bvh, cam, fr["width"], fr["height"], models=S.models_with_materials(fr["material_ids"]),
+                           materials=S.materials(fr["materials"]), shade_flags=fr["flags"], bvh_depth=fr["depth"])
+    assert sha(img) == fr["texels_sha256"]
+
+
 def test_closest_hit_watertight_config0(ctx, config0):
     tris, models, cam, w, h, bvh = config0
     rays = O.raygen(cam, w, h)
