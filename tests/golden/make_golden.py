@@ -53,6 +53,11 @@ def build_cases():
     m[2, 0:16] = np.array([0, 2, 0, 0, -1, 0, 0, 0, 0, 0, 0.5, 0, 0.125, 1, -1, 1], np.float32)
     cases.append(("soup_n2000_models3", t, 2000, m))
     cases.append(("dup_n64", np.repeat(S.uniform_soup(1, seed=79), 64, axis=0), 64, S.identity_models(1)))
+    # the renderer's own buffer: N triangles padded with zero records to 65,536 (scene.cpp:26-40)
+    for n in (1, 3, 1000):
+        t = S.uniform_soup(n, seed=600 + n)
+        cases.append((f"soup_n{n}_padded65536", np.concatenate([t, np.zeros((65536 - n, 16), np.float32)]), n,
+                      S.identity_models(1)))
     return cases
 
 

@@ -104,3 +104,45 @@ def test_adapter_compiles_and_links_against_reference_header(lib, tmp_path):
     libdir = os.path.join(ROOT, "realtimeraytracing_gb300")
     subprocess.run([gxx, "-std=gnu++20", main, obj, *inc, "-L", libdir, "-lcrt", f"-Wl,-rpath,{libdir}",
                     "-o", os.path.join(tmp, "main")], check=True)
+
+
+LAYOUT_PROBE = r"""
+#include <cstddef>
+#include <cstdio>
+#include <typeinfo>
+#include "bvh.hpp"
+#define OFF(T, m) std::printf(#T "." #m " %zu\n", offsetof(cr::T, m))
+int main() {
+    std::printf("TriangleGPU %zu MeshModelGPU %zu AABB_GPU %zu BVH_NodeGPU %zu\n", sizeof(cr::TriangleGPU),
+                sizeof(cr::MeshModelGPU), sizeof(cr::AABB_GPU), sizeof(cr::BVH_NodeGPU));
+    OFF(TriangleGPU, _P1); OFF(TriangleGPU, _P2); OFF(TriangleGPU, _ModelId); OFF(MeshModelGPU, _MaterialId);
+    OFF(AABB_GPU, _Max); OFF(BVH_NodeGPU, _TriangleId); OFF(BVH_NodeGPU, _LeftChild); OFF(BVH_NodeGPU, _RightChild);
+    std::printf("%s\n%s\n%s\n%s\n%s\n%s\n%s\n%s\n", typeid(decltype(cr::BVH_Params::_Clusters)).name(),
+                typeid(decltype(cr::BVH_Params::_IsLeaf)).name(), typeid(decltype(cr::BVH_Params::_Parent)).name(),
+                typeid(decltype(cr::BVH_Params::_LeftChild)).name(), typeid(decltype(cr::BVH_Params::_RightChild)).name(),
+                typeid(decltype(cr::BVH_Params::_TriangleIndices)).name(), typeid(decltype(cr::BVH_Params::_UnsortedTriangles)).name(),
+                typeid(decltype(cr::BVH::_InternalStruct)).name());
+    std::printf("%u %zu\n", static_cast<unsigned>(cr::Triangle::MAX_NB_TRIANGLES), sizeof(cr::BVH_Params::_NbTriangles));
+    return 0;
+}
+"""
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(_reference_dir(), "srcCommon")),
+                    reason="reference checkout not present")
+def test_adapter_stand_in_header_matches_the_reference_header(tmp_path):
+    """tests/adapter_iface/bvh.hpp (used to run the adapter where the
+    reference checkout is absent) declares the reference header's records
+    with the same sizes and member offsets, and BVH_Params members of the
+    same types."""
+    gxx = shutil.which("g++")
+    src = os.path.join(str(tmp_path), "probe.cpp")
+    with open(src, "w") as f:
+        f.write(LAYOUT_PROBE)
+    outs = []
+    for hdr in (os.path.join(_reference_dir(), "srcCommon", "scene", "geometry"), os.path.join(ROOT, "tests", "adapter_iface")):
+        exe = os.path.join(str(tmp_path), "probe")
+        subprocess.run([gxx, "-std=gnu++20", "-w", src, "-I", hdr, "-I", os.path.join(ROOT, "oracle", "glm_shim"),
+                        "-o", exe], check=True)
+        outs.append(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)
+    assert outs[0] == outs[1], outs
