@@ -128,6 +128,10 @@ typedef struct crt_camera {
 #define CRT_TRACE_COMPRESSED  0x80u /* walk 64-byte compressed 4-wide nodes: 8-bit child boxes rounded
                                        outward, exact leaf boxes re-checked (same hits); the reference
                                        layout stays the export format */
+#define CRT_TRACE_PER_RAY_THREADS 0x100u /* closest-hit crt_trace of >= 65,536 rays normally runs on
+                                       persistent warps whose lanes take a new ray as soon as theirs
+                                       is done; this flag keeps one thread per ray for its whole walk
+                                       instead (same hits) */
 
 typedef struct crt_config {
     int device;                 /* CUDA device ordinal, default 0 */

@@ -31,6 +31,7 @@ TRACE_WIDE = 0x10
 PREDICTOR_ORDER = 0x20  # CRT_TRACE_PREDICTOR_ORDER: trace rays grouped by predicted treelet
 SORT_RAYS = 0x40  # CRT_TRACE_SORT_RAYS: trace rays ordered by origin cell and direction
 TRACE_COMPRESSED = 0x80  # CRT_TRACE_COMPRESSED: walk 64-byte compressed 4-wide nodes
+PER_RAY_THREADS = 0x100  # CRT_TRACE_PER_RAY_THREADS: one thread per ray instead of persistent refilling warps
 USE_PREDICTOR = TRACE_USE_PREDICTOR
 MISS = 0xFFFFFFFF
 

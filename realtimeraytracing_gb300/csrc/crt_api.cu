@@ -186,6 +186,7 @@ struct crt_ctx {
     DevBuf mesh_vertices, mesh_indices, mesh_out;  // crt_triangles_from_indexed staging
     DevBuf probe_flag;                             // crt_selftest_wait
     DevBuf step_in, step_out;                      // crt_radix_digit_counts / _offsets
+    DevBuf pool_counter;                           // persistent traversal: next ray to take
     DevBuf opt_scratch;                            // crt_optimize
     uint64_t last_trace_stats[2] = {0, 0};
     // pinned host staging
@@ -307,7 +308,7 @@ crt_status crt_destroy(crt_ctx* x) {
                       &x->ray_order, &x->ray_order_scratch, &x->shade_models, &x->shade_materials,
                       &x->shade_rays, &x->shade_hits, &x->image, &x->refit_state, &x->xtri_sorted,
                       &x->mesh_vertices, &x->mesh_indices, &x->mesh_out, &x->probe_flag, &x->step_in,
-                      &x->step_out};
+                      &x->step_out, &x->pool_counter};
     for (DevBuf* b : bufs) b->release();
     for (auto& e : x->ev)
         if (e) cudaEventDestroy(e);
@@ -666,7 +667,7 @@ crt_status copy_out(crt_ctx* x, void* dst, const void* src, size_t bytes) {
 
 crt_status check_trace_flags(const crt_bvh* b, uint32_t flags) {
     if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_USE_PREDICTOR | CRT_TRACE_STATS | CRT_TRACE_WIDE |
-                  CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_SORT_RAYS | CRT_TRACE_COMPRESSED))
+                  CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_SORT_RAYS | CRT_TRACE_COMPRESSED | CRT_TRACE_PER_RAY_THREADS))
         return fail(CRT_ERR_INVALID_ARG, "crt_trace: unknown flags 0x%x", flags);
     if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && !b->predictor)
         return fail(CRT_ERR_UNSUPPORTED, "crt_trace: no predictor bound to this bvh (crt_predictor_create)");
@@ -698,6 +699,8 @@ crt_status ensure_cwide(crt_ctx* x, const crt_bvh* b) {
 }
 
 // Enqueues one traversal launch on device-resident rays/hits (no sync).
+constexpr uint32_t kPoolMinRays = 65536;  // below this a launch of one thread per ray fills the GPU as well
+
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
                         crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0) {
     if (n_rays == 0) return CRT_OK;
@@ -759,8 +762,16 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     const bool deep = (b->depth_bound + 2 > 64) || (3 * ((b->depth_bound + 2) / 2) + 3 > 96);
     const uint32_t launch_flags =
         (flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED)) | (deep ? (1u << 16) : 0u);
+    // Large closest-hit batches over the binary nodes: persistent warps that
+    // refill finished lanes (the rays of a batch differ widely in walk
+    // length); pixels in 8x4 tiles, any-hit, seeded and wide walks keep one
+    // thread per ray, which shares node fetches between a tile's rays.
+    const bool pool = !(flags & (CRT_TRACE_ANY | CRT_TRACE_WIDE | CRT_TRACE_COMPRESSED | CRT_TRACE_PER_RAY_THREADS)) &&
+                      !p.pred_class && tile_width == 0 && n_rays >= kPoolMinRays;
+    if (pool) CRT_TRY(x->pool_counter.reserve(16));
     CRT_CUDA(cudaEventRecord(x->tev[1], x->stream));
-    crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
+    if (pool) crt::launch_trace_pool(p, launch_flags, x->pool_counter.as<uint32_t>(), x->stream);
+    else crt::launch_trace(p, launch_flags, static_cast<int>(x->cfg.trace_block), x->stream);
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->tev[2], x->stream));
     x->tev_valid = true;

@@ -157,6 +157,10 @@ struct TraceParams {
     const uint32_t* order = nullptr;
 };
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s);
+// Closest hit of many rays by persistent warps that refill finished lanes from
+// a ray counter (next_ray: one device word, reset here); binary nodes, no
+// seeding, rays in caller order or p.order.
+void launch_trace_pool(const TraceParams& p, uint32_t flags, uint32_t* next_ray, cudaStream_t s);
 
 // Shading (getColor + imageStore) inputs; the BVH, leaf records and error
 // word come from the TraceParams it runs with.

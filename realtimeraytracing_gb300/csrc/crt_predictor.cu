@@ -546,18 +546,65 @@ __global__ void __launch_bounds__(128) tc_wait_probe_kernel(int complete, uint32
 }
 
 // ------------------------------------------------------------ optimiser
-__global__ void adam_kernel(PredictorDev P, float* grad, float scale, float lr, float b1t, float b2t) {
+// The fp16 copy (and, for the weight matrices, the transposed copy) of
+// master parameter i, as the forward and backward kernels read them.
+__device__ __forceinline__ void store_fp16(const PredictorDev& P, size_t i, __half h) {
+    if (i < oB1) {                       // W1 [64][32]
+        P.w16[hW1 + i] = h;
+        P.w16[hW1T + (i % 32) * 64 + i / 32] = h;
+    } else if (i >= oW2 && i < oB2) {    // W2 [64][64]
+        const size_t k = i - oW2;
+        P.w16[hW2 + k] = h;
+        P.w16[hW2T + (k % 64) * 64 + k / 64] = h;
+    } else if (i >= oW3 && i < oB3) {    // W3 [128][64]
+        const size_t k = i - oW3;
+        P.w16[hW3 + k] = h;
+        P.w16[hW3T + (k % 64) * 128 + k / 64] = h;
+    }
+}
+
+// Adam on every parameter, then its fp16 copies, four parameters per thread
+// (the parameter blocks all start at multiples of 4, so no group straddles
+// two): one pass over the FP32 state instead of an update pass and a
+// conversion pass.  Adam (Kingma & Ba 2015) with b1 = 0.9, b2 = 0.999,
+// eps = 1e-8 and bias corrections b1t = 1 - b1^t, b2t = 1 - b2^t; the
+// gradient is scaled by 1 / batch and cleared for the next step.
+__global__ void __launch_bounds__(256) adam_fp16_kernel(PredictorDev P, float scale, float lr, float b1t, float b2t) {
+    static_assert(kParams % 4 == 0 && oB1 % 4 == 0 && oW2 % 4 == 0 && oB2 % 4 == 0 && oW3 % 4 == 0 &&
+                  oB3 % 4 == 0 && oEo % 4 == 0 && oEd % 4 == 0, "parameter blocks on float4 boundaries");
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < kParams;
-         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-        const float g = grad[i] * scale;
-        grad[i] = 0.f;
-        const float m = b1 * P.m[i] + (1.f - b1) * g;
-        const float v = b2 * P.v[i] + (1.f - b2) * g * g;
-        P.m[i] = m;
-        P.v[i] = v;
-        const float w = P.master[i] - lr * (m / b1t) / (sqrtf(v / b2t) + eps);
-        P.master[i] = w;
+    float4* g4 = reinterpret_cast<float4*>(P.grad);
+    float4* m4 = reinterpret_cast<float4*>(P.m);
+    float4* v4 = reinterpret_cast<float4*>(P.v);
+    float4* w4 = reinterpret_cast<float4*>(P.master);
+    for (size_t q = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; q < kParams / 4;
+         q += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        float g[4], m[4], v[4], w[4];
+        *reinterpret_cast<float4*>(g) = g4[q];
+        *reinterpret_cast<float4*>(m) = m4[q];
+        *reinterpret_cast<float4*>(v) = v4[q];
+        *reinterpret_cast<float4*>(w) = w4[q];
+        g4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __half h[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float gk = g[k] * scale;
+            m[k] = b1 * m[k] + (1.f - b1) * gk;
+            v[k] = b2 * v[k] + (1.f - b2) * gk * gk;
+            w[k] = w[k] - lr * (m[k] / b1t) / (sqrtf(v[k] / b2t) + eps);
+            h[k] = __float2half_rn(w[k]);
+        }
+        m4[q] = *reinterpret_cast<float4*>(m);
+        v4[q] = *reinterpret_cast<float4*>(v);
+        w4[q] = *reinterpret_cast<float4*>(w);
+        const size_t i = 4 * q;
+        if (i >= oEo) {                  // embeddings: one 8-byte store of four halves
+            __half* dst = P.w16 + (i < oEd ? hEo + (i - oEo) : hEd + (i - oEd));
+            *reinterpret_cast<uint2*>(dst) = *reinterpret_cast<const uint2*>(h);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) store_fp16(P, i + k, h[k]);
+        }
     }
 }
 
@@ -871,8 +918,7 @@ cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, co
 void pred_adam(const PredictorDev& P, float scale, float lr, uint32_t step, cudaStream_t s) {
     const float b1t = 1.f - std::pow(0.9f, static_cast<float>(step));
     const float b2t = 1.f - std::pow(0.999f, static_cast<float>(step));
-    pred::adam_kernel<<<kNumSms * 8, 256, 0, s>>>(P, P.grad, scale, lr, b1t, b2t);
-    pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
+    pred::adam_fp16_kernel<<<kNumSms * 8, 256, 0, s>>>(P, scale, lr, b1t, b2t);
 }
 
 void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s) {

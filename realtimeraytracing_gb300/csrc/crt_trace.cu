@@ -21,6 +21,186 @@ __global__ void __launch_bounds__(BLOCK) trace_kernel(TraceParams p) {
     trace_ray<ANY, WT, STACK, SEED, WALK>(p, i);
 }
 
+// ------------------------------------------------ persistent ray pool
+// Closest-hit traversal of many incoherent rays.  One ray per lane, walked
+// exactly as trace_one's binary walk (children box-tested at their parent,
+// leaves tested at once, nearer child entered, pruning by the best hit's
+// bound), but the warps are persistent: after every BURST node visits the
+// lanes whose ray has finished take the next rays from a global counter (one
+// atomic per warp), so a warp no longer runs as long as its slowest ray
+// while most of its lanes idle.  Rays are taken in caller order, or in
+// p.order.  The hits are those of trace_kernel: a ray's closest hit (and its
+// tie rule) does not depend on the order its nodes are visited in.
+template <bool WT, int STACK>
+struct PoolRay {
+    RayCtx r;
+    WRay w;
+    float tmin, tmax, bt, bu, bv, bound;
+    uint32_t bkey, btri, cur;
+    int sp;
+    bool have;
+
+    __device__ __forceinline__ void test_leaf(const TraceParams& p, uint32_t L, uint32_t n_leaves, uint32_t& tested,
+                                              bool& corrupt) {
+        if (L >= n_leaves) { corrupt = true; return; }
+        ++tested;
+        const float4* t = p.xtri + 3 * static_cast<size_t>(L);
+        const float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
+        const float3 A = make_float3(a.x, a.y, a.z), B = make_float3(b.x, b.y, b.z), C = make_float3(c.x, c.y, c.z);
+        const HitRes h = WT ? tri_watertight(r.o, tmin, tmax, w, A, B, C) : tri_reference(r.o, r.d, tmin, tmax, A, B, C);
+        if (!h.did) return;
+        const uint32_t tri = __float_as_uint(a.w);
+        const uint32_t key = WT ? tri : ~L;
+        if (!have || h.t < bt || (h.t == bt && key < bkey)) {
+            have = true; bt = h.t; bu = h.u; bv = h.v; bkey = key; btri = tri;
+            bound = prune_bound(bt, p.abs_eps);
+        }
+    }
+
+    // Sets up ray (r0, r1) and enters the root; false when the ray is already finished.
+    __device__ __forceinline__ bool start(const TraceParams& p, float4 r0, float4 r1, uint32_t n_leaves,
+                                          uint32_t& tested, bool& corrupt) {
+        r.o = make_float3(r0.x, r0.y, r0.z);
+        r.d = make_float3(r1.x, r1.y, r1.z);
+        tmin = r0.w;
+        tmax = r1.w;
+        have = false;
+        bt = tmax; bu = 0.f; bv = 0.f;
+        bkey = 0xFFFFFFFFu; btri = CRT_MISS;
+        sp = 0;
+        cur = 0xFFFFFFFFu;
+        if (!(tmin <= tmax) || p.n_nodes == 0) return false;
+        r.inv = make_float3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+        r.oi = make_float3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
+        r.exact = !(isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && r.inv.x != 0.f && r.inv.y != 0.f &&
+                    r.inv.z != 0.f);
+        if (WT) w = wt_setup(r.d);
+        bound = prune_bound(bt, p.abs_eps);
+        const float4* n4 = reinterpret_cast<const float4*>(p.nodes);
+        const uint4 lr = __ldg(reinterpret_cast<const uint4*>(n4 + 2));
+        float te;
+        if (!slab<WT>(r, __ldg(n4), __ldg(n4 + 1), WT ? p.abs_eps : 0.f, te) || te > bound) return false;
+        if (lr.y == 0u && lr.z == 0u) {  // a one-leaf tree
+            test_leaf(p, 0u, n_leaves, tested, corrupt);
+            return false;
+        }
+        cur = 0u;
+        return true;
+    }
+
+    // One node visit; false when the walk has finished.
+    __device__ __forceinline__ bool step(const TraceParams& p, float* st_t, uint32_t* st_node, uint32_t n_leaves,
+                                         uint32_t& fetched, uint32_t& tested, bool& corrupt, bool& overflow) {
+        if (cur >= n_leaves - 1) { corrupt = true; return false; }
+        ++fetched;
+        const float4* nd = p.wide + 4 * static_cast<size_t>(cur);
+        const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
+        const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
+        float t0, t1;
+        bool h0, h1;
+        if (WT) {
+            h0 = slab_wt(r, w0, w1, t0);
+            h1 = slab_wt(r, w2, w3, t1);
+        } else {
+            h0 = slab<false>(r, w0, w1, 0.f, t0);
+            h1 = slab<false>(r, w2, w3, 0.f, t1);
+        }
+        const float bnd = bound;
+        h0 = h0 && t0 <= bnd;
+        h1 = h1 && t1 <= bnd;
+        if (h0 && (ref0 & kLeafRef)) { test_leaf(p, ref0 & ~kLeafRef, n_leaves, tested, corrupt); h0 = false; }
+        if (h1 && (ref1 & kLeafRef)) { test_leaf(p, ref1 & ~kLeafRef, n_leaves, tested, corrupt); h1 = false; }
+        if (h0 || h1) {
+            const float bnd2 = bound;
+            h0 = h0 && t0 <= bnd2;
+            h1 = h1 && t1 <= bnd2;
+        }
+        if (h0 && h1) {
+            const bool near1 = t1 < t0;
+            if (sp < STACK) {
+                st_node[sp] = near1 ? ref0 : ref1;
+                st_t[sp] = near1 ? t0 : t1;
+                ++sp;
+            } else {
+                overflow = true;
+            }
+            cur = near1 ? ref1 : ref0;
+            return true;
+        }
+        if (h0) { cur = ref0; return true; }
+        if (h1) { cur = ref1; return true; }
+        const float bnd3 = bound;
+        while (sp > 0) {
+            --sp;
+            if (st_t[sp] <= bnd3) { cur = st_node[sp]; return true; }
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ uint4 hit() const {
+        return have ? make_uint4(btri, __float_as_uint(bt), __float_as_uint(bu), __float_as_uint(bv))
+                    : make_uint4(CRT_MISS, 0u, 0u, 0u);
+    }
+};
+
+template <bool WT, int STACK, int BLOCK, int BURST>
+__global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32_t* __restrict__ next_ray) {
+    constexpr uint32_t kIdle = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
+    const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
+    const uint32_t n_leaves = (p.n_nodes + 1) / 2;
+    PoolRay<WT, STACK> ray;
+    uint32_t st_node[STACK];
+    float st_t[STACK];
+    uint32_t i = kIdle, fetched = 0, tested = 0;
+    bool corrupt = false, overflow = false;
+    while (true) {
+        const bool idle = (i == kIdle);
+        const uint32_t need = __ballot_sync(0xFFFFFFFFu, idle);
+        if (need) {
+            uint32_t base = 0;
+            const int leader = __ffs(need) - 1;
+            if (lane == static_cast<uint32_t>(leader)) base = atomicAdd(next_ray, static_cast<uint32_t>(__popc(need)));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (idle) {
+                const uint32_t k = base + static_cast<uint32_t>(__popc(need & lt_mask));
+                if (k >= p.n_rays) {
+                    i = kDone;
+                } else {
+                    i = p.order ? __ldg(p.order + k) : k;
+                    if (i >= p.n_rays) {
+                        raise_corrupt(p.err, 7, k, i);
+                        i = kDone;
+                    } else {
+                        const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
+                        const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
+                        if (!ray.start(p, r0, r1, n_leaves, tested, corrupt)) {
+                            reinterpret_cast<uint4*>(p.hits)[i] = ray.hit();
+                            i = kIdle;
+                        }
+                    }
+                }
+            }
+        }
+        if (__all_sync(0xFFFFFFFFu, i == kDone)) break;
+        if (i < kDone) {
+            bool walking = true;
+#pragma unroll 1
+            for (int s = 0; s < BURST && walking; ++s)
+                walking = ray.step(p, st_t, st_node, n_leaves, fetched, tested, corrupt, overflow);
+            if (!walking) {
+                reinterpret_cast<uint4*>(p.hits)[i] = ray.hit();
+                i = kIdle;
+            }
+        }
+    }
+    if (corrupt) raise_corrupt(p.err, 5, blockIdx.x, threadIdx.x);
+    else if (overflow) raise_error(p.err, kDevStackOverflow);
+    if (p.stats) {
+        atomicAdd(p.stats + 0, static_cast<unsigned long long>(fetched));
+        atomicAdd(p.stats + 1, static_cast<unsigned long long>(tested));
+    }
+}
+
 // Many scenes in one launch: ray i belongs to the scene whose ray range holds
 // it and is traced against that scene's BVH (same walk as above).
 template <bool ANY, bool WT, int STACK, int BLOCK>
@@ -184,6 +364,34 @@ static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed
     if (block == 256) launch_trace_b<ANY, WT, 256>(p, deep, seed, walk, s);
     else if (block == 64) launch_trace_b<ANY, WT, 64>(p, deep, seed, walk, s);
     else launch_trace_b<ANY, WT, 128>(p, deep, seed, walk, s);
+}
+
+template <bool WT, int STACK>
+static void launch_pool_s(const TraceParams& p, uint32_t* next_ray, cudaStream_t s) {
+    constexpr int kBlock = 128, kBurst = 8;
+    static int grid = 0;
+    if (grid == 0) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_pool_kernel<WT, STACK, kBlock, kBurst>, kBlock, 0);
+        grid = kNumSms * (per_sm > 0 ? per_sm : 1);
+    }
+    cudaMemsetAsync(next_ray, 0, 4, s);
+    const uint32_t want = (p.n_rays + kBlock - 1) / kBlock;
+    trace_pool_kernel<WT, STACK, kBlock, kBurst>
+        <<<want < static_cast<uint32_t>(grid) ? want : static_cast<uint32_t>(grid), kBlock, 0, s>>>(p, next_ray);
+}
+
+void launch_trace_pool(const TraceParams& p, uint32_t flags, uint32_t* next_ray, cudaStream_t s) {
+    const bool wt = flags & CRT_TRI_WATERTIGHT;
+    const bool deep = (flags >> 16) != 0;
+    if (p.n_rays == 0) return;
+    if (wt) {
+        if (deep) launch_pool_s<true, 1024>(p, next_ray, s);
+        else launch_pool_s<true, 64>(p, next_ray, s);
+    } else {
+        if (deep) launch_pool_s<false, 1024>(p, next_ray, s);
+        else launch_pool_s<false, 64>(p, next_ray, s);
+    }
 }
 
 void launch_trace(const TraceParams& p, uint32_t flags, int block, cudaStream_t s) {

@@ -187,3 +187,28 @@ def test_mma_wait_times_out_frees_tensor_memory_and_the_context_stays_usable(ctx
     assert np.array_equal(seeded.view(np.uint32), hits.view(np.uint32))
     pred.free()
     bvh.free()
+
+
+def test_adam_step_matches_numpy(ctx):
+    """One training step over a single batch equals Adam (b1 0.9, b2 0.999,
+    eps 1e-8, bias-corrected) applied in numpy to the mean of the kernels'
+    own gradients (crt_predictor_gradients), for every parameter."""
+    tris = S.clustered_soup(50_000, 16, 0.03, 0.004, 0.5, seed=93)
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    rays = S.sphere_rays(4096, seed=94)
+    hits = ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)
+    pred = crt.Predictor(ctx, bvh, seed=7, lr=1e-3, train_stride=1, batch=4096)
+    p0 = pred.params()
+    targets = pred.classes_of_hits(hits)
+    grad, _ = pred.gradients(rays, targets)
+    pred.train(rays, hits, offset=0)
+    p1 = pred.params()
+    g = grad.astype(np.float64) / 4096.0
+    m = 0.1 * g
+    v = 0.001 * g * g
+    want = p0 - 1e-3 * (m / 0.1) / (np.sqrt(v / 0.001) + 1e-8)
+    np.testing.assert_allclose(p1, want, rtol=2e-5, atol=2e-7)
+    assert np.abs(p1 - p0).max() > 1e-4  # the step moved the weights
+    pred.free()
+    bvh.free()

@@ -251,3 +251,31 @@ def test_trace_from_page_locked_host_rays(ctx, config0, flags):
     pinned_hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, pin_memory=True)
     ctx.trace(bvh, pinned_rays, flags, out=pinned_hits)
     _cmp_hits(pinned_hits.numpy(), ref, any_hit=bool(flags & crt.TRACE_ANY))
+
+
+@pytest.mark.parametrize("flags", [crt.TRI_WATERTIGHT, crt.TRI_REFERENCE])
+def test_persistent_warps_equal_one_thread_per_ray(ctx, flags):
+    """Large closest-hit batches run on persistent warps that refill finished
+    lanes; CRT_TRACE_PER_RAY_THREADS keeps one thread per ray.  Same hits bit
+    for bit, and the same node fetches and triangle tests (every ray walks the
+    same nodes either way), on incoherent rays: rays between sphere points
+    and cube points, and bounce rays from their hits, in caller order and
+    in sorted order."""
+    tris = S.clustered_soup(200_000, 64, 0.03, 0.004, 0.5, seed=95)
+    if flags == crt.TRI_REFERENCE:   # large triangles, so that the shader's predicate finds hits
+        tris[:, [0, 1, 2, 4, 5, 6, 8, 9, 10]] = (tris[:, [0, 1, 2, 4, 5, 6, 8, 9, 10]] - 0.5) * 8.0 + 0.5
+    models = S.identity_models(1)
+    bvh = ctx.build(tris, models=models)
+    rays = S.sphere_rays(150_000, seed=96)
+    prim = ctx.trace(bvh, rays, flags)
+    bounce = S.bounce_rays(rays, prim, tris, 120_000, seed=3)
+    for rs in (rays, bounce):
+        for order in (0, crt.SORT_RAYS):
+            a = ctx.trace(bvh, rs, flags | order | crt.TRACE_STATS)
+            sa = ctx.last_trace_stats()
+            b = ctx.trace(bvh, rs, flags | order | crt.PER_RAY_THREADS | crt.TRACE_STATS)
+            sb = ctx.last_trace_stats()
+            np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+            assert sa == sb
+            assert (a[:, 0].view(np.uint32) != crt.MISS).sum() > 1000
+    bvh.free()
