@@ -391,7 +391,7 @@ static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed
 #define CRT_POOL_BLOCK 128
 #endif
 #ifndef CRT_POOL_BURST
-#define CRT_POOL_BURST 8
+#define CRT_POOL_BURST 16
 #endif
 #ifndef CRT_POOL_CHUNK
 #define CRT_POOL_CHUNK 0
