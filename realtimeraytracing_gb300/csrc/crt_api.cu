@@ -622,11 +622,13 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
     if (N == 1) {
         crt::launch_single_leaf(x->node_box.as<float4>(), b->nodes.as<crt_bvh_node>(), leaves, s);
     } else if (!laid_out) {
+        uint32_t* dfs = x->clus_a.as<uint32_t>();  // the cluster buffers are free after PLOC
         for (int k = static_cast<int>(iters) - 1; k >= 0; --k)
-            crt::launch_layout_nodes(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(),
-                                     x->it_host[k].y, x->it_host[k + 1].y, N, b->nodes.as<crt_bvh_node>(),
-                                     b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves,
-                                     st, err, s);
+            crt::launch_layout_level(x->node_kids.as<uint4>(), x->pos.as<uint2>(),
+                                     x->it_host[k].y, x->it_host[k + 1].y, N, dfs, err, s);
+        crt::launch_layout_emit(x->node_box.as<float4>(), x->node_kids.as<uint4>(), x->pos.as<uint2>(), N, dfs,
+                                b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(), b->wide_wt.as<float4>(),
+                                b->depth_odd.as<uint8_t>(), leaves, st, err, s);
     }
     CRT_CUDA(cudaGetLastError());
     CRT_CUDA(cudaEventRecord(x->ev[4], s));
@@ -1108,11 +1110,12 @@ crt_status crt_optimize(crt_ctx* x, crt_bvh* b, uint32_t passes) {
     crt::SceneState* st = reinterpret_cast<crt::SceneState*>(base + o_st);
     CRT_CUDA(cudaMemcpyAsync(st, &hst, sizeof(hst), cudaMemcpyHostToDevice, s));
     uint2* pf = reinterpret_cast<uint2*>(base + o_pf);
-    crt::LeafOut leaves{xtri_old, b->xtri.as<float4>(), b->inv_perm.as<uint32_t>()};
+    uint32_t* dfs = reinterpret_cast<uint32_t*>(base + o_dfs);
     for (uint32_t h = H; h >= 1; --h)
-        crt::launch_layout_nodes(box2, kids2, pf, N + h_off[h], N + h_off[h + 1], N, b->nodes.as<crt_bvh_node>(),
-                                 b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves,
-                                 st, err, s);
+        crt::launch_layout_level(kids2, pf, N + h_off[h], N + h_off[h + 1], N, dfs, err, s);
+    crt::LeafOut leaves{xtri_old, b->xtri.as<float4>(), b->inv_perm.as<uint32_t>()};
+    crt::launch_layout_emit(box2, kids2, pf, N, dfs, b->nodes.as<crt_bvh_node>(), b->wide.as<float4>(),
+                            b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves, st, err, s);
     CRT_CUDA(cudaGetLastError());
     b->wide4_ready = false;
     b->cwide_ready = false;

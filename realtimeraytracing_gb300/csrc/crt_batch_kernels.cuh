@@ -350,9 +350,10 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
         }
         if (!grid_barrier(bar, err, spin_limit)) return;
     }
-    // DFS layout: step r lays out level (iters - 1 - r) of every scene that has
-    // it (layout_node writes every output record of a node, so no pass over
-    // the positions follows).
+    // DFS layout: step r handles level (iters - 1 - r) of every scene that has
+    // it, recording node ids by DFS position in dfs (the first cluster buffer,
+    // free now); then every position is emitted in order.
+    uint32_t* dfs = reinterpret_cast<uint32_t*>(ca);
     uint32_t max_it = 0;
     for (uint32_t k = 0; k < n_scenes; ++k) max_it = max(max_it, __ldcg(&scenes[k].iters));
     for (uint32_t r = 0; r < max_it; ++r) {
@@ -379,16 +380,38 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
                 if (s_tile_pre[mid] <= q) lo = mid; else hi = mid - 1;
             }
             const BatchScene B = scenes[lo];
-            const uint32_t level = B.iters - 1 - r;
-            const uint32_t X = __ldcg(it + B.it_off + level).y + (q - s_tile_pre[lo]);
-            const LeafOut slv{lv.xtri_sorted + 3 * static_cast<size_t>(B.tri_off),
-                              lv.xtri + 3 * static_cast<size_t>(B.tri_off), lv.leaf_of_tri + B.tri_off};
-            layout_node(X, node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off, pf + B.tri_off,
-                        B.n_tris, nodes + B.node_off, wide + 4 * static_cast<size_t>(B.wide_off),
-                        wide_wt + 4 * static_cast<size_t>(B.wide_off), depth_odd + B.wide_off, slv, B.abs_eps, err);
+            const uint32_t lv = B.iters - 1 - r;
+            const uint32_t X = __ldcg(it + B.it_off + lv).y + (q - s_tile_pre[lo]);
+            layout_down(X, node_kids + B.tri_off, pf + B.tri_off, B.n_tris,
+                        dfs + B.node_off, err);
         }
-        if (r + 1 < max_it)
-            if (!grid_barrier(bar, err, spin_limit)) return;
+        if (!grid_barrier(bar, err, spin_limit)) return;
+    }
+    // every DFS position of every scene with more than one triangle, in order
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t k = 0; k < n_scenes; ++k) {
+            s_tile_pre[k] = run;
+            if (scenes[k].n_tris > 1) run += 2 * scenes[k].n_tris - 1;
+        }
+        s_tile_pre[n_scenes] = run;
+    }
+    __syncthreads();
+    const uint32_t total_slots = s_tile_pre[n_scenes];
+    for (uint32_t q = blockIdx.x * BLOCK + threadIdx.x; q < total_slots; q += gridDim.x * BLOCK) {
+        uint32_t lo = 0, hi = n_scenes - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (s_tile_pre[mid] <= q) lo = mid; else hi = mid - 1;
+        }
+        const BatchScene B = scenes[lo];
+        const LeafOut slv{lv.xtri_sorted + 3 * static_cast<size_t>(B.tri_off), lv.xtri + 3 * static_cast<size_t>(B.tri_off),
+                          lv.leaf_of_tri + B.tri_off};
+        layout_emit(q - s_tile_pre[lo], node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off,
+                    pf + B.tri_off, B.n_tris, dfs + B.node_off, nodes + B.node_off,
+                    wide + 4 * static_cast<size_t>(B.wide_off), wide_wt + 4 * static_cast<size_t>(B.wide_off),
+                    depth_odd + B.wide_off, slv, B.abs_eps, err);
     }
 }
 

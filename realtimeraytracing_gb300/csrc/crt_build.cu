@@ -828,88 +828,6 @@ __device__ __forceinline__ void layout_emit(uint32_t p, const float4* __restrict
     g[3] = make_float4(cmx[1].x + grow, cmx[1].y + grow, cmx[1].z + grow, __uint_as_float(lcb));
 }
 
-// The whole layout of internal node X in one step of the top-down pass, with
-// no emit pass after it: X knows its DFS position p, first leaf f and depth
-// parity from pf (written by its parent); it writes the tail of its own
-// reference record (tri 0, children's positions), both children's boxes into
-// their records (a leaf child also gets its triangle id there, and its
-// transformed triangle moved into tree order), its two 64-byte traversal
-// nodes, and its internal children's (position, first leaf, parity).  The
-// root writes its own box too.  Every record byte is written once.
-__device__ __forceinline__ void layout_node(uint32_t X, const float4* __restrict__ node_box,
-                                            const uint4* __restrict__ node_kids, uint2* __restrict__ pf, uint32_t N,
-                                            crt_bvh_node* __restrict__ out, float4* __restrict__ wide,
-                                            float4* __restrict__ wide_wt, uint8_t* __restrict__ depth_odd,
-                                            const LeafOut& lv, float grow, uint32_t* err) {
-    const uint2 me = layout_place(X, pf, N);
-    const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
-    const uint4 kids = __ldcg(node_kids + (X - N));  // left id, right id, their leaf counts
-    const uint32_t a = kids.x, b = kids.y, lca = kids.z, lcb = kids.w;
-    const uint32_t pl = p + 1, pr = p + 2 * lca;
-    if (pr >= 2 * N - 1 || p < f || p - f >= N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
-        raise_corrupt(err, 4, X, pr);
-        return;
-    }
-    if (X == 2 * N - 2) {  // the root's own box
-        const float4 rmn = __ldcg(node_box + 2 * static_cast<size_t>(X)), rmx = __ldcg(node_box + 2 * static_cast<size_t>(X) + 1);
-        float4* o = reinterpret_cast<float4*>(out);
-        o[0] = make_float4(rmn.x, rmn.y, rmn.z, 0.f);
-        o[1] = make_float4(rmx.x, rmx.y, rmx.z, 0.f);
-    }
-    reinterpret_cast<uint4*>(out + p)[2] = make_uint4(0u, pl, pr, 0u);
-    const uint32_t nodd = (odd ^ 1u) << 31;
-    const uint32_t ch[2] = {a, b}, cp[2] = {pl, pr}, cf[2] = {f, f + lca};
-    float4 cmn[2], cmx[2];
-    uint32_t cref[2];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-        cmn[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]));
-        cmx[c] = __ldcg(node_box + 2 * static_cast<size_t>(ch[c]) + 1);
-        float4* o = reinterpret_cast<float4*>(out + cp[c]);
-        o[0] = make_float4(cmn[c].x, cmn[c].y, cmn[c].z, 0.f);
-        o[1] = make_float4(cmx[c].x, cmx[c].y, cmx[c].z, 0.f);
-        if (ch[c] < N) {  // leaf: its triangle, its place in tree order
-            reinterpret_cast<uint4*>(o)[2] = make_uint4(__float_as_uint(cmn[c].w), 0u, 0u, 0u);
-            cref[c] = kLeafRef | cf[c];
-            if (cf[c] >= N) { raise_corrupt(err, 6, p, cf[c]); continue; }
-            const float4* src = lv.xtri_sorted + 3 * static_cast<size_t>(ch[c]);
-            float4* dst = lv.xtri + 3 * static_cast<size_t>(cf[c]);
-            const float4 t0 = __ldcg(src), t1 = __ldcg(src + 1), t2 = __ldcg(src + 2);
-            dst[0] = t0;
-            dst[1] = t1;
-            dst[2] = t2;
-            const uint32_t ti = __float_as_uint(t0.w);
-            if (ti < N) lv.leaf_of_tri[ti] = cf[c];
-            else raise_corrupt(err, 6, p, ti);
-        } else {          // internal: its rank among internal nodes in DFS order
-            cref[c] = cp[c] - cf[c];
-            pf[ch[c] - N] = make_uint2(cp[c], cf[c] | nodd);
-        }
-    }
-    if (depth_odd) depth_odd[p - f] = static_cast<uint8_t>(odd);
-    float4* w = wide + 4 * static_cast<size_t>(p - f);
-    w[0] = make_float4(cmn[0].x, cmn[0].y, cmn[0].z, __uint_as_float(cref[0]));
-    w[1] = make_float4(cmx[0].x, cmx[0].y, cmx[0].z, __uint_as_float(cref[1]));
-    w[2] = make_float4(cmn[1].x, cmn[1].y, cmn[1].z, __uint_as_float(lca));  // leaf counts of the children
-    w[3] = make_float4(cmx[1].x, cmx[1].y, cmx[1].z, __uint_as_float(lcb));
-    float4* g = wide_wt + 4 * static_cast<size_t>(p - f);
-    g[0] = make_float4(cmn[0].x - grow, cmn[0].y - grow, cmn[0].z - grow, __uint_as_float(cref[0]));
-    g[1] = make_float4(cmx[0].x + grow, cmx[0].y + grow, cmx[0].z + grow, __uint_as_float(cref[1]));
-    g[2] = make_float4(cmn[1].x - grow, cmn[1].y - grow, cmn[1].z - grow, __uint_as_float(lca));
-    g[3] = make_float4(cmx[1].x + grow, cmx[1].y + grow, cmx[1].z + grow, __uint_as_float(lcb));
-}
-
-__global__ void __launch_bounds__(256) layout_nodes_kernel(const float4* __restrict__ node_box,
-                                                           const uint4* __restrict__ node_kids, uint2* __restrict__ pf,
-                                                           uint32_t id_begin, uint32_t id_end, uint32_t N,
-                                                           crt_bvh_node* __restrict__ out, float4* __restrict__ wide,
-                                                           float4* __restrict__ wide_wt, uint8_t* __restrict__ depth_odd,
-                                                           LeafOut lv, const SceneState* __restrict__ st, uint32_t* err) {
-    const uint32_t X = id_begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (X >= id_end) return;
-    layout_node(X, node_box, node_kids, pf, N, out, wide, wide_wt, depth_odd, lv, st->abs_eps, err);
-}
-
 __global__ void __launch_bounds__(256) layout_level_kernel(const uint4* __restrict__ node_kids,
                                                            uint2* __restrict__ pf, uint32_t id_begin, uint32_t id_end,
                                                            uint32_t N, uint32_t* __restrict__ dfs, uint32_t* err) {
@@ -930,9 +848,61 @@ __global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restri
     layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, st->abs_eps, err);
 }
 
-#ifndef CRT_LAYOUT_MERGED
-#define CRT_LAYOUT_MERGED 1
-#endif
+// (DFS position, first leaf | depth parity << 31) of the M internal nodes
+// T0 .. T0 + M - 1 that form the top of the tree (the root, 2N - 2, among
+// them; every parent of one of them is one of them), written to pf, by one
+// block: each node gets its parent and its offset from it (left child: +1
+// position; right child: +2 leaves(left) positions, +leaves(left) first
+// leaf; one level deeper), and `levels` (the top part's height) bounds the
+// log2 rounds of pointer jumping that sum the offsets up to the root.
+// scratch: 6 M words.
+template <int BLOCK>
+__device__ void top_positions(const uint4* __restrict__ node_kids, uint32_t N, uint32_t T0, uint32_t M, uint32_t levels,
+                              uint32_t* scratch, uint2* __restrict__ pf, uint32_t* err) {
+    constexpr uint32_t kNone = 0xFFFFFFFFu, kOdd = 0x80000000u, kLow = 0x7FFFFFFFu;
+    uint32_t* par[2] = {scratch, scratch + M};
+    uint2* off[2] = {reinterpret_cast<uint2*>(scratch + 2 * M), reinterpret_cast<uint2*>(scratch + 4 * M)};
+    for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
+        par[0][j] = kNone;
+        off[0][j] = make_uint2(0u, 0u);
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
+        const uint4 kids = __ldcg(node_kids + (T0 + j - N));
+        if (kids.x >= T0 && kids.x - T0 < M) {
+            par[0][kids.x - T0] = j;
+            off[0][kids.x - T0] = make_uint2(1u, kOdd);
+        }
+        if (kids.y >= T0 && kids.y - T0 < M) {
+            par[0][kids.y - T0] = j;
+            off[0][kids.y - T0] = make_uint2(2u * kids.z, kids.z | kOdd);
+        }
+    }
+    __syncthreads();
+    int cur = 0;
+    for (uint32_t reach = 1; reach <= levels; reach <<= 1) {  // after the round, every node skips 2 x reach levels
+        for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
+            const uint32_t q = par[cur][j];
+            uint2 o = off[cur][j];
+            uint32_t pq = kNone;
+            if (q != kNone) {
+                const uint2 oq = off[cur][q];
+                o = make_uint2(o.x + oq.x, ((o.y & kLow) + (oq.y & kLow)) | ((o.y ^ oq.y) & kOdd));
+                pq = par[cur][q];
+            }
+            par[cur ^ 1][j] = pq;
+            off[cur ^ 1][j] = o;
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
+        const uint32_t X = T0 + j;
+        if (par[cur][j] != kNone) { raise_corrupt(err, 8, X, par[cur][j]); continue; }
+        if (X != 2 * N - 2) pf[X - N] = off[cur][j];
+    }
+    __syncthreads();
+}
 
 // ================================== K3+K4 fused: one persistent launch
 // All PLOC iterations, then all layout levels, separated by a grid-wide
@@ -1027,36 +997,33 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     // The top levels hold a few nodes each: block 0 lays them out alone, with
     // block barriers between levels, and one grid barrier ends that part.
     uint32_t* dfs = reinterpret_cast<uint32_t*>(ca);
-    const float grow = st->abs_eps;
-    // one node's layout: the merged pass (CRT_LAYOUT_MERGED) or the position pass of the two-pass layout
-    auto lay = [&](uint32_t X) {
-        if (CRT_LAYOUT_MERGED) layout_node(X, node_box, node_kids, pf, N, out, wide, wide_wt, depth_odd, lv, grow, err);
-        else layout_down(X, node_kids, pf, N, dfs, err);
-    };
     constexpr uint32_t kSmallLevel = 4 * BLOCK;
     int k = iter - 1;
     int k_small = k;
     while (k_small >= 0 && __ldcg(it + k_small + 1).y - __ldcg(it + k_small).y <= kSmallLevel) --k_small;
     if (k_small < k) {
+        // The top levels (created by the last PLOC iterations, few nodes each):
+        // block 0 finds every top node's (position, first leaf, parity) by
+        // pointer jumping instead of one dependent round per level, then runs
+        // the position pass over all of them at once.
         if (blockIdx.x == 0) {
-            for (int kk = k; kk > k_small; --kk) {
-                const uint32_t lo = __ldcg(it + kk).y, hi = __ldcg(it + kk + 1).y;
-                for (uint32_t X = lo + threadIdx.x; X < hi; X += BLOCK) lay(X);
-                __syncthreads();
-            }
+            const uint32_t T0 = __ldcg(it + k_small + 1).y, T1 = 2 * N - 1;
+            top_positions<BLOCK>(node_kids, N, T0, T1 - T0, static_cast<uint32_t>(k - k_small),
+                                 reinterpret_cast<uint32_t*>(cb), pf, err);
+            for (uint32_t X = T0 + threadIdx.x; X < T1; X += BLOCK) layout_down(X, node_kids, pf, N, dfs, err);
         }
         if (!grid_barrier(bar, err, spin_limit)) return;
         k = k_small;
     }
     for (; k >= 0; --k) {
         const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
-        for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK) lay(X);
-        if (!CRT_LAYOUT_MERGED || k > 0)
-            if (!grid_barrier(bar, err, spin_limit)) return;
+        for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
+            layout_down(X, node_kids, pf, N, dfs, err);
+        if (!grid_barrier(bar, err, spin_limit)) return;
     }
-    if (!CRT_LAYOUT_MERGED)
-        for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
-            layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, grow, err);
+    const float grow = st->abs_eps;
+    for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
+        layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, grow, err);
     __syncthreads();
     if (threadIdx.x == 0 && atomicAdd(iters_out + 1, 1u) + 1u == gridDim.x) stamp[2] = global_ns();
 }
@@ -1337,15 +1304,6 @@ void launch_layout_level(const uint4* node_kids, uint2* pf, uint32_t id_begin,
     if (id_end <= id_begin || id_end > 2 * N - 1) return;
     const uint32_t cnt = id_end - id_begin;
     layout_level_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_kids, pf, id_begin, id_end, N, dfs, err);
-}
-
-void launch_layout_nodes(const float4* node_box, const uint4* node_kids, uint2* pf, uint32_t id_begin, uint32_t id_end,
-                         uint32_t N, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                         const LeafOut& lv, const SceneState* st, uint32_t* err, cudaStream_t s) {
-    const uint32_t cnt = id_end - id_begin;
-    if (cnt == 0) return;
-    layout_nodes_kernel<<<(cnt + 255) / 256, 256, 0, s>>>(node_box, node_kids, pf, id_begin, id_end, N, out, wide,
-                                                          wide_wt, depth_odd, lv, st, err);
 }
 
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,

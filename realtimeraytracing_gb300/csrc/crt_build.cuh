@@ -89,11 +89,6 @@ struct LeafOut {
 // DFS layout as separate launches: one top-down level (nodes [id_begin,
 // id_end)) recording dfs[position] = node, then the emit pass over all
 // positions.
-// The merged layout of the internal nodes [id_begin, id_end) of one PLOC
-// level (their parents laid out before): every output record, no emit pass.
-void launch_layout_nodes(const float4* node_box, const uint4* node_kids, uint2* pf, uint32_t id_begin, uint32_t id_end,
-                         uint32_t N, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                         const LeafOut& lv, const SceneState* st, uint32_t* err, cudaStream_t s);
 void launch_layout_level(const uint4* node_kids, uint2* pf, uint32_t id_begin,
                          uint32_t id_end, uint32_t N, uint32_t* dfs, uint32_t* err, cudaStream_t s);
 void launch_layout_emit(const float4* node_box, const uint4* node_kids, const uint2* pf, uint32_t N,
