@@ -326,6 +326,8 @@ def run_ours(args):
     reps = max(3, min(args.steps, 10))
     t_plain = statistics.mean(run_steps(WT, reps, 2, out)[0])
     identical = identical and same(out)
+    t_per_ray = statistics.mean(run_steps(WT | crt.PER_RAY_THREADS, reps, 2, out)[0])
+    identical = identical and same(out)
     t_sorted = statistics.mean(run_steps(WT | crt.SORT_RAYS, reps, 2, out)[0])
     identical = identical and same(out)
     t_seeded = statistics.mean(run_steps(WT | crt.USE_PREDICTOR, reps, 2, out)[0])
@@ -358,14 +360,14 @@ def run_ours(args):
     hit = truth != 127
     hit_rate = float((pc[hit] == truth[hit]).mean()) if hit.any() else 0.0
 
-    # ---- the dominant kernel (trace_kernel in the learned step), timed by
-    # the library's CUDA events on its stream around that launch
+    # ---- the dominant kernel (trace_pool_kernel in the learned step), timed
+    # by the library's CUDA events on its stream around that launch
     k_ms = statistics.mean(k[1] for k in kern)
     order_ms = statistics.mean(k[0] for k in kern)
     alg_bytes = 64.0 * f_learned + 48.0 * tt_learned + (32.0 + 16.0 + 4.0) * n  # nodes, triangles, ray, hit, order
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-    traffic = read_profile_value("trace_kernel_bounce_config3.md", "traffic_bytes_per_launch")
+    traffic = read_profile_value("trace_pool_kernel_bounce_config3.md", "traffic_bytes_per_launch")
     l2_gbs = l2_copy_gbs(torch, dev, stream)
 
     # ---- end to end through the public API: host rays in, host hits out
@@ -427,6 +429,7 @@ def run_ours(args):
             "learned_vs_plain": {
                 "learned_mrays_s": round(value / world, 2), "plain_mrays_s": round(n / t_plain / 1e3, 2),
                 "speedup": round(t_plain / t_step, 3), "identical_hits": identical,
+                "plain_one_thread_per_ray_mrays_s": round(n / t_per_ray / 1e3, 2),
                 "no_network_sorted_mrays_s": round(n / t_sorted / 1e3, 2),
                 "no_network_speedup": round(t_plain / t_sorted, 3),
                 "learned_vs_no_network": round(t_sorted / t_step, 3),
@@ -442,7 +445,8 @@ def run_ours(args):
                 "modes": "learned = CRT_TRACE_PREDICTOR_ORDER (inference + order by predicted treelet, origin "
                          "cell, direction bin + trace); no network = CRT_TRACE_SORT_RAYS (order by origin cell and "
                          "direction bin + trace); seeded = CRT_TRACE_USE_PREDICTOR (t_max from an exact search of "
-                         "the predicted treelet)"},
+                         "the predicted treelet); plain and ordered modes trace on persistent warps that refill "
+                         "finished lanes, one_thread_per_ray = CRT_TRACE_PER_RAY_THREADS (the launch-per-ray kernel)"},
             "build_ms": round(build_ms, 4),
             "build_ms_wall": round(statistics.median(b[1] for b in builds), 4),
             "build_stages_ms": stages,
@@ -452,8 +456,9 @@ def run_ours(args):
                     "transfer": "crt_trace on page-locked host rays (copied in on the library stream) and host hits "
                                 "(written by the trace kernel over the CPU-GPU link), host-timed around the call"},
             "gpu_launches": 7 * args.steps,
-            "gpu_launches_note": "per step: infer_kernel, order_keys_kernel, 4 onesweep_kernel passes, trace_kernel",
-            "roofline": {"kernel": "trace_kernel (learned step: rays in predicted order, closest hit, watertight)",
+            "gpu_launches_note": "per step: infer_kernel, order_keys_kernel, 4 onesweep_kernel passes, trace_pool_kernel",
+            "roofline": {"kernel": "trace_pool_kernel (learned step: persistent warps over the rays in predicted "
+                                   "order, closest hit, watertight)",
                          "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                          "ms_per_launch": round(k_ms, 4), "alg_bytes_per_launch": int(alg_bytes),
