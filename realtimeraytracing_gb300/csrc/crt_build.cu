@@ -745,11 +745,17 @@ __global__ void __launch_bounds__(BLOCK) ploc_iteration_kernel(const float4* __r
 // transformed triangle into that order.  The traversal's tie rule (equal t:
 // the leaf later in DFS order, which the shader visits first) and every
 // subtree's leaves forming one contiguous range rest on this order.
+constexpr uint32_t kLayoutUnset = 0xFFFFFFFFu;  // a position not yet published (dataflow layout)
+
 __device__ __forceinline__ uint2 layout_place(uint32_t X, const uint2* __restrict__ pf, uint32_t N) {
     // (DFS position, first leaf below | depth parity << 31) of X; the root sits at (0, 0)
     return (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
 }
 
+// PUBLISH: each internal child's record is written second word first, then
+// its position with a release store, so that a thread waiting for it (the
+// dataflow layout below) sees the whole record once the position is there.
+template <bool PUBLISH = false>
 __device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict__ node_kids, uint2* __restrict__ pf, uint32_t N,
                                             uint32_t* __restrict__ dfs, uint32_t* err) {
     const uint2 me = layout_place(X, pf, N);
@@ -763,6 +769,21 @@ __device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict_
     }
     dfs[p] = X;
     const uint32_t nodd = (odd ^ 1u) << 31;
+    if (PUBLISH) {
+        if (a < N) {
+            dfs[pl] = a;
+        } else {
+            pf[a - N].y = f | nodd;
+            st_release_u32(&pf[a - N].x, pl);
+        }
+        if (b < N) {
+            dfs[pr] = b;
+        } else {
+            pf[b - N].y = (f + lca) | nodd;
+            st_release_u32(&pf[b - N].x, pr);
+        }
+        return;
+    }
     if (a < N) dfs[pl] = a; else pf[a - N] = make_uint2(pl, f | nodd);
     if (b < N) dfs[pr] = b; else pf[b - N] = make_uint2(pr, (f + lca) | nodd);
 }
@@ -848,62 +869,6 @@ __global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restri
     layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, st->abs_eps, err);
 }
 
-// (DFS position, first leaf | depth parity << 31) of the M internal nodes
-// T0 .. T0 + M - 1 that form the top of the tree (the root, 2N - 2, among
-// them; every parent of one of them is one of them), written to pf, by one
-// block: each node gets its parent and its offset from it (left child: +1
-// position; right child: +2 leaves(left) positions, +leaves(left) first
-// leaf; one level deeper), and `levels` (the top part's height) bounds the
-// log2 rounds of pointer jumping that sum the offsets up to the root.
-// scratch: 6 M words.
-template <int BLOCK>
-__device__ void top_positions(const uint4* __restrict__ node_kids, uint32_t N, uint32_t T0, uint32_t M, uint32_t levels,
-                              uint32_t* scratch, uint2* __restrict__ pf, uint32_t* err) {
-    constexpr uint32_t kNone = 0xFFFFFFFFu, kOdd = 0x80000000u, kLow = 0x7FFFFFFFu;
-    uint32_t* par[2] = {scratch, scratch + M};
-    uint2* off[2] = {reinterpret_cast<uint2*>(scratch + 2 * M), reinterpret_cast<uint2*>(scratch + 4 * M)};
-    for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
-        par[0][j] = kNone;
-        off[0][j] = make_uint2(0u, 0u);
-    }
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
-        const uint4 kids = __ldcg(node_kids + (T0 + j - N));
-        if (kids.x >= T0 && kids.x - T0 < M) {
-            par[0][kids.x - T0] = j;
-            off[0][kids.x - T0] = make_uint2(1u, kOdd);
-        }
-        if (kids.y >= T0 && kids.y - T0 < M) {
-            par[0][kids.y - T0] = j;
-            off[0][kids.y - T0] = make_uint2(2u * kids.z, kids.z | kOdd);
-        }
-    }
-    __syncthreads();
-    int cur = 0;
-    for (uint32_t reach = 1; reach <= levels; reach <<= 1) {  // after the round, every node skips 2 x reach levels
-        for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
-            const uint32_t q = par[cur][j];
-            uint2 o = off[cur][j];
-            uint32_t pq = kNone;
-            if (q != kNone) {
-                const uint2 oq = off[cur][q];
-                o = make_uint2(o.x + oq.x, ((o.y & kLow) + (oq.y & kLow)) | ((o.y ^ oq.y) & kOdd));
-                pq = par[cur][q];
-            }
-            par[cur ^ 1][j] = pq;
-            off[cur ^ 1][j] = o;
-        }
-        __syncthreads();
-        cur ^= 1;
-    }
-    for (uint32_t j = threadIdx.x; j < M; j += BLOCK) {
-        const uint32_t X = T0 + j;
-        if (par[cur][j] != kNone) { raise_corrupt(err, 8, X, par[cur][j]); continue; }
-        if (X != 2 * N - 2) pf[X - N] = off[cur][j];
-    }
-    __syncthreads();
-}
-
 // ================================== K3+K4 fused: one persistent launch
 // All PLOC iterations, then all layout levels, separated by a grid-wide
 // barrier (co-residency guaranteed by a cooperative launch; every wait is
@@ -943,6 +908,11 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     // stamps: start, end of the PLOC loop, end of the layout.
     unsigned long long* stamp = reinterpret_cast<unsigned long long*>(iters_out + 2);
     if (blockIdx.x == 0 && threadIdx.x == 0) stamp[0] = global_ns();
+    // The layout's records start unset: a node's position arrives from its
+    // parent (pf is not touched by the PLOC iterations, whose grid barriers
+    // order this reset before the layout).
+    for (uint32_t j = blockIdx.x * BLOCK + threadIdx.x; j + 1 < N; j += gridDim.x * BLOCK)
+        pf[j] = make_uint2(kLayoutUnset, 0u);
     int iter = 0;
     bool tail = false;
     for (;; ++iter) {
@@ -992,35 +962,31 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
         iters_out[0] = static_cast<uint32_t>(iter);
         stamp[1] = global_ns();
     }
-    // DFS layout: top-down levels, last iteration's nodes first, into dfs
-    // (the first cluster buffer, free now), then every position in order.
-    // The top levels hold a few nodes each: block 0 lays them out alone, with
-    // block barriers between levels, and one grid barrier ends that part.
+    // DFS layout, position pass as dataflow: internal node ids grow with the
+    // PLOC iteration that made them, so a parent's id is larger than its
+    // children's and decreasing ids are a top-down order.  Every thread takes
+    // the ids 2N-2, 2N-3, ... in grid-stride order and, before laying node X
+    // out, waits (bounded) until X's parent has published X's position.  The
+    // unfinished node with the largest id never waits (its parent is done), so
+    // the co-resident grid always progresses; one grid barrier before the
+    // emit pass replaces one barrier per PLOC level.
     uint32_t* dfs = reinterpret_cast<uint32_t*>(ca);
-    constexpr uint32_t kSmallLevel = 4 * BLOCK;
-    int k = iter - 1;
-    int k_small = k;
-    while (k_small >= 0 && __ldcg(it + k_small + 1).y - __ldcg(it + k_small).y <= kSmallLevel) --k_small;
-    if (k_small < k) {
-        // The top levels (created by the last PLOC iterations, few nodes each):
-        // block 0 finds every top node's (position, first leaf, parity) by
-        // pointer jumping instead of one dependent round per level, then runs
-        // the position pass over all of them at once.
-        if (blockIdx.x == 0) {
-            const uint32_t T0 = __ldcg(it + k_small + 1).y, T1 = 2 * N - 1;
-            top_positions<BLOCK>(node_kids, N, T0, T1 - T0, static_cast<uint32_t>(k - k_small),
-                                 reinterpret_cast<uint32_t*>(cb), pf, err);
-            for (uint32_t X = T0 + threadIdx.x; X < T1; X += BLOCK) layout_down(X, node_kids, pf, N, dfs, err);
+    bool gave_up = false;
+    for (uint32_t t = blockIdx.x * BLOCK + threadIdx.x; t + 1 < N && !gave_up; t += gridDim.x * BLOCK) {
+        const uint32_t X = 2 * N - 2 - t;
+        if (X != 2 * N - 2) {
+            SpinBound spin(spin_limit);
+            while (ld_acquire_u32(&pf[X - N].x) == kLayoutUnset)
+                if (!spin.step()) {
+                    raise_error(err, kDevTimeout);
+                    gave_up = true;
+                    break;
+                }
+            if (gave_up) break;
         }
-        if (!grid_barrier(bar, err, spin_limit)) return;
-        k = k_small;
+        layout_down<true>(X, node_kids, pf, N, dfs, err);
     }
-    for (; k >= 0; --k) {
-        const uint32_t lo = __ldcg(it + k).y, hi = __ldcg(it + k + 1).y;
-        for (uint32_t X = lo + blockIdx.x * BLOCK + threadIdx.x; X < hi; X += gridDim.x * BLOCK)
-            layout_down(X, node_kids, pf, N, dfs, err);
-        if (!grid_barrier(bar, err, spin_limit)) return;
-    }
+    if (!grid_barrier(bar, err, spin_limit)) return;
     const float grow = st->abs_eps;
     for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
         layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, grow, err);
