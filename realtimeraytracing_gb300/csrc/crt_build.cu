@@ -752,13 +752,14 @@ __device__ __forceinline__ uint2 layout_place(uint32_t X, const uint2* __restric
     return (X == 2 * N - 2) ? make_uint2(0u, 0u) : __ldcg(pf + (X - N));
 }
 
-// PUBLISH: each internal child's record is written second word first, then
-// its position with a release store, so that a thread waiting for it (the
-// dataflow layout below) sees the whole record once the position is there.
-template <bool PUBLISH = false>
-__device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict__ node_kids, uint2* __restrict__ pf, uint32_t N,
-                                            uint32_t* __restrict__ dfs, uint32_t* err) {
-    const uint2 me = layout_place(X, pf, N);
+// Position pass for internal node X placed at me = (position, first leaf |
+// parity << 31).  PUBLISH: each internal child's record goes out as one
+// 64-bit relaxed store, which a thread polling for it (the dataflow layout
+// below) reads whole; the record is all it needs from the parent.
+template <bool PUBLISH>
+__device__ __forceinline__ void layout_down_at(uint32_t X, uint2 me, const uint4* __restrict__ node_kids,
+                                               uint2* __restrict__ pf, uint32_t N, uint32_t* __restrict__ dfs,
+                                               uint32_t* err) {
     const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
     const uint4 kids = __ldcg(node_kids + (X - N));  // left id, right id, their leaf counts
     const uint32_t a = kids.x, b = kids.y, lca = kids.z;
@@ -770,22 +771,22 @@ __device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict_
     dfs[p] = X;
     const uint32_t nodd = (odd ^ 1u) << 31;
     if (PUBLISH) {
-        if (a < N) {
-            dfs[pl] = a;
-        } else {
-            pf[a - N].y = f | nodd;
-            st_release_u32(&pf[a - N].x, pl);
-        }
-        if (b < N) {
-            dfs[pr] = b;
-        } else {
-            pf[b - N].y = (f + lca) | nodd;
-            st_release_u32(&pf[b - N].x, pr);
-        }
+        auto word = [](uint32_t pos, uint32_t first) {
+            return (static_cast<unsigned long long>(first) << 32) | pos;
+        };
+        if (a < N) dfs[pl] = a;
+        else st_relaxed_u64(reinterpret_cast<unsigned long long*>(pf + (a - N)), word(pl, f | nodd));
+        if (b < N) dfs[pr] = b;
+        else st_relaxed_u64(reinterpret_cast<unsigned long long*>(pf + (b - N)), word(pr, (f + lca) | nodd));
         return;
     }
     if (a < N) dfs[pl] = a; else pf[a - N] = make_uint2(pl, f | nodd);
     if (b < N) dfs[pr] = b; else pf[b - N] = make_uint2(pr, (f + lca) | nodd);
+}
+
+__device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict__ node_kids, uint2* __restrict__ pf,
+                                            uint32_t N, uint32_t* __restrict__ dfs, uint32_t* err) {
+    layout_down_at<false>(X, layout_place(X, pf, N), node_kids, pf, N, dfs, err);
 }
 
 // grow: the scene's abs_eps; wide_wt receives the traversal nodes with every
@@ -974,17 +975,23 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     bool gave_up = false;
     for (uint32_t t = blockIdx.x * BLOCK + threadIdx.x; t + 1 < N && !gave_up; t += gridDim.x * BLOCK) {
         const uint32_t X = 2 * N - 2 - t;
+        uint2 me = make_uint2(0u, 0u);  // the root's place
         if (X != 2 * N - 2) {
+            const unsigned long long* w = reinterpret_cast<const unsigned long long*>(pf + (X - N));
+            unsigned long long v = ld_relaxed_u64(w);
             SpinBound spin(spin_limit);
-            while (ld_acquire_u32(&pf[X - N].x) == kLayoutUnset)
+            while (static_cast<uint32_t>(v) == kLayoutUnset) {
                 if (!spin.step()) {
                     raise_error(err, kDevTimeout);
                     gave_up = true;
                     break;
                 }
+                v = ld_relaxed_u64(w);
+            }
             if (gave_up) break;
+            me = make_uint2(static_cast<uint32_t>(v), static_cast<uint32_t>(v >> 32));
         }
-        layout_down<true>(X, node_kids, pf, N, dfs, err);
+        layout_down_at<true>(X, me, node_kids, pf, N, dfs, err);
     }
     if (!grid_barrier(bar, err, spin_limit)) return;
     const float grow = st->abs_eps;
