@@ -484,6 +484,22 @@ crt_status crt_batch_scene_info(const crt_batch* batch, uint32_t scene, uint32_t
 crt_status crt_batch_autotune(crt_ctx* ctx, crt_batch* batch, const crt_triangle* tris, const crt_ray* rays,
                               uint32_t flags, crt_hit* hits, crt_config* best, float* best_ms);
 
+/* A predictor over every scene of a batch (no counterpart in the reference):
+ * one network for all scenes; a ray's class is a treelet of its own scene
+ * (each scene's BVH cut into <= 127 subtrees) or "miss", its features its
+ * origin cell on its scene's box (the cell index moved by a hash of the scene
+ * index) and its direction bin.  Create it after the batch's first build and
+ * call crt_predictor_retarget after every rebuild.  crt_predictor_train,
+ * _infer, _classes_of_hits and _gradients take the batch's concatenated rays
+ * and hits (ray i belongs to the scene whose ray range holds it; hits carry
+ * scene-local triangle ids).  crt_batch_trace and crt_batch_run then accept
+ * CRT_TRACE_PREDICTOR_ORDER (rays ordered by scene, predicted treelet, origin
+ * cell, direction) and CRT_TRACE_USE_PREDICTOR (each ray first searches its
+ * predicted treelet exactly), with the same hits as without them; a captured
+ * graph includes the inference and reads the current weights. */
+crt_status crt_batch_predictor_create(crt_ctx* ctx, crt_batch* batch, const crt_predictor_config* cfg,
+                                      crt_predictor** out);
+
 /* ---- allocation-free Morton + sort ------------------------------------
  * No counterpart in the reference (its build allocates std::vectors freely).
  * For callers that must not have this library allocate device memory — e.g.

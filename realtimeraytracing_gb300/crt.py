@@ -46,7 +46,7 @@ EXPORTS = [
     "crt_stream", "crt_build", "crt_rebuild", "crt_bvh_free", "crt_bvh_node_count", "crt_bvh_triangle_count",
     "crt_bvh_nodes_device", "crt_bvh_copy_nodes", "crt_bvh_copy_codes", "crt_bvh_copy_perm", "crt_last_build_stats",
     "crt_raygen_pinhole", "crt_shadow_rays", "crt_trace", "crt_last_trace_stats", "crt_trace_frame",
-    "crt_morton_sort_noalloc", "crt_predictor_default_config", "crt_predictor_create", "crt_predictor_destroy",
+    "crt_morton_sort_noalloc", "crt_predictor_default_config", "crt_predictor_create", "crt_batch_predictor_create", "crt_predictor_destroy",
     "crt_predictor_retarget", "crt_predictor_train", "crt_predictor_infer", "crt_predictor_classes_of_hits",
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
@@ -119,6 +119,7 @@ def lib():
             "crt_morton_sort_noalloc": ([vp, u32, u32, vp, u32, vp, vp, vp], i32),
             "crt_predictor_default_config": ([vp], None),
             "crt_predictor_create": ([vp, vp, vp, C.POINTER(vp)], i32),
+            "crt_batch_predictor_create": ([vp, vp, vp, C.POINTER(vp)], i32),
             "crt_predictor_destroy": ([vp], i32),
             "crt_predictor_retarget": ([vp, vp], i32),
             "crt_predictor_train": ([vp, vp, vp, vp, u32, u32, vp], i32),
@@ -240,14 +241,17 @@ class PredictorConfig(C.Structure):
 class Predictor:
     """The learned hit predictor bound to one BVH (crt_predictor)."""
 
-    def __init__(self, ctx: "Context", bvh: "Bvh", seed: int = 1, lr: float = 1e-3, train_stride: int = 20,
+    def __init__(self, ctx: "Context", bvh, seed: int = 1, lr: float = 1e-3, train_stride: int = 20,
                  batch: int = 16384, miss_threshold: float = 0.9):
+        """bvh: a Bvh, or a Batch (crt_batch_predictor_create: one network over
+        every scene of the batch, created after the batch's first build)."""
         cfg = PredictorConfig()
         lib().crt_predictor_default_config(C.byref(cfg))
         cfg.seed, cfg.lr, cfg.train_stride, cfg.batch = seed, lr, train_stride, batch
         cfg.miss_threshold = miss_threshold
         h = C.c_void_p()
-        _check(lib().crt_predictor_create(ctx.handle, bvh.handle, C.byref(cfg), C.byref(h)))
+        create = lib().crt_batch_predictor_create if isinstance(bvh, Batch) else lib().crt_predictor_create
+        _check(create(ctx.handle, bvh.handle, C.byref(cfg), C.byref(h)))
         self.ctx, self.bvh, self.handle = ctx, bvh, h
 
     def info(self) -> dict:

@@ -145,7 +145,12 @@ struct crt_bvh {
 };
 
 struct crt_predictor {
-    crt_bvh* bvh = nullptr;
+    crt_bvh* bvh = nullptr;        // bound to one BVH ...
+    crt_batch* batch = nullptr;    // ... or to every scene of a batch
+    // a batch's device scene table, node array and triangle count (fixed at crt_batch_create)
+    const crt::BatchScene* batch_scenes = nullptr;
+    const crt_bvh_node* batch_nodes = nullptr;
+    uint32_t batch_n_scenes = 0, batch_n_tris = 0;
     crt_predictor_config cfg{};
     DevBuf params;      // master | m | v | grad, CRT_PREDICTOR_PARAMS floats each
     DevBuf w16;         // fp16 copies
@@ -166,9 +171,13 @@ struct crt_predictor {
         d.grad = base + 3 * crt::pred::kParams;
         d.w16 = w16.as<__half>();
         d.tri_class = tri_class.as<uint8_t>();
-        d.n_tris = bvh ? bvh->n : 0;
+        d.n_tris = bvh ? bvh->n : batch_n_tris;
+        d.scenes = batch_scenes;
+        d.n_scenes = batch ? batch_n_scenes : 0u;
         return d;
     }
+    bool bound() const { return bvh != nullptr || batch != nullptr; }
+    const crt_bvh_node* nodes() const { return bvh ? bvh->nodes.as<crt_bvh_node>() : batch_nodes; }
 };
 
 struct crt_ctx {
@@ -743,7 +752,7 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
         if (flags & CRT_TRACE_PREDICTOR_ORDER) {  // includes the coherence order of CRT_TRACE_SORT_RAYS
             CRT_TRY(pr->order.reserve(4ull * n_rays));
             CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
-            crt::pred_order(b->nodes.as<crt_bvh_node>(), d_rays, pr->classes.as<uint16_t>(), n_rays,
+            crt::pred_order(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, pr->classes.as<uint16_t>(), n_rays,
                             pr->order.as<uint32_t>(), pr->order_scratch.p, x->err.as<uint32_t>(), x->cfg.spin_limit,
                             x->stream);
             CRT_CUDA(cudaGetLastError());
@@ -1452,7 +1461,30 @@ crt_status stage_in_once(crt_ctx* x, DevBuf& buf, const void* src, size_t bytes,
     return stage_in(x, buf, src, bytes, dev);
 }
 
+// The batch's traversal nodes and leaf records, and dropping its predictor
+// (defined with crt_batch below).
+const float4* batch_wide(const crt_batch* bt);
+const float4* batch_xtri(const crt_batch* bt);
+void batch_unbind(crt_batch* bt);
+
 crt_status predictor_targets(crt_ctx* x, crt_predictor* pr) {
+    if (pr->batch) {  // every scene cut into its own treelets
+        const uint32_t ns = pr->batch_n_scenes;
+        CRT_TRY(pr->tri_class.reserve(pr->batch_n_tris));
+        CRT_TRY(pr->treelets.reserve(sizeof(crt::Treelet) * 128 * ns + 4ull * ns + 16));
+        CRT_CUDA(cudaMemsetAsync(pr->tri_class.p, crt::pred::kMissClass, pr->batch_n_tris, x->stream));
+        uint32_t* n_tl = reinterpret_cast<uint32_t*>(pr->treelets.as<crt::Treelet>() + 128 * ns);
+        crt::pred_treelets_batch(pr->batch_scenes, ns, pr->batch_n_tris, pr->batch_nodes,
+                                 batch_wide(pr->batch), batch_xtri(pr->batch), pr->treelets.as<crt::Treelet>(), n_tl,
+                                 pr->tri_class.as<uint8_t>(), x->stream);
+        CRT_CUDA(cudaGetLastError());
+        std::vector<uint32_t> counts(ns);
+        CRT_CUDA(cudaMemcpyAsync(counts.data(), n_tl, 4ull * ns, cudaMemcpyDeviceToHost, x->stream));
+        CRT_CUDA(cudaStreamSynchronize(x->stream));
+        pr->n_treelets = 0;
+        for (uint32_t c : counts) pr->n_treelets += c;
+        return CRT_OK;
+    }
     crt_bvh* b = pr->bvh;
     CRT_TRY(pr->tri_class.reserve(b->n));
     CRT_TRY(pr->treelets.reserve(sizeof(crt::Treelet) * 128 + 16));
@@ -1464,14 +1496,6 @@ crt_status predictor_targets(crt_ctx* x, crt_predictor* pr) {
     CRT_CUDA(cudaMemcpyAsync(&pr->n_treelets, n_tl, 4, cudaMemcpyDeviceToHost, x->stream));
     CRT_CUDA(cudaStreamSynchronize(x->stream));
     return CRT_OK;
-}
-
-__global__ void classes_of_hits_kernel(const crt_hit* hits, uint32_t n, const uint8_t* tri_class, uint32_t n_tris,
-                                       uint16_t* out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t t = hits[i].tri;
-    out[i] = (t == CRT_MISS || t >= n_tris) ? static_cast<uint16_t>(crt::pred::kMissClass) : tri_class[t];
 }
 
 }  // namespace
@@ -1518,6 +1542,7 @@ crt_status crt_predictor_create(crt_ctx* x, crt_bvh* b, const crt_predictor_conf
 crt_status crt_predictor_destroy(crt_predictor* pr) {
     if (!pr) return CRT_OK;
     if (pr->bvh) pr->bvh->predictor = nullptr;
+    if (pr->batch) batch_unbind(pr->batch);
     DevBuf* bufs[] = {&pr->params, &pr->w16, &pr->tri_class, &pr->treelets, &pr->classes, &pr->scratch,
                       &pr->rays_in, &pr->hits_in, &pr->targets_in, &pr->order, &pr->order_scratch};
     for (DevBuf* d : bufs) d->release();
@@ -1526,14 +1551,14 @@ crt_status crt_predictor_destroy(crt_predictor* pr) {
 }
 
 crt_status crt_predictor_retarget(crt_ctx* x, crt_predictor* pr) {
-    if (!x || !pr || !pr->bvh) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_retarget: null or unbound predictor");
+    if (!x || !pr || !pr->bound()) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_retarget: null or unbound predictor");
     CRT_CUDA(cudaSetDevice(x->device));
     return predictor_targets(x, pr);
 }
 
 crt_status crt_predictor_train(crt_ctx* x, crt_predictor* pr, const crt_ray* rays, const crt_hit* hits,
                                uint32_t n_rays, uint32_t offset, float* loss) {
-    if (!x || !pr || !pr->bvh || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_train: null argument");
+    if (!x || !pr || !pr->bound() || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_train: null argument");
     CRT_CUDA(cudaSetDevice(x->device));
     const void* d_rays;
     const void* d_hits;
@@ -1545,7 +1570,7 @@ crt_status crt_predictor_train(crt_ctx* x, crt_predictor* pr, const crt_ray* ray
     CRT_CUDA(cudaMemsetAsync(pr->scratch.p, 0, 16, x->stream));
     for (uint32_t done = 0; done < total; done += pr->cfg.batch) {
         const uint32_t nb = std::min(pr->cfg.batch, total - done);
-        CRT_CUDA(crt::pred_train_step(pr->dev(), pr->bvh->nodes.as<crt_bvh_node>(),
+        CRT_CUDA(crt::pred_train_step(pr->dev(), pr->nodes(),
                                       static_cast<const crt_ray*>(d_rays), n_rays, static_cast<const crt_hit*>(d_hits),
                                       nullptr, nb, stride, offset + done * stride, pr->scratch.as<float>(),
                                       x->err.as<uint32_t>(), x->stream));
@@ -1561,7 +1586,7 @@ crt_status crt_predictor_train(crt_ctx* x, crt_predictor* pr, const crt_ray* ray
 }
 
 crt_status crt_predictor_infer(crt_ctx* x, crt_predictor* pr, const crt_ray* rays, uint32_t n, uint16_t* classes) {
-    if (!x || !pr || !pr->bvh || !rays || !classes) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_infer: null argument");
+    if (!x || !pr || !pr->bound() || !rays || !classes) return fail(CRT_ERR_INVALID_ARG, "crt_predictor_infer: null argument");
     CRT_CUDA(cudaSetDevice(x->device));
     if (n == 0) return CRT_OK;
     const void* d_rays;
@@ -1575,7 +1600,7 @@ crt_status crt_predictor_infer(crt_ctx* x, crt_predictor* pr, const crt_ray* ray
         d_out = pr->classes.as<uint16_t>();
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
-    CRT_CUDA(crt::pred_infer(pr->dev(), pr->bvh->nodes.as<crt_bvh_node>(), static_cast<const crt_ray*>(d_rays), n,
+    CRT_CUDA(crt::pred_infer(pr->dev(), pr->nodes(), static_cast<const crt_ray*>(d_rays), n,
                              d_out, pr->cfg.miss_threshold, x->err.as<uint32_t>(), x->stream));
     if (!dev_out) CRT_CUDA(cudaMemcpyAsync(classes, d_out, 2ull * n, cudaMemcpyDeviceToHost, x->stream));
     return x->check_device_error();
@@ -1583,7 +1608,7 @@ crt_status crt_predictor_infer(crt_ctx* x, crt_predictor* pr, const crt_ray* ray
 
 crt_status crt_predictor_classes_of_hits(crt_ctx* x, crt_predictor* pr, const crt_hit* hits, uint32_t n,
                                          uint16_t* classes) {
-    if (!x || !pr || !pr->bvh || !hits || !classes) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    if (!x || !pr || !pr->bound() || !hits || !classes) return fail(CRT_ERR_INVALID_ARG, "null argument");
     CRT_CUDA(cudaSetDevice(x->device));
     if (n == 0) return CRT_OK;
     const void* d_hits;
@@ -1596,8 +1621,7 @@ crt_status crt_predictor_classes_of_hits(crt_ctx* x, crt_predictor* pr, const cr
         CRT_TRY(pr->targets_in.reserve(2ull * n));
         d_out = pr->targets_in.as<uint16_t>();
     }
-    classes_of_hits_kernel<<<(n + 255) / 256, 256, 0, x->stream>>>(static_cast<const crt_hit*>(d_hits), n,
-                                                                    pr->tri_class.as<uint8_t>(), pr->bvh->n, d_out);
+    crt::pred_classes_of_hits(pr->dev(), static_cast<const crt_hit*>(d_hits), n, d_out, x->stream);
     CRT_CUDA(cudaGetLastError());
     if (!dev_out) CRT_CUDA(cudaMemcpyAsync(classes, d_out, 2ull * n, cudaMemcpyDeviceToHost, x->stream));
     CRT_CUDA(cudaStreamSynchronize(x->stream));
@@ -1606,7 +1630,7 @@ crt_status crt_predictor_classes_of_hits(crt_ctx* x, crt_predictor* pr, const cr
 
 crt_status crt_predictor_gradients(crt_ctx* x, crt_predictor* pr, const crt_ray* rays, const uint16_t* targets,
                                    uint32_t n, float* grad, float* loss) {
-    if (!x || !pr || !pr->bvh || !rays || !targets || !grad) return fail(CRT_ERR_INVALID_ARG, "null argument");
+    if (!x || !pr || !pr->bound() || !rays || !targets || !grad) return fail(CRT_ERR_INVALID_ARG, "null argument");
     CRT_CUDA(cudaSetDevice(x->device));
     const void* d_rays;
     const void* d_t;
@@ -1616,7 +1640,7 @@ crt_status crt_predictor_gradients(crt_ctx* x, crt_predictor* pr, const crt_ray*
     CRT_CUDA(cudaMemsetAsync(d.grad, 0, sizeof(float) * crt::pred::kParams, x->stream));
     CRT_CUDA(cudaMemsetAsync(pr->scratch.p, 0, 16, x->stream));
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
-    CRT_CUDA(crt::pred_train_step(d, pr->bvh->nodes.as<crt_bvh_node>(), static_cast<const crt_ray*>(d_rays), n, nullptr,
+    CRT_CUDA(crt::pred_train_step(d, pr->nodes(), static_cast<const crt_ray*>(d_rays), n, nullptr,
                                   static_cast<const uint16_t*>(d_t), n, 1, 0, pr->scratch.as<float>(),
                                   x->err.as<uint32_t>(), x->stream));
     CRT_CUDA(cudaMemcpyAsync(grad, d.grad, sizeof(float) * crt::pred::kParams,
@@ -1687,6 +1711,8 @@ crt_status crt_bounce_rays(crt_ctx* x, const crt_bvh* b, const crt_ray* primary,
 // ===================================================================== batches
 struct crt_batch {
     crt_ctx* ctx = nullptr;
+    crt_predictor* predictor = nullptr;  // crt_batch_predictor_create
+    bool built = false;                  // a build has completed
     uint32_t n_scenes = 0;
     uint32_t n_tris = 0, n_rays = 0;
     std::vector<crt::BatchScene> hs;
@@ -1713,6 +1739,10 @@ struct crt_batch {
 
 namespace {
 
+const float4* batch_wide(const crt_batch* bt) { return bt->wide.as<float4>(); }
+const float4* batch_xtri(const crt_batch* bt) { return bt->xtri.as<float4>(); }
+void batch_unbind(crt_batch* bt) { bt->predictor = nullptr; bt->drop_graph(); }
+
 crt_status batch_upload_models(crt_ctx* x, crt_batch* bt, const crt_mesh_model* models, uint32_t n_models) {
     std::vector<float> hm(2 * 64 * 16);
     for (uint32_t m = 0; m < 64; ++m) {
@@ -1728,6 +1758,58 @@ crt_status batch_upload_models(crt_ctx* x, crt_batch* bt, const crt_mesh_model* 
 }
 
 // Enqueue build (and trace when rays != null) without synchronising.
+// The trace of every scene's rays, one launch (after the ordering or learned
+// steps the flags ask for), on x's stream; no allocation, so it can be
+// captured into the batch's graph.
+crt_status batch_trace_enqueue(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint32_t flags, crt_hit* hits,
+                               bool deep) {
+    cudaStream_t s = x->stream;
+    uint32_t* err = bt->err.as<uint32_t>();
+    crt::TraceParams p{};
+    p.nodes = bt->nodes.as<crt_bvh_node>();
+    p.wide = (flags & CRT_TRI_WATERTIGHT) ? bt->wide_wt.as<float4>() : bt->wide.as<float4>();
+    p.xtri = bt->xtri.as<float4>();
+    p.rays = rays;
+    p.hits = hits;
+    p.n_rays = bt->n_rays;
+    p.err = err;
+    if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && bt->n_rays > 0) {
+        crt_predictor* pr = bt->predictor;
+        CRT_CUDA(crt::pred_infer(pr->dev(), pr->nodes(), rays, bt->n_rays, pr->classes.as<uint16_t>(),
+                                 pr->cfg.miss_threshold, err, s));
+        if (flags & CRT_TRACE_USE_PREDICTOR) {
+            p.pred_class = pr->classes.as<uint16_t>();
+            p.treelets = pr->treelets.as<crt::Treelet>();
+            p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128 * bt->n_scenes);
+        }
+        if ((flags & CRT_TRACE_PREDICTOR_ORDER) && bt->n_rays > 1) {
+            crt::pred_order(pr->dev(), pr->nodes(), rays, pr->classes.as<uint16_t>(), bt->n_rays, pr->order.as<uint32_t>(),
+                            pr->order_scratch.p, err, x->cfg.spin_limit, s);
+            p.order = pr->order.as<uint32_t>();
+        }
+    }
+    if ((flags & CRT_TRACE_SORT_RAYS) && !p.order && bt->n_rays > 1) {
+        crt::launch_ray_order(rays, bt->n_rays, bt->nodes.as<crt_bvh_node>(), bt->scenes.as<crt::BatchScene>(),
+                              bt->n_scenes, bt->ray_order.as<uint32_t>(), bt->ray_order_scratch.p, err, x->cfg.spin_limit,
+                              s);
+        p.order = bt->ray_order.as<uint32_t>();
+    }
+    crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
+                            flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block), deep, s);
+    CRT_CUDA(cudaGetLastError());
+    return CRT_OK;
+}
+
+// Flags a batch trace accepts: the learned ones need the batch's predictor.
+crt_status batch_trace_flags(const crt_batch* bt, uint32_t flags, const char* who) {
+    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS | CRT_TRACE_USE_PREDICTOR |
+                  CRT_TRACE_PREDICTOR_ORDER))
+        return fail(CRT_ERR_INVALID_ARG, "%s: unsupported flags 0x%x", who, flags);
+    if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && !bt->predictor)
+        return fail(CRT_ERR_UNSUPPORTED, "%s: the batch has no predictor (crt_batch_predictor_create)", who);
+    return CRT_OK;
+}
+
 crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
                          crt_hit* hits, cudaEvent_t ev_built) {
     cudaStream_t s = x->stream;
@@ -1781,26 +1863,7 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
     }
     CRT_CUDA(cudaGetLastError());
     if (ev_built) CRT_CUDA(cudaEventRecord(ev_built, s));
-    if (rays) {
-        crt::TraceParams p{};
-        p.nodes = bt->nodes.as<crt_bvh_node>();
-        p.wide = (flags & CRT_TRI_WATERTIGHT) ? bt->wide_wt.as<float4>() : bt->wide.as<float4>();
-        p.xtri = bt->xtri.as<float4>();
-        p.rays = rays;
-        p.hits = hits;
-        p.n_rays = bt->n_rays;
-        p.err = err;
-        if ((flags & CRT_TRACE_SORT_RAYS) && bt->n_rays > 1) {
-            crt::launch_ray_order(rays, bt->n_rays, bt->nodes.as<crt_bvh_node>(), bt->scenes.as<crt::BatchScene>(),
-                                  bt->n_scenes, bt->ray_order.as<uint32_t>(), bt->ray_order_scratch.p, err,
-                                  x->cfg.spin_limit, s);
-            p.order = bt->ray_order.as<uint32_t>();
-        }
-        crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
-                                flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block),
-                                bt->cfg.stack_depth > 64, s);
-        CRT_CUDA(cudaGetLastError());
-    }
+    if (rays) CRT_TRY(batch_trace_enqueue(x, bt, rays, flags, hits, bt->cfg.stack_depth > 64));
     return CRT_OK;
 }
 
@@ -1927,6 +1990,11 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
 crt_status crt_batch_free(crt_batch* bt) {
     if (!bt) return CRT_OK;
     bt->drop_graph();
+    if (bt->predictor) {  // the predictor stays valid but unbound
+        bt->predictor->batch = nullptr;
+        bt->predictor->batch_scenes = nullptr;
+        bt->predictor->batch_nodes = nullptr;
+    }
     DevBuf* bufs[] = {&bt->scenes, &bt->seg_off, &bt->seg_hist, &bt->chunks, &bt->states, &bt->models, &bt->err,
                       &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
                       &bt->perm_local, &bt->node_box, &bt->node_kids, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
@@ -1970,46 +2038,68 @@ crt_status crt_batch_build(crt_ctx* x, crt_batch* bt, const crt_triangle* tris) 
     CRT_TRY(check_aligned16(tris, "crt_batch_build: triangles"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_enqueue(x, bt, tris, nullptr, 0, nullptr, nullptr));
-    return batch_check(x, bt);
+    CRT_TRY(batch_check(x, bt));
+    bt->built = true;
+    return CRT_OK;
+}
+
+crt_status crt_batch_predictor_create(crt_ctx* x, crt_batch* bt, const crt_predictor_config* cfg, crt_predictor** out) {
+    if (!x || !bt || !out) return fail(CRT_ERR_INVALID_ARG, "crt_batch_predictor_create: null argument");
+    if (bt->predictor) return fail(CRT_ERR_INVALID_ARG, "crt_batch_predictor_create: the batch already has a predictor");
+    if (!bt->built) return fail(CRT_ERR_INVALID_ARG, "crt_batch_predictor_create: build the batch first");
+    CRT_CUDA(cudaSetDevice(x->device));
+    crt_predictor* pr = new crt_predictor();
+    crt_predictor_default_config(&pr->cfg);
+    if (cfg) pr->cfg = *cfg;
+    if (pr->cfg.train_stride == 0) pr->cfg.train_stride = 1;
+    if (pr->cfg.batch == 0) pr->cfg.batch = 16384;
+    pr->batch = bt;
+    pr->batch_scenes = bt->scenes.as<crt::BatchScene>();
+    pr->batch_nodes = bt->nodes.as<crt_bvh_node>();
+    pr->batch_n_scenes = bt->n_scenes;
+    pr->batch_n_tris = bt->n_tris;
+    const size_t n_rays = bt->n_rays;
+    crt_status s = pr->params.reserve(4 * sizeof(float) * crt::pred::kParams);
+    if (s == CRT_OK) s = pr->w16.reserve(sizeof(__half) * crt::pred::kHalfs);
+    if (s == CRT_OK) s = pr->scratch.reserve(16);
+    // the trace's inference and ordering buffers, sized now so that a captured graph allocates nothing
+    if (s == CRT_OK) s = pr->classes.reserve(2 * n_rays + 16);
+    if (s == CRT_OK) s = pr->order.reserve(4 * n_rays + 16);
+    if (s == CRT_OK) s = pr->order_scratch.reserve(crt::pred_order_scratch_bytes(static_cast<uint32_t>(n_rays)));
+    if (s == CRT_OK && crt::pred_prepare() != cudaSuccess) s = fail(CRT_ERR_CUDA, "predictor kernel attributes");
+    if (s == CRT_OK) {
+        crt::pred_init(pr->dev(), pr->cfg.seed, x->stream);
+        s = predictor_targets(x, pr);
+    }
+    if (s != CRT_OK) {
+        pr->batch = nullptr;
+        crt_predictor_destroy(pr);
+        return s;
+    }
+    bt->predictor = pr;
+    bt->drop_graph();
+    *out = pr;
+    return CRT_OK;
 }
 
 crt_status crt_batch_trace(crt_ctx* x, crt_batch* bt, const crt_ray* rays, uint32_t flags, crt_hit* hits) {
     if (!x || !bt || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: null argument");
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS))
-        return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: unsupported flags");
+    CRT_TRY(batch_trace_flags(bt, flags, "crt_batch_trace"));
     if (!is_device_ptr(rays) || !is_device_ptr(hits)) return fail(CRT_ERR_INVALID_ARG, "crt_batch_trace: device memory only");
     CRT_TRY(check_aligned16(rays, "crt_batch_trace: rays"));
     CRT_TRY(check_aligned16(hits, "crt_batch_trace: hits"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_order_buffers(bt, flags));
     CRT_CUDA(cudaMemsetAsync(bt->err.p, 0, 16, x->stream));
-    crt::TraceParams p{};
-    p.nodes = bt->nodes.as<crt_bvh_node>();
-    p.wide = (flags & CRT_TRI_WATERTIGHT) ? bt->wide_wt.as<float4>() : bt->wide.as<float4>();
-    p.xtri = bt->xtri.as<float4>();
-    p.rays = rays;
-    p.hits = hits;
-    p.n_rays = bt->n_rays;
-    p.err = bt->err.as<uint32_t>();
     const bool deep = bt->cfg.stack_depth > 64 || bt->max_iters + 2 > 64;
-    if ((flags & CRT_TRACE_SORT_RAYS) && bt->n_rays > 1) {
-        crt::launch_ray_order(rays, bt->n_rays, bt->nodes.as<crt_bvh_node>(), bt->scenes.as<crt::BatchScene>(),
-                              bt->n_scenes, bt->ray_order.as<uint32_t>(), bt->ray_order_scratch.p, p.err,
-                              x->cfg.spin_limit, x->stream);
-        p.order = bt->ray_order.as<uint32_t>();
-    }
-    crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
-                            flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block), deep,
-                            x->stream);
-    CRT_CUDA(cudaGetLastError());
+    CRT_TRY(batch_trace_enqueue(x, bt, rays, flags, hits, deep));
     return batch_check(x, bt);
 }
 
 crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
                          crt_hit* hits, int use_graph, int* graph_used) {
     if (!x || !bt || !tris || !rays || !hits) return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: null argument");
-    if (flags & ~(CRT_TRACE_ANY | CRT_TRI_WATERTIGHT | CRT_TRACE_SORT_RAYS))
-        return fail(CRT_ERR_INVALID_ARG, "crt_batch_run: unsupported flags");
+    CRT_TRY(batch_trace_flags(bt, flags, "crt_batch_run"));
     CRT_TRY(check_batch_buffers(tris, rays, hits, "crt_batch_run"));
     CRT_CUDA(cudaSetDevice(x->device));
     CRT_TRY(batch_order_buffers(bt, flags));  // before any graph capture: no allocation inside it
@@ -2038,11 +2128,15 @@ crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
         if (bt->graph) {
             CRT_CUDA(cudaGraphLaunch(bt->graph, x->stream));
             if (graph_used) *graph_used = 1;
-            return batch_check(x, bt);
+            CRT_TRY(batch_check(x, bt));
+            bt->built = true;
+            return CRT_OK;
         }
     }
     CRT_TRY(batch_enqueue(x, bt, tris, rays, flags, hits, nullptr));
-    return batch_check(x, bt);
+    CRT_TRY(batch_check(x, bt));
+    bt->built = true;
+    return CRT_OK;
 }
 
 crt_status crt_batch_copy_nodes(crt_ctx* x, const crt_batch* bt, uint32_t scene, crt_bvh_node* dst) {

@@ -67,6 +67,41 @@ __device__ __forceinline__ void ray_keys(const float4 r0, const float4 r1, const
     bin = static_cast<uint32_t>(bu) * kDirBins + bv;
 }
 
+// The scene of global ray i in a batch (the last scene whose first ray is <= i).
+__device__ __forceinline__ uint32_t scene_of_ray(const BatchScene* sc, uint32_t n_scenes, uint32_t i) {
+    uint32_t lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&sc[mid].ray_off) <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Features of ray i: its origin cell and direction bin; in a batch, on its
+// scene's box, with the cell index moved by a per-scene hash so that the
+// scenes share the cell embeddings without sharing cells.  *scene: the
+// ray's scene (0 for one BVH).
+__device__ __forceinline__ void ray_features(const PredictorDev& P, const crt_bvh_node* nodes, const SceneFrame& fr,
+                                             uint32_t i, float4 r0, float4 r1, uint32_t& cell, uint32_t& bin,
+                                             uint32_t& scene) {
+    if (P.n_scenes == 0) {
+        scene = 0;
+        ray_keys(r0, r1, fr, cell, bin);
+        return;
+    }
+    scene = scene_of_ray(P.scenes, P.n_scenes, i);
+    ray_keys(r0, r1, scene_frame(nodes + __ldg(&P.scenes[scene].node_off)), cell, bin);
+    cell = (cell + scene * 0x9E3779B1u) & static_cast<uint32_t>(kEo - 1);
+}
+
+// Class of the closest hit `tri` (scene-local id in a batch) of a ray of `scene`.
+__device__ __forceinline__ int hit_class(const PredictorDev& P, uint32_t scene, uint32_t tri) {
+    if (tri == CRT_MISS) return kMissClass;
+    if (P.n_scenes == 0) return tri < P.n_tris ? P.tri_class[tri] : kMissClass;
+    const uint32_t off = __ldg(&P.scenes[scene].tri_off), n = __ldg(&P.scenes[scene].n_tris);
+    return tri < n ? P.tri_class[off + tri] : kMissClass;
+}
+
 // ---------------------------------------------------- smem tile helpers
 // Copy a row-major fp16 matrix (rows x cols) into the K-major core layout.
 __device__ __forceinline__ void load_kmajor(unsigned char* dst, const __half* src, int rows, int cols) {
@@ -203,8 +238,8 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         if (valid) {
             const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
             const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
-            uint32_t cell, bin;
-            ray_keys(r0, r1, fr, cell, bin);
+            uint32_t cell, bin, scene;
+            ray_features(P, nodes, fr, i, r0, r1, cell, bin, scene);
             const uint4* eo = reinterpret_cast<const uint4*>(P.w16 + hEo + static_cast<size_t>(cell) * kEmb);
             const uint4* ed = reinterpret_cast<const uint4*>(P.w16 + hEd + static_cast<size_t>(bin) * kEmb);
             e[0] = __ldg(eo); e[1] = __ldg(eo + 1); e[2] = __ldg(ed); e[3] = __ldg(ed + 1);
@@ -326,15 +361,15 @@ __global__ void __launch_bounds__(128) train_kernel(PredictorDev P, const crt_bv
     if (valid) {
         const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + ri));
         const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + ri) + 1);
-        ray_keys(r0, r1, scene_frame(nodes), cell, bin);
+        uint32_t scene;
+        ray_features(P, nodes, scene_frame(nodes), static_cast<uint32_t>(ri), r0, r1, cell, bin, scene);
         const uint4* eo = reinterpret_cast<const uint4*>(P.w16 + hEo + static_cast<size_t>(cell) * kEmb);
         const uint4* ed = reinterpret_cast<const uint4*>(P.w16 + hEd + static_cast<size_t>(bin) * kEmb);
         e[0] = __ldg(eo); e[1] = __ldg(eo + 1); e[2] = __ldg(ed); e[3] = __ldg(ed + 1);
         if (targets) {
             target = targets[ri];
         } else {
-            const uint32_t tri = __ldg(reinterpret_cast<const uint32_t*>(hits + ri));
-            target = (tri == CRT_MISS || tri >= P.n_tris) ? kMissClass : P.tri_class[tri];
+            target = hit_class(P, scene, __ldg(reinterpret_cast<const uint32_t*>(hits + ri)));
         }
         if (target < 0 || target >= kClasses) target = kMissClass;
     }
@@ -662,9 +697,8 @@ __global__ void init_kernel(PredictorDev P, uint32_t seed) {
 // Cut the BVH into at most kClasses-1 subtrees: starting from the root,
 // repeatedly split the frontier subtree with the most leaves (its children
 // come from the 64-byte traversal node).  Single thread; <= 127 splits.
-__global__ void treelet_cut_kernel(const crt_bvh_node* nodes, const float4* wide, uint32_t n_leaves, Treelet* out,
-                                   uint32_t* n_out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void treelet_cut(const crt_bvh_node* nodes, const float4* wide, uint32_t n_leaves, Treelet* out,
+                            uint32_t* n_out) {
     const float4 rmn = reinterpret_cast<const float4*>(nodes)[0];
     const float4 rmx = reinterpret_cast<const float4*>(nodes)[1];
     const uint4 lr = reinterpret_cast<const uint4*>(nodes)[2];
@@ -701,13 +735,25 @@ __global__ void treelet_cut_kernel(const crt_bvh_node* nodes, const float4* wide
     *n_out = cnt;
 }
 
+__global__ void treelet_cut_kernel(const crt_bvh_node* nodes, const float4* wide, uint32_t n_leaves, Treelet* out,
+                                   uint32_t* n_out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    treelet_cut(nodes, wide, n_leaves, out, n_out);
+}
+
+// One block per scene of a batch: that scene's cut at out + 128 k.
+__global__ void treelet_cut_batch_kernel(const BatchScene* scenes, const crt_bvh_node* nodes, const float4* wide,
+                                         Treelet* out, uint32_t* n_out) {
+    if (threadIdx.x != 0) return;
+    const BatchScene sc = scenes[blockIdx.x];
+    treelet_cut(nodes + sc.node_off, wide + 4 * static_cast<size_t>(sc.wide_off), sc.n_tris,
+                out + 128 * static_cast<size_t>(blockIdx.x), n_out + blockIdx.x);
+}
+
 // Class of every triangle: the treelet whose leaf range (in the tree's
 // left-to-right leaf order, the order of the leaf records) holds its leaf.
-__global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, const float4* xtri, uint32_t n_leaves,
-                                     uint8_t* tri_class) {
-    const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
-    if (L >= n_leaves) return;
-    const uint32_t n = *n_tl;
+__device__ __forceinline__ void label_leaf(const Treelet* tl, uint32_t n, const float4* xtri, uint32_t L,
+                                           uint32_t n_leaves, uint8_t* tri_class) {
     int lo = 0, hi = static_cast<int>(n) - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) / 2;
@@ -715,6 +761,37 @@ __global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, co
     }
     const uint32_t tri = __float_as_uint(xtri[3 * static_cast<size_t>(L)].w);
     if (tri < n_leaves) tri_class[tri] = static_cast<uint8_t>(lo);
+}
+
+__global__ void treelet_label_kernel(const Treelet* tl, const uint32_t* n_tl, const float4* xtri, uint32_t n_leaves,
+                                     uint8_t* tri_class) {
+    const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= n_leaves) return;
+    label_leaf(tl, *n_tl, xtri, L, n_leaves, tri_class);
+}
+
+// Leaf g of the concatenated scenes (scene k's leaves from its tri_off).
+__global__ void treelet_label_batch_kernel(const BatchScene* scenes, uint32_t n_scenes, uint32_t n_total,
+                                           const Treelet* tl, const uint32_t* n_tl, const float4* xtri,
+                                           uint8_t* tri_class) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n_total) return;
+    uint32_t lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&scenes[mid].tri_off) <= g) lo = mid; else hi = mid - 1;
+    }
+    const BatchScene sc = scenes[lo];
+    label_leaf(tl + 128 * static_cast<size_t>(lo), n_tl[lo], xtri + 3 * static_cast<size_t>(sc.tri_off), g - sc.tri_off,
+               sc.n_tris, tri_class + sc.tri_off);
+}
+
+// Class of the hit of each ray (a batch's rays, or one BVH's).
+__global__ void classes_of_hits_kernel(PredictorDev P, const crt_hit* hits, uint32_t n, uint16_t* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t scene = P.n_scenes ? scene_of_ray(P.scenes, P.n_scenes, i) : 0u;
+    out[i] = static_cast<uint16_t>(hit_class(P, scene, hits[i].tri));
 }
 
 // ------------------------------------------------------------ bounce rays
@@ -816,7 +893,8 @@ __device__ __forceinline__ uint32_t spread5(uint32_t v) {
     return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6) | ((v & 16u) << 8);
 }
 
-__global__ void __launch_bounds__(256) order_keys_kernel(const crt_bvh_node* nodes, const crt_ray* __restrict__ rays,
+__global__ void __launch_bounds__(256) order_keys_kernel(PredictorDev P, const crt_bvh_node* nodes,
+                                                         const crt_ray* __restrict__ rays,
                                                          const uint16_t* __restrict__ classes, uint32_t n,
                                                          uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
     __shared__ uint32_t h[4 * 256];
@@ -826,11 +904,20 @@ __global__ void __launch_bounds__(256) order_keys_kernel(const crt_bvh_node* nod
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
         const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
-        uint32_t cell, bin;
-        ray_keys(r0, r1, fr, cell, bin);
-        const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
-        const uint32_t m = (spread5(cx >> 1) << 2) | (spread5(cy >> 1) << 1) | spread5(cz >> 1);
-        const uint32_t key = ((static_cast<uint32_t>(classes[i]) & 0x7Fu) << 25) | (m << 10) | (bin & 1023u);
+        uint32_t cell, bin, key;
+        const uint32_t cls = static_cast<uint32_t>(classes[i]) & 0x7Fu;
+        if (P.n_scenes == 0) {
+            ray_keys(r0, r1, fr, cell, bin);
+            const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
+            const uint32_t m = (spread5(cx >> 1) << 2) | (spread5(cy >> 1) << 1) | spread5(cz >> 1);
+            key = (cls << 25) | (m << 10) | (bin & 1023u);
+        } else {  // (scene, class, 16^3 origin cell, first direction coordinate): 8 + 7 + 12 + 5 bits
+            const uint32_t sc = scene_of_ray(P.scenes, P.n_scenes, i);
+            ray_keys(r0, r1, scene_frame(nodes + __ldg(&P.scenes[sc].node_off)), cell, bin);
+            const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
+            const uint32_t m = (spread5(cx >> 2) << 2) | (spread5(cy >> 2) << 1) | spread5(cz >> 2);
+            key = ((sc & 0xFFu) << 24) | (cls << 17) | ((m & 0xFFFu) << 5) | ((bin >> 5) & 31u);
+        }
         keys[i] = key;
 #pragma unroll
         for (int p = 0; p < 4; ++p) atomicAdd(&h[p * 256 + ((key >> (8 * p)) & 255u)], 1u);
@@ -848,8 +935,8 @@ size_t pred_order_scratch_bytes(uint32_t n) {
     return 4 * (3 * static_cast<size_t>(n) + 4 * 256 + 4 * (tiles * 256 + 1) + 64);
 }
 
-void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes, uint32_t n, uint32_t* order,
-                void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+void pred_order(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes,
+                uint32_t n, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
     if (n == 0) return;
     uint32_t* ka = static_cast<uint32_t*>(scratch);
     uint32_t* kb = ka + n;
@@ -860,7 +947,7 @@ void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* 
     const size_t lb_words = tiles * 256 + 1;
     cudaMemsetAsync(hist, 0, 4 * (4 * 256 + 4 * lb_words), s);
     const uint32_t grid = std::min<uint32_t>((n + 255) / 256, kNumSms * 8);
-    pred::order_keys_kernel<<<grid, 256, 0, s>>>(nodes, rays, classes, n, ka, hist);
+    pred::order_keys_kernel<<<grid, 256, 0, s>>>(P, nodes, rays, classes, n, ka, hist);
     // four stable 8-bit passes; pass 0 synthesises the ray indices
     const uint32_t* kin[4] = {ka, kb, ka, kb};
     uint32_t* kout[4] = {kb, ka, kb, ka};
@@ -879,6 +966,14 @@ cudaError_t tc_wait_probe(int complete, uint32_t limit, uint32_t* err, float* ou
 void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s) {
     pred::init_kernel<<<kNumSms * 8, 256, 0, s>>>(P, seed);
     pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
+}
+
+cudaError_t pred_prepare() {
+    cudaError_t e = cudaFuncSetAttribute(pred::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         pred::kInferSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pred::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pred::kTrainSmem);
+    return e;
 }
 
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
@@ -929,6 +1024,20 @@ void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const float4* 
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s) {
     pred::treelet_cut_kernel<<<1, 1, 0, s>>>(nodes, wide, n_leaves, tl, n_tl);
     pred::treelet_label_kernel<<<(n_leaves + 255) / 256, 256, 0, s>>>(tl, n_tl, xtri, n_leaves, tri_class);
+}
+
+void pred_treelets_batch(const BatchScene* scenes, uint32_t n_scenes, uint32_t n_tris, const crt_bvh_node* nodes,
+                         const float4* wide, const float4* xtri, Treelet* tl, uint32_t* n_tl, uint8_t* tri_class,
+                         cudaStream_t s) {
+    if (n_scenes == 0) return;
+    pred::treelet_cut_batch_kernel<<<n_scenes, 32, 0, s>>>(scenes, nodes, wide, tl, n_tl);
+    pred::treelet_label_batch_kernel<<<(n_tris + 255) / 256, 256, 0, s>>>(scenes, n_scenes, n_tris, tl, n_tl, xtri,
+                                                                          tri_class);
+}
+
+void pred_classes_of_hits(const PredictorDev& P, const crt_hit* hits, uint32_t n, uint16_t* out, cudaStream_t s) {
+    if (n == 0) return;
+    pred::classes_of_hits_kernel<<<(n + 255) / 256, 256, 0, s>>>(P, hits, n, out);
 }
 
 size_t bounce_scratch_bytes(uint32_t n_prim) {

@@ -47,14 +47,22 @@ constexpr size_t kHalfs = hEd + kEd * kEmb;
 
 }  // namespace pred
 
+struct BatchScene;
+
 struct PredictorDev {
     float* master = nullptr;
     float* m = nullptr;
     float* v = nullptr;
     float* grad = nullptr;
     __half* w16 = nullptr;
-    const uint8_t* tri_class = nullptr;   // triangle id -> treelet class
+    const uint8_t* tri_class = nullptr;   // triangle id -> treelet class (a batch: concatenated scenes)
     uint32_t n_tris = 0;
+    // A predictor over a batch of scenes: the batch's scene table.  A ray
+    // belongs to the scene whose ray range holds it; its features are taken
+    // on that scene's box, with the origin cell hashed by the scene index;
+    // its class is a treelet of that scene (or miss).  n_scenes 0: one BVH.
+    const BatchScene* scenes = nullptr;
+    uint32_t n_scenes = 0;
 };
 
 // A subtree of the BVH cut: its box, traversal reference and leaf range.
@@ -69,6 +77,9 @@ struct Treelet {
 static_assert(sizeof(Treelet) == 48, "treelet record");
 
 void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s);
+// Sets the kernels' shared-memory attributes (done again on first use; call
+// before capturing predictor work into a graph).
+cudaError_t pred_prepare();
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
                        uint16_t* classes, float miss_threshold, uint32_t* err, cudaStream_t s);
 cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n_rays,
@@ -81,10 +92,19 @@ void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s);
 // sort of 32-bit keys); order[k] = index of the k-th ray.  scratch holds
 // pred_order_scratch_bytes(n).
 size_t pred_order_scratch_bytes(uint32_t n);
-void pred_order(const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes, uint32_t n, uint32_t* order,
-                void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
+// With P.n_scenes != 0 (a batch) the key is (scene, predicted class, origin
+// cell on a 16^3 grid of the scene's box, direction bin's first coordinate).
+void pred_order(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes,
+                uint32_t n, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const float4* xtri, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
+// Every scene of a batch cut into <= 127 treelets: scene k's at tl + 128 k,
+// their count at n_tl[k]; tri_class of the concatenated triangles.
+void pred_treelets_batch(const BatchScene* scenes, uint32_t n_scenes, uint32_t n_tris, const crt_bvh_node* nodes,
+                         const float4* wide, const float4* xtri, Treelet* tl, uint32_t* n_tl, uint8_t* tri_class,
+                         cudaStream_t s);
+// Class of each hit of a batch's rays (treelet of its triangle in the ray's scene, or miss).
+void pred_classes_of_hits(const PredictorDev& P, const crt_hit* hits, uint32_t n, uint16_t* out, cudaStream_t s);
 // Failure-detection probe of the predictor kernels' MMA wait (one CTA, one
 // MMA or none): out[128] receives 16.0 per thread when complete != 0.
 cudaError_t tc_wait_probe(int complete, uint32_t limit, uint32_t* err, float* out, cudaStream_t s);

@@ -222,7 +222,9 @@ __global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32
 
 // Many scenes in one launch: ray i belongs to the scene whose ray range holds
 // it and is traced against that scene's BVH (same walk as above).
-template <bool ANY, bool WT, int STACK, int BLOCK>
+// SEED: learned seeding in a batch; base.pred_class holds every ray's class,
+// base.treelets / base.n_treelets every scene's cut (scene k's at 128 k / k).
+template <bool ANY, bool WT, int STACK, bool SEED, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, const BatchScene* __restrict__ scenes,
                                                             uint32_t n_scenes, uint32_t n_rays_total) {
     __shared__ uint32_t s_ray_off[kMaxBatchScenes + 1];
@@ -245,7 +247,11 @@ __global__ void __launch_bounds__(BLOCK) trace_batch_kernel(TraceParams base, co
     p.xtri = base.xtri + 3 * static_cast<size_t>(sc.tri_off);
     p.n_nodes = 2 * sc.n_tris - 1;
     p.abs_eps = sc.abs_eps;
-    trace_ray<ANY, WT, STACK, false, 0>(p, i);
+    if (SEED) {
+        p.treelets = base.treelets + 128 * static_cast<size_t>(lo);
+        p.n_treelets = base.n_treelets + lo;
+    }
+    trace_ray<ANY, WT, STACK, SEED, 0>(p, i);
 }
 
 // ------------------------------------------------------ ray ordering
@@ -443,8 +449,13 @@ static void launch_batch_b(const TraceParams& p, const BatchScene* scenes, uint3
                            bool deep, cudaStream_t s) {
     const uint32_t grid = (n_rays + BLOCK - 1) / BLOCK;
     if (grid == 0) return;
-    if (deep) trace_batch_kernel<ANY, WT, 1024, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
-    else trace_batch_kernel<ANY, WT, 64, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+    if (p.pred_class) {
+        if (deep) trace_batch_kernel<ANY, WT, 1024, true, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+        else trace_batch_kernel<ANY, WT, 64, true, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+    } else {
+        if (deep) trace_batch_kernel<ANY, WT, 1024, false, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+        else trace_batch_kernel<ANY, WT, 64, false, BLOCK><<<grid, BLOCK, 0, s>>>(p, scenes, n_scenes, n_rays);
+    }
 }
 
 template <bool ANY, bool WT>

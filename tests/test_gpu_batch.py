@@ -103,3 +103,50 @@ def test_batch_sorted_rays_same_hits(ctx, batch_data, flags):
         assert torch.equal(_i32(h0)[:, 0] == -1, _i32(h2)[:, 0] == -1)
     else:
         assert torch.equal(_i32(h0), _i32(h2))
+
+
+def test_batch_learned_modes_give_the_plain_hits(ctx):
+    """A predictor over every scene of a batch (crt_batch_predictor_create):
+    trained online on the batch's own exact hits, it lowers its loss; traces
+    ordered by its prediction (CRT_TRACE_PREDICTOR_ORDER), seeded by it
+    (CRT_TRACE_USE_PREDICTOR) or both, direct or replayed from the batch's
+    CUDA graph, return the plain batch trace's hits bit for bit, for both
+    triangle predicates and closest or any hit."""
+    sizes = [30000, 1, 5000, 60000, 2]
+    n_rays = [20000, 30, 6000, 40000, 10]
+    scenes = [S.clustered_soup(n, 16, 0.03, 0.004, 0.5, seed=40 + k) if n > 2 else S.uniform_soup(n, seed=40 + k)
+              for k, n in enumerate(sizes)]
+    rays = [S.sphere_rays(m, seed=50 + k) for k, m in enumerate(n_rays)]
+    tris = torch.from_numpy(np.concatenate(scenes)).cuda()
+    r = torch.from_numpy(np.concatenate(rays)).cuda()
+    b = crt.Batch(ctx, sizes, n_rays, models=S.identity_models(1))
+    b.build(tris)
+    total = int(sum(n_rays))
+    plain = torch.empty((total, 4), dtype=torch.float32, device="cuda")
+    b.trace(r, plain, crt.TRI_WATERTIGHT)
+    pred = crt.Predictor(ctx, b, seed=4, train_stride=1, batch=8192)
+    assert pred.info()["treelets"] > 100
+    truth = pred.classes_of_hits(plain)
+    pc = plain[:, 0].view(torch.int32).cpu().numpy()
+    assert ((truth == 127) == (pc == -1)).all()
+    losses = [pred.train(r, plain, offset=0) for _ in range(8)]
+    assert losses[-1] < losses[0]
+    got = torch.empty_like(plain)
+    for pf in (crt.TRI_WATERTIGHT, crt.TRI_REFERENCE):
+        ref = torch.empty_like(plain)
+        b.trace(r, ref, pf)
+        for lf in (crt.PREDICTOR_ORDER, crt.USE_PREDICTOR, crt.PREDICTOR_ORDER | crt.USE_PREDICTOR):
+            b.trace(r, got, pf | lf)
+            assert torch.equal(_i32(got), _i32(ref)), (pf, lf)
+    anyref = torch.empty_like(plain)
+    b.trace(r, anyref, crt.TRI_WATERTIGHT | crt.TRACE_ANY)
+    b.trace(r, got, crt.TRI_WATERTIGHT | crt.TRACE_ANY | crt.PREDICTOR_ORDER | crt.USE_PREDICTOR)
+    assert torch.equal(_i32(got)[:, 0] == -1, _i32(anyref)[:, 0] == -1)
+    # build + learned trace replayed from the graph; a rebuild needs a retarget
+    for _ in range(2):
+        used = b.run(tris, r, got, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER, graph=True)
+        pred.retarget()
+        assert torch.equal(_i32(got), _i32(plain))
+    assert used
+    pred.free()
+    b.free()
