@@ -860,16 +860,113 @@ def run_dynamic_experiment(ctx, torch, crt, dev, args, frames=60):
             out["bounce_trace_ms"] = compare
         return out
 
+    def animate_batch(learned):
+        """The same frames on the batched persistent graph: a one-scene
+        crt_batch with room for 2 bounce rays per pixel.  Per frame the
+        batch's CUDA graph replays the rebuild (batched Morton, sort, PLOC and
+        layout launches) and the primary trace; crt_batch_bounce_rays makes
+        the bounce rays, crt_batch_set_ray_counts switches the batch to them,
+        and crt_batch_trace traces them, in predicted-treelet order with the
+        predictor retrained on the frame's hits (learned) or plain."""
+        b = crt.Batch(ctx, [n], [2 * W * H], models=S.identity_models(1))
+        bounce = torch.empty((2 * W * H, 8), dtype=torch.float32, device=dev)
+        hb = torch.empty((2 * W * H, 4), dtype=torch.float32, device=dev)
+        hb_cmp = torch.empty((2 * W * H, 4), dtype=torch.float32, device=dev)
+        ctx.raygen(cam, W, H, out=prim)
+        tris.copy_(base)
+        b.set_ray_counts([W * H])
+        b.run(tris, prim, hp, crt.TRI_WATERTIGHT, graph=True)
+        pred = crt.Predictor(ctx, b, seed=3) if learned else None
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        frame_ms, run_ms, bounce_ms, rays_traced, compare = [], [], [], [], []
+        identical, graph_frames = True, 0
+        for f in range(frames):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tris[:, [1, 5, 9]] = y0 + 0.01 * torch.sin(2 * np.pi * f / 60 + 7 * x0)
+            b.set_ray_counts([W * H])
+            stream.wait_stream(torch.cuda.current_stream(dev))
+            e[0].record(stream)
+            graph_frames += int(b.run(tris, prim, hp, crt.TRI_WATERTIGHT, graph=True))
+            e[1].record(stream)
+            hv = hp.view(torch.int32).to(torch.int64)
+            digest = int(((hv[:, 0] * 1000003 + hv[:, 1]) * (torch.arange(W * H, device=dev) + 1)).sum().item())
+            identical = identical and primary_sums.get(f) == digest
+            n_hits = int((hp[:, 0].view(torch.int32) != -1).sum().item())
+            nb = max(2 * n_hits, 1)
+            br, hs = bounce[:nb], hb[:nb]
+            b.bounce_rays(0, prim, hp, nb, seed=100 + f, out=br)
+            b.set_ray_counts([nb])
+            ts = time.perf_counter()
+            if learned:
+                pred.retarget()
+                b.trace(br, hs, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER)
+                torch.cuda.synchronize()
+                bounce_ms.append((time.perf_counter() - ts) * 1e3)
+                pred.train(br, hs, offset=f % 20)
+            else:
+                b.trace(br, hs, crt.TRI_WATERTIGHT)
+                torch.cuda.synchronize()
+                bounce_ms.append((time.perf_counter() - ts) * 1e3)
+            torch.cuda.synchronize()
+            frame_ms.append((time.perf_counter() - t0) * 1e3)
+            run_ms.append(e[0].elapsed_time(e[1]))
+            rays_traced.append(W * H + nb)
+            if learned and (f % 15 == 0 or f == frames - 1):
+                # the same bounce rays through the batch plain, seeded and sorted without the network
+                row = {"rays": int(nb), "predictor_ordered_ms": round(bounce_ms[-1], 3)}
+                for name, fl in (("plain_ms", 0), ("seeded_ms", crt.USE_PREDICTOR),
+                                 ("sorted_no_network_ms", crt.SORT_RAYS)):
+                    tp = time.perf_counter()
+                    b.trace(br, hb_cmp[:nb], crt.TRI_WATERTIGHT | fl)
+                    torch.cuda.synchronize()
+                    row[name] = round((time.perf_counter() - tp) * 1e3, 3)
+                    identical = identical and bool(torch.equal(hb_cmp[:nb].view(torch.int32), hs.view(torch.int32)))
+                compare.append(row)
+        if pred is not None:
+            pred.free()
+        b.set_ray_counts([W * H])
+        bms = []
+        for _ in range(3):   # the batched rebuild alone, host-timed around the call
+            torch.cuda.synchronize()
+            ts = time.perf_counter()
+            b.build(tris)
+            bms.append((time.perf_counter() - ts) * 1e3)
+        b.free()
+        fm = np.array(frame_ms[1:])
+        out = {"frame_ms_p50": round(float(np.percentile(fm, 50)), 3),
+               "frame_ms_p99": round(float(np.percentile(fm, 99)), 3),
+               "rebuild_and_primary_ms_p50": round(float(np.median(run_ms[1:])), 3),
+               "bounce_trace_ms_p50": round(float(np.median(bounce_ms[1:])), 3),
+               "batch_build_ms": round(float(np.median(bms)), 3),
+               "mrays_s": round(float(sum(rays_traced[1:]) / fm.sum() / 1e3), 1),
+               "graph_replayed_frames": graph_frames,
+               "identical_hits": identical}
+        if learned:
+            out["bounce_trace_ms"] = compare
+        return out
+
     rebuild = animate(refit=False)
     refit = animate(refit=True)
-    return dict(rebuild, **{
+    batch_learned = animate_batch(learned=True)
+    batch_plain = animate_batch(learned=False)
+    return {
         "workload": "16,777,216-tri clustered soup (1024 clusters), 60 animated frames, full rebuild per frame, "
-                    "1920x1080 primary + 2 bounce rays per hit traced in predicted-treelet order, predictor retrained "
-                    "per frame",
+                    "1920x1080 primary + 2 bounce rays per hit; on the batched graph (rebuild + primary replayed, "
+                    "bounce rays traced in predicted-treelet order, predictor retrained per frame) against the same "
+                    "frames with plain bounce traces, and through the single-scene calls",
         "frames": frames,
+        "batched_graph": dict(batch_learned, note="crt_batch of one scene: crt_batch_run replays the captured "
+                              "rebuild + primary trace every frame; bounce rays by crt_batch_bounce_rays, traced by "
+                              "crt_batch_trace with CRT_TRACE_PREDICTOR_ORDER after crt_predictor_retarget, then "
+                              "crt_predictor_train on the frame's hits; identical_hits: every frame's primary hits "
+                              "equal the single-scene run's and every sampled learned bounce trace equals plain"),
+        "batched_graph_plain": dict(batch_plain, note="the same frames, bounce rays traced plain, no predictor"),
+        "learned_vs_plain_frame": round(batch_plain["frame_ms_p50"] / batch_learned["frame_ms_p50"], 3),
+        "single_scene": rebuild,
         "refit": dict(refit, note="the same 60 frames with crt_refit of the frame-0 tree instead of a rebuild; "
                                   "identical_hits compares every frame's primary hits with the rebuild run's"),
-    })
+    }
 
 
 def sah_cost(nodes, ci=1.2):

@@ -474,6 +474,19 @@ crt_status crt_batch_trace(crt_ctx* ctx, crt_batch* batch, const crt_ray* rays, 
  * reports whether the graph path ran. */
 crt_status crt_batch_run(crt_ctx* ctx, crt_batch* batch, const crt_triangle* tris, const crt_ray* rays, uint32_t flags,
                          crt_hit* hits, int use_graph, int* graph_used);
+/* New per-scene ray counts for the following traces (no counterpart in the
+ * reference): ray_counts[n_scenes], in total at most the rays the batch was
+ * created with; the scenes' rays stay concatenated in scene order.  A graph
+ * that crt_batch_run captured replays only with the counts it was captured
+ * with (other counts capture a new one), so a frame can switch between a
+ * fixed primary ray set (build + trace replayed) and a varying secondary one
+ * (crt_batch_trace). */
+crt_status crt_batch_set_ray_counts(crt_ctx* ctx, crt_batch* batch, const uint32_t* ray_counts);
+/* crt_bounce_rays over one scene of a built batch: primary rays and their
+ * hits (scene-local triangle ids) in, n_out cosine bounce rays out; device
+ * memory. */
+crt_status crt_batch_bounce_rays(crt_ctx* ctx, crt_batch* batch, uint32_t scene, const crt_ray* primary,
+                                 const crt_hit* hits, uint32_t n_primary, uint32_t n_out, uint32_t seed, crt_ray* out);
 crt_status crt_batch_copy_nodes(crt_ctx* ctx, const crt_batch* batch, uint32_t scene, crt_bvh_node* dst);
 /* info[0] = triangles, [1] = rays, [2] = PLOC iterations, [3] = first triangle (concatenated index). */
 crt_status crt_batch_scene_info(const crt_batch* batch, uint32_t scene, uint32_t info[4]);

@@ -51,6 +51,7 @@ EXPORTS = [
     "crt_predictor_gradients", "crt_predictor_params", "crt_predictor_info", "crt_bounce_rays", "crt_trace_seeded",
     "crt_batch_create", "crt_batch_free", "crt_batch_set_models", "crt_batch_set_config", "crt_batch_get_config",
     "crt_batch_build", "crt_batch_trace", "crt_batch_run", "crt_batch_copy_nodes", "crt_batch_scene_info",
+    "crt_batch_set_ray_counts", "crt_batch_bounce_rays",
     "crt_batch_autotune", "crt_shade", "crt_render_frame", "crt_refit", "crt_optimize", "crt_bvh_from_nodes",
     "crt_validate_nodes", "crt_obj_parse",
     "crt_triangles_from_indexed", "crt_selftest_wait", "crt_selftest_tc_wait", "crt_last_trace_timing",
@@ -140,6 +141,8 @@ def lib():
             "crt_batch_run": ([vp, vp, vp, vp, u32, vp, i32, vp], i32),
             "crt_batch_copy_nodes": ([vp, vp, u32, vp], i32),
             "crt_batch_scene_info": ([vp, u32, vp], i32),
+            "crt_batch_set_ray_counts": ([vp, vp, vp], i32),
+            "crt_batch_bounce_rays": ([vp, vp, u32, vp, vp, u32, u32, u32, vp], i32),
             "crt_batch_autotune": ([vp, vp, vp, vp, u32, vp, vp, vp], i32),
             "crt_shade": ([vp, vp, vp, vp, u32, vp, vp], i32),
             "crt_render_frame": ([vp, vp, vp, u32, u32, u32, vp, vp], i32),
@@ -358,6 +361,24 @@ class Batch:
         _check(lib().crt_batch_run(self.ctx.handle, self.handle, _ptr(tris), _ptr(rays), flags, _ptr(hits),
                                    1 if graph else 0, C.byref(used)))
         return bool(used.value)
+
+    def set_ray_counts(self, ray_counts):
+        """Per-scene ray counts for the following traces (at most the batch's
+        rays in total); a captured graph replays only with its own counts."""
+        rc = np.ascontiguousarray(ray_counts, np.uint32)
+        assert rc.shape == (self.n_scenes,)
+        _check(lib().crt_batch_set_ray_counts(self.ctx.handle, self.handle, _ptr(rc)))
+        self.ray_counts = rc
+
+    def bounce_rays(self, scene: int, primary, hits, n_out: int, seed: int = 7, out=None):
+        """crt_batch_bounce_rays: n_out cosine bounce rays from scene's primary hits."""
+        self.ctx._after_torch()
+        if out is None:
+            import torch
+            out = torch.empty((n_out, 8), dtype=torch.float32, device=primary.device)
+        _check(lib().crt_batch_bounce_rays(self.ctx.handle, self.handle, scene, _ptr(primary), _ptr(hits),
+                                           int(primary.shape[0]), n_out, seed, _ptr(out)))
+        return out
 
     def nodes(self, scene: int):
         n = int(self.tri_counts[scene])

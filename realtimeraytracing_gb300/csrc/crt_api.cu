@@ -1715,8 +1715,9 @@ struct crt_batch {
     bool built = false;                  // a build has completed
     uint32_t n_scenes = 0;
     uint32_t n_tris = 0, n_rays = 0;
+    uint32_t ray_cap = 0;                // rays reserved at creation; crt_batch_set_ray_counts stays within it
     std::vector<crt::BatchScene> hs;
-    std::vector<uint32_t> tri_off, ray_off;
+    std::vector<uint32_t> tri_off;
     uint32_t n_chunks = 0, lb_cap = 0, max_n = 0, max_iters = 0;
     crt_config cfg{};
     DevBuf scenes, seg_off, seg_hist, chunks, states, models, err;
@@ -1731,6 +1732,12 @@ struct crt_batch {
     const void* g_hits = nullptr;
     uint32_t g_flags = 0;
     crt_config g_cfg{};
+    std::vector<uint32_t> g_counts;      // per-scene ray counts the graph was captured with
+    std::vector<uint32_t> ray_counts() const {
+        std::vector<uint32_t> c(n_scenes);
+        for (uint32_t k = 0; k < n_scenes; ++k) c[k] = hs[k].n_rays;
+        return c;
+    }
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -1869,9 +1876,11 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
 
 // Scratch of CRT_TRACE_SORT_RAYS for a batch, reserved outside graph capture.
 crt_status batch_order_buffers(crt_batch* bt, uint32_t flags) {
-    if (!(flags & CRT_TRACE_SORT_RAYS) || bt->n_rays <= 1) return CRT_OK;
-    CRT_TRY(bt->ray_order.reserve(4ull * bt->n_rays));
-    CRT_TRY(bt->ray_order_scratch.reserve(crt::ray_order_scratch_bytes(bt->n_rays)));
+    // sized for the batch's ray capacity, so a later crt_batch_set_ray_counts
+    // never moves a buffer that a captured graph points at
+    if (!(flags & CRT_TRACE_SORT_RAYS) || bt->ray_cap <= 1) return CRT_OK;
+    CRT_TRY(bt->ray_order.reserve(4ull * bt->ray_cap));
+    CRT_TRY(bt->ray_order_scratch.reserve(crt::ray_order_scratch_bytes(bt->ray_cap)));
     return CRT_OK;
 }
 
@@ -1936,6 +1945,7 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
     if (nt >= (1ull << 30) || nr >= (1ull << 31)) { delete bt; return fail(CRT_ERR_INVALID_ARG, "crt_batch_create: too large"); }
     bt->n_tris = static_cast<uint32_t>(nt);
     bt->n_rays = static_cast<uint32_t>(nr);
+    bt->ray_cap = bt->n_rays;
     bt->hs = hs;
     bt->n_chunks = static_cast<uint32_t>(chunks.size() / 4);
     bt->lb_cap = static_cast<uint32_t>(lb);
@@ -2058,7 +2068,7 @@ crt_status crt_batch_predictor_create(crt_ctx* x, crt_batch* bt, const crt_predi
     pr->batch_nodes = bt->nodes.as<crt_bvh_node>();
     pr->batch_n_scenes = bt->n_scenes;
     pr->batch_n_tris = bt->n_tris;
-    const size_t n_rays = bt->n_rays;
+    const size_t n_rays = bt->ray_cap;
     crt_status s = pr->params.reserve(4 * sizeof(float) * crt::pred::kParams);
     if (s == CRT_OK) s = pr->w16.reserve(sizeof(__half) * crt::pred::kHalfs);
     if (s == CRT_OK) s = pr->scratch.reserve(16);
@@ -2106,8 +2116,12 @@ crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
     if (graph_used) *graph_used = 0;
     if (bt->max_iters + 2 > 64) bt->cfg.stack_depth = 1024;
     if (use_graph) {
+        // the graph bakes in the ray count of every launch; the scene table it
+        // reads holds the current counts, so it replays only with the counts
+        // it was captured with
         const bool same = bt->graph && bt->g_tris == tris && bt->g_rays == rays && bt->g_hits == hits &&
-                          bt->g_flags == flags && std::memcmp(&bt->g_cfg, &bt->cfg, sizeof(crt_config)) == 0;
+                          bt->g_flags == flags && std::memcmp(&bt->g_cfg, &bt->cfg, sizeof(crt_config)) == 0 &&
+                          bt->g_counts == bt->ray_counts();
         if (!same) {
             bt->drop_graph();
             cudaGraph_t g = nullptr;
@@ -2123,6 +2137,7 @@ crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
                 bt->graph = nullptr;
             } else {
                 bt->g_tris = tris; bt->g_rays = rays; bt->g_hits = hits; bt->g_flags = flags; bt->g_cfg = bt->cfg;
+                bt->g_counts = bt->ray_counts();
             }
         }
         if (bt->graph) {
@@ -2136,6 +2151,53 @@ crt_status crt_batch_run(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
     CRT_TRY(batch_enqueue(x, bt, tris, rays, flags, hits, nullptr));
     CRT_TRY(batch_check(x, bt));
     bt->built = true;
+    return CRT_OK;
+}
+
+crt_status crt_batch_set_ray_counts(crt_ctx* x, crt_batch* bt, const uint32_t* ray_counts) {
+    if (!x || !bt || !ray_counts) return fail(CRT_ERR_INVALID_ARG, "crt_batch_set_ray_counts: null argument");
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < bt->n_scenes; ++k) total += ray_counts[k];
+    if (total > bt->ray_cap)
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_set_ray_counts: %llu rays exceed the batch's %u",
+                    static_cast<unsigned long long>(total), bt->ray_cap);
+    CRT_CUDA(cudaSetDevice(x->device));
+    // the device table also holds what the last build wrote (slack, iterations): take it, change the ray fields
+    CRT_CUDA(cudaMemcpyAsync(bt->hs.data(), bt->scenes.p, sizeof(crt::BatchScene) * bt->n_scenes, cudaMemcpyDeviceToHost,
+                             x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    uint32_t off = 0;
+    for (uint32_t k = 0; k < bt->n_scenes; ++k) {
+        bt->hs[k].ray_off = off;
+        bt->hs[k].n_rays = ray_counts[k];
+        off += ray_counts[k];
+    }
+    CRT_CUDA(cudaMemcpyAsync(bt->scenes.p, bt->hs.data(), sizeof(crt::BatchScene) * bt->n_scenes, cudaMemcpyHostToDevice,
+                             x->stream));
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
+    bt->n_rays = off;
+    return CRT_OK;
+}
+
+crt_status crt_batch_bounce_rays(crt_ctx* x, crt_batch* bt, uint32_t scene, const crt_ray* primary, const crt_hit* hits,
+                                 uint32_t n_primary, uint32_t n_out, uint32_t seed, crt_ray* out) {
+    if (!x || !bt || !primary || !hits || !out || scene >= bt->n_scenes)
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_bounce_rays: bad argument");
+    if (!bt->built) return fail(CRT_ERR_INVALID_ARG, "crt_batch_bounce_rays: build the batch first");
+    if (!is_device_ptr(primary) || !is_device_ptr(hits) || !is_device_ptr(out))
+        return fail(CRT_ERR_INVALID_ARG, "crt_batch_bounce_rays: device memory only");
+    CRT_TRY(check_aligned16(primary, "crt_batch_bounce_rays: primary rays"));
+    CRT_TRY(check_aligned16(hits, "crt_batch_bounce_rays: hits"));
+    CRT_TRY(check_aligned16(out, "crt_batch_bounce_rays: rays"));
+    CRT_CUDA(cudaSetDevice(x->device));
+    if (n_out == 0) return CRT_OK;
+    const crt::BatchScene& sc = bt->hs[scene];
+    CRT_TRY(x->pos.reserve(crt::bounce_scratch_bytes(n_primary)));
+    crt::launch_bounce(primary, hits, n_primary, bt->xtri.as<float4>() + 3 * static_cast<size_t>(sc.tri_off),
+                       bt->inv_perm.as<uint32_t>() + sc.tri_off, sc.n_tris, n_out, seed, out, x->pos.as<uint32_t>(),
+                       x->stream);
+    CRT_CUDA(cudaGetLastError());
+    CRT_CUDA(cudaStreamSynchronize(x->stream));
     return CRT_OK;
 }
 

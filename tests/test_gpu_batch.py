@@ -150,3 +150,69 @@ def test_batch_learned_modes_give_the_plain_hits(ctx):
     assert used
     pred.free()
     b.free()
+
+
+def test_batch_ray_counts_graph_key_and_bounce_rays(ctx):
+    """crt_batch_set_ray_counts: traces of fewer rays per scene (within the
+    batch's capacity) equal the single-scene traces of the same rays; the
+    graph captured with one set of counts replays when those counts return and
+    is recaptured for others; crt_batch_bounce_rays equals crt_bounce_rays on
+    the scene built alone, bit for bit; a learned trace after a count change
+    keeps the plain hits; counts above the capacity are refused."""
+    sizes = [20000, 3, 9000]
+    cap = [12000, 40, 8000]
+    scenes = [S.clustered_soup(n, 8, 0.05, 0.004, 0.5, seed=60 + k) if n > 3 else S.uniform_soup(n, seed=60 + k)
+              for k, n in enumerate(sizes)]
+    rays = [S.sphere_rays(m, seed=70 + k) for k, m in enumerate(cap)]
+    tris = torch.from_numpy(np.concatenate(scenes)).cuda()
+    r_full = torch.from_numpy(np.concatenate(rays)).cuda()
+    b = crt.Batch(ctx, sizes, cap, models=S.identity_models(1))
+    h_full = torch.empty((r_full.shape[0], 4), dtype=torch.float32, device="cuda")
+    assert b.run(tris, r_full, h_full, crt.TRI_WATERTIGHT, graph=True)
+    singles = [ctx.build(sc, models=S.identity_models(1)) for sc in scenes]
+    # fewer rays per scene, one of them none at all
+    small = [5000, 0, 7999]
+    r_small = torch.from_numpy(np.concatenate([rays[k][:m] for k, m in enumerate(small)])).cuda()
+    h_small = torch.empty((r_small.shape[0], 4), dtype=torch.float32, device="cuda")
+    b.set_ray_counts(small)
+    assert b.scene_info(2)["rays"] == 7999
+    for flags in (crt.TRI_WATERTIGHT, crt.TRI_REFERENCE, crt.TRI_WATERTIGHT | crt.SORT_RAYS):
+        b.trace(r_small, h_small, flags)
+        got = h_small.cpu().numpy()
+        off = 0
+        for k, m in enumerate(small):
+            if m:
+                ref = ctx.trace(singles[k], rays[k][:m], flags & ~crt.SORT_RAYS)
+                np.testing.assert_array_equal(got[off:off + m].view(np.uint32), ref.view(np.uint32), err_msg=f"{k} {flags}")
+            off += m
+    # the graph of the full counts replays once they are back
+    b.set_ray_counts(cap)
+    h2 = torch.empty_like(h_full)
+    assert b.run(tris, r_full, h2, crt.TRI_WATERTIGHT, graph=True)
+    assert torch.equal(_i32(h2), _i32(h_full))
+    with pytest.raises(crt.CrtError):
+        b.set_ray_counts([cap[0] + cap[1] + cap[2] + 1, 0, 0])
+    # bounce rays from scene 2's primary hits, as the single-scene call makes them
+    off2 = cap[0] + cap[1]
+    prim2, hit2 = r_full[off2:], h_full[off2:]
+    n_out = 2 * int((hit2[:, 0].view(torch.int32) != -1).sum().item())
+    assert n_out > 400
+    got = b.bounce_rays(2, prim2, hit2, n_out, seed=5)
+    want = torch.empty_like(got)
+    ctx.bounce_rays(singles[2], prim2, hit2, n_out, seed=5, out=want)
+    assert torch.equal(_i32(got), _i32(want))
+    # a learned trace of those bounce rays as the batch's only rays
+    b.set_ray_counts([0, 0, n_out])
+    pred = crt.Predictor(ctx, b, seed=2, train_stride=1, batch=4096)
+    plain = torch.empty((n_out, 4), dtype=torch.float32, device="cuda")
+    b.trace(got, plain, crt.TRI_WATERTIGHT)
+    pred.train(got, plain, offset=0)
+    learned = torch.empty_like(plain)
+    b.trace(got, learned, crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER | crt.USE_PREDICTOR)
+    assert torch.equal(_i32(learned), _i32(plain))
+    ref = ctx.trace(singles[2], got.cpu().numpy(), crt.TRI_WATERTIGHT)
+    np.testing.assert_array_equal(plain.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+    pred.free()
+    for s_ in singles:
+        s_.free()
+    b.free()
