@@ -1725,6 +1725,7 @@ struct crt_batch {
     DevBuf node_box, node_kids, pf, clus_a, clus_b, it, ploc_lb, hist, sort_lb;
     DevBuf nodes, wide, wide_wt, depth_odd, xtri, xtri_sorted, inv_perm;
     DevBuf ray_order, ray_order_scratch;  // CRT_TRACE_SORT_RAYS
+    DevBuf pool_counter;                  // the persistent trace's ray counter
     bool models_set = false;
     cudaGraphExec_t graph = nullptr;
     const void* g_tris = nullptr;
@@ -1801,8 +1802,15 @@ crt_status batch_trace_enqueue(crt_ctx* x, crt_batch* bt, const crt_ray* rays, u
                               s);
         p.order = bt->ray_order.as<uint32_t>();
     }
-    crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
-                            flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block), deep, s);
+    // large closest-hit batches: the persistent ray pool, each lane walking
+    // its ray's scene (as trace_device does for one scene)
+    if (!(flags & CRT_TRACE_ANY) && !p.pred_class && bt->n_rays >= kPoolMinRays)
+        crt::launch_trace_batch_pool(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, flags & CRT_TRI_WATERTIGHT, deep,
+                                     bt->pool_counter.as<uint32_t>(), s);
+    else
+        crt::launch_trace_batch(p, bt->scenes.as<crt::BatchScene>(), bt->n_scenes, bt->n_rays,
+                                flags & (CRT_TRACE_ANY | CRT_TRI_WATERTIGHT), static_cast<int>(bt->cfg.trace_block), deep,
+                                s);
     CRT_CUDA(cudaGetLastError());
     return CRT_OK;
 }
@@ -1978,6 +1986,7 @@ crt_status crt_batch_create(crt_ctx* x, const uint32_t* tri_counts, const uint32
     R(bt->depth_odd, N);
     R(bt->xtri, 48ull * N);
     R(bt->xtri_sorted, 48ull * N);
+    R(bt->pool_counter, 16);
     if (st != CRT_OK) { crt_batch_free(bt); return st; }
     std::vector<uint32_t> seg(n_scenes + 1), segh(256, 0);
     for (uint32_t k = 0; k < n_scenes; ++k) { seg[k] = hs[k].tri_off; segh[k] = hs[k].n_tris; }
@@ -2009,7 +2018,7 @@ crt_status crt_batch_free(crt_batch* bt) {
                       &bt->codes_a, &bt->codes_b, &bt->vals_a, &bt->vals_b, &bt->codes, &bt->perm_global,
                       &bt->perm_local, &bt->node_box, &bt->node_kids, &bt->pf, &bt->clus_a, &bt->clus_b, &bt->it,
                       &bt->ploc_lb, &bt->hist, &bt->sort_lb, &bt->nodes, &bt->wide, &bt->wide_wt, &bt->depth_odd, &bt->xtri, &bt->ray_order, &bt->ray_order_scratch,
-                      &bt->inv_perm, &bt->xtri_sorted};
+                      &bt->inv_perm, &bt->xtri_sorted, &bt->pool_counter};
     for (DevBuf* b : bufs) b->release();
     delete bt;
     return CRT_OK;

@@ -463,11 +463,13 @@ __global__ void __launch_bounds__(256) leaf_init_kernel(const crt_triangle* __re
 // next id).
 //
 // Boxes of positions [s-2R, e+2R) are staged in shared memory as separate
-// min/max coordinate arrays.  Each thread keeps the boxes of its 4
-// consecutive positions in registers and walks the 2R+4 boxes around them
-// once, so a box read serves up to 4 area evaluations.  The threads of a warp
-// read at a stride of 4 positions; the index swizzle ploc_swz makes those
-// reads free of bank conflicts.
+// min/max coordinate arrays, position s-2R+w at index w; window entries
+// outside [0, n) hold an infinite box (area +inf, never chosen under the strict
+// minimum, as the reference never considers them).  Each thread keeps the
+// boxes of its 4 consecutive positions in registers and walks the 2R+4 boxes
+// around them once, reading two consecutive entries per 8-byte shared load
+// (an even R keeps them aligned), so one load serves up to 8 area
+// evaluations.
 //
 // The search compares areas computed from fminf/fmaxf boxes; those differ
 // from the std::min/max boxes only in the sign of a zero, which changes no
@@ -484,10 +486,10 @@ __device__ __forceinline__ float sa_merged(float4 amn, float4 amx, float4 bmn, f
 }
 
 template <int TILE, int BLOCK, int MAXR>
-struct PlocSmem {
+struct __align__(16) PlocSmem {
     static_assert(TILE == 4 * BLOCK, "four nearest-neighbour positions per thread");
     static constexpr int kWin = TILE + 2 * MAXR;  // positions [s-2R, e+2R), e - s <= TILE - 2R
-    static_assert(kWin % 32 == 0, "the swizzle stays inside 32-entry rows");
+    static_assert(kWin % 4 == 0, "aligned coordinate arrays");
     float mnx[kWin], mny[kWin], mnz[kWin], mxx[kWin], mxy[kWin], mxz[kWin];
     uint32_t id[kWin], lc[kWin];
     uint32_t nn[TILE];  // nearest neighbour of position s - R + i
@@ -495,50 +497,67 @@ struct PlocSmem {
     unsigned long long prefix;
 };
 
-// Bank-conflict-free index of window entry w for reads at a stride of 4.
-__device__ __forceinline__ int ploc_swz(int w) { return w ^ ((w >> 5) & 3); }
+__device__ __forceinline__ float2 lds2(const float* a) { return *reinterpret_cast<const float2*>(a); }
 
 // Nearest neighbours of this thread's positions q0..q0+3, q0 = s - R + 4t.
-// RC > 0: the radius is the compile-time RC; RC == 0: runtime radius R.
+// RC > 0: the radius is the compile-time RC (even); RC == 0:
+// runtime radius R, scalar loads.
 template <int RC, int TILE, int BLOCK, int MAXR>
 __device__ __forceinline__ void ploc_nearest(PlocSmem<TILE, BLOCK, MAXR>& S, int s, int e, int n, int R_rt) {
     const int R = RC > 0 ? RC : R_rt;
     const int q0 = s - R + 4 * static_cast<int>(threadIdx.x);
+    if (q0 >= e + R) return;  // none of its positions is stored (no barrier in here)
     const int wq = 4 * static_cast<int>(threadIdx.x) + R;  // window index of q0
     float amnx[4], amny[4], amnz[4], amxx[4], amxy[4], amxz[4], best[4];
     int bj[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const int w = ploc_swz(wq + i);
-        amnx[i] = S.mnx[w]; amny[i] = S.mny[w]; amnz[i] = S.mnz[w];
-        amxx[i] = S.mxx[w]; amxy[i] = S.mxy[w]; amxz[i] = S.mxz[w];
+        amnx[i] = S.mnx[wq + i]; amny[i] = S.mny[wq + i]; amnz[i] = S.mnz[wq + i];
+        amxx[i] = S.mxx[wq + i]; amxy[i] = S.mxy[wq + i]; amxz[i] = S.mxz[wq + i];
         best[i] = __int_as_float(0x7F800000);
         bj[i] = q0 + i;
     }
-    auto visit = [&](int d, int i) {
-        const int j = q0 + d;
-        const int w = ploc_swz(wq + d);
-        const float dx = fmaxf(amxx[i], S.mxx[w]) - fminf(amnx[i], S.mnx[w]);
-        const float dy = fmaxf(amxy[i], S.mxy[w]) - fminf(amny[i], S.mny[w]);
-        const float dz = fmaxf(amxz[i], S.mxz[w]) - fminf(amnz[i], S.mnz[w]);
+    // candidate at window offset d (position q0 + d) for own position i
+    auto visit = [&](int d, int i, float bnx, float bny, float bnz, float bxx, float bxy, float bxz) {
+        const float dx = fmaxf(amxx[i], bxx) - fminf(amnx[i], bnx);
+        const float dy = fmaxf(amxy[i], bxy) - fminf(amny[i], bny);
+        const float dz = fmaxf(amxz[i], bxz) - fminf(amnz[i], bnz);
         const float v = 2.0f * (dx * dy + dy * dz + dz * dx);
-        if (static_cast<unsigned>(j) < static_cast<unsigned>(n) && v < best[i]) { best[i] = v; bj[i] = j; }
+        if (v < best[i]) { best[i] = v; bj[i] = q0 + d; }
     };
     if (RC > 0) {
+        static_assert(RC % 2 == 0, "aligned window pairs");
 #pragma unroll
-        for (int d = -RC; d <= RC + 3; ++d)
+        for (int g = -RC; g <= RC + 2; g += 2) {
+            const int w = wq + g;  // even: an 8-byte aligned pair of entries
+            const float2 nx = lds2(S.mnx + w), ny = lds2(S.mny + w), nz = lds2(S.mnz + w);
+            const float2 xx = lds2(S.mxx + w), xy = lds2(S.mxy + w), xz = lds2(S.mxz + w);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int k = d - i;
-                if (k != 0 && k >= -RC && k <= RC) visit(d, i);
+            for (int u = 0; u < 2; ++u) {
+                const int d = g + u;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int k = d - i;
+                    if (k != 0 && k >= -RC && k <= RC)
+                        visit(d, i, u ? nx.y : nx.x, u ? ny.y : ny.x, u ? nz.y : nz.x, u ? xx.y : xx.x,
+                              u ? xy.y : xy.x, u ? xz.y : xz.x);
+                }
             }
+            // keeps the next pair's loads below this pair's work: without it
+            // every load of the unrolled walk is hoisted and the persistent
+            // kernels (80 registers at 3 blocks per SM) spill
+            asm volatile("" ::: "memory");
+        }
     } else {
-        for (int d = -R; d <= R + 3; ++d)
+        for (int d = -R; d <= R + 3; ++d) {
+            const int w = wq + d;
+            const float bnx = S.mnx[w], bny = S.mny[w], bnz = S.mnz[w], bxx = S.mxx[w], bxy = S.mxy[w], bxz = S.mxz[w];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const int k = d - i;
-                if (k != 0 && k >= -R && k <= R) visit(d, i);
+                if (k != 0 && k >= -R && k <= R) visit(d, i, bnx, bny, bnz, bxx, bxy, bxz);
             }
+        }
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -568,9 +587,19 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
     for (int p = lo + threadIdx.x; p < hi; p += BLOCK) {
         const float4 a = __ldcg(cin + 2 * static_cast<size_t>(p));
         const float4 b = __ldcg(cin + 2 * static_cast<size_t>(p) + 1);
-        const int w = ploc_swz(p - wbase);
+        const int w = p - wbase;
         S.mnx[w] = a.x; S.mny[w] = a.y; S.mnz[w] = a.z; S.id[w] = __float_as_uint(a.w);
         S.mxx[w] = b.x; S.mxy[w] = b.y; S.mxz[w] = b.z; S.lc[w] = __float_as_uint(b.w);
+    }
+    {  // window entries of positions outside [0, n): infinite boxes
+        constexpr int kWin = PlocSmem<TILE, BLOCK, MAXR>::kWin;
+        const float inf = __int_as_float(0x7F800000);
+        const int below = lo - wbase, above = hi - wbase;
+        for (int w = threadIdx.x; w < kWin; w += BLOCK) {
+            if (w >= below && w < above) continue;
+            S.mnx[w] = -inf; S.mny[w] = -inf; S.mnz[w] = -inf;
+            S.mxx[w] = inf; S.mxy[w] = inf; S.mxz[w] = inf;
+        }
     }
     __syncthreads();
     switch (R) {
@@ -624,6 +653,10 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
             if (lane == 0) st_relaxed_u64(&lb_cur[0], kPlPrefix | (tv << 31) | tm);
         } else {
             if (lane == 0) st_relaxed_u64(&lb_cur[tile], kPlAgg | (tv << 31) | tm);
+            // Lane l reads the status word of tile k0 - l (32 predecessors per
+            // round trip, nearest first); the sum runs down to the nearest
+            // inclusive prefix.  (Four words per lane was measured slower:
+            // the nearest prefix is usually a few tiles back.)
             long long k0 = static_cast<long long>(tile) - 1;
             SpinBound spin(spin_limit);
             while (true) {
@@ -666,12 +699,12 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
     for (int q = 0; q < IPT; ++q) {
         if (!(flags & (1u << q))) continue;
         const int p = s + static_cast<int>(threadIdx.x) * IPT + q;
-        const int wp = ploc_swz(p - wbase);
+        const int wp = p - wbase;
         float4 mn = make_float4(S.mnx[wp], S.mny[wp], S.mnz[wp], __uint_as_float(S.id[wp]));
         float4 mx = make_float4(S.mxx[wp], S.mxy[wp], S.mxz[wp], __uint_as_float(S.lc[wp]));
         if (flags & (1u << (16 + q))) {
             const int j = static_cast<int>(S.nn[p - nbase]);
-            const int wj = ploc_swz(j - wbase);
+            const int wj = j - wbase;
             const uint32_t id = out_m++;
             if (id >= 2 * N - 1 || id < N) { raise_corrupt(err, 2 + (iter << 8), p, id); continue; }
             float4 m0, m1;  // AABB::merge (bvh.cpp:401-413), first argument = lower position
@@ -691,6 +724,199 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
         cout[2 * static_cast<size_t>(out_v)] = mn;
         cout[2 * static_cast<size_t>(out_v) + 1] = mx;
         ++out_v;
+    }
+}
+
+// Nearest neighbour of position p (< n) in a whole-array window (position q
+// at window index q + 2R, entries outside [0, n) infinite): the thread's one
+// position, the 2R candidates in increasing j (strict minimum: lowest j on
+// ties).  RC > 0: compile-time radius.
+template <int RC, int TILE, int BLOCK, int MAXR>
+__device__ __forceinline__ uint32_t ploc_nearest_one(const PlocSmem<TILE, BLOCK, MAXR>& S, int p, int R_rt) {
+    const int R = RC > 0 ? RC : R_rt;
+    const int w = p + 2 * R;
+    const float amnx = S.mnx[w], amny = S.mny[w], amnz = S.mnz[w], amxx = S.mxx[w], amxy = S.mxy[w], amxz = S.mxz[w];
+    float best = __int_as_float(0x7F800000);
+    int bj = p;
+    auto visit = [&](int d) {
+        const int wj = w + d;
+        const float dx = fmaxf(amxx, S.mxx[wj]) - fminf(amnx, S.mnx[wj]);
+        const float dy = fmaxf(amxy, S.mxy[wj]) - fminf(amny, S.mny[wj]);
+        const float dz = fmaxf(amxz, S.mxz[wj]) - fminf(amnz, S.mnz[wj]);
+        const float v = 2.0f * (dx * dy + dy * dz + dz * dx);
+        if (v < best) { best = v; bj = p + d; }
+    };
+    if (RC > 0) {
+#pragma unroll
+        for (int d = -RC; d <= RC; ++d)
+            if (d != 0) visit(d);
+    } else {
+        for (int d = -R; d <= R; ++d)
+            if (d != 0) visit(d);
+    }
+    return static_cast<uint32_t>(bj);
+}
+
+// The last PLOC iterations, once every live cluster fits in one tile (n <=
+// ploc_own(R)): one block runs them with the clusters held in shared memory,
+// in the window layout of a single tile starting at position 0 (position q at
+// index q + 2R, infinite boxes outside [0, n)), so an iteration costs no
+// global round trip; only the new nodes and the iteration records are written
+// out.  Each iteration is the same reference iteration as ploc_tile's: the
+// same nearest-neighbour search (ploc_nearest over the whole array while n >
+// BLOCK, one position per thread below), mutual pairs merged at the lower
+// position (AABB::merge), new ids in position order, survivors compacted in
+// order.  Thread t decides positions [k t, k t + k), k = ceil(n / BLOCK) <=
+// TILE / BLOCK; the compaction is in place, after a barrier that ends every
+// read of the iteration's clusters.  Returns the iteration count.
+template <int RC, int TILE, int BLOCK, int MAXR>
+__device__ __noinline__ int ploc_tail_r(PlocSmem<TILE, BLOCK, MAXR>& S, int iter, int n, uint32_t idb,
+                                           float4* __restrict__ node_box, uint4* __restrict__ node_kids, uint2* it,
+                                           uint32_t N, int R_rt, uint32_t* err) {
+    constexpr int PMAX = TILE / BLOCK;
+    const int R = RC > 0 ? RC : R_rt;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float inf = __int_as_float(0x7F800000);
+    while (n > 1) {
+        if (static_cast<uint32_t>(iter) + 1 >= N) {
+            if (threadIdx.x == 0) raise_error(err, kDevIterLimit);
+            break;
+        }
+        if (n > BLOCK) {
+            ploc_nearest<RC>(S, 0, n, n, R);  // S.nn[p + R] for p < n
+        } else if (static_cast<int>(threadIdx.x) < n) {
+            S.nn[threadIdx.x + R] = ploc_nearest_one<RC>(S, static_cast<int>(threadIdx.x), R);
+        }
+        __syncthreads();
+        const int k = (n + BLOCK - 1) / BLOCK;
+        const int p0 = k * static_cast<int>(threadIdx.x);
+        uint32_t flags = 0, nv = 0, nm = 0;
+#pragma unroll
+        for (int q = 0; q < PMAX; ++q) {
+            const int p = p0 + q;
+            if (q >= k || p >= n) continue;
+            const int j = static_cast<int>(S.nn[p + R]);
+            const bool mutual = (j != p) && (static_cast<int>(S.nn[j + R]) == p);
+            if (!(mutual && p > j)) { flags |= 1u << q; ++nv; }
+            if (mutual && p < j) { flags |= 1u << (16 + q); ++nm; }
+        }
+        // exclusive scan of (survivors, merges) in position order, 16|16 bits
+        const uint32_t packed = (nv << 16) | nm;
+        uint32_t incl = packed;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) S.wsum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t ws = lane < BLOCK / 32 ? static_cast<uint32_t>(S.wsum[lane]) : 0u;
+            uint32_t wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            if (lane < BLOCK / 32) S.wsum[lane] = wi - ws;
+            if (lane == 31) S.prefix = wi;  // block totals
+        }
+        __syncthreads();
+        const uint32_t excl = static_cast<uint32_t>(S.wsum[warp]) + (incl - packed);
+        const uint32_t total = static_cast<uint32_t>(S.prefix);
+        uint32_t out_v = excl >> 16;
+        uint32_t out_m = idb + (excl & 0xFFFFu);
+        float4 omn[PMAX], omx[PMAX];
+#pragma unroll
+        for (int q = 0; q < PMAX; ++q) {
+            if (!(flags & (1u << q))) continue;
+            const int p = p0 + q, wp = p + 2 * R;
+            float4 mn = make_float4(S.mnx[wp], S.mny[wp], S.mnz[wp], __uint_as_float(S.id[wp]));
+            float4 mx = make_float4(S.mxx[wp], S.mxy[wp], S.mxz[wp], __uint_as_float(S.lc[wp]));
+            if (flags & (1u << (16 + q))) {
+                const int wj = static_cast<int>(S.nn[p + R]) + 2 * R;
+                const uint32_t id = out_m++;
+                if (id >= 2 * N - 1 || id < N) {
+                    raise_corrupt(err, 13 + (iter << 8), p, id);
+                    flags &= ~(1u << q);
+                    continue;
+                }
+                float4 m0, m1;  // AABB::merge (bvh.cpp:401-413), first argument = lower position
+                m0.x = min_std(mn.x, S.mnx[wj]); m0.y = min_std(mn.y, S.mny[wj]); m0.z = min_std(mn.z, S.mnz[wj]);
+                m1.x = max_std(mx.x, S.mxx[wj]); m1.y = max_std(mx.y, S.mxy[wj]); m1.z = max_std(mx.z, S.mxz[wj]);
+                m0.w = mn.w;                      // left child id
+                m1.w = __uint_as_float(S.id[wj]); // right child id
+                node_box[2 * static_cast<size_t>(id)] = m0;
+                node_box[2 * static_cast<size_t>(id) + 1] = m1;
+                node_kids[id - N] = make_uint4(S.id[wp], S.id[wj], S.lc[wp], S.lc[wj]);
+                mn = make_float4(m0.x, m0.y, m0.z, __uint_as_float(id));
+                mx = make_float4(m1.x, m1.y, m1.z, __uint_as_float(S.lc[wp] + S.lc[wj]));
+            }
+            omn[q] = mn;
+            omx[q] = mx;
+        }
+        __syncthreads();  // every read of this iteration's clusters is done: compact in place
+        const int n_next = static_cast<int>(total >> 16);
+        const uint32_t merges = total & 0xFFFFu;
+#pragma unroll
+        for (int q = 0; q < PMAX; ++q) {
+            if (!(flags & (1u << q))) continue;
+            if (out_v >= static_cast<uint32_t>(n_next)) {
+                raise_corrupt(err, 14 + (iter << 8), p0 + q, out_v);
+                continue;
+            }
+            const int w = static_cast<int>(out_v) + 2 * R;
+            S.mnx[w] = omn[q].x; S.mny[w] = omn[q].y; S.mnz[w] = omn[q].z; S.id[w] = __float_as_uint(omn[q].w);
+            S.mxx[w] = omx[q].x; S.mxy[w] = omx[q].y; S.mxz[w] = omx[q].z; S.lc[w] = __float_as_uint(omx[q].w);
+            ++out_v;
+        }
+        for (int q = n_next + static_cast<int>(threadIdx.x); q < n; q += BLOCK) {  // vacated positions
+            const int w = q + 2 * R;
+            S.mnx[w] = -inf; S.mny[w] = -inf; S.mnz[w] = -inf;
+            S.mxx[w] = inf; S.mxy[w] = inf; S.mxz[w] = inf;
+        }
+        if (threadIdx.x == 0) it[iter + 1] = make_uint2(static_cast<uint32_t>(n_next), idb + merges);
+        n = n_next;
+        idb += merges;
+        ++iter;
+        __syncthreads();
+    }
+    return iter;
+}
+
+// Stages the tail's clusters (input of iteration iter) and runs ploc_tail_r
+// with the compile-time radius when there is one.
+template <int TILE, int BLOCK, int MAXR>
+__device__ __forceinline__ int ploc_tail(PlocSmem<TILE, BLOCK, MAXR>& S, int iter, const float4* __restrict__ cin,
+                                         float4* __restrict__ node_box, uint4* __restrict__ node_kids, uint2* it,
+                                         uint32_t N, int R, uint32_t* err) {
+    constexpr int kWin = PlocSmem<TILE, BLOCK, MAXR>::kWin;
+    __syncthreads();
+    const uint2 cur = __ldcg(it + iter);
+    const int n = static_cast<int>(cur.x);
+    if (n + 4 * R > kWin || n > TILE) {  // the caller checked n <= ploc_own(R); only corruption gets here
+        if (threadIdx.x == 0) raise_corrupt(err, 12, static_cast<uint32_t>(iter), static_cast<uint32_t>(n));
+        return iter;
+    }
+    const float inf = __int_as_float(0x7F800000);
+    for (int w = threadIdx.x; w < kWin; w += BLOCK) {
+        const int p = w - 2 * R;
+        if (p >= 0 && p < n) {
+            const float4 a = __ldcg(cin + 2 * static_cast<size_t>(p));
+            const float4 b = __ldcg(cin + 2 * static_cast<size_t>(p) + 1);
+            S.mnx[w] = a.x; S.mny[w] = a.y; S.mnz[w] = a.z; S.id[w] = __float_as_uint(a.w);
+            S.mxx[w] = b.x; S.mxy[w] = b.y; S.mxz[w] = b.z; S.lc[w] = __float_as_uint(b.w);
+        } else {
+            S.mnx[w] = -inf; S.mny[w] = -inf; S.mnz[w] = -inf;
+            S.mxx[w] = inf; S.mxy[w] = inf; S.mxz[w] = inf;
+        }
+    }
+    __syncthreads();
+    switch (R) {
+        case 8: return ploc_tail_r<8>(S, iter, n, cur.y, node_box, node_kids, it, N, R, err);
+        case 16: return ploc_tail_r<16>(S, iter, n, cur.y, node_box, node_kids, it, N, R, err);
+        case 32: return ploc_tail_r<32>(S, iter, n, cur.y, node_box, node_kids, it, N, R, err);
+        default: return ploc_tail_r<0>(S, iter, n, cur.y, node_box, node_kids, it, N, R, err);
     }
 }
 
@@ -924,6 +1150,21 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
         float4* cout = (iter & 1) ? ca : cb;
         unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
         unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
+        const uint32_t n_tiles = (cur.x + ploc_own(R) - 1) / ploc_own(R);
+        if (n_tiles <= gridDim.x) {
+            // One wave: block b runs tile b (all tiles are co-resident, so
+            // every look-back wait ends), with no ticket round trips.
+            if (blockIdx.x == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
+            if (blockIdx.x < n_tiles)
+                ploc_tile<TILE, BLOCK, MAXR>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur,
+                                             lb_next, err, spin_limit);
+            if (!grid_barrier(bar, err, spin_limit)) return;
+            if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
+            continue;
+        }
+        // More tiles than blocks: a block takes its next ticket only when it
+        // has finished a tile, so tickets follow completion order and a
+        // tile's look-back finds its predecessors already published.
         for (;;) {
             __syncthreads();
             if (threadIdx.x == 0) s_tile = atomicAdd(&tickets[iter & 1], 1u);
@@ -940,20 +1181,9 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     if (tail) {
         // The remaining iterations fit in one tile each (the last few hundred
         // clusters, which merge a few pairs per iteration): block 0 runs them
-        // alone, with block barriers only, while the others wait once.
+        // alone on shared memory, while the others wait once.
         if (blockIdx.x == 0) {
-            for (;; ++iter) {
-                __syncthreads();  // the previous iteration's clusters and record are written
-                const uint2 cur = __ldcg(it + iter);
-                if (cur.x <= 1u) break;
-                if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); break; }
-                const float4* cin = (iter & 1) ? cb : ca;
-                float4* cout = (iter & 1) ? ca : cb;
-                unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
-                unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
-                ploc_tile<TILE, BLOCK, MAXR>(S, 0u, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur,
-                                             lb_next, err, spin_limit);
-            }
+            iter = ploc_tail<TILE, BLOCK, MAXR>(S, iter, (iter & 1) ? cb : ca, node_box, node_kids, it, N, R, err);
             if (threadIdx.x == 0) iters_out[0] = static_cast<uint32_t>(iter);
         }
         if (!grid_barrier(bar, err, spin_limit)) return;

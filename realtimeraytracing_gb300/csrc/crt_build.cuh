@@ -206,6 +206,10 @@ struct BatchScene {
 static_assert(sizeof(BatchScene) == 48, "batch scene record");
 void launch_trace_batch(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t n_rays,
                         uint32_t flags, int block, bool deep, cudaStream_t s);
+// The persistent ray pool over a batch: closest hit, no seeding; p holds the
+// batch's node arrays and p.n_rays the batch's ray count.
+void launch_trace_batch_pool(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t flags,
+                             bool deep, uint32_t* next_ray, cudaStream_t s);
 // CRT_TRACE_SORT_RAYS: order[k] = k-th ray by coherence key (origin cell,
 // direction; with scenes, scene first).  scratch: ray_order_scratch_bytes(n).
 size_t ray_order_scratch_bytes(uint32_t n);

@@ -31,6 +31,16 @@ __global__ void __launch_bounds__(BLOCK) trace_kernel(TraceParams p) {
 // while most of its lanes idle.  Rays are taken in caller order, or in
 // p.order.  The hits are those of trace_kernel: a ray's closest hit (and its
 // tie rule) does not depend on the order its nodes are visited in.
+// The scene a lane's ray is walked in: traversal nodes, leaf triangles, the
+// watertight slack and the leaf count (one scene, or the ray's scene of a batch).
+struct PoolScene {
+    const crt_bvh_node* nodes;
+    const float4* wide;
+    const float4* xtri;
+    float abs_eps;
+    uint32_t n_leaves;
+};
+
 template <bool WT, int STACK>
 struct PoolRay {
     RayCtx r;
@@ -39,12 +49,15 @@ struct PoolRay {
     uint32_t bkey, btri, cur;
     int sp;
     bool have;
+    // one postponed leaf (kNoLeaf: none) and the entry distance of its box
+    uint32_t pend;
+    float pend_t;
+    static constexpr uint32_t kNoLeaf = 0xFFFFFFFFu;
 
-    __device__ __forceinline__ void test_leaf(const TraceParams& p, uint32_t L, uint32_t n_leaves, uint32_t& tested,
-                                              bool& corrupt) {
-        if (L >= n_leaves) { corrupt = true; return; }
+    __device__ __forceinline__ void test_leaf(const PoolScene& sc, uint32_t L, uint32_t& tested, bool& corrupt) {
+        if (L >= sc.n_leaves) { corrupt = true; return; }
         ++tested;
-        const float4* t = p.xtri + 3 * static_cast<size_t>(L);
+        const float4* t = sc.xtri + 3 * static_cast<size_t>(L);
         const float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
         const float3 A = make_float3(a.x, a.y, a.z), B = make_float3(b.x, b.y, b.z), C = make_float3(c.x, c.y, c.z);
         const HitRes h = WT ? tri_watertight(r.o, tmin, tmax, w, A, B, C) : tri_reference(r.o, r.d, tmin, tmax, A, B, C);
@@ -53,13 +66,12 @@ struct PoolRay {
         const uint32_t key = WT ? tri : ~L;
         if (!have || h.t < bt || (h.t == bt && key < bkey)) {
             have = true; bt = h.t; bu = h.u; bv = h.v; bkey = key; btri = tri;
-            bound = prune_bound(bt, p.abs_eps);
+            bound = prune_bound(bt, sc.abs_eps);
         }
     }
 
     // Sets up ray (r0, r1) and enters the root; false when the ray is already finished.
-    __device__ __forceinline__ bool start(const TraceParams& p, float4 r0, float4 r1, uint32_t n_leaves,
-                                          uint32_t& tested, bool& corrupt) {
+    __device__ __forceinline__ bool start(const PoolScene& sc, float4 r0, float4 r1, uint32_t& tested, bool& corrupt) {
         r.o = make_float3(r0.x, r0.y, r0.z);
         r.d = make_float3(r1.x, r1.y, r1.z);
         tmin = r0.w;
@@ -69,31 +81,52 @@ struct PoolRay {
         bkey = 0xFFFFFFFFu; btri = CRT_MISS;
         sp = 0;
         cur = 0xFFFFFFFFu;
-        if (!(tmin <= tmax) || p.n_nodes == 0) return false;
+        pend = kNoLeaf;
+        if (!(tmin <= tmax) || sc.n_leaves == 0) return false;
         r.inv = make_float3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
         r.oi = make_float3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
         r.exact = !(isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && r.inv.x != 0.f && r.inv.y != 0.f &&
                     r.inv.z != 0.f);
         if (WT) w = wt_setup(r.d);
-        bound = prune_bound(bt, p.abs_eps);
-        const float4* n4 = reinterpret_cast<const float4*>(p.nodes);
+        bound = prune_bound(bt, sc.abs_eps);
+        const float4* n4 = reinterpret_cast<const float4*>(sc.nodes);
         const uint4 lr = __ldg(reinterpret_cast<const uint4*>(n4 + 2));
         float te;
-        if (!slab<WT>(r, __ldg(n4), __ldg(n4 + 1), WT ? p.abs_eps : 0.f, te) || te > bound) return false;
+        if (!slab<WT>(r, __ldg(n4), __ldg(n4 + 1), WT ? sc.abs_eps : 0.f, te) || te > bound) return false;
         if (lr.y == 0u && lr.z == 0u) {  // a one-leaf tree
-            test_leaf(p, 0u, n_leaves, tested, corrupt);
+            test_leaf(sc, 0u, tested, corrupt);
             return false;
         }
         cur = 0u;
         return true;
     }
 
-    // One node visit; false when the walk has finished.
-    __device__ __forceinline__ bool step(const TraceParams& p, float* st_t, uint32_t* st_node, uint32_t n_leaves,
-                                         uint32_t& fetched, uint32_t& tested, bool& corrupt, bool& overflow) {
-        if (cur >= n_leaves - 1) { corrupt = true; return false; }
+    // A hit leaf child: parked in the free slot (PEND), else tested now.
+    template <bool PEND>
+    __device__ __forceinline__ void leaf(const PoolScene& sc, uint32_t L, float t, uint32_t& tested, bool& corrupt) {
+        if (PEND && pend == kNoLeaf) { pend = L; pend_t = t; return; }
+        test_leaf(sc, L, tested, corrupt);
+    }
+
+    // Tests the parked leaf unless the best hit found since prunes it (the
+    // same entry-distance rule a leaf tested at its parent gets).
+    __device__ __forceinline__ void flush(const PoolScene& sc, uint32_t& tested, bool& corrupt) {
+        if (pend == kNoLeaf) return;
+        if (pend_t <= bound) test_leaf(sc, pend, tested, corrupt);
+        pend = kNoLeaf;
+    }
+
+    // One node visit; false when the walk has finished.  PEND: hit leaf
+    // children are parked (one slot) instead of tested at once, so that the
+    // warp can test many lanes' leaves together (flush); a ray's closest hit
+    // does not depend on when its leaves are tested, and pruning by a bound
+    // that is not yet tightened only visits more nodes.
+    template <bool PEND>
+    __device__ __forceinline__ bool step(const PoolScene& sc, float* st_t, uint32_t* st_node, uint32_t& fetched,
+                                         uint32_t& tested, bool& corrupt, bool& overflow) {
+        if (cur >= sc.n_leaves - 1) { corrupt = true; return false; }
         ++fetched;
-        const float4* nd = p.wide + 4 * static_cast<size_t>(cur);
+        const float4* nd = sc.wide + 4 * static_cast<size_t>(cur);
         const float4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3);
         const uint32_t ref0 = __float_as_uint(w0.w), ref1 = __float_as_uint(w1.w);
         float t0, t1;
@@ -108,8 +141,8 @@ struct PoolRay {
         const float bnd = bound;
         h0 = h0 && t0 <= bnd;
         h1 = h1 && t1 <= bnd;
-        if (h0 && (ref0 & kLeafRef)) { test_leaf(p, ref0 & ~kLeafRef, n_leaves, tested, corrupt); h0 = false; }
-        if (h1 && (ref1 & kLeafRef)) { test_leaf(p, ref1 & ~kLeafRef, n_leaves, tested, corrupt); h1 = false; }
+        if (h0 && (ref0 & kLeafRef)) { leaf<PEND>(sc, ref0 & ~kLeafRef, t0, tested, corrupt); h0 = false; }
+        if (h1 && (ref1 & kLeafRef)) { leaf<PEND>(sc, ref1 & ~kLeafRef, t1, tested, corrupt); h1 = false; }
         if (h0 || h1) {
             const float bnd2 = bound;
             h0 = h0 && t0 <= bnd2;
@@ -147,11 +180,27 @@ struct PoolRay {
 // its idle lanes as they free up, so that a warp's lanes hold neighbouring
 // rays of the (possibly coherence-sorted) order; otherwise it takes exactly
 // as many as it has idle lanes.
-template <bool WT, int STACK, int BLOCK, int BURST, bool CHUNK>
-__global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32_t* __restrict__ next_ray) {
+//
+// BATCH: many scenes in one launch (crt_batch_trace): a lane that takes ray i
+// finds i's scene by binary search over the scenes' ray offsets and walks
+// that scene's tree; p.nodes / p.wide / p.xtri are the batch's arrays.
+//
+// PEND: leaf tests are postponed (PoolRay::step<true>) and run for the whole
+// warp at once when at least FLUSH lanes hold a parked leaf, or when a lane
+// whose walk has ended still holds one (it must be tested before the hit is
+// written).
+template <bool WT, int STACK, int BLOCK, int BURST, bool CHUNK, bool BATCH, bool PEND, int FLUSH>
+__global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32_t* __restrict__ next_ray,
+                                                           const BatchScene* __restrict__ scenes, uint32_t n_scenes) {
     constexpr uint32_t kIdle = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
+    __shared__ uint32_t s_ray_off[BATCH ? kMaxBatchScenes + 1 : 1];
+    if (BATCH) {
+        for (uint32_t k = threadIdx.x; k <= n_scenes; k += BLOCK)
+            s_ray_off[k] = k < n_scenes ? scenes[k].ray_off : scenes[n_scenes - 1].ray_off + scenes[n_scenes - 1].n_rays;
+        __syncthreads();
+    }
     const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
-    const uint32_t n_leaves = (p.n_nodes + 1) / 2;
+    PoolScene sc{p.nodes, p.wide, p.xtri, p.abs_eps, (p.n_nodes + 1) / 2};
     PoolRay<WT, STACK> ray;
     uint32_t st_node[STACK];
     float st_t[STACK];
@@ -190,9 +239,22 @@ __global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32
                         raise_corrupt(p.err, 7, k, i);
                         i = kDone;
                     } else {
+                        if (BATCH) {
+                            uint32_t lo = 0, hi = n_scenes - 1;
+                            while (lo < hi) {
+                                const uint32_t mid = (lo + hi + 1) >> 1;
+                                if (s_ray_off[mid] <= i) lo = mid; else hi = mid - 1;
+                            }
+                            const BatchScene bs = scenes[lo];
+                            sc.nodes = p.nodes + bs.node_off;
+                            sc.wide = p.wide + 4 * static_cast<size_t>(bs.wide_off);
+                            sc.xtri = p.xtri + 3 * static_cast<size_t>(bs.tri_off);
+                            sc.abs_eps = bs.abs_eps;
+                            sc.n_leaves = bs.n_tris;
+                        }
                         const float4 r0 = __ldg(reinterpret_cast<const float4*>(p.rays + i));
                         const float4 r1 = __ldg(reinterpret_cast<const float4*>(p.rays + i) + 1);
-                        if (!ray.start(p, r0, r1, n_leaves, tested, corrupt)) {
+                        if (!ray.start(sc, r0, r1, tested, corrupt)) {
                             reinterpret_cast<uint4*>(p.hits)[i] = ray.hit();
                             i = kIdle;
                         }
@@ -201,11 +263,27 @@ __global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32
             }
         }
         if (__all_sync(0xFFFFFFFFu, i == kDone)) break;
-        if (i < kDone) {
+        if (PEND) {
+            bool walking = i < kDone;
+#pragma unroll 1
+            for (int s = 0; s < BURST; ++s) {
+                if (walking) walking = ray.template step<true>(sc, st_t, st_node, fetched, tested, corrupt, overflow);
+                const bool parked = i < kDone && ray.pend != PoolRay<WT, STACK>::kNoLeaf;
+                const uint32_t pm = __ballot_sync(0xFFFFFFFFu, parked);
+                if (__popc(pm) >= FLUSH || __any_sync(0xFFFFFFFFu, parked && !walking)) {
+                    if (parked) ray.flush(sc, tested, corrupt);
+                }
+                if (!__any_sync(0xFFFFFFFFu, walking)) break;
+            }
+            if (i < kDone && !walking) {
+                reinterpret_cast<uint4*>(p.hits)[i] = ray.hit();
+                i = kIdle;
+            }
+        } else if (i < kDone) {
             bool walking = true;
 #pragma unroll 1
             for (int s = 0; s < BURST && walking; ++s)
-                walking = ray.step(p, st_t, st_node, n_leaves, fetched, tested, corrupt, overflow);
+                walking = ray.template step<false>(sc, st_t, st_node, fetched, tested, corrupt, overflow);
             if (!walking) {
                 reinterpret_cast<uint4*>(p.hits)[i] = ray.hit();
                 i = kIdle;
@@ -392,7 +470,8 @@ static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed
 }
 
 // Launch shape of the persistent traversal (measured on GB300 over 8M
-// incoherent bounce rays: block, node visits between refills, chunked refill).
+// incoherent bounce rays: block, node visits between refills, chunked refill,
+// postponed leaf tests and the parked lanes that trigger a warp's flush).
 #ifndef CRT_POOL_BLOCK
 #define CRT_POOL_BLOCK 128
 #endif
@@ -402,22 +481,30 @@ static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed
 #ifndef CRT_POOL_CHUNK
 #define CRT_POOL_CHUNK 0
 #endif
+#ifndef CRT_POOL_PEND
+#define CRT_POOL_PEND 1
+#endif
+#ifndef CRT_POOL_FLUSH
+#define CRT_POOL_FLUSH 16
+#endif
 
-template <bool WT, int STACK>
-static void launch_pool_s(const TraceParams& p, uint32_t* next_ray, cudaStream_t s) {
-    constexpr int kBlock = CRT_POOL_BLOCK, kBurst = CRT_POOL_BURST;
-    constexpr bool kChunk = CRT_POOL_CHUNK != 0;
+template <bool WT, int STACK, bool BATCH>
+static void launch_pool_s(const TraceParams& p, uint32_t* next_ray, const BatchScene* scenes, uint32_t n_scenes,
+                          cudaStream_t s) {
+    constexpr int kBlock = CRT_POOL_BLOCK, kBurst = CRT_POOL_BURST, kFlush = CRT_POOL_FLUSH;
+    constexpr bool kChunk = CRT_POOL_CHUNK != 0, kPend = CRT_POOL_PEND != 0;
     static int grid = 0;
     if (grid == 0) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_pool_kernel<WT, STACK, kBlock, kBurst, kChunk>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_pool_kernel<WT, STACK, kBlock, kBurst, kChunk, BATCH, kPend, kFlush>,
                                                       kBlock, 0);
         grid = kNumSms * (per_sm > 0 ? per_sm : 1);
     }
     cudaMemsetAsync(next_ray, 0, 4, s);
     const uint32_t want = (p.n_rays + kBlock - 1) / kBlock;
-    trace_pool_kernel<WT, STACK, kBlock, kBurst, kChunk>
-        <<<want < static_cast<uint32_t>(grid) ? want : static_cast<uint32_t>(grid), kBlock, 0, s>>>(p, next_ray);
+    trace_pool_kernel<WT, STACK, kBlock, kBurst, kChunk, BATCH, kPend, kFlush>
+        <<<want < static_cast<uint32_t>(grid) ? want : static_cast<uint32_t>(grid), kBlock, 0, s>>>(p, next_ray, scenes,
+                                                                                                   n_scenes);
 }
 
 void launch_trace_pool(const TraceParams& p, uint32_t flags, uint32_t* next_ray, cudaStream_t s) {
@@ -425,11 +512,24 @@ void launch_trace_pool(const TraceParams& p, uint32_t flags, uint32_t* next_ray,
     const bool deep = (flags >> 16) != 0;
     if (p.n_rays == 0) return;
     if (wt) {
-        if (deep) launch_pool_s<true, 1024>(p, next_ray, s);
-        else launch_pool_s<true, 64>(p, next_ray, s);
+        if (deep) launch_pool_s<true, 1024, false>(p, next_ray, nullptr, 0, s);
+        else launch_pool_s<true, 64, false>(p, next_ray, nullptr, 0, s);
     } else {
-        if (deep) launch_pool_s<false, 1024>(p, next_ray, s);
-        else launch_pool_s<false, 64>(p, next_ray, s);
+        if (deep) launch_pool_s<false, 1024, false>(p, next_ray, nullptr, 0, s);
+        else launch_pool_s<false, 64, false>(p, next_ray, nullptr, 0, s);
+    }
+}
+
+void launch_trace_batch_pool(const TraceParams& p, const BatchScene* scenes, uint32_t n_scenes, uint32_t flags,
+                             bool deep, uint32_t* next_ray, cudaStream_t s) {
+    const bool wt = flags & CRT_TRI_WATERTIGHT;
+    if (p.n_rays == 0 || n_scenes == 0) return;
+    if (wt) {
+        if (deep) launch_pool_s<true, 1024, true>(p, next_ray, scenes, n_scenes, s);
+        else launch_pool_s<true, 64, true>(p, next_ray, scenes, n_scenes, s);
+    } else {
+        if (deep) launch_pool_s<false, 1024, true>(p, next_ray, scenes, n_scenes, s);
+        else launch_pool_s<false, 64, true>(p, next_ray, scenes, n_scenes, s);
     }
 }
 

@@ -256,11 +256,12 @@ def test_trace_from_page_locked_host_rays(ctx, config0, flags):
 @pytest.mark.parametrize("flags", [crt.TRI_WATERTIGHT, crt.TRI_REFERENCE])
 def test_persistent_warps_equal_one_thread_per_ray(ctx, flags):
     """Large closest-hit batches run on persistent warps that refill finished
-    lanes; CRT_TRACE_PER_RAY_THREADS keeps one thread per ray.  Same hits bit
-    for bit, and the same node fetches and triangle tests (every ray walks the
-    same nodes either way), on incoherent rays: rays between sphere points
-    and cube points, and bounce rays from their hits, in caller order and
-    in sorted order."""
+    lanes and postpone leaf tests until many lanes hold one;
+    CRT_TRACE_PER_RAY_THREADS keeps one thread per ray testing leaves at once.
+    Same hits bit for bit, on incoherent rays: rays between sphere points and
+    cube points, and bounce rays from their hits, in caller order and in
+    sorted order.  A postponed leaf tightens the pruning bound later, so the
+    persistent walk may fetch a few more nodes and test a few more triangles."""
     tris = S.clustered_soup(200_000, 64, 0.03, 0.004, 0.5, seed=95)
     if flags == crt.TRI_REFERENCE:   # large triangles, so that the shader's predicate finds hits
         tris[:, [0, 1, 2, 4, 5, 6, 8, 9, 10]] = (tris[:, [0, 1, 2, 4, 5, 6, 8, 9, 10]] - 0.5) * 8.0 + 0.5
@@ -276,6 +277,6 @@ def test_persistent_warps_equal_one_thread_per_ray(ctx, flags):
             b = ctx.trace(bvh, rs, flags | order | crt.PER_RAY_THREADS | crt.TRACE_STATS)
             sb = ctx.last_trace_stats()
             np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
-            assert sa == sb
+            assert 0.9 * sb[0] <= sa[0] <= 1.25 * sb[0] and 0.9 * sb[1] <= sa[1] <= 1.5 * sb[1], (sa, sb)
             assert (a[:, 0].view(np.uint32) != crt.MISS).sum() > 1000
     bvh.free()
