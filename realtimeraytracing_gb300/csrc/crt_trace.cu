@@ -485,7 +485,7 @@ static void launch_trace_t(const TraceParams& p, int block, bool deep, bool seed
 #define CRT_POOL_PEND 1
 #endif
 #ifndef CRT_POOL_FLUSH
-#define CRT_POOL_FLUSH 16
+#define CRT_POOL_FLUSH 6
 #endif
 
 template <bool WT, int STACK, bool BATCH>
