@@ -559,7 +559,8 @@ crt_status build_impl(crt_ctx* x, crt_bvh* b, const crt_triangle* tris, uint32_t
         const cudaError_t e = crt::launch_ploc_persistent(
             x->clus_a.as<float4>(), x->clus_b.as<float4>(), x->node_box.as<float4>(), x->node_kids.as<uint4>(), d_it, N,
             static_cast<int>(x->cfg.ploc_radius), lb, tail, ploc_tiles, x->pos.as<uint2>(), b->nodes.as<crt_bvh_node>(),
-            b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves, st, tail + 2, tail + 4,
+            b->wide.as<float4>(), b->wide_wt.as<float4>(), b->depth_odd.as<uint8_t>(), leaves, st,
+            reinterpret_cast<unsigned long long*>(tail + 2), tail + 4,
             err, x->cfg.spin_limit, s);
         if (e == cudaSuccess) {
             CRT_CUDA(cudaEventRecord(x->ev[3], s));
@@ -1872,7 +1873,8 @@ crt_status batch_enqueue(crt_ctx* x, crt_batch* bt, const crt_triangle* tris, co
             bt->node_box.as<float4>(), bt->node_kids.as<uint4>(), bt->it.as<uint2>(), static_cast<int>(bt->cfg.ploc_radius),
             lb, bt->lb_cap, tail, bt->pf.as<uint2>(), bt->nodes.as<crt_bvh_node>(), bt->wide.as<float4>(),
             bt->wide_wt.as<float4>(), bt->depth_odd.as<uint8_t>(),
-            crt::LeafOut{bt->xtri_sorted.as<float4>(), bt->xtri.as<float4>(), bt->inv_perm.as<uint32_t>()}, tail + 2,
+            crt::LeafOut{bt->xtri_sorted.as<float4>(), bt->xtri.as<float4>(), bt->inv_perm.as<uint32_t>()},
+            reinterpret_cast<unsigned long long*>(tail + 2),
             bt->max_n + 1, err, x->cfg.spin_limit, s);
         if (e != cudaSuccess) return fail(CRT_ERR_UNSUPPORTED, "batched PLOC launch failed: %s", cudaGetErrorString(e));
     }

@@ -256,9 +256,10 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
                                                            float4* node_box, uint4* node_kids, uint2* it, int R,
                                                            unsigned long long* lookback, uint32_t lb_cap, uint32_t* tickets,
                                                            uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
-                                                           uint8_t* depth_odd, LeafOut lv, unsigned int* bar,
+                                                           uint8_t* depth_odd, LeafOut lv, unsigned long long* bar,
                                                            uint32_t max_iters, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
+    unsigned long long bar_target = 0;  // grid barriers passed x gridDim (thread 0)
     __shared__ uint32_t s_tile_pre[kMaxBatchScenes + 1];
     __shared__ uint32_t s_n[kMaxBatchScenes];
     __shared__ uint32_t s_tile;
@@ -293,24 +294,15 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
             for (uint32_t sc = blockIdx.x; sc < n_scenes; sc += gridDim.x) {
                 if (s_n[sc] <= 1u) continue;  // finished before this iteration
                 const BatchScene B = scenes[sc];
-                for (uint32_t k = static_cast<uint32_t>(iter);; ++k) {
-                    __syncthreads();  // the previous iteration's clusters and record are written
-                    const uint2 cur = __ldcg(it + B.it_off + k);
-                    if (cur.x <= 1u) {
-                        if (threadIdx.x == 0) scenes[sc].iters = k;
-                        break;
-                    }
-                    if (k >= max_iters) { raise_error(err, kDevIterLimit); break; }
-                    float4* cin = ((k & 1) ? cb : ca) + 2 * static_cast<size_t>(B.tri_off);
-                    float4* cout = ((k & 1) ? ca : cb) + 2 * static_cast<size_t>(B.tri_off);
-                    unsigned long long* lb_cur = lookback + static_cast<size_t>(k & 1) * lb_cap + B.lb_off;
-                    unsigned long long* lb_next = lookback + static_cast<size_t>((k + 1) & 1) * lb_cap + B.lb_off;
-                    ploc_tile<TILE, BLOCK, MAXR>(S, 0u, cur, static_cast<int>(k), cin, cout,
-                                                 node_box + 2 * static_cast<size_t>(B.node_off), node_kids + B.tri_off,
-                                                 it + B.it_off, B.n_tris, R, lb_cur, lb_next, err, spin_limit);
-                }
+                // the scene's remaining iterations on shared memory (ploc_tail);
+                // its iteration count cannot exceed the scene's N - 1
+                const float4* cin = ((iter & 1) ? cb : ca) + 2 * static_cast<size_t>(B.tri_off);
+                const int k = ploc_tail<TILE, BLOCK, MAXR>(S, iter, cin, node_box + 2 * static_cast<size_t>(B.node_off),
+                                                          node_kids + B.tri_off, it + B.it_off, B.n_tris, R, err);
+                if (threadIdx.x == 0) scenes[sc].iters = static_cast<uint32_t>(k);
+                __syncthreads();
             }
-            if (!grid_barrier(bar, err, spin_limit)) return;
+            if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
             break;
         }
         if (threadIdx.x == 0) {
@@ -348,7 +340,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
                 if (it[B.it_off + iter + 1].x <= 1u) scenes[sc].iters = static_cast<uint32_t>(iter + 1);
             }
         }
-        if (!grid_barrier(bar, err, spin_limit)) return;
+        if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
     }
     // DFS layout: step r handles level (iters - 1 - r) of every scene that has
     // it, recording node ids by DFS position in dfs (the first cluster buffer,
@@ -385,7 +377,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) batch_ploc_kernel(Bat
             layout_down(X, node_kids + B.tri_off, pf + B.tri_off, B.n_tris,
                         dfs + B.node_off, err);
         }
-        if (!grid_barrier(bar, err, spin_limit)) return;
+        if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
     }
     // every DFS position of every scene with more than one triangle, in order
     __syncthreads();
@@ -463,7 +455,7 @@ void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchSce
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
                               uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
-                              uint8_t* depth_odd, LeafOut lv, unsigned int* bar, uint32_t max_iters, uint32_t* err,
+                              uint8_t* depth_odd, LeafOut lv, unsigned long long* bar, uint32_t max_iters, uint32_t* err,
                               uint32_t spin_limit, cudaStream_t s) {
     const int grid = batch_ploc_grid();
     if (grid <= 0) return cudaErrorNotSupported;

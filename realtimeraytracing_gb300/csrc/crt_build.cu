@@ -1101,21 +1101,20 @@ __global__ void __launch_bounds__(256) layout_emit_kernel(const float4* __restri
 // barrier (co-residency guaranteed by a cooperative launch; every wait is
 // bounded and a timeout ends every block).  Saves the per-iteration launch
 // and the host round trips the multi-launch path needs.
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, uint32_t* err, uint32_t spin_limit) {
+__device__ __forceinline__ bool grid_barrier(unsigned long long* bar, unsigned long long& target, uint32_t* err,
+                                             uint32_t spin_limit) {
+    // A 64-bit arrival counter that only grows (zeroed before the launch):
+    // barrier k is complete when it reaches k * gridDim, so a block needs one
+    // fence and one atomic, then polls; no reset and no release step.
+    // `target` is this block's running count (thread 0's copy is used).
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned int gen = ld_acquire_u32(bar + 1);
+        target += gridDim.x;
         __threadfence();
-        const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
-        if (arrived == gridDim.x) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            st_release_u32(bar + 1, gen + 1u);
-        } else {
-            SpinBound spin(spin_limit);
-            while (ld_acquire_u32(bar + 1) == gen)
-                if (!spin.step()) { raise_error(err, kDevTimeout); break; }
-        }
+        atomicAdd(bar, 1ull);
+        SpinBound spin(spin_limit);
+        while (ld_acquire_u64(bar) < target)
+            if (!spin.step()) { raise_error(err, kDevTimeout); break; }
     }
     __syncthreads();
     return (ld_acquire_u32(err) & kDevTimeout) == 0u;
@@ -1127,10 +1126,11 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
                                                                 int R, unsigned long long* lookback, uint32_t* tickets,
                                                                 uint32_t n_tiles_cap, uint2* pf, crt_bvh_node* out,
                                                                 float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                                                                LeafOut lv, const SceneState* st, unsigned int* bar,
+                                                                LeafOut lv, const SceneState* st, unsigned long long* bar,
                                                                 uint32_t* iters_out, uint32_t* err, uint32_t spin_limit) {
     __shared__ PlocSmem<TILE, BLOCK, MAXR> S;
     __shared__ uint32_t s_tile;
+    unsigned long long bar_target = 0;  // grid barriers passed x gridDim (thread 0)
     // iters_out[0]: iterations; [1]: blocks finished; then 64-bit globaltimer
     // stamps: start, end of the PLOC loop, end of the layout.
     unsigned long long* stamp = reinterpret_cast<unsigned long long*>(iters_out + 2);
@@ -1158,7 +1158,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
             if (blockIdx.x < n_tiles)
                 ploc_tile<TILE, BLOCK, MAXR>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur,
                                              lb_next, err, spin_limit);
-            if (!grid_barrier(bar, err, spin_limit)) return;
+            if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
             if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
             continue;
         }
@@ -1175,7 +1175,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
             ploc_tile<TILE, BLOCK, MAXR>(S, tile, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur, lb_next,
                                          err, spin_limit);
         }
-        if (!grid_barrier(bar, err, spin_limit)) return;
+        if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
         if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
     }
     if (tail) {
@@ -1186,7 +1186,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
             iter = ploc_tail<TILE, BLOCK, MAXR>(S, iter, (iter & 1) ? cb : ca, node_box, node_kids, it, N, R, err);
             if (threadIdx.x == 0) iters_out[0] = static_cast<uint32_t>(iter);
         }
-        if (!grid_barrier(bar, err, spin_limit)) return;
+        if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
         iter = static_cast<int>(__ldcg(iters_out));
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
         }
         layout_down_at<true>(X, me, node_kids, pf, N, dfs, err);
     }
-    if (!grid_barrier(bar, err, spin_limit)) return;
+    if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
     const float grow = st->abs_eps;
     for (uint32_t p = blockIdx.x * BLOCK + threadIdx.x; p < 2 * N - 1; p += gridDim.x * BLOCK)
         layout_emit(p, node_box, node_kids, pf, N, dfs, out, wide, wide_wt, depth_odd, lv, grow, err);
@@ -1538,7 +1538,7 @@ int ploc_persistent_grid() {
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
                                    uint2* pf, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                                   LeafOut lv, const SceneState* st, unsigned int* bar, uint32_t* iters_out,
+                                   LeafOut lv, const SceneState* st, unsigned long long* bar, uint32_t* iters_out,
                                    uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
     const int grid = ploc_persistent_grid();
     if (grid <= 0) return cudaErrorNotSupported;

@@ -106,7 +106,7 @@ void launch_single_leaf(const float4* node_box, crt_bvh_node* out, LeafOut leave
 cudaError_t launch_ploc_persistent(float4* ca, float4* cb, float4* node_box, uint4* node_kids, uint2* it, uint32_t N,
                                    int radius, unsigned long long* lookback, uint32_t* tickets, uint32_t n_tiles_cap,
                                    uint2* pf, crt_bvh_node* out, float4* wide, float4* wide_wt, uint8_t* depth_odd,
-                                   LeafOut leaves, const SceneState* st, unsigned int* bar, uint32_t* iters_out,
+                                   LeafOut leaves, const SceneState* st, unsigned long long* bar, uint32_t* iters_out,
                                    uint32_t* err, uint32_t spin_limit, cudaStream_t s);
 
 // Refit (crt_refit.cu).  The slack of the refit tree's root box goes to
@@ -231,7 +231,7 @@ void launch_batch_leaf_init(const crt_triangle* tris, uint32_t n_total, BatchSce
 cudaError_t launch_batch_ploc(BatchScene* scenes, uint32_t n_scenes, float4* ca, float4* cb, float4* node_box,
                               uint4* node_kids, uint2* it, int radius, unsigned long long* lookback, uint32_t lb_cap,
                               uint32_t* tickets, uint2* pf, crt_bvh_node* nodes, float4* wide, float4* wide_wt,
-                              uint8_t* depth_odd, LeafOut leaves, unsigned int* bar, uint32_t max_iters, uint32_t* err,
+                              uint8_t* depth_odd, LeafOut leaves, unsigned long long* bar, uint32_t max_iters, uint32_t* err,
                               uint32_t spin_limit, cudaStream_t s);
 // Treelet restructuring (crt_optimize.cu).  Ids: leaves 0..N-1 in tree
 // leaf order, internal nodes N + DFS rank (root N).
