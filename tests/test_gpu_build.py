@@ -80,8 +80,11 @@ def test_model_matrices(ctx):
     _check_build(ctx, tris, n, models)
 
 
-@pytest.mark.parametrize("radius", [8, 32])
+@pytest.mark.parametrize("radius", [8, 32, 1, 5, 12, 31])
 def test_other_radius(ctx, radius):
+    """Radii with a compiled search (8, 16, 32) and the generic one (any
+    other radius in [1, 32]), through the tile iterations and the
+    shared-memory tail: the oracle's tree bit for bit."""
     from realtimeraytracing_gb300 import crt
     c = crt.Context(ploc_radius=radius)
     n = 20000

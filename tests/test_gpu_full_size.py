@@ -106,3 +106,47 @@ def test_config3_build_and_bounce_rays(ctx):
     bvh.optimize(1)
     np.testing.assert_array_equal(_u(ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)), _u(plain))
     bvh.free()
+
+
+def test_config2_batch_full_scale_matches_single_scenes(ctx):
+    """The batched workload at its full size: 64 scenes with log-uniform 1k-2M
+    triangles (17.1 M in total; even scenes uniform soups, odd scenes 32-blob
+    clustered soups) and their own log-uniform 64k-4M rays (55 M in total),
+    built and traced as one graph-replayed launch per stage.  Every hit equals
+    the single-scene crt_build + crt_trace of its scene, bit for bit (both
+    predicates; the shader's rejects every triangle this small, so its hits
+    are all misses), and so do the node arrays of every 8th scene and of the
+    largest one; the sorted trace of the batch returns the same hits."""
+    torch = pytest.importorskip("torch")
+    tri_n, ray_n = S.config2_sizes(64, seed=0)
+    assert int(tri_n.sum()) > 16_000_000 and int(ray_n.sum()) > 50_000_000
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(2)
+    tris = torch.cat([S.device_soup(int(n), gen, clustered=(k % 2 == 1)) for k, n in enumerate(tri_n)])
+    rays = torch.cat([S.device_sphere_rays(int(m), gen) for m in ray_n])
+    models = S.identity_models(1)
+    b = crt.Batch(ctx, tri_n, ray_n, models=models)
+    tri_off = np.concatenate([[0], np.cumsum(tri_n)]).astype(np.int64)
+    ray_off = np.concatenate([[0], np.cumsum(ray_n)]).astype(np.int64)
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device="cuda")
+    seq = torch.empty_like(hits)
+    check_nodes = set(range(0, 64, 8)) | {int(np.argmax(tri_n))}
+    for flags in (crt.TRI_WATERTIGHT, crt.TRI_REFERENCE):
+        assert b.run(tris, rays, hits, flags, graph=True)
+        b.run(tris, rays, hits, flags, graph=True)  # replayed
+        for k in range(64):
+            tk = tris[int(tri_off[k]):int(tri_off[k + 1])]
+            bv = ctx.build(tk, models=models)
+            ctx.trace(bv, rays[int(ray_off[k]):int(ray_off[k + 1])], flags, out=seq[int(ray_off[k]):int(ray_off[k + 1])])
+            if flags == crt.TRI_WATERTIGHT and k in check_nodes:
+                np.testing.assert_array_equal(_u(b.nodes(k)), _u(bv.nodes()), err_msg=f"scene {k}")
+            bv.free()
+        torch.cuda.synchronize()
+        assert torch.equal(seq.view(torch.int32), hits.view(torch.int32)), flags
+        if flags == crt.TRI_WATERTIGHT:  # the shader's predicate rejects these small triangles
+            assert int((hits[:, 0].view(torch.int32) != -1).sum().item()) > 1_000_000
+            srt = torch.empty_like(hits)
+            b.trace(rays, srt, flags | crt.SORT_RAYS)
+            assert torch.equal(srt.view(torch.int32), hits.view(torch.int32))
+            del srt
+    b.free()
