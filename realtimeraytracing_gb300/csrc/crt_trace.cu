@@ -122,8 +122,8 @@ struct PoolRay {
     // does not depend on when its leaves are tested, and pruning by a bound
     // that is not yet tightened only visits more nodes.
     template <bool PEND>
-    __device__ __forceinline__ bool step(const PoolScene& sc, float* st_t, uint32_t* st_node, uint32_t& fetched,
-                                         uint32_t& tested, bool& corrupt, bool& overflow) {
+    __device__ __forceinline__ bool step(const PoolScene& sc, uint2* st, uint32_t& fetched, uint32_t& tested,
+                                         bool& corrupt, bool& overflow) {
         if (cur >= sc.n_leaves - 1) { corrupt = true; return false; }
         ++fetched;
         const float4* nd = sc.wide + 4 * static_cast<size_t>(cur);
@@ -150,9 +150,8 @@ struct PoolRay {
         }
         if (h0 && h1) {
             const bool near1 = t1 < t0;
-            if (sp < STACK) {
-                st_node[sp] = near1 ? ref0 : ref1;
-                st_t[sp] = near1 ? t0 : t1;
+            if (sp < STACK) {  // (node, entry distance) as one 8-byte entry
+                st[sp] = make_uint2(near1 ? ref0 : ref1, __float_as_uint(near1 ? t0 : t1));
                 ++sp;
             } else {
                 overflow = true;
@@ -165,7 +164,8 @@ struct PoolRay {
         const float bnd3 = bound;
         while (sp > 0) {
             --sp;
-            if (st_t[sp] <= bnd3) { cur = st_node[sp]; return true; }
+            const uint2 e = st[sp];
+            if (__uint_as_float(e.y) <= bnd3) { cur = e.x; return true; }
         }
         return false;
     }
@@ -202,8 +202,7 @@ __global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32
     const uint32_t lane = threadIdx.x & 31u, lt_mask = (1u << lane) - 1u;
     PoolScene sc{p.nodes, p.wide, p.xtri, p.abs_eps, (p.n_nodes + 1) / 2};
     PoolRay<WT, STACK> ray;
-    uint32_t st_node[STACK];
-    float st_t[STACK];
+    uint2 st[STACK];
     uint32_t i = kIdle, fetched = 0, tested = 0;
     uint32_t chunk_next = 0, chunk_end = 0;  // CHUNK: the warp's rays not yet handed out (warp-uniform)
     bool corrupt = false, overflow = false;
@@ -267,7 +266,7 @@ __global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32
             bool walking = i < kDone;
 #pragma unroll 1
             for (int s = 0; s < BURST; ++s) {
-                if (walking) walking = ray.template step<true>(sc, st_t, st_node, fetched, tested, corrupt, overflow);
+                if (walking) walking = ray.template step<true>(sc, st, fetched, tested, corrupt, overflow);
                 const bool parked = i < kDone && ray.pend != PoolRay<WT, STACK>::kNoLeaf;
                 const uint32_t pm = __ballot_sync(0xFFFFFFFFu, parked);
                 if (__popc(pm) >= FLUSH || __any_sync(0xFFFFFFFFu, parked && !walking)) {
@@ -283,7 +282,7 @@ __global__ void __launch_bounds__(BLOCK) trace_pool_kernel(TraceParams p, uint32
             bool walking = true;
 #pragma unroll 1
             for (int s = 0; s < BURST && walking; ++s)
-                walking = ray.template step<false>(sc, st_t, st_node, fetched, tested, corrupt, overflow);
+                walking = ray.template step<false>(sc, st, fetched, tested, corrupt, overflow);
             if (!walking) {
                 reinterpret_cast<uint4*>(p.hits)[i] = ray.hit();
                 i = kIdle;

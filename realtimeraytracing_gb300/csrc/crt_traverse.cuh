@@ -230,8 +230,7 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
         }
     };
 
-    uint32_t st_node[STACK];
-    float st_t[STACK];
+    uint2 st[STACK];  // (node, entry distance) per entry: one 8-byte local store / load
     // Depth-first walk below internal node `cur` (children box-tested at
     // their parent, leaves tested at once, nearer child entered directly).
     // `skip` names a subtree already searched exactly (the seeded treelet).
@@ -268,8 +267,7 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
                 // occluder of a ray leaving a surface is rarely next to its origin)
                 const bool near1 = ANY ? !(t1 < t0) : (t1 < t0);
                 if (sp < STACK) {
-                    st_node[sp] = near1 ? ref0 : ref1;
-                    st_t[sp] = near1 ? t0 : t1;
+                    st[sp] = make_uint2(near1 ? ref0 : ref1, __float_as_uint(near1 ? t0 : t1));
                     ++sp;
                 } else {
                     overflow = true;
@@ -283,7 +281,8 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
             const float bnd3 = bound;
             while (sp > 0) {
                 --sp;
-                if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
+                const uint2 e = st[sp];
+                if (__uint_as_float(e.y) <= bnd3) { cur = e.x; break; }
             }
         }
     };
@@ -384,8 +383,7 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
             for (int c = 3; c >= 1; --c) {
                 if (hr[c] == 0xFFFFFFFFu) continue;
                 if (sp < STACK) {
-                    st_node[sp] = hr[c];
-                    st_t[sp] = ht[c];
+                    st[sp] = make_uint2(hr[c], __float_as_uint(ht[c]));
                     ++sp;
                 } else {
                     overflow = true;
@@ -396,7 +394,8 @@ __device__ __forceinline__ uint4 trace_one(const TraceParams& p, const uint32_t 
             const float bnd3 = bound;
             while (sp > 0) {
                 --sp;
-                if (st_t[sp] <= bnd3) { cur = st_node[sp]; break; }
+                const uint2 e = st[sp];
+                if (__uint_as_float(e.y) <= bnd3) { cur = e.x; break; }
             }
         }
     };
