@@ -424,7 +424,7 @@ def run_ours(args):
                 "treelet_hit_rate": round(hit_rate, 4), "rays_hitting": round(float(hit.mean()), 4),
                 "training": {"passes": passes, "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4),
                              "ms_per_pass": round(train_ms, 3), "samples_per_pass": n // 20},
-                "modes": "learned = CRT_TRACE_PREDICTOR_ORDER (inference + order by predicted treelet, origin "
+                "modes": "learned = CRT_TRACE_PREDICTOR_ORDER (inference + order by the likeliest class, origin "
                          "cell, direction bin + trace); no network = CRT_TRACE_SORT_RAYS (order by origin cell and "
                          "direction bin + trace); seeded = CRT_TRACE_USE_PREDICTOR (t_max from an exact search of "
                          "the predicted treelet); plain and ordered modes trace on persistent warps that refill "

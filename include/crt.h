@@ -123,7 +123,8 @@ typedef struct crt_camera {
 #define CRT_TRACE_USE_PREDICTOR 0x4u /* seed t_max from the learned hit predictor */
 #define CRT_TRACE_STATS       0x8u  /* count visited nodes / tested triangles (slower) */
 #define CRT_TRACE_WIDE        0x10u /* walk the 4-wide nodes instead of the binary ones (same hits) */
-#define CRT_TRACE_PREDICTOR_ORDER 0x20u /* trace the rays grouped by their predicted treelet (same hits) */
+#define CRT_TRACE_PREDICTOR_ORDER 0x20u /* trace the rays grouped by the predictor's likeliest class (a treelet,
+                                           or miss) (same hits) */
 #define CRT_TRACE_SORT_RAYS   0x40u /* trace the rays ordered by origin cell and direction (same hits) */
 #define CRT_TRACE_COMPRESSED  0x80u /* walk 64-byte compressed 4-wide nodes: 8-bit child boxes rounded
                                        outward, exact leaf boxes re-checked (same hits); the reference
@@ -153,8 +154,8 @@ typedef struct crt_build_stats {
     uint32_t ploc_iterations;
     float ms_morton;     /* scene box + Morton codes */
     float ms_sort;       /* radix sort of (code, index) */
-    float ms_ploc;       /* PLOC iterations (+ the DFS layout on the one-launch path) */
-    float ms_layout;     /* DFS node layout when it runs as separate launches */
+    float ms_ploc;       /* PLOC iterations */
+    float ms_layout;     /* DFS node layout (inside the one-launch path: from its own timer stamps) */
     float ms_total;
     float scene_box[6];  /* min xyz, max xyz over the scanned buffer */
 } crt_build_stats;
@@ -529,9 +530,8 @@ crt_status crt_batch_predictor_create(crt_ctx* ctx, crt_batch* batch, const crt_
  * the process exits, which caps n_tris at CRT_NOALLOC_MAX_TRIANGLES (larger
  * inputs return CRT_ERR_INVALID_ARG).  All calls share that array: calls whose
  * work overlaps on the GPU race and must be serialised by the caller.  The
- * first call on a device looks up the array's device address and must come
- * before any stream capture on that device.  Returns after the stream
- * synchronises. */
+ * first call on a device looks up the array's device address.  Returns after
+ * the stream synchronises. */
 #define CRT_NOALLOC_MAX_TRIANGLES 262144u
 crt_status crt_morton_sort_noalloc(const crt_triangle* tris, uint32_t n_buffer, uint32_t n_tris,
                                    const crt_mesh_model* models, uint32_t n_models, uint32_t* codes_out,

@@ -743,8 +743,10 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     } else if (flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) {
         crt_predictor* pr = b->predictor;
         CRT_TRY(pr->classes.reserve(2ull * n_rays));
+        // ordering alone needs only the likeliest class; seeding needs the miss rule
         CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, n_rays, pr->classes.as<uint16_t>(),
-                                 pr->cfg.miss_threshold, x->err.as<uint32_t>(), x->stream));
+                                 pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), x->err.as<uint32_t>(),
+                                 x->stream));
         if (flags & CRT_TRACE_USE_PREDICTOR) {
             p.pred_class = pr->classes.as<uint16_t>();
             p.treelets = pr->treelets.as<crt::Treelet>();
@@ -1602,7 +1604,7 @@ crt_status crt_predictor_infer(crt_ctx* x, crt_predictor* pr, const crt_ray* ray
     }
     CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     CRT_CUDA(crt::pred_infer(pr->dev(), pr->nodes(), static_cast<const crt_ray*>(d_rays), n,
-                             d_out, pr->cfg.miss_threshold, x->err.as<uint32_t>(), x->stream));
+                             d_out, pr->cfg.miss_threshold, false, x->err.as<uint32_t>(), x->stream));
     if (!dev_out) CRT_CUDA(cudaMemcpyAsync(classes, d_out, 2ull * n, cudaMemcpyDeviceToHost, x->stream));
     return x->check_device_error();
 }
@@ -1785,7 +1787,7 @@ crt_status batch_trace_enqueue(crt_ctx* x, crt_batch* bt, const crt_ray* rays, u
     if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && bt->n_rays > 0) {
         crt_predictor* pr = bt->predictor;
         CRT_CUDA(crt::pred_infer(pr->dev(), pr->nodes(), rays, bt->n_rays, pr->classes.as<uint16_t>(),
-                                 pr->cfg.miss_threshold, err, s));
+                                 pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), err, s));
         if (flags & CRT_TRACE_USE_PREDICTOR) {
             p.pred_class = pr->classes.as<uint16_t>();
             p.treelets = pr->treelets.as<crt::Treelet>();

@@ -20,7 +20,7 @@
 //
 // Host code cannot use the array's name as a device address, so the first
 // call on each device looks the address up with cudaGetSymbolAddress while
-// that device is current; make that first call before any stream capture.
+// that device is current.
 // The address is kept per device together with the unique id of the CUDA
 // context it was looked up in (cuCtxGetId): after cudaDeviceReset the device
 // gets a new primary context, the library's device code is loaded again and

@@ -203,8 +203,13 @@ constexpr int kInferCtasPerSm = 4;
 static_assert(kInferSmemUsed <= kInferSmem && kInferCtasPerSm * kInferSmem <= 228 * 1024 &&
               (kInferCtasPerSm + 1) * kInferSmem > 228 * 1024, "inference tile layout and residency");
 
+// argmax: the class is the likeliest of all 128 (miss included), which is all
+// that ordering rays by class needs; otherwise the likeliest treelet unless
+// the miss class holds at least miss_threshold of the probability mass (the
+// seeding rule), which needs the softmax sum.
 __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bvh_node* nodes, const crt_ray* rays,
-                                                    uint32_t n, uint16_t* classes, float miss_threshold, uint32_t* err) {
+                                                    uint32_t n, uint16_t* classes, float miss_threshold, bool argmax,
+                                                    uint32_t* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sW1 = smem;
     unsigned char* sW2 = sW1 + 64 * 32 * 2;
@@ -286,15 +291,19 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
                 else if (l > best) { best = l; bc = c + j; }
             }
         }
-        float sum = 0.f;
-        for (int c = 0; c < 128; c += 16) {
-            float v[16];
-            tc::tmem_ld16(lane_addr(tb, c), v);
+        if (argmax) {
+            if (valid) classes[i] = static_cast<uint16_t>(lmiss >= best ? kMissClass : bc);
+        } else {
+            float sum = 0.f;
+            for (int c = 0; c < 128; c += 16) {
+                float v[16];
+                tc::tmem_ld16(lane_addr(tb, c), v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - lmax);
+                for (int j = 0; j < 16; ++j) sum += __expf(v[j] + sB[128 + c + j] - lmax);
+            }
+            const float p_miss = __expf(lmiss - lmax) / sum;
+            if (valid) classes[i] = static_cast<uint16_t>(p_miss >= miss_threshold ? kMissClass : bc);
         }
-        const float p_miss = __expf(lmiss - lmax) / sum;
-        if (valid) classes[i] = static_cast<uint16_t>(p_miss >= miss_threshold ? kMissClass : bc);
         tc::fence_before_sync();
         __syncthreads();
     }
@@ -977,7 +986,7 @@ cudaError_t pred_prepare() {
 }
 
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
-                       uint16_t* classes, float miss_threshold, uint32_t* err, cudaStream_t s) {
+                       uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(pred::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -989,7 +998,7 @@ cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const c
     const uint32_t cap = static_cast<uint32_t>(pred::kInferCtasPerSm) * kNumSms;
     const uint32_t grid = tiles < cap ? tiles : cap;
     if (grid == 0) return cudaSuccess;
-    pred::infer_kernel<<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold, err);
+    pred::infer_kernel<<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold, argmax, err);
     return cudaGetLastError();
 }
 

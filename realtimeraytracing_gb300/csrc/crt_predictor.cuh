@@ -80,8 +80,11 @@ void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s);
 // Sets the kernels' shared-memory attributes (done again on first use; call
 // before capturing predictor work into a graph).
 cudaError_t pred_prepare();
+// classes[i]: with argmax the likeliest of the 128 classes (treelets and
+// miss), used to order rays; otherwise the likeliest treelet unless P(miss) >=
+// miss_threshold (then the miss class), the seeding rule.
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
-                       uint16_t* classes, float miss_threshold, uint32_t* err, cudaStream_t s);
+                       uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s);
 cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n_rays,
                             const crt_hit* hits, const uint16_t* targets, uint32_t n_samples, uint32_t stride,
                             uint32_t offset, float* loss_sum, uint32_t* err, cudaStream_t s);
