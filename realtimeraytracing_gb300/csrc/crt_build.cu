@@ -213,8 +213,8 @@ __global__ void __launch_bounds__(256) morton_kernel(const crt_triangle* __restr
 //  * warp multisplit: each lane ORs its bit into the warp's shared-memory
 //    mask of its digit, so the lanes holding the same digit read their group
 //    back (fewer instructions than BITS ballots, and than match.any, on this
-//    part); the highest of them adds the group's size to the warp's digit
-//    counter and broadcasts the old count;
+//    part); every lane reads the warp's count of its digit, then the highest
+//    of the group adds the group's size (no branch to a leader, no shuffle);
 //  * chained-scan decoupled look-back across tiles for the global digit
 //    offsets; each digit's thread reads a window of LB_WIN predecessor tiles
 //    per round trip with relaxed loads (flag and count share one word);
@@ -301,15 +301,16 @@ __global__ void __launch_bounds__(BLOCK, 3) onesweep_kernel(const uint32_t* __re
         if (ok) atomicOr(my_match + d, 1u << lane);
         __syncwarp();
         const uint32_t peers = ok ? my_match[d] : 0u;
+        // every lane reads its digit's running count (the lanes of one digit
+        // read one word: a broadcast); after the warp has read, the group's
+        // highest lane alone adds the group's size and clears the mask
+        const uint32_t base = my_hist[d];
         __syncwarp();
-        const int leader = 31 - __clz(peers | 1u);  // the highest peer; lanes without a key read lane 0
-        uint32_t base = 0;
-        if (ok && lane == static_cast<uint32_t>(leader)) {  // one leader per digit: plain updates
-            base = my_hist[d];
+        if (ok && (peers >> lane) == 1u) {
             my_hist[d] = base + static_cast<uint32_t>(__popc(peers));
             my_match[d] = 0u;
         }
-        pos[j] = __shfl_sync(0xFFFFFFFFu, base, leader) + __popc(peers & lt_mask);
+        pos[j] = base + __popc(peers & lt_mask);
         __syncwarp();
     }
     __syncthreads();
