@@ -204,6 +204,11 @@ struct crt_ctx {
     cudaEvent_t ev[6] = {};
     // crt_trace timing: start, traversal kernel launch, end (on the stream)
     cudaEvent_t tev[3] = {};
+    // host rays copied in chunks on a second stream so that each chunk's
+    // predictor inference runs while the next chunk is in flight
+    static constexpr int kCopyChunks = 8;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_ev[kCopyChunks + 1] = {};
     bool tev_valid = false;
     crt_build_stats stats{};
     std::vector<uint2> it_host;
@@ -286,6 +291,10 @@ crt_status crt_create(crt_ctx** out, const crt_config* cfg) {
         if (s == CRT_OK && cudaEventCreate(&e) != cudaSuccess) s = fail(CRT_ERR_CUDA, "event");
     for (auto& e : x->tev)
         if (s == CRT_OK && cudaEventCreate(&e) != cudaSuccess) s = fail(CRT_ERR_CUDA, "event");
+    if (s == CRT_OK && cudaStreamCreateWithFlags(&x->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+        s = fail(CRT_ERR_CUDA, "stream");
+    for (auto& e : x->copy_ev)
+        if (s == CRT_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) s = fail(CRT_ERR_CUDA, "event");
     if (s == CRT_OK) s = x->scene_state.reserve(sizeof(crt::SceneState));
     if (s == CRT_OK) s = x->err.reserve(16);
     if (s == CRT_OK) s = x->models.reserve(2 * 64 * 16 * sizeof(float));
@@ -323,7 +332,13 @@ crt_status crt_destroy(crt_ctx* x) {
         if (e) cudaEventDestroy(e);
     for (auto& e : x->tev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : x->copy_ev)
+        if (e) cudaEventDestroy(e);
     if (x->pinned) cudaFreeHost(x->pinned);
+    if (x->copy_stream) {
+        cudaStreamSynchronize(x->copy_stream);
+        cudaStreamDestroy(x->copy_stream);
+    }
     if (x->stream) cudaStreamDestroy(x->stream);
     delete x;
     return CRT_OK;
@@ -710,9 +725,13 @@ crt_status ensure_cwide(crt_ctx* x, const crt_bvh* b) {
 
 // Enqueues one traversal launch on device-resident rays/hits (no sync).
 constexpr uint32_t kPoolMinRays = 65536;  // below this a launch of one thread per ray fills the GPU as well
+constexpr uint32_t kChunkedCopyMinRays = 1u << 20;  // crt_trace: smaller host batches copy in one piece
 
+// classes_ready: the predictor's classes of these rays are already in its
+// class buffer (crt_trace's chunked copy ran the inference per chunk).
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
-                        crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0) {
+                        crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0,
+                        bool classes_ready = false) {
     if (n_rays == 0) return CRT_OK;
     if (flags & CRT_TRACE_WIDE) CRT_TRY(ensure_wide4(x, b));
     if (flags & CRT_TRACE_COMPRESSED) CRT_TRY(ensure_cwide(x, b));
@@ -744,9 +763,10 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
         crt_predictor* pr = b->predictor;
         CRT_TRY(pr->classes.reserve(2ull * n_rays));
         // ordering alone needs only the likeliest class; seeding needs the miss rule
-        CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, n_rays, pr->classes.as<uint16_t>(),
-                                 pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), x->err.as<uint32_t>(),
-                                 x->stream));
+        if (!classes_ready)
+            CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, n_rays, pr->classes.as<uint16_t>(),
+                                     pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), x->err.as<uint32_t>(),
+                                     x->stream));
         if (flags & CRT_TRACE_USE_PREDICTOR) {
             p.pred_class = pr->classes.as<uint16_t>();
             p.treelets = pr->treelets.as<crt::Treelet>();
@@ -1256,13 +1276,43 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
     if (is_device_ptr(rays)) CRT_TRY(check_aligned16(rays, "crt_trace: rays"));
     if (is_device_ptr(hits)) CRT_TRY(check_aligned16(hits, "crt_trace: hits"));
     const crt_ray* d_rays = rays;
+    bool classes_ready = false;
+    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
     if (!is_device_ptr(rays)) {
         // Page-locked host rays are read in place by the trace kernel when it
         // reads each ray once, in order; reordered or predicted traces read
         // them more than once and out of order, so those copy them in first.
         const bool once = !(flags & (CRT_TRACE_SORT_RAYS | CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_USE_PREDICTOR));
+        const bool chunked = (flags & CRT_TRACE_PREDICTOR_ORDER) && !(flags & CRT_TRACE_USE_PREDICTOR) &&
+                             b->predictor && n_rays >= kChunkedCopyMinRays;
         if (void* m = once ? mapped_host_ptr(const_cast<crt_ray*>(rays)) : nullptr) {
             d_rays = static_cast<const crt_ray*>(m);
+        } else if (chunked) {
+            // Ordering by the predictor: copy the rays in kCopyChunks pieces on
+            // the copy stream and run each piece's inference on the context's
+            // stream as soon as it has landed, so the inference hides behind the
+            // copy; the ordering and the trace then wait for the last piece.
+            crt_predictor* pr = b->predictor;
+            CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
+            CRT_TRY(pr->classes.reserve(2ull * n_rays));
+            crt_ray* dst = x->rays_in.as<crt_ray>();
+            CRT_CUDA(cudaEventRecord(x->copy_ev[crt_ctx::kCopyChunks], x->stream));  // earlier readers of rays_in
+            CRT_CUDA(cudaStreamWaitEvent(x->copy_stream, x->copy_ev[crt_ctx::kCopyChunks], 0));
+            const uint32_t per = ((n_rays + crt_ctx::kCopyChunks - 1) / crt_ctx::kCopyChunks + 127u) & ~127u;
+            for (int c = 0; c < crt_ctx::kCopyChunks; ++c) {
+                const uint32_t off = static_cast<uint32_t>(c) * per;
+                if (off >= n_rays) break;
+                const uint32_t cnt = std::min(per, n_rays - off);
+                CRT_CUDA(cudaMemcpyAsync(dst + off, rays + off, sizeof(crt_ray) * cnt, cudaMemcpyHostToDevice,
+                                         x->copy_stream));
+                CRT_CUDA(cudaEventRecord(x->copy_ev[c], x->copy_stream));
+                CRT_CUDA(cudaStreamWaitEvent(x->stream, x->copy_ev[c], 0));
+                CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), dst + off, cnt,
+                                         pr->classes.as<uint16_t>() + off, pr->cfg.miss_threshold, true,
+                                         x->err.as<uint32_t>(), x->stream));
+            }
+            d_rays = dst;
+            classes_ready = true;
         } else {
             CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
             CRT_CUDA(cudaMemcpyAsync(x->rays_in.p, rays, sizeof(crt_ray) * n_rays, cudaMemcpyHostToDevice, x->stream));
@@ -1281,8 +1331,7 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
         CRT_TRY(x->hits_out.reserve(sizeof(crt_hit) * n_rays));
         d_hits = x->hits_out.as<crt_hit>();
     }
-    CRT_CUDA(cudaMemsetAsync(x->err.p, 0, 16, x->stream));
-    CRT_TRY(trace_device(x, b, d_rays, n_rays, flags, d_hits));
+    CRT_TRY(trace_device(x, b, d_rays, n_rays, flags, d_hits, nullptr, 0, classes_ready));
     if (!dev_out) CRT_CUDA(cudaMemcpyAsync(hits, d_hits, sizeof(crt_hit) * n_rays, cudaMemcpyDeviceToHost, x->stream));
     CRT_TRY(x->check_device_error());
     if (flags & CRT_TRACE_STATS)

@@ -212,3 +212,25 @@ def test_adam_step_matches_numpy(ctx):
     assert np.abs(p1 - p0).max() > 1e-4  # the step moved the weights
     pred.free()
     bvh.free()
+
+
+def test_learned_order_from_host_rays_in_pieces(ctx, scene):
+    """crt_trace of 1 M or more host rays with CRT_TRACE_PREDICTOR_ORDER copies
+    the rays in pieces on a second stream and runs each piece's inference as
+    soon as it has landed; the hits equal the plain trace's bit for bit, from
+    pageable and from page-locked host memory, and below the piece threshold."""
+    bvh, _ = scene
+    pred = crt.Predictor(ctx, bvh, seed=9)
+    rays = S.sphere_rays(1_200_000, seed=97)
+    plain = ctx.trace(bvh, rays, crt.TRI_WATERTIGHT)
+    pred.train(rays[:200_000], plain[:200_000], offset=0)
+    flags = crt.TRI_WATERTIGHT | crt.PREDICTOR_ORDER
+    got = ctx.trace(bvh, rays, flags)
+    np.testing.assert_array_equal(got.view(np.uint32), plain.view(np.uint32))
+    pinned_rays = torch.from_numpy(rays).pin_memory()
+    pinned_hits = torch.empty((rays.shape[0], 4), dtype=torch.float32).pin_memory()
+    ctx.trace(bvh, pinned_rays, flags, out=pinned_hits)
+    np.testing.assert_array_equal(pinned_hits.numpy().view(np.uint32), plain.view(np.uint32))
+    small = ctx.trace(bvh, rays[:300_001], flags)
+    np.testing.assert_array_equal(small.view(np.uint32), plain[:300_001].view(np.uint32))
+    pred.free()
