@@ -567,21 +567,57 @@ __device__ __forceinline__ void ploc_nearest(PlocSmem<TILE, BLOCK, MAXR>& S, int
     }
 }
 
+// Nearest neighbour of position p, whose box is at window index w (window
+// entries outside [0, n) infinite): the 2R candidates in increasing j (strict
+// minimum: lowest j on ties).  RC > 0: compile-time radius.
+template <int RC, int TILE, int BLOCK, int MAXR>
+__device__ __forceinline__ uint32_t ploc_nearest_at(const PlocSmem<TILE, BLOCK, MAXR>& S, int p, int w, int R_rt) {
+    const int R = RC > 0 ? RC : R_rt;
+    const float amnx = S.mnx[w], amny = S.mny[w], amnz = S.mnz[w], amxx = S.mxx[w], amxy = S.mxy[w], amxz = S.mxz[w];
+    float best = __int_as_float(0x7F800000);
+    int bj = p;
+    auto visit = [&](int d) {
+        const int wj = w + d;
+        const float dx = fmaxf(amxx, S.mxx[wj]) - fminf(amnx, S.mnx[wj]);
+        const float dy = fmaxf(amxy, S.mxy[wj]) - fminf(amny, S.mny[wj]);
+        const float dz = fmaxf(amxz, S.mxz[wj]) - fminf(amnz, S.mnz[wj]);
+        const float v = 2.0f * (dx * dy + dy * dz + dz * dx);
+        if (v < best) { best = v; bj = p + d; }
+    };
+    if (RC > 0) {
+#pragma unroll
+        for (int d = -RC; d <= RC; ++d)
+            if (d != 0) visit(d);
+    } else {
+        for (int d = -R; d <= R; ++d)
+            if (d != 0) visit(d);
+    }
+    return static_cast<uint32_t>(bj);
+}
+
 // One tile of one PLOC iteration (see above).  Reads of data other blocks
 // wrote (the cluster array) bypass L1 (__ldcg), so the same code is correct
 // inside the persistent kernel, where no launch boundary separates iterations.
-template <int TILE, int BLOCK, int MAXR>
+// SMALL: a tile owns ploc_own_small(R) = BLOCK - 2R positions and each thread
+// searches one position (instead of four): for iterations whose tiles all run
+// at once, one per SM or fewer, where a tile's latency is the iteration's.
+template <int BLOCK>
+__host__ __device__ constexpr uint32_t ploc_own_small(int radius) {
+    return static_cast<uint32_t>(BLOCK) - 2u * static_cast<uint32_t>(radius);
+}
+template <int TILE, int BLOCK, int MAXR, bool SMALL = false>
 __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32_t tile, const uint2 cur, int iter,
                                           const float4* __restrict__ cin, float4* __restrict__ cout,
                                           float4* __restrict__ node_box, uint4* __restrict__ node_kids, uint2* it,
                                           uint32_t N, int R, unsigned long long* lb_cur, unsigned long long* lb_next,
                                           uint32_t* err, uint32_t spin_limit) {
-    constexpr int IPT = 4;
+    constexpr int IPT = SMALL ? 1 : 4;
+    const int own = static_cast<int>(SMALL ? ploc_own_small<BLOCK>(R) : ploc_own(R));
     const int n = static_cast<int>(cur.x);
-    const int s = static_cast<int>(tile * ploc_own(R));
+    const int s = static_cast<int>(tile) * own;
     __syncthreads();  // the previous tile of this block is done with S
     if (threadIdx.x == 0) st_relaxed_u64(&lb_next[tile], 0ull);
-    const int e = min(n, s + static_cast<int>(ploc_own(R)));
+    const int e = min(n, s + own);
     const int wbase = s - 2 * R;  // window index 0
     const int lo = max(0, wbase);
     const int hi = min(n, e + 2 * R);
@@ -593,7 +629,7 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
         S.mxx[w] = b.x; S.mxy[w] = b.y; S.mxz[w] = b.z; S.lc[w] = __float_as_uint(b.w);
     }
     {  // window entries of positions outside [0, n): infinite boxes
-        constexpr int kWin = PlocSmem<TILE, BLOCK, MAXR>::kWin;
+        const int kWin = SMALL ? BLOCK + 2 * R : PlocSmem<TILE, BLOCK, MAXR>::kWin;  // the entries the search reads
         const float inf = __int_as_float(0x7F800000);
         const int below = lo - wbase, above = hi - wbase;
         for (int w = threadIdx.x; w < kWin; w += BLOCK) {
@@ -603,11 +639,27 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
         }
     }
     __syncthreads();
-    switch (R) {
-        case 8: ploc_nearest<8>(S, s, e, n, R); break;
-        case 16: ploc_nearest<16>(S, s, e, n, R); break;
-        case 32: ploc_nearest<32>(S, s, e, n, R); break;
-        default: ploc_nearest<0>(S, s, e, n, R); break;
+    if (SMALL) {
+        // thread t: position q = s - R + t at window index t + R; [s - R, e + R)
+        // fits since e - s <= BLOCK - 2R
+        const int t = static_cast<int>(threadIdx.x), q = s - R + t;
+        if (q >= 0 && q < n && q < e + R) {
+            uint32_t j;
+            switch (R) {
+                case 8: j = ploc_nearest_at<8>(S, q, t + R, R); break;
+                case 16: j = ploc_nearest_at<16>(S, q, t + R, R); break;
+                case 32: j = ploc_nearest_at<32>(S, q, t + R, R); break;
+                default: j = ploc_nearest_at<0>(S, q, t + R, R); break;
+            }
+            S.nn[t] = j;
+        }
+    } else {
+        switch (R) {
+            case 8: ploc_nearest<8>(S, s, e, n, R); break;
+            case 16: ploc_nearest<16>(S, s, e, n, R); break;
+            case 32: ploc_nearest<32>(S, s, e, n, R); break;
+            default: ploc_nearest<0>(S, s, e, n, R); break;
+        }
     }
     __syncthreads();
 
@@ -728,34 +780,10 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
     }
 }
 
-// Nearest neighbour of position p (< n) in a whole-array window (position q
-// at window index q + 2R, entries outside [0, n) infinite): the thread's one
-// position, the 2R candidates in increasing j (strict minimum: lowest j on
-// ties).  RC > 0: compile-time radius.
+// The same for a whole-array window (position q at window index q + 2R).
 template <int RC, int TILE, int BLOCK, int MAXR>
 __device__ __forceinline__ uint32_t ploc_nearest_one(const PlocSmem<TILE, BLOCK, MAXR>& S, int p, int R_rt) {
-    const int R = RC > 0 ? RC : R_rt;
-    const int w = p + 2 * R;
-    const float amnx = S.mnx[w], amny = S.mny[w], amnz = S.mnz[w], amxx = S.mxx[w], amxy = S.mxy[w], amxz = S.mxz[w];
-    float best = __int_as_float(0x7F800000);
-    int bj = p;
-    auto visit = [&](int d) {
-        const int wj = w + d;
-        const float dx = fmaxf(amxx, S.mxx[wj]) - fminf(amnx, S.mnx[wj]);
-        const float dy = fmaxf(amxy, S.mxy[wj]) - fminf(amny, S.mny[wj]);
-        const float dz = fmaxf(amxz, S.mxz[wj]) - fminf(amnz, S.mnz[wj]);
-        const float v = 2.0f * (dx * dy + dy * dz + dz * dx);
-        if (v < best) { best = v; bj = p + d; }
-    };
-    if (RC > 0) {
-#pragma unroll
-        for (int d = -RC; d <= RC; ++d)
-            if (d != 0) visit(d);
-    } else {
-        for (int d = -R; d <= R; ++d)
-            if (d != 0) visit(d);
-    }
-    return static_cast<uint32_t>(bj);
+    return ploc_nearest_at<RC>(S, p, p + 2 * (RC > 0 ? RC : R_rt), R_rt);
 }
 
 // The last PLOC iterations, once every live cluster fits in one tile (n <=
@@ -1152,13 +1180,28 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
         unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
         unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
         const uint32_t n_tiles = (cur.x + ploc_own(R) - 1) / ploc_own(R);
-        if (n_tiles <= gridDim.x) {
+        const uint32_t n_small = (cur.x + ploc_own_small<BLOCK>(R) - 1) / ploc_own_small<BLOCK>(R);
+        // one position per thread while the small tiles number at most one
+        // per SM (and fit the look-back arrays): the iteration then costs one
+        // tile's latency, and a thread searches one position instead of four
+        const bool small = n_small <= gridDim.x / kPlocBlocksPerSm && n_small <= n_tiles_cap;
+        if (small || n_tiles <= gridDim.x) {
             // One wave: block b runs tile b (all tiles are co-resident, so
             // every look-back wait ends), with no ticket round trips.
             if (blockIdx.x == 0 && threadIdx.x == 0) tickets[(iter + 1) & 1] = 0u;
-            if (blockIdx.x < n_tiles)
+            // Every block clears its word of the next iteration's look-back
+            // array: the next iteration may cut its (fewer) clusters into more,
+            // smaller tiles than this one has, and a tile clears only its own
+            // word (the grid barrier below orders these stores before any read).
+            if (threadIdx.x == 0 && blockIdx.x < n_tiles_cap) st_relaxed_u64(&lb_next[blockIdx.x], 0ull);
+            if (small) {
+                if (blockIdx.x < n_small)
+                    ploc_tile<TILE, BLOCK, MAXR, true>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R,
+                                                       lb_cur, lb_next, err, spin_limit);
+            } else if (blockIdx.x < n_tiles) {
                 ploc_tile<TILE, BLOCK, MAXR>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur,
                                              lb_next, err, spin_limit);
+            }
             if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
             if (static_cast<uint32_t>(iter) + 1 >= N) { raise_error(err, kDevIterLimit); return; }
             continue;
