@@ -598,21 +598,22 @@ __device__ __forceinline__ uint32_t ploc_nearest_at(const PlocSmem<TILE, BLOCK, 
 // One tile of one PLOC iteration (see above).  Reads of data other blocks
 // wrote (the cluster array) bypass L1 (__ldcg), so the same code is correct
 // inside the persistent kernel, where no launch boundary separates iterations.
-// SMALL: a tile owns ploc_own_small(R) = BLOCK - 2R positions and each thread
-// searches one position (instead of four): for iterations whose tiles all run
-// at once, one per SM or fewer, where a tile's latency is the iteration's.
-template <int BLOCK>
-__host__ __device__ constexpr uint32_t ploc_own_small(int radius) {
-    return static_cast<uint32_t>(BLOCK) - 2u * static_cast<uint32_t>(radius);
+// IPT < 4: a tile owns ploc_own_ipt(R) = IPT*BLOCK - 2R positions and each
+// thread searches IPT positions (instead of four): for iterations whose tiles
+// all run at once, where a tile's latency is the iteration's.
+template <int IPT, int BLOCK>
+__host__ __device__ constexpr uint32_t ploc_own_ipt(int radius) {
+    return static_cast<uint32_t>(IPT * BLOCK) - 2u * static_cast<uint32_t>(radius);
 }
-template <int TILE, int BLOCK, int MAXR, bool SMALL = false>
+template <int TILE, int BLOCK, int MAXR, int IPT = 4>
 __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32_t tile, const uint2 cur, int iter,
                                           const float4* __restrict__ cin, float4* __restrict__ cout,
                                           float4* __restrict__ node_box, uint4* __restrict__ node_kids, uint2* it,
                                           uint32_t N, int R, unsigned long long* lb_cur, unsigned long long* lb_next,
                                           uint32_t* err, uint32_t spin_limit) {
-    constexpr int IPT = SMALL ? 1 : 4;
-    const int own = static_cast<int>(SMALL ? ploc_own_small<BLOCK>(R) : ploc_own(R));
+    static_assert(IPT == 1 || IPT == 2 || IPT == 4, "one, two or four positions per thread");
+    constexpr bool SMALL = IPT < 4;
+    const int own = static_cast<int>(SMALL ? ploc_own_ipt<IPT, BLOCK>(R) : ploc_own(R));
     const int n = static_cast<int>(cur.x);
     const int s = static_cast<int>(tile) * own;
     __syncthreads();  // the previous tile of this block is done with S
@@ -629,7 +630,7 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
         S.mxx[w] = b.x; S.mxy[w] = b.y; S.mxz[w] = b.z; S.lc[w] = __float_as_uint(b.w);
     }
     {  // window entries of positions outside [0, n): infinite boxes
-        const int kWin = SMALL ? BLOCK + 2 * R : PlocSmem<TILE, BLOCK, MAXR>::kWin;  // the entries the search reads
+        const int kWin = SMALL ? IPT * BLOCK + 2 * R : PlocSmem<TILE, BLOCK, MAXR>::kWin;  // the entries the search reads
         const float inf = __int_as_float(0x7F800000);
         const int below = lo - wbase, above = hi - wbase;
         for (int w = threadIdx.x; w < kWin; w += BLOCK) {
@@ -640,18 +641,21 @@ __device__ __forceinline__ void ploc_tile(PlocSmem<TILE, BLOCK, MAXR>& S, uint32
     }
     __syncthreads();
     if (SMALL) {
-        // thread t: position q = s - R + t at window index t + R; [s - R, e + R)
-        // fits since e - s <= BLOCK - 2R
-        const int t = static_cast<int>(threadIdx.x), q = s - R + t;
-        if (q >= 0 && q < n && q < e + R) {
-            uint32_t j;
-            switch (R) {
-                case 8: j = ploc_nearest_at<8>(S, q, t + R, R); break;
-                case 16: j = ploc_nearest_at<16>(S, q, t + R, R); break;
-                case 32: j = ploc_nearest_at<32>(S, q, t + R, R); break;
-                default: j = ploc_nearest_at<0>(S, q, t + R, R); break;
+        // thread t: positions q = s - R + IPT*t + i at window index IPT*t + i + R;
+        // [s - R, e + R) fits since e - s <= IPT*BLOCK - 2R
+#pragma unroll
+        for (int i = 0; i < IPT; ++i) {
+            const int t = IPT * static_cast<int>(threadIdx.x) + i, q = s - R + t;
+            if (q >= 0 && q < n && q < e + R) {
+                uint32_t j;
+                switch (R) {
+                    case 8: j = ploc_nearest_at<8>(S, q, t + R, R); break;
+                    case 16: j = ploc_nearest_at<16>(S, q, t + R, R); break;
+                    case 32: j = ploc_nearest_at<32>(S, q, t + R, R); break;
+                    default: j = ploc_nearest_at<0>(S, q, t + R, R); break;
+                }
+                S.nn[t] = j;
             }
-            S.nn[t] = j;
         }
     } else {
         switch (R) {
@@ -1011,12 +1015,12 @@ __device__ __forceinline__ uint2 layout_place(uint32_t X, const uint2* __restric
 // parity << 31).  PUBLISH: each internal child's record goes out as one
 // 64-bit relaxed store, which a thread polling for it (the dataflow layout
 // below) reads whole; the record is all it needs from the parent.
+// kids: X's node_kids record (left id, right id, their leaf counts), which the
+// dataflow pass loads before it waits for X's position.
 template <bool PUBLISH>
-__device__ __forceinline__ void layout_down_at(uint32_t X, uint2 me, const uint4* __restrict__ node_kids,
-                                               uint2* __restrict__ pf, uint32_t N, uint32_t* __restrict__ dfs,
-                                               uint32_t* err) {
+__device__ __forceinline__ void layout_down_at(uint32_t X, uint2 me, const uint4 kids, uint2* __restrict__ pf,
+                                               uint32_t N, uint32_t* __restrict__ dfs, uint32_t* err) {
     const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
-    const uint4 kids = __ldcg(node_kids + (X - N));  // left id, right id, their leaf counts
     const uint32_t a = kids.x, b = kids.y, lca = kids.z;
     const uint32_t pl = p + 1, pr = p + 2 * lca;
     if (pr >= 2 * N - 1 || p < f || p - f >= N - 1 || (b >= N && b - N >= N - 1) || (a >= N && a - N >= N - 1)) {
@@ -1039,9 +1043,36 @@ __device__ __forceinline__ void layout_down_at(uint32_t X, uint2 me, const uint4
     if (b < N) dfs[pr] = b; else pf[b - N] = make_uint2(pr, (f + lca) | nodd);
 }
 
+// The dataflow pass also publishes the places of X's grandchildren (from its
+// children's node_kids records kc[0], kc[1], loaded while X waited), so
+// places travel two levels per round trip through L2.  X's internal child
+// later publishes the same words (the same arithmetic on the same inputs);
+// whichever store lands first, the word is the same.  Out-of-range records
+// are skipped here: the child's own pass reports them.
+__device__ __forceinline__ void layout_publish_grandchildren(uint2 me, const uint4 kids, const uint4 kc[2],
+                                                            uint2* __restrict__ pf, uint32_t N) {
+    const uint32_t p = me.x, f = me.y & 0x7FFFFFFFu, odd = me.y >> 31;
+    const uint32_t cp[2] = {p + 1, p + 2 * kids.z}, cf[2] = {f, f + kids.z};
+    const uint32_t gpar = odd << 31;  // two levels down: X's own depth parity
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const uint32_t id = c ? kids.y : kids.x;
+        if (id < N || id - N >= N - 1) continue;  // a leaf child (or corrupt)
+        const uint32_t ga = kc[c].x, gb = kc[c].y, lga = kc[c].z;
+        const uint32_t gpl = cp[c] + 1, gpr = cp[c] + 2 * lga;
+        if (gpr >= 2 * N - 1) continue;
+        if (ga >= N && ga - N < N - 1)
+            st_relaxed_u64(reinterpret_cast<unsigned long long*>(pf + (ga - N)),
+                           (static_cast<unsigned long long>(cf[c] | gpar) << 32) | gpl);
+        if (gb >= N && gb - N < N - 1)
+            st_relaxed_u64(reinterpret_cast<unsigned long long*>(pf + (gb - N)),
+                           (static_cast<unsigned long long>((cf[c] + lga) | gpar) << 32) | gpr);
+    }
+}
+
 __device__ __forceinline__ void layout_down(uint32_t X, const uint4* __restrict__ node_kids, uint2* __restrict__ pf,
                                             uint32_t N, uint32_t* __restrict__ dfs, uint32_t* err) {
-    layout_down_at<false>(X, layout_place(X, pf, N), node_kids, pf, N, dfs, err);
+    layout_down_at<false>(X, layout_place(X, pf, N), __ldcg(node_kids + (X - N)), pf, N, dfs, err);
 }
 
 // grow: the scene's abs_eps; wide_wt receives the traversal nodes with every
@@ -1180,11 +1211,16 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
         unsigned long long* lb_cur = lookback + static_cast<size_t>(iter & 1) * n_tiles_cap;
         unsigned long long* lb_next = lookback + static_cast<size_t>((iter + 1) & 1) * n_tiles_cap;
         const uint32_t n_tiles = (cur.x + ploc_own(R) - 1) / ploc_own(R);
-        const uint32_t n_small = (cur.x + ploc_own_small<BLOCK>(R) - 1) / ploc_own_small<BLOCK>(R);
-        // one position per thread while the small tiles number at most one
-        // per SM (and fit the look-back arrays): the iteration then costs one
-        // tile's latency, and a thread searches one position instead of four
-        const bool small = n_small <= gridDim.x / kPlocBlocksPerSm && n_small <= n_tiles_cap;
+        const uint32_t n_t1 = (cur.x + ploc_own_ipt<1, BLOCK>(R) - 1) / ploc_own_ipt<1, BLOCK>(R);
+        const uint32_t n_t2 = (cur.x + ploc_own_ipt<2, BLOCK>(R) - 1) / ploc_own_ipt<2, BLOCK>(R);
+        // one (two) positions per thread while those smaller tiles number at
+        // most kPlocSmallTiles1 (kPlocSmallTiles2) per SM and fit the look-back
+        // arrays: the iteration then costs one short tile's latency
+        const uint32_t per_sm = gridDim.x / kPlocBlocksPerSm;
+        const int ipt = (n_t1 <= kPlocSmallTiles1 * per_sm && n_t1 <= n_tiles_cap)   ? 1
+                        : (n_t2 <= kPlocSmallTiles2 * per_sm && n_t2 <= n_tiles_cap) ? 2
+                                                                                      : 4;
+        const bool small = ipt < 4;
         if (small || n_tiles <= gridDim.x) {
             // One wave: block b runs tile b (all tiles are co-resident, so
             // every look-back wait ends), with no ticket round trips.
@@ -1194,10 +1230,14 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
             // smaller tiles than this one has, and a tile clears only its own
             // word (the grid barrier below orders these stores before any read).
             if (threadIdx.x == 0 && blockIdx.x < n_tiles_cap) st_relaxed_u64(&lb_next[blockIdx.x], 0ull);
-            if (small) {
-                if (blockIdx.x < n_small)
-                    ploc_tile<TILE, BLOCK, MAXR, true>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R,
-                                                       lb_cur, lb_next, err, spin_limit);
+            if (ipt == 1) {
+                if (blockIdx.x < n_t1)
+                    ploc_tile<TILE, BLOCK, MAXR, 1>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R,
+                                                    lb_cur, lb_next, err, spin_limit);
+            } else if (ipt == 2) {
+                if (blockIdx.x < n_t2)
+                    ploc_tile<TILE, BLOCK, MAXR, 2>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R,
+                                                    lb_cur, lb_next, err, spin_limit);
             } else if (blockIdx.x < n_tiles) {
                 ploc_tile<TILE, BLOCK, MAXR>(S, blockIdx.x, cur, iter, cin, cout, node_box, node_kids, it, N, R, lb_cur,
                                              lb_next, err, spin_limit);
@@ -1249,6 +1289,14 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
     bool gave_up = false;
     for (uint32_t t = blockIdx.x * BLOCK + threadIdx.x; t + 1 < N && !gave_up; t += gridDim.x * BLOCK) {
         const uint32_t X = 2 * N - 2 - t;
+        // X's record (and, for the grid's first round of nodes, the top of the
+        // tree, where the chain of places is the latency that counts, its
+        // internal children's), in flight while X's place is awaited
+        const bool top = t < gridDim.x * BLOCK;
+        const uint4 kids = __ldcg(node_kids + (X - N));
+        uint4 kc[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+        if (top && kids.x >= N && kids.x - N < N - 1) kc[0] = __ldcg(node_kids + (kids.x - N));
+        if (top && kids.y >= N && kids.y - N < N - 1) kc[1] = __ldcg(node_kids + (kids.y - N));
         uint2 me = make_uint2(0u, 0u);  // the root's place
         if (X != 2 * N - 2) {
             const unsigned long long* w = reinterpret_cast<const unsigned long long*>(pf + (X - N));
@@ -1265,7 +1313,8 @@ __global__ void __launch_bounds__(BLOCK, kPlocBlocksPerSm) ploc_persistent_kerne
             if (gave_up) break;
             me = make_uint2(static_cast<uint32_t>(v), static_cast<uint32_t>(v >> 32));
         }
-        layout_down_at<true>(X, me, node_kids, pf, N, dfs, err);
+        if (top) layout_publish_grandchildren(me, kids, kc, pf, N);
+        layout_down_at<true>(X, me, kids, pf, N, dfs, err);
     }
     if (!grid_barrier(bar, bar_target, err, spin_limit)) return;
     const float grow = st->abs_eps;

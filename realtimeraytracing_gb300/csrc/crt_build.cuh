@@ -19,6 +19,11 @@ constexpr uint32_t kPlocSpan = 1024;
 constexpr int kPlocMaxRadius = 32;        // largest supported PLOC radius
 // Co-resident blocks per SM of the persistent (cooperative) PLOC launches.
 constexpr int kPlocBlocksPerSm = 3;
+// One-wave PLOC iterations search one (two) positions per thread once those
+// smaller tiles number at most this many per SM (all co-resident).
+constexpr uint32_t kPlocSmallTiles1 = 3;  // measured best of 1-3 (1.31 M build: PLOC 0.72 -> 0.67 ms)
+constexpr uint32_t kPlocSmallTiles2 = 3;
+static_assert(kPlocSmallTiles1 <= kPlocBlocksPerSm && kPlocSmallTiles2 <= kPlocBlocksPerSm, "co-resident tiles");
 constexpr uint32_t kPlocMinOwn = kPlocSpan - 2u * kPlocMaxRadius;  // sizes look-back arrays for any radius
 __host__ __device__ constexpr uint32_t ploc_own(int radius) { return kPlocSpan - 2u * static_cast<uint32_t>(radius); }
 constexpr uint32_t kLeafRef = 0x80000000u;  // traversal child reference: leaf flag | sorted position
