@@ -437,8 +437,9 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(n * 16), "ms_per_step": round(e2e_t, 4),
                     "transfer": "crt_trace on page-locked host rays (copied in on the library stream) and host hits "
                                 "(written by the trace kernel over the CPU-GPU link), host-timed around the call"},
-            "gpu_launches": 7 * args.steps,
-            "gpu_launches_note": "per step: infer_kernel, order_keys_kernel, 4 onesweep_kernel passes, trace_pool_kernel",
+            "gpu_launches": 6 * args.steps,
+            "gpu_launches_note": "per step: infer_kernel (which also writes the order keys and their digit histograms), "
+                                 "4 onesweep_kernel passes, trace_pool_kernel",
             "roofline": {"kernel": "trace_pool_kernel (learned step: persistent warps over the rays in predicted "
                                    "order, closest hit, watertight)",
                          "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

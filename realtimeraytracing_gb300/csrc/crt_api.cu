@@ -728,7 +728,8 @@ constexpr uint32_t kPoolMinRays = 65536;  // below this a launch of one thread p
 constexpr uint32_t kChunkedCopyMinRays = 1u << 20;  // crt_trace: smaller host batches copy in one piece
 
 // classes_ready: the predictor's classes of these rays are already in its
-// class buffer (crt_trace's chunked copy ran the inference per chunk).
+// class buffer, and with CRT_TRACE_PREDICTOR_ORDER their order keys in its
+// order scratch (crt_trace's chunked copy ran the inference per chunk).
 crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uint32_t n_rays, uint32_t flags,
                         crt_hit* d_hits, const uint16_t* seed_classes = nullptr, uint32_t tile_width = 0,
                         bool classes_ready = false) {
@@ -762,22 +763,29 @@ crt_status trace_device(crt_ctx* x, const crt_bvh* b, const crt_ray* d_rays, uin
     } else if (flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) {
         crt_predictor* pr = b->predictor;
         CRT_TRY(pr->classes.reserve(2ull * n_rays));
-        // ordering alone needs only the likeliest class; seeding needs the miss rule
-        if (!classes_ready)
+        // ordering alone needs only the likeliest class, and then the inference
+        // also writes the trace order keys; seeding needs the miss rule
+        const bool fuse = (flags & CRT_TRACE_PREDICTOR_ORDER) && !(flags & CRT_TRACE_USE_PREDICTOR);
+        if (flags & CRT_TRACE_PREDICTOR_ORDER) {
+            CRT_TRY(pr->order.reserve(4ull * n_rays));
+            CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
+        }
+        if (!classes_ready) {
+            uint32_t *okeys = nullptr, *ohist = nullptr;
+            if (fuse) crt::pred_order_begin(pr->order_scratch.p, n_rays, &okeys, &ohist, x->stream);
             CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, n_rays, pr->classes.as<uint16_t>(),
                                      pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), x->err.as<uint32_t>(),
-                                     x->stream));
+                                     x->stream, okeys, ohist));
+        }
         if (flags & CRT_TRACE_USE_PREDICTOR) {
             p.pred_class = pr->classes.as<uint16_t>();
             p.treelets = pr->treelets.as<crt::Treelet>();
             p.n_treelets = reinterpret_cast<const uint32_t*>(pr->treelets.as<crt::Treelet>() + 128);
         }
         if (flags & CRT_TRACE_PREDICTOR_ORDER) {  // includes the coherence order of CRT_TRACE_SORT_RAYS
-            CRT_TRY(pr->order.reserve(4ull * n_rays));
-            CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
             crt::pred_order(pr->dev(), b->nodes.as<crt_bvh_node>(), d_rays, pr->classes.as<uint16_t>(), n_rays,
                             pr->order.as<uint32_t>(), pr->order_scratch.p, x->err.as<uint32_t>(), x->cfg.spin_limit,
-                            x->stream);
+                            x->stream, fuse);
             CRT_CUDA(cudaGetLastError());
             p.order = pr->order.as<uint32_t>();
         }
@@ -1295,6 +1303,10 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
             crt_predictor* pr = b->predictor;
             CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
             CRT_TRY(pr->classes.reserve(2ull * n_rays));
+            CRT_TRY(pr->order.reserve(4ull * n_rays));
+            CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
+            uint32_t *okeys = nullptr, *ohist = nullptr;  // every piece's order keys, one histogram
+            crt::pred_order_begin(pr->order_scratch.p, n_rays, &okeys, &ohist, x->stream);
             crt_ray* dst = x->rays_in.as<crt_ray>();
             CRT_CUDA(cudaEventRecord(x->copy_ev[crt_ctx::kCopyChunks], x->stream));  // earlier readers of rays_in
             CRT_CUDA(cudaStreamWaitEvent(x->copy_stream, x->copy_ev[crt_ctx::kCopyChunks], 0));
@@ -1309,7 +1321,7 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
                 CRT_CUDA(cudaStreamWaitEvent(x->stream, x->copy_ev[c], 0));
                 CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), dst + off, cnt,
                                          pr->classes.as<uint16_t>() + off, pr->cfg.miss_threshold, true,
-                                         x->err.as<uint32_t>(), x->stream));
+                                         x->err.as<uint32_t>(), x->stream, okeys + off, ohist));
             }
             d_rays = dst;
             classes_ready = true;
@@ -1835,8 +1847,11 @@ crt_status batch_trace_enqueue(crt_ctx* x, crt_batch* bt, const crt_ray* rays, u
     p.err = err;
     if ((flags & (CRT_TRACE_USE_PREDICTOR | CRT_TRACE_PREDICTOR_ORDER)) && bt->n_rays > 0) {
         crt_predictor* pr = bt->predictor;
+        const bool fuse = (flags & CRT_TRACE_PREDICTOR_ORDER) && !(flags & CRT_TRACE_USE_PREDICTOR) && bt->n_rays > 1;
+        uint32_t *okeys = nullptr, *ohist = nullptr;  // the inference writes the order keys too
+        if (fuse) crt::pred_order_begin(pr->order_scratch.p, bt->n_rays, &okeys, &ohist, s);
         CRT_CUDA(crt::pred_infer(pr->dev(), pr->nodes(), rays, bt->n_rays, pr->classes.as<uint16_t>(),
-                                 pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), err, s));
+                                 pr->cfg.miss_threshold, !(flags & CRT_TRACE_USE_PREDICTOR), err, s, okeys, ohist));
         if (flags & CRT_TRACE_USE_PREDICTOR) {
             p.pred_class = pr->classes.as<uint16_t>();
             p.treelets = pr->treelets.as<crt::Treelet>();
@@ -1844,7 +1859,7 @@ crt_status batch_trace_enqueue(crt_ctx* x, crt_batch* bt, const crt_ray* rays, u
         }
         if ((flags & CRT_TRACE_PREDICTOR_ORDER) && bt->n_rays > 1) {
             crt::pred_order(pr->dev(), pr->nodes(), rays, pr->classes.as<uint16_t>(), bt->n_rays, pr->order.as<uint32_t>(),
-                            pr->order_scratch.p, err, x->cfg.spin_limit, s);
+                            pr->order_scratch.p, err, x->cfg.spin_limit, s, fuse);
             p.order = pr->order.as<uint32_t>();
         }
     }

@@ -81,17 +81,43 @@ __device__ __forceinline__ uint32_t scene_of_ray(const BatchScene* sc, uint32_t 
 // scene's box, with the cell index moved by a per-scene hash so that the
 // scenes share the cell embeddings without sharing cells.  *scene: the
 // ray's scene (0 for one BVH).
+// *cell_raw: the cell before that move (the one the trace order key uses).
 __device__ __forceinline__ void ray_features(const PredictorDev& P, const crt_bvh_node* nodes, const SceneFrame& fr,
                                              uint32_t i, float4 r0, float4 r1, uint32_t& cell, uint32_t& bin,
-                                             uint32_t& scene) {
+                                             uint32_t& scene, uint32_t& cell_raw) {
     if (P.n_scenes == 0) {
         scene = 0;
         ray_keys(r0, r1, fr, cell, bin);
+        cell_raw = cell;
         return;
     }
     scene = scene_of_ray(P.scenes, P.n_scenes, i);
     ray_keys(r0, r1, scene_frame(nodes + __ldg(&P.scenes[scene].node_off)), cell, bin);
+    cell_raw = cell;
     cell = (cell + scene * 0x9E3779B1u) & static_cast<uint32_t>(kEo - 1);
+}
+
+// Trace order of a ray: predicted class (7 bits) | Morton code of its origin
+// cell on a 32^3 grid of the scene box (15 bits) | direction bin (10 bits).
+// Rays of one class go together, and within a class nearby origins and
+// similar directions.  In a batch: (scene, class, origin cell on a 16^3 grid
+// of the scene's box, the direction bin's first coordinate), 8 + 7 + 12 + 5
+// bits.  cell: the unmoved origin cell (ray_keys).
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {
+    v &= 31u;
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6) | ((v & 16u) << 8);
+}
+
+__device__ __forceinline__ uint32_t order_key(uint32_t n_scenes, uint32_t cell, uint32_t bin, uint32_t scene,
+                                              uint32_t cls) {
+    const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
+    cls &= 0x7Fu;
+    if (n_scenes == 0) {
+        const uint32_t m = (spread5(cx >> 1) << 2) | (spread5(cy >> 1) << 1) | spread5(cz >> 1);
+        return (cls << 25) | (m << 10) | (bin & 1023u);
+    }
+    const uint32_t m = (spread5(cx >> 2) << 2) | (spread5(cy >> 2) << 1) | spread5(cz >> 2);
+    return ((scene & 0xFFu) << 24) | (cls << 17) | ((m & 0xFFFu) << 5) | ((bin >> 5) & 31u);
 }
 
 // Class of the closest hit `tri` (scene-local id in a batch) of a ray of `scene`.
@@ -194,22 +220,31 @@ __device__ __forceinline__ uint32_t lane_addr(uint32_t tbase, uint32_t col) {
 // then the logits over both once H2 is out of D2.  Shared memory: weights, X,
 // and one activation buffer that holds H1 and then H2 (H1 is dead once the
 // second GEMM has completed).
+// The last 2 KB: the CTA's trace order key histograms (4 digits x 256
+// values, 16-bit counters in pairs), when the kernel writes order keys.
 constexpr int kInferSmemUsed = 64 * 32 * 2 + 64 * 64 * 2 + 128 * 64 * 2 + 128 * 32 * 2 + 128 * 64 * 2 +
-                               (64 + 64 + 128) * 4 + 64;
+                               (64 + 64 + 128) * 4 + 64 + 2048;
 // Requested size caps residency at four CTAs per SM, the number whose
 // 128-column TMEM allocations fit the SM's 512 columns together.
-constexpr int kInferSmem = 54 * 1024;
+constexpr int kInferSmem = 56 * 1024;
+// tiles of 128 rays between flushes of the 16-bit key histograms (< 65536 rays)
+constexpr uint32_t kHistFlushTiles = 256;
 constexpr int kInferCtasPerSm = 4;
 static_assert(kInferSmemUsed <= kInferSmem && kInferCtasPerSm * kInferSmem <= 228 * 1024 &&
               (kInferCtasPerSm + 1) * kInferSmem > 228 * 1024, "inference tile layout and residency");
 
-// argmax: the class is the likeliest of all 128 (miss included), which is all
+// ARGMAX: the class is the likeliest of all 128 (miss included), which is all
 // that ordering rays by class needs; otherwise the likeliest treelet unless
 // the miss class holds at least miss_threshold of the probability mass (the
-// seeding rule), which needs the softmax sum.
+// seeding rule), which needs the softmax sum.  KEYS (with ARGMAX): the kernel
+// also writes each ray's trace order key (order_key) to keys[i] and adds the
+// keys' four 8-bit digit histograms into hist (4 x 256), so that the ordering
+// needs no second pass over the rays.
+template <bool ARGMAX, bool KEYS>
 __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bvh_node* nodes, const crt_ray* rays,
-                                                    uint32_t n, uint16_t* classes, float miss_threshold, bool argmax,
-                                                    uint32_t* err) {
+                                                    uint32_t n, uint16_t* classes, float miss_threshold,
+                                                    uint32_t* keys, uint32_t* hist, uint32_t* err) {
+    static_assert(ARGMAX || !KEYS, "order keys come with the argmax class");
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sW1 = smem;
     unsigned char* sW2 = sW1 + 64 * 32 * 2;
@@ -220,6 +255,7 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
     float* sB = reinterpret_cast<float*>(sH1 + 128 * 64 * 2);
     uint32_t* sT = reinterpret_cast<uint32_t*>(sB + 256);
     uint64_t* sM = reinterpret_cast<uint64_t*>(sT + 2);
+    uint32_t* sHist = sT + 16;  // 512 words: counter k in half (k & 1) of word k >> 1
 
     load_kmajor(sW1, P.w16 + hW1, 64, 32);
     load_kmajor(sW2, P.w16 + hW2, 64, 64);
@@ -228,6 +264,20 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         const float b = i < 64 ? P.master[oB1 + i] : (i < 128 ? P.master[oB2 + i - 64] : P.master[oB3 + i - 128]);
         sB[i] = b;
     }
+    if (KEYS)
+        for (int w = threadIdx.x; w < 512; w += 128) sHist[w] = 0u;
+    // adds the CTA's counts into hist and clears them (every thread calls it)
+    auto flush_hist = [&]() {
+        __syncthreads();
+        for (int w = threadIdx.x; w < 512; w += 128) {
+            const uint32_t v = sHist[w];
+            if (v & 0xFFFFu) atomicAdd(hist + 2 * w, v & 0xFFFFu);
+            if (v >> 16) atomicAdd(hist + 2 * w + 1, v >> 16);
+            sHist[w] = 0u;
+        }
+        __syncthreads();
+    };
+    uint32_t tiles_done = 0;
     if (threadIdx.x < 32) { tc::tmem_alloc(sT, 128); tc::tmem_relinquish(); }
     if (threadIdx.x == 0) tc::mbar_init(sM, 1);
     Sync sy{sM, 0, err};
@@ -240,11 +290,14 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         const uint32_t i = tile * 128 + tid;
         const bool valid = i < n;
         uint4 e[4] = {};
+        uint32_t key_cell = 0, key_bin = 0, key_scene = 0;
         if (valid) {
             const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
             const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
             uint32_t cell, bin, scene;
-            ray_features(P, nodes, fr, i, r0, r1, cell, bin, scene);
+            ray_features(P, nodes, fr, i, r0, r1, cell, bin, scene, key_cell);
+            key_bin = bin;
+            key_scene = scene;
             const uint4* eo = reinterpret_cast<const uint4*>(P.w16 + hEo + static_cast<size_t>(cell) * kEmb);
             const uint4* ed = reinterpret_cast<const uint4*>(P.w16 + hEd + static_cast<size_t>(bin) * kEmb);
             e[0] = __ldg(eo); e[1] = __ldg(eo + 1); e[2] = __ldg(ed); e[3] = __ldg(ed + 1);
@@ -286,13 +339,23 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const float l = v[j] + sB[128 + c + j];
-                lmax = fmaxf(lmax, l);
+                if (!ARGMAX) lmax = fmaxf(lmax, l);
                 if (c + j == kMissClass) lmiss = l;
                 else if (l > best) { best = l; bc = c + j; }
             }
         }
-        if (argmax) {
-            if (valid) classes[i] = static_cast<uint16_t>(lmiss >= best ? kMissClass : bc);
+        if (ARGMAX) {
+            const uint32_t cls = lmiss >= best ? kMissClass : static_cast<uint32_t>(bc);
+            if (valid) classes[i] = static_cast<uint16_t>(cls);
+            if (KEYS && valid) {
+                const uint32_t key = order_key(P.n_scenes, key_cell, key_bin, key_scene, cls);
+                keys[i] = key;
+#pragma unroll
+                for (int d = 0; d < 4; ++d) {
+                    const uint32_t k = static_cast<uint32_t>(d) * 256u + ((key >> (8 * d)) & 255u);
+                    atomicAdd(sHist + (k >> 1), 1u << (16u * (k & 1u)));
+                }
+            }
         } else {
             float sum = 0.f;
             for (int c = 0; c < 128; c += 16) {
@@ -306,10 +369,17 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         }
         tc::fence_before_sync();
         __syncthreads();
+        if (KEYS && ++tiles_done == kHistFlushTiles) {  // block-uniform
+            flush_hist();
+            tiles_done = 0;
+        }
     }
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x < 32) tc::tmem_dealloc(tb, 128);
+    // counts of tiles that gave up (an error is raised) are flushed too; the
+    // caller reports the error and ignores the order
+    if (KEYS) flush_hist();
 }
 
 // ------------------------------------------------------------ training
@@ -370,8 +440,8 @@ __global__ void __launch_bounds__(128) train_kernel(PredictorDev P, const crt_bv
     if (valid) {
         const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + ri));
         const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + ri) + 1);
-        uint32_t scene;
-        ray_features(P, nodes, scene_frame(nodes), static_cast<uint32_t>(ri), r0, r1, cell, bin, scene);
+        uint32_t scene, cell_raw;
+        ray_features(P, nodes, scene_frame(nodes), static_cast<uint32_t>(ri), r0, r1, cell, bin, scene, cell_raw);
         const uint4* eo = reinterpret_cast<const uint4*>(P.w16 + hEo + static_cast<size_t>(cell) * kEmb);
         const uint4* ed = reinterpret_cast<const uint4*>(P.w16 + hEd + static_cast<size_t>(bin) * kEmb);
         e[0] = __ldg(eo); e[1] = __ldg(eo + 1); e[2] = __ldg(ed); e[3] = __ldg(ed + 1);
@@ -893,15 +963,8 @@ __global__ void bounce_kernel(const crt_ray* prim, const crt_hit* hits, const ui
     o[1] = make_float4(dx * dl, dy * dl, dz * dl, __int_as_float(0x7F800000));
 }
 
-// Trace order of a ray: predicted class (7 bits) | Morton code of its origin
-// cell on a 32^3 grid of the scene box (15 bits) | direction bin (10 bits),
-// with the histograms of the four 8-bit digits.  Rays of one class go
-// together, and within a class nearby origins and similar directions.
-__device__ __forceinline__ uint32_t spread5(uint32_t v) {
-    v &= 31u;
-    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6) | ((v & 16u) << 8);
-}
-
+// Trace order keys (order_key) with the histograms of their four 8-bit
+// digits, for classes computed without them.
 __global__ void __launch_bounds__(256) order_keys_kernel(PredictorDev P, const crt_bvh_node* nodes,
                                                          const crt_ray* __restrict__ rays,
                                                          const uint16_t* __restrict__ classes, uint32_t n,
@@ -913,20 +976,9 @@ __global__ void __launch_bounds__(256) order_keys_kernel(PredictorDev P, const c
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
         const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
-        uint32_t cell, bin, key;
-        const uint32_t cls = static_cast<uint32_t>(classes[i]) & 0x7Fu;
-        if (P.n_scenes == 0) {
-            ray_keys(r0, r1, fr, cell, bin);
-            const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
-            const uint32_t m = (spread5(cx >> 1) << 2) | (spread5(cy >> 1) << 1) | spread5(cz >> 1);
-            key = (cls << 25) | (m << 10) | (bin & 1023u);
-        } else {  // (scene, class, 16^3 origin cell, first direction coordinate): 8 + 7 + 12 + 5 bits
-            const uint32_t sc = scene_of_ray(P.scenes, P.n_scenes, i);
-            ray_keys(r0, r1, scene_frame(nodes + __ldg(&P.scenes[sc].node_off)), cell, bin);
-            const uint32_t cx = cell / (kGrid * kGrid), cy = (cell / kGrid) % kGrid, cz = cell % kGrid;
-            const uint32_t m = (spread5(cx >> 2) << 2) | (spread5(cy >> 2) << 1) | spread5(cz >> 2);
-            key = ((sc & 0xFFu) << 24) | (cls << 17) | ((m & 0xFFFu) << 5) | ((bin >> 5) & 31u);
-        }
+        uint32_t cell, bin, scene, cell_raw;
+        ray_features(P, nodes, fr, i, r0, r1, cell, bin, scene, cell_raw);
+        const uint32_t key = order_key(P.n_scenes, cell_raw, bin, scene, classes[i]);
         keys[i] = key;
 #pragma unroll
         for (int p = 0; p < 4; ++p) atomicAdd(&h[p * 256 + ((key >> (8 * p)) & 255u)], 1u);
@@ -944,8 +996,19 @@ size_t pred_order_scratch_bytes(uint32_t n) {
     return 4 * (3 * static_cast<size_t>(n) + 4 * 256 + 4 * (tiles * 256 + 1) + 64);
 }
 
+void pred_order_begin(void* scratch, uint32_t n, uint32_t** keys, uint32_t** hist, cudaStream_t s) {
+    uint32_t* ka = static_cast<uint32_t*>(scratch);
+    uint32_t* h = ka + 3 * static_cast<size_t>(n);
+    const size_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
+    const size_t lb_words = tiles * 256 + 1;
+    cudaMemsetAsync(h, 0, 4 * (4 * 256 + 4 * lb_words), s);
+    *keys = ka;
+    *hist = h;
+}
+
 void pred_order(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes,
-                uint32_t n, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s) {
+                uint32_t n, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s,
+                bool keys_ready) {
     if (n == 0) return;
     uint32_t* ka = static_cast<uint32_t*>(scratch);
     uint32_t* kb = ka + n;
@@ -954,9 +1017,11 @@ void pred_order(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray*
     uint32_t* lb = hist + 4 * 256;  // per pass: ticket, then the look-back words
     const size_t tiles = (n + sort_tile_keys(8) - 1) / sort_tile_keys(8);
     const size_t lb_words = tiles * 256 + 1;
-    cudaMemsetAsync(hist, 0, 4 * (4 * 256 + 4 * lb_words), s);
-    const uint32_t grid = std::min<uint32_t>((n + 255) / 256, kNumSms * 8);
-    pred::order_keys_kernel<<<grid, 256, 0, s>>>(P, nodes, rays, classes, n, ka, hist);
+    if (!keys_ready) {
+        cudaMemsetAsync(hist, 0, 4 * (4 * 256 + 4 * lb_words), s);
+        const uint32_t grid = std::min<uint32_t>((n + 255) / 256, kNumSms * 8);
+        pred::order_keys_kernel<<<grid, 256, 0, s>>>(P, nodes, rays, classes, n, ka, hist);
+    }
     // four stable 8-bit passes; pass 0 synthesises the ray indices
     const uint32_t* kin[4] = {ka, kb, ka, kb};
     uint32_t* kout[4] = {kb, ka, kb, ka};
@@ -977,20 +1042,31 @@ void pred_init(const PredictorDev& P, uint32_t seed, cudaStream_t s) {
     pred::convert_kernel<<<kNumSms * 8, 256, 0, s>>>(P);
 }
 
-cudaError_t pred_prepare() {
-    cudaError_t e = cudaFuncSetAttribute(pred::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+static cudaError_t infer_attributes() {
+    cudaError_t e = cudaFuncSetAttribute(pred::infer_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          pred::kInferSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pred::infer_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 pred::kInferSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pred::infer_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 pred::kInferSmem);
+    return e;
+}
+
+cudaError_t pred_prepare() {
+    cudaError_t e = infer_attributes();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(pred::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pred::kTrainSmem);
     return e;
 }
 
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
-                       uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s) {
+                       uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s,
+                       uint32_t* order_keys, uint32_t* order_hist) {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(pred::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             pred::kInferSmem);
+        cudaError_t e = infer_attributes();
         if (e != cudaSuccess) return e;
         attr = true;
     }
@@ -998,7 +1074,15 @@ cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const c
     const uint32_t cap = static_cast<uint32_t>(pred::kInferCtasPerSm) * kNumSms;
     const uint32_t grid = tiles < cap ? tiles : cap;
     if (grid == 0) return cudaSuccess;
-    pred::infer_kernel<<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold, argmax, err);
+    if (!argmax)
+        pred::infer_kernel<false, false><<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold,
+                                                                             nullptr, nullptr, err);
+    else if (!order_keys)
+        pred::infer_kernel<true, false><<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold,
+                                                                            nullptr, nullptr, err);
+    else
+        pred::infer_kernel<true, true><<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold,
+                                                                           order_keys, order_hist, err);
     return cudaGetLastError();
 }
 

@@ -83,8 +83,13 @@ cudaError_t pred_prepare();
 // classes[i]: with argmax the likeliest of the 128 classes (treelets and
 // miss), used to order rays; otherwise the likeliest treelet unless P(miss) >=
 // miss_threshold (then the miss class), the seeding rule.
+// order_keys (with argmax): also each ray's trace order key (see pred_order)
+// at order_keys[i], and the keys' digit histograms added into order_hist,
+// both from pred_order_begin; rays in several calls (pieces of one array)
+// pass order_keys + the piece's offset and the same order_hist.
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
-                       uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s);
+                       uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s,
+                       uint32_t* order_keys = nullptr, uint32_t* order_hist = nullptr);
 cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n_rays,
                             const crt_hit* hits, const uint16_t* targets, uint32_t n_samples, uint32_t stride,
                             uint32_t offset, float* loss_sum, uint32_t* err, cudaStream_t s);
@@ -97,8 +102,14 @@ void pred_refresh_fp16(const PredictorDev& P, cudaStream_t s);
 size_t pred_order_scratch_bytes(uint32_t n);
 // With P.n_scenes != 0 (a batch) the key is (scene, predicted class, origin
 // cell on a 16^3 grid of the scene's box, direction bin's first coordinate).
+// keys_ready: the keys and histograms are already in scratch (pred_order_begin,
+// then pred_infer with them); otherwise they are computed from the classes.
 void pred_order(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, const uint16_t* classes,
-                uint32_t n, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s);
+                uint32_t n, uint32_t* order, void* scratch, uint32_t* err, uint32_t spin_limit, cudaStream_t s,
+                bool keys_ready = false);
+// Clears the ordering's histograms and look-back words in scratch (sized for
+// n rays) and returns where pred_infer writes the keys and histograms.
+void pred_order_begin(void* scratch, uint32_t n, uint32_t** keys, uint32_t** hist, cudaStream_t s);
 void pred_treelets(const crt_bvh_node* nodes, const float4* wide, const float4* xtri, uint32_t n_leaves,
                    Treelet* tl, uint32_t* n_tl, uint8_t* tri_class, cudaStream_t s);
 // Every scene of a batch cut into <= 127 treelets: scene k's at tl + 128 k,
