@@ -435,8 +435,9 @@ def run_ours(args):
             "ploc_iterations": builds[-1][0]["ploc_iterations"],
             "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(n * 32),
                     "d2h_bytes_per_step": int(n * 16), "ms_per_step": round(e2e_t, 4),
-                    "transfer": "crt_trace on page-locked host rays (copied in on the library stream) and host hits "
-                                "(written by the trace kernel over the CPU-GPU link), host-timed around the call"},
+                    "transfer": "crt_trace on page-locked host rays (read across the CPU-GPU link by the inference "
+                                "kernel, which stores the device copy the trace reads) and host hits (written by the "
+                                "trace kernel over the link), host-timed around the call"},
             "gpu_launches": 6 * args.steps,
             "gpu_launches_note": "per step: infer_kernel (which also writes the order keys and their digit histograms), "
                                  "4 onesweep_kernel passes, trace_pool_kernel",

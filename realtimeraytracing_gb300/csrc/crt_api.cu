@@ -1291,13 +1291,32 @@ crt_status crt_trace(crt_ctx* x, const crt_bvh* b, const crt_ray* rays, uint32_t
         // reads each ray once, in order; reordered or predicted traces read
         // them more than once and out of order, so those copy them in first.
         const bool once = !(flags & (CRT_TRACE_SORT_RAYS | CRT_TRACE_PREDICTOR_ORDER | CRT_TRACE_USE_PREDICTOR));
-        const bool chunked = (flags & CRT_TRACE_PREDICTOR_ORDER) && !(flags & CRT_TRACE_USE_PREDICTOR) &&
-                             b->predictor && n_rays >= kChunkedCopyMinRays;
+        const bool learned_order = (flags & CRT_TRACE_PREDICTOR_ORDER) && !(flags & CRT_TRACE_USE_PREDICTOR) &&
+                                   b->predictor;
+        const bool chunked = learned_order && n_rays >= kChunkedCopyMinRays;
         if (void* m = once ? mapped_host_ptr(const_cast<crt_ray*>(rays)) : nullptr) {
             d_rays = static_cast<const crt_ray*>(m);
+        } else if (void* mi = learned_order ? mapped_host_ptr(const_cast<crt_ray*>(rays)) : nullptr) {
+            // Ordering by the predictor over page-locked host rays: the inference
+            // kernel reads them across the CPU-GPU link itself, once, on every
+            // SM under its own work, and stores the device copy the ordering and
+            // the trace read (the copy engines alone moved them at about 200 GB/s
+            // ahead of the inference).
+            crt_predictor* pr = b->predictor;
+            CRT_TRY(x->rays_in.reserve(sizeof(crt_ray) * n_rays));
+            CRT_TRY(pr->classes.reserve(2ull * n_rays));
+            CRT_TRY(pr->order.reserve(4ull * n_rays));
+            CRT_TRY(pr->order_scratch.reserve(crt::pred_order_scratch_bytes(n_rays)));
+            uint32_t *okeys = nullptr, *ohist = nullptr;
+            crt::pred_order_begin(pr->order_scratch.p, n_rays, &okeys, &ohist, x->stream);
+            CRT_CUDA(crt::pred_infer(pr->dev(), b->nodes.as<crt_bvh_node>(), static_cast<const crt_ray*>(mi), n_rays,
+                                     pr->classes.as<uint16_t>(), pr->cfg.miss_threshold, true, x->err.as<uint32_t>(),
+                                     x->stream, okeys, ohist, x->rays_in.as<crt_ray>()));
+            d_rays = x->rays_in.as<crt_ray>();
+            classes_ready = true;
         } else if (chunked) {
-            // Ordering by the predictor: copy the rays in kCopyChunks pieces on
-            // the copy stream and run each piece's inference on the context's
+            // Ordering by the predictor over pageable host rays: copy the rays in
+            // kCopyChunks pieces on the copy stream and run each piece's inference on the context's
             // stream as soon as it has landed, so the inference hides behind the
             // copy; the ordering and the trace then wait for the last piece.
             crt_predictor* pr = b->predictor;

@@ -239,11 +239,14 @@ static_assert(kInferSmemUsed <= kInferSmem && kInferCtasPerSm * kInferSmem <= 22
 // seeding rule), which needs the softmax sum.  KEYS (with ARGMAX): the kernel
 // also writes each ray's trace order key (order_key) to keys[i] and adds the
 // keys' four 8-bit digit histograms into hist (4 x 256), so that the ordering
-// needs no second pass over the rays.
+// needs no second pass over the rays.  rays_copy (optional): ray i is also
+// stored to rays_copy[i] (rays in page-locked host memory are read across the
+// CPU-GPU link once, by this kernel, and the trace reads the device copy).
 template <bool ARGMAX, bool KEYS>
 __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bvh_node* nodes, const crt_ray* rays,
                                                     uint32_t n, uint16_t* classes, float miss_threshold,
-                                                    uint32_t* keys, uint32_t* hist, uint32_t* err) {
+                                                    uint32_t* keys, uint32_t* hist, crt_ray* rays_copy,
+                                                    uint32_t* err) {
     static_assert(ARGMAX || !KEYS, "order keys come with the argmax class");
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sW1 = smem;
@@ -294,6 +297,11 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         if (valid) {
             const float4 r0 = __ldg(reinterpret_cast<const float4*>(rays + i));
             const float4 r1 = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+            if (rays_copy) {
+                float4* c = reinterpret_cast<float4*>(rays_copy + i);
+                c[0] = r0;
+                c[1] = r1;
+            }
             uint32_t cell, bin, scene;
             ray_features(P, nodes, fr, i, r0, r1, cell, bin, scene, key_cell);
             key_bin = bin;
@@ -1063,7 +1071,7 @@ cudaError_t pred_prepare() {
 
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
                        uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s,
-                       uint32_t* order_keys, uint32_t* order_hist) {
+                       uint32_t* order_keys, uint32_t* order_hist, crt_ray* rays_copy) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = infer_attributes();
@@ -1076,13 +1084,13 @@ cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const c
     if (grid == 0) return cudaSuccess;
     if (!argmax)
         pred::infer_kernel<false, false><<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold,
-                                                                             nullptr, nullptr, err);
+                                                                             nullptr, nullptr, rays_copy, err);
     else if (!order_keys)
         pred::infer_kernel<true, false><<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold,
-                                                                            nullptr, nullptr, err);
+                                                                            nullptr, nullptr, rays_copy, err);
     else
         pred::infer_kernel<true, true><<<grid, 128, pred::kInferSmem, s>>>(P, nodes, rays, n, classes, miss_threshold,
-                                                                           order_keys, order_hist, err);
+                                                                           order_keys, order_hist, rays_copy, err);
     return cudaGetLastError();
 }
 

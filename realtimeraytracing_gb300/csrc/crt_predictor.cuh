@@ -86,10 +86,12 @@ cudaError_t pred_prepare();
 // order_keys (with argmax): also each ray's trace order key (see pred_order)
 // at order_keys[i], and the keys' digit histograms added into order_hist,
 // both from pred_order_begin; rays in several calls (pieces of one array)
-// pass order_keys + the piece's offset and the same order_hist.
+// pass order_keys + the piece's offset and the same order_hist.  rays_copy
+// (device, optional): receives a copy of the rays, which may then be read from
+// page-locked host memory (its device-mapped address, 16-byte aligned).
 cudaError_t pred_infer(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n,
                        uint16_t* classes, float miss_threshold, bool argmax, uint32_t* err, cudaStream_t s,
-                       uint32_t* order_keys = nullptr, uint32_t* order_hist = nullptr);
+                       uint32_t* order_keys = nullptr, uint32_t* order_hist = nullptr, crt_ray* rays_copy = nullptr);
 cudaError_t pred_train_step(const PredictorDev& P, const crt_bvh_node* nodes, const crt_ray* rays, uint32_t n_rays,
                             const crt_hit* hits, const uint16_t* targets, uint32_t n_samples, uint32_t stride,
                             uint32_t offset, float* loss_sum, uint32_t* err, cudaStream_t s);

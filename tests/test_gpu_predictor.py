@@ -215,10 +215,12 @@ def test_adam_step_matches_numpy(ctx):
 
 
 def test_learned_order_from_host_rays_in_pieces(ctx, scene):
-    """crt_trace of 1 M or more host rays with CRT_TRACE_PREDICTOR_ORDER copies
-    the rays in pieces on a second stream and runs each piece's inference as
-    soon as it has landed; the hits equal the plain trace's bit for bit, from
-    pageable and from page-locked host memory, and below the piece threshold."""
+    """crt_trace of host rays with CRT_TRACE_PREDICTOR_ORDER: from pageable
+    memory (1 M rays or more) the rays are copied in pieces on a second stream
+    and each piece's inference runs as soon as it has landed; from page-locked
+    memory the inference kernel reads them in place and stores the device copy
+    the trace reads.  The hits equal the plain trace's bit for bit, both ways,
+    above and below the piece threshold."""
     bvh, _ = scene
     pred = crt.Predictor(ctx, bvh, seed=9)
     rays = S.sphere_rays(1_200_000, seed=97)
@@ -233,4 +235,7 @@ def test_learned_order_from_host_rays_in_pieces(ctx, scene):
     np.testing.assert_array_equal(pinned_hits.numpy().view(np.uint32), plain.view(np.uint32))
     small = ctx.trace(bvh, rays[:300_001], flags)
     np.testing.assert_array_equal(small.view(np.uint32), plain[:300_001].view(np.uint32))
+    small_pinned = torch.from_numpy(rays[:300_001]).pin_memory()
+    small_hits = ctx.trace(bvh, small_pinned, flags)
+    np.testing.assert_array_equal(small_hits.view(np.uint32), plain[:300_001].view(np.uint32))
     pred.free()
