@@ -341,15 +341,26 @@ __global__ void __launch_bounds__(128) infer_kernel(PredictorDev P, const crt_bv
         // `miss_threshold` of the probability mass.
         float best = -INFINITY, lmax = -INFINITY, lmiss = 0.f;
         int bc = 0;
-        for (int c = 0; c < 128; c += 16) {
+        static_assert(kMissClass == 127, "the miss class is the last logit");
+        for (int c = 0; c < 112; c += 16) {  // the first 112 logits: treelets only
             float v[16];
             tc::tmem_ld16(lane_addr(tb, c), v);
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
                 const float l = v[j] + sB[128 + c + j];
                 if (!ARGMAX) lmax = fmaxf(lmax, l);
-                if (c + j == kMissClass) lmiss = l;
-                else if (l > best) { best = l; bc = c + j; }
+                if (l > best) { best = l; bc = c + j; }
+            }
+        }
+        {  // the last 16, the miss class among them
+            float v[16];
+            tc::tmem_ld16(lane_addr(tb, 112), v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float l = v[j] + sB[128 + 112 + j];
+                if (!ARGMAX) lmax = fmaxf(lmax, l);
+                if (112 + j == kMissClass) lmiss = l;
+                else if (l > best) { best = l; bc = 112 + j; }
             }
         }
         if (ARGMAX) {
