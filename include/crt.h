@@ -323,7 +323,9 @@ crt_status crt_last_trace_stats(crt_ctx* ctx, uint64_t out[2]);
  * crt_trace_seeded or the multi-launch frame paths, from CUDA events on the
  * context's stream: ms[0] = the work before the traversal kernel (predictor
  * inference, ray keys and their radix sort; 0 for a plain trace), ms[1] =
- * the traversal kernel itself.  Waits for that work to finish. */
+ * the traversal kernel itself.  With host rays and predictor ordering the
+ * inference runs while the rays come in, before the first event, so ms[0]
+ * is the sort alone.  Waits for that work to finish. */
 crt_status crt_last_trace_timing(crt_ctx* ctx, float ms[2]);
 
 /* One frame of the reference's compute pass (Application::drawOneFrame,
